@@ -1,0 +1,175 @@
+// Internal declarations of libfvmgpu: handles, device buffers, kernel launchers.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstddef>
+#include <string>
+#include <vector>
+#include <memory>
+#include <stdexcept>
+#include <functional>
+#include "../../include/fvm_gpu.h"
+
+namespace fvm {
+
+// ---- errors ------------------------------------------------------------------------
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+void set_last_error(const std::string& msg);
+[[noreturn]] void fail(int code, const std::string& msg);
+void cuda_check(cudaError_t e, const char* what);
+#define FVM_CUDA(x) ::fvm::cuda_check((x), #x)
+
+// ---- device buffer (RAII) ------------------------------------------------------------
+struct DBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    DBuf() = default;
+    DBuf(const DBuf&) = delete;
+    DBuf& operator=(const DBuf&) = delete;
+    ~DBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    void alloc(size_t n) {
+        release();
+        if (n == 0) return;
+        cudaError_t e = cudaMalloc(&p, n);
+        if (e != cudaSuccess) {
+            p = nullptr;
+            cudaGetLastError();
+            fail(e == cudaErrorMemoryAllocation ? FVM_ERR_OUT_OF_MEMORY : FVM_ERR_CUDA,
+                 std::string("cudaMalloc(") + std::to_string(n) + " bytes): " + cudaGetErrorString(e));
+        }
+        bytes = n;
+    }
+    template <class T> void upload(const std::vector<T>& v) {
+        alloc(v.size() * sizeof(T));
+        if (!v.empty()) FVM_CUDA(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    }
+    template <class T> T* as() const { return static_cast<T*>(p); }
+};
+
+// ---- sliced-ELL operator (slice height 32, one warp per slice, column-major slots) ----
+constexpr int kSlice = 32;
+
+struct SellPattern {
+    int64_t nrows = 0, nslices = 0, nslots = 0, nnz = 0;
+    std::vector<int64_t> slice_ptr;  // [nslices+1] slot offsets (multiples of 32)
+    std::vector<int32_t> width;      // [nslices]
+    std::vector<int32_t> col;        // [nslots] internal column (pad: the row itself)
+    std::vector<int64_t> rowptr;     // CSR view: [nrows+1]
+    std::vector<int32_t> csr_col;    // CSR columns (sorted)
+    std::vector<int64_t> csr_slot;   // CSR entry -> SELL slot
+    DBuf d_slice_ptr, d_width, d_col;
+    // slot of (row, col), or -1
+    int64_t find(int32_t row, int32_t c) const;
+};
+
+// ---- mesh ----------------------------------------------------------------------------
+struct Tiles {
+    bool built = false;
+    int tile_vertices = 0;
+    int64_t ntiles = 0, nelem = 0, nbelem = 0;
+    std::vector<int64_t> off, boff;            // [ntiles+1]
+    std::vector<int32_t> etri, ebedge;         // element -> caller triangle / boundary edge
+    std::vector<int32_t> ev;                   // [3][nelem] internal vertex ids (SoA)
+    std::vector<int32_t> bv;                   // [3][nbelem] (i, j, k) internal
+    DBuf d_off, d_boff, d_ev, d_bv;
+    DBuf d_g, d_bg;                            // geometric flux coefficients [6][nelem], [3][nbelem]
+};
+
+}  // namespace fvm
+
+struct fvm_mesh {
+    int64_t np = 0, nt = 0, nbe = 0, nv = 0;   // points, triangles, boundary edges, vertices
+    std::vector<double> pts;                    // [2*np] caller order
+    std::vector<int32_t> tri;                   // [3*nt]
+    std::vector<int32_t> be;                    // [2*nbe]
+    std::vector<int32_t> badj;                  // [nbe]
+    std::vector<int32_t> btri;                  // [nbe] triangle holding the boundary edge
+    std::vector<uint8_t> has_vertex;            // [np]
+    std::vector<double> vol;                    // [np] control-volume areas
+    std::vector<double> props;                  // [24*nt] TriangleProperties
+    std::vector<int32_t> perm, iperm;           // perm[internal] = caller, iperm[caller] = internal
+    fvm::SellPattern pat;                       // vertex-neighbour operator pattern (internal)
+    fvm::Tiles tiles;
+    fvm::DBuf d_perm, d_iperm, d_invV;          // d_invV internal order
+    int tile_vertices_req = 0;
+    void build_tiles();
+};
+
+struct fvm_problem {
+    fvm_mesh* mesh = nullptr;
+    int precision = FVM_FP64;
+    int dif_deg = 0, neu_deg = 0, src_deg = 0, dudt_deg = 0;
+    bool linear = true;                         // every form is affine in u (quadratic only on the diagonal)
+    std::vector<int8_t> code;                   // [np] caller order
+    std::vector<int8_t> bneu;                   // [nbe]
+    std::vector<double> dualD, quarterD, quarterN, src, dudt, dirv;  // copies of the descriptor arrays
+    // linear operator path: du = rowscale * (A u) + b + q u^2
+    fvm::DBuf d_val64, d_val32, d_b, d_q, d_rowscale;
+    bool has_b = false, has_q = false;
+    // triangle path
+    bool tri_ready = false;
+    fvm::DBuf d_ec, d_bc;                       // element coefficients, boundary-element coefficients
+    fvm::DBuf d_code, d_vsrc, d_vdudt;          // internal order vertex data
+    // Dirichlet list
+    int64_t ndir = 0;
+    fvm::DBuf d_dir_idx, d_dir_val;
+    // work buffers (internal order)
+    fvm::DBuf d_u, d_du, d_ref;
+    void ensure_work();
+    void build_triangle_path();
+};
+
+struct fvm_template {
+    fvm_problem* prob = nullptr;
+    int kind = 0;
+    fvm::DBuf d_val64, d_val32, d_b;
+    std::vector<double> val, b;                 // SELL values (internal), b internal
+    // steady solve (reduced SPD-like system on free rows)
+    bool steady_ready = false;
+    int symmetric = 0;
+    double bnorm = 0;
+    fvm::DBuf d_bval64, d_bval32, d_bdiag_inv64, d_bdiag_inv32, d_rhs_red;  // reduced operator B, rhs
+    fvm::DBuf d_xfix, d_invV_free64, d_invV_free32;
+    fvm::DBuf d_fixed_mask;                      // 1 on rows fixed by Dirichlet / missing vertex
+    void build_steady();
+};
+
+namespace fvm {
+// kernels (fvm_kernels.cu)
+void launch_sell_apply64(const SellPattern& p, const double* val, const double* x, double* y,
+                         const double* rowscale, const double* b, const double* q, cudaStream_t s);
+void launch_sell_apply32(const SellPattern& p, const float* val, const double* x, double* y,
+                         const double* rowscale, const double* b, const double* q, cudaStream_t s);
+void launch_permute_in(const int32_t* perm, const double* xref, double* xint, int64_t n, cudaStream_t s);
+void launch_permute_out(const int32_t* perm, const double* xint, double* xref, int64_t n, cudaStream_t s);
+void launch_dirichlet(const int32_t* idx, const double* val, double* u, int64_t n, cudaStream_t s);
+void launch_triangle_rhs(const fvm_mesh* m, const fvm_problem* p, const double* u, double* du, cudaStream_t s);
+// Tsit5 stage: y = u + dt * sum_j a[j] * k[j]  (nk vectors)
+void launch_stage(double* y, const double* u, const double* const* k, const double* a, int nk, double dt,
+                  int64_t n, cudaStream_t s);
+// err_i = dt * sum_j bt[j] k[j]; accumulates sum((err_i / (abstol + max(|u|,|unew|) reltol))^2)
+void launch_error_norm(const double* u, const double* unew, const double* const* k, const double* bt,
+                       double dt, double abstol, double reltol, int64_t n, double* d_acc, cudaStream_t s);
+void launch_hermite(double* out, const double* u0, const double* u1, const double* f0, const double* f1,
+                    double dt, double theta, int64_t n, cudaStream_t s);
+// Krylov helpers
+void launch_fill(double* x, double v, int64_t n, cudaStream_t s);
+
+// Right-hand side in the internal numbering plus the per-step callback (Dirichlet update).
+struct OdeRhs {
+    std::function<void(const double*, double*, double, cudaStream_t)> f;
+    std::function<void(double*, double, cudaStream_t)> callback;  // may be empty
+};
+void tsit5_run_internal(OdeRhs& rhs, int64_t n, const double* u0_int, const fvm_ode_options& o, double* out_int,
+                        fvm_ode_stats* st, cudaStream_t s);
+int guard_call(const std::function<int()>& f);
+void problem_rhs_internal(fvm_problem* p, const double* u, double* du, bool force_triangle, cudaStream_t s);
+}  // namespace fvm

@@ -1,0 +1,337 @@
+// Device kernels of libfvmgpu (sm_103a).  Every kernel here is HBM- or FP64-issue-bound
+// gather/scatter/stream work; none is a dense contraction, so no tensor-core path exists.
+#include "fvm_internal.h"
+
+namespace fvm {
+
+// ---------------------------------------------------------------------------------------
+// Sliced-ELL operator: y = rowscale .* (A x) + b + q .* x.^2
+// One warp per 32-row slice, one lane per row, slots column-major so each slot step of a
+// warp reads 32 consecutive values and columns (fully coalesced).  x gathers hit L2.
+// ---------------------------------------------------------------------------------------
+template <class V, class Acc>
+__global__ void __launch_bounds__(256) sell_apply_kernel(const int64_t* __restrict__ slice_ptr,
+                                                         const int32_t* __restrict__ width,
+                                                         const int32_t* __restrict__ col,
+                                                         const V* __restrict__ val, const double* __restrict__ x,
+                                                         double* __restrict__ y, const double* __restrict__ rowscale,
+                                                         const double* __restrict__ b, const double* __restrict__ q,
+                                                         int64_t nrows, int64_t nslices) {
+    int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t s = gt >> 5;
+    int lane = threadIdx.x & 31;
+    if (s >= nslices) return;
+    int64_t base = __ldg(&slice_ptr[s]) + lane;
+    int w = __ldg(&width[s]);
+    Acc acc0 = 0, acc1 = 0;
+    int k = 0;
+    for (; k + 1 < w; k += 2) {
+        int64_t i0 = base + (int64_t)k * kSlice, i1 = i0 + kSlice;
+        int32_t c0 = __ldg(&col[i0]), c1 = __ldg(&col[i1]);
+        V v0 = __ldg(&val[i0]), v1 = __ldg(&val[i1]);
+        acc0 += (Acc)v0 * (Acc)__ldg(&x[c0]);
+        acc1 += (Acc)v1 * (Acc)__ldg(&x[c1]);
+    }
+    if (k < w) {
+        int64_t i0 = base + (int64_t)k * kSlice;
+        acc0 += (Acc)__ldg(&val[i0]) * (Acc)__ldg(&x[__ldg(&col[i0])]);
+    }
+    int64_t r = s * kSlice + lane;
+    if (r >= nrows) return;
+    double out = (double)(acc0 + acc1);
+    if (rowscale) out *= rowscale[r];
+    if (b) out += b[r];
+    if (q) {
+        double xr = x[r];
+        out += q[r] * xr * xr;
+    }
+    y[r] = out;
+}
+
+static inline unsigned grid_for(int64_t threads, int block) { return (unsigned)((threads + block - 1) / block); }
+
+void launch_sell_apply64(const SellPattern& p, const double* val, const double* x, double* y, const double* rowscale,
+                         const double* b, const double* q, cudaStream_t s) {
+    if (p.nslices == 0) return;
+    sell_apply_kernel<double, double><<<grid_for(p.nslices * 32, 256), 256, 0, s>>>(
+        p.d_slice_ptr.as<int64_t>(), p.d_width.as<int32_t>(), p.d_col.as<int32_t>(), val, x, y, rowscale, b, q, p.nrows,
+        p.nslices);
+}
+
+void launch_sell_apply32(const SellPattern& p, const float* val, const double* x, double* y, const double* rowscale,
+                         const double* b, const double* q, cudaStream_t s) {
+    if (p.nslices == 0) return;
+    sell_apply_kernel<float, float><<<grid_for(p.nslices * 32, 256), 256, 0, s>>>(
+        p.d_slice_ptr.as<int64_t>(), p.d_width.as<int32_t>(), p.d_col.as<int32_t>(), val, x, y, rowscale, b, q, p.nrows,
+        p.nslices);
+}
+
+// ---------------------------------------------------------------------------------------
+// Permutation between the caller's numbering and the internal (Hilbert) numbering.
+// ---------------------------------------------------------------------------------------
+__global__ void permute_in_kernel(const int32_t* __restrict__ perm, const double* __restrict__ xref,
+                                  double* __restrict__ xint, int64_t n) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) xint[i] = __ldg(&xref[__ldg(&perm[i])]);
+}
+__global__ void permute_out_kernel(const int32_t* __restrict__ perm, const double* __restrict__ xint,
+                                   double* __restrict__ xref, int64_t n) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) xref[__ldg(&perm[i])] = xint[i];
+}
+void launch_permute_in(const int32_t* perm, const double* xref, double* xint, int64_t n, cudaStream_t s) {
+    if (n) permute_in_kernel<<<grid_for(n, 256), 256, 0, s>>>(perm, xref, xint, n);
+}
+void launch_permute_out(const int32_t* perm, const double* xint, double* xref, int64_t n, cudaStream_t s) {
+    if (n) permute_out_kernel<<<grid_for(n, 256), 256, 0, s>>>(perm, xint, xref, n);
+}
+
+// Dirichlet update: u_i <- a(x_i, y_i) on the Dirichlet list (dirichlet.jl:20-26).
+__global__ void dirichlet_kernel(const int32_t* __restrict__ idx, const double* __restrict__ val,
+                                 double* __restrict__ u, int64_t n) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) u[idx[i]] = val[i];
+}
+void launch_dirichlet(const int32_t* idx, const double* val, double* u, int64_t n, cudaStream_t s) {
+    if (n) dirichlet_kernel<<<grid_for(n, 256), 256, 0, s>>>(idx, val, u, n);
+}
+
+// ---------------------------------------------------------------------------------------
+// Per-triangle flux kernel (generic fvm_eqs! for any device-coded form).
+// One CTA per vertex tile; the CTA walks every triangle touching the tile (coalesced SoA
+// streams), evaluates the three dual-edge fluxes, and accumulates the tile's du in shared
+// memory; boundary half edges follow; then the tile's vertices are finalised in place
+// (du/V + S, Dudt, Dirichlet / missing-vertex zero) and written once.
+// ---------------------------------------------------------------------------------------
+struct TriArgs {
+    const int64_t* off;
+    const int64_t* boff;
+    const int32_t* ev;   // [3][nelem]
+    const double* g;     // [6][nelem] geometric coefficients (DDEG>0)
+    const double* ec;    // [6][nelem] folded coefficients (DDEG==0) or [3*(DDEG+1)][nelem] D polys
+    const int32_t* bv;   // [3][nbelem]
+    const double* bg;    // [3][nbelem] g_i, g_j, l_h
+    const double* bc;    // [1 + 2(DDEG+1) + 6][nbelem]
+    const int8_t* code;
+    const double* invV;
+    const double* vsrc;  // [3][np] or null
+    const double* vdudt; // [3][np] or null
+    const double* u;
+    double* du;
+    int64_t nelem, nbelem, np;
+    int tv;
+};
+
+template <int DDEG>
+__device__ __forceinline__ double dpoly(const double* c, int64_t stride, int64_t e, double x) {
+    double r = __ldg(&c[e]);
+    if (DDEG >= 1) {
+        double c1 = __ldg(&c[stride + e]);
+        if (DDEG >= 2) c1 += x * __ldg(&c[2 * stride + e]);
+        r += x * c1;
+    }
+    return r;
+}
+
+template <int DDEG>
+__global__ void __launch_bounds__(256) triangle_rhs_kernel(TriArgs a) {
+    extern __shared__ double acc[];
+    const int64_t tile = blockIdx.x;
+    const int64_t v0 = tile * a.tv;
+    for (int i = threadIdx.x; i < a.tv; i += blockDim.x) acc[i] = 0.0;
+    __syncthreads();
+    const int64_t N = a.nelem;
+    const int64_t e0 = a.off[tile], e1 = a.off[tile + 1];
+    for (int64_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+        int32_t va = __ldg(&a.ev[e]), vb = __ldg(&a.ev[N + e]), vc = __ldg(&a.ev[2 * N + e]);
+        double ua = __ldg(&a.u[va]), ub = __ldg(&a.u[vb]), uc = __ldg(&a.u[vc]);
+        double dac = ua - uc, dbc = ub - uc;
+        double Q[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const double* gc = DDEG == 0 ? a.ec : a.g;
+            double G = __ldg(&gc[(2 * d) * N + e]) * dac + __ldg(&gc[(2 * d + 1) * N + e]) * dbc;
+            if (DDEG == 0) {
+                Q[d] = G;
+            } else {
+                // u at the dual-edge midpoint (5 p_a + 5 p_b + 2 p_c)/12 of edge d
+                double us = d == 0 ? (5.0 * (ua + ub) + 2.0 * uc) / 12.0
+                          : d == 1 ? (5.0 * (ub + uc) + 2.0 * ua) / 12.0
+                                   : (5.0 * (uc + ua) + 2.0 * ub) / 12.0;
+                Q[d] = dpoly<DDEG>(a.ec + (int64_t)(d * (DDEG + 1)) * N, N, e, us) * G;
+            }
+        }
+        uint64_t la = (uint64_t)(va - v0), lb = (uint64_t)(vb - v0), lc = (uint64_t)(vc - v0);
+        if (la < (uint64_t)a.tv) atomicAdd(&acc[la], Q[2] - Q[0]);
+        if (lb < (uint64_t)a.tv) atomicAdd(&acc[lb], Q[0] - Q[1]);
+        if (lc < (uint64_t)a.tv) atomicAdd(&acc[lc], Q[1] - Q[2]);
+    }
+    // boundary half edges (boundary_edge_contributions.jl:41-65)
+    const int64_t NB = a.nbelem;
+    const int nd = DDEG + 1;
+    const int64_t b0 = a.boff[tile], b1 = a.boff[tile + 1];
+    for (int64_t e = b0 + threadIdx.x; e < b1; e += blockDim.x) {
+        int32_t vi = a.bv[e], vj = a.bv[NB + e], vk = a.bv[2 * NB + e];
+        double ui = a.u[vi], uj = a.u[vj], uk = a.u[vk];
+        double umi = (3.0 * ui + uj) / 4.0, umj = (ui + 3.0 * uj) / 4.0;
+        double lh = a.bg[2 * NB + e];
+        double Qi, Qj;
+        if (a.bc[e] != 0.0) {  // Neumann: q.n = a(m, u(m))
+            const double* n = a.bc + (int64_t)(1 + 2 * nd) * NB;
+            Qi = (n[e] + umi * (n[NB + e] + umi * n[2 * NB + e])) * lh;
+            Qj = (n[3 * NB + e] + umj * (n[4 * NB + e] + umj * n[5 * NB + e])) * lh;
+        } else {
+            double G = a.bg[e] * (ui - uk) + a.bg[NB + e] * (uj - uk);
+            Qi = dpoly<DDEG>(a.bc + NB, NB, e, umi) * G;
+            Qj = dpoly<DDEG>(a.bc + (int64_t)(1 + nd) * NB, NB, e, umj) * G;
+        }
+        uint64_t li = (uint64_t)(vi - v0), lj = (uint64_t)(vj - v0);
+        if (li < (uint64_t)a.tv) atomicAdd(&acc[li], -Qi);
+        if (lj < (uint64_t)a.tv) atomicAdd(&acc[lj], -Qj);
+    }
+    __syncthreads();
+    // finalise (source_contributions.jl:33-47)
+    for (int i = threadIdx.x; i < a.tv; i += blockDim.x) {
+        int64_t v = v0 + i;
+        if (v >= a.np) break;
+        int c = a.code[v];
+        double uu = a.u[v];
+        double r = 0.0;
+        if (c == FVM_VERTEX_FREE) {
+            r = acc[i] * a.invV[v];
+            if (a.vsrc) r += a.vsrc[v] + uu * (a.vsrc[a.np + v] + uu * a.vsrc[2 * a.np + v]);
+        } else if (c == FVM_VERTEX_DUDT) {
+            if (a.vdudt) r = a.vdudt[v] + uu * (a.vdudt[a.np + v] + uu * a.vdudt[2 * a.np + v]);
+        }
+        a.du[v] = r;
+    }
+}
+
+void launch_triangle_rhs(const fvm_mesh* m, const fvm_problem* p, const double* u, double* du, cudaStream_t s) {
+    const Tiles& T = m->tiles;
+    TriArgs a;
+    a.off = T.d_off.as<int64_t>();
+    a.boff = T.d_boff.as<int64_t>();
+    a.ev = T.d_ev.as<int32_t>();
+    a.g = T.d_g.as<double>();
+    a.ec = p->d_ec.as<double>();
+    a.bv = T.d_bv.as<int32_t>();
+    a.bg = T.d_bg.as<double>();
+    a.bc = p->d_bc.as<double>();
+    a.code = p->d_code.as<int8_t>();
+    a.invV = m->d_invV.as<double>();
+    a.vsrc = p->src.empty() ? nullptr : p->d_vsrc.as<double>();
+    a.vdudt = p->dudt.empty() ? nullptr : p->d_vdudt.as<double>();
+    a.u = u;
+    a.du = du;
+    a.nelem = T.nelem;
+    a.nbelem = T.nbelem;
+    a.np = m->np;
+    a.tv = T.tile_vertices;
+    size_t smem = sizeof(double) * T.tile_vertices;
+    switch (p->dif_deg) {
+        case 0: triangle_rhs_kernel<0><<<(unsigned)T.ntiles, 256, smem, s>>>(a); break;
+        case 1: triangle_rhs_kernel<1><<<(unsigned)T.ntiles, 256, smem, s>>>(a); break;
+        default: triangle_rhs_kernel<2><<<(unsigned)T.ntiles, 256, smem, s>>>(a); break;
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// Tsit5 stage combination, error norm, dense output
+// ---------------------------------------------------------------------------------------
+struct StageArgs {
+    const double* k[7];
+    double a[7];
+};
+
+__global__ void stage_kernel(double* __restrict__ y, const double* __restrict__ u, StageArgs sa, int nk, double dt,
+                             int64_t n) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double acc = 0.0;
+#pragma unroll
+    for (int j = 0; j < 7; ++j)
+        if (j < nk) acc += sa.a[j] * sa.k[j][i];
+    y[i] = u[i] + dt * acc;
+}
+
+void launch_stage(double* y, const double* u, const double* const* k, const double* a, int nk, double dt, int64_t n,
+                  cudaStream_t s) {
+    StageArgs sa;
+    for (int j = 0; j < 7; ++j) {
+        sa.k[j] = j < nk ? k[j] : nullptr;
+        sa.a[j] = j < nk ? a[j] : 0.0;
+    }
+    stage_kernel<<<grid_for(n, 256), 256, 0, s>>>(y, u, sa, nk, dt, n);
+}
+
+// Deterministic two-pass sum of squares of the scaled error (ODE_DEFAULT_NORM, RMS).
+__global__ void error_partial_kernel(const double* __restrict__ u, const double* __restrict__ unew, StageArgs sa,
+                                     double dt, double abstol, double reltol, int64_t n, double* __restrict__ part) {
+    __shared__ double red[256];
+    double acc = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double e = 0.0;
+#pragma unroll
+        for (int j = 0; j < 7; ++j) e += sa.a[j] * sa.k[j][i];
+        e *= dt;
+        double sc = abstol + fmax(fabs(u[i]), fabs(unew[i])) * reltol;
+        double r = e / sc;
+        acc += r * r;
+    }
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+__global__ void sum_partials_kernel(const double* __restrict__ part, int n, double* __restrict__ out) {
+    __shared__ double red[256];
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) acc += part[i];
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[0] = red[0];
+}
+constexpr int kErrBlocks = 304;
+void launch_error_norm(const double* u, const double* unew, const double* const* k, const double* bt, double dt,
+                       double abstol, double reltol, int64_t n, double* d_acc, cudaStream_t s) {
+    StageArgs sa;
+    for (int j = 0; j < 7; ++j) {
+        sa.k[j] = k[j];
+        sa.a[j] = bt[j];
+    }
+    error_partial_kernel<<<kErrBlocks, 256, 0, s>>>(u, unew, sa, dt, abstol, reltol, n, d_acc + 1);
+    sum_partials_kernel<<<1, 256, 0, s>>>(d_acc + 1, kErrBlocks, d_acc);
+}
+
+// cubic Hermite on [t_n, t_n + dt] from (u0, f0) and (u1, f1) at theta in [0, 1]
+__global__ void hermite_kernel(double* __restrict__ out, const double* __restrict__ u0, const double* __restrict__ u1,
+                               const double* __restrict__ f0, const double* __restrict__ f1, double dt, double th,
+                               int64_t n) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double t2 = th * th, t3 = t2 * th;
+    double h00 = 2 * t3 - 3 * t2 + 1, h10 = t3 - 2 * t2 + th, h01 = -2 * t3 + 3 * t2, h11 = t3 - t2;
+    out[i] = h00 * u0[i] + h10 * dt * f0[i] + h01 * u1[i] + h11 * dt * f1[i];
+}
+void launch_hermite(double* out, const double* u0, const double* u1, const double* f0, const double* f1, double dt,
+                    double theta, int64_t n, cudaStream_t s) {
+    hermite_kernel<<<grid_for(n, 256), 256, 0, s>>>(out, u0, u1, f0, f1, dt, theta, n);
+}
+
+__global__ void fill_kernel(double* x, double v, int64_t n) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) x[i] = v;
+}
+void launch_fill(double* x, double v, int64_t n, cudaStream_t s) {
+    if (n) fill_kernel<<<grid_for(n, 256), 256, 0, s>>>(x, v, n);
+}
+
+}  // namespace fvm

@@ -1,0 +1,391 @@
+// Host side of the mesh: geometry (FVMGeometry), Hilbert renumbering, the vertex-neighbour
+// operator pattern (sliced ELL) and the vertex tiles of the per-triangle flux kernel.
+// Compiled with -ffp-contract=off so the geometry arithmetic rounds like the reference.
+#include "fvm_internal.h"
+#include <algorithm>
+#include <cmath>
+#include <numeric>
+#include <unordered_map>
+
+namespace fvm {
+
+int64_t SellPattern::find(int32_t row, int32_t c) const {
+    int64_t lo = rowptr[row], hi = rowptr[row + 1];
+    const int32_t* b = csr_col.data();
+    const int32_t* it = std::lower_bound(b + lo, b + hi, c);
+    if (it == b + hi || *it != c) return -1;
+    return csr_slot[it - b];
+}
+
+// Hilbert index of (x, y) on a 2^16 x 2^16 grid (the standard rotate-and-reflect walk).
+static uint64_t hilbert_index(uint32_t x, uint32_t y) {
+    const uint32_t n = 1u << 16;
+    uint64_t d = 0;
+    for (uint32_t s = n / 2; s > 0; s /= 2) {
+        uint32_t rx = (x & s) ? 1u : 0u;
+        uint32_t ry = (y & s) ? 1u : 0u;
+        d += (uint64_t)s * s * ((3u * rx) ^ ry);
+        if (ry == 0) {
+            if (rx == 1) {
+                x = s - 1 - (x & (s - 1));
+                y = s - 1 - (y & (s - 1));
+            } else {
+                x &= (s - 1);
+                y &= (s - 1);
+            }
+            std::swap(x, y);
+        } else {
+            x &= (s - 1);
+            y &= (s - 1);
+        }
+    }
+    return d;
+}
+
+}  // namespace fvm
+
+using namespace fvm;
+
+// Geometry of one triangle, in the operation order of src/geometry.jl:107-161.
+static void triangle_geometry(const double* P, int32_t i, int32_t j, int32_t k, double* props, double S[3]) {
+    double px = P[2 * i], py = P[2 * i + 1];
+    double qx = P[2 * j], qy = P[2 * j + 1];
+    double rx = P[2 * k], ry = P[2 * k + 1];
+    // DelaunayTriangulation statistics: centroid and edge midpoints
+    double cx = (px + qx + rx) / 3, cy = (py + qy + ry) / 3;
+    double m1x = (px + qx) / 2, m1y = (py + qy) / 2;
+    double m2x = (qx + rx) / 2, m2y = (qy + ry) / 2;
+    double m3x = (rx + px) / 2, m3y = (ry + py) / 2;
+    double pcx = cx - px, pcy = cy - py;
+    double qcx = cx - qx, qcy = cy - qy;
+    double rcx = cx - rx, rcy = cy - ry;
+    double m13x = m1x - m3x, m13y = m1y - m3y;
+    double m21x = m2x - m1x, m21y = m2y - m1y;
+    double m32x = m3x - m2x, m32y = m3y - m2y;
+    S[0] = 0.5 * std::fabs(pcx * m13y - pcy * m13x);
+    S[1] = 0.5 * std::fabs(qcx * m21y - qcy * m21x);
+    S[2] = 0.5 * std::fabs(rcx * m32y - rcy * m32x);
+    double D = qx * ry - qy * rx - px * ry + rx * py + px * qy - qx * py;
+    props[0] = (qy - ry) / D;
+    props[1] = (ry - py) / D;
+    props[2] = (py - qy) / D;
+    props[3] = (rx - qx) / D;
+    props[4] = (px - rx) / D;
+    props[5] = (qx - px) / D;
+    props[6] = (qx * ry - rx * qy) / D;
+    props[7] = (rx * py - px * ry) / D;
+    props[8] = (px * qy - qx * py) / D;
+    double mx[3] = {m1x, m2x, m3x}, my[3] = {m1y, m2y, m3y};
+    for (int e = 0; e < 3; ++e) {
+        props[9 + 2 * e] = (mx[e] + cx) / 2;
+        props[10 + 2 * e] = (my[e] + cy) / 2;
+        double ex = cx - mx[e], ey = cy - my[e];
+        double l = std::sqrt(ex * ex + ey * ey);  // LinearAlgebra.norm of a 2-tuple, no rescaling needed
+        props[15 + 2 * e] = ey / l;
+        props[16 + 2 * e] = -ex / l;
+        props[21 + e] = l;
+    }
+}
+
+static inline uint64_t edge_key(int64_t a, int64_t b) { return ((uint64_t)(uint32_t)a << 32) | (uint32_t)b; }
+
+extern "C" int fvm_mesh_create_impl(const double* points, int64_t npoints, const int32_t* triangles, int64_t ntri,
+                                     const int32_t* boundary_edges, const int32_t* boundary_adjacent,
+                                     int64_t nbedge, int32_t tile_vertices, int32_t flags, fvm_mesh** out) {
+    if (!out) fail(FVM_ERR_INVALID_ARGUMENT, "out is NULL");
+    *out = nullptr;
+    if (npoints <= 0 || ntri <= 0 || nbedge < 0) fail(FVM_ERR_INVALID_ARGUMENT, "mesh sizes must be positive");
+    if (!points || !triangles || (nbedge > 0 && !boundary_edges)) fail(FVM_ERR_INVALID_ARGUMENT, "NULL mesh array");
+    if (npoints >= (int64_t)INT32_MAX || ntri >= (int64_t)INT32_MAX) fail(FVM_ERR_INVALID_ARGUMENT, "mesh too large for 32-bit indices");
+    std::unique_ptr<fvm_mesh> m(new fvm_mesh());
+    m->np = npoints;
+    m->nt = ntri;
+    m->nbe = nbedge;
+    m->tile_vertices_req = tile_vertices;
+    m->pts.assign(points, points + 2 * npoints);
+    m->tri.assign(triangles, triangles + 3 * ntri);
+    m->be.assign(boundary_edges, boundary_edges + 2 * nbedge);
+    for (int64_t t = 0; t < 3 * ntri; ++t)
+        if (m->tri[t] < 0 || m->tri[t] >= npoints)
+            fail(FVM_ERR_BAD_MESH, "triangle " + std::to_string(t / 3) + " has a vertex index out of range");
+    for (int64_t e = 0; e < 2 * nbedge; ++e)
+        if (m->be[e] < 0 || m->be[e] >= npoints)
+            fail(FVM_ERR_BAD_MESH, "boundary edge " + std::to_string(e / 2) + " has a vertex index out of range");
+
+    // geometry (src/geometry.jl:99-169), triangles in the caller's order
+    m->vol.assign(npoints, 0.0);
+    m->props.resize((size_t)24 * ntri);
+    m->has_vertex.assign(npoints, 0);
+    const double* P = m->pts.data();
+    for (int64_t t = 0; t < ntri; ++t) {
+        int32_t i = m->tri[3 * t], j = m->tri[3 * t + 1], k = m->tri[3 * t + 2];
+        double px = P[2 * i], py = P[2 * i + 1], qx = P[2 * j], qy = P[2 * j + 1], rx = P[2 * k], ry = P[2 * k + 1];
+        double D = qx * ry - qy * rx - px * ry + rx * py + px * qy - qx * py;
+        if (!(D > 0))
+            fail(FVM_ERR_BAD_MESH, "triangle " + std::to_string(t) + " is clockwise or degenerate (determinant " +
+                                       std::to_string(D) + ")");
+        double S[3];
+        triangle_geometry(P, i, j, k, &m->props[24 * t], S);
+        m->vol[i] += S[0];
+        m->vol[j] += S[1];
+        m->vol[k] += S[2];
+        m->has_vertex[i] = m->has_vertex[j] = m->has_vertex[k] = 1;
+    }
+    m->nv = 0;
+    for (int64_t v = 0; v < npoints; ++v) m->nv += m->has_vertex[v];
+
+    // boundary edge -> triangle (get_adjacent + _safe_get_triangle_props, src/utils.jl:1-11)
+    {
+        std::unordered_map<uint64_t, int32_t> dir;
+        dir.reserve((size_t)ntri * 3 * 2);
+        for (int64_t t = 0; t < ntri; ++t)
+            for (int e = 0; e < 3; ++e) {
+                int32_t a = m->tri[3 * t + e], b = m->tri[3 * t + (e + 1) % 3];
+                dir[edge_key(a, b)] = (int32_t)t;
+            }
+        m->btri.resize(nbedge);
+        m->badj.resize(nbedge);
+        for (int64_t e = 0; e < nbedge; ++e) {
+            int32_t i = m->be[2 * e], j = m->be[2 * e + 1];
+            auto it = dir.find(edge_key(i, j));
+            if (it == dir.end())
+                fail(FVM_ERR_BAD_MESH, "boundary edge " + std::to_string(e) + " (" + std::to_string(i) + ", " +
+                                           std::to_string(j) + ") has no solid triangle on its left");
+            int32_t t = it->second;
+            int32_t k = -1;
+            for (int c = 0; c < 3; ++c) {
+                int32_t v = m->tri[3 * t + c];
+                if (v != i && v != j) k = v;
+            }
+            if (boundary_adjacent && boundary_adjacent[e] != k)
+                fail(FVM_ERR_BAD_MESH, "boundary_adjacent[" + std::to_string(e) + "] does not match the triangle on the edge");
+            m->btri[e] = t;
+            m->badj[e] = k;
+        }
+    }
+
+    // Hilbert renumbering of vertices; points that are not vertices go last
+    m->perm.resize(npoints);
+    m->iperm.resize(npoints);
+    if (flags & FVM_MESH_NO_RENUMBER) {
+        std::iota(m->perm.begin(), m->perm.end(), 0);
+    } else {
+        double xmin = 1e300, xmax = -1e300, ymin = 1e300, ymax = -1e300;
+        for (int64_t v = 0; v < npoints; ++v) {
+            xmin = std::min(xmin, P[2 * v]);
+            xmax = std::max(xmax, P[2 * v]);
+            ymin = std::min(ymin, P[2 * v + 1]);
+            ymax = std::max(ymax, P[2 * v + 1]);
+        }
+        double span = std::max(xmax - xmin, ymax - ymin);
+        if (!(span > 0)) span = 1.0;
+        std::vector<std::pair<uint64_t, int32_t>> key(npoints);
+        for (int64_t v = 0; v < npoints; ++v) {
+            uint32_t hx = (uint32_t)std::min(65535.0, std::floor((P[2 * v] - xmin) / span * 65535.0));
+            uint32_t hy = (uint32_t)std::min(65535.0, std::floor((P[2 * v + 1] - ymin) / span * 65535.0));
+            uint64_t h = hilbert_index(hx, hy);
+            if (!m->has_vertex[v]) h = ~0ull;
+            key[v] = {h, (int32_t)v};
+        }
+        std::sort(key.begin(), key.end());
+        for (int64_t v = 0; v < npoints; ++v) m->perm[v] = key[v].second;
+    }
+    for (int64_t v = 0; v < npoints; ++v) m->iperm[m->perm[v]] = (int32_t)v;
+
+    // vertex-neighbour pattern (internal numbering): diagonal + every pair within a triangle
+    {
+        SellPattern& pat = m->pat;
+        pat.nrows = npoints;
+        std::vector<int64_t> cnt(npoints + 1, 0);
+        for (int64_t v = 0; v < npoints; ++v) cnt[v] = 1;
+        for (int64_t t = 0; t < ntri; ++t)
+            for (int a = 0; a < 3; ++a) cnt[m->iperm[m->tri[3 * t + a]]] += 2;
+        std::vector<int64_t> start(npoints + 1, 0);
+        for (int64_t v = 0; v < npoints; ++v) start[v + 1] = start[v] + cnt[v];
+        std::vector<int32_t> tmp(start[npoints]);
+        std::vector<int64_t> fillp(start.begin(), start.end() - 1);
+        for (int64_t v = 0; v < npoints; ++v) tmp[fillp[v]++] = (int32_t)v;
+        for (int64_t t = 0; t < ntri; ++t) {
+            int32_t w[3] = {m->iperm[m->tri[3 * t]], m->iperm[m->tri[3 * t + 1]], m->iperm[m->tri[3 * t + 2]]};
+            for (int a = 0; a < 3; ++a)
+                for (int b = 0; b < 3; ++b)
+                    if (a != b) tmp[fillp[w[a]]++] = w[b];
+        }
+        pat.rowptr.assign(npoints + 1, 0);
+        pat.csr_col.clear();
+        pat.csr_col.reserve(start[npoints] / 2 + npoints);
+        for (int64_t v = 0; v < npoints; ++v) {
+            std::sort(tmp.begin() + start[v], tmp.begin() + start[v + 1]);
+            int32_t last = -1;
+            for (int64_t q = start[v]; q < start[v + 1]; ++q)
+                if (tmp[q] != last) {
+                    pat.csr_col.push_back(tmp[q]);
+                    last = tmp[q];
+                }
+            pat.rowptr[v + 1] = (int64_t)pat.csr_col.size();
+        }
+        pat.nnz = (int64_t)pat.csr_col.size();
+        pat.nslices = (npoints + kSlice - 1) / kSlice;
+        pat.slice_ptr.assign(pat.nslices + 1, 0);
+        pat.width.assign(pat.nslices, 0);
+        for (int64_t s = 0; s < pat.nslices; ++s) {
+            int32_t w = 0;
+            for (int64_t r = s * kSlice; r < std::min<int64_t>(npoints, (s + 1) * kSlice); ++r)
+                w = std::max<int32_t>(w, (int32_t)(pat.rowptr[r + 1] - pat.rowptr[r]));
+            pat.width[s] = w;
+            pat.slice_ptr[s + 1] = pat.slice_ptr[s] + (int64_t)w * kSlice;
+        }
+        pat.nslots = pat.slice_ptr[pat.nslices];
+        pat.col.assign(pat.nslots, 0);
+        pat.csr_slot.assign(pat.nnz, 0);
+        for (int64_t s = 0; s < pat.nslices; ++s)
+            for (int lane = 0; lane < kSlice; ++lane) {
+                int64_t r = s * kSlice + lane;
+                int64_t len = r < npoints ? pat.rowptr[r + 1] - pat.rowptr[r] : 0;
+                int32_t pad = r < npoints ? (int32_t)r : (int32_t)(npoints - 1);
+                for (int32_t q = 0; q < pat.width[s]; ++q) {
+                    int64_t slot = pat.slice_ptr[s] + (int64_t)q * kSlice + lane;
+                    if (q < len) {
+                        pat.col[slot] = pat.csr_col[pat.rowptr[r] + q];
+                        pat.csr_slot[pat.rowptr[r] + q] = slot;
+                    } else {
+                        pat.col[slot] = pad;
+                    }
+                }
+            }
+        pat.d_slice_ptr.upload(pat.slice_ptr);
+        pat.d_width.upload(pat.width);
+        pat.d_col.upload(pat.col);
+    }
+
+    // device-side vertex data
+    m->d_perm.upload(m->perm);
+    m->d_iperm.upload(m->iperm);
+    {
+        std::vector<double> invV(npoints, 0.0);
+        for (int64_t v = 0; v < npoints; ++v) {
+            double V = m->vol[m->perm[v]];
+            invV[v] = V > 0 ? 1.0 / V : 0.0;
+        }
+        m->d_invV.upload(invV);
+    }
+    *out = m.release();
+    return FVM_OK;
+}
+
+// Tiles of the per-triangle flux kernel: vertex range [t*TV, (t+1)*TV) of the internal
+// numbering; a tile lists every triangle (and boundary edge) that scatters into it.
+void fvm_mesh::build_tiles() {
+    if (tiles.built) return;
+    Tiles& T = tiles;
+    int TV = tile_vertices_req > 0 ? tile_vertices_req : 1024;
+    if (TV % 32 || TV > 4096) fail(FVM_ERR_INVALID_ARGUMENT, "tile_vertices must be a multiple of 32 and <= 4096");
+    T.tile_vertices = TV;
+    T.ntiles = (np + TV - 1) / TV;
+    // triangles ordered by their smallest internal vertex
+    std::vector<int32_t> order(nt);
+    std::iota(order.begin(), order.end(), 0);
+    std::vector<int32_t> minv(nt);
+    for (int64_t t = 0; t < nt; ++t)
+        minv[t] = std::min({iperm[tri[3 * t]], iperm[tri[3 * t + 1]], iperm[tri[3 * t + 2]]});
+    std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) { return minv[a] < minv[b]; });
+    std::vector<int64_t> cnt(T.ntiles + 1, 0);
+    auto tiles_of = [&](const int32_t* w, int n, int64_t* out) {
+        int c = 0;
+        for (int a = 0; a < n; ++a) {
+            int64_t tt = w[a] / TV;
+            bool dup = false;
+            for (int b = 0; b < c; ++b) dup |= out[b] == tt;
+            if (!dup) out[c++] = tt;
+        }
+        return c;
+    };
+    for (int64_t t = 0; t < nt; ++t) {
+        int32_t w[3] = {iperm[tri[3 * t]], iperm[tri[3 * t + 1]], iperm[tri[3 * t + 2]]};
+        int64_t ts[3];
+        int c = tiles_of(w, 3, ts);
+        for (int a = 0; a < c; ++a) cnt[ts[a]]++;
+    }
+    T.off.assign(T.ntiles + 1, 0);
+    for (int64_t t = 0; t < T.ntiles; ++t) T.off[t + 1] = T.off[t] + cnt[t];
+    T.nelem = T.off[T.ntiles];
+    T.etri.assign(T.nelem, 0);
+    T.ev.assign(3 * T.nelem, 0);
+    std::vector<int64_t> fill(T.off.begin(), T.off.end() - 1);
+    for (int64_t q = 0; q < nt; ++q) {
+        int32_t t = order[q];
+        int32_t w[3] = {iperm[tri[3 * t]], iperm[tri[3 * t + 1]], iperm[tri[3 * t + 2]]};
+        int64_t ts[3];
+        int c = tiles_of(w, 3, ts);
+        for (int a = 0; a < c; ++a) {
+            int64_t e = fill[ts[a]]++;
+            T.etri[e] = t;
+            T.ev[e] = w[0];
+            T.ev[T.nelem + e] = w[1];
+            T.ev[2 * T.nelem + e] = w[2];
+        }
+    }
+    // geometric flux coefficients g[e][v] = -l_e (s_v n_ex + s_{3+v} n_ey), v = 0, 1 in the
+    // difference basis (u_v - u_2): Q_e = D_e (g[e][0] (u0 - u2) + g[e][1] (u1 - u2))
+    std::vector<double> g(6 * T.nelem);
+    for (int64_t e = 0; e < T.nelem; ++e) {
+        const double* pr = &props[24 * (size_t)T.etri[e]];
+        for (int d = 0; d < 3; ++d) {
+            double nx = pr[15 + 2 * d], ny = pr[16 + 2 * d], l = pr[21 + d];
+            for (int v = 0; v < 2; ++v) g[(2 * d + v) * T.nelem + e] = -l * (pr[v] * nx + pr[3 + v] * ny);
+        }
+    }
+    // boundary edges
+    std::vector<int64_t> bcnt(T.ntiles + 1, 0);
+    for (int64_t e = 0; e < nbe; ++e) {
+        int32_t w[2] = {iperm[be[2 * e]], iperm[be[2 * e + 1]]};
+        int64_t ts[2];
+        int c = tiles_of(w, 2, ts);
+        for (int a = 0; a < c; ++a) bcnt[ts[a]]++;
+    }
+    T.boff.assign(T.ntiles + 1, 0);
+    for (int64_t t = 0; t < T.ntiles; ++t) T.boff[t + 1] = T.boff[t] + bcnt[t];
+    T.nbelem = T.boff[T.ntiles];
+    T.ebedge.assign(T.nbelem, 0);
+    T.bv.assign(3 * T.nbelem, 0);
+    std::vector<double> bg(3 * std::max<int64_t>(T.nbelem, 1));
+    std::vector<int64_t> bfill(T.boff.begin(), T.boff.end() - 1);
+    for (int64_t e = 0; e < nbe; ++e) {
+        int32_t i = be[2 * e], j = be[2 * e + 1], k = badj[e];
+        int32_t w[2] = {iperm[i], iperm[j]};
+        int64_t ts[2];
+        int c = tiles_of(w, 2, ts);
+        // G = -l_h (alpha nx + beta ny) in the basis (u_i - u_k), (u_j - u_k)
+        double px = pts[2 * i], py = pts[2 * i + 1], qx = pts[2 * j], qy = pts[2 * j + 1];
+        double lij = std::sqrt((qx - px) * (qx - px) + (qy - py) * (qy - py));
+        double nx = (qy - py) / lij, ny = -(qx - px) / lij;
+        double mijx = (px + qx) / 2, mijy = (py + qy) / 2;
+        double lh = std::sqrt((mijx - px) * (mijx - px) + (mijy - py) * (mijy - py));
+        const double* pr = &props[24 * (size_t)btri[e]];
+        int32_t tv[3] = {tri[3 * btri[e]], tri[3 * btri[e] + 1], tri[3 * btri[e] + 2]};
+        double gi = 0, gj = 0;
+        for (int v = 0; v < 3; ++v) {
+            double c0 = -lh * (pr[v] * nx + pr[3 + v] * ny);
+            if (tv[v] == i) gi = c0;
+            if (tv[v] == j) gj = c0;
+        }
+        for (int a = 0; a < c; ++a) {
+            int64_t q = bfill[ts[a]]++;
+            T.ebedge[q] = (int32_t)e;
+            T.bv[q] = iperm[i];
+            T.bv[T.nbelem + q] = iperm[j];
+            T.bv[2 * T.nbelem + q] = iperm[k];
+            bg[q] = gi;
+            bg[T.nbelem + q] = gj;
+            bg[2 * T.nbelem + q] = lh;
+        }
+    }
+    T.d_off.upload(T.off);
+    T.d_boff.upload(T.boff);
+    T.d_ev.upload(T.ev);
+    T.d_bv.upload(T.bv);
+    T.d_g.upload(g);
+    bg.resize(3 * T.nbelem);
+    T.d_bg.upload(bg);
+    T.built = true;
+}

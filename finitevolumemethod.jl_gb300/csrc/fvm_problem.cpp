@@ -1,0 +1,272 @@
+// Problem set-up: copies the sampled closure forms, folds linear forms into the
+// vertex-neighbour operator, and prepares the per-triangle path for nonlinear forms.
+#include "fvm_internal.h"
+#include <algorithm>
+#include <cmath>
+
+using namespace fvm;
+
+static void check_deg(int d, const char* what) {
+    if (d < 0 || d > 2) fail(FVM_ERR_UNSUPPORTED_FORM, std::string(what) + " degree must be 0, 1 or 2");
+}
+
+void fvm_problem::ensure_work() {
+    const fvm_mesh* m = mesh;
+    if (!d_u.p) d_u.alloc(sizeof(double) * m->np);
+    if (!d_du.p) d_du.alloc(sizeof(double) * m->np);
+    if (!d_ref.p) d_ref.alloc(sizeof(double) * m->np);
+}
+
+// Linear operator values of the generic RHS (fvm_eqs!), in the internal numbering.
+// Row i of a FREE vertex: (sum of triangle and boundary fluxes)/V_i + S_i
+// (triangle_contributions.jl:10-15, boundary_edge_contributions.jl:61-65,
+// source_contributions.jl:41), with every flux linear in u:
+//   triangle dual edge e of T = (a, b, c): Q_e = -D_e l_e (alpha n_x + beta n_y)
+//   boundary half edge (non-Neumann):      Q_h = -D_h l_h (alpha n_x + beta n_y)
+//   boundary half edge (Neumann, a = n0 + n1 u(m)): Q_h = l_h (n0 + n1 u(m)).
+static void assemble_generic(fvm_problem* p, std::vector<double>& A, std::vector<double>& b,
+                             std::vector<double>& q, std::vector<double>& rowscale) {
+    const fvm_mesh* m = p->mesh;
+    const SellPattern& pat = m->pat;
+    A.assign(pat.nslots, 0.0);
+    b.assign(m->np, 0.0);
+    q.assign(m->np, 0.0);
+    rowscale.assign(m->np, 0.0);
+    auto add = [&](int32_t r, int32_t c, double v) {
+        int64_t s = pat.find(m->iperm[r], m->iperm[c]);
+        A[s] += v;
+    };
+    const int nd = p->dif_deg + 1;
+    for (int64_t t = 0; t < m->nt; ++t) {
+        const int32_t* w = &m->tri[3 * t];
+        const double* pr = &m->props[24 * t];
+        for (int e = 0; e < 3; ++e) {
+            int32_t e1 = w[e], e2 = w[(e + 1) % 3];
+            double D = p->dualD.empty() ? 0.0 : p->dualD[(3 * t + e) * nd];
+            double Dl = D * pr[21 + e];
+            double nx = pr[15 + 2 * e], ny = pr[16 + 2 * e];
+            bool f1 = p->code[e1] == FVM_VERTEX_FREE, f2 = p->code[e2] == FVM_VERTEX_FREE;
+            for (int v = 0; v < 3; ++v) {
+                double a = Dl * (pr[v] * nx + pr[3 + v] * ny);
+                if (f1) add(e1, w[v], a / m->vol[e1]);
+                if (f2) add(e2, w[v], -a / m->vol[e2]);
+            }
+        }
+    }
+    const int nn = p->neu_deg + 1;
+    for (int64_t e = 0; e < m->nbe; ++e) {
+        int32_t i = m->be[2 * e], j = m->be[2 * e + 1];
+        double px = m->pts[2 * i], py = m->pts[2 * i + 1], qx = m->pts[2 * j], qy = m->pts[2 * j + 1];
+        double lij = std::sqrt((qx - px) * (qx - px) + (qy - py) * (qy - py));
+        double nx = (qy - py) / lij, ny = -(qx - px) / lij;
+        double mijx = (px + qx) / 2, mijy = (py + qy) / 2;
+        double lh = std::sqrt((mijx - px) * (mijx - px) + (mijy - py) * (mijy - py));
+        bool fi = p->code[i] == FVM_VERTEX_FREE, fj = p->code[j] == FVM_VERTEX_FREE;
+        if (p->bneu[e]) {
+            double n0i = p->quarterN.empty() ? 0.0 : p->quarterN[(2 * e) * nn];
+            double n0j = p->quarterN.empty() ? 0.0 : p->quarterN[(2 * e + 1) * nn];
+            double n1i = (nn > 1 && !p->quarterN.empty()) ? p->quarterN[(2 * e) * nn + 1] : 0.0;
+            double n1j = (nn > 1 && !p->quarterN.empty()) ? p->quarterN[(2 * e + 1) * nn + 1] : 0.0;
+            if (fi) {
+                b[m->iperm[i]] -= lh * n0i / m->vol[i];
+                if (n1i != 0) {
+                    add(i, i, -lh * n1i * 0.75 / m->vol[i]);
+                    add(i, j, -lh * n1i * 0.25 / m->vol[i]);
+                }
+            }
+            if (fj) {
+                b[m->iperm[j]] -= lh * n0j / m->vol[j];
+                if (n1j != 0) {
+                    add(j, i, -lh * n1j * 0.25 / m->vol[j]);
+                    add(j, j, -lh * n1j * 0.75 / m->vol[j]);
+                }
+            }
+            continue;
+        }
+        int32_t t = m->btri[e];
+        const int32_t* w = &m->tri[3 * t];
+        const double* pr = &m->props[24 * t];
+        double Di = p->quarterD.empty() ? 0.0 : p->quarterD[(2 * e) * nd];
+        double Dj = p->quarterD.empty() ? 0.0 : p->quarterD[(2 * e + 1) * nd];
+        for (int v = 0; v < 3; ++v) {
+            double c = lh * (pr[v] * nx + pr[3 + v] * ny);
+            if (fi) add(i, w[v], Di * c / m->vol[i]);
+            if (fj) add(j, w[v], Dj * c / m->vol[j]);
+        }
+    }
+    const int ns = p->src_deg + 1, nu = p->dudt_deg + 1;
+    for (int64_t v = 0; v < m->np; ++v) {
+        int32_t r = m->iperm[v];
+        int c = p->code[v];
+        if (c == FVM_VERTEX_FREE) {
+            rowscale[r] = 1.0 / m->vol[v];
+            if (!p->src.empty()) {
+                b[r] += p->src[v * ns];
+                if (ns > 1 && p->src[v * ns + 1] != 0) add((int32_t)v, (int32_t)v, p->src[v * ns + 1]);
+                if (ns > 2) q[r] = p->src[v * ns + 2];
+            }
+        } else if (c == FVM_VERTEX_DUDT) {
+            rowscale[r] = 1.0;
+            if (!p->dudt.empty()) {
+                b[r] = p->dudt[v * nu];
+                if (nu > 1 && p->dudt[v * nu + 1] != 0) add((int32_t)v, (int32_t)v, p->dudt[v * nu + 1]);
+                if (nu > 2) q[r] = p->dudt[v * nu + 2];
+            }
+        }
+    }
+}
+
+extern "C" int fvm_problem_create_impl(fvm_mesh* mesh, const fvm_problem_desc* d, fvm_problem** out) {
+    if (!mesh || !d || !out) fail(FVM_ERR_INVALID_ARGUMENT, "NULL argument");
+    *out = nullptr;
+    if (!d->vertex_code) fail(FVM_ERR_INVALID_ARGUMENT, "vertex_code is required");
+    if (mesh->nbe > 0 && !d->bedge_neumann) fail(FVM_ERR_INVALID_ARGUMENT, "bedge_neumann is required");
+    check_deg(d->diffusion_degree, "diffusion");
+    check_deg(d->neumann_degree, "Neumann");
+    check_deg(d->source_degree, "source");
+    check_deg(d->dudt_degree, "Dudt");
+    if (d->precision != FVM_FP64 && d->precision != FVM_FP32) fail(FVM_ERR_INVALID_ARGUMENT, "precision must be FVM_FP64 or FVM_FP32");
+    std::unique_ptr<fvm_problem> p(new fvm_problem());
+    const fvm_mesh* m = mesh;
+    p->mesh = mesh;
+    p->precision = d->precision;
+    p->dif_deg = d->diffusion_degree;
+    p->neu_deg = d->neumann_degree;
+    p->src_deg = d->source_degree;
+    p->dudt_deg = d->dudt_degree;
+    p->code.assign(d->vertex_code, d->vertex_code + m->np);
+    for (int64_t v = 0; v < m->np; ++v) {
+        int c = p->code[v];
+        if (c < 0 || c > 3) fail(FVM_ERR_INVALID_ARGUMENT, "vertex_code[" + std::to_string(v) + "] is not an FVM_VERTEX_* code");
+        if (!m->has_vertex[v] && c != FVM_VERTEX_NOT_A_VERTEX)
+            fail(FVM_ERR_INVALID_ARGUMENT, "point " + std::to_string(v) + " is in no triangle but its code is not FVM_VERTEX_NOT_A_VERTEX");
+        if (m->has_vertex[v] && c == FVM_VERTEX_NOT_A_VERTEX)
+            fail(FVM_ERR_INVALID_ARGUMENT, "point " + std::to_string(v) + " is a vertex but its code is FVM_VERTEX_NOT_A_VERTEX");
+    }
+    p->bneu.assign(m->nbe, 0);
+    for (int64_t e = 0; e < m->nbe; ++e) p->bneu[e] = d->bedge_neumann[e] ? 1 : 0;
+    auto copy = [](const double* src, size_t n, std::vector<double>& dst) {
+        if (src) dst.assign(src, src + n);
+    };
+    copy(d->dual_edge_D, (size_t)m->nt * 3 * (p->dif_deg + 1), p->dualD);
+    copy(d->quarter_D, (size_t)m->nbe * 2 * (p->dif_deg + 1), p->quarterD);
+    copy(d->quarter_neumann, (size_t)m->nbe * 2 * (p->neu_deg + 1), p->quarterN);
+    copy(d->source, (size_t)m->np * (p->src_deg + 1), p->src);
+    copy(d->dudt, (size_t)m->np * (p->dudt_deg + 1), p->dudt);
+    copy(d->dirichlet, (size_t)m->np, p->dirv);
+    for (const auto* arr : {&p->dualD, &p->quarterD, &p->quarterN, &p->src, &p->dudt, &p->dirv})
+        for (double x : *arr)
+            if (!std::isfinite(x)) fail(FVM_ERR_INVALID_ARGUMENT, "sampled closure values must be finite");
+    // a form is linear when it is affine in u, except a u^2 term on a vertex's own value
+    auto nonzero_deg = [](const std::vector<double>& a, int deg, int k) {
+        if (a.empty() || deg < k) return false;
+        for (size_t i = k; i < a.size(); i += deg + 1)
+            if (a[i] != 0) return true;
+        return false;
+    };
+    p->linear = !(nonzero_deg(p->dualD, p->dif_deg, 1) || nonzero_deg(p->dualD, p->dif_deg, 2) ||
+                  nonzero_deg(p->quarterD, p->dif_deg, 1) || nonzero_deg(p->quarterD, p->dif_deg, 2) ||
+                  nonzero_deg(p->quarterN, p->neu_deg, 2));
+
+    // vertex classification and Dirichlet list (internal numbering)
+    {
+        std::vector<int8_t> code_int(m->np);
+        for (int64_t v = 0; v < m->np; ++v) code_int[m->iperm[v]] = p->code[v];
+        p->d_code.upload(code_int);
+        std::vector<int32_t> idx;
+        std::vector<double> val;
+        for (int64_t v = 0; v < m->np; ++v)
+            if (p->code[v] == FVM_VERTEX_DIRICHLET) {
+                idx.push_back(m->iperm[v]);
+                val.push_back(p->dirv.empty() ? 0.0 : p->dirv[v]);
+            }
+        p->ndir = (int64_t)idx.size();
+        p->d_dir_idx.upload(idx);
+        p->d_dir_val.upload(val);
+    }
+    if (p->linear) {
+        std::vector<double> A, b, q, rs;
+        assemble_generic(p.get(), A, b, q, rs);
+        p->d_val64.upload(A);
+        p->has_b = std::any_of(b.begin(), b.end(), [](double x) { return x != 0; });
+        p->has_q = std::any_of(q.begin(), q.end(), [](double x) { return x != 0; });
+        if (p->has_b) p->d_b.upload(b);
+        if (p->has_q) p->d_q.upload(q);
+        if (p->precision == FVM_FP32) {
+            std::vector<float> A32(A.size(), 0.0f);
+            const SellPattern& pat = m->pat;
+            for (int64_t s = 0; s < pat.nslices; ++s)
+                for (int lane = 0; lane < kSlice; ++lane) {
+                    int64_t r = s * kSlice + lane;
+                    if (r >= m->np) continue;
+                    double sc = rs[r];
+                    for (int32_t k = 0; k < pat.width[s]; ++k) {
+                        int64_t slot = pat.slice_ptr[s] + (int64_t)k * kSlice + lane;
+                        A32[slot] = sc != 0 ? (float)(A[slot] / sc) : 0.0f;
+                    }
+                }
+            p->d_val32.upload(A32);
+            p->d_rowscale.upload(rs);
+        }
+    }
+    *out = p.release();
+    return FVM_OK;
+}
+
+// Per-element data of the per-triangle flux kernel (used for nonlinear forms, or on request).
+void fvm_problem::build_triangle_path() {
+    if (tri_ready) return;
+    fvm_mesh* m = mesh;
+    m->build_tiles();
+    const Tiles& T = m->tiles;
+    const int nd = dif_deg + 1;
+    if (dif_deg == 0) {
+        // fold D into the geometric coefficients: c[e][v] = D_e g[e][v]
+        std::vector<double> g(6 * T.nelem);
+        FVM_CUDA(cudaMemcpy(g.data(), T.d_g.p, g.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        for (int64_t e = 0; e < T.nelem; ++e)
+            for (int d = 0; d < 3; ++d) {
+                double D = dualD.empty() ? 0.0 : dualD[(3 * (size_t)T.etri[e] + d) * nd];
+                g[(2 * d) * T.nelem + e] *= D;
+                g[(2 * d + 1) * T.nelem + e] *= D;
+            }
+        d_ec.upload(g);
+    } else {
+        std::vector<double> c((size_t)3 * nd * T.nelem, 0.0);
+        for (int64_t e = 0; e < T.nelem; ++e)
+            for (int d = 0; d < 3; ++d)
+                for (int k = 0; k < nd; ++k)
+                    c[(size_t)(d * nd + k) * T.nelem + e] = dualD.empty() ? 0.0 : dualD[(3 * (size_t)T.etri[e] + d) * nd + k];
+        d_ec.upload(c);
+    }
+    // boundary elements: [0] Neumann flag, D(m_i) poly, D(m_j) poly, N(m_i) poly (3), N(m_j) poly (3)
+    const int nrow = 1 + 2 * nd + 6;
+    std::vector<double> bc((size_t)nrow * std::max<int64_t>(T.nbelem, 1), 0.0);
+    const int nn = neu_deg + 1;
+    for (int64_t q = 0; q < T.nbelem; ++q) {
+        int32_t e = T.ebedge[q];
+        auto at = [&](int row) -> double& { return bc[(size_t)row * T.nbelem + q]; };
+        at(0) = bneu[e] ? 1.0 : 0.0;
+        for (int k = 0; k < nd; ++k) {
+            at(1 + k) = quarterD.empty() ? 0.0 : quarterD[(2 * (size_t)e) * nd + k];
+            at(1 + nd + k) = quarterD.empty() ? 0.0 : quarterD[(2 * (size_t)e + 1) * nd + k];
+        }
+        for (int k = 0; k < nn; ++k) {
+            at(1 + 2 * nd + k) = quarterN.empty() ? 0.0 : quarterN[(2 * (size_t)e) * nn + k];
+            at(1 + 2 * nd + 3 + k) = quarterN.empty() ? 0.0 : quarterN[(2 * (size_t)e + 1) * nn + k];
+        }
+    }
+    bc.resize((size_t)nrow * T.nbelem);
+    d_bc.upload(bc);
+    // per-vertex polynomials (internal numbering), [3][np]
+    std::vector<double> vs(3 * m->np, 0.0), vd(3 * m->np, 0.0);
+    const int ns = src_deg + 1, nu = dudt_deg + 1;
+    for (int64_t v = 0; v < m->np; ++v) {
+        int32_t r = m->iperm[v];
+        for (int k = 0; k < ns && !src.empty(); ++k) vs[k * m->np + r] = src[v * ns + k];
+        for (int k = 0; k < nu && !dudt.empty(); ++k) vd[k * m->np + r] = dudt[v * nu + k];
+    }
+    d_vsrc.upload(vs);
+    d_vdudt.upload(vd);
+    tri_ready = true;
+}

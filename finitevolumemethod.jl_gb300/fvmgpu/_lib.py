@@ -1,0 +1,235 @@
+"""ctypes binding of libfvmgpu.so (the C ABI declared in include/fvm_gpu.h).
+
+There is no CPU fallback: when the library is missing or no GPU is present, every compute
+call raises.  Build the library with `fvmgpu._build.build()`.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+from . import _build
+
+FVM_OK = 0
+FVM_ERR_INVALID_ARGUMENT = 1
+FVM_ERR_BAD_MESH = 2
+FVM_ERR_UNSUPPORTED_FORM = 3
+FVM_ERR_CUDA = 4
+FVM_ERR_OUT_OF_MEMORY = 5
+FVM_ERR_NOT_CONVERGED = 6
+FVM_ERR_UNSUPPORTED = 7
+FVM_ERR_STEP_LIMIT = 8
+
+FVM_VERTEX_FREE, FVM_VERTEX_DIRICHLET, FVM_VERTEX_DUDT, FVM_VERTEX_NOT_A_VERTEX = 0, 1, 2, 3
+FVM_PTR_HOST, FVM_PTR_DEVICE, FVM_PTR_DEVICE_INTERNAL = 0, 1, 2
+FVM_RHS_FORCE_TRIANGLE = 16
+FVM_FP64, FVM_FP32 = 0, 1
+FVM_MESH_NO_RENUMBER = 1
+FVM_TEMPLATE_DIFFUSION, FVM_TEMPLATE_LINEAR_REACTION_DIFFUSION = 0, 1
+FVM_TEMPLATE_POISSON, FVM_TEMPLATE_MEAN_EXIT_TIME = 2, 3
+FVM_SOLVER_AUTO, FVM_SOLVER_CG, FVM_SOLVER_BICGSTAB = 0, 1, 2
+FVM_PRECOND_JACOBI, FVM_PRECOND_CHEBYSHEV = 0, 1
+FVM_SOLVE_FP64, FVM_SOLVE_MIXED = 0, 1
+
+
+class FVMError(RuntimeError):
+    """A non-zero status from libfvmgpu."""
+
+    def __init__(self, code, msg):
+        super().__init__(f"[fvm status {code}] {msg}")
+        self.code = code
+
+
+class UnsupportedFormError(FVMError, ValueError):
+    pass
+
+
+class NotConvergedError(FVMError):
+    pass
+
+
+c_double_p = C.POINTER(C.c_double)
+c_int32_p = C.POINTER(C.c_int32)
+c_int64_p = C.POINTER(C.c_int64)
+c_int8_p = C.POINTER(C.c_int8)
+
+
+class ProblemDesc(C.Structure):
+    _fields_ = [
+        ("vertex_code", c_int8_p),
+        ("bedge_neumann", c_int8_p),
+        ("diffusion_degree", C.c_int32),
+        ("dual_edge_D", c_double_p),
+        ("quarter_D", c_double_p),
+        ("neumann_degree", C.c_int32),
+        ("quarter_neumann", c_double_p),
+        ("source_degree", C.c_int32),
+        ("source", c_double_p),
+        ("dudt_degree", C.c_int32),
+        ("dudt", c_double_p),
+        ("dirichlet", c_double_p),
+        ("precision", C.c_int32),
+    ]
+
+
+class OdeOptions(C.Structure):
+    _fields_ = [
+        ("t0", C.c_double), ("tf", C.c_double), ("dt", C.c_double),
+        ("adaptive", C.c_int32), ("abstol", C.c_double), ("reltol", C.c_double),
+        ("max_steps", C.c_int64), ("saveat", c_double_p), ("nsave", C.c_int64),
+        ("use_graph", C.c_int32), ("precision", C.c_int32),
+    ]
+
+
+class OdeStats(C.Structure):
+    _fields_ = [
+        ("naccept", C.c_int64), ("nreject", C.c_int64), ("nrhs", C.c_int64),
+        ("t_final", C.c_double), ("elapsed_ms", C.c_double),
+    ]
+
+
+class SolverOptions(C.Structure):
+    _fields_ = [
+        ("rtol", C.c_double), ("max_iters", C.c_int64), ("method", C.c_int32), ("precond", C.c_int32),
+        ("cheb_degree", C.c_int32), ("mode", C.c_int32), ("inner_reduction", C.c_double),
+    ]
+
+
+class SolverStats(C.Structure):
+    _fields_ = [
+        ("iterations", C.c_int64), ("refinements", C.c_int64), ("rel_residual", C.c_double),
+        ("elapsed_ms", C.c_double), ("method_used", C.c_int32), ("symmetric", C.c_int32),
+    ]
+
+
+# name -> (restype, argtypes); exactly the declarations of include/fvm_gpu.h
+SIGNATURES = {
+    "fvm_version": (C.c_int, []),
+    "fvm_last_error": (C.c_int, [C.c_char_p, C.c_size_t]),
+    "fvm_device_count": (C.c_int, [C.POINTER(C.c_int)]),
+    "fvm_mesh_create": (C.c_int, [c_double_p, C.c_int64, c_int32_p, C.c_int64, c_int32_p, c_int32_p, C.c_int64,
+                                  C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
+    "fvm_mesh_destroy": (C.c_int, [C.c_void_p]),
+    "fvm_mesh_info": (C.c_int, [C.c_void_p, c_int64_p]),
+    "fvm_mesh_geometry": (C.c_int, [C.c_void_p, c_double_p, c_double_p]),
+    "fvm_mesh_sample_points": (C.c_int, [C.c_void_p, c_double_p, c_double_p]),
+    "fvm_mesh_permutation": (C.c_int, [C.c_void_p, c_int32_p]),
+    "fvm_mesh_export_connectivity": (C.c_int, [C.c_void_p, c_int32_p, c_int32_p]),
+    "fvm_problem_create": (C.c_int, [C.c_void_p, C.POINTER(ProblemDesc), C.POINTER(C.c_void_p)]),
+    "fvm_problem_destroy": (C.c_int, [C.c_void_p]),
+    "fvm_problem_export_codes": (C.c_int, [C.c_void_p, c_int8_p, c_int8_p]),
+    "fvm_rhs": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int32, C.c_void_p]),
+    "fvm_dirichlet_apply": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_int32, C.c_void_p]),
+    "fvm_tsit5_solve": (C.c_int, [C.c_void_p, c_double_p, C.POINTER(OdeOptions), c_double_p, C.POINTER(OdeStats),
+                                  C.c_void_p]),
+    "fvm_template_create": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p)]),
+    "fvm_template_destroy": (C.c_int, [C.c_void_p]),
+    "fvm_template_export": (C.c_int, [C.c_void_p, c_int64_p, c_int32_p, c_int32_p, c_double_p, c_double_p]),
+    "fvm_template_apply": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_void_p]),
+    "fvm_template_tsit5_solve": (C.c_int, [C.c_void_p, c_double_p, C.POINTER(OdeOptions), c_double_p,
+                                           C.POINTER(OdeStats), C.c_void_p]),
+    "fvm_template_steady_solve": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(SolverOptions),
+                                            C.POINTER(SolverStats), C.c_int32, C.c_void_p]),
+}
+
+_LIB = None
+
+
+def load(build_if_missing: bool = False):
+    """Load libfvmgpu.so; raises if it was not built."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = _build.lib_path()
+    if not path.exists():
+        if build_if_missing:
+            _build.build()
+        else:
+            raise RuntimeError(f"libfvmgpu.so is not built ({path}); run fvmgpu._build.build() "
+                               "(there is no CPU fallback)")
+    lib = C.CDLL(str(path))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _LIB = lib
+    return lib
+
+
+def last_error() -> str:
+    buf = C.create_string_buffer(4096)
+    load().fvm_last_error(buf, len(buf))
+    return buf.value.decode(errors="replace")
+
+
+def check(status: int):
+    if status == FVM_OK:
+        return
+    msg = last_error()
+    if status == FVM_ERR_UNSUPPORTED_FORM:
+        raise UnsupportedFormError(status, msg)
+    if status == FVM_ERR_UNSUPPORTED:
+        raise ValueError(msg)
+    if status == FVM_ERR_NOT_CONVERGED:
+        raise NotConvergedError(status, msg)
+    raise FVMError(status, msg)
+
+
+def device_count() -> int:
+    n = C.c_int(0)
+    check(load().fvm_device_count(C.byref(n)))
+    return n.value
+
+
+def require_gpu():
+    if device_count() < 1:
+        raise RuntimeError("libfvmgpu needs a CUDA device; none is visible (there is no CPU fallback)")
+
+
+def dptr(a: np.ndarray, ctype=c_double_p):
+    return a.ctypes.data_as(ctype) if a is not None else None
+
+
+def as_f64(a) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(a, dtype=np.float64))
+
+
+def as_i32(a) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(a, dtype=np.int32))
+
+
+def as_i8(a) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(a, dtype=np.int8))
+
+
+def array_pointer(x):
+    """(void pointer, location flag) of a numpy array (host) or a CUDA torch tensor (device)."""
+    if isinstance(x, np.ndarray):
+        if x.dtype != np.float64 or not x.flags.c_contiguous:
+            raise TypeError("host arrays must be contiguous float64")
+        return C.c_void_p(x.ctypes.data), FVM_PTR_HOST
+    try:
+        import torch
+    except ImportError:  # pragma: no cover
+        torch = None
+    if torch is not None and isinstance(x, torch.Tensor):
+        if x.dtype != torch.float64 or not x.is_contiguous():
+            raise TypeError("tensors must be contiguous float64")
+        if x.is_cuda:
+            return C.c_void_p(x.data_ptr()), FVM_PTR_DEVICE
+        return C.c_void_p(x.data_ptr()), FVM_PTR_HOST
+    raise TypeError(f"unsupported array type {type(x)}")
+
+
+def current_stream_handle():
+    """cudaStream_t of torch's current stream when torch is loaded with CUDA, else NULL."""
+    try:
+        import torch
+        if torch.cuda.is_available():
+            return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    except Exception:  # pragma: no cover
+        pass
+    return C.c_void_p(0)

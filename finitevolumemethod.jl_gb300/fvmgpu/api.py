@@ -1,0 +1,803 @@
+"""Host mirror of FiniteVolumeMethod.jl's public API for the vertex-centred hot path.
+
+Names, argument meanings and error behaviour follow the reference (FiniteVolumeMethod.jl
+1.2.3); indices are 0-based (Python), function indices included.  Every compute call goes
+through libfvmgpu.so (include/fvm_gpu.h); there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import enum
+from dataclasses import dataclass, field
+from typing import Any, Callable, Dict, Optional, Sequence, Tuple
+
+import numpy as np
+
+from . import _lib
+from ._lib import (FVM_FP32, FVM_FP64, FVM_VERTEX_DIRICHLET, FVM_VERTEX_DUDT, FVM_VERTEX_FREE,
+                   FVM_VERTEX_NOT_A_VERTEX, as_f64, as_i8, as_i32, check, dptr, load)
+from .forms import classify_flux, classify_xytu, sample_xy
+from .meshes import Triangulation
+
+
+# --------------------------------------------------------------------------------------
+# conditions (src/conditions.jl)
+# --------------------------------------------------------------------------------------
+class ConditionType(enum.Enum):
+    """src/conditions.jl:36-41."""
+
+    Neumann = 0
+    Dudt = 1
+    Dirichlet = 2
+    Constrained = 3
+
+
+Neumann = ConditionType.Neumann
+Dudt = ConditionType.Dudt
+Dirichlet = ConditionType.Dirichlet
+Constrained = ConditionType.Constrained
+
+
+class ParametrisedFunction:
+    """f(args...) = fnc(args..., parameters) (src/conditions.jl:16-20)."""
+
+    __slots__ = ("fnc", "parameters")
+
+    def __init__(self, fnc, parameters=None):
+        self.fnc = fnc
+        self.parameters = parameters
+
+    def __call__(self, *args):
+        return self.fnc(*args, self.parameters)
+
+
+def _as_tuple(x):
+    return tuple(x) if isinstance(x, (tuple, list)) else (x,)
+
+
+def _functions_and_parameters(functions, parameters):
+    """A single function takes `parameters` as its own p (conditions.jl:246-251,262-269);
+    a tuple of functions takes a tuple of parameters, one each (default nothing)."""
+    if not isinstance(functions, (tuple, list)):
+        return (functions,), (parameters,)
+    fs = tuple(functions)
+    ps = tuple(parameters) if parameters is not None else (None,) * len(fs)
+    return fs, ps
+
+
+class BoundaryConditions:
+    """BoundaryConditions(mesh, functions, types; parameters) (src/conditions.jl:164-172,237-251).
+
+    functions[s] and types[s] belong to boundary segment s (ghost vertex -(s+1))."""
+
+    def __init__(self, mesh, functions, types, parameters=None):
+        fs, ps = _functions_and_parameters(functions, parameters)
+        ts = _as_tuple(types)
+        if len(fs) != len(ts):
+            raise AssertionError("The number of functions and types must be the same.")
+        if not all(isinstance(t, ConditionType) for t in ts):
+            raise AssertionError("The condition types must be ConditionType instances.")
+        if len(fs) != mesh.triangulation.num_ghost_vertices:
+            raise AssertionError("The number of boundary conditions must be the same as the number of parts of the "
+                                 "mesh's boundary.")
+        if len(ps) != len(fs):
+            raise AssertionError("The number of parameters must match the number of functions.")
+        self.functions = tuple(ParametrisedFunction(f, p) for f, p in zip(fs, ps))
+        self.condition_types = ts
+
+    def __repr__(self):
+        n = len(self.functions)
+        return f"BoundaryConditions with {n} boundary condition{'s' if n > 1 else ''} with types {self.condition_types}"
+
+
+class InternalConditions:
+    """InternalConditions(functions; dirichlet_nodes, dudt_nodes, parameters)
+    (src/conditions.jl:223-230,253-269).  Node -> function index (0-based)."""
+
+    def __init__(self, functions=(), dirichlet_nodes: Optional[Dict[int, int]] = None,
+                 dudt_nodes: Optional[Dict[int, int]] = None, parameters=None):
+        fs, ps = _functions_and_parameters(functions, parameters)
+        if len(ps) != len(fs):
+            raise AssertionError("The number of parameters must match the number of functions.")
+        self.functions = tuple(ParametrisedFunction(f, p) for f, p in zip(fs, ps))
+        self.dirichlet_nodes = dict(dirichlet_nodes or {})
+        self.dudt_nodes = dict(dudt_nodes or {})
+
+    def __repr__(self):
+        return f"InternalConditions with {len(self.dirichlet_nodes)} Dirichlet nodes and {len(self.dudt_nodes)} Dudt nodes"
+
+
+class Conditions:
+    """Merged conditions (src/conditions.jl:310-324; prepare_conditions :486-504;
+    merge_conditions! :506-544).  Internal functions come first, then one function per
+    boundary segment.  Segments are merged in increasing segment order, so on a node
+    shared by two Dirichlet (or two Dudt) segments the later segment's function wins."""
+
+    def __init__(self, mesh, bc: BoundaryConditions, ic: Optional[InternalConditions] = None):
+        ic = ic or InternalConditions()
+        tri = mesh.triangulation
+        nif = len(ic.functions)
+        self.functions = ic.functions + bc.functions
+        self.neumann_edges: Dict[Tuple[int, int], int] = {}
+        self.constrained_edges: Dict[Tuple[int, int], int] = {}
+        self.dirichlet_nodes: Dict[int, int] = dict(ic.dirichlet_nodes)
+        self.dudt_nodes: Dict[int, int] = dict(ic.dudt_nodes)
+        for s, nodes in enumerate(tri.boundary_nodes):
+            ctype = bc.condition_types[s]
+            f = s + nif
+            for a in range(len(nodes) - 1):
+                u, v = int(nodes[a]), int(nodes[a + 1])
+                if ctype is Neumann:
+                    self.neumann_edges[(u, v)] = f
+                elif ctype is Constrained:
+                    self.constrained_edges[(u, v)] = f
+                elif ctype is Dirichlet:
+                    self.dirichlet_nodes[u] = f
+                    self.dirichlet_nodes[v] = f
+                else:
+                    self.dudt_nodes[u] = f
+                    self.dudt_nodes[v] = f
+
+    # predicates of src/conditions.jl:342-484
+    def is_dirichlet_node(self, i):
+        return i in self.dirichlet_nodes
+
+    def is_dudt_node(self, i):
+        return i in self.dudt_nodes
+
+    def is_neumann_edge(self, i, j):
+        return (i, j) in self.neumann_edges
+
+    def is_constrained_edge(self, i, j):
+        return (i, j) in self.constrained_edges
+
+    def has_condition(self, i):
+        return i in self.dudt_nodes or i in self.dirichlet_nodes
+
+    def has_dirichlet_nodes(self):
+        return bool(self.dirichlet_nodes)
+
+    def has_dudt_nodes(self):
+        return bool(self.dudt_nodes)
+
+    def has_neumann_edges(self):
+        return bool(self.neumann_edges)
+
+    def has_constrained_edges(self):
+        return bool(self.constrained_edges)
+
+    def eval_condition_fnc(self, fidx, x, y, t, u):
+        return self.functions[fidx](x, y, t, u)
+
+    def vertex_tables(self, has_vertex: np.ndarray):
+        """Per-point FVM_VERTEX_* code and function index (Dirichlet before Dudt:
+        source_contributions.jl:5-11)."""
+        n = has_vertex.shape[0]
+        code = np.zeros(n, dtype=np.int8)
+        fidx = np.full(n, -1, dtype=np.int32)
+        for i, f in self.dudt_nodes.items():
+            code[i], fidx[i] = FVM_VERTEX_DUDT, f
+        for i, f in self.dirichlet_nodes.items():
+            code[i], fidx[i] = FVM_VERTEX_DIRICHLET, f
+        code[~has_vertex] = FVM_VERTEX_NOT_A_VERTEX
+        fidx[~has_vertex] = -1
+        return code, fidx
+
+    def neumann_table(self, boundary_edges: np.ndarray):
+        out = np.full(boundary_edges.shape[0], -1, dtype=np.int32)
+        for m, (u, v) in enumerate(boundary_edges):
+            out[m] = self.neumann_edges.get((int(u), int(v)), -1)
+        return out
+
+    def __repr__(self):
+        return (f"Conditions with\n   {len(self.neumann_edges)} Neumann edges\n   {len(self.constrained_edges)} "
+                f"Constrained edges\n   {len(self.dirichlet_nodes)} Dirichlet nodes\n   {len(self.dudt_nodes)} Dudt nodes")
+
+
+# --------------------------------------------------------------------------------------
+# geometry (src/geometry.jl)
+# --------------------------------------------------------------------------------------
+@dataclass(frozen=True)
+class TriangleProperties:
+    """src/geometry.jl:21-26."""
+
+    shape_function_coefficients: Tuple[float, ...]
+    cv_edge_midpoints: Tuple[Tuple[float, float], ...]
+    cv_edge_normals: Tuple[Tuple[float, float], ...]
+    cv_edge_lengths: Tuple[float, float, float]
+
+
+class FVMGeometry:
+    """FVMGeometry(tri) (src/geometry.jl:44-49,99-169): the mesh flattened once into
+    Hilbert-ordered device arrays by libfvmgpu.  `cv_volumes` and `triangle_props` keep the
+    reference's meaning (caller numbering)."""
+
+    def __init__(self, tri: Triangulation, tile_vertices: int = 0, renumber: bool = True):
+        lib = load()
+        _lib.require_gpu()
+        self.triangulation = tri
+        pts = as_f64(tri.points)
+        tris = as_i32(tri.triangles)
+        be = as_i32(tri.boundary_edges)
+        badj = as_i32(tri.boundary_adjacent)
+        h = C.c_void_p()
+        check(lib.fvm_mesh_create(dptr(pts), tri.num_points, dptr(tris, _lib.c_int32_p), tri.num_triangles,
+                                  dptr(be, _lib.c_int32_p), dptr(badj, _lib.c_int32_p), tri.num_boundary_edges,
+                                  int(tile_vertices), 0 if renumber else _lib.FVM_MESH_NO_RENUMBER, C.byref(h)))
+        self._h = h
+        self.cv_volumes = np.empty(tri.num_points)
+        self._props = np.empty((tri.num_triangles, 24))
+        check(lib.fvm_mesh_geometry(h, dptr(self.cv_volumes), dptr(self._props)))
+        self._triangle_props = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def props_array(self) -> np.ndarray:
+        """(ntri, 24): s1..s9, dual-edge midpoints, unit normals, lengths."""
+        return self._props
+
+    @property
+    def triangle_props(self) -> Dict[Tuple[int, int, int], TriangleProperties]:
+        if self._triangle_props is None:
+            d = {}
+            for t, (i, j, k) in enumerate(self.triangulation.triangles):
+                p = self._props[t]
+                d[(int(i), int(j), int(k))] = TriangleProperties(
+                    tuple(p[0:9]), tuple(map(tuple, p[9:15].reshape(3, 2))), tuple(map(tuple, p[15:21].reshape(3, 2))),
+                    tuple(p[21:24]))
+            self._triangle_props = d
+        return self._triangle_props
+
+    def sample_points(self):
+        """(dual-edge midpoints (ntri, 3, 2), boundary quarter points (nbe, 2, 2))."""
+        tri = self.triangulation
+        dual = np.empty((tri.num_triangles, 3, 2))
+        quarter = np.empty((tri.num_boundary_edges, 2, 2))
+        check(load().fvm_mesh_sample_points(self._h, dptr(dual), dptr(quarter)))
+        return dual, quarter
+
+    def info(self) -> Dict[str, int]:
+        a = np.zeros(10, dtype=np.int64)
+        check(load().fvm_mesh_info(self._h, dptr(a, _lib.c_int64_p)))
+        keys = ["npoints", "ntri", "nbedge", "nvertices", "ntiles", "ntile_elements", "nbedge_elements",
+                "tile_vertices", "operator_slots", "operator_nnz"]
+        return dict(zip(keys, (int(v) for v in a)))
+
+    def permutation(self) -> np.ndarray:
+        p = np.empty(self.triangulation.num_points, dtype=np.int32)
+        check(load().fvm_mesh_permutation(self._h, dptr(p, _lib.c_int32_p)))
+        return p
+
+    def export_connectivity(self):
+        tri = self.triangulation
+        t = np.empty((tri.num_triangles, 3), dtype=np.int32)
+        b = np.empty((tri.num_boundary_edges, 3), dtype=np.int32)
+        check(load().fvm_mesh_export_connectivity(self._h, dptr(t, _lib.c_int32_p), dptr(b, _lib.c_int32_p)))
+        return t, b
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib._LIB is not None:
+            _lib._LIB.fvm_mesh_destroy(h)
+            self._h = None
+
+    def __repr__(self):
+        tri = self.triangulation
+        return f"FVMGeometry with {int(tri.has_vertex().sum())} control volumes, {tri.num_triangles} triangles"
+
+
+# --------------------------------------------------------------------------------------
+# problem descriptors
+# --------------------------------------------------------------------------------------
+class _Desc:
+    """Owns the numpy arrays behind a ProblemDesc."""
+
+    def __init__(self):
+        self.keep = []
+        self.c = _lib.ProblemDesc()
+
+    def arr(self, name, a, ctype=_lib.c_double_p):
+        if a is None:
+            setattr(self.c, name, None)
+            return
+        self.keep.append(a)
+        setattr(self.c, name, a.ctypes.data_as(ctype))
+
+
+def _group_eval(points_by_entity, fidx_by_entity, functions, t0, what, max_degree):
+    """Classify condition functions per function index over the entities that use them.
+    points_by_entity: (n, k, 2); returns coefficients (n, k, deg+1) and deg."""
+    n, k = points_by_entity.shape[:2]
+    results = {}
+    deg = 0
+    for f in np.unique(fidx_by_entity[fidx_by_entity >= 0]):
+        sel = fidx_by_entity == f
+        P = points_by_entity[sel].reshape(-1, 2)
+        c, d = classify_xytu(functions[int(f)], P[:, 0], P[:, 1], t0, f"{what} function {int(f)}", max_degree)
+        results[int(f)] = (sel, c)
+        deg = max(deg, d)
+    out = np.zeros((n, k, deg + 1))
+    for f, (sel, c) in results.items():
+        cc = np.zeros((c.shape[0], deg + 1))
+        cc[:, : c.shape[1]] = c
+        out[sel] = cc.reshape(-1, k, deg + 1)
+    return out, deg
+
+
+def _precision(p):
+    if p in (FVM_FP64, "fp64", "float64", np.float64, None):
+        return FVM_FP64
+    if p in (FVM_FP32, "fp32", "float32", np.float32):
+        return FVM_FP32
+    raise ValueError(f"unknown precision {p!r}")
+
+
+class FVMProblem:
+    """FVMProblem(mesh, boundary_conditions[, internal_conditions]; ...)
+    (src/problem.jl:96-163).  The closures are classified into device-coded forms when the
+    problem is created; forms outside the device-coded set raise UnsupportedFormError.
+
+    precision: "fp64" (default) or "fp32" (FP32 flux assembly with FP64 control-volume
+    division; linear forms only)."""
+
+    def __init__(self, mesh: FVMGeometry, boundary_conditions: BoundaryConditions,
+                 internal_conditions: Optional[InternalConditions] = None, *, diffusion_function=None,
+                 diffusion_parameters=None, source_function=None, source_parameters=None, flux_function=None,
+                 flux_parameters=None, initial_condition, initial_time=0.0, final_time, precision="fp64"):
+        tri = mesh.triangulation
+        ic = np.asarray(initial_condition, dtype=np.float64)
+        if ic.shape[0] != tri.num_points:
+            raise AssertionError("The initial condition must have the same number of elements as the number of "
+                                 "nodes in the mesh (including nodes that aren't vertices in the mesh itself).")
+        if flux_function is None and diffusion_function is None:
+            raise ValueError("provide a diffusion_function or a flux_function")
+        self.mesh = mesh
+        self.conditions = Conditions(mesh, boundary_conditions, internal_conditions)
+        self.diffusion_function = diffusion_function
+        self.diffusion_parameters = diffusion_parameters
+        self.flux_function = flux_function
+        self.flux_parameters = flux_parameters
+        self.source_function = source_function
+        self.source_parameters = source_parameters
+        self.initial_condition = ic
+        self.initial_time = float(initial_time)
+        self.final_time = float(final_time)
+        self.precision = _precision(precision)
+        self._h = None
+        self._build()
+
+    # construct_flux_function (src/problem.jl:425-440) happens through the device form:
+    # q = -D(x, y, u(x_sigma)) grad u, D a polynomial of degree <= 2 in u.
+    def _build(self):
+        mesh, tri, conds = self.mesh, self.mesh.triangulation, self.conditions
+        t0 = self.initial_time
+        hv = tri.has_vertex()
+        code, fidx = conds.vertex_tables(hv)
+        neu = conds.neumann_table(tri.boundary_edges)
+        dual, quarter = mesh.sample_points()
+        d = _Desc()
+        self._code, self._fidx, self._neu = code, fidx, neu
+        d.arr("vertex_code", as_i8(code), _lib.c_int8_p)
+        d.arr("bedge_neumann", as_i8(neu >= 0), _lib.c_int8_p)
+        if self.flux_function is not None:
+            q = ParametrisedFunction(self.flux_function, self.flux_parameters)
+            Dd = classify_flux(q, dual[..., 0].ravel(), dual[..., 1].ravel(), t0)
+            Dq = classify_flux(q, quarter[..., 0].ravel(), quarter[..., 1].ravel(), t0) if tri.num_boundary_edges else np.zeros(0)
+            ddeg, dual_c, quarter_c = 0, Dd.reshape(-1, 1), Dq.reshape(-1, 1)
+        else:
+            Df = ParametrisedFunction(self.diffusion_function, self.diffusion_parameters)
+            allp = np.concatenate([dual.reshape(-1, 2), quarter.reshape(-1, 2)])
+            c, ddeg = classify_xytu(Df, allp[:, 0], allp[:, 1], t0, "diffusion_function")
+            nd = dual.reshape(-1, 2).shape[0]
+            dual_c, quarter_c = c[:nd], c[nd:]
+        d.c.diffusion_degree = ddeg
+        d.arr("dual_edge_D", as_f64(dual_c))
+        d.arr("quarter_D", as_f64(quarter_c) if quarter_c.size else None)
+        # Neumann q.n = a(x, y, t, u) at the quarter points of each Neumann edge
+        if np.any(neu >= 0):
+            nc, ndeg = _group_eval(quarter, neu, conds.functions, t0, "Neumann", 2)
+            d.c.neumann_degree = ndeg
+            d.arr("quarter_neumann", as_f64(nc.reshape(-1, ndeg + 1)))
+        else:
+            d.c.neumann_degree = 0
+            d.arr("quarter_neumann", None)
+        P = tri.points
+        # source on free vertices
+        free = code == FVM_VERTEX_FREE
+        if self.source_function is not None and np.any(free):
+            S = ParametrisedFunction(self.source_function, self.source_parameters)
+            c, sdeg = classify_xytu(S, P[free, 0], P[free, 1], t0, "source_function")
+            src = np.zeros((tri.num_points, sdeg + 1))
+            src[free] = c
+            d.c.source_degree = sdeg
+            d.arr("source", as_f64(src))
+        else:
+            d.c.source_degree = 0
+            d.arr("source", None)
+        # Dudt and Dirichlet values per function group
+        pts3 = P.reshape(-1, 1, 2)
+        dfidx = np.where(code == FVM_VERTEX_DUDT, fidx, -1)
+        if np.any(dfidx >= 0):
+            dc, udeg = _group_eval(pts3, dfidx, conds.functions, t0, "Dudt", 2)
+            d.c.dudt_degree = udeg
+            d.arr("dudt", as_f64(dc.reshape(-1, udeg + 1)))
+        else:
+            d.c.dudt_degree = 0
+            d.arr("dudt", None)
+        rfidx = np.where(code == FVM_VERTEX_DIRICHLET, fidx, -1)
+        if np.any(rfidx >= 0):
+            rc, _ = _group_eval(pts3, rfidx, conds.functions, t0, "Dirichlet", 0)
+            d.arr("dirichlet", as_f64(rc.reshape(-1)))
+        else:
+            d.arr("dirichlet", None)
+        d.c.precision = self.precision
+        h = C.c_void_p()
+        check(load().fvm_problem_create(mesh.handle, C.byref(d.c), C.byref(h)))
+        self._h = h
+        self._desc = d
+        self.diffusion_degree = ddeg
+
+    @property
+    def handle(self):
+        return self._h
+
+    def export_codes(self):
+        tri = self.mesh.triangulation
+        code = np.empty(tri.num_points, dtype=np.int8)
+        neu = np.empty(tri.num_boundary_edges, dtype=np.int8)
+        check(load().fvm_problem_export_codes(self._h, dptr(code, _lib.c_int8_p), dptr(neu, _lib.c_int8_p)))
+        return code, neu
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib._LIB is not None:
+            _lib._LIB.fvm_problem_destroy(h)
+            self._h = None
+
+    def __repr__(self):
+        return (f"FVMProblem with {int(self.mesh.triangulation.has_vertex().sum())} nodes and time span "
+                f"({self.initial_time}, {self.final_time})")
+
+
+def _prob_of(p):
+    if isinstance(p, (FVMProblem, _Template)):
+        return p
+    if isinstance(p, dict):
+        return p["prob"]
+    return getattr(p, "prob")
+
+
+def fvm_eqs(du, u, p, t, *, force_triangle=False, stream=None):
+    """fvm_eqs!(du, u, p, t) (src/equations/main_equations.jl:28-81).  `p` is the problem or
+    any object / dict with a `prob` entry.  du, u: float64 numpy arrays (host) or CUDA torch
+    tensors (device), caller numbering.  Returns du."""
+    prob = _prob_of(p)
+    if isinstance(prob, _Template):
+        return prob.apply(du, u, stream=stream)
+    up, ul = _lib.array_pointer(u)
+    dp, dl = _lib.array_pointer(du)
+    if ul != dl:
+        raise TypeError("u and du must both be host arrays or both device tensors")
+    flags = ul | (_lib.FVM_RHS_FORCE_TRIANGLE if force_triangle else 0)
+    s = stream if stream is not None else _lib.current_stream_handle()
+    check(load().fvm_rhs(prob.handle, up, dp, float(t), flags, s))
+    return du
+
+
+def update_dirichlet_nodes(u, prob, t=0.0, stream=None):
+    """update_dirichlet_nodes! (src/equations/dirichlet.jl:78-86), in place."""
+    up, ul = _lib.array_pointer(u)
+    s = stream if stream is not None else _lib.current_stream_handle()
+    check(load().fvm_dirichlet_apply(_prob_of(prob).handle, up, float(t), ul, s))
+    return u
+
+
+# --------------------------------------------------------------------------------------
+# templates (src/specific_problems/)
+# --------------------------------------------------------------------------------------
+class _Template:
+    kind = -1
+    steady = False
+
+    def _create(self, mesh, BCs, ICs, D, Dp, source=None, source_parameters=None, source_as_reaction=False):
+        tri = mesh.triangulation
+        self.mesh = mesh
+        self.conditions = conds = Conditions(mesh, BCs, ICs)
+        hv = tri.has_vertex()
+        code, fidx = conds.vertex_tables(hv)
+        neu = conds.neumann_table(tri.boundary_edges)
+        dual, quarter = mesh.sample_points()
+        d = _Desc()
+        d.arr("vertex_code", as_i8(code), _lib.c_int8_p)
+        d.arr("bedge_neumann", as_i8(neu >= 0), _lib.c_int8_p)
+        d.c.diffusion_degree = 0
+        d.arr("dual_edge_D", as_f64(sample_xy(D, dual[..., 0].ravel(), dual[..., 1].ravel(), Dp, what="diffusion_function")))
+        if tri.num_boundary_edges:
+            d.arr("quarter_D", as_f64(sample_xy(D, quarter[..., 0].ravel(), quarter[..., 1].ravel(), Dp,
+                                                what="diffusion_function")))
+        # condition functions are called with t = u = nothing (abstract_templates.jl:112,131,185)
+        fns = conds.functions
+        if np.any(neu >= 0):
+            qn = np.zeros((tri.num_boundary_edges, 2))
+            for f in np.unique(neu[neu >= 0]):
+                sel = neu == f
+                Q = quarter[sel]
+                qn[sel] = sample_xy(fns[int(f)], Q[..., 0].ravel(), Q[..., 1].ravel(), None, None,
+                                    what=f"Neumann function {int(f)}").reshape(-1, 2)
+            d.c.neumann_degree = 0
+            d.arr("quarter_neumann", as_f64(qn.reshape(-1, 1)))
+        P = tri.points
+        vals = np.zeros(tri.num_points)
+        for kind_code in (FVM_VERTEX_DUDT, FVM_VERTEX_DIRICHLET):
+            for f in np.unique(fidx[code == kind_code]):
+                sel = (code == kind_code) & (fidx == f)
+                vals[sel] = sample_xy(fns[int(f)], P[sel, 0], P[sel, 1], None, None, what=f"condition function {int(f)}")
+        d.c.dudt_degree = 0
+        d.arr("dudt", as_f64(np.where(code == FVM_VERTEX_DUDT, vals, 0.0)))
+        self._dirichlet_values = np.where(code == FVM_VERTEX_DIRICHLET, vals, 0.0)
+        d.arr("dirichlet", as_f64(self._dirichlet_values))
+        if source is not None:
+            sv = sample_xy(source, P[:, 0], P[:, 1], source_parameters, what="source_function")
+            if source_as_reaction:
+                d.c.source_degree = 1
+                d.arr("source", as_f64(np.stack([np.zeros_like(sv), sv], axis=1)))
+            else:
+                d.c.source_degree = 0
+                d.arr("source", as_f64(sv))
+        d.c.precision = FVM_FP64
+        self._code = code
+        hp = C.c_void_p()
+        check(load().fvm_problem_create(mesh.handle, C.byref(d.c), C.byref(hp)))
+        self._hp = hp
+        self._desc = d
+        ht = C.c_void_p()
+        check(load().fvm_template_create(hp, self.kind, C.byref(ht)))
+        self._ht = ht
+        self._A = None
+        self._b = None
+
+    @property
+    def handle(self):
+        return self._ht
+
+    def _export(self):
+        lib = load()
+        nnz = C.c_int64()
+        check(lib.fvm_template_export(self._ht, C.byref(nnz), None, None, None, None))
+        n = self.mesh.triangulation.num_points
+        rowptr = np.empty(n + 1, dtype=np.int32)
+        col = np.empty(nnz.value, dtype=np.int32)
+        val = np.empty(nnz.value)
+        b = np.empty(n)
+        check(lib.fvm_template_export(self._ht, C.byref(nnz), dptr(rowptr, _lib.c_int32_p), dptr(col, _lib.c_int32_p),
+                                      dptr(val), dptr(b)))
+        from scipy.sparse import csr_matrix
+
+        self._A = csr_matrix((val, col, rowptr), shape=(n, n))
+        self._b = b
+
+    @property
+    def A(self):
+        if self._A is None:
+            self._export()
+        return self._A
+
+    @property
+    def b(self):
+        if self._b is None:
+            self._export()
+        return self._b
+
+    def apply(self, du, u, precision="fp64", stream=None):
+        """du = A u + b: the MatrixOperator product."""
+        up, ul = _lib.array_pointer(u)
+        dp, dl = _lib.array_pointer(du)
+        if ul != dl:
+            raise TypeError("u and du must both be host arrays or both device tensors")
+        s = stream if stream is not None else _lib.current_stream_handle()
+        check(load().fvm_template_apply(self._ht, up, dp, _precision(precision), ul, s))
+        return du
+
+    def __del__(self):
+        if _lib._LIB is None:
+            return
+        if getattr(self, "_ht", None):
+            _lib._LIB.fvm_template_destroy(self._ht)
+            self._ht = None
+        if getattr(self, "_hp", None):
+            _lib._LIB.fvm_problem_destroy(self._hp)
+            self._hp = None
+
+
+class _TimeTemplate(_Template):
+    def _init_time(self, initial_condition, initial_time, final_time):
+        ic = np.array(initial_condition, dtype=np.float64)
+        if ic.shape[0] != self.mesh.triangulation.num_points:
+            raise AssertionError("initial condition length must equal the number of points")
+        self.initial_condition = ic
+        # apply_dirichlet_conditions! (abstract_templates.jl:109-117)
+        u0 = ic.copy()
+        dmask = self._code == FVM_VERTEX_DIRICHLET
+        u0[dmask] = self._dirichlet_values[dmask]
+        self.u0 = u0
+        self.initial_time = float(initial_time)
+        self.final_time = float(final_time)
+
+
+class DiffusionEquation(_TimeTemplate):
+    """DiffusionEquation (src/specific_problems/diffusion_equation.jl:49-101):
+    du/dt = A u + b.  Solutions carry the reference's extra last component (= 1)."""
+
+    kind = _lib.FVM_TEMPLATE_DIFFUSION
+
+    def __init__(self, mesh, BCs, ICs=None, *, diffusion_function, diffusion_parameters=None, initial_condition,
+                 initial_time=0.0, final_time, **kwargs):
+        self.diffusion_function, self.diffusion_parameters = diffusion_function, diffusion_parameters
+        self._create(mesh, BCs, ICs, diffusion_function, diffusion_parameters)
+        self._init_time(initial_condition, initial_time, final_time)
+
+    def __repr__(self):
+        return f"DiffusionEquation with {self.mesh.triangulation.num_points} nodes and time span ({self.initial_time}, {self.final_time})"
+
+
+class LinearReactionDiffusionEquation(_TimeTemplate):
+    """LinearReactionDiffusionEquation (linear_reaction_diffusion_equations.jl:53-125):
+    du/dt = div(D grad u) + f(x) u."""
+
+    kind = _lib.FVM_TEMPLATE_LINEAR_REACTION_DIFFUSION
+
+    def __init__(self, mesh, BCs, ICs=None, *, diffusion_function, diffusion_parameters=None, source_function,
+                 source_parameters=None, initial_condition, initial_time=0.0, final_time, **kwargs):
+        self.diffusion_function, self.diffusion_parameters = diffusion_function, diffusion_parameters
+        self.source_function, self.source_parameters = source_function, source_parameters
+        self._create(mesh, BCs, ICs, diffusion_function, diffusion_parameters, source_function, source_parameters,
+                     source_as_reaction=True)
+        self._init_time(initial_condition, initial_time, final_time)
+
+
+class PoissonsEquation(_Template):
+    """PoissonsEquation (poissons_equation.jl:42-88): div(D grad u) = f, A u = b."""
+
+    kind = _lib.FVM_TEMPLATE_POISSON
+    steady = True
+
+    def __init__(self, mesh, BCs, ICs=None, *, diffusion_function=lambda x, y, p: 1.0 + 0.0 * x,
+                 diffusion_parameters=None, source_function, source_parameters=None, **kwargs):
+        self.diffusion_function, self.diffusion_parameters = diffusion_function, diffusion_parameters
+        self.source_function, self.source_parameters = source_function, source_parameters
+        self._create(mesh, BCs, ICs, diffusion_function, diffusion_parameters, source_function, source_parameters)
+
+
+class MeanExitTimeProblem(_Template):
+    """MeanExitTimeProblem (mean_exit_time.jl:43-94): div(D grad T) = -1."""
+
+    kind = _lib.FVM_TEMPLATE_MEAN_EXIT_TIME
+    steady = True
+
+    def __init__(self, mesh, BCs, ICs=None, *, diffusion_function, diffusion_parameters=None, **kwargs):
+        conds = Conditions(mesh, BCs, ICs)
+        if conds.has_dudt_nodes():
+            raise ValueError("MeanExitTimeProblem does not support Dudt nodes.")
+        if conds.has_constrained_edges():
+            raise ValueError("MeanExitTimeProblem does not support Constrained edges.")
+        self.diffusion_function, self.diffusion_parameters = diffusion_function, diffusion_parameters
+        self._create(mesh, BCs, ICs, diffusion_function, diffusion_parameters)
+
+
+# --------------------------------------------------------------------------------------
+# solve
+# --------------------------------------------------------------------------------------
+class Tsit5:
+    """Tsitouras 5(4) explicit Runge-Kutta (the algorithm the reference's README uses)."""
+
+    def __repr__(self):
+        return "Tsit5()"
+
+
+@dataclass
+class KrylovSolver:
+    """GPU steady solver: method "auto" (CG if symmetric, else BiCGStab), "cg", "bicgstab";
+    mode "fp64" or "mixed" (FP32 inner iterations with FP64 reliable updates)."""
+
+    mode: str = "fp64"
+    method: str = "auto"
+    rtol: float = 1e-10
+    max_iters: int = 1_000_000
+    inner_reduction: float = 1e-2
+
+
+@dataclass
+class ODESolution:
+    t: np.ndarray
+    u: list
+    stats: Dict[str, Any] = field(default_factory=dict)
+    retcode: str = "Success"
+
+    def __getitem__(self, i):
+        return self.u[i]
+
+    def __len__(self):
+        return len(self.u)
+
+
+@dataclass
+class LinearSolution:
+    u: np.ndarray
+    stats: Dict[str, Any] = field(default_factory=dict)
+    retcode: str = "Success"
+
+
+def _saveat_times(saveat, t0, tf):
+    if saveat is None:
+        return np.array([t0, tf])
+    if np.isscalar(saveat):
+        step = float(saveat)
+        n = int(np.floor((tf - t0) / step + 1e-9))
+        ts = t0 + step * np.arange(n + 1)
+        if ts[-1] < tf - 1e-12 * max(1.0, abs(tf)):
+            ts = np.append(ts, tf)
+        return ts
+    return np.asarray(saveat, dtype=np.float64)
+
+
+def solve(prob, alg=None, *, saveat=None, dt=None, adaptive=None, abstol=1e-6, reltol=1e-3, max_steps=0,
+          use_graph=True, parallel=True, precision="fp64", stream=None, **kwargs):
+    """solve(prob, alg; saveat, ...) (src/solve.jl:197-220; abstract_templates.jl:58-60).
+
+    Time-dependent problems step with Tsit5 (adaptive unless `dt` is given with
+    adaptive=False); steady templates solve A u = b with the GPU Krylov solver."""
+    lib = load()
+    s = stream if stream is not None else _lib.current_stream_handle()
+    if isinstance(prob, _Template) and prob.steady:
+        opt = alg if isinstance(alg, KrylovSolver) else KrylovSolver()
+        so = _lib.SolverOptions()
+        so.rtol = opt.rtol
+        so.max_iters = opt.max_iters
+        so.method = {"auto": _lib.FVM_SOLVER_AUTO, "cg": _lib.FVM_SOLVER_CG,
+                     "bicgstab": _lib.FVM_SOLVER_BICGSTAB}[opt.method]
+        so.precond = _lib.FVM_PRECOND_JACOBI
+        so.mode = _lib.FVM_SOLVE_MIXED if opt.mode == "mixed" else _lib.FVM_SOLVE_FP64
+        so.inner_reduction = opt.inner_reduction
+        x = np.zeros(prob.mesh.triangulation.num_points)
+        st = _lib.SolverStats()
+        check(lib.fvm_template_steady_solve(prob.handle, C.c_void_p(x.ctypes.data), C.byref(so), C.byref(st),
+                                            _lib.FVM_PTR_HOST, s))
+        return LinearSolution(x, {"iterations": st.iterations, "refinements": st.refinements,
+                                  "rel_residual": st.rel_residual, "elapsed_ms": st.elapsed_ms,
+                                  "method": "cg" if st.method_used == _lib.FVM_SOLVER_CG else "bicgstab",
+                                  "symmetric": bool(st.symmetric)})
+    if isinstance(prob, _TimeTemplate):
+        t0, tf, u0 = prob.initial_time, prob.final_time, prob.u0
+    elif isinstance(prob, FVMProblem):
+        t0, tf, u0 = prob.initial_time, prob.final_time, prob.initial_condition
+    else:
+        raise TypeError(f"cannot solve {type(prob).__name__}")
+    ts = _saveat_times(saveat, t0, tf)
+    n = prob.mesh.triangulation.num_points
+    out = np.empty((ts.size, n))
+    o = _lib.OdeOptions()
+    o.t0, o.tf = t0, tf
+    if adaptive is None:
+        adaptive = dt is None
+    o.adaptive = 1 if adaptive else 0
+    o.dt = float(dt) if dt is not None else 0.0
+    o.abstol, o.reltol = abstol, reltol
+    o.max_steps = int(max_steps)
+    tsc = as_f64(ts)
+    o.saveat = dptr(tsc)
+    o.nsave = ts.size
+    o.use_graph = 1 if use_graph else 0
+    o.precision = _precision(precision)
+    st = _lib.OdeStats()
+    u0c = as_f64(u0)
+    if isinstance(prob, _TimeTemplate):
+        check(lib.fvm_template_tsit5_solve(prob.handle, dptr(u0c), C.byref(o), dptr(out), C.byref(st), s))
+        us = [np.append(row, 1.0) for row in out]  # the augmented component of the MatrixOperator form
+    else:
+        check(lib.fvm_tsit5_solve(prob.handle, dptr(u0c), C.byref(o), dptr(out), C.byref(st), s))
+        us = [row.copy() for row in out]
+    return ODESolution(ts, us, {"naccept": st.naccept, "nreject": st.nreject, "nrhs": st.nrhs,
+                                "t_final": st.t_final, "elapsed_ms": st.elapsed_ms})

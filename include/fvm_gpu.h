@@ -1,0 +1,225 @@
+/*
+ * fvm_gpu.h - C ABI of the GB300 vertex-centred finite-volume library (libfvmgpu.so).
+ *
+ * Every entry point returns an int status (FVM_OK = 0) and never aborts the
+ * process; fvm_last_error() gives the message of the last failure on the
+ * calling thread.  Handles are opaque and owned by the library; free them with
+ * the matching *_destroy.  Input host arrays are copied at creation.  All
+ * vertex, triangle and edge indices are 0-based and in the caller's
+ * ("reference") numbering; internally the library renumbers vertices along a
+ * Hilbert curve and maps back at the boundary.
+ *
+ * Reference interfaces replaced (FiniteVolumeMethod.jl 1.2.3, paths relative
+ * to the project root) are cited beside each declaration.  The reference is
+ * pure Julia and has no FFI of its own: the Julia layer in
+ * julia/FiniteVolumeMethodGPU ccalls exactly these symbols.
+ */
+#ifndef FVM_GPU_H
+#define FVM_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes --------------------------------------------------------------- */
+#define FVM_OK 0
+#define FVM_ERR_INVALID_ARGUMENT 1 /* null pointer, bad size, bad enum */
+#define FVM_ERR_BAD_MESH 2         /* index out of range, clockwise or degenerate triangle, open boundary edge */
+#define FVM_ERR_UNSUPPORTED_FORM 3 /* closure form outside the device-coded set */
+#define FVM_ERR_CUDA 4             /* CUDA runtime error (message has the CUDA string) */
+#define FVM_ERR_OUT_OF_MEMORY 5
+#define FVM_ERR_NOT_CONVERGED 6    /* iterative solver hit its iteration limit */
+#define FVM_ERR_UNSUPPORTED 7      /* condition type not allowed by a template (reference ArgumentError) */
+#define FVM_ERR_STEP_LIMIT 8       /* ODE solver hit max_steps or dt underflow */
+
+/* ---- vertex condition codes (per point) ------------------------------------------ */
+#define FVM_VERTEX_FREE 0          /* no condition: du = (sum of fluxes)/V + S */
+#define FVM_VERTEX_DIRICHLET 1     /* du = 0, u set by the Dirichlet update */
+#define FVM_VERTEX_DUDT 2          /* du = a(x, y, t, u) */
+#define FVM_VERTEX_NOT_A_VERTEX 3  /* point in no solid triangle: du = 0 */
+
+/* ---- pointer-location flags ------------------------------------------------------- */
+#define FVM_PTR_HOST 0             /* host arrays, reference numbering (copied in/out) */
+#define FVM_PTR_DEVICE 1           /* device arrays, reference numbering */
+#define FVM_PTR_DEVICE_INTERNAL 2  /* device arrays, internal (Hilbert) numbering */
+#define FVM_RHS_FORCE_TRIANGLE 16  /* evaluate by the per-triangle flux kernel even for linear forms */
+
+/* ---- precision ---------------------------------------------------------------------- */
+#define FVM_FP64 0
+#define FVM_FP32 1                 /* FP32 flux assembly / SpMV, FP64 control-volume division and output */
+
+typedef struct fvm_mesh fvm_mesh;
+typedef struct fvm_problem fvm_problem;
+typedef struct fvm_template fvm_template;
+
+int fvm_version(void);
+/* Copies the last error message of the calling thread into buf (NUL-terminated). */
+int fvm_last_error(char* buf, size_t len);
+/* Number of CUDA devices visible (0 when none); a query, never an error. */
+int fvm_device_count(int* count);
+
+/* ---- mesh --------------------------------------------------------------------------- */
+/* Replaces FVMGeometry(tri) (src/geometry.jl:99-169) and the triangulation queries of
+ * the hot loop: each_solid_triangle (src/equations/triangle_contributions.jl:39),
+ * get_boundary_edge_map / get_adjacent (src/equations/boundary_edge_contributions.jl:79,90).
+ *   points            [2*npoints]   (x, y) interleaved
+ *   triangles         [3*ntri]      counter-clockwise solid triangles
+ *   boundary_edges    [2*nbedge]    (i, j) with the domain on the left
+ *   boundary_adjacent [nbedge]      k = get_adjacent(tri, i, j), or NULL to look it up
+ *   tile_vertices     vertices per tile of the triangle kernel (0 = default)
+ *   flags             FVM_MESH_NO_RENUMBER keeps the caller's numbering internally */
+#define FVM_MESH_NO_RENUMBER 1
+int fvm_mesh_create(const double* points, int64_t npoints, const int32_t* triangles, int64_t ntri,
+                    const int32_t* boundary_edges, const int32_t* boundary_adjacent, int64_t nbedge,
+                    int32_t tile_vertices, int32_t flags, fvm_mesh** out);
+int fvm_mesh_destroy(fvm_mesh* mesh);
+/* info[0..9] = npoints, ntri, nbedge, nvertices, ntiles, ntile_elements, nbedge_elements,
+ * tile_vertices, operator_slots (sliced-ELL, padded), operator_nnz (structural). */
+int fvm_mesh_info(const fvm_mesh* mesh, int64_t* info);
+/* FVMGeometry fields: cv_volumes [npoints] (src/geometry.jl:41,130-135) and, per triangle in
+ * the caller's order, TriangleProperties (src/geometry.jl:21-26) as 24 doubles:
+ * s1..s9, dual-edge midpoints (3 x (x,y)), unit normals (3 x (x,y)), lengths (3).
+ * Either output may be NULL. */
+int fvm_mesh_geometry(const fvm_mesh* mesh, double* cv_volumes, double* triangle_props);
+/* Points where (x, y) closures are sampled: dual-edge midpoints [ntri*3*2] (edge order
+ * (i,j), (j,k), (k,i): src/geometry.jl:149-151) and boundary quarter points [nbedge*2*2]
+ * (m_i, m_j: src/equations/control_volumes.jl:47-49). Either output may be NULL. */
+int fvm_mesh_sample_points(const fvm_mesh* mesh, double* dual_midpoints, double* quarter_points);
+/* perm[internal] = caller index. */
+int fvm_mesh_permutation(const fvm_mesh* mesh, int32_t* perm);
+/* Reads the device-resident connectivity back and maps it to the caller's numbering:
+ * triangles [3*ntri] in the caller's triangle order (rotation as given), boundary
+ * elements [3*nbedge] = (i, j, k).  For the bit-exact connectivity check. */
+int fvm_mesh_export_connectivity(const fvm_mesh* mesh, int32_t* triangles, int32_t* boundary_elements);
+
+/* ---- problem -------------------------------------------------------------------------- */
+/* Device-coded closure forms.  Closures of (x, y) are sampled by the host at the points
+ * fvm_mesh_sample_points gives; closures of (u) are polynomials of degree <= 2 in u whose
+ * coefficients are (x, y)-sampled: f = c0 + c1 u + c2 u^2.  Arrays are laid out
+ * [entity][degree+1].  A NULL array means the form is identically zero. */
+typedef struct fvm_problem_desc {
+    /* conditions (src/conditions.jl:310-324 after merge_conditions!, :506-544) */
+    const int8_t* vertex_code;      /* [npoints] FVM_VERTEX_* */
+    const int8_t* bedge_neumann;    /* [nbedge] 1 if the edge has a Neumann condition, else 0 */
+    /* diffusion flux q = -D(x, y, u) grad u (src/problem.jl:425-440), D at dual-edge midpoints
+     * and boundary quarter points */
+    int32_t diffusion_degree;       /* 0, 1 or 2 */
+    const double* dual_edge_D;      /* [ntri*3][deg+1] */
+    const double* quarter_D;        /* [nbedge*2][deg+1] */
+    /* Neumann q.n = a(x, y, u(m)) at the quarter points (boundary_edge_contributions.jl:2-13) */
+    int32_t neumann_degree;
+    const double* quarter_neumann;  /* [nbedge*2][deg+1] */
+    /* source S(x, y, u) at vertices (source_contributions.jl:2-14) */
+    int32_t source_degree;
+    const double* source;           /* [npoints][deg+1] */
+    /* Dudt a(x, y, u) at vertices with code DUDT */
+    int32_t dudt_degree;
+    const double* dudt;             /* [npoints][deg+1] */
+    /* Dirichlet u = a(x, y) at vertices with code DIRICHLET (dirichlet.jl:2-8) */
+    const double* dirichlet;        /* [npoints] */
+    int32_t precision;              /* FVM_FP64 or FVM_FP32 */
+} fvm_problem_desc;
+
+/* Replaces FVMProblem(mesh, BCs, ICs; ...) (src/problem.jl:118-163) together with
+ * Conditions(mesh, BCs, ICs) (src/conditions.jl:546-552). */
+int fvm_problem_create(fvm_mesh* mesh, const fvm_problem_desc* desc, fvm_problem** out);
+int fvm_problem_destroy(fvm_problem* prob);
+/* Reads the device-resident classification back in the caller's numbering. */
+int fvm_problem_export_codes(const fvm_problem* prob, int8_t* vertex_code, int8_t* bedge_neumann);
+
+/* Replaces fvm_eqs!(du, u, p, t) (src/equations/main_equations.jl:28-81): triangle fluxes,
+ * boundary-edge fluxes and per-vertex source / condition finalisation.  stream is a
+ * cudaStream_t (NULL = default stream).  flags: FVM_PTR_* | FVM_RHS_FORCE_TRIANGLE. */
+int fvm_rhs(fvm_problem* prob, const double* u, double* du, double t, int32_t flags, void* stream);
+/* Replaces update_dirichlet_nodes! (src/equations/dirichlet.jl:78-86). */
+int fvm_dirichlet_apply(fvm_problem* prob, double* u, double t, int32_t flags, void* stream);
+
+/* ---- time stepping (solve(prob, Tsit5(); saveat), src/solve.jl:167-208) ---------------- */
+typedef struct fvm_ode_options {
+    double t0, tf;
+    double dt;            /* fixed step, or initial step when adaptive (0 = automatic) */
+    int32_t adaptive;     /* 0: fixed dt; 1: PI-controlled with the Tsit5 error estimate */
+    double abstol, reltol;
+    int64_t max_steps;
+    const double* saveat; /* [nsave] output times (host); NULL with nsave = 1 saves tf */
+    int64_t nsave;
+    int32_t use_graph;    /* capture the fixed step in a CUDA graph */
+    int32_t precision;    /* FVM_FP64 */
+} fvm_ode_options;
+
+typedef struct fvm_ode_stats {
+    int64_t naccept, nreject, nrhs;
+    double t_final;
+    double elapsed_ms;    /* device time of the stepping loop (CUDA events) */
+} fvm_ode_stats;
+
+/* Tsit5 on a generic problem, with the Dirichlet callback after every step
+ * (src/solve.jl:133-165).  u0 and out are host arrays in the caller's numbering;
+ * out is [nsave][npoints]. */
+int fvm_tsit5_solve(fvm_problem* prob, const double* u0, const fvm_ode_options* opt, double* out,
+                    fvm_ode_stats* stats, void* stream);
+
+/* ---- linear templates (src/specific_problems/) ------------------------------------------- */
+#define FVM_TEMPLATE_DIFFUSION 0                 /* diffusion_equation.jl:69-101 */
+#define FVM_TEMPLATE_LINEAR_REACTION_DIFFUSION 1 /* linear_reaction_diffusion_equations.jl:76-125 */
+#define FVM_TEMPLATE_POISSON 2                   /* poissons_equation.jl:58-88 */
+#define FVM_TEMPLATE_MEAN_EXIT_TIME 3            /* mean_exit_time.jl:57-94 */
+
+/* Assembles A and b of a template straight into the device operator (no dense matrix).
+ * The problem supplies D (degree 0), the source (Poisson f / reaction coefficient as
+ * source c0 / c1), Neumann values, Dudt and Dirichlet values, all sampled with
+ * t = u = nothing as the reference does. */
+int fvm_template_create(fvm_problem* prob, int32_t kind, fvm_template** out);
+int fvm_template_destroy(fvm_template* tmpl);
+/* A in CSR (caller numbering, sorted columns, structural zeros dropped) and b.
+ * Call with col = val = NULL to get nnz. */
+int fvm_template_export(const fvm_template* tmpl, int64_t* nnz, int32_t* rowptr, int32_t* col,
+                        double* val, double* b);
+/* du = A u + b: the MatrixOperator product (diffusion_equation.jl:93-94). precision:
+ * FVM_FP64 or FVM_FP32 (FP32 values, FP32 accumulation). */
+int fvm_template_apply(fvm_template* tmpl, const double* u, double* du, int32_t precision,
+                       int32_t flags, void* stream);
+/* Tsit5 on du/dt = A u + b (the template's ODEProblem). */
+int fvm_template_tsit5_solve(fvm_template* tmpl, const double* u0, const fvm_ode_options* opt,
+                             double* out, fvm_ode_stats* stats, void* stream);
+
+/* ---- steady solve (LinearProblem(A, b) + solve, poissons_equation.jl:81, mean_exit_time.jl:76) */
+#define FVM_SOLVER_AUTO 0      /* CG when the reduced operator is symmetric, else BiCGStab */
+#define FVM_SOLVER_CG 1
+#define FVM_SOLVER_BICGSTAB 2
+#define FVM_PRECOND_JACOBI 0
+#define FVM_PRECOND_CHEBYSHEV 1
+#define FVM_SOLVE_FP64 0       /* plain FP64 Krylov */
+#define FVM_SOLVE_MIXED 1      /* FP32 inner iterations, FP64 reliable residual / refinement */
+
+typedef struct fvm_solver_options {
+    double rtol;           /* on ||b - A x|| / ||b|| with the reference operator, FP64 */
+    int64_t max_iters;
+    int32_t method;        /* FVM_SOLVER_* */
+    int32_t precond;       /* FVM_PRECOND_* */
+    int32_t cheb_degree;
+    int32_t mode;          /* FVM_SOLVE_FP64 or FVM_SOLVE_MIXED */
+    double inner_reduction;/* residual reduction between FP64 reliable updates (mixed), e.g. 1e-2 */
+} fvm_solver_options;
+
+typedef struct fvm_solver_stats {
+    int64_t iterations;     /* Krylov iterations (all precisions) */
+    int64_t refinements;    /* FP64 residual recomputations */
+    double rel_residual;    /* final ||b - A x|| / ||b|| (FP64, reference operator) */
+    double elapsed_ms;      /* device time (CUDA events) */
+    int32_t method_used;
+    int32_t symmetric;
+} fvm_solver_stats;
+
+/* Solves A x = b of a Poisson or mean-exit-time template.  x: in = initial guess,
+ * out = solution, FVM_PTR_HOST or FVM_PTR_DEVICE (caller numbering). */
+int fvm_template_steady_solve(fvm_template* tmpl, double* x, const fvm_solver_options* opt,
+                              fvm_solver_stats* stats, int32_t flags, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FVM_GPU_H */

@@ -1,0 +1,756 @@
+"""CPU oracle for the vertex-centred finite-volume hot path (TEST INFRASTRUCTURE).
+
+This module is the checker, never the product: only `tests/`,
+`__graft_entry__.smoke()` and the CPU-baseline leg of `bench.py` may import it.
+It restates, in numpy, the reference's CPU algorithm (FiniteVolumeMethod.jl
+1.2.3); every function cites the file:line it follows.  Paths are relative to
+the reference project root.
+
+Parity status: pinned by the reference's own known-answer tests, restated in
+tests/test_oracle_pins.py (control-volume areas against polygon areas,
+shape-function identities, dual-edge geometry, single-triangle scatter signs,
+boundary quarter-point fluxes, source finalisation, the independent per-vertex
+control-volume integrator of test/test_functions.jl:601-657 and the exact
+corner-point test of test/equations.jl:37-92).  The Tsit5 stepper follows the
+published Tsitouras (2011) tableau; its agreement with OrdinaryDiffEq itself is
+unpinned (no reference test fixes Tsit5 numerics).
+
+Indices are 0-based.  Closures keep the reference signatures:
+flux `q(x, y, t, alpha, beta, gamma, p) -> (qx, qy)`, diffusion
+`D(x, y, t, u, p)`, source `S(x, y, t, u, p)`, condition `a(x, y, t, u, p)`
+(parameters are bound by the caller, so the oracle calls `f(x, y, t, u)`).
+Closures are called with numpy arrays when they accept them, else per point.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+FREE, DIRICHLET, DUDT, NOT_A_VERTEX = 0, 1, 2, 3
+NEUMANN_T, DUDT_T, DIRICHLET_T, CONSTRAINED_T = "Neumann", "Dudt", "Dirichlet", "Constrained"
+
+
+# --------------------------------------------------------------------------------------
+# closure evaluation helper
+# --------------------------------------------------------------------------------------
+def call_pointwise(f, *args):
+    """Evaluate closure f at broadcast array arguments; per-point fallback."""
+    arrs = [np.asarray(a, dtype=np.float64) if a is not None else None for a in args]
+    shape = np.broadcast_shapes(*[a.shape for a in arrs if a is not None])
+    try:
+        with np.errstate(all="ignore"):
+            out = f(*[a if a is None else a for a in arrs])
+        if isinstance(out, tuple):
+            res = tuple(np.broadcast_to(np.asarray(o, dtype=np.float64), shape).copy() for o in out)
+            return res
+        out = np.asarray(out, dtype=np.float64)
+        return np.broadcast_to(out, shape).copy()
+    except (ValueError, TypeError):
+        pass
+    bargs = [None if a is None else np.broadcast_to(a, shape).ravel() for a in arrs]
+    n = int(np.prod(shape)) if shape else 1
+    first = f(*[None if a is None else float(a[0]) for a in bargs])
+    if isinstance(first, tuple):
+        outs = [np.empty(n) for _ in first]
+        for m in range(n):
+            r = f(*[None if a is None else float(a[m]) for a in bargs])
+            for c in range(len(outs)):
+                outs[c][m] = r[c]
+        return tuple(o.reshape(shape) for o in outs)
+    out = np.empty(n)
+    for m in range(n):
+        out[m] = f(*[None if a is None else float(a[m]) for a in bargs])
+    return out.reshape(shape)
+
+
+# --------------------------------------------------------------------------------------
+# geometry: src/geometry.jl:99-169
+# --------------------------------------------------------------------------------------
+class Geometry:
+    """FVMGeometry restated (src/geometry.jl:99-169).
+
+    Attributes
+    ----------
+    cv_volumes : (npoints,)
+    s : (ntri, 9) shape-function coefficients s1..s9 (geometry.jl:137-147)
+    mid : (ntri, 3, 2) dual-edge midpoints (m_e + c)/2 (geometry.jl:149-151)
+    nrm : (ntri, 3, 2) unit normals (e_y, -e_x)/l with e = c - m_e (:153-161)
+    length : (ntri, 3) dual-edge lengths
+    """
+
+    def __init__(self, points, triangles):
+        P = np.asarray(points, dtype=np.float64)
+        T = np.asarray(triangles, dtype=np.int64)
+        self.points, self.triangles = P, T
+        i, j, k = T[:, 0], T[:, 1], T[:, 2]
+        px, py = P[i, 0], P[i, 1]
+        qx, qy = P[j, 0], P[j, 1]
+        rx, ry = P[k, 0], P[k, 1]
+        # DelaunayTriangulation statistics: centroid (p+q+r)/3, edge midpoints (p+q)/2, (q+r)/2, (r+p)/2
+        cx, cy = (px + qx + rx) / 3, (py + qy + ry) / 3
+        m1x, m1y = (px + qx) / 2, (py + qy) / 2
+        m2x, m2y = (qx + rx) / 2, (qy + ry) / 2
+        m3x, m3y = (rx + px) / 2, (ry + py) / 2
+        pcx, pcy = cx - px, cy - py
+        qcx, qcy = cx - qx, cy - qy
+        rcx, rcy = cx - rx, cy - ry
+        m13x, m13y = m1x - m3x, m1y - m3y
+        m21x, m21y = m2x - m1x, m2y - m1y
+        m32x, m32y = m3x - m2x, m3y - m2y
+        S1 = 1 / 2 * np.abs(pcx * m13y - pcy * m13x)
+        S2 = 1 / 2 * np.abs(qcx * m21y - qcy * m21x)
+        S3 = 1 / 2 * np.abs(rcx * m32y - rcy * m32x)
+        vol = np.zeros(P.shape[0])
+        # geometry.jl:133-135 accumulates triangle by triangle
+        stacked_idx = np.stack([i, j, k], axis=1).ravel()
+        stacked_val = np.stack([S1, S2, S3], axis=1).ravel()
+        np.add.at(vol, stacked_idx, stacked_val)
+        self.cv_volumes = vol
+        D = qx * ry - qy * rx - px * ry + rx * py + px * qy - qx * py
+        s = np.empty((T.shape[0], 9))
+        s[:, 0] = (qy - ry) / D
+        s[:, 1] = (ry - py) / D
+        s[:, 2] = (py - qy) / D
+        s[:, 3] = (rx - qx) / D
+        s[:, 4] = (px - rx) / D
+        s[:, 5] = (qx - px) / D
+        s[:, 6] = (qx * ry - rx * qy) / D
+        s[:, 7] = (rx * py - px * ry) / D
+        s[:, 8] = (px * qy - qx * py) / D
+        self.s = s
+        mid = np.empty((T.shape[0], 3, 2))
+        mid[:, 0, 0], mid[:, 0, 1] = (m1x + cx) / 2, (m1y + cy) / 2
+        mid[:, 1, 0], mid[:, 1, 1] = (m2x + cx) / 2, (m2y + cy) / 2
+        mid[:, 2, 0], mid[:, 2, 1] = (m3x + cx) / 2, (m3y + cy) / 2
+        self.mid = mid
+        nrm = np.empty((T.shape[0], 3, 2))
+        length = np.empty((T.shape[0], 3))
+        for e, (mx, my) in enumerate(((m1x, m1y), (m2x, m2y), (m3x, m3y))):
+            ex, ey = cx - mx, cy - my
+            l = np.sqrt(ex * ex + ey * ey)  # LinearAlgebra.norm of a 2-tuple
+            length[:, e] = l
+            nrm[:, e, 0], nrm[:, e, 1] = ey / l, -ex / l
+        self.nrm, self.length = nrm, length
+        # key lookup for _safe_get_triangle_props (src/utils.jl:1-11)
+        n = max(P.shape[0], 1)
+        self._key = {}
+        keys = i * n * n + j * n + k
+        self._keys_sorted = np.argsort(keys)
+        self._keys = keys[self._keys_sorted]
+        self._n = n
+
+    def find_triangle(self, a, b, c):
+        """Index and rotation of triangle (a,b,c) as stored (utils.jl:1-11).
+
+        Tries (a,b,c), (b,c,a), (c,a,b) in that order, like
+        `_safe_get_triangle_props`.  Vectorised over arrays.
+        """
+        a, b, c = (np.asarray(x, dtype=np.int64) for x in (a, b, c))
+        n = self._n
+        out = np.full(a.shape, -1, dtype=np.int64)
+        rot = np.zeros(a.shape, dtype=np.int64)
+        for r, (x, y, z) in enumerate(((a, b, c), (b, c, a), (c, a, b))):
+            q = x * n * n + y * n + z
+            pos = np.searchsorted(self._keys, q)
+            pos = np.minimum(pos, self._keys.size - 1)
+            hit = (self._keys[pos] == q) & (out < 0)
+            out[hit] = self._keys_sorted[pos[hit]]
+            rot[hit] = r
+        if np.any(out < 0):
+            raise KeyError("triangle not found in geometry")
+        return out, rot
+
+
+def boundary_cv_components(points, i, j):
+    """get_boundary_cv_components (src/equations/control_volumes.jl:41-56)."""
+    P = points
+    px, py = P[i, 0], P[i, 1]
+    qx, qy = P[j, 0], P[j, 1]
+    lij = np.sqrt((qx - px) ** 2 + (qy - py) ** 2)
+    nx, ny = (qy - py) / lij, -(qx - px) / lij
+    mijx, mijy = (px + qx) / 2, (py + qy) / 2
+    mix, miy = (px + mijx) / 2, (py + mijy) / 2
+    mjx, mjy = (qx + mijx) / 2, (qy + mijy) / 2
+    li = np.sqrt((mijx - px) ** 2 + (mijy - py) ** 2)
+    return nx, ny, mix, miy, mjx, mjy, li
+
+
+# --------------------------------------------------------------------------------------
+# conditions: src/conditions.jl:486-552
+# --------------------------------------------------------------------------------------
+class Conditions:
+    """Conditions restated (src/conditions.jl:310-324, 486-552).
+
+    `functions` = internal functions first, then one per boundary segment
+    (conditions.jl:499,518).  Segments are visited in increasing order; the
+    reference visits them in the iteration order of DelaunayTriangulation's
+    ghost-vertex Dict, which only matters for a node shared by two Dirichlet
+    (or two Dudt) segments with different functions (the last visit wins).
+    """
+
+    def __init__(self, tri, bc_functions, bc_types, ic_functions=(), dirichlet_nodes=None, dudt_nodes=None):
+        if len(bc_functions) != tri.num_ghost_vertices:
+            raise AssertionError("The number of boundary conditions must be the same as the number of parts of the mesh's boundary.")
+        nif = len(ic_functions)
+        self.functions = tuple(ic_functions) + tuple(bc_functions)
+        self.neumann_edges = {}
+        self.constrained_edges = {}
+        self.dirichlet_nodes = dict(dirichlet_nodes or {})
+        self.dudt_nodes = dict(dudt_nodes or {})
+        for s, nodes in enumerate(tri.boundary_nodes):
+            cond = bc_types[s]
+            fidx = s + nif
+            for a in range(len(nodes) - 1):
+                u, v = int(nodes[a]), int(nodes[a + 1])
+                if cond == NEUMANN_T:
+                    self.neumann_edges[(u, v)] = fidx
+                elif cond == CONSTRAINED_T:
+                    self.constrained_edges[(u, v)] = fidx
+                elif cond == DIRICHLET_T:
+                    self.dirichlet_nodes[u] = fidx
+                    self.dirichlet_nodes[v] = fidx
+                else:
+                    self.dudt_nodes[u] = fidx
+                    self.dudt_nodes[v] = fidx
+
+    def has_condition(self, i):
+        return i in self.dudt_nodes or i in self.dirichlet_nodes
+
+    def vertex_tables(self, npoints, has_vertex):
+        """Per-point code and function index, the classification the kernels consume.
+
+        code: NOT_A_VERTEX if the point is in no solid triangle
+        (source_contributions.jl:36-37), else DIRICHLET if a Dirichlet node,
+        else DUDT if a Dudt node (Dirichlet takes precedence:
+        source_contributions.jl:7-11), else FREE.
+        """
+        code = np.zeros(npoints, dtype=np.int8)
+        fidx = np.full(npoints, -1, dtype=np.int32)
+        for i, f in self.dudt_nodes.items():
+            code[i], fidx[i] = DUDT, f
+        for i, f in self.dirichlet_nodes.items():
+            code[i], fidx[i] = DIRICHLET, f
+        code[~has_vertex] = NOT_A_VERTEX
+        fidx[~has_vertex] = -1
+        return code, fidx
+
+    def edge_tables(self, boundary_edges):
+        """Per boundary edge: Neumann function index or -1 (boundary_edge_contributions.jl:6)."""
+        out = np.full(boundary_edges.shape[0], -1, dtype=np.int32)
+        for m, (u, v) in enumerate(boundary_edges):
+            out[m] = self.neumann_edges.get((int(u), int(v)), -1)
+        return out
+
+
+# --------------------------------------------------------------------------------------
+# problem
+# --------------------------------------------------------------------------------------
+def diffusion_flux(D):
+    """construct_flux_function (src/problem.jl:425-440)."""
+
+    def q(x, y, t, a, b, g):
+        u = a * x + b * y + g
+        Dval = D(x, y, t, u)
+        return (-Dval * a, -Dval * b)
+
+    return q
+
+
+class Problem:
+    """FVMProblem restated (src/problem.jl:96-163); closures take (x,y,t,u)."""
+
+    def __init__(self, tri, conds, flux=None, D=None, source=None, u0=None, t0=0.0, tf=1.0):
+        self.tri = tri
+        self.geo = Geometry(tri.points, tri.triangles)
+        self.conds = conds
+        self.flux = flux if flux is not None else diffusion_flux(D)
+        self.source = source if source is not None else (lambda x, y, t, u: 0.0 * u)
+        self.u0 = None if u0 is None else np.asarray(u0, dtype=np.float64)
+        self.t0, self.tf = t0, tf
+        self.has_vertex = tri.has_vertex()
+        self.code, self.fidx = conds.vertex_tables(tri.num_points, self.has_vertex)
+        self.neumann_fidx = conds.edge_tables(tri.boundary_edges)
+        # boundary edge -> stored triangle (src/equations/boundary_edge_contributions.jl:79-81)
+        be = tri.boundary_edges
+        self.bnd_tri, self.bnd_rot = self.geo.find_triangle(be[:, 0], be[:, 1], tri.boundary_adjacent)
+
+
+def _alpha_beta_gamma(s, ui, uj, uk):
+    """get_shape_function_coefficients (src/equations/shape_functions.jl:2-9)."""
+    a = s[:, 0] * ui + s[:, 1] * uj + s[:, 2] * uk
+    b = s[:, 3] * ui + s[:, 4] * uj + s[:, 5] * uk
+    g = s[:, 6] * ui + s[:, 7] * uj + s[:, 8] * uk
+    return a, b, g
+
+
+def triangle_fluxes(prob, u, t):
+    """Per-triangle Q_e = (q(x_e) . n_e) l_e, e = 1..3 (triangle_contributions.jl:2-7,
+    individual_flux_contributions.jl:2-6,27-33, control_volumes.jl:16-21)."""
+    g = prob.geo
+    T = g.triangles
+    a, b, c = _alpha_beta_gamma(g.s, u[T[:, 0]], u[T[:, 1]], u[T[:, 2]])
+    Q = np.empty((T.shape[0], 3))
+    for e in range(3):
+        x, y = g.mid[:, e, 0], g.mid[:, e, 1]
+        qx, qy = call_pointwise(prob.flux, x, y, t, a, b, c)
+        qn = qx * g.nrm[:, e, 0] + qy * g.nrm[:, e, 1]
+        Q[:, e] = qn * g.length[:, e]
+    return Q
+
+
+def boundary_fluxes(prob, u, t):
+    """Per boundary edge (Q_i, Q_j) (boundary_edge_contributions.jl:2-13,41-48,77-86)."""
+    tri, g = prob.tri, prob.geo
+    be = tri.boundary_edges
+    i, j = be[:, 0], be[:, 1]
+    Tk = g.triangles[prob.bnd_tri]
+    a, b, c = _alpha_beta_gamma(g.s[prob.bnd_tri], u[Tk[:, 0]], u[Tk[:, 1]], u[Tk[:, 2]])
+    nx, ny, mix, miy, mjx, mjy, l = boundary_cv_components(tri.points, i, j)
+    out = []
+    for mx, my in ((mix, miy), (mjx, mjy)):
+        um = a * mx + b * my + c
+        qx, qy = call_pointwise(prob.flux, mx, my, t, a, b, c)
+        qn = qx * nx + qy * ny
+        neu = prob.neumann_fidx >= 0
+        for f in np.unique(prob.neumann_fidx[neu]):
+            sel = prob.neumann_fidx == f
+            qn[sel] = call_pointwise(prob.conds.functions[f], mx[sel], my[sel], t, um[sel])
+        out.append(qn * l)
+    return out[0], out[1]
+
+
+def fvm_eqs(prob, u, t):
+    """serial_fvm_eqs! (src/equations/main_equations.jl:38-44).
+
+    Vectorised over entities; the scatter order (np.add.at, in entity order)
+    matches a serial loop's order of contributions per vertex, though each
+    triangle's pair (Q3 - Q1) is formed before it is added.
+    """
+    u = np.asarray(u, dtype=np.float64)
+    n = u.shape[0]
+    du = np.zeros(n)
+    T = prob.geo.triangles
+    Q = triangle_fluxes(prob, u, t)
+    # update_du! (triangle_contributions.jl:10-15)
+    idx = np.stack([T[:, 0], T[:, 1], T[:, 2]], axis=1).ravel()
+    val = np.stack([Q[:, 2] - Q[:, 0], Q[:, 0] - Q[:, 1], Q[:, 1] - Q[:, 2]], axis=1).ravel()
+    np.add.at(du, idx, val)
+    # boundary edges (boundary_edge_contributions.jl:61-65)
+    Qi, Qj = boundary_fluxes(prob, u, t)
+    be = prob.tri.boundary_edges
+    np.add.at(du, np.stack([be[:, 0], be[:, 1]], axis=1).ravel(), -np.stack([Qi, Qj], axis=1).ravel())
+    return source_contributions(prob, du, u, t)
+
+
+def source_contributions(prob, du, u, t):
+    """get_source_contributions! (src/equations/source_contributions.jl:2-14,33-47,71-76)."""
+    P = prob.tri.points
+    code, fidx = prob.code, prob.fidx
+    out = du.copy()
+    free = code == FREE
+    if np.any(free):
+        S = call_pointwise(prob.source, P[free, 0], P[free, 1], t, u[free])
+        out[free] = du[free] / prob.geo.cv_volumes[free] + S
+    out[code == DIRICHLET] = 0.0
+    out[code == NOT_A_VERTEX] = 0.0
+    dd = code == DUDT
+    for f in np.unique(fidx[dd]):
+        sel = dd & (fidx == f)
+        out[sel] = call_pointwise(prob.conds.functions[f], P[sel, 0], P[sel, 1], t, u[sel])
+    return out
+
+
+def fvm_eqs_loop(prob, u, t):
+    """Line-by-line serial restatement (main_equations.jl:38-44) for small meshes."""
+    g, tri = prob.geo, prob.tri
+    du = np.zeros(u.shape[0])
+    for m, (i, j, k) in enumerate(g.triangles):
+        s = g.s[m]
+        a = s[0] * u[i] + s[1] * u[j] + s[2] * u[k]
+        b = s[3] * u[i] + s[4] * u[j] + s[5] * u[k]
+        c = s[6] * u[i] + s[7] * u[j] + s[8] * u[k]
+        Q = []
+        for e in range(3):
+            x, y = g.mid[m, e]
+            qx, qy = prob.flux(x, y, t, a, b, c)
+            Q.append((qx * g.nrm[m, e, 0] + qy * g.nrm[m, e, 1]) * g.length[m, e])
+        du[i] = du[i] + Q[2] - Q[0]
+        du[j] = du[j] + Q[0] - Q[1]
+        du[k] = du[k] + Q[1] - Q[2]
+    for m, (i, j) in enumerate(tri.boundary_edges):
+        tm = prob.bnd_tri[m]
+        ti, tj, tk = g.triangles[tm]
+        s = g.s[tm]
+        a = s[0] * u[ti] + s[1] * u[tj] + s[2] * u[tk]
+        b = s[3] * u[ti] + s[4] * u[tj] + s[5] * u[tk]
+        c = s[6] * u[ti] + s[7] * u[tj] + s[8] * u[tk]
+        nx, ny, mix, miy, mjx, mjy, l = boundary_cv_components(tri.points, i, j)
+        qs = []
+        for mx, my in ((mix, miy), (mjx, mjy)):
+            if prob.neumann_fidx[m] >= 0:
+                qn = prob.conds.functions[prob.neumann_fidx[m]](mx, my, t, a * mx + b * my + c)
+            else:
+                qx, qy = prob.flux(mx, my, t, a, b, c)
+                qn = qx * nx + qy * ny
+            qs.append(qn * l)
+        du[i] = du[i] - qs[0]
+        du[j] = du[j] - qs[1]
+    out = du.copy()
+    for i in range(u.shape[0]):
+        x, y = tri.points[i]
+        cde = prob.code[i]
+        if cde == NOT_A_VERTEX:
+            out[i] = 0.0
+        elif cde == FREE:
+            out[i] = du[i] / g.cv_volumes[i] + prob.source(x, y, t, u[i])
+        elif cde == DIRICHLET:
+            out[i] = 0.0
+        else:
+            out[i] = prob.conds.functions[prob.fidx[i]](x, y, t, u[i])
+    return out
+
+
+def update_dirichlet_nodes(prob, u, t):
+    """update_dirichlet_nodes! (src/equations/dirichlet.jl:2-8,20-26,38-43)."""
+    u = u.copy()
+    P = prob.tri.points
+    for f in set(prob.conds.dirichlet_nodes.values()):
+        nodes = np.array([i for i, g in prob.conds.dirichlet_nodes.items() if g == f], dtype=np.int64)
+        u[nodes] = call_pointwise(prob.conds.functions[f], P[nodes, 0], P[nodes, 1], t, u[nodes])
+    return u
+
+
+# --------------------------------------------------------------------------------------
+# linear templates: src/specific_problems/*.jl, assembled sparse (not dense)
+# --------------------------------------------------------------------------------------
+def _template_A_entries(tri, geo, conds, D, rows, cols, vals):
+    """triangle_contributions! (src/specific_problems/abstract_templates.jl:73-99)."""
+    T = geo.triangles
+    V = geo.cv_volumes
+    hc = np.zeros(tri.num_points, dtype=bool)
+    for d in (conds.dirichlet_nodes, conds.dudt_nodes):
+        hc[list(d.keys())] = True
+    s = geo.s
+    for e, (a1, a2) in enumerate(((0, 1), (1, 2), (2, 0))):
+        x, y = geo.mid[:, e, 0], geo.mid[:, e, 1]
+        nx, ny = geo.nrm[:, e, 0], geo.nrm[:, e, 1]
+        Dl = call_pointwise(D, x, y) * geo.length[:, e]
+        e1, e2 = T[:, a1], T[:, a2]
+        for vert in range(3):
+            a = Dl * (s[:, vert] * nx + s[:, 3 + vert] * ny)
+            m1 = ~hc[e1]
+            rows.append(e1[m1]); cols.append(T[m1, vert]); vals.append(a[m1] / V[e1[m1]])
+            m2 = ~hc[e2]
+            rows.append(e2[m2]); cols.append(T[m2, vert]); vals.append(-a[m2] / V[e2[m2]])
+    return hc
+
+
+def _template_boundary(tri, geo, conds, D, hc, rows, cols, vals, b, with_neumann=True):
+    """boundary_edge_contributions! (abstract_templates.jl:149-191,237-267).
+
+    Reproduces the reference's use of V_i for row j in the non-Neumann part
+    (abstract_templates.jl:262)."""
+    V = geo.cv_volumes
+    be = tri.boundary_edges
+    tidx, _ = geo.find_triangle(be[:, 0], be[:, 1], tri.boundary_adjacent)
+    for m, (i, j) in enumerate(be):
+        i, j = int(i), int(j)
+        nx, ny, mix, miy, mjx, mjy, l = boundary_cv_components(tri.points, i, j)
+        Di = float(call_pointwise(D, mix, miy))
+        Dj = float(call_pointwise(D, mjx, mjy))
+        if (i, j) in conds.neumann_edges:
+            if not with_neumann:
+                continue
+            f = conds.functions[conds.neumann_edges[(i, j)]]
+            ai = float(np.asarray(f(mix, miy, None, None)))
+            aj = float(np.asarray(f(mjx, mjy, None, None)))
+            if not conds.has_condition(i):
+                b[i] += Di * ai * l / V[i]
+            if not conds.has_condition(j):
+                b[j] += Dj * aj * l / V[j]
+            continue
+        tm = tidx[m]
+        ijk = geo.triangles[tm]
+        s = geo.s[tm]
+        for vert in range(3):
+            w = s[vert] * nx + s[3 + vert] * ny
+            if not hc[i]:
+                rows.append(np.array([i])); cols.append(np.array([ijk[vert]])); vals.append(np.array([Di * l * w / V[i]]))
+            if not hc[j]:
+                rows.append(np.array([j])); cols.append(np.array([ijk[vert]])); vals.append(np.array([Dj * l * w / V[i]]))
+
+
+def _csr(n, rows, cols, vals):
+    from scipy.sparse import coo_matrix
+
+    r = np.concatenate(rows) if rows else np.zeros(0, np.int64)
+    c = np.concatenate(cols) if cols else np.zeros(0, np.int64)
+    v = np.concatenate(vals) if vals else np.zeros(0)
+    A = coo_matrix((v, (r, c)), shape=(n, n)).tocsr()
+    A.sum_duplicates()
+    return A
+
+
+def _eval_at_points(f, P, nodes):
+    return np.array([float(np.asarray(f(P[i, 0], P[i, 1], None, None))) for i in nodes]) if len(nodes) else np.zeros(0)
+
+
+def template_diffusion(tri, conds, D, ic, reaction=None):
+    """DiffusionEquation / LinearReactionDiffusionEquation assembly
+    (diffusion_equation.jl:69-101; linear_reaction_diffusion_equations.jl:76-125).
+
+    Returns (A, b, u0) with du/dt = A u + b; u0 has Dirichlet values applied
+    (abstract_templates.jl:109-117)."""
+    geo = Geometry(tri.points, tri.triangles)
+    n = tri.num_points
+    rows, cols, vals = [], [], []
+    b = np.zeros(n)
+    hc = _template_A_entries(tri, geo, conds, D, rows, cols, vals)
+    _template_boundary(tri, geo, conds, D, hc, rows, cols, vals, b)
+    if reaction is not None:  # linear_source_contributions! (:115-125)
+        free = np.nonzero(~hc & tri.has_vertex())[0]
+        rows.append(free); cols.append(free); vals.append(call_pointwise(reaction, tri.points[free, 0], tri.points[free, 1]))
+    # apply_dudt_conditions! (abstract_templates.jl:127-135)
+    P = tri.points
+    for i, f in conds.dudt_nodes.items():
+        if i not in conds.dirichlet_nodes:
+            b[i] = float(np.asarray(conds.functions[f](P[i, 0], P[i, 1], None, None)))
+    u0 = np.array(ic, dtype=np.float64)
+    for i, f in conds.dirichlet_nodes.items():
+        u0[i] = float(np.asarray(conds.functions[f](P[i, 0], P[i, 1], None, None)))
+    # fix_missing_vertices! (:317-325)
+    miss = np.nonzero(~tri.has_vertex())[0]
+    rows.append(miss); cols.append(miss); vals.append(np.ones(miss.size)); b[miss] = 0.0
+    return _csr(n, rows, cols, vals), b, u0
+
+
+def template_poisson(tri, conds, D, f):
+    """PoissonsEquation assembly (poissons_equation.jl:58-88; create_rhs_b
+    abstract_templates.jl:278-288; apply_steady_dirichlet_conditions! :302-309)."""
+    if conds.dudt_nodes:
+        raise ValueError("PoissonsEquation does not support Dudt nodes.")
+    geo = Geometry(tri.points, tri.triangles)
+    n = tri.num_points
+    P = tri.points
+    hv = tri.has_vertex()
+    b = np.zeros(n)
+    nd = np.array([i for i in range(n) if hv[i] and i not in conds.dirichlet_nodes], dtype=np.int64)
+    if nd.size:
+        b[nd] = call_pointwise(f, P[nd, 0], P[nd, 1])
+    rows, cols, vals = [], [], []
+    hc = _template_A_entries(tri, geo, conds, D, rows, cols, vals)
+    _template_boundary(tri, geo, conds, D, hc, rows, cols, vals, b)
+    for i, g in conds.dirichlet_nodes.items():
+        b[i] = float(np.asarray(conds.functions[g](P[i, 0], P[i, 1], None, None)))
+    dn = np.array(sorted(conds.dirichlet_nodes), dtype=np.int64)
+    A = _csr(n, rows, cols, vals)
+    A = _set_diag(A, dn, 1.0)
+    miss = np.nonzero(~hv)[0]
+    A = _set_diag(A, miss, 1.0)
+    b[miss] = 0.0
+    return A, b
+
+
+def template_mean_exit_time(tri, conds, D):
+    """MeanExitTimeProblem assembly (mean_exit_time.jl:57-94): triangle
+    contributions only; b = -1 off Dirichlet nodes, A_ii = 1 on them."""
+    if conds.dudt_nodes:
+        raise ValueError("MeanExitTimeProblem does not support Dudt nodes.")
+    if conds.constrained_edges:
+        raise ValueError("MeanExitTimeProblem does not support Constrained edges.")
+    geo = Geometry(tri.points, tri.triangles)
+    n = tri.num_points
+    hv = tri.has_vertex()
+    rows, cols, vals = [], [], []
+    _template_A_entries(tri, geo, conds, D, rows, cols, vals)
+    b = np.zeros(n)
+    dmask = np.zeros(n, dtype=bool)
+    dmask[list(conds.dirichlet_nodes.keys())] = True
+    b[hv & ~dmask] = -1.0
+    A = _csr(n, rows, cols, vals)
+    A = _set_diag(A, np.nonzero(hv & dmask)[0], 1.0)
+    miss = np.nonzero(~hv)[0]
+    A = _set_diag(A, miss, 1.0)
+    b[miss] = 0.0
+    return A, b
+
+
+def _set_diag(A, idx, value):
+    """A[i, i] = value for i in idx (assignment, not accumulation)."""
+    if len(idx) == 0:
+        return A
+    A = A.tolil()
+    for i in idx:
+        A[i, i] = value
+    return A.tocsr()
+
+
+# --------------------------------------------------------------------------------------
+# Tsit5 (Tsitouras 2011), restated from the published tableau
+# --------------------------------------------------------------------------------------
+TSIT5_C = np.array([0.0, 0.161, 0.327, 0.9, 0.9800255409045097, 1.0, 1.0])
+TSIT5_A = [
+    [],
+    [0.161],
+    [-0.008480655492356989, 0.335480655492357],
+    [2.897153057105493, -6.359448489975075, 4.3622954328695815],
+    [5.325864828439257, -11.748883564062828, 7.4955393428898365, -0.09249506636175525],
+    [5.86145544294642, -12.92096931784711, 8.159367898576159, -0.071584973281401, -0.028269050394068383],
+    [0.09646076681806523, 0.01, 0.4798896504144996, 1.379008574103742, -3.290069515436081, 2.324710524099774],
+]
+TSIT5_B = np.array(TSIT5_A[6] + [0.0])
+# b - bhat (error estimate weights)
+TSIT5_BT = np.array([
+    -0.00178001105222577714, -0.0008164344596567469, 0.007880878010261995,
+    -0.1447110071732629, 0.5823571654525552, -0.45808210592918697, 0.015151515151515152,
+])
+
+
+def tsit5_step(f, u, t, dt, k1=None):
+    """One Tsit5 step.  Returns (u_new, k list of 7 stage derivatives)."""
+    k = [f(u, t) if k1 is None else k1]
+    for s in range(1, 7):
+        y = u.copy()
+        for j, a in enumerate(TSIT5_A[s]):
+            y += dt * a * k[j]
+        k.append(f(y, t + TSIT5_C[s] * dt))
+    # the 7th stage point equals u_new (FSAL)
+    unew = u.copy()
+    for j in range(6):
+        unew += dt * TSIT5_B[j] * k[j]
+    return unew, k
+
+
+def tsit5_fixed(prob, u0, t0, dt, nsteps, rhs=None, dirichlet=True):
+    """Fixed-step Tsit5 with the Dirichlet callback after every step
+    (src/solve.jl:133-144: DiscreteCallback with condition true)."""
+    f = rhs or (lambda u, t: fvm_eqs(prob, u, t))
+    u = np.array(u0, dtype=np.float64)
+    t = t0
+    k1 = None
+    for _ in range(nsteps):
+        u, k = tsit5_step(f, u, t, dt, k1)
+        t = t0 + (_ + 1) * dt
+        if dirichlet and prob is not None and prob.conds.dirichlet_nodes:
+            u = update_dirichlet_nodes(prob, u, t)
+            k1 = None  # the callback modified u: FSAL derivative re-evaluated
+        else:
+            k1 = k[6]
+    return u
+
+
+def hermite(u0, u1, f0, f1, dt, th):
+    """Cubic Hermite interpolant on one step (the saveat interpolant of this build)."""
+    t2, t3 = th * th, th * th * th
+    return ((2 * t3 - 3 * t2 + 1) * u0 + (t3 - 2 * t2 + th) * dt * f0 + (-2 * t3 + 3 * t2) * u1
+            + (t3 - t2) * dt * f1)
+
+
+def tsit5_solve(f, u0, t0, tf, saveat, dt=None, adaptive=True, abstol=1e-6, reltol=1e-3, callback=None,
+                max_steps=10_000_000):
+    """Tsit5 driver with the step control of OrdinaryDiffEq's defaults for Tsit5 (PI
+    controller beta1 = 7/50, beta2 = 2/25, qmin = 1/5, qmax = 10, gamma = 9/10,
+    qoldinit = 1e-4; RMS error norm; Hairer initial step) and a per-step callback applied
+    after each accepted step (src/solve.jl:133-144).  saveat values inside a step are
+    cubic-Hermite interpolated from the pre-callback step; values at a step end are the
+    post-callback state.  Returns (snapshots, stats)."""
+    u = np.array(u0, dtype=np.float64)
+    n = u.size
+    saveat = list(saveat)
+    out = []
+    si = 0
+    t = t0
+    while si < len(saveat) and saveat[si] == t0:
+        out.append(u.copy())
+        si += 1
+    k1 = f(u, t)
+    nrhs = 1
+    tspan = tf - t0
+    rms = lambda v: np.sqrt(np.sum(v * v) / max(1, n))  # noqa: E731
+    if adaptive and not dt:
+        sc = abstol + np.abs(u) * reltol
+        d0, d1 = rms(u / sc), rms(k1 / sc)
+        dt0 = 1e-6 if (d0 < 1e-5 or d1 < 1e-5) else 0.01 * d0 / d1
+        dt0 = min(dt0, tspan)
+        f1 = f(u + dt0 * k1, t + dt0)
+        nrhs += 1
+        d2 = rms((f1 - k1) / sc) / dt0
+        md = max(d1, d2)
+        dt1 = max(1e-6, dt0 * 1e-3) if md <= 1e-15 else 10.0 ** (-(2.0 + np.log10(md)) / 5.0)
+        dt = min(100 * dt0, dt1, tspan)
+    beta1, beta2, qmin, qmax, gamma = 7 / 50, 2 / 25, 0.2, 10.0, 0.9
+    qold = 1e-4
+    nfixed = 0 if adaptive else int(np.ceil(tspan / dt - 1e-9))
+    step = naccept = nreject = 0
+    first_cb = True
+    while (t < tf) if adaptive else (step < nfixed):
+        if step >= max_steps:
+            raise RuntimeError("max_steps")
+        if adaptive:
+            last = t + dt >= tf
+            h = tf - t if last else dt
+        else:
+            last = step + 1 == nfixed
+            tn_ = tf if last else t0 + (step + 1) * dt
+            h = tn_ - t
+        k = [k1]
+        for s_ in range(1, 7):
+            y = u.copy()
+            for j, a in enumerate(TSIT5_A[s_]):
+                y += h * a * k[j]
+            if s_ < 6:
+                k.append(f(y, t + TSIT5_C[s_] * h))
+                nrhs += 1
+        unew = y
+        k.append(f(unew, t + h))
+        nrhs += 1
+        if adaptive:
+            err = h * sum(TSIT5_BT[j] * k[j] for j in range(7))
+            EEst = rms(err / (abstol + np.maximum(np.abs(u), np.abs(unew)) * reltol))
+            if EEst == 0:
+                q = 1 / qmax
+                q11 = 0.0
+            else:
+                q11 = EEst ** beta1
+                q = max(1 / qmax, min(1 / qmin, q11 / qold ** beta2 / gamma))
+            if EEst > 1:
+                nreject += 1
+                step += 1
+                dt = h / min(1 / qmin, q11 / gamma)
+                continue
+        tn = tf if last else (t + h if adaptive else t0 + (step + 1) * dt)
+        while si < len(saveat) and saveat[si] < tn:
+            out.append(hermite(u, unew, k[0], k[6], h, (saveat[si] - t) / h))
+            si += 1
+        u = unew
+        t = tn
+        naccept += 1
+        step += 1
+        reeval = False
+        if callback is not None:
+            u = callback(u, t)
+            reeval = first_cb
+            first_cb = False
+        while si < len(saveat) and saveat[si] == t:
+            out.append(u.copy())
+            si += 1
+        if reeval:
+            k1 = f(u, t)
+            nrhs += 1
+        else:
+            k1 = k[6]
+        if adaptive:
+            qold = max(EEst, 1e-4)
+            dt = min(h / q, tspan)
+        if last:
+            break
+    while si < len(saveat):
+        out.append(u.copy())
+        si += 1
+    return np.array(out), {"naccept": naccept, "nreject": nreject, "nrhs": nrhs}
+
+
+def steady_solve(A, b):
+    """Direct sparse solve of A u = b (stands in for LinearSolve's KLU in the docs)."""
+    from scipy.sparse.linalg import spsolve
+
+    return spsolve(A.tocsc(), b)

@@ -1,0 +1,134 @@
+"""Problems of the reference's tests and documentation, restated once and built both for
+the oracle and for the GPU API from the same closures (signatures as in the reference:
+conditions a(x, y, t, u, p), diffusion D(x, y, t, u, p), flux q(x, y, t, a, b, g, p),
+source S(x, y, t, u, p))."""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+from typing import Any, Callable, Dict, Optional, Tuple
+
+import numpy as np
+
+import fvm_oracle as O
+from fvmgpu.meshes import triangulate_annulus, triangulate_disk, triangulate_rectangle
+
+
+@dataclass
+class Spec:
+    tri: Any
+    bc_fns: Tuple
+    bc_types: Tuple[str, ...]
+    bc_params: Tuple
+    ic_fns: Tuple = ()
+    ic_params: Tuple = ()
+    dirichlet_nodes: Dict[int, int] = field(default_factory=dict)
+    dudt_nodes: Dict[int, int] = field(default_factory=dict)
+    D: Optional[Callable] = None
+    Dp: Any = None
+    flux: Optional[Callable] = None
+    fluxp: Any = None
+    S: Optional[Callable] = None
+    Sp: Any = None
+    u0: Any = None
+    t0: float = 0.0
+    tf: float = 1.0
+
+
+def _bind(f, p):
+    return lambda *a: f(*a, p)
+
+
+def oracle_problem(s: Spec) -> O.Problem:
+    conds = O.Conditions(s.tri, [_bind(f, p) for f, p in zip(s.bc_fns, s.bc_params)], list(s.bc_types),
+                         [_bind(f, p) for f, p in zip(s.ic_fns, s.ic_params)], s.dirichlet_nodes, s.dudt_nodes)
+    return O.Problem(s.tri, conds,
+                     flux=_bind(s.flux, s.fluxp) if s.flux else None,
+                     D=_bind(s.D, s.Dp) if s.D else None,
+                     source=_bind(s.S, s.Sp) if s.S else None, u0=s.u0, t0=s.t0, tf=s.tf)
+
+
+def api_problem(s: Spec, precision="fp64", mesh=None, tile_vertices=0):
+    import fvmgpu as F
+
+    mesh = mesh or F.FVMGeometry(s.tri, tile_vertices=tile_vertices)
+    types = tuple(getattr(F, t) for t in s.bc_types)
+    BCs = F.BoundaryConditions(mesh, tuple(s.bc_fns), types, parameters=tuple(s.bc_params))
+    ICs = F.InternalConditions(tuple(s.ic_fns), dirichlet_nodes=s.dirichlet_nodes, dudt_nodes=s.dudt_nodes,
+                               parameters=tuple(s.ic_params)) if (s.ic_fns or s.dirichlet_nodes or s.dudt_nodes) else None
+    return F.FVMProblem(mesh, BCs, ICs, diffusion_function=s.D, diffusion_parameters=s.Dp, flux_function=s.flux,
+                        flux_parameters=s.fluxp, source_function=s.S, source_parameters=s.Sp, initial_condition=s.u0,
+                        initial_time=s.t0, final_time=s.tf, precision=precision)
+
+
+# ---- README / example_diffusion_problem (test/README.jl:4-15; test_functions.jl:304-317) ----
+def readme_diffusion(n=50) -> Spec:
+    tri = triangulate_rectangle(0.0, 2.0, 0.0, 2.0, n, n, single_boundary=True)
+    u0 = np.where(tri.points[:, 1] <= 1.0, 50.0, 0.0)
+    return Spec(tri, (lambda x, y, t, u, p: 0.0 * x,), ("Dirichlet",), (None,),
+                D=lambda x, y, t, u, p: 1 / 9 + 0.0 * x, u0=u0, tf=0.5)
+
+
+# ---- heat convection, Neumann on all four sides (test_functions.jl:336-374) ------------------
+def heat_convection(n=200) -> Spec:
+    tri = triangulate_rectangle(0.0, 1.0, 0.0, 1.0, n, n, single_boundary=False)
+    P = dict(alpha=80e-6, q=10.0, k=237.0, h=25.0, Tinf=10.0)
+    bot = lambda x, y, t, T, p: -p["alpha"] * p["q"] / p["k"] + 0.0 * x  # noqa: E731
+    right = lambda x, y, t, T, p: 0.0 * x  # noqa: E731
+    top = lambda x, y, t, T, p: -p["alpha"] * p["h"] / p["k"] * (p["Tinf"] - T)  # noqa: E731
+    left = lambda x, y, t, T, p: 0.0 * x  # noqa: E731
+    flux = lambda x, y, t, a, b, g, p: (-p["alpha"] * a, -p["alpha"] * b)  # noqa: E731
+    u0 = np.full(tri.num_points, 10.0)
+    return Spec(tri, (bot, right, top, left), ("Neumann",) * 4, (P, None, P, None), flux=flux, fluxp=P, u0=u0,
+                tf=2000.0)
+
+
+# ---- mixed conditions on an annulus (the reference's example_tri + example_bc_setup kinds) ------
+def mixed_annulus(nr=9, ntheta=48, seed=1) -> Spec:
+    tri = triangulate_annulus(0.5, 1.0, nr, ntheta, nsegments=4)
+    rng = np.random.default_rng(seed)
+    fns = (
+        lambda x, y, t, u, p: x * y - p + 0.0 * x,       # 0 Dirichlet
+        lambda x, y, t, u, p: u * p - 0.3 * x,           # 1 Dudt (affine in u)
+        lambda x, y, t, u, p: x + 0.0 * y,               # 2 Neumann
+        lambda x, y, t, u, p: y - x,                     # 3 Constrained (never called)
+        lambda x, y, t, u, p: p * (1.5 - u),             # 4 Neumann, Robin type
+        lambda x, y, t, u, p: 0.2 + 0.0 * x,             # 5 Dirichlet
+        lambda x, y, t, u, p: 0.1 * u * u - y,           # 6 Dudt (quadratic in u)
+        lambda x, y, t, u, p: 0.0 * x,                   # 7 Neumann, homogeneous
+    )
+    types = ("Dirichlet", "Dudt", "Neumann", "Constrained", "Neumann", "Dirichlet", "Dudt", "Neumann")
+    params = (0.7, 0.3, None, None, 0.8, None, None, None)
+    interior = np.nonzero(np.linalg.norm(tri.points, axis=1) < 0.9)[0]
+    interior = interior[np.linalg.norm(tri.points[interior], axis=1) > 0.6]
+    dnode, dudtnode = int(interior[3]), int(interior[11])
+    ic_fns = (lambda x, y, t, u, p: x + y + p + 0.0 * x, lambda x, y, t, u, p: -0.5 * u + p)
+    u0 = rng.standard_normal(tri.num_points)
+    return Spec(tri, fns, types, params, ic_fns=ic_fns, ic_params=(0.29, 0.1),
+                dirichlet_nodes={dnode: 0}, dudt_nodes={dudtnode: 1},
+                D=lambda x, y, t, u, p: 1.0 + x * x + 0.5 * y + 0.0 * u,
+                S=lambda x, y, t, u, p: p * u - 0.1 * u * u + x, Sp=0.5, u0=u0, t0=0.0, tf=0.1)
+
+
+# ---- nonlinear diffusion D(u) (porous-medium-like, polynomial in u) -------------------------
+def nonlinear_rect(n=30, seed=2) -> Spec:
+    tri = triangulate_rectangle(0.0, 1.0, 0.0, 1.0, n, n, single_boundary=False)
+    rng = np.random.default_rng(seed)
+    fns = (lambda x, y, t, u, p: 0.0 * x, lambda x, y, t, u, p: 0.1 * u,
+           lambda x, y, t, u, p: 1.0 + 0.0 * x, lambda x, y, t, u, p: 0.05 * u * u)
+    types = ("Dirichlet", "Neumann", "Dirichlet", "Neumann")
+    u0 = 0.5 + 0.2 * rng.random(tri.num_points)
+    return Spec(tri, fns, types, (None,) * 4, D=lambda x, y, t, u, p: 1.0 + x + 0.5 * u * u,
+                S=lambda x, y, t, u, p: u * (1 - u), u0=u0, tf=0.01)
+
+
+# ---- DiffusionEquation-style field D(x, y) = 1 + 0.5 sin(2 pi x) sin(2 pi y) -----------------
+def sine_diffusion(n=64) -> Spec:
+    tri = triangulate_rectangle(0.0, 1.0, 0.0, 1.0, n, n, single_boundary=True)
+    P = tri.points
+    u0 = np.exp(-50 * ((P[:, 0] - 0.5) ** 2 + (P[:, 1] - 0.5) ** 2))
+    D = lambda x, y, t, u, p: 1 + 0.5 * np.sin(2 * np.pi * x) * np.sin(2 * np.pi * y)  # noqa: E731
+    return Spec(tri, (lambda x, y, t, u, p: 0.0 * x,), ("Dirichlet",), (None,), D=D, u0=u0, tf=1e-4)
+
+
+def disk_poisson_mesh(n_interior=3000, n_boundary=128, seed=0):
+    return triangulate_disk(n_interior, n_boundary, seed=seed)

@@ -1,0 +1,167 @@
+"""GPU parity of fvm_eqs! (libfvmgpu through the C ABI) against the oracle.
+
+Tolerances: FP64 RHS within 1e-12 relative (normwise, and max-norm relative to max|du|);
+FP32 assembly within 2e-5 relative.  Integer tables (connectivity, classification) bit-exact.
+"""
+import numpy as np
+import pytest
+
+import fvm_oracle as O
+from problems import (api_problem, heat_convection, mixed_annulus, nonlinear_rect, oracle_problem, readme_diffusion,
+                      sine_diffusion)
+
+pytestmark = pytest.mark.gpu
+
+FP64_RTOL = 1e-12
+FP32_RTOL = 2e-5
+
+
+def rel_err(got, ref):
+    den = max(np.linalg.norm(ref), 1e-300)
+    return np.linalg.norm(got - ref) / den, np.max(np.abs(got - ref)) / max(np.max(np.abs(ref)), 1e-300)
+
+
+BUILDERS = {
+    "readme50": lambda: readme_diffusion(50),
+    "heat_convection200": lambda: heat_convection(200),
+    "mixed_annulus": mixed_annulus,
+    "sine64": lambda: sine_diffusion(64),
+    "nonlinear30": lambda: nonlinear_rect(30),
+}
+
+
+@pytest.mark.parametrize("name", list(BUILDERS))
+def test_rhs_parity_fp64(gpu_lib, name):
+    import fvmgpu as F
+
+    spec = BUILDERS[name]()
+    oprob = oracle_problem(spec)
+    rng = np.random.default_rng(11)
+    for trial in range(2):
+        u = spec.u0 if trial == 0 else spec.u0 + rng.standard_normal(spec.tri.num_points) * 0.1
+        ref = O.fvm_eqs(oprob, u, spec.t0)
+        prob = api_problem(spec)
+        for force in (False, True):
+            du = np.zeros_like(u)
+            F.fvm_eqs(du, np.ascontiguousarray(u), prob, spec.t0, force_triangle=force)
+            e2, einf = rel_err(du, ref)
+            assert e2 <= FP64_RTOL and einf <= FP64_RTOL, (name, force, e2, einf)
+
+
+def test_rhs_parity_device_pointers(gpu_lib):
+    import torch
+    import fvmgpu as F
+
+    spec = mixed_annulus()
+    oprob = oracle_problem(spec)
+    prob = api_problem(spec)
+    u = torch.tensor(spec.u0, dtype=torch.float64, device="cuda")
+    du = torch.zeros_like(u)
+    F.fvm_eqs(du, u, {"prob": prob}, 0.0)
+    torch.cuda.synchronize()
+    ref = O.fvm_eqs(oprob, spec.u0, 0.0)
+    e2, einf = rel_err(du.cpu().numpy(), ref)
+    assert e2 <= FP64_RTOL and einf <= FP64_RTOL
+
+
+@pytest.mark.parametrize("name", ["readme50", "heat_convection200", "sine64", "mixed_annulus"])
+def test_rhs_parity_fp32(gpu_lib, name):
+    import fvmgpu as F
+
+    spec = BUILDERS[name]()
+    ref = O.fvm_eqs(oracle_problem(spec), spec.u0, 0.0)
+    prob = api_problem(spec, precision="fp32")
+    du = np.zeros_like(spec.u0)
+    F.fvm_eqs(du, np.ascontiguousarray(spec.u0, dtype=np.float64), prob, 0.0)
+    e2, _ = rel_err(du, ref)
+    assert e2 <= FP32_RTOL, e2
+
+
+@pytest.mark.parametrize("tile", [64, 256, 1024])
+def test_tile_sizes_agree(gpu_lib, tile):
+    import fvmgpu as F
+
+    spec = nonlinear_rect(40)
+    ref = O.fvm_eqs(oracle_problem(spec), spec.u0, 0.0)
+    prob = api_problem(spec, tile_vertices=tile)
+    du = np.zeros_like(spec.u0)
+    F.fvm_eqs(du, spec.u0.copy(), prob, 0.0)
+    e2, einf = rel_err(du, ref)
+    assert e2 <= FP64_RTOL and einf <= FP64_RTOL
+
+
+@pytest.mark.parametrize("name", ["mixed_annulus", "heat_convection200"])
+def test_connectivity_and_classification_bit_exact(gpu_lib, name):
+    """Device-resident triangles / boundary elements / vertex codes / Neumann flags, read back
+    and mapped to the caller's numbering, equal the oracle's tables exactly."""
+    spec = BUILDERS[name]()
+    oprob = oracle_problem(spec)
+    prob = api_problem(spec)
+    tris, belems = prob.mesh.export_connectivity()
+    assert np.array_equal(tris, spec.tri.triangles)
+    assert np.array_equal(belems[:, :2], spec.tri.boundary_edges)
+    assert np.array_equal(belems[:, 2], spec.tri.boundary_adjacent)
+    code, neu = prob.export_codes()
+    assert np.array_equal(code, oprob.code)
+    assert np.array_equal(neu, (oprob.neumann_fidx >= 0).astype(np.int8))
+    perm = prob.mesh.permutation()
+    assert np.array_equal(np.sort(perm), np.arange(spec.tri.num_points))
+    assert np.allclose(prob.mesh.cv_volumes, oprob.geo.cv_volumes, rtol=1e-14, atol=0)
+
+
+def test_dirichlet_update(gpu_lib):
+    import fvmgpu as F
+
+    spec = mixed_annulus()
+    oprob = oracle_problem(spec)
+    prob = api_problem(spec)
+    u = spec.u0.copy()
+    F.update_dirichlet_nodes(u, prob, 0.0)
+    ref = O.update_dirichlet_nodes(oprob, spec.u0, 0.0)
+    assert np.array_equal(u, ref)
+
+
+def test_unsupported_forms_are_rejected(gpu_lib):
+    import fvmgpu as F
+
+    spec = readme_diffusion(10)
+    spec.D = lambda x, y, t, u, p: 1.0 + np.exp(u)
+    with pytest.raises(F.UnsupportedFormError):
+        api_problem(spec)
+    spec = readme_diffusion(10)
+    spec.D = lambda x, y, t, u, p: 1.0 + t + 0.0 * x
+    with pytest.raises(F.UnsupportedFormError):
+        api_problem(spec)
+    spec = readme_diffusion(10)
+    spec.flux = lambda x, y, t, a, b, g, p: (-a + 0.1 * g, -b)
+    spec.D = None
+    with pytest.raises(F.UnsupportedFormError):
+        api_problem(spec)
+
+
+def test_full_size_properties(gpu_lib):
+    """1000 x 1000 (1M vertices): RHS of a constant field vanishes on free rows; linearity;
+    operator path and triangle path agree."""
+    import fvmgpu as F
+
+    spec = sine_diffusion(1000)
+    prob = api_problem(spec)
+    n = spec.tri.num_points
+    one = np.ones(n)
+    du = np.zeros(n)
+    F.fvm_eqs(du, one, prob, 0.0)
+    code, _ = prob.export_codes()
+    free = code == 0
+    scale = np.max(np.abs(F.fvm_eqs(np.zeros(n), spec.u0.copy(), prob, 0.0)))
+    assert np.max(np.abs(du[free])) <= 1e-12 * scale * 1e3
+    rng = np.random.default_rng(12)
+    u, v = rng.random(n), rng.random(n)
+    a, b = 0.7, -1.3
+    fu = F.fvm_eqs(np.zeros(n), u, prob, 0.0)
+    fv = F.fvm_eqs(np.zeros(n), v, prob, 0.0)
+    fw = F.fvm_eqs(np.zeros(n), a * u + b * v, prob, 0.0)
+    e2, _ = rel_err(fw, a * fu + b * fv)
+    assert e2 <= 1e-12
+    ft = F.fvm_eqs(np.zeros(n), u, prob, 0.0, force_triangle=True)
+    e2, einf = rel_err(ft, fu)
+    assert e2 <= 1e-12 and einf <= 1e-12
