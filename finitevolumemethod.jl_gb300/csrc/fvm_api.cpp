@@ -307,12 +307,13 @@ static void rhs_outputs(fvm_problem* p, double* du, int32_t loc, cudaStream_t s)
 void problem_rhs_internal(fvm_problem* p, const double* u, double* du, bool force_triangle, cudaStream_t s) {
     fvm_mesh* m = p->mesh;
     if (p->linear && !force_triangle) {
+        const double* dg = p->has_d ? p->d_d.as<double>() : nullptr;
+        const double* b = p->has_b ? p->d_b.as<double>() : nullptr;
+        const double* q = p->has_q ? p->d_q.as<double>() : nullptr;
         if (p->precision == FVM_FP32)
-            launch_sell_apply32(m->pat, p->d_val32.as<float>(), u, du, p->d_rowscale.as<double>(),
-                                p->has_b ? p->d_b.as<double>() : nullptr, p->has_q ? p->d_q.as<double>() : nullptr, s);
+            launch_sell_diff32(m->pat_off, p->d_val32.as<float>(), u, du, p->d_rowscale.as<double>(), dg, b, q, s);
         else
-            launch_sell_apply64(m->pat, p->d_val64.as<double>(), u, du, nullptr,
-                                p->has_b ? p->d_b.as<double>() : nullptr, p->has_q ? p->d_q.as<double>() : nullptr, s);
+            launch_sell_diff64(m->pat_off, p->d_val64.as<double>(), u, du, nullptr, dg, b, q, s);
     } else {
         if (p->precision == FVM_FP32 && !p->linear)
             fail(FVM_ERR_UNSUPPORTED_FORM, "FP32 assembly is available for linear forms only");
@@ -466,6 +467,19 @@ int fvm_problem_create(fvm_mesh* mesh, const fvm_problem_desc* desc, fvm_problem
 int fvm_problem_destroy(fvm_problem* p) {
     return guard([&] {
         delete p;
+        return FVM_OK;
+    });
+}
+
+int fvm_problem_info(const fvm_problem* p, int64_t* info) {
+    return guard([&] {
+        if (!p || !info) fail(FVM_ERR_INVALID_ARGUMENT, "NULL argument");
+        info[0] = p->linear ? 1 : 0;
+        info[1] = p->op_nonzeros;
+        info[2] = p->mesh->pat.nslots;
+        info[3] = p->has_b ? 1 : 0;
+        info[4] = p->has_q ? 1 : 0;
+        info[5] = p->precision;
         return FVM_OK;
     });
 }

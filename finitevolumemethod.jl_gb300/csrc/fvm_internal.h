@@ -96,7 +96,8 @@ struct fvm_mesh {
     std::vector<double> vol;                    // [np] control-volume areas
     std::vector<double> props;                  // [24*nt] TriangleProperties
     std::vector<int32_t> perm, iperm;           // perm[internal] = caller, iperm[caller] = internal
-    fvm::SellPattern pat;                       // vertex-neighbour operator pattern (internal)
+    fvm::SellPattern pat;                       // vertex-neighbour pattern with the diagonal (templates)
+    fvm::SellPattern pat_off;                   // off-diagonal neighbours only (difference-form RHS)
     fvm::Tiles tiles;
     fvm::DBuf d_perm, d_iperm, d_invV;          // d_invV internal order
     int tile_vertices_req = 0;
@@ -111,9 +112,11 @@ struct fvm_problem {
     std::vector<int8_t> code;                   // [np] caller order
     std::vector<int8_t> bneu;                   // [nbe]
     std::vector<double> dualD, quarterD, quarterN, src, dudt, dirv;  // copies of the descriptor arrays
-    // linear operator path: du = rowscale * (A u) + b + q u^2
-    fvm::DBuf d_val64, d_val32, d_b, d_q, d_rowscale;
-    bool has_b = false, has_q = false;
+    // linear operator path (difference form on the off-diagonal pattern):
+    //   du_i = rowscale_i * sum_{j != i} K_ij (u_j - u_i) + d_i u_i + b_i + q_i u_i^2
+    fvm::DBuf d_val64, d_val32, d_b, d_q, d_d, d_rowscale;
+    bool has_b = false, has_q = false, has_d = false;
+    int64_t op_nonzeros = 0;
     // triangle path
     bool tri_ready = false;
     fvm::DBuf d_ec, d_bc;                       // element coefficients, boundary-element coefficients
@@ -148,6 +151,11 @@ void launch_sell_apply64(const SellPattern& p, const double* val, const double* 
                          const double* rowscale, const double* b, const double* q, cudaStream_t s);
 void launch_sell_apply32(const SellPattern& p, const float* val, const double* x, double* y,
                          const double* rowscale, const double* b, const double* q, cudaStream_t s);
+// y_i = rowscale_i * sum_j K_ij (x_j - x_i) + d_i x_i + b_i + q_i x_i^2 (any of rowscale, d, b, q may be null)
+void launch_sell_diff64(const SellPattern& p, const double* val, const double* x, double* y, const double* rowscale,
+                        const double* d, const double* b, const double* q, cudaStream_t s);
+void launch_sell_diff32(const SellPattern& p, const float* val, const double* x, double* y, const double* rowscale,
+                        const double* d, const double* b, const double* q, cudaStream_t s);
 void launch_permute_in(const int32_t* perm, const double* xref, double* xint, int64_t n, cudaStream_t s);
 void launch_permute_out(const int32_t* perm, const double* xint, double* xref, int64_t n, cudaStream_t s);
 void launch_dirichlet(const int32_t* idx, const double* val, double* u, int64_t n, cudaStream_t s);

@@ -67,6 +67,69 @@ void launch_sell_apply32(const SellPattern& p, const float* val, const double* x
 }
 
 // ---------------------------------------------------------------------------------------
+// Difference-form operator of the generic RHS:
+//   y_i = rowscale_i * sum_{j != i} K_ij (x_j - x_i) + d_i x_i + b_i + q_i x_i^2
+// Padding slots point at the row itself (x_i - x_i = 0).  The FP32 variant forms the
+// differences of FP32-rounded values and accumulates in FP32; the scaling and the
+// remaining terms are FP64.
+// ---------------------------------------------------------------------------------------
+template <class V, class Acc>
+__global__ void __launch_bounds__(256) sell_diff_kernel(const int64_t* __restrict__ slice_ptr,
+                                                        const int32_t* __restrict__ width,
+                                                        const int32_t* __restrict__ col,
+                                                        const V* __restrict__ val, const double* __restrict__ x,
+                                                        double* __restrict__ y, const double* __restrict__ rowscale,
+                                                        const double* __restrict__ d, const double* __restrict__ b,
+                                                        const double* __restrict__ q, int64_t nrows,
+                                                        int64_t nslices) {
+    int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t s = gt >> 5;
+    int lane = threadIdx.x & 31;
+    if (s >= nslices) return;
+    int64_t r = s * kSlice + lane;
+    int64_t base = __ldg(&slice_ptr[s]) + lane;
+    int w = __ldg(&width[s]);
+    const double xr = __ldg(&x[r < nrows ? r : nrows - 1]);
+    const Acc xa = (Acc)xr;
+    Acc acc0 = 0, acc1 = 0;
+    int k = 0;
+    for (; k + 1 < w; k += 2) {
+        int64_t i0 = base + (int64_t)k * kSlice, i1 = i0 + kSlice;
+        int32_t c0 = __ldg(&col[i0]), c1 = __ldg(&col[i1]);
+        V v0 = __ldg(&val[i0]), v1 = __ldg(&val[i1]);
+        acc0 += (Acc)v0 * ((Acc)__ldg(&x[c0]) - xa);
+        acc1 += (Acc)v1 * ((Acc)__ldg(&x[c1]) - xa);
+    }
+    if (k < w) {
+        int64_t i0 = base + (int64_t)k * kSlice;
+        acc0 += (Acc)__ldg(&val[i0]) * ((Acc)__ldg(&x[__ldg(&col[i0])]) - xa);
+    }
+    if (r >= nrows) return;
+    double out = (double)(acc0 + acc1);
+    if (rowscale) out *= rowscale[r];
+    if (d) out += d[r] * xr;
+    if (b) out += b[r];
+    if (q) out += q[r] * xr * xr;
+    y[r] = out;
+}
+
+void launch_sell_diff64(const SellPattern& p, const double* val, const double* x, double* y, const double* rowscale,
+                        const double* d, const double* b, const double* q, cudaStream_t s) {
+    if (p.nslices == 0) return;
+    sell_diff_kernel<double, double><<<grid_for(p.nslices * 32, 256), 256, 0, s>>>(
+        p.d_slice_ptr.as<int64_t>(), p.d_width.as<int32_t>(), p.d_col.as<int32_t>(), val, x, y, rowscale, d, b, q,
+        p.nrows, p.nslices);
+}
+
+void launch_sell_diff32(const SellPattern& p, const float* val, const double* x, double* y, const double* rowscale,
+                        const double* d, const double* b, const double* q, cudaStream_t s) {
+    if (p.nslices == 0) return;
+    sell_diff_kernel<float, float><<<grid_for(p.nslices * 32, 256), 256, 0, s>>>(
+        p.d_slice_ptr.as<int64_t>(), p.d_width.as<int32_t>(), p.d_col.as<int32_t>(), val, x, y, rowscale, d, b, q,
+        p.nrows, p.nslices);
+}
+
+// ---------------------------------------------------------------------------------------
 // Permutation between the caller's numbering and the internal (Hilbert) numbering.
 // ---------------------------------------------------------------------------------------
 __global__ void permute_in_kernel(const int32_t* __restrict__ perm, const double* __restrict__ xref,

@@ -89,6 +89,43 @@ static void triangle_geometry(const double* P, int32_t i, int32_t j, int32_t k, 
 
 static inline uint64_t edge_key(int64_t a, int64_t b) { return ((uint64_t)(uint32_t)a << 32) | (uint32_t)b; }
 
+// Sliced ELL from the CSR view (rowptr, csr_col): slices of 32 rows, width = longest row in the
+// slice, slots column-major; padding slots point at the row itself with value 0.
+static void finalize_sell(SellPattern& pat, int64_t nrows) {
+    pat.nnz = (int64_t)pat.csr_col.size();
+    pat.nslices = (nrows + kSlice - 1) / kSlice;
+    pat.slice_ptr.assign(pat.nslices + 1, 0);
+    pat.width.assign(pat.nslices, 0);
+    for (int64_t s = 0; s < pat.nslices; ++s) {
+        int32_t w = 0;
+        for (int64_t r = s * kSlice; r < std::min<int64_t>(nrows, (s + 1) * kSlice); ++r)
+            w = std::max<int32_t>(w, (int32_t)(pat.rowptr[r + 1] - pat.rowptr[r]));
+        pat.width[s] = w;
+        pat.slice_ptr[s + 1] = pat.slice_ptr[s] + (int64_t)w * kSlice;
+    }
+    pat.nslots = pat.slice_ptr[pat.nslices];
+    pat.col.assign(pat.nslots, 0);
+    pat.csr_slot.assign(pat.nnz, 0);
+    for (int64_t s = 0; s < pat.nslices; ++s)
+        for (int lane = 0; lane < kSlice; ++lane) {
+            int64_t r = s * kSlice + lane;
+            int64_t len = r < nrows ? pat.rowptr[r + 1] - pat.rowptr[r] : 0;
+            int32_t pad = r < nrows ? (int32_t)r : (int32_t)(nrows - 1);
+            for (int32_t q = 0; q < pat.width[s]; ++q) {
+                int64_t slot = pat.slice_ptr[s] + (int64_t)q * kSlice + lane;
+                if (q < len) {
+                    pat.col[slot] = pat.csr_col[pat.rowptr[r] + q];
+                    pat.csr_slot[pat.rowptr[r] + q] = slot;
+                } else {
+                    pat.col[slot] = pad;
+                }
+            }
+        }
+    pat.d_slice_ptr.upload(pat.slice_ptr);
+    pat.d_width.upload(pat.width);
+    pat.d_col.upload(pat.col);
+}
+
 extern "C" int fvm_mesh_create_impl(const double* points, int64_t npoints, const int32_t* triangles, int64_t ntri,
                                      const int32_t* boundary_edges, const int32_t* boundary_adjacent,
                                      int64_t nbedge, int32_t tile_vertices, int32_t flags, fvm_mesh** out) {
@@ -224,38 +261,18 @@ extern "C" int fvm_mesh_create_impl(const double* points, int64_t npoints, const
                 }
             pat.rowptr[v + 1] = (int64_t)pat.csr_col.size();
         }
-        pat.nnz = (int64_t)pat.csr_col.size();
-        pat.nslices = (npoints + kSlice - 1) / kSlice;
-        pat.slice_ptr.assign(pat.nslices + 1, 0);
-        pat.width.assign(pat.nslices, 0);
-        for (int64_t s = 0; s < pat.nslices; ++s) {
-            int32_t w = 0;
-            for (int64_t r = s * kSlice; r < std::min<int64_t>(npoints, (s + 1) * kSlice); ++r)
-                w = std::max<int32_t>(w, (int32_t)(pat.rowptr[r + 1] - pat.rowptr[r]));
-            pat.width[s] = w;
-            pat.slice_ptr[s + 1] = pat.slice_ptr[s] + (int64_t)w * kSlice;
+        finalize_sell(pat, npoints);
+        // the same neighbourhoods without the diagonal
+        SellPattern& off = m->pat_off;
+        off.nrows = npoints;
+        off.rowptr.assign(npoints + 1, 0);
+        off.csr_col.reserve(pat.nnz);
+        for (int64_t v = 0; v < npoints; ++v) {
+            for (int64_t q = pat.rowptr[v]; q < pat.rowptr[v + 1]; ++q)
+                if (pat.csr_col[q] != v) off.csr_col.push_back(pat.csr_col[q]);
+            off.rowptr[v + 1] = (int64_t)off.csr_col.size();
         }
-        pat.nslots = pat.slice_ptr[pat.nslices];
-        pat.col.assign(pat.nslots, 0);
-        pat.csr_slot.assign(pat.nnz, 0);
-        for (int64_t s = 0; s < pat.nslices; ++s)
-            for (int lane = 0; lane < kSlice; ++lane) {
-                int64_t r = s * kSlice + lane;
-                int64_t len = r < npoints ? pat.rowptr[r + 1] - pat.rowptr[r] : 0;
-                int32_t pad = r < npoints ? (int32_t)r : (int32_t)(npoints - 1);
-                for (int32_t q = 0; q < pat.width[s]; ++q) {
-                    int64_t slot = pat.slice_ptr[s] + (int64_t)q * kSlice + lane;
-                    if (q < len) {
-                        pat.col[slot] = pat.csr_col[pat.rowptr[r] + q];
-                        pat.csr_slot[pat.rowptr[r] + q] = slot;
-                    } else {
-                        pat.col[slot] = pad;
-                    }
-                }
-            }
-        pat.d_slice_ptr.upload(pat.slice_ptr);
-        pat.d_width.upload(pat.width);
-        pat.d_col.upload(pat.col);
+        finalize_sell(off, npoints);
     }
 
     // device-side vertex data

@@ -24,18 +24,29 @@ void fvm_problem::ensure_work() {
 //   triangle dual edge e of T = (a, b, c): Q_e = -D_e l_e (alpha n_x + beta n_y)
 //   boundary half edge (non-Neumann):      Q_h = -D_h l_h (alpha n_x + beta n_y)
 //   boundary half edge (Neumann, a = n0 + n1 u(m)): Q_h = l_h (n0 + n1 u(m)).
-static void assemble_generic(fvm_problem* p, std::vector<double>& A, std::vector<double>& b,
-                             std::vector<double>& q, std::vector<double>& rowscale) {
+// Stored in difference form on the off-diagonal pattern:
+//   du_i = sum_{j != i} K_ij (u_j - u_i) + d_i u_i + b_i + q_i u_i^2.
+// A dual-edge flux is a combination of u with coefficients summing to zero (constant u carries
+// no flux), so its diagonal coefficient is implied and dropped: constant fields give exactly
+// zero flux, as in the reference's alpha = s1 u_i + s2 u_j + s3 u_k.  Non-flux terms
+// (Neumann u(m) dependence, source, Dudt) keep their full row sum in d_i.
+static void assemble_generic(fvm_problem* p, std::vector<double>& A, std::vector<double>& dg,
+                             std::vector<double>& b, std::vector<double>& q, std::vector<double>& rowscale) {
     const fvm_mesh* m = p->mesh;
-    const SellPattern& pat = m->pat;
+    const SellPattern& pat = m->pat_off;
     A.assign(pat.nslots, 0.0);
+    dg.assign(m->np, 0.0);
     b.assign(m->np, 0.0);
     q.assign(m->np, 0.0);
     rowscale.assign(m->np, 0.0);
-    auto add = [&](int32_t r, int32_t c, double v) {
-        int64_t s = pat.find(m->iperm[r], m->iperm[c]);
-        A[s] += v;
+    auto flux = [&](int32_t r, int32_t c, double v) {
+        if (r != c) A[pat.find(m->iperm[r], m->iperm[c])] += v;
     };
+    auto lin = [&](int32_t r, int32_t c, double v) {
+        if (r != c) A[pat.find(m->iperm[r], m->iperm[c])] += v;
+        dg[m->iperm[r]] += v;
+    };
+    auto add = flux;
     const int nd = p->dif_deg + 1;
     for (int64_t t = 0; t < m->nt; ++t) {
         const int32_t* w = &m->tri[3 * t];
@@ -70,15 +81,15 @@ static void assemble_generic(fvm_problem* p, std::vector<double>& A, std::vector
             if (fi) {
                 b[m->iperm[i]] -= lh * n0i / m->vol[i];
                 if (n1i != 0) {
-                    add(i, i, -lh * n1i * 0.75 / m->vol[i]);
-                    add(i, j, -lh * n1i * 0.25 / m->vol[i]);
+                    lin(i, i, -lh * n1i * 0.75 / m->vol[i]);
+                    lin(i, j, -lh * n1i * 0.25 / m->vol[i]);
                 }
             }
             if (fj) {
                 b[m->iperm[j]] -= lh * n0j / m->vol[j];
                 if (n1j != 0) {
-                    add(j, i, -lh * n1j * 0.25 / m->vol[j]);
-                    add(j, j, -lh * n1j * 0.75 / m->vol[j]);
+                    lin(j, i, -lh * n1j * 0.25 / m->vol[j]);
+                    lin(j, j, -lh * n1j * 0.75 / m->vol[j]);
                 }
             }
             continue;
@@ -102,14 +113,14 @@ static void assemble_generic(fvm_problem* p, std::vector<double>& A, std::vector
             rowscale[r] = 1.0 / m->vol[v];
             if (!p->src.empty()) {
                 b[r] += p->src[v * ns];
-                if (ns > 1 && p->src[v * ns + 1] != 0) add((int32_t)v, (int32_t)v, p->src[v * ns + 1]);
+                if (ns > 1) dg[r] += p->src[v * ns + 1];
                 if (ns > 2) q[r] = p->src[v * ns + 2];
             }
         } else if (c == FVM_VERTEX_DUDT) {
             rowscale[r] = 1.0;
             if (!p->dudt.empty()) {
                 b[r] = p->dudt[v * nu];
-                if (nu > 1 && p->dudt[v * nu + 1] != 0) add((int32_t)v, (int32_t)v, p->dudt[v * nu + 1]);
+                if (nu > 1) dg[r] += p->dudt[v * nu + 1];
                 if (nu > 2) q[r] = p->dudt[v * nu + 2];
             }
         }
@@ -185,16 +196,20 @@ extern "C" int fvm_problem_create_impl(fvm_mesh* mesh, const fvm_problem_desc* d
         p->d_dir_val.upload(val);
     }
     if (p->linear) {
-        std::vector<double> A, b, q, rs;
-        assemble_generic(p.get(), A, b, q, rs);
+        std::vector<double> A, dg, b, q, rs;
+        assemble_generic(p.get(), A, dg, b, q, rs);
         p->d_val64.upload(A);
-        p->has_b = std::any_of(b.begin(), b.end(), [](double x) { return x != 0; });
-        p->has_q = std::any_of(q.begin(), q.end(), [](double x) { return x != 0; });
+        auto nz = [](double x) { return x != 0; };
+        p->op_nonzeros = std::count_if(A.begin(), A.end(), nz);
+        p->has_b = std::any_of(b.begin(), b.end(), nz);
+        p->has_q = std::any_of(q.begin(), q.end(), nz);
+        p->has_d = std::any_of(dg.begin(), dg.end(), nz);
         if (p->has_b) p->d_b.upload(b);
         if (p->has_q) p->d_q.upload(q);
+        if (p->has_d) p->d_d.upload(dg);
         if (p->precision == FVM_FP32) {
             std::vector<float> A32(A.size(), 0.0f);
-            const SellPattern& pat = m->pat;
+            const SellPattern& pat = m->pat_off;
             for (int64_t s = 0; s < pat.nslices; ++s)
                 for (int lane = 0; lane < kSlice; ++lane) {
                     int64_t r = s * kSlice + lane;

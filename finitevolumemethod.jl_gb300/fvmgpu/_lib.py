@@ -120,6 +120,7 @@ SIGNATURES = {
     "fvm_mesh_export_connectivity": (C.c_int, [C.c_void_p, c_int32_p, c_int32_p]),
     "fvm_problem_create": (C.c_int, [C.c_void_p, C.POINTER(ProblemDesc), C.POINTER(C.c_void_p)]),
     "fvm_problem_destroy": (C.c_int, [C.c_void_p]),
+    "fvm_problem_info": (C.c_int, [C.c_void_p, c_int64_p]),
     "fvm_problem_export_codes": (C.c_int, [C.c_void_p, c_int8_p, c_int8_p]),
     "fvm_rhs": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int32, C.c_void_p]),
     "fvm_dirichlet_apply": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_int32, C.c_void_p]),

@@ -444,6 +444,12 @@ class FVMProblem:
     def handle(self):
         return self._h
 
+    def info(self) -> Dict[str, int]:
+        a = np.zeros(6, dtype=np.int64)
+        check(load().fvm_problem_info(self._h, dptr(a, _lib.c_int64_p)))
+        keys = ["linear", "operator_nonzeros", "operator_slots", "has_constant", "has_quadratic", "precision"]
+        return dict(zip(keys, (int(v) for v in a)))
+
     def export_codes(self):
         tri = self.mesh.triangulation
         code = np.empty(tri.num_points, dtype=np.int8)
@@ -470,10 +476,12 @@ def _prob_of(p):
     return getattr(p, "prob")
 
 
-def fvm_eqs(du, u, p, t, *, force_triangle=False, stream=None):
+def fvm_eqs(du, u, p, t, *, force_triangle=False, internal=False, stream=None):
     """fvm_eqs!(du, u, p, t) (src/equations/main_equations.jl:28-81).  `p` is the problem or
     any object / dict with a `prob` entry.  du, u: float64 numpy arrays (host) or CUDA torch
-    tensors (device), caller numbering.  Returns du."""
+    tensors (device), caller numbering; internal=True takes device tensors already in the
+    library's internal (Hilbert) numbering, as a device-resident time loop holds them.
+    Returns du."""
     prob = _prob_of(p)
     if isinstance(prob, _Template):
         return prob.apply(du, u, stream=stream)
@@ -481,6 +489,10 @@ def fvm_eqs(du, u, p, t, *, force_triangle=False, stream=None):
     dp, dl = _lib.array_pointer(du)
     if ul != dl:
         raise TypeError("u and du must both be host arrays or both device tensors")
+    if internal:
+        if ul != _lib.FVM_PTR_DEVICE:
+            raise TypeError("internal=True needs device tensors")
+        ul = _lib.FVM_PTR_DEVICE_INTERNAL
     flags = ul | (_lib.FVM_RHS_FORCE_TRIANGLE if force_triangle else 0)
     s = stream if stream is not None else _lib.current_stream_handle()
     check(load().fvm_rhs(prob.handle, up, dp, float(t), flags, s))
@@ -591,12 +603,17 @@ class _Template:
             self._export()
         return self._b
 
-    def apply(self, du, u, precision="fp64", stream=None):
-        """du = A u + b: the MatrixOperator product."""
+    def apply(self, du, u, precision="fp64", internal=False, stream=None):
+        """du = A u + b: the MatrixOperator product (internal=True: device tensors in the
+        library's internal numbering)."""
         up, ul = _lib.array_pointer(u)
         dp, dl = _lib.array_pointer(du)
         if ul != dl:
             raise TypeError("u and du must both be host arrays or both device tensors")
+        if internal:
+            if ul != _lib.FVM_PTR_DEVICE:
+                raise TypeError("internal=True needs device tensors")
+            ul = _lib.FVM_PTR_DEVICE_INTERNAL
         s = stream if stream is not None else _lib.current_stream_handle()
         check(load().fvm_template_apply(self._ht, up, dp, _precision(precision), ul, s))
         return du

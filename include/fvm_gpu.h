@@ -127,6 +127,9 @@ typedef struct fvm_problem_desc {
  * Conditions(mesh, BCs, ICs) (src/conditions.jl:546-552). */
 int fvm_problem_create(fvm_mesh* mesh, const fvm_problem_desc* desc, fvm_problem** out);
 int fvm_problem_destroy(fvm_problem* prob);
+/* info[0..5] = linear (1 when the folded vertex-neighbour operator evaluates fvm_eqs!),
+ * operator nonzeros, operator slots (padded), has constant term, has u^2 term, precision. */
+int fvm_problem_info(const fvm_problem* prob, int64_t* info);
 /* Reads the device-resident classification back in the caller's numbering. */
 int fvm_problem_export_codes(const fvm_problem* prob, int8_t* vertex_code, int8_t* bedge_neumann);
 

@@ -1,0 +1,103 @@
+"""Build recipe of the oracle's C restatement (TEST / BASELINE INFRASTRUCTURE).
+
+Compiles oracle/fvm_oracle_c.c into oracle/build/liborc.so with gcc -O3 -fopenmp, and wraps
+it with ctypes for the tests and bench.py's CPU-baseline leg.  The reference itself is pure
+Julia (no C/C++ sources), so there is nothing of the reference to compile here.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+SRC = HERE / "fvm_oracle_c.c"
+LIB = HERE / "build" / "liborc.so"
+
+D_CONST, D_SINE, D_JUMP = 0, 1, 2
+
+
+class OrcProblem(C.Structure):
+    _fields_ = [
+        ("np", C.c_int64), ("nt", C.c_int64), ("nbe", C.c_int64),
+        ("tri", C.POINTER(C.c_int32)), ("props", C.POINTER(C.c_double)), ("pts", C.POINTER(C.c_double)),
+        ("vol", C.POINTER(C.c_double)), ("bedge", C.POINTER(C.c_int32)), ("code", C.POINTER(C.c_int8)),
+        ("d_kind", C.c_int), ("d_param", C.c_double * 4),
+    ]
+
+
+def build(force: bool = False) -> Path:
+    LIB.parent.mkdir(parents=True, exist_ok=True)
+    if force or not LIB.exists() or LIB.stat().st_mtime < SRC.stat().st_mtime:
+        cmd = ["gcc", "-O3", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", str(SRC), "-o", str(LIB) + ".tmp",
+               "-lm"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode:
+            raise RuntimeError(f"oracle build failed: {r.stderr}")
+        Path(str(LIB) + ".tmp").replace(LIB)
+    return LIB
+
+
+_lib = None
+
+
+def load():
+    global _lib
+    if _lib is None:
+        build()
+        lib = C.CDLL(str(LIB))
+        lib.orc_rhs_serial.argtypes = [C.POINTER(OrcProblem), C.c_void_p, C.c_void_p, C.c_double]
+        lib.orc_rhs_threaded.argtypes = [C.POINTER(OrcProblem), C.c_void_p, C.c_void_p, C.c_double, C.c_int,
+                                         C.c_void_p]
+        lib.orc_max_threads.restype = C.c_int
+        _lib = lib
+    return _lib
+
+
+class CProblem:
+    """The C restatement's problem for a diffusion FVMProblem with a built-in D closure and
+    Dirichlet / free vertex codes (the benchmark configurations)."""
+
+    def __init__(self, geo, tri, code, d_kind, d_param, bnd_tri):
+        self.keep = [np.ascontiguousarray(tri.triangles, dtype=np.int32),
+                     np.ascontiguousarray(np.concatenate([geo.s, geo.mid.reshape(-1, 6), geo.nrm.reshape(-1, 6),
+                                                          geo.length], axis=1)),
+                     np.ascontiguousarray(tri.points, dtype=np.float64),
+                     np.ascontiguousarray(geo.cv_volumes),
+                     np.ascontiguousarray(np.concatenate([tri.boundary_edges, bnd_tri.reshape(-1, 1)], axis=1),
+                                          dtype=np.int32),
+                     np.ascontiguousarray(code, dtype=np.int8)]
+        p = OrcProblem()
+        p.np, p.nt, p.nbe = tri.num_points, tri.num_triangles, tri.num_boundary_edges
+        p.tri = self.keep[0].ctypes.data_as(C.POINTER(C.c_int32))
+        p.props = self.keep[1].ctypes.data_as(C.POINTER(C.c_double))
+        p.pts = self.keep[2].ctypes.data_as(C.POINTER(C.c_double))
+        p.vol = self.keep[3].ctypes.data_as(C.POINTER(C.c_double))
+        p.bedge = self.keep[4].ctypes.data_as(C.POINTER(C.c_int32))
+        p.code = self.keep[5].ctypes.data_as(C.POINTER(C.c_int8))
+        p.d_kind = d_kind
+        for i, v in enumerate(d_param[:4]):
+            p.d_param[i] = v
+        self.p = p
+        self.np = tri.num_points
+        self._dup = None
+
+    def rhs_serial(self, u, t=0.0):
+        du = np.empty(self.np)
+        load().orc_rhs_serial(C.byref(self.p), u.ctypes.data, du.ctypes.data, t)
+        return du
+
+    def rhs_threaded(self, u, t=0.0, nthreads=0, du=None):
+        lib = load()
+        nth = nthreads or lib.orc_max_threads()
+        if self._dup is None or self._dup.size < self.np * nth:
+            self._dup = np.empty(self.np * nth)
+        du = np.empty(self.np) if du is None else du
+        lib.orc_rhs_threaded(C.byref(self.p), u.ctypes.data, du.ctypes.data, t, nth, self._dup.ctypes.data)
+        return du
+
+
+def max_threads() -> int:
+    return load().orc_max_threads()

@@ -1,0 +1,154 @@
+/*
+ * C restatement of the reference's CPU fvm_eqs! (TEST / BASELINE INFRASTRUCTURE).
+ *
+ * Only the tests and the CPU-baseline leg of bench.py load this file's library.  It follows
+ * FiniteVolumeMethod.jl 1.2.3 (paths relative to the reference project root):
+ *   serial_fvm_eqs!    src/equations/main_equations.jl:38-44
+ *   parallel_fvm_eqs!  src/equations/main_equations.jl:47-81 (per-thread duplicated du, then
+ *                      combine_duplicated_du!)
+ *   triangle fluxes    src/equations/triangle_contributions.jl:2-15,28-35;
+ *                      individual_flux_contributions.jl:2-6,27-33; shape_functions.jl:2-9;
+ *                      construct_flux_function src/problem.jl:425-440
+ *   boundary edges     src/equations/boundary_edge_contributions.jl:2-13,41-48,61-65,77-86;
+ *                      control_volumes.jl:41-56
+ *   sources            src/equations/source_contributions.jl:2-14,33-47
+ * Geometry (TriangleProperties, 24 doubles per triangle) comes in precomputed as
+ * FVMGeometry stores it (src/geometry.jl:99-169).  The diffusion closure is evaluated at
+ * every dual edge on every call, as the reference's flux closure is.  Unlike the reference,
+ * triangles are visited by index rather than through Dict lookups, so this restatement is
+ * faster than the Julia original.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* closures of the benchmark configurations: D(x, y, t, u, p) */
+enum { ORC_D_CONST = 0, ORC_D_SINE = 1, ORC_D_JUMP = 2 };
+
+static inline double closure_D(int kind, const double* p, double x, double y, double t, double u) {
+    (void)t;
+    (void)u;
+    switch (kind) {
+        case ORC_D_SINE: return 1.0 + p[0] * sin(2.0 * M_PI * x) * sin(2.0 * M_PI * y);
+        case ORC_D_JUMP: return (x * x + y * y < 0.25) ? p[0] : p[1];
+        default: return p[0];
+    }
+}
+
+typedef struct {
+    int64_t np, nt, nbe;
+    const int32_t* tri;     /* [3*nt] */
+    const double* props;    /* [24*nt] s1..s9, mid(3x2), nrm(3x2), len(3) */
+    const double* pts;      /* [2*np] */
+    const double* vol;      /* [np] */
+    const int32_t* bedge;   /* [3*nbe] i, j, stored triangle index */
+    const int8_t* code;     /* [np] 0 free, 1 Dirichlet, 2 Dudt (value 0 here), 3 not a vertex */
+    int d_kind;
+    double d_param[4];
+} orc_problem;
+
+static inline void triangle_update(const orc_problem* P, int64_t t, const double* u, double* du, double tt) {
+    const int32_t* T = P->tri + 3 * t;
+    const double* pr = P->props + 24 * t;
+    int32_t i = T[0], j = T[1], k = T[2];
+    double ui = u[i], uj = u[j], uk = u[k];
+    double a = pr[0] * ui + pr[1] * uj + pr[2] * uk;
+    double b = pr[3] * ui + pr[4] * uj + pr[5] * uk;
+    double g = pr[6] * ui + pr[7] * uj + pr[8] * uk;
+    double Q[3];
+    for (int e = 0; e < 3; ++e) {
+        double x = pr[9 + 2 * e], y = pr[10 + 2 * e];
+        double uu = a * x + b * y + g;
+        double D = closure_D(P->d_kind, P->d_param, x, y, tt, uu);
+        double qx = -D * a, qy = -D * b;
+        double qn = qx * pr[15 + 2 * e] + qy * pr[16 + 2 * e];
+        Q[e] = qn * pr[21 + e];
+    }
+    du[i] = du[i] + Q[2] - Q[0];
+    du[j] = du[j] + Q[0] - Q[1];
+    du[k] = du[k] + Q[1] - Q[2];
+}
+
+static inline void bedge_update(const orc_problem* P, int64_t e, const double* u, double* du, double tt) {
+    int32_t i = P->bedge[3 * e], j = P->bedge[3 * e + 1], t = P->bedge[3 * e + 2];
+    const int32_t* T = P->tri + 3 * (int64_t)t;
+    const double* pr = P->props + 24 * (int64_t)t;
+    double u0 = u[T[0]], u1 = u[T[1]], u2 = u[T[2]];
+    double a = pr[0] * u0 + pr[1] * u1 + pr[2] * u2;
+    double b = pr[3] * u0 + pr[4] * u1 + pr[5] * u2;
+    double g = pr[6] * u0 + pr[7] * u1 + pr[8] * u2;
+    double px = P->pts[2 * i], py = P->pts[2 * i + 1], qx = P->pts[2 * j], qy = P->pts[2 * j + 1];
+    double lij = sqrt((qx - px) * (qx - px) + (qy - py) * (qy - py));
+    double nx = (qy - py) / lij, ny = -(qx - px) / lij;
+    double mijx = (px + qx) / 2, mijy = (py + qy) / 2;
+    double mix = (px + mijx) / 2, miy = (py + mijy) / 2;
+    double mjx = (qx + mijx) / 2, mjy = (qy + mijy) / 2;
+    double l = sqrt((mijx - px) * (mijx - px) + (mijy - py) * (mijy - py));
+    double Di = closure_D(P->d_kind, P->d_param, mix, miy, tt, a * mix + b * miy + g);
+    double Dj = closure_D(P->d_kind, P->d_param, mjx, mjy, tt, a * mjx + b * mjy + g);
+    double q1 = (-Di * a * nx + -Di * b * ny) * l;
+    double q2 = (-Dj * a * nx + -Dj * b * ny) * l;
+    du[i] = du[i] - q1;
+    du[j] = du[j] - q2;
+}
+
+static inline void source_update(const orc_problem* P, int64_t i, double* du) {
+    int c = P->code[i];
+    if (c == 0)
+        du[i] = du[i] / P->vol[i];
+    else
+        du[i] = 0.0;
+}
+
+void orc_rhs_serial(const orc_problem* P, const double* u, double* du, double t) {
+    memset(du, 0, sizeof(double) * P->np);
+    for (int64_t q = 0; q < P->nt; ++q) triangle_update(P, q, u, du, t);
+    for (int64_t e = 0; e < P->nbe; ++e) bedge_update(P, e, u, du, t);
+    for (int64_t i = 0; i < P->np; ++i) source_update(P, i, du);
+}
+
+/* parallel_fvm_eqs!: chunk c accumulates into column c of dup (np x nthreads), then the
+ * columns are summed into du and the per-vertex sources run in parallel. */
+void orc_rhs_threaded(const orc_problem* P, const double* u, double* du, double t, int nthreads, double* dup) {
+#ifdef _OPENMP
+    if (nthreads <= 0) nthreads = omp_get_max_threads();
+#else
+    nthreads = 1;
+#endif
+    const int64_t np = P->np;
+    memset(du, 0, sizeof(double) * np);
+#pragma omp parallel num_threads(nthreads)
+    {
+#ifdef _OPENMP
+        int c = omp_get_thread_num();
+        int nth = omp_get_num_threads();
+#else
+        int c = 0, nth = 1;
+#endif
+        double* col = dup + (int64_t)c * np;
+        memset(col, 0, sizeof(double) * np);
+        int64_t t0 = P->nt * c / nth, t1 = P->nt * (c + 1) / nth;
+        for (int64_t q = t0; q < t1; ++q) triangle_update(P, q, u, col, t);
+        int64_t e0 = P->nbe * c / nth, e1 = P->nbe * (c + 1) / nth;
+        for (int64_t e = e0; e < e1; ++e) bedge_update(P, e, u, col, t);
+#pragma omp barrier
+        int64_t v0 = np * c / nth, v1 = np * (c + 1) / nth;
+        for (int w = 0; w < nth; ++w) {
+            const double* cw = dup + (int64_t)w * np;
+            for (int64_t i = v0; i < v1; ++i) du[i] += cw[i];
+        }
+        for (int64_t i = v0; i < v1; ++i) source_update(P, i, du);
+    }
+}
+
+int orc_max_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
