@@ -59,6 +59,7 @@ constexpr int kSlice = 32;
 
 struct SellPattern {
     int64_t nrows = 0, nslices = 0, nslots = 0, nnz = 0;
+    int maxw = 0;                    // widest slice
     std::vector<int64_t> slice_ptr;  // [nslices+1] slot offsets (multiples of 32)
     std::vector<int32_t> width;      // [nslices]
     std::vector<int32_t> col;        // [nslots] internal column (pad: the row itself)

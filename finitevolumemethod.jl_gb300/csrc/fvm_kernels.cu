@@ -1,132 +1,82 @@
 // Device kernels of libfvmgpu (sm_103a).  Every kernel here is HBM- or FP64-issue-bound
 // gather/scatter/stream work; none is a dense contraction, so no tensor-core path exists.
 #include "fvm_internal.h"
+#include "fvm_sell.cuh"
 
 namespace fvm {
 
+static inline unsigned grid_for(int64_t threads, int block) { return (unsigned)((threads + block - 1) / block); }
+
 // ---------------------------------------------------------------------------------------
-// Sliced-ELL operator: y = rowscale .* (A x) + b + q .* x.^2
-// One warp per 32-row slice, one lane per row, slots column-major so each slot step of a
-// warp reads 32 consecutive values and columns (fully coalesced).  x gathers hit L2.
+// Sliced-ELL operators (one warp per 32-row slice; see fvm_sell.cuh).
+//   explicit (templates, A u + b):  y_i = rowscale_i * sum_j A_ij x_j + b_i + q_i x_i^2
+//   difference form (generic RHS):  y_i = rowscale_i * sum_{j != i} K_ij (x_j - x_i)
+//                                         + d_i x_i + b_i + q_i x_i^2
+// In the difference form padding slots point at the row itself (x_i - x_i = 0).  FP32
+// variants round x to FP32, accumulate in FP32 and apply rowscale, d, b, q in FP64.
 // ---------------------------------------------------------------------------------------
-template <class V, class Acc>
-__global__ void __launch_bounds__(256) sell_apply_kernel(const int64_t* __restrict__ slice_ptr,
-                                                         const int32_t* __restrict__ width,
-                                                         const int32_t* __restrict__ col,
-                                                         const V* __restrict__ val, const double* __restrict__ x,
-                                                         double* __restrict__ y, const double* __restrict__ rowscale,
-                                                         const double* __restrict__ b, const double* __restrict__ q,
-                                                         int64_t nrows, int64_t nslices) {
-    int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    int64_t s = gt >> 5;
-    int lane = threadIdx.x & 31;
-    if (s >= nslices) return;
-    int64_t base = __ldg(&slice_ptr[s]) + lane;
-    int w = __ldg(&width[s]);
-    Acc acc0 = 0, acc1 = 0;
-    int k = 0;
-    for (; k + 1 < w; k += 2) {
-        int64_t i0 = base + (int64_t)k * kSlice, i1 = i0 + kSlice;
-        int32_t c0 = __ldg(&col[i0]), c1 = __ldg(&col[i1]);
-        V v0 = __ldg(&val[i0]), v1 = __ldg(&val[i1]);
-        acc0 += (Acc)v0 * (Acc)__ldg(&x[c0]);
-        acc1 += (Acc)v1 * (Acc)__ldg(&x[c1]);
-    }
-    if (k < w) {
-        int64_t i0 = base + (int64_t)k * kSlice;
-        acc0 += (Acc)__ldg(&val[i0]) * (Acc)__ldg(&x[__ldg(&col[i0])]);
-    }
-    int64_t r = s * kSlice + lane;
-    if (r >= nrows) return;
-    double out = (double)(acc0 + acc1);
-    if (rowscale) out *= rowscale[r];
-    if (b) out += b[r];
-    if (q) {
-        double xr = x[r];
-        out += q[r] * xr * xr;
-    }
-    y[r] = out;
+struct SellArgs {
+    const int64_t* slice_ptr;
+    const int32_t* width;
+    const int32_t* col;
+    const void* val;
+    const double* x;
+    double* y;
+    const double* rowscale;
+    const double* d;
+    const double* b;
+    const double* q;
+    int64_t nrows, nslices;
+};
+
+template <class V, class Acc, bool DIFF, int MAXW>
+__global__ void __launch_bounds__(256) sell_kernel(SellArgs a) {
+    const int64_t s = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (s >= a.nslices) return;
+    const int64_t r = s * kSlice + lane;
+    const double xr = __ldg(&a.x[r < a.nrows ? r : a.nrows - 1]);
+    Acc acc = sell_row_product<V, Acc, double, DIFF, MAXW>(a.slice_ptr, a.width, a.col, (const V*)a.val, a.x, (Acc)xr,
+                                                           s, lane);
+    if (r >= a.nrows) return;
+    double out = (double)acc;
+    if (a.rowscale) out *= a.rowscale[r];
+    if (a.d) out += a.d[r] * xr;
+    if (a.b) out += a.b[r];
+    if (a.q) out += a.q[r] * xr * xr;
+    a.y[r] = out;
 }
 
-static inline unsigned grid_for(int64_t threads, int block) { return (unsigned)((threads + block - 1) / block); }
+template <class V, class Acc, bool DIFF>
+static void launch_sell(const SellPattern& p, const V* val, const double* x, double* y, const double* rowscale,
+                        const double* d, const double* b, const double* q, cudaStream_t s) {
+    if (p.nslices == 0) return;
+    SellArgs a{p.d_slice_ptr.as<int64_t>(), p.d_width.as<int32_t>(), p.d_col.as<int32_t>(), val, x, y, rowscale, d, b,
+               q, p.nrows, p.nslices};
+    unsigned grid = grid_for(p.nslices * 32, 256);
+#define FVM_LAUNCH_SELL(W) sell_kernel<V, Acc, DIFF, W><<<grid, 256, 0, s>>>(a)
+    FVM_SELL_DISPATCH(p.maxw, FVM_LAUNCH_SELL)
+#undef FVM_LAUNCH_SELL
+}
 
 void launch_sell_apply64(const SellPattern& p, const double* val, const double* x, double* y, const double* rowscale,
                          const double* b, const double* q, cudaStream_t s) {
-    if (p.nslices == 0) return;
-    sell_apply_kernel<double, double><<<grid_for(p.nslices * 32, 256), 256, 0, s>>>(
-        p.d_slice_ptr.as<int64_t>(), p.d_width.as<int32_t>(), p.d_col.as<int32_t>(), val, x, y, rowscale, b, q, p.nrows,
-        p.nslices);
+    launch_sell<double, double, false>(p, val, x, y, rowscale, nullptr, b, q, s);
 }
 
 void launch_sell_apply32(const SellPattern& p, const float* val, const double* x, double* y, const double* rowscale,
                          const double* b, const double* q, cudaStream_t s) {
-    if (p.nslices == 0) return;
-    sell_apply_kernel<float, float><<<grid_for(p.nslices * 32, 256), 256, 0, s>>>(
-        p.d_slice_ptr.as<int64_t>(), p.d_width.as<int32_t>(), p.d_col.as<int32_t>(), val, x, y, rowscale, b, q, p.nrows,
-        p.nslices);
-}
-
-// ---------------------------------------------------------------------------------------
-// Difference-form operator of the generic RHS:
-//   y_i = rowscale_i * sum_{j != i} K_ij (x_j - x_i) + d_i x_i + b_i + q_i x_i^2
-// Padding slots point at the row itself (x_i - x_i = 0).  The FP32 variant forms the
-// differences of FP32-rounded values and accumulates in FP32; the scaling and the
-// remaining terms are FP64.
-// ---------------------------------------------------------------------------------------
-template <class V, class Acc>
-__global__ void __launch_bounds__(256) sell_diff_kernel(const int64_t* __restrict__ slice_ptr,
-                                                        const int32_t* __restrict__ width,
-                                                        const int32_t* __restrict__ col,
-                                                        const V* __restrict__ val, const double* __restrict__ x,
-                                                        double* __restrict__ y, const double* __restrict__ rowscale,
-                                                        const double* __restrict__ d, const double* __restrict__ b,
-                                                        const double* __restrict__ q, int64_t nrows,
-                                                        int64_t nslices) {
-    int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    int64_t s = gt >> 5;
-    int lane = threadIdx.x & 31;
-    if (s >= nslices) return;
-    int64_t r = s * kSlice + lane;
-    int64_t base = __ldg(&slice_ptr[s]) + lane;
-    int w = __ldg(&width[s]);
-    const double xr = __ldg(&x[r < nrows ? r : nrows - 1]);
-    const Acc xa = (Acc)xr;
-    Acc acc0 = 0, acc1 = 0;
-    int k = 0;
-    for (; k + 1 < w; k += 2) {
-        int64_t i0 = base + (int64_t)k * kSlice, i1 = i0 + kSlice;
-        int32_t c0 = __ldg(&col[i0]), c1 = __ldg(&col[i1]);
-        V v0 = __ldg(&val[i0]), v1 = __ldg(&val[i1]);
-        acc0 += (Acc)v0 * ((Acc)__ldg(&x[c0]) - xa);
-        acc1 += (Acc)v1 * ((Acc)__ldg(&x[c1]) - xa);
-    }
-    if (k < w) {
-        int64_t i0 = base + (int64_t)k * kSlice;
-        acc0 += (Acc)__ldg(&val[i0]) * ((Acc)__ldg(&x[__ldg(&col[i0])]) - xa);
-    }
-    if (r >= nrows) return;
-    double out = (double)(acc0 + acc1);
-    if (rowscale) out *= rowscale[r];
-    if (d) out += d[r] * xr;
-    if (b) out += b[r];
-    if (q) out += q[r] * xr * xr;
-    y[r] = out;
+    launch_sell<float, float, false>(p, val, x, y, rowscale, nullptr, b, q, s);
 }
 
 void launch_sell_diff64(const SellPattern& p, const double* val, const double* x, double* y, const double* rowscale,
                         const double* d, const double* b, const double* q, cudaStream_t s) {
-    if (p.nslices == 0) return;
-    sell_diff_kernel<double, double><<<grid_for(p.nslices * 32, 256), 256, 0, s>>>(
-        p.d_slice_ptr.as<int64_t>(), p.d_width.as<int32_t>(), p.d_col.as<int32_t>(), val, x, y, rowscale, d, b, q,
-        p.nrows, p.nslices);
+    launch_sell<double, double, true>(p, val, x, y, rowscale, d, b, q, s);
 }
 
 void launch_sell_diff32(const SellPattern& p, const float* val, const double* x, double* y, const double* rowscale,
                         const double* d, const double* b, const double* q, cudaStream_t s) {
-    if (p.nslices == 0) return;
-    sell_diff_kernel<float, float><<<grid_for(p.nslices * 32, 256), 256, 0, s>>>(
-        p.d_slice_ptr.as<int64_t>(), p.d_width.as<int32_t>(), p.d_col.as<int32_t>(), val, x, y, rowscale, d, b, q,
-        p.nrows, p.nslices);
+    launch_sell<float, float, true>(p, val, x, y, rowscale, d, b, q, s);
 }
 
 // ---------------------------------------------------------------------------------------

@@ -101,6 +101,7 @@ static void finalize_sell(SellPattern& pat, int64_t nrows) {
         for (int64_t r = s * kSlice; r < std::min<int64_t>(nrows, (s + 1) * kSlice); ++r)
             w = std::max<int32_t>(w, (int32_t)(pat.rowptr[r + 1] - pat.rowptr[r]));
         pat.width[s] = w;
+        pat.maxw = std::max(pat.maxw, (int)w);
         pat.slice_ptr[s + 1] = pat.slice_ptr[s] + (int64_t)w * kSlice;
     }
     pat.nslots = pat.slice_ptr[pat.nslices];

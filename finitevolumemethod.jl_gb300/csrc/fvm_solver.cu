@@ -12,8 +12,11 @@
 // recurrence residual has dropped by `inner_reduction`.  The stopping test is always the
 // FP64 residual ||b - A x|| / ||b|| of the reference operator.
 #include "fvm_internal.h"
+#include "fvm_sell.cuh"
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 
 namespace fvm {
@@ -78,25 +81,14 @@ __device__ void block_reduce_publish(double (&v)[NV], double* part, KState* st, 
 }
 
 // ---- sliced-ELL SpMV with a fused inner product: y = B x, dot(w, y) --------------------
-// x gathered as X, accumulated in T.  Each block covers 8 slices (256 rows).
+// x gathered and accumulated in T.  Each block covers 8 slices (256 rows).  Slices of at
+// most 8 slots (every triangulation here) take the fully unrolled path; the branch is
+// uniform across the warp.
 template <class V, class T>
 __device__ __forceinline__ T sell_row(const int64_t* slice_ptr, const int32_t* width, const int32_t* col, const V* val,
                                       const T* x, int64_t s, int lane) {
-    int64_t base = __ldg(&slice_ptr[s]) + lane;
-    int w = __ldg(&width[s]);
-    T a0 = 0, a1 = 0;
-    int k = 0;
-    for (; k + 1 < w; k += 2) {
-        int64_t i0 = base + (int64_t)k * kSlice, i1 = i0 + kSlice;
-        int32_t c0 = __ldg(&col[i0]), c1 = __ldg(&col[i1]);
-        a0 += (T)__ldg(&val[i0]) * __ldg(&x[c0]);
-        a1 += (T)__ldg(&val[i1]) * __ldg(&x[c1]);
-    }
-    if (k < w) {
-        int64_t i0 = base + (int64_t)k * kSlice;
-        a0 += (T)__ldg(&val[i0]) * __ldg(&x[__ldg(&col[i0])]);
-    }
-    return a0 + a1;
+    if (__ldg(&width[s]) <= 8) return sell_row_product<V, T, T, false, 8>(slice_ptr, width, col, val, x, T(0), s, lane);
+    return sell_row_product<V, T, T, false, 0>(slice_ptr, width, col, val, x, T(0), s, lane);
 }
 
 struct SpmvArgs {
@@ -210,14 +202,11 @@ __global__ void __launch_bounds__(kRedBlock) residual_kernel(SpmvArgs A, const d
     }
 }
 
-// z64 += x32 (or x64); x = 0
+// z64 += sign * x (x in the inner precision)
 template <class T>
-__global__ void accumulate_kernel(double* z, T* x, int64_t n) {
+__global__ void accumulate_kernel(double* z, const T* x, double sign, int64_t n) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) {
-        z[i] += (double)x[i];
-        x[i] = 0;
-    }
+    if (i < n) z[i] += sign * (double)x[i];
 }
 
 // ---- BiCGStab pieces --------------------------------------------------------------------
@@ -530,12 +519,14 @@ static void run_krylov(fvm_template* Tm, Solver& S, bool cg, bool mixed, const f
     double rn = true_residual(true);
     const int chunk = 16;
     int64_t it = 0;
-    int stagnation = 0;
+    int stagnation = 0, rejects = 0;
     double rn_last_update = rn;
     double best = rn;
-    // inner target: the FP32 recurrence is trusted down to `red` of the last true residual
+    double red_cur = red;
+    static const bool trace = std::getenv("FVM_SOLVER_TRACE") != nullptr;
+    // inner target: the FP32 recurrence is trusted down to `red_cur` of the last true residual
     auto inner_tol2 = [&]() {
-        double t = mixed ? std::max(tol, red * rn_last_update) : tol;
+        double t = mixed ? std::max(tol, red_cur * rn_last_update) : tol;
         return t * t;
     };
     bool need_start = !cg;
@@ -565,9 +556,24 @@ static void run_krylov(fvm_template* Tm, Solver& S, bool cg, bool mixed, const f
         it += chunk;  // iterations issued (kernels after convergence return at once)
         if (!h.done) continue;
         // reliable update: fold the correction into the FP64 solution, recompute the residual
-        accumulate_kernel<T><<<S.nb, kRedBlock, 0, s>>>(S.z64, v.x, n);
+        accumulate_kernel<T><<<S.nb, kRedBlock, 0, s>>>(S.z64, v.x, 1.0, n);
         bool restart = !cg || h.breakdown;
-        rn = true_residual(restart);
+        double rn_new = true_residual(restart);
+        if (trace)
+            std::fprintf(stderr, "[fvm solver] %s %s it=%lld rn=%.3e (recurrence %.3e) breakdown=%d\n",
+                         cg ? "cg" : "bicgstab", mixed ? "mixed" : "fp64", (long long)it, rn_new / Tm->bnorm,
+                         std::sqrt(h.rn2) / Tm->bnorm, h.breakdown);
+        if (!(rn_new < rn)) {
+            // the correction raised the true residual (inner-precision drift or breakdown):
+            // undo it, restart from the FP64 residual with a milder inner reduction
+            accumulate_kernel<T><<<S.nb, kRedBlock, 0, s>>>(S.z64, v.x, -1.0, n);
+            rn_new = true_residual(true);
+            restart = true;
+            red_cur = std::min(0.5, red_cur * 4);
+            if (++rejects > 6) break;
+        }
+        FVM_CUDA(cudaMemsetAsync(v.x, 0, sizeof(T) * n, s));
+        rn = rn_new;
         if (!cg) need_start = true;
         if (rn < 0.9 * best) {
             best = rn;
@@ -577,7 +583,7 @@ static void run_krylov(fvm_template* Tm, Solver& S, bool cg, bool mixed, const f
         }
         rn_last_update = rn;
     }
-    stats.iterations = it;
+    stats.iterations += it;
     stats.rel_residual = Tm->bnorm > 0 ? rn / Tm->bnorm : rn;
     if (rn > tol) fail(FVM_ERR_NOT_CONVERGED, "steady solve did not reach rtol (relative residual " +
                                                   std::to_string(stats.rel_residual) + ")");
@@ -629,10 +635,18 @@ extern "C" int fvm_template_steady_solve(fvm_template* Tm, double* x, const fvm_
         int status = FVM_OK;
         std::string msg;
         try {
-            if (mixed)
-                run_krylov<float, float>(Tm, S, cg, true, *opt, st);
-            else
+            if (mixed) {
+                try {
+                    run_krylov<float, float>(Tm, S, cg, true, *opt, st);
+                } catch (const Error& e) {
+                    if (e.code != FVM_ERR_NOT_CONVERGED) throw;
+                    // the FP32 inner iteration stalled: finish in FP64 from the current solution
+                    st.fallback_fp64 = 1;
+                    run_krylov<double, double>(Tm, S, cg, false, *opt, st);
+                }
+            } else {
                 run_krylov<double, double>(Tm, S, cg, false, *opt, st);
+            }
         } catch (const Error& e) {
             if (e.code != FVM_ERR_NOT_CONVERGED) {
                 cudaEventDestroy(e0);

@@ -102,6 +102,7 @@ class SolverStats(C.Structure):
     _fields_ = [
         ("iterations", C.c_int64), ("refinements", C.c_int64), ("rel_residual", C.c_double),
         ("elapsed_ms", C.c_double), ("method_used", C.c_int32), ("symmetric", C.c_int32),
+        ("fallback_fp64", C.c_int32),
     ]
 
 

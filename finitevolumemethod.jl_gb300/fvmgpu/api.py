@@ -785,7 +785,7 @@ def solve(prob, alg=None, *, saveat=None, dt=None, adaptive=None, abstol=1e-6, r
         return LinearSolution(x, {"iterations": st.iterations, "refinements": st.refinements,
                                   "rel_residual": st.rel_residual, "elapsed_ms": st.elapsed_ms,
                                   "method": "cg" if st.method_used == _lib.FVM_SOLVER_CG else "bicgstab",
-                                  "symmetric": bool(st.symmetric)})
+                                  "symmetric": bool(st.symmetric), "fallback_fp64": bool(st.fallback_fp64)})
     if isinstance(prob, _TimeTemplate):
         t0, tf, u0 = prob.initial_time, prob.final_time, prob.u0
     elif isinstance(prob, FVMProblem):

@@ -215,6 +215,7 @@ typedef struct fvm_solver_stats {
     double elapsed_ms;      /* device time (CUDA events) */
     int32_t method_used;
     int32_t symmetric;
+    int32_t fallback_fp64;  /* mixed mode finished in FP64 after the FP32 inner iteration stalled */
 } fvm_solver_stats;
 
 /* Solves A x = b of a Poisson or mean-exit-time template.  x: in = initial guess,

@@ -37,8 +37,14 @@ def test_rhs_parity_fp64(gpu_lib, name):
     spec = BUILDERS[name]()
     oprob = oracle_problem(spec)
     rng = np.random.default_rng(11)
+    P = spec.tri.points
+    # non-constant fields: on a constant field the reference's own RHS is rounding noise
+    # (alpha = s1 u_i + s2 u_j + s3 u_k cancels to ~1e-12 |s| |u|), see test_constant_field_exact
     for trial in range(2):
-        u = spec.u0 if trial == 0 else spec.u0 + rng.standard_normal(spec.tri.num_points) * 0.1
+        if trial == 0:
+            u = spec.u0 + 0.05 * np.sin(3 * P[:, 0] + 2 * P[:, 1])
+        else:
+            u = spec.u0 + rng.standard_normal(spec.tri.num_points) * 0.1
         ref = O.fvm_eqs(oprob, u, spec.t0)
         prob = api_problem(spec)
         for force in (False, True):
@@ -46,6 +52,28 @@ def test_rhs_parity_fp64(gpu_lib, name):
             F.fvm_eqs(du, np.ascontiguousarray(u), prob, spec.t0, force_triangle=force)
             e2, einf = rel_err(du, ref)
             assert e2 <= FP64_RTOL and einf <= FP64_RTOL, (name, force, e2, einf)
+
+
+def test_constant_field_exact(gpu_lib):
+    """test/equations.jl:37-92 on the GPU: heat convection at T = 10 everywhere.  Interior
+    fluxes vanish exactly (difference form), the corner vertex matches the hand-computed
+    value, and only Neumann boundary rows are non-zero."""
+    import fvmgpu as F
+
+    spec = heat_convection(200)
+    prob = api_problem(spec)
+    du = F.fvm_eqs(np.zeros(spec.tri.num_points), spec.u0.copy(), prob, 0.0)
+    P = spec.tri.points
+    x1, y1 = P[1, 0], P[200, 1]
+    A = 0.5 * abs((x1 / 2) * (y1 / 3) - (x1 / 3) * 0.0) + 0.5 * abs((x1 / 3) * (y1 / 2) - 0.0 * (y1 / 3))
+    Pm = spec.bc_params[0]
+    fl = -(1 / A) * (-Pm["alpha"] * Pm["q"] / Pm["k"] * (x1 / 2))
+    assert np.isclose(du[0], fl, rtol=1e-12)
+    interior = np.ones(spec.tri.num_points, bool)
+    interior[np.concatenate(spec.tri.boundary_nodes)] = False
+    assert np.all(du[interior] == 0.0)
+    top = spec.tri.boundary_nodes[2]
+    assert np.max(np.abs(du[top])) <= 1e-14 * np.max(np.abs(du))
 
 
 def test_rhs_parity_device_pointers(gpu_lib):

@@ -1,0 +1,75 @@
+"""GPU Tsit5 (fixed step, CUDA-graph replay, adaptive PI control with saveat) against the
+oracle's Tsit5 driver, which restates the same step control.  Tolerance: 1e-10 relative to
+max|u| for fixed steps, 1e-8 for adaptive runs (identical step sequences, rounding only)."""
+import numpy as np
+import pytest
+
+import fvm_oracle as O
+from problems import api_problem, mixed_annulus, oracle_problem, readme_diffusion, sine_diffusion
+
+pytestmark = pytest.mark.gpu
+
+
+def _oracle_run(spec, saveat, dt=None, adaptive=True):
+    prob = oracle_problem(spec)
+    cb = (lambda u, t: O.update_dirichlet_nodes(prob, u, t)) if prob.conds.dirichlet_nodes else None
+    return O.tsit5_solve(lambda u, t: O.fvm_eqs(prob, u, t), spec.u0, spec.t0, spec.tf, saveat, dt=dt,
+                         adaptive=adaptive, callback=cb)
+
+
+@pytest.mark.parametrize("use_graph", [True, False])
+def test_fixed_step_tsit5(gpu_lib, use_graph):
+    import fvmgpu as F
+
+    spec = sine_diffusion(32)
+    spec.tf = 2e-3
+    prob = api_problem(spec)
+    sol = F.solve(prob, F.Tsit5(), dt=1e-4, adaptive=False, saveat=[spec.tf], use_graph=use_graph)
+    ref, st = _oracle_run(spec, [spec.tf], dt=1e-4, adaptive=False)
+    err = np.max(np.abs(sol.u[-1] - ref[-1])) / np.max(np.abs(ref[-1]))
+    assert err < 1e-10, err
+    assert sol.stats["naccept"] == st["naccept"] == 20
+
+
+def test_adaptive_readme_saveat(gpu_lib):
+    """README diffusion (test/README.jl): Tsit5 to t = 0.5 with saveat = 0.001."""
+    import fvmgpu as F
+
+    spec = readme_diffusion(50)
+    prob = api_problem(spec)
+    sol = F.solve(prob, F.Tsit5(), saveat=0.001)
+    assert len(sol.u) == 501 and np.isclose(sol.t[-1], 0.5)
+    ref, st = _oracle_run(spec, list(sol.t))
+    assert sol.stats["naccept"] == st["naccept"] and sol.stats["nreject"] == st["nreject"]
+    err = np.max(np.abs(np.array(sol.u) - ref)) / 50.0
+    assert err < 1e-8, err
+    # sanity: the solution decays and stays within the initial bounds
+    assert np.all(np.array(sol.u) <= 50 + 1e-9) and np.all(np.array(sol.u) >= -1e-9)
+
+
+def test_adaptive_mixed_conditions(gpu_lib):
+    import fvmgpu as F
+
+    spec = mixed_annulus()
+    prob = api_problem(spec)
+    sol = F.solve(prob, F.Tsit5(), saveat=0.02)
+    ref, st = _oracle_run(spec, list(sol.t))
+    err = np.max(np.abs(np.array(sol.u) - ref)) / np.max(np.abs(ref))
+    assert err < 1e-8, err
+
+
+def test_template_tsit5_matches_oracle(gpu_lib):
+    import fvmgpu as F
+
+    spec = sine_diffusion(40)
+    mesh = F.FVMGeometry(spec.tri)
+    BCs = F.BoundaryConditions(mesh, spec.bc_fns[0], F.Dirichlet)
+    D = lambda x, y, p: spec.D(x, y, 0, 0, None)  # noqa: E731
+    tmpl = F.DiffusionEquation(mesh, BCs, diffusion_function=D, initial_condition=spec.u0, final_time=1e-3)
+    sol = F.solve(tmpl, F.Tsit5(), saveat=[1e-3], dt=5e-5, adaptive=False)
+    assert sol.u[-1].shape[0] == spec.tri.num_points + 1 and sol.u[-1][-1] == 1.0
+    conds = O.Conditions(spec.tri, [lambda x, y, t, u: 0.0 * x], ["Dirichlet"])
+    A, b, u0 = O.template_diffusion(spec.tri, conds, lambda x, y: D(x, y, None), spec.u0)
+    ref, _ = O.tsit5_solve(lambda u, t: A @ u + b, u0, 0.0, 1e-3, [1e-3], dt=5e-5, adaptive=False)
+    err = np.max(np.abs(sol.u[-1][:-1] - ref[-1])) / np.max(np.abs(ref[-1]))
+    assert err < 1e-10, err

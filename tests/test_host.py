@@ -1,0 +1,106 @@
+"""Host-side logic without a GPU: mesh generators, condition merging, closure classification."""
+import numpy as np
+import pytest
+
+import fvm_oracle as O
+from fvmgpu import forms
+from fvmgpu.api import BoundaryConditions, Conditions, InternalConditions, _saveat_times
+from fvmgpu.meshes import triangulate_annulus, triangulate_disk, triangulate_rectangle
+import fvmgpu.api as api
+
+
+class _Mesh:
+    def __init__(self, tri):
+        self.triangulation = tri
+
+
+def test_rectangle_numbering_matches_reference_tests():
+    tri = triangulate_rectangle(0.0, 2.0, 0.0, 5.0, 12, 19, single_boundary=False)
+    P = tri.points
+    # vertex i + (j-1) nx (1-based) = (i-1) + (j-1) nx (0-based), x fastest (test_functions.jl:112)
+    assert np.allclose(P[6 + 3 * 12], [6 * 2.0 / 11, 3 * 5.0 / 18])
+    t200 = triangulate_rectangle(0.0, 1.0, 0.0, 1.0, 200, 200)
+    assert (0, 1, 200) in set(map(tuple, t200.triangles.tolist()))  # test/equations.jl:42
+    assert tri.num_triangles == 2 * 11 * 18 and tri.num_boundary_edges == 2 * 11 + 2 * 18
+    assert [len(s) for s in tri.boundary_nodes] == [12, 19, 12, 19]
+    assert np.all(P[tri.boundary_nodes[0], 1] == 0.0) and np.all(P[tri.boundary_nodes[1], 0] == 2.0)
+    assert np.all(P[tri.boundary_nodes[2], 1] == 5.0) and np.all(P[tri.boundary_nodes[3], 0] == 0.0)
+    single = triangulate_rectangle(0.0, 1.0, 0.0, 1.0, 5, 5, single_boundary=True)
+    assert single.num_ghost_vertices == 1 and single.boundary_nodes[0][0] == single.boundary_nodes[0][-1]
+
+
+def test_triangles_ccw_and_boundary_adjacency():
+    for tri in (triangulate_rectangle(0, 1, 0, 1, 7, 9), triangulate_annulus(0.5, 1.0, 5, 24),
+                triangulate_disk(400, 32, seed=1)):
+        P, T = tri.points, tri.triangles
+        det = ((P[T[:, 1], 0] - P[T[:, 0], 0]) * (P[T[:, 2], 1] - P[T[:, 0], 1])
+               - (P[T[:, 1], 1] - P[T[:, 0], 1]) * (P[T[:, 2], 0] - P[T[:, 0], 0]))
+        assert np.all(det > 0)
+        tset = {tuple(t) for t in T.tolist()}
+        for (i, j), k in zip(tri.boundary_edges, tri.boundary_adjacent):
+            assert (i, j, k) in tset or (j, k, i) in tset or (k, i, j) in tset
+    d = triangulate_disk(1000, 64, seed=0)
+    assert d.num_triangles == 2 * d.num_points - 64 - 2
+    assert d.num_boundary_edges == 64
+
+
+def test_conditions_merge_matches_oracle_bit_exact():
+    tri = triangulate_annulus(0.5, 1.0, 6, 32, nsegments=4)
+    types = ("Dirichlet", "Dudt", "Neumann", "Constrained", "Neumann", "Dirichlet", "Dudt", "Neumann")
+    fns = tuple((lambda x, y, t, u, p, k=k: k + 0.0 * x) for k in range(8))
+    mesh = _Mesh(tri)
+    bc = BoundaryConditions(mesh, fns, tuple(getattr(api, t) for t in types))
+    ic = InternalConditions((lambda x, y, t, u, p: x,), dirichlet_nodes={40: 0, 0: 0}, dudt_nodes={41: 0})
+    c = Conditions(mesh, bc, ic)
+    oc = O.Conditions(tri, [lambda x, y, t, u: x] * 8, list(types), [lambda x, y, t, u: x], {40: 0, 0: 0}, {41: 0})
+    assert c.neumann_edges == oc.neumann_edges
+    assert c.constrained_edges == oc.constrained_edges
+    assert c.dirichlet_nodes == oc.dirichlet_nodes
+    assert c.dudt_nodes == oc.dudt_nodes
+    hv = tri.has_vertex()
+    code, fidx = c.vertex_tables(hv)
+    ocode, ofidx = oc.vertex_tables(tri.num_points, hv)
+    assert np.array_equal(code, ocode) and np.array_equal(fidx, ofidx)
+    assert np.array_equal(c.neumann_table(tri.boundary_edges), oc.edge_tables(tri.boundary_edges))
+
+
+def test_boundary_conditions_argument_checks():
+    tri = triangulate_rectangle(0, 1, 0, 1, 4, 4, single_boundary=False)
+    mesh = _Mesh(tri)
+    f = lambda x, y, t, u, p: x  # noqa: E731
+    with pytest.raises(AssertionError):
+        BoundaryConditions(mesh, f, api.Dirichlet)  # 4 boundary parts need 4 conditions
+    with pytest.raises(AssertionError):
+        BoundaryConditions(mesh, (f,) * 4, (api.Dirichlet,) * 3)
+    bc = BoundaryConditions(triangulate_rectangle(0, 1, 0, 1, 4, 4, single_boundary=True) and
+                            _Mesh(triangulate_rectangle(0, 1, 0, 1, 4, 4, single_boundary=True)), f, api.Dirichlet,
+                            parameters=(0.3, 0.6, -1.0))
+    assert bc.functions[0].parameters == (0.3, 0.6, -1.0)  # a lone function keeps its tuple p
+
+
+def test_form_classification():
+    x = np.linspace(0, 1, 50)
+    y = np.linspace(1, 2, 50)
+    c, d = forms.classify_xytu(lambda x, y, t, u: 1 / 9 + 0.0 * x, x, y, 0.0, "D")
+    assert d == 0 and np.allclose(c[:, 0], 1 / 9)
+    c, d = forms.classify_xytu(lambda x, y, t, u: x * y + 2.0 * u, x, y, 0.0, "a")
+    assert d == 1 and np.allclose(c[:, 0], x * y) and np.allclose(c[:, 1], 2.0)
+    c, d = forms.classify_xytu(lambda x, y, t, u: u * (1 - u), x, y, 0.0, "S")
+    assert d == 2 and np.allclose(c, [[0.0, 1.0, -1.0]] * 50)
+    c, d = forms.classify_xytu(lambda x, y, t, u: 50.0 if y <= 1.5 else 0.0, x, y, 0.0, "branching closure")
+    assert d == 0 and np.allclose(c[:, 0], np.where(y <= 1.5, 50.0, 0.0))
+    for bad in (lambda x, y, t, u: np.exp(u), lambda x, y, t, u: t + 0.0 * x, lambda x, y, t, u: u ** 3,
+                lambda x, y, t, u: 1 / (x - x)):
+        with pytest.raises(forms.UnsupportedFormError):
+            forms.classify_xytu(bad, x, y, 0.0, "bad")
+    D = forms.classify_flux(lambda x, y, t, a, b, g: (-(1 + x) * a, -(1 + x) * b), x, y, 0.0)
+    assert np.allclose(D, 1 + x)
+    with pytest.raises(forms.UnsupportedFormError):
+        forms.classify_flux(lambda x, y, t, a, b, g: (-a * (a * x + b * y + g), -b), x, y, 0.0)
+
+
+def test_saveat_times_follow_julia_ranges():
+    ts = _saveat_times(0.001, 0.0, 0.5)
+    assert ts.size == 501 and ts[0] == 0.0 and abs(ts[-1] - 0.5) < 1e-12
+    assert np.array_equal(_saveat_times([0.1, 0.2], 0.0, 1.0), [0.1, 0.2])
+    assert np.array_equal(_saveat_times(None, 0.0, 1.0), [0.0, 1.0])
