@@ -313,7 +313,7 @@ def run_gpu(args):
                    "layout": "device-resident u/du in the library's Hilbert numbering",
                    "parallelism": f"replicas x{ws}"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "kernel": "sell_diff_kernel<double,double>",
+                     "traffic": traffic, "kernel": "sell_kernel<double,double,double,explicit,8>",
                      "alg_bytes_per_launch": alg_bytes, "peak_source": f"{peak_kind} hbm_gbs (burst copy)"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n,
                 "ms_per_step": float(ms_e2e.mean()), "path": "fvm_rhs C ABI, pinned host buffers"},
@@ -345,12 +345,21 @@ def run_extras(args, F, torch, tri, mesh, prob, flush, perm, u_int, peak):
         p32 = c2_problem(mesh, precision="fp32")
         i32 = p32.info()
         ms = timed_steps(lambda: F.fvm_eqs(du, u_int, p32, 0.0, internal=True), K, 5, flush, torch)
-        b32 = 8 * i32["operator_nonzeros"] + 16 * n
+        # to_f32 pass (read u 8 B, write u32 4 B) + operator 8 B / entry + u32 4 B + rowscale 8 B + du 8 B
+        b32 = 8 * i32["operator_nonzeros"] + 32 * n
         out["rhs_fp32"] = {"value": units / (ms.mean() / 1e3), "unit": UNIT, "ms": float(ms.mean()),
                            "achieved_gbs": b32 / (ms.mean() / 1e3) / 1e9, "alg_bytes": b32}
         del p32
     except Exception as e:  # noqa: BLE001
         out["rhs_fp32"] = {"error": repr(e)}
+    try:
+        ms = timed_steps(lambda: F.fvm_eqs(du, u_int, prob, 0.0, internal=True, conservative=True), K, 5, flush,
+                         torch)
+        bc = 12 * (info_c := prob.info())["operator_nonzeros"] - 12 * n + 16 * n
+        out["rhs_fp64_conservative"] = {"value": units / (ms.mean() / 1e3), "unit": UNIT, "ms": float(ms.mean()),
+                                        "achieved_gbs": bc / (ms.mean() / 1e3) / 1e9, "alg_bytes": bc}
+    except Exception as e:  # noqa: BLE001
+        out["rhs_fp64_conservative"] = {"error": repr(e)}
     try:
         ms = timed_steps(lambda: F.fvm_eqs(du, u_int, prob, 0.0, internal=True, force_triangle=True), K, 5, flush,
                          torch)

@@ -332,16 +332,26 @@ static void rhs_outputs(fvm_problem* p, double* du, int32_t loc, cudaStream_t s)
 }
 
 // fvm_eqs! in the internal numbering
-void problem_rhs_internal(fvm_problem* p, const double* u, double* du, bool force_triangle, cudaStream_t s) {
+void problem_rhs_internal(fvm_problem* p, const double* u, double* du, bool force_triangle, cudaStream_t s,
+                          bool conservative) {
     fvm_mesh* m = p->mesh;
     if (p->linear && !force_triangle) {
         const double* dg = p->has_d ? p->d_d.as<double>() : nullptr;
         const double* b = p->has_b ? p->d_b.as<double>() : nullptr;
         const double* q = p->has_q ? p->d_q.as<double>() : nullptr;
-        if (p->precision == FVM_FP32)
-            launch_sell_diff32(m->pat_off, p->d_val32.as<float>(), u, du, p->d_rowscale.as<double>(), dg, b, q, s);
-        else
-            launch_sell_diff64(m->pat_off, p->d_val64.as<double>(), u, du, nullptr, dg, b, q, s);
+        if (p->precision == FVM_FP32) {
+            launch_to_f32(u, p->d_u32.as<float>(), m->np, s);
+            if (conservative)
+                launch_sell_diff32(m->pat_off, p->d_kval32.as<float>(), p->d_u32.as<float>(), u, du,
+                                   p->d_rowscale.as<double>(), dg, b, q, s);
+            else
+                launch_sell_apply32(m->pat, p->d_val32.as<float>(), p->d_u32.as<float>(), u, du,
+                                    p->d_rowscale.as<double>(), b, q, s);
+        } else if (conservative) {
+            launch_sell_diff64(m->pat_off, p->d_kval64.as<double>(), u, du, nullptr, dg, b, q, s);
+        } else {
+            launch_sell_apply64(m->pat, p->d_val64.as<double>(), u, du, nullptr, b, q, s);
+        }
     } else {
         if (p->precision == FVM_FP32 && !p->linear)
             fail(FVM_ERR_UNSUPPORTED_FORM, "FP32 assembly is available for linear forms only");
@@ -544,7 +554,8 @@ int fvm_rhs(fvm_problem* p, const double* u, double* du, double t, int32_t flags
         (void)t;  // device-coded forms are time independent
         IoPlan io;
         rhs_inputs(p, u, du, loc, io, s);
-        problem_rhs_internal(p, io.uin, io.dout, (flags & FVM_RHS_FORCE_TRIANGLE) != 0, s);
+        problem_rhs_internal(p, io.uin, io.dout, (flags & FVM_RHS_FORCE_TRIANGLE) != 0, s,
+                             (flags & FVM_RHS_CONSERVATIVE) != 0);
         check_launch();
         rhs_outputs(p, du, loc, s);
         return FVM_OK;

@@ -113,9 +113,13 @@ struct fvm_problem {
     std::vector<int8_t> code;                   // [np] caller order
     std::vector<int8_t> bneu;                   // [nbe]
     std::vector<double> dualD, quarterD, quarterN, src, dudt, dirv;  // copies of the descriptor arrays
-    // linear operator path (difference form on the off-diagonal pattern):
+    // linear operator path, explicit form on the pattern with the diagonal (default):
+    //   du_i = rowscale_i * sum_j A_ij u_j + b_i + q_i u_i^2
+    // and difference form on the off-diagonal pattern (FVM_RHS_CONSERVATIVE):
     //   du_i = rowscale_i * sum_{j != i} K_ij (u_j - u_i) + d_i u_i + b_i + q_i u_i^2
-    fvm::DBuf d_val64, d_val32, d_b, d_q, d_d, d_rowscale;
+    fvm::DBuf d_val64, d_val32;                 // explicit A (FP64; FP32 unscaled by 1/V)
+    fvm::DBuf d_kval64, d_kval32, d_d;          // difference form K, d
+    fvm::DBuf d_b, d_q, d_rowscale, d_u32;
     bool has_b = false, has_q = false, has_d = false;
     int64_t op_nonzeros = 0;
     // triangle path
@@ -134,7 +138,7 @@ struct fvm_problem {
 struct fvm_template {
     fvm_problem* prob = nullptr;
     int kind = 0;
-    fvm::DBuf d_val64, d_val32, d_b;
+    fvm::DBuf d_val64, d_val32, d_b, d_u32;
     std::vector<double> val, b;                 // SELL values (internal), b internal
     // steady solve (reduced SPD-like system on free rows)
     bool steady_ready = false;
@@ -150,13 +154,15 @@ namespace fvm {
 // kernels (fvm_kernels.cu)
 void launch_sell_apply64(const SellPattern& p, const double* val, const double* x, double* y,
                          const double* rowscale, const double* b, const double* q, cudaStream_t s);
-void launch_sell_apply32(const SellPattern& p, const float* val, const double* x, double* y,
+// FP32 variants gather x32 (an FP32 copy of x made by launch_to_f32) and use x for the row's own terms
+void launch_sell_apply32(const SellPattern& p, const float* val, const float* x32, const double* x, double* y,
                          const double* rowscale, const double* b, const double* q, cudaStream_t s);
 // y_i = rowscale_i * sum_j K_ij (x_j - x_i) + d_i x_i + b_i + q_i x_i^2 (any of rowscale, d, b, q may be null)
 void launch_sell_diff64(const SellPattern& p, const double* val, const double* x, double* y, const double* rowscale,
                         const double* d, const double* b, const double* q, cudaStream_t s);
-void launch_sell_diff32(const SellPattern& p, const float* val, const double* x, double* y, const double* rowscale,
-                        const double* d, const double* b, const double* q, cudaStream_t s);
+void launch_sell_diff32(const SellPattern& p, const float* val, const float* x32, const double* x, double* y,
+                        const double* rowscale, const double* d, const double* b, const double* q, cudaStream_t s);
+void launch_to_f32(const double* x, float* y, int64_t n, cudaStream_t s);
 void launch_permute_in(const int32_t* perm, const double* xref, double* xint, int64_t n, cudaStream_t s);
 void launch_permute_out(const int32_t* perm, const double* xint, double* xref, int64_t n, cudaStream_t s);
 void launch_dirichlet(const int32_t* idx, const double* val, double* u, int64_t n, cudaStream_t s);
@@ -180,5 +186,6 @@ struct OdeRhs {
 void tsit5_run_internal(OdeRhs& rhs, int64_t n, const double* u0_int, const fvm_ode_options& o, double* out_int,
                         fvm_ode_stats* st, cudaStream_t s);
 int guard_call(const std::function<int()>& f);
-void problem_rhs_internal(fvm_problem* p, const double* u, double* du, bool force_triangle, cudaStream_t s);
+void problem_rhs_internal(fvm_problem* p, const double* u, double* du, bool force_triangle, cudaStream_t s,
+                          bool conservative = false);
 }  // namespace fvm

@@ -13,14 +13,17 @@ static inline unsigned grid_for(int64_t threads, int block) { return (unsigned)(
 //   difference form (generic RHS):  y_i = rowscale_i * sum_{j != i} K_ij (x_j - x_i)
 //                                         + d_i x_i + b_i + q_i x_i^2
 // In the difference form padding slots point at the row itself (x_i - x_i = 0).  FP32
-// variants round x to FP32, accumulate in FP32 and apply rowscale, d, b, q in FP64.
+// variants gather an FP32 copy of x (converted once per row by to_f32_kernel: gathering
+// doubles would spend an FP64-pipe conversion per entry), accumulate in FP32 and apply
+// rowscale, d, b, q in FP64 with the row's FP64 value.
 // ---------------------------------------------------------------------------------------
 struct SellArgs {
     const int64_t* slice_ptr;
     const int32_t* width;
     const int32_t* col;
     const void* val;
-    const double* x;
+    const void* xg;   // gathered x (double or float)
+    const double* x;  // the row's own FP64 value
     double* y;
     const double* rowscale;
     const double* d;
@@ -29,54 +32,66 @@ struct SellArgs {
     int64_t nrows, nslices;
 };
 
-template <class V, class Acc, bool DIFF, int MAXW>
+template <class V, class Acc, class X, bool DIFF, int MAXW>
 __global__ void __launch_bounds__(256) sell_kernel(SellArgs a) {
     const int64_t s = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (s >= a.nslices) return;
     const int64_t r = s * kSlice + lane;
-    const double xr = __ldg(&a.x[r < a.nrows ? r : a.nrows - 1]);
-    Acc acc = sell_row_product<V, Acc, double, DIFF, MAXW>(a.slice_ptr, a.width, a.col, (const V*)a.val, a.x, (Acc)xr,
-                                                           s, lane);
+    const int64_t rc = r < a.nrows ? r : a.nrows - 1;
+    const X* xg = (const X*)a.xg;
+    Acc xa = DIFF ? (Acc)__ldg(&xg[rc]) : Acc(0);
+    Acc acc = sell_row_product<V, Acc, X, DIFF, MAXW>(a.slice_ptr, a.width, a.col, (const V*)a.val, xg, xa, s, lane);
     if (r >= a.nrows) return;
     double out = (double)acc;
     if (a.rowscale) out *= a.rowscale[r];
-    if (a.d) out += a.d[r] * xr;
+    if (a.d || a.q) {
+        const double xr = a.x[r];
+        if (a.d) out += a.d[r] * xr;
+        if (a.q) out += a.q[r] * xr * xr;
+    }
     if (a.b) out += a.b[r];
-    if (a.q) out += a.q[r] * xr * xr;
     a.y[r] = out;
 }
 
-template <class V, class Acc, bool DIFF>
-static void launch_sell(const SellPattern& p, const V* val, const double* x, double* y, const double* rowscale,
-                        const double* d, const double* b, const double* q, cudaStream_t s) {
+template <class V, class Acc, class X, bool DIFF>
+static void launch_sell(const SellPattern& p, const V* val, const X* xg, const double* x, double* y,
+                        const double* rowscale, const double* d, const double* b, const double* q, cudaStream_t s) {
     if (p.nslices == 0) return;
-    SellArgs a{p.d_slice_ptr.as<int64_t>(), p.d_width.as<int32_t>(), p.d_col.as<int32_t>(), val, x, y, rowscale, d, b,
-               q, p.nrows, p.nslices};
+    SellArgs a{p.d_slice_ptr.as<int64_t>(), p.d_width.as<int32_t>(), p.d_col.as<int32_t>(), val, xg, x, y, rowscale,
+               d, b, q, p.nrows, p.nslices};
     unsigned grid = grid_for(p.nslices * 32, 256);
-#define FVM_LAUNCH_SELL(W) sell_kernel<V, Acc, DIFF, W><<<grid, 256, 0, s>>>(a)
+#define FVM_LAUNCH_SELL(W) sell_kernel<V, Acc, X, DIFF, W><<<grid, 256, 0, s>>>(a)
     FVM_SELL_DISPATCH(p.maxw, FVM_LAUNCH_SELL)
 #undef FVM_LAUNCH_SELL
 }
 
 void launch_sell_apply64(const SellPattern& p, const double* val, const double* x, double* y, const double* rowscale,
                          const double* b, const double* q, cudaStream_t s) {
-    launch_sell<double, double, false>(p, val, x, y, rowscale, nullptr, b, q, s);
+    launch_sell<double, double, double, false>(p, val, x, x, y, rowscale, nullptr, b, q, s);
 }
 
-void launch_sell_apply32(const SellPattern& p, const float* val, const double* x, double* y, const double* rowscale,
-                         const double* b, const double* q, cudaStream_t s) {
-    launch_sell<float, float, false>(p, val, x, y, rowscale, nullptr, b, q, s);
+void launch_sell_apply32(const SellPattern& p, const float* val, const float* x32, const double* x, double* y,
+                         const double* rowscale, const double* b, const double* q, cudaStream_t s) {
+    launch_sell<float, float, float, false>(p, val, x32, x, y, rowscale, nullptr, b, q, s);
 }
 
 void launch_sell_diff64(const SellPattern& p, const double* val, const double* x, double* y, const double* rowscale,
                         const double* d, const double* b, const double* q, cudaStream_t s) {
-    launch_sell<double, double, true>(p, val, x, y, rowscale, d, b, q, s);
+    launch_sell<double, double, double, true>(p, val, x, x, y, rowscale, d, b, q, s);
 }
 
-void launch_sell_diff32(const SellPattern& p, const float* val, const double* x, double* y, const double* rowscale,
-                        const double* d, const double* b, const double* q, cudaStream_t s) {
-    launch_sell<float, float, true>(p, val, x, y, rowscale, d, b, q, s);
+void launch_sell_diff32(const SellPattern& p, const float* val, const float* x32, const double* x, double* y,
+                        const double* rowscale, const double* d, const double* b, const double* q, cudaStream_t s) {
+    launch_sell<float, float, float, true>(p, val, x32, x, y, rowscale, d, b, q, s);
+}
+
+__global__ void to_f32_kernel(const double* __restrict__ x, float* __restrict__ y, int64_t n) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = (float)x[i];
+}
+void launch_to_f32(const double* x, float* y, int64_t n, cudaStream_t s) {
+    if (n) to_f32_kernel<<<grid_for(n, 256), 256, 0, s>>>(x, y, n);
 }
 
 // ---------------------------------------------------------------------------------------

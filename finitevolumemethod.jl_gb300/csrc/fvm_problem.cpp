@@ -24,25 +24,31 @@ void fvm_problem::ensure_work() {
 //   triangle dual edge e of T = (a, b, c): Q_e = -D_e l_e (alpha n_x + beta n_y)
 //   boundary half edge (non-Neumann):      Q_h = -D_h l_h (alpha n_x + beta n_y)
 //   boundary half edge (Neumann, a = n0 + n1 u(m)): Q_h = l_h (n0 + n1 u(m)).
-// Stored in difference form on the off-diagonal pattern:
-//   du_i = sum_{j != i} K_ij (u_j - u_i) + d_i u_i + b_i + q_i u_i^2.
-// A dual-edge flux is a combination of u with coefficients summing to zero (constant u carries
-// no flux), so its diagonal coefficient is implied and dropped: constant fields give exactly
-// zero flux, as in the reference's alpha = s1 u_i + s2 u_j + s3 u_k.  Non-flux terms
-// (Neumann u(m) dependence, source, Dudt) keep their full row sum in d_i.
-static void assemble_generic(fvm_problem* p, std::vector<double>& A, std::vector<double>& dg,
+// Two equivalent storages are produced from the same contributions:
+//  explicit (pattern with the diagonal): du_i = sum_j A_ij u_j + b_i + q_i u_i^2, one FP64
+//    FMA per entry (GB300 runs FP64 at 1/58 of the FP32 rate, so this is the default);
+//  difference form (off-diagonal pattern): du_i = sum_{j != i} K_ij (u_j - u_i) + d_i u_i
+//    + b_i + q_i u_i^2.  A dual-edge flux is a combination of u whose coefficients sum to
+//    zero (constant u carries no flux), so its diagonal coefficient is implied and dropped:
+//    constant fields give exactly zero flux.  Non-flux terms (Neumann u(m) dependence, source,
+//    Dudt) keep their full row sum in d_i.
+static void assemble_generic(fvm_problem* p, std::vector<double>& E, std::vector<double>& A, std::vector<double>& dg,
                              std::vector<double>& b, std::vector<double>& q, std::vector<double>& rowscale) {
     const fvm_mesh* m = p->mesh;
     const SellPattern& pat = m->pat_off;
+    const SellPattern& pate = m->pat;
+    E.assign(pate.nslots, 0.0);
     A.assign(pat.nslots, 0.0);
     dg.assign(m->np, 0.0);
     b.assign(m->np, 0.0);
     q.assign(m->np, 0.0);
     rowscale.assign(m->np, 0.0);
     auto flux = [&](int32_t r, int32_t c, double v) {
+        E[pate.find(m->iperm[r], m->iperm[c])] += v;
         if (r != c) A[pat.find(m->iperm[r], m->iperm[c])] += v;
     };
     auto lin = [&](int32_t r, int32_t c, double v) {
+        E[pate.find(m->iperm[r], m->iperm[c])] += v;
         if (r != c) A[pat.find(m->iperm[r], m->iperm[c])] += v;
         dg[m->iperm[r]] += v;
     };
@@ -113,14 +119,14 @@ static void assemble_generic(fvm_problem* p, std::vector<double>& A, std::vector
             rowscale[r] = 1.0 / m->vol[v];
             if (!p->src.empty()) {
                 b[r] += p->src[v * ns];
-                if (ns > 1) dg[r] += p->src[v * ns + 1];
+                if (ns > 1 && p->src[v * ns + 1] != 0) lin((int32_t)v, (int32_t)v, p->src[v * ns + 1]);
                 if (ns > 2) q[r] = p->src[v * ns + 2];
             }
         } else if (c == FVM_VERTEX_DUDT) {
             rowscale[r] = 1.0;
             if (!p->dudt.empty()) {
                 b[r] = p->dudt[v * nu];
-                if (nu > 1) dg[r] += p->dudt[v * nu + 1];
+                if (nu > 1 && p->dudt[v * nu + 1] != 0) lin((int32_t)v, (int32_t)v, p->dudt[v * nu + 1]);
                 if (nu > 2) q[r] = p->dudt[v * nu + 2];
             }
         }
@@ -196,11 +202,12 @@ extern "C" int fvm_problem_create_impl(fvm_mesh* mesh, const fvm_problem_desc* d
         p->d_dir_val.upload(val);
     }
     if (p->linear) {
-        std::vector<double> A, dg, b, q, rs;
-        assemble_generic(p.get(), A, dg, b, q, rs);
-        p->d_val64.upload(A);
+        std::vector<double> E, A, dg, b, q, rs;
+        assemble_generic(p.get(), E, A, dg, b, q, rs);
+        p->d_val64.upload(E);
+        p->d_kval64.upload(A);
         auto nz = [](double x) { return x != 0; };
-        p->op_nonzeros = std::count_if(A.begin(), A.end(), nz);
+        p->op_nonzeros = std::count_if(E.begin(), E.end(), nz);
         p->has_b = std::any_of(b.begin(), b.end(), nz);
         p->has_q = std::any_of(q.begin(), q.end(), nz);
         p->has_d = std::any_of(dg.begin(), dg.end(), nz);
@@ -208,20 +215,25 @@ extern "C" int fvm_problem_create_impl(fvm_mesh* mesh, const fvm_problem_desc* d
         if (p->has_q) p->d_q.upload(q);
         if (p->has_d) p->d_d.upload(dg);
         if (p->precision == FVM_FP32) {
-            std::vector<float> A32(A.size(), 0.0f);
-            const SellPattern& pat = m->pat_off;
-            for (int64_t s = 0; s < pat.nslices; ++s)
-                for (int lane = 0; lane < kSlice; ++lane) {
-                    int64_t r = s * kSlice + lane;
-                    if (r >= m->np) continue;
-                    double sc = rs[r];
-                    for (int32_t k = 0; k < pat.width[s]; ++k) {
-                        int64_t slot = pat.slice_ptr[s] + (int64_t)k * kSlice + lane;
-                        A32[slot] = sc != 0 ? (float)(A[slot] / sc) : 0.0f;
+            // FP32 values carry no 1/V (the control-volume division stays FP64 via rowscale)
+            auto unscale = [&](const SellPattern& pat, const std::vector<double>& src) {
+                std::vector<float> out(src.size(), 0.0f);
+                for (int64_t s = 0; s < pat.nslices; ++s)
+                    for (int lane = 0; lane < kSlice; ++lane) {
+                        int64_t r = s * kSlice + lane;
+                        if (r >= m->np) continue;
+                        double sc = rs[r];
+                        for (int32_t k = 0; k < pat.width[s]; ++k) {
+                            int64_t slot = pat.slice_ptr[s] + (int64_t)k * kSlice + lane;
+                            out[slot] = sc != 0 ? (float)(src[slot] / sc) : 0.0f;
+                        }
                     }
-                }
-            p->d_val32.upload(A32);
+                return out;
+            };
+            p->d_val32.upload(unscale(m->pat, E));
+            p->d_kval32.upload(unscale(m->pat_off, A));
             p->d_rowscale.upload(rs);
+            p->d_u32.alloc(sizeof(float) * m->np);
         }
     }
     *out = p.release();

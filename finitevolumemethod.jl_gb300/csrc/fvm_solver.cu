@@ -339,6 +339,23 @@ __global__ void __launch_bounds__(kRedBlock) bicg_start_kernel(T* rhat, const T*
     }
 }
 
+// After a reliable update replaced r by the true residual: rho' = rhat . r, and the pending
+// beta is rescaled to it (beta = (rho'/rho_old) (alpha/omega) with the recurrence rho replaced).
+template <class T>
+__global__ void __launch_bounds__(kRedBlock) bicg_rho_fix_kernel(const T* rhat, const T* r, int64_t n, double* part,
+                                                                 KState* st) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    double d[1] = {0.0};
+    if (i < n) d[0] = (double)(rhat[i] * r[i]);
+    bool last;
+    block_reduce_publish<1>(d, part, st, gridDim.x, last);
+    if (last && threadIdx.x == 0) {
+        if (st->rho != 0.0) st->beta *= d[0] / st->rho;
+        st->rho = d[0];
+        if (d[0] == 0.0) st->breakdown = 1;
+    }
+}
+
 template <class T>
 __global__ void to_type_kernel(T* dst, const double* src, int64_t n) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -557,12 +574,14 @@ static void run_krylov(fvm_template* Tm, Solver& S, bool cg, bool mixed, const f
         if (!h.done) continue;
         // reliable update: fold the correction into the FP64 solution, recompute the residual
         accumulate_kernel<T><<<S.nb, kRedBlock, 0, s>>>(S.z64, v.x, 1.0, n);
-        bool restart = !cg || h.breakdown;
+        bool restart = h.breakdown != 0;
+        const double rec = std::sqrt(h.rn2);
+        const int brk = h.breakdown;
         double rn_new = true_residual(restart);
         if (trace)
             std::fprintf(stderr, "[fvm solver] %s %s it=%lld rn=%.3e (recurrence %.3e) breakdown=%d\n",
                          cg ? "cg" : "bicgstab", mixed ? "mixed" : "fp64", (long long)it, rn_new / Tm->bnorm,
-                         std::sqrt(h.rn2) / Tm->bnorm, h.breakdown);
+                         rec / Tm->bnorm, brk);
         if (!(rn_new < rn)) {
             // the correction raised the true residual (inner-precision drift or breakdown):
             // undo it, restart from the FP64 residual with a milder inner reduction
@@ -574,7 +593,16 @@ static void run_krylov(fvm_template* Tm, Solver& S, bool cg, bool mixed, const f
         }
         FVM_CUDA(cudaMemsetAsync(v.x, 0, sizeof(T) * n, s));
         rn = rn_new;
-        if (!cg) need_start = true;
+        if (!cg) {
+            if (restart) {
+                need_start = true;
+            } else {
+                // keep the BiCGStab recurrences; only rho (and the pending beta) follow the new r
+                bicg_rho_fix_kernel<T><<<S.nb, kRedBlock, 0, s>>>(v.rhat, v.r, n, S.part, S.st);
+                read_state();
+                if (h.breakdown) need_start = true;
+            }
+        }
         if (rn < 0.9 * best) {
             best = rn;
             stagnation = 0;
@@ -606,7 +634,9 @@ extern "C" int fvm_template_steady_solve(fvm_template* Tm, double* x, const fvm_
         st.symmetric = Tm->symmetric;
         if (opt->precond != FVM_PRECOND_JACOBI) fail(FVM_ERR_INVALID_ARGUMENT, "only the Jacobi preconditioner is available");
         Solver S(Tm, s);
-        size_t elem = mixed ? sizeof(float) : sizeof(double);
+        // vectors sized for FP64 even in mixed mode: a stalled mixed solve finishes in FP64
+        // (run_krylov<double, double>) on the same workspace
+        size_t elem = sizeof(double);
         size_t bytes = sizeof(KState) + sizeof(double) * 8 * (size_t)std::max(S.nb, S.nbs) + sizeof(double) * 3 * n +
                        elem * 8 * n + 256;
         S.ws.alloc(bytes);

@@ -110,6 +110,16 @@ static void assemble_template(fvm_template* T) {
         }
 }
 
+// FP32 copy of the template values and the FP32 gather buffer (first FP32 use)
+static void ensure_fp32(fvm_template* T) {
+    if (!T->d_val32.p) {
+        std::vector<float> v32(T->val.size());
+        for (size_t i = 0; i < v32.size(); ++i) v32[i] = (float)T->val[i];
+        T->d_val32.upload(v32);
+    }
+    if (!T->d_u32.p) T->d_u32.alloc(sizeof(float) * T->prob->mesh->np);
+}
+
 extern "C" {
 
 int fvm_template_create(fvm_problem* prob, int32_t kind, fvm_template** out) {
@@ -189,12 +199,10 @@ int fvm_template_apply(fvm_template* T, const double* u, double* du, int32_t pre
             dout = p->d_du.as<double>();
         }
         if (precision == FVM_FP32) {
-            if (!T->d_val32.p) {
-                std::vector<float> v32(T->val.size());
-                for (size_t i = 0; i < v32.size(); ++i) v32[i] = (float)T->val[i];
-                T->d_val32.upload(v32);
-            }
-            launch_sell_apply32(m->pat, T->d_val32.as<float>(), uin, dout, nullptr, T->d_b.as<double>(), nullptr, s);
+            ensure_fp32(T);
+            launch_to_f32(uin, T->d_u32.as<float>(), m->np, s);
+            launch_sell_apply32(m->pat, T->d_val32.as<float>(), T->d_u32.as<float>(), uin, dout, nullptr,
+                                T->d_b.as<double>(), nullptr, s);
         } else {
             launch_sell_apply64(m->pat, T->d_val64.as<double>(), uin, dout, nullptr, T->d_b.as<double>(), nullptr, s);
         }
@@ -228,16 +236,14 @@ int fvm_template_tsit5_solve(fvm_template* T, const double* u0, const fvm_ode_op
         FVM_CUDA(cudaMemcpyAsync(d_ref, u0, sizeof(double) * n, cudaMemcpyHostToDevice, s));
         launch_permute_in(m->d_perm.as<int32_t>(), d_ref, d_u0, n, s);
         const bool fp32 = opt->precision == FVM_FP32;
-        if (fp32 && !T->d_val32.p) {
-            std::vector<float> v32(T->val.size());
-            for (size_t i = 0; i < v32.size(); ++i) v32[i] = (float)T->val[i];
-            T->d_val32.upload(v32);
-        }
+        if (fp32) ensure_fp32(T);
         OdeRhs rhs;
         rhs.f = [T, m, fp32](const double* u, double* du, double, cudaStream_t st) {
-            if (fp32)
-                launch_sell_apply32(m->pat, T->d_val32.as<float>(), u, du, nullptr, T->d_b.as<double>(), nullptr, st);
-            else
+            if (fp32) {
+                launch_to_f32(u, T->d_u32.as<float>(), m->np, st);
+                launch_sell_apply32(m->pat, T->d_val32.as<float>(), T->d_u32.as<float>(), u, du, nullptr,
+                                    T->d_b.as<double>(), nullptr, st);
+            } else
                 launch_sell_apply64(m->pat, T->d_val64.as<double>(), u, du, nullptr, T->d_b.as<double>(), nullptr, st);
         };
         tsit5_run_internal(rhs, n, d_u0, *opt, d_out.as<double>(), stats, s);

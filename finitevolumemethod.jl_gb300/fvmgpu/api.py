@@ -476,7 +476,7 @@ def _prob_of(p):
     return getattr(p, "prob")
 
 
-def fvm_eqs(du, u, p, t, *, force_triangle=False, internal=False, stream=None):
+def fvm_eqs(du, u, p, t, *, force_triangle=False, conservative=False, internal=False, stream=None):
     """fvm_eqs!(du, u, p, t) (src/equations/main_equations.jl:28-81).  `p` is the problem or
     any object / dict with a `prob` entry.  du, u: float64 numpy arrays (host) or CUDA torch
     tensors (device), caller numbering; internal=True takes device tensors already in the
@@ -493,7 +493,8 @@ def fvm_eqs(du, u, p, t, *, force_triangle=False, internal=False, stream=None):
         if ul != _lib.FVM_PTR_DEVICE:
             raise TypeError("internal=True needs device tensors")
         ul = _lib.FVM_PTR_DEVICE_INTERNAL
-    flags = ul | (_lib.FVM_RHS_FORCE_TRIANGLE if force_triangle else 0)
+    flags = ul | (_lib.FVM_RHS_FORCE_TRIANGLE if force_triangle else 0) | (
+        _lib.FVM_RHS_CONSERVATIVE if conservative else 0)
     s = stream if stream is not None else _lib.current_stream_handle()
     check(load().fvm_rhs(prob.handle, up, dp, float(t), flags, s))
     return du
@@ -723,7 +724,7 @@ class KrylovSolver:
     method: str = "auto"
     rtol: float = 1e-10
     max_iters: int = 1_000_000
-    inner_reduction: float = 1e-2
+    inner_reduction: float = 1e-1
 
 
 @dataclass

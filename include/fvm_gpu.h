@@ -46,6 +46,8 @@ extern "C" {
 #define FVM_PTR_DEVICE 1           /* device arrays, reference numbering */
 #define FVM_PTR_DEVICE_INTERNAL 2  /* device arrays, internal (Hilbert) numbering */
 #define FVM_RHS_FORCE_TRIANGLE 16  /* evaluate by the per-triangle flux kernel even for linear forms */
+#define FVM_RHS_CONSERVATIVE 32    /* linear forms in difference form sum_j K_ij (u_j - u_i): constant fields
+                                      carry exactly zero flux (one more FP64 instruction per neighbour) */
 
 /* ---- precision ---------------------------------------------------------------------- */
 #define FVM_FP64 0

@@ -47,6 +47,41 @@ def oracle_problem(s: Spec) -> O.Problem:
                      source=_bind(s.S, s.Sp) if s.S else None, u0=s.u0, t0=s.t0, tf=s.tf)
 
 
+def rhs_term_scale(prob: O.Problem, u, t):
+    """Per-vertex sum of the magnitudes of the terms fvm_eqs! adds up: for each dual edge
+    |q(|alpha|, |beta|, |gamma|) . n| l with alpha, beta, gamma formed from |s_v u_v|, scattered
+    to both sides; the same for boundary half edges (|Neumann value| l on Neumann edges);
+    divided by V; plus |S| or |Dudt value|.  A floating-point evaluation of the RHS is only
+    defined to within ~eps times this scale, so parity bounds use
+    ||du - ref|| <= tol (||ref|| + ||scale||)."""
+    g = prob.geo
+    T = g.triangles
+    ua = np.abs(np.asarray(u, dtype=np.float64))
+    s = np.abs(g.s)
+    a = s[:, 0] * ua[T[:, 0]] + s[:, 1] * ua[T[:, 1]] + s[:, 2] * ua[T[:, 2]]
+    b = s[:, 3] * ua[T[:, 0]] + s[:, 4] * ua[T[:, 1]] + s[:, 5] * ua[T[:, 2]]
+    c = s[:, 6] * ua[T[:, 0]] + s[:, 7] * ua[T[:, 1]] + s[:, 8] * ua[T[:, 2]]
+    acc = np.zeros(prob.tri.num_points)
+    for e, (a1, a2) in enumerate(((0, 1), (1, 2), (2, 0))):
+        qx, qy = O.call_pointwise(prob.flux, g.mid[:, e, 0], g.mid[:, e, 1], t, a, b, c)
+        m = (np.abs(qx * g.nrm[:, e, 0]) + np.abs(qy * g.nrm[:, e, 1])) * g.length[:, e]
+        np.add.at(acc, T[:, a1], m)
+        np.add.at(acc, T[:, a2], m)
+    be = prob.tri.boundary_edges
+    if be.size:
+        Qi, Qj = O.boundary_fluxes(prob, np.asarray(u, dtype=np.float64) * 0 + ua, t)
+        np.add.at(acc, be[:, 0], np.abs(Qi))
+        np.add.at(acc, be[:, 1], np.abs(Qj))
+    out = acc / np.where(prob.geo.cv_volumes > 0, prob.geo.cv_volumes, 1.0)
+    src = O.source_contributions(prob, np.zeros_like(acc), ua, t)
+    return np.abs(out) + np.abs(src)
+
+
+def parity_error(got, ref, scale):
+    """||got - ref|| / (||ref|| + ||scale||)."""
+    return np.linalg.norm(got - ref) / (np.linalg.norm(ref) + np.linalg.norm(scale))
+
+
 def api_problem(s: Spec, precision="fp64", mesh=None, tile_vertices=0):
     import fvmgpu as F
 

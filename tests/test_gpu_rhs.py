@@ -1,14 +1,17 @@
 """GPU parity of fvm_eqs! (libfvmgpu through the C ABI) against the oracle.
 
-Tolerances: FP64 RHS within 1e-12 relative (normwise, and max-norm relative to max|du|);
-FP32 assembly within 2e-5 relative.  Integer tables (connectivity, classification) bit-exact.
+Tolerances, relative to the size of what is summed: ||du - ref|| <= tol (||ref|| + ||scale||),
+where scale is the per-vertex sum of term magnitudes (problems.rhs_term_scale) - any
+floating-point evaluation, the reference's included, is defined only to ~eps times it.
+FP64: tol = 1e-12 (normwise and max-norm); FP32 assembly: tol = 2e-5.  Integer tables
+(connectivity, classification) bit-exact.
 """
 import numpy as np
 import pytest
 
 import fvm_oracle as O
-from problems import (api_problem, heat_convection, mixed_annulus, nonlinear_rect, oracle_problem, readme_diffusion,
-                      sine_diffusion)
+from problems import (api_problem, heat_convection, mixed_annulus, nonlinear_rect, oracle_problem, parity_error,
+                      readme_diffusion, rhs_term_scale, sine_diffusion)
 
 pytestmark = pytest.mark.gpu
 
@@ -16,9 +19,12 @@ FP64_RTOL = 1e-12
 FP32_RTOL = 2e-5
 
 
-def rel_err(got, ref):
-    den = max(np.linalg.norm(ref), 1e-300)
-    return np.linalg.norm(got - ref) / den, np.max(np.abs(got - ref)) / max(np.max(np.abs(ref)), 1e-300)
+def rel_err(got, ref, scale=None):
+    """(normwise, max-norm) error relative to |ref| + scale."""
+    sc = np.zeros_like(ref) if scale is None else scale
+    e2 = parity_error(got, ref, sc)
+    einf = np.max(np.abs(got - ref)) / max(np.max(np.abs(ref) + sc), 1e-300)
+    return e2, einf
 
 
 BUILDERS = {
@@ -38,31 +44,31 @@ def test_rhs_parity_fp64(gpu_lib, name):
     oprob = oracle_problem(spec)
     rng = np.random.default_rng(11)
     P = spec.tri.points
-    # non-constant fields: on a constant field the reference's own RHS is rounding noise
-    # (alpha = s1 u_i + s2 u_j + s3 u_k cancels to ~1e-12 |s| |u|), see test_constant_field_exact
+    # a smooth field on the problem's own offset, and a rough one
     for trial in range(2):
         if trial == 0:
             u = spec.u0 + 0.05 * np.sin(3 * P[:, 0] + 2 * P[:, 1])
         else:
             u = spec.u0 + rng.standard_normal(spec.tri.num_points) * 0.1
         ref = O.fvm_eqs(oprob, u, spec.t0)
+        scale = rhs_term_scale(oprob, u, spec.t0)
         prob = api_problem(spec)
-        for force in (False, True):
+        for force, cons in ((False, False), (False, True), (True, False)):
             du = np.zeros_like(u)
-            F.fvm_eqs(du, np.ascontiguousarray(u), prob, spec.t0, force_triangle=force)
-            e2, einf = rel_err(du, ref)
-            assert e2 <= FP64_RTOL and einf <= FP64_RTOL, (name, force, e2, einf)
+            F.fvm_eqs(du, np.ascontiguousarray(u), prob, spec.t0, force_triangle=force, conservative=cons)
+            e2, einf = rel_err(du, ref, scale)
+            assert e2 <= FP64_RTOL and einf <= FP64_RTOL, (name, force, cons, e2, einf)
 
 
 def test_constant_field_exact(gpu_lib):
-    """test/equations.jl:37-92 on the GPU: heat convection at T = 10 everywhere.  Interior
-    fluxes vanish exactly (difference form), the corner vertex matches the hand-computed
-    value, and only Neumann boundary rows are non-zero."""
+    """test/equations.jl:37-92 on the GPU: heat convection at T = 10 everywhere.  With
+    FVM_RHS_CONSERVATIVE interior fluxes vanish exactly, the corner vertex matches the
+    hand-computed value, and only Neumann boundary rows are non-zero."""
     import fvmgpu as F
 
     spec = heat_convection(200)
     prob = api_problem(spec)
-    du = F.fvm_eqs(np.zeros(spec.tri.num_points), spec.u0.copy(), prob, 0.0)
+    du = F.fvm_eqs(np.zeros(spec.tri.num_points), spec.u0.copy(), prob, 0.0, conservative=True)
     P = spec.tri.points
     x1, y1 = P[1, 0], P[200, 1]
     A = 0.5 * abs((x1 / 2) * (y1 / 3) - (x1 / 3) * 0.0) + 0.5 * abs((x1 / 3) * (y1 / 2) - 0.0 * (y1 / 3))
@@ -97,12 +103,15 @@ def test_rhs_parity_fp32(gpu_lib, name):
     import fvmgpu as F
 
     spec = BUILDERS[name]()
-    ref = O.fvm_eqs(oracle_problem(spec), spec.u0, 0.0)
+    oprob = oracle_problem(spec)
+    ref = O.fvm_eqs(oprob, spec.u0, 0.0)
+    scale = rhs_term_scale(oprob, spec.u0, 0.0)
     prob = api_problem(spec, precision="fp32")
-    du = np.zeros_like(spec.u0)
-    F.fvm_eqs(du, np.ascontiguousarray(spec.u0, dtype=np.float64), prob, 0.0)
-    e2, _ = rel_err(du, ref)
-    assert e2 <= FP32_RTOL, e2
+    for cons in (False, True):
+        du = np.zeros_like(spec.u0)
+        F.fvm_eqs(du, np.ascontiguousarray(spec.u0, dtype=np.float64), prob, 0.0, conservative=cons)
+        e2, _ = rel_err(du, ref, scale)
+        assert e2 <= FP32_RTOL, (cons, e2)
 
 
 @pytest.mark.parametrize("tile", [64, 256, 1024])
