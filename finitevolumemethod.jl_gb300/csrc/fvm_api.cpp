@@ -75,32 +75,6 @@ static double host_rms(const std::vector<double>& v, const std::vector<double>& 
     return std::sqrt(s / std::max<size_t>(1, v.size()));
 }
 
-// A stream that can be captured: the caller's, or a private one ordered after the legacy
-// default stream (which cannot be captured) and joined back into it on destruction.
-struct CaptureStream {
-    cudaStream_t user, s, own = nullptr;
-    CaptureStream(cudaStream_t u, bool need) : user(u), s(u) {
-        if (!need || u != nullptr) return;
-        FVM_CUDA(cudaStreamCreateWithFlags(&own, cudaStreamNonBlocking));
-        cudaEvent_t e;
-        FVM_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-        FVM_CUDA(cudaEventRecord(e, user));
-        FVM_CUDA(cudaStreamWaitEvent(own, e, 0));
-        cudaEventDestroy(e);
-        s = own;
-    }
-    ~CaptureStream() {
-        if (!own) return;
-        cudaEvent_t e;
-        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess) {
-            cudaEventRecord(e, own);
-            cudaStreamWaitEvent(user, e, 0);
-            cudaEventDestroy(e);
-        }
-        cudaStreamDestroy(own);
-    }
-};
-
 // Tsit5 driver.  u0_int: device, internal numbering.  out_int: device [nsave][n] internal.
 static void tsit5_run(OdeRhs& rhs, int64_t n, const double* u0_int, const fvm_ode_options& o, double* out_int,
                       fvm_ode_stats* st, cudaStream_t user_stream) {

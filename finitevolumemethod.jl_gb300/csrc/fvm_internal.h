@@ -69,6 +69,8 @@ struct SellPattern {
     DBuf d_slice_ptr, d_width, d_col;
     // slot of (row, col), or -1
     int64_t find(int32_t row, int32_t c) const;
+    // CSR position of (row, col), or -1
+    int64_t find_csr(int32_t row, int32_t c) const;
 };
 
 // ---- mesh ----------------------------------------------------------------------------
@@ -177,6 +179,41 @@ void launch_hermite(double* out, const double* u0, const double* u1, const doubl
                     double dt, double theta, int64_t n, cudaStream_t s);
 // Krylov helpers
 void launch_fill(double* x, double v, int64_t n, cudaStream_t s);
+
+}  // namespace fvm
+
+// Linear terms of a problem's RHS: emit(row, col, coef, didx, flux), rows and columns in the
+// caller's numbering; the coefficient multiplies D[didx] when didx >= 0 (fvm_problem.cpp).
+using LinearTermSink = std::function<void(int32_t, int32_t, double, int64_t, bool)>;
+void fvm_visit_linear_terms(const fvm_problem* p, const LinearTermSink& emit, std::vector<double>& b,
+                            std::vector<double>& q, std::vector<double>& rowscale);
+
+namespace fvm {
+// A stream that can be captured: the caller's, or a private one ordered after the legacy
+// default stream (which cannot be captured) and joined back into it on destruction.
+struct CaptureStream {
+    cudaStream_t user, s, own = nullptr;
+    CaptureStream(cudaStream_t u, bool need) : user(u), s(u) {
+        if (!need || u != nullptr) return;
+        FVM_CUDA(cudaStreamCreateWithFlags(&own, cudaStreamNonBlocking));
+        cudaEvent_t e;
+        FVM_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        FVM_CUDA(cudaEventRecord(e, user));
+        FVM_CUDA(cudaStreamWaitEvent(own, e, 0));
+        cudaEventDestroy(e);
+        s = own;
+    }
+    ~CaptureStream() {
+        if (!own) return;
+        cudaEvent_t e;
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess) {
+            cudaEventRecord(e, own);
+            cudaStreamWaitEvent(user, e, 0);
+            cudaEventDestroy(e);
+        }
+        cudaStreamDestroy(own);
+    }
+};
 
 // Right-hand side in the internal numbering plus the per-step callback (Dirichlet update).
 struct OdeRhs {

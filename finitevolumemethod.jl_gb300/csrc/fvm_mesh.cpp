@@ -9,12 +9,17 @@
 
 namespace fvm {
 
-int64_t SellPattern::find(int32_t row, int32_t c) const {
+int64_t SellPattern::find_csr(int32_t row, int32_t c) const {
     int64_t lo = rowptr[row], hi = rowptr[row + 1];
     const int32_t* b = csr_col.data();
     const int32_t* it = std::lower_bound(b + lo, b + hi, c);
     if (it == b + hi || *it != c) return -1;
-    return csr_slot[it - b];
+    return it - b;
+}
+
+int64_t SellPattern::find(int32_t row, int32_t c) const {
+    int64_t q = find_csr(row, c);
+    return q < 0 ? -1 : csr_slot[q];
 }
 
 // Hilbert index of (x, y) on a 2^16 x 2^16 grid (the standard rotate-and-reflect walk).

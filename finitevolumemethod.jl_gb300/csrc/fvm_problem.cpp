@@ -17,60 +17,39 @@ void fvm_problem::ensure_work() {
     if (!d_ref.p) d_ref.alloc(sizeof(double) * m->np);
 }
 
-// Linear operator values of the generic RHS (fvm_eqs!), in the internal numbering.
-// Row i of a FREE vertex: (sum of triangle and boundary fluxes)/V_i + S_i
-// (triangle_contributions.jl:10-15, boundary_edge_contributions.jl:61-65,
-// source_contributions.jl:41), with every flux linear in u:
+// Linear terms of the generic RHS (fvm_eqs!).  Row i of a FREE vertex is
+// (sum of triangle and boundary fluxes)/V_i + S_i (triangle_contributions.jl:10-15,
+// boundary_edge_contributions.jl:61-65, source_contributions.jl:41), every flux linear in u:
 //   triangle dual edge e of T = (a, b, c): Q_e = -D_e l_e (alpha n_x + beta n_y)
 //   boundary half edge (non-Neumann):      Q_h = -D_h l_h (alpha n_x + beta n_y)
 //   boundary half edge (Neumann, a = n0 + n1 u(m)): Q_h = l_h (n0 + n1 u(m)).
-// Two equivalent storages are produced from the same contributions:
-//  explicit (pattern with the diagonal): du_i = sum_j A_ij u_j + b_i + q_i u_i^2, one FP64
-//    FMA per entry (GB300 runs FP64 at 1/58 of the FP32 rate, so this is the default);
-//  difference form (off-diagonal pattern): du_i = sum_{j != i} K_ij (u_j - u_i) + d_i u_i
-//    + b_i + q_i u_i^2.  A dual-edge flux is a combination of u whose coefficients sum to
-//    zero (constant u carries no flux), so its diagonal coefficient is implied and dropped:
-//    constant fields give exactly zero flux.  Non-flux terms (Neumann u(m) dependence, source,
-//    Dudt) keep their full row sum in d_i.
-static void assemble_generic(fvm_problem* p, std::vector<double>& E, std::vector<double>& A, std::vector<double>& dg,
-                             std::vector<double>& b, std::vector<double>& q, std::vector<double>& rowscale) {
+// The visitor reports each coefficient as emit(row, col, coef, didx, flux) (caller numbering):
+// the contribution to A_row,col is coef * D[didx] when didx >= 0 (D indexed over the dual edges,
+// 3 per triangle, then the boundary quarter points, 2 per edge), coef otherwise.  `flux` marks
+// dual-edge fluxes, whose coefficients along a row sum to zero.  Constant terms go to b,
+// quadratic ones to q; rowscale is 1/V on FREE rows, 1 on Dudt rows.
+void fvm_visit_linear_terms(const fvm_problem* p, const LinearTermSink& emit, std::vector<double>& b,
+                            std::vector<double>& q, std::vector<double>& rowscale) {
     const fvm_mesh* m = p->mesh;
-    const SellPattern& pat = m->pat_off;
-    const SellPattern& pate = m->pat;
-    E.assign(pate.nslots, 0.0);
-    A.assign(pat.nslots, 0.0);
-    dg.assign(m->np, 0.0);
     b.assign(m->np, 0.0);
     q.assign(m->np, 0.0);
     rowscale.assign(m->np, 0.0);
-    auto flux = [&](int32_t r, int32_t c, double v) {
-        E[pate.find(m->iperm[r], m->iperm[c])] += v;
-        if (r != c) A[pat.find(m->iperm[r], m->iperm[c])] += v;
-    };
-    auto lin = [&](int32_t r, int32_t c, double v) {
-        E[pate.find(m->iperm[r], m->iperm[c])] += v;
-        if (r != c) A[pat.find(m->iperm[r], m->iperm[c])] += v;
-        dg[m->iperm[r]] += v;
-    };
-    auto add = flux;
-    const int nd = p->dif_deg + 1;
     for (int64_t t = 0; t < m->nt; ++t) {
         const int32_t* w = &m->tri[3 * t];
         const double* pr = &m->props[24 * t];
         for (int e = 0; e < 3; ++e) {
             int32_t e1 = w[e], e2 = w[(e + 1) % 3];
-            double D = p->dualD.empty() ? 0.0 : p->dualD[(3 * t + e) * nd];
-            double Dl = D * pr[21 + e];
-            double nx = pr[15 + 2 * e], ny = pr[16 + 2 * e];
+            double l = pr[21 + e], nx = pr[15 + 2 * e], ny = pr[16 + 2 * e];
             bool f1 = p->code[e1] == FVM_VERTEX_FREE, f2 = p->code[e2] == FVM_VERTEX_FREE;
             for (int v = 0; v < 3; ++v) {
-                double a = Dl * (pr[v] * nx + pr[3 + v] * ny);
-                if (f1) add(e1, w[v], a / m->vol[e1]);
-                if (f2) add(e2, w[v], -a / m->vol[e2]);
+                double a = l * (pr[v] * nx + pr[3 + v] * ny);
+                if (f1) emit(e1, w[v], a / m->vol[e1], 3 * t + e, true);
+                if (f2) emit(e2, w[v], -a / m->vol[e2], 3 * t + e, true);
             }
         }
     }
     const int nn = p->neu_deg + 1;
+    const int64_t q0 = 3 * m->nt;
     for (int64_t e = 0; e < m->nbe; ++e) {
         int32_t i = m->be[2 * e], j = m->be[2 * e + 1];
         double px = m->pts[2 * i], py = m->pts[2 * i + 1], qx = m->pts[2 * j], qy = m->pts[2 * j + 1];
@@ -87,15 +66,15 @@ static void assemble_generic(fvm_problem* p, std::vector<double>& E, std::vector
             if (fi) {
                 b[m->iperm[i]] -= lh * n0i / m->vol[i];
                 if (n1i != 0) {
-                    lin(i, i, -lh * n1i * 0.75 / m->vol[i]);
-                    lin(i, j, -lh * n1i * 0.25 / m->vol[i]);
+                    emit(i, i, -lh * n1i * 0.75 / m->vol[i], -1, false);
+                    emit(i, j, -lh * n1i * 0.25 / m->vol[i], -1, false);
                 }
             }
             if (fj) {
                 b[m->iperm[j]] -= lh * n0j / m->vol[j];
                 if (n1j != 0) {
-                    lin(j, i, -lh * n1j * 0.25 / m->vol[j]);
-                    lin(j, j, -lh * n1j * 0.75 / m->vol[j]);
+                    emit(j, i, -lh * n1j * 0.25 / m->vol[j], -1, false);
+                    emit(j, j, -lh * n1j * 0.75 / m->vol[j], -1, false);
                 }
             }
             continue;
@@ -103,12 +82,10 @@ static void assemble_generic(fvm_problem* p, std::vector<double>& E, std::vector
         int32_t t = m->btri[e];
         const int32_t* w = &m->tri[3 * t];
         const double* pr = &m->props[24 * t];
-        double Di = p->quarterD.empty() ? 0.0 : p->quarterD[(2 * e) * nd];
-        double Dj = p->quarterD.empty() ? 0.0 : p->quarterD[(2 * e + 1) * nd];
         for (int v = 0; v < 3; ++v) {
             double c = lh * (pr[v] * nx + pr[3 + v] * ny);
-            if (fi) add(i, w[v], Di * c / m->vol[i]);
-            if (fj) add(j, w[v], Dj * c / m->vol[j]);
+            if (fi) emit(i, w[v], c / m->vol[i], q0 + 2 * e, true);
+            if (fj) emit(j, w[v], c / m->vol[j], q0 + 2 * e + 1, true);
         }
     }
     const int ns = p->src_deg + 1, nu = p->dudt_deg + 1;
@@ -119,18 +96,51 @@ static void assemble_generic(fvm_problem* p, std::vector<double>& E, std::vector
             rowscale[r] = 1.0 / m->vol[v];
             if (!p->src.empty()) {
                 b[r] += p->src[v * ns];
-                if (ns > 1 && p->src[v * ns + 1] != 0) lin((int32_t)v, (int32_t)v, p->src[v * ns + 1]);
+                if (ns > 1 && p->src[v * ns + 1] != 0) emit((int32_t)v, (int32_t)v, p->src[v * ns + 1], -1, false);
                 if (ns > 2) q[r] = p->src[v * ns + 2];
             }
         } else if (c == FVM_VERTEX_DUDT) {
             rowscale[r] = 1.0;
             if (!p->dudt.empty()) {
                 b[r] = p->dudt[v * nu];
-                if (nu > 1 && p->dudt[v * nu + 1] != 0) lin((int32_t)v, (int32_t)v, p->dudt[v * nu + 1]);
+                if (nu > 1 && p->dudt[v * nu + 1] != 0) emit((int32_t)v, (int32_t)v, p->dudt[v * nu + 1], -1, false);
                 if (nu > 2) q[r] = p->dudt[v * nu + 2];
             }
         }
     }
+}
+
+// Two equivalent storages are produced from the same contributions:
+//  explicit (pattern with the diagonal): du_i = sum_j A_ij u_j + b_i + q_i u_i^2, one FP64
+//    FMA per entry (GB300 runs FP64 at 1/58 of the FP32 rate, so this is the default);
+//  difference form (off-diagonal pattern): du_i = sum_{j != i} K_ij (u_j - u_i) + d_i u_i
+//    + b_i + q_i u_i^2.  A dual-edge flux is a combination of u whose coefficients sum to
+//    zero (constant u carries no flux), so its diagonal coefficient is implied and dropped:
+//    constant fields give exactly zero flux.  Non-flux terms (Neumann u(m) dependence, source,
+//    Dudt) keep their full row sum in d_i.
+static void assemble_generic(fvm_problem* p, std::vector<double>& E, std::vector<double>& A, std::vector<double>& dg,
+                             std::vector<double>& b, std::vector<double>& q, std::vector<double>& rowscale) {
+    const fvm_mesh* m = p->mesh;
+    const SellPattern& pat = m->pat_off;
+    const SellPattern& pate = m->pat;
+    E.assign(pate.nslots, 0.0);
+    A.assign(pat.nslots, 0.0);
+    dg.assign(m->np, 0.0);
+    const int nd = p->dif_deg + 1;
+    const int64_t q0 = 3 * m->nt;
+    auto Dval = [&](int64_t idx) {
+        if (idx < q0) return p->dualD.empty() ? 0.0 : p->dualD[idx * nd];
+        return p->quarterD.empty() ? 0.0 : p->quarterD[(idx - q0) * nd];
+    };
+    fvm_visit_linear_terms(
+        p,
+        [&](int32_t r, int32_t c, double coef, int64_t didx, bool flux) {
+            double v = didx >= 0 ? coef * Dval(didx) : coef;
+            E[pate.find(m->iperm[r], m->iperm[c])] += v;
+            if (r != c) A[pat.find(m->iperm[r], m->iperm[c])] += v;
+            if (!flux) dg[m->iperm[r]] += v;
+        },
+        b, q, rowscale);
 }
 
 extern "C" int fvm_problem_create_impl(fvm_mesh* mesh, const fvm_problem_desc* d, fvm_problem** out) {

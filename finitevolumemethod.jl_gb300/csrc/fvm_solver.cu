@@ -613,8 +613,12 @@ static void run_krylov(fvm_template* Tm, Solver& S, bool cg, bool mixed, const f
     }
     stats.iterations += it;
     stats.rel_residual = Tm->bnorm > 0 ? rn / Tm->bnorm : rn;
-    if (rn > tol) fail(FVM_ERR_NOT_CONVERGED, "steady solve did not reach rtol (relative residual " +
-                                                  std::to_string(stats.rel_residual) + ")");
+    if (rn > tol) {
+        char msg[160];
+        std::snprintf(msg, sizeof msg, "steady solve did not reach rtol %.3e (relative residual %.3e after %lld iterations)",
+                      o.rtol, stats.rel_residual, (long long)stats.iterations);
+        fail(FVM_ERR_NOT_CONVERGED, msg);
+    }
 }
 
 extern "C" int fvm_template_steady_solve(fvm_template* Tm, double* x, const fvm_solver_options* opt,

@@ -3,11 +3,12 @@
 The compute path is libfvmgpu.so (hand-written sm_103a CUDA kernels behind the C ABI of
 include/fvm_gpu.h); this package is the host-side mirror of the reference interface.
 """
-from .meshes import Triangulation, triangulate_rectangle, triangulate_annulus, triangulate_disk, triangulate_points
+from .meshes import (Triangulation, triangulate_rectangle, triangulate_annulus, triangulate_disk, triangulate_points,
+                     disjoint_union)
 from .api import (ConditionType, Neumann, Dudt, Dirichlet, Constrained, ParametrisedFunction, BoundaryConditions,
                   InternalConditions, Conditions, TriangleProperties, FVMGeometry, FVMProblem, fvm_eqs,
                   update_dirichlet_nodes, DiffusionEquation, LinearReactionDiffusionEquation, PoissonsEquation,
-                  MeanExitTimeProblem, Tsit5, KrylovSolver, ODESolution, LinearSolution, solve)
+                  MeanExitTimeProblem, Tsit5, KrylovSolver, ODESolution, LinearSolution, solve, BatchedProblem)
 from ._lib import FVMError, UnsupportedFormError, NotConvergedError
 from ._build import build, lib_path
 
@@ -16,6 +17,7 @@ __all__ = [
     "ConditionType", "Neumann", "Dudt", "Dirichlet", "Constrained", "ParametrisedFunction", "BoundaryConditions",
     "InternalConditions", "Conditions", "TriangleProperties", "FVMGeometry", "FVMProblem", "fvm_eqs",
     "update_dirichlet_nodes", "DiffusionEquation", "LinearReactionDiffusionEquation", "PoissonsEquation",
-    "MeanExitTimeProblem", "Tsit5", "KrylovSolver", "ODESolution", "LinearSolution", "solve", "FVMError",
+    "MeanExitTimeProblem", "Tsit5", "KrylovSolver", "ODESolution", "LinearSolution", "solve", "BatchedProblem",
+    "disjoint_union", "FVMError",
     "UnsupportedFormError", "NotConvergedError", "build", "lib_path",
 ]

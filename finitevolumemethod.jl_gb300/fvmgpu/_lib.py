@@ -129,6 +129,13 @@ SIGNATURES = {
     "fvm_dirichlet_apply": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_int32, C.c_void_p]),
     "fvm_tsit5_solve": (C.c_int, [C.c_void_p, c_double_p, C.POINTER(OdeOptions), c_double_p, C.POINTER(OdeStats),
                                   C.c_void_p]),
+    "fvm_batch_create": (C.c_int, [C.c_void_p, C.c_int32, c_double_p, c_double_p, C.c_int32,
+                                   C.POINTER(C.c_void_p)]),
+    "fvm_batch_destroy": (C.c_int, [C.c_void_p]),
+    "fvm_batch_rhs": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int32, C.c_void_p]),
+    "fvm_batch_tsit5_solve": (C.c_int, [C.c_void_p, c_double_p, C.POINTER(OdeOptions), c_double_p,
+                                        C.POINTER(OdeStats), C.c_void_p]),
+    "fvm_batch_tuning": (C.c_int, [C.c_void_p, c_int32_p]),
     "fvm_template_create": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p)]),
     "fvm_template_destroy": (C.c_int, [C.c_void_p]),
     "fvm_template_export": (C.c_int, [C.c_void_p, c_int64_p, c_int32_p, c_int32_p, c_double_p, c_double_p]),
@@ -209,19 +216,19 @@ def as_i8(a) -> np.ndarray:
     return np.ascontiguousarray(np.asarray(a, dtype=np.int8))
 
 
-def array_pointer(x):
+def array_pointer(x, dtype="float64"):
     """(void pointer, location flag) of a numpy array (host) or a CUDA torch tensor (device)."""
     if isinstance(x, np.ndarray):
-        if x.dtype != np.float64 or not x.flags.c_contiguous:
-            raise TypeError("host arrays must be contiguous float64")
+        if x.dtype != np.dtype(dtype) or not x.flags.c_contiguous:
+            raise TypeError(f"host arrays must be contiguous {dtype}")
         return C.c_void_p(x.ctypes.data), FVM_PTR_HOST
     try:
         import torch
     except ImportError:  # pragma: no cover
         torch = None
     if torch is not None and isinstance(x, torch.Tensor):
-        if x.dtype != torch.float64 or not x.is_contiguous():
-            raise TypeError("tensors must be contiguous float64")
+        if x.dtype != getattr(torch, dtype) or not x.is_contiguous():
+            raise TypeError(f"tensors must be contiguous {dtype}")
         if x.is_cuda:
             return C.c_void_p(x.data_ptr()), FVM_PTR_DEVICE
         return C.c_void_p(x.data_ptr()), FVM_PTR_HOST

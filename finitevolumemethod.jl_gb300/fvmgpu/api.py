@@ -509,6 +509,91 @@ def update_dirichlet_nodes(u, prob, t=0.0, stream=None):
 
 
 # --------------------------------------------------------------------------------------
+# batched instances
+# --------------------------------------------------------------------------------------
+class BatchedProblem:
+    """B instances of a linear FVMProblem that differ only in their diffusion field
+    D_b(x, y) (what the reference would run as B FVMProblems, e.g. an EnsembleProblem).
+
+    State arrays are (npoints, B), instance index fastest.  `diffusion_functions` is a
+    sequence of closures D_b(x, y, t, u, p) of (x, y) alone, sampled at the dual-edge midpoints
+    and boundary quarter points, or an array (B, 3 ntri + 2 nbedge) of those samples.
+    precision "fp32" keeps values, state and accumulation in FP32."""
+
+    def __init__(self, prob: FVMProblem, diffusion_functions, diffusion_parameters=None, precision="fp64"):
+        mesh = prob.mesh
+        tri = mesh.triangulation
+        nd, nq = 3 * tri.num_triangles, 2 * tri.num_boundary_edges
+        if isinstance(diffusion_functions, np.ndarray):
+            Dall = np.ascontiguousarray(diffusion_functions, dtype=np.float64)
+            if Dall.ndim != 2 or Dall.shape[1] != nd + nq:
+                raise ValueError(f"D samples must be (B, {nd + nq})")
+        else:
+            dual, quarter = mesh.sample_points()
+            pts = np.concatenate([dual.reshape(-1, 2), quarter.reshape(-1, 2)])
+            rows = []
+            for Db in diffusion_functions:
+                c, deg = classify_xytu(ParametrisedFunction(Db, diffusion_parameters), pts[:, 0], pts[:, 1],
+                                       prob.initial_time, "batched diffusion_function", max_degree=0)
+                rows.append(c[:, 0])
+            Dall = np.ascontiguousarray(np.stack(rows))
+        self.prob, self.B = prob, Dall.shape[0]
+        self.precision = _precision(precision)
+        self.dtype = np.float32 if self.precision == FVM_FP32 else np.float64
+        dualD = np.ascontiguousarray(Dall[:, :nd])
+        quarterD = np.ascontiguousarray(Dall[:, nd:]) if nq else None
+        h = C.c_void_p()
+        check(load().fvm_batch_create(prob.handle, self.B, dptr(dualD), dptr(quarterD) if quarterD is not None else None,
+                                      self.precision, C.byref(h)))
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def rhs(self, du, u, t=0.0, internal=False, stream=None):
+        """du[:, b] = fvm_eqs!(u[:, b]) for every instance."""
+        dt = "float32" if self.precision == FVM_FP32 else "float64"
+        up, ul = _lib.array_pointer(u, dt)
+        dp, dl = _lib.array_pointer(du, dt)
+        if ul != dl:
+            raise TypeError("u and du must both be host arrays or both device tensors")
+        if internal:
+            if ul != _lib.FVM_PTR_DEVICE:
+                raise TypeError("internal=True needs device tensors")
+            ul = _lib.FVM_PTR_DEVICE_INTERNAL
+        s = stream if stream is not None else _lib.current_stream_handle()
+        check(load().fvm_batch_rhs(self._h, up, dp, float(t), ul, s))
+        return du
+
+    def tuning(self):
+        a = np.zeros(3, dtype=np.int32)
+        check(load().fvm_batch_tuning(self._h, dptr(a, _lib.c_int32_p)))
+        return {"block": int(a[0]), "instances_per_thread": int(a[1]), "grid": int(a[2])}
+
+    def solve(self, u0, dt, saveat=None, use_graph=True, stream=None):
+        """Fixed-step Tsit5 on every instance; returns (times, array (nsave, npoints, B), stats)."""
+        p = self.prob
+        ts = _saveat_times(saveat, p.initial_time, p.final_time) if saveat is not None else np.array([p.final_time])
+        n = p.mesh.triangulation.num_points
+        u0c = np.ascontiguousarray(np.broadcast_to(np.asarray(u0, dtype=np.float64).reshape(n, -1), (n, self.B)))
+        out = np.empty((ts.size, n, self.B))
+        o = _lib.OdeOptions()
+        o.t0, o.tf, o.dt, o.adaptive = p.initial_time, p.final_time, float(dt), 0
+        tsc = as_f64(ts)
+        o.saveat, o.nsave, o.use_graph = dptr(tsc), ts.size, 1 if use_graph else 0
+        st = _lib.OdeStats()
+        s = stream if stream is not None else _lib.current_stream_handle()
+        check(load().fvm_batch_tsit5_solve(self._h, dptr(u0c), C.byref(o), dptr(out), C.byref(st), s))
+        return ts, out, {"steps": st.naccept, "nrhs": st.nrhs, "elapsed_ms": st.elapsed_ms}
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib._LIB is not None:
+            _lib._LIB.fvm_batch_destroy(self._h)
+            self._h = None
+
+
+# --------------------------------------------------------------------------------------
 # templates (src/specific_problems/)
 # --------------------------------------------------------------------------------------
 class _Template:

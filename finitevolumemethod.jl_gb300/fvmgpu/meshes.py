@@ -105,6 +105,25 @@ class Triangulation:
         self.boundary_adjacent = third[order[pos]] if q.size else np.zeros(0, dtype=np.int64)
 
 
+def disjoint_union(tris):
+    """One Triangulation holding several meshes side by side (no shared points).
+
+    Mesh m's points are offset by the point counts of the meshes before it; its boundary
+    segments follow those of the meshes before it.  A problem on the union is block-diagonal,
+    so one launch per RHS (one captured graph per Tsit5 step) advances every mesh: the
+    multi-mesh batch of uneven sizes.  Returns (union, point offsets, segment offsets)."""
+    pts, trs, segs = [], [], []
+    poff, soff = [0], [0]
+    for t in tris:
+        o = poff[-1]
+        pts.append(t.points)
+        trs.append(t.triangles + o)
+        segs += [np.asarray(s) + o for s in t.boundary_nodes]
+        poff.append(o + t.num_points)
+        soff.append(soff[-1] + t.num_ghost_vertices)
+    return Triangulation(np.concatenate(pts), np.concatenate(trs), segs), np.array(poff), np.array(soff)
+
+
 def _orient_ccw(points, tris):
     p, q, r = points[tris[:, 0]], points[tris[:, 1]], points[tris[:, 2]]
     det = (q[:, 0] - p[:, 0]) * (r[:, 1] - p[:, 1]) - (q[:, 1] - p[:, 1]) * (r[:, 0] - p[:, 0])

@@ -183,6 +183,29 @@ typedef struct fvm_ode_stats {
 int fvm_tsit5_solve(fvm_problem* prob, const double* u0, const fvm_ode_options* opt, double* out,
                     fvm_ode_stats* stats, void* stream);
 
+/* ---- batched instances (many parameter sets on one mesh) -------------------------------- */
+/* B instances of one linear problem that differ in their diffusion field D_b(x, y), the
+ * batched counterpart of solving B FVMProblems (an EnsembleProblem over D in the reference).
+ * State is laid out [npoints][batch] (batch fastest) so the mesh is read once for all
+ * instances.  prob supplies conditions, Neumann / source / Dudt / Dirichlet forms (shared);
+ * its own D is ignored.
+ *   dual_edge_D [batch][ntri*3], quarter_D [batch][nbedge*2] (NULL when no boundary edge uses D)
+ *   precision   FVM_FP64, or FVM_FP32 (FP32 values, state and accumulation) */
+typedef struct fvm_batch fvm_batch;
+int fvm_batch_create(fvm_problem* prob, int32_t batch, const double* dual_edge_D, const double* quarter_D,
+                     int32_t precision, fvm_batch** out);
+int fvm_batch_destroy(fvm_batch* b);
+/* du_b = fvm_eqs!(u_b) for every instance; u, du [npoints][batch] of the batch's precision, in
+ * the caller's numbering (FVM_PTR_HOST / FVM_PTR_DEVICE) or internal (FVM_PTR_DEVICE_INTERNAL). */
+int fvm_batch_rhs(fvm_batch* b, const void* u, void* du, double t, int32_t flags, void* stream);
+/* Fixed-step Tsit5 on every instance, one captured CUDA graph per step, Dirichlet update after
+ * each step.  u0 [npoints][batch] and out [nsave][npoints][batch] are host FP64 arrays. */
+int fvm_batch_tsit5_solve(fvm_batch* b, const double* u0, const fvm_ode_options* opt, double* out,
+                          fvm_ode_stats* stats, void* stream);
+/* Autotuned launch shape of the batched operator: tune[0..2] = block size, instances per thread,
+ * grid blocks (chosen by timing the candidates on the first batched call). */
+int fvm_batch_tuning(const fvm_batch* b, int32_t* tune);
+
 /* ---- linear templates (src/specific_problems/) ------------------------------------------- */
 #define FVM_TEMPLATE_DIFFUSION 0                 /* diffusion_equation.jl:69-101 */
 #define FVM_TEMPLATE_LINEAR_REACTION_DIFFUSION 1 /* linear_reaction_diffusion_equations.jl:76-125 */
