@@ -38,6 +38,12 @@ static int guard(F&& f) {
 }
 
 static void check_launch() { FVM_CUDA(cudaGetLastError()); }
+// after a stream synchronisation: reports a kernel whose bounded wait ran out
+static void check_device_error() {
+    if (unsigned e = take_device_error())
+        fail(FVM_ERR_CUDA, "a streamed kernel timed out waiting for its copies (device error bits " +
+                               std::to_string(e) + ")");
+}
 
 // Tsit5 tableau (Tsitouras 2011, as published).
 static const double kC[7] = {0.0, 0.161, 0.327, 0.9, 0.9800255409045097, 1.0, 1.0};
@@ -300,6 +306,7 @@ static void rhs_outputs(fvm_problem* p, double* du, int32_t loc, cudaStream_t s)
         launch_permute_out(m->d_perm.as<int32_t>(), p->d_du.as<double>(), p->d_ref.as<double>(), m->np, s);
         FVM_CUDA(cudaMemcpyAsync(du, p->d_ref.p, sizeof(double) * m->np, cudaMemcpyDeviceToHost, s));
         FVM_CUDA(cudaStreamSynchronize(s));
+        check_device_error();
     } else {
         launch_permute_out(m->d_perm.as<int32_t>(), p->d_du.as<double>(), du, m->np, s);
     }
@@ -593,6 +600,7 @@ int fvm_tsit5_solve(fvm_problem* p, const double* u0, const fvm_ode_options* opt
         }
         FVM_CUDA(cudaStreamSynchronize(s));
         check_launch();
+        check_device_error();
         return FVM_OK;
     });
 }

@@ -165,6 +165,8 @@ void launch_sell_diff64(const SellPattern& p, const double* val, const double* x
 void launch_sell_diff32(const SellPattern& p, const float* val, const float* x32, const double* x, double* y,
                         const double* rowscale, const double* d, const double* b, const double* q, cudaStream_t s);
 void launch_to_f32(const double* x, float* y, int64_t n, cudaStream_t s);
+// error bits left by a kernel whose bounded wait ran out (0 = none); reading clears them
+unsigned take_device_error();
 void launch_permute_in(const int32_t* perm, const double* xref, double* xint, int64_t n, cudaStream_t s);
 void launch_permute_out(const int32_t* perm, const double* xint, double* xref, int64_t n, cudaStream_t s);
 void launch_dirichlet(const int32_t* idx, const double* val, double* u, int64_t n, cudaStream_t s);
@@ -187,6 +189,7 @@ void launch_fill(double* x, double v, int64_t n, cudaStream_t s);
 using LinearTermSink = std::function<void(int32_t, int32_t, double, int64_t, bool)>;
 void fvm_visit_linear_terms(const fvm_problem* p, const LinearTermSink& emit, std::vector<double>& b,
                             std::vector<double>& q, std::vector<double>& rowscale);
+
 
 namespace fvm {
 // A stream that can be captured: the caller's, or a private one ordered after the legacy

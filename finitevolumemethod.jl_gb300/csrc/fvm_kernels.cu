@@ -2,6 +2,9 @@
 // gather/scatter/stream work; none is a dense contraction, so no tensor-core path exists.
 #include "fvm_internal.h"
 #include "fvm_sell.cuh"
+#include "fvm_tma.cuh"
+
+#include <algorithm>
 
 namespace fvm {
 
@@ -54,16 +57,310 @@ __global__ void __launch_bounds__(256) sell_kernel(SellArgs a) {
     a.y[r] = out;
 }
 
+// ---------------------------------------------------------------------------------------
+// Streamed sliced-ELL operator (the default for slices up to 16 slots wide).
+//
+// A persistent grid (resident CTAs x SMs, more when a CTA's slice range would not fit its
+// window); CTA c owns the contiguous slice range [nslices c / G, nslices (c+1) / G).  At start
+// one bulk copy brings the range's slice offsets into shared memory, so no later step waits on
+// a global load for them.  The slices are then processed in stages of NW consecutive slices,
+// whose column and value slots are contiguous in HBM: one producer thread streams each stage
+// into shared memory with two cp.async.bulk copies completing on the stage's `full` mbarrier,
+// up to NST stages ahead of the consumers.  Consumer warp w takes slice w of each stage: it
+// reads its slots from shared memory (lane = row, conflict-free), gathers x through L2,
+// releases the stage (`empty` mbarrier) and finishes the row while the next copies land.
+// The sum runs over the slots in the same order as sell_row_product; the stage loop is
+// software-pipelined so that gathers overlap the previous slice's sums.
+// ---------------------------------------------------------------------------------------
+__device__ unsigned g_dev_error = 0;
+
+struct StreamArgs {
+    const int64_t* slice_ptr;  // nslices + 1 offsets, padded with two more
+    const int32_t* col;
+    const void* val;
+    const void* xg;
+    const double* x;
+    double* y;
+    const double* rowscale;
+    const double* d;
+    const double* b;
+    const double* q;
+    int64_t nrows, nslices;
+    int nst;    // pipeline stages held in shared memory
+    int spwin;  // slice offsets held per CTA: its range plus alignment slack, a multiple of 16
+};
+
+constexpr int kSpWindowMax = 1024;
+
+template <class V, int MAXW, int NW>
+struct StreamLayout {
+    static constexpr int kSlots = NW * MAXW * kSlice;  // slots per stage
+    static constexpr size_t kStageBytes = (size_t)kSlots * (sizeof(int32_t) + sizeof(V));
+    __host__ __device__ static size_t sp_offset(int nst) { return (size_t)nst * kStageBytes; }
+    __host__ __device__ static size_t bar_offset(int nst, int spwin) {
+        return sp_offset(nst) + (size_t)spwin * sizeof(int64_t);
+    }
+    __host__ __device__ static size_t bytes(int nst, int spwin) {
+        return bar_offset(nst, spwin) + (2 * (size_t)nst + 1) * sizeof(uint64_t);
+    }
+};
+
+// one consumer warp's slice between its fetch and its sums (registers)
+template <class Acc, int MAXW>
+struct SliceRegs {
+    Acc x[MAXW];  // gathered x of the lane's slots
+    Acc xa;       // the row's own x (difference form)
+    int64_t r;    // row
+    int st;       // stage buffer
+    int off;      // shared-memory slot of the lane's first entry
+    int cw;       // slots in the slice
+    bool have;
+};
+
+// slices up to 8 slots wide are software-pipelined (two slices in registers per warp, two
+// CTAs per SM); wider ones are summed as soon as they are fetched
+template <int MAXW>
+constexpr bool kStreamPipelined = MAXW <= 8;
+
+template <class V, class Acc, class X, bool DIFF, int MAXW, int NW>
+__global__ void __launch_bounds__((NW + 1) * 32, kStreamPipelined<MAXW> ? 2 : 1) sell_stream_kernel(StreamArgs a) {
+    using L = StreamLayout<V, MAXW, NW>;
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int nst = a.nst;
+    int32_t* colbuf = reinterpret_cast<int32_t*>(smem);
+    V* valbuf = reinterpret_cast<V*>(smem + (size_t)nst * L::kSlots * sizeof(int32_t));
+    int64_t* spw = reinterpret_cast<int64_t*>(smem + L::sp_offset(nst));
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + L::bar_offset(nst, a.spwin));
+    uint64_t* empty = full + nst;
+    uint64_t* spbar = empty + nst;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t G = gridDim.x;
+    const int64_t sb = a.nslices * (int64_t)blockIdx.x / G, se = a.nslices * ((int64_t)blockIdx.x + 1) / G;
+    const int64_t nstage = (se - sb + NW - 1) / NW;
+    // window of slice offsets: from sb rounded down to even (16-byte aligned), an even count
+    // covering sp[sb .. se]; the launcher keeps it within a.spwin entries and the array is
+    // padded so that the rounded-up end stays inside it
+    const int64_t w0 = sb & ~(int64_t)1;
+    const uint32_t wcount = (uint32_t)(((se + 1 - w0) + 1) & ~(int64_t)1);
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < nst; ++i) {
+            mbar_init(&full[i], 1);
+            mbar_init(&empty[i], NW);
+        }
+        mbar_init(spbar, 1);
+        mbar_init_fence();
+        mbar_arrive_expect_tx(spbar, wcount * (uint32_t)sizeof(int64_t));
+        bulk_copy_g2s(spw, a.slice_ptr + w0, wcount * (uint32_t)sizeof(int64_t), spbar);
+    }
+    __syncthreads();
+
+    if (warp == NW) {  // producer
+        if (lane != 0 || nstage == 0) return;
+        // streams stage k (slots [c0, c1)) into its buffer once the buffer is free
+        auto issue = [&](int64_t k, int64_t c0, int64_t c1) -> bool {
+            const int st = (int)(k % nst);
+            if (k >= nst && !mbar_wait(&empty[st], (uint32_t)((k / nst - 1) & 1))) return false;
+            const uint32_t n = (uint32_t)(c1 - c0);  // <= kSlots: NW slices of at most MAXW slots
+            if (n == 0) {  // slices without slots: nothing to copy
+                mbar_arrive(&full[st]);
+                return true;
+            }
+            mbar_arrive_expect_tx(&full[st], n * (uint32_t)(sizeof(int32_t) + sizeof(V)));
+            bulk_copy_g2s(colbuf + (size_t)st * L::kSlots, a.col + c0, n * (uint32_t)sizeof(int32_t), &full[st]);
+            bulk_copy_g2s(valbuf + (size_t)st * L::kSlots, (const V*)a.val + c0, n * (uint32_t)sizeof(V), &full[st]);
+            return true;
+        };
+        // stage 0 from two global loads, in parallel with the window copy
+        bool ok = issue(0, __ldg(&a.slice_ptr[sb]), __ldg(&a.slice_ptr[min(sb + NW, se)]));
+        int64_t issued = ok ? 1 : 0;
+        if (ok && !mbar_wait(spbar, 0)) ok = false;
+        const int64_t* sp = spw - w0;
+        for (int64_t k = 1; ok && k < nstage; ++k) {
+            const int64_t s0 = sb + k * NW;
+            if ((ok = issue(k, sp[s0], sp[min(s0 + NW, se)]))) issued = k + 1;
+        }
+        if (!ok) {
+            atomicOr(&g_dev_error, kDevErrEmptyWait);
+            // wait (bounded) for the copies already issued into the stages still in flight
+            for (int64_t j = (issued > nst ? issued - nst : 0); j < issued; ++j)
+                mbar_wait(&full[j % nst], (uint32_t)((j / nst) & 1));
+        }
+        return;
+    }
+
+    if (!mbar_wait(spbar, 0)) {
+        if (lane == 0) atomicOr(&g_dev_error, kDevErrFullWait);
+        return;
+    }
+    const int64_t* sp = spw - w0;  // sp[s] for s in [w0, w0 + wcount)
+
+    // consumers, software-pipelined by one stage: the gathers of stage k + 1 are in flight
+    // while the FP64 sums of stage k run.  A warp holds two stages at a time (the one it
+    // sums, the one it gathers for), so a CTA needs at least four.
+    const X* __restrict__ xg = (const X*)a.xg;
+    const V* __restrict__ vb0 = valbuf;
+    // waits for stage k, reads this warp's columns from shared memory and issues its gathers;
+    // false when the wait ran out
+    auto fetch = [&](int64_t k, SliceRegs<Acc, MAXW>& R) -> bool {
+        const int64_t s0 = sb + k * NW, s = s0 + warp;
+        R.have = s < se;
+        R.r = s * kSlice + lane;
+        R.st = (int)(k % nst);
+        R.cw = 0;
+        R.xa = 0;
+        if (DIFF && R.have) R.xa = (Acc)__ldg(&xg[R.r < a.nrows ? R.r : a.nrows - 1]);
+        if (!mbar_wait(&full[R.st], (uint32_t)((k / nst) & 1))) return false;
+        if (R.have) {
+            const int64_t cb = sp[s];
+            R.cw = (int)((sp[s + 1] - cb) / kSlice);
+            R.off = R.st * L::kSlots + (int)(cb - sp[s0]) + lane;
+            int32_t c[MAXW];
+#pragma unroll
+            for (int j = 0; j < MAXW; ++j)
+                if (j < R.cw) c[j] = colbuf[R.off + j * kSlice];
+#pragma unroll
+            for (int j = 0; j < MAXW; ++j)
+                if (j < R.cw) R.x[j] = (Acc)__ldg(&xg[c[j]]);
+        }
+        return true;
+    };
+    // sums the slice with its values from shared memory (slot order, one FMA per slot: the
+    // FP64 pipe is the kernel's floor), releases the stage and writes the lane's row
+    auto finish = [&](const SliceRegs<Acc, MAXW>& R) {
+        Acc acc = 0;
+        if (R.have) {
+#pragma unroll
+            for (int j = 0; j < MAXW; ++j)
+                if (j < R.cw) {
+                    const Acc v = (Acc)vb0[R.off + j * kSlice];
+                    if constexpr (DIFF)
+                        acc += v * (R.x[j] - R.xa);
+                    else
+                        acc += v * R.x[j];
+                }
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[R.st]);
+        if (!R.have || R.r >= a.nrows) return;
+        const int64_t r = R.r;
+        double out = (double)acc;
+        if (a.rowscale) out *= a.rowscale[r];
+        if (a.d || a.q) {
+            const double xr = a.x[r];
+            if (a.d) out += a.d[r] * xr;
+            if (a.q) out += a.q[r] * xr * xr;
+        }
+        if (a.b) out += a.b[r];
+        a.y[r] = out;
+    };
+    bool ok = true;
+    if constexpr (kStreamPipelined<MAXW>) {
+        SliceRegs<Acc, MAXW> A, B;
+        ok = nstage == 0 || fetch(0, A);
+        for (int64_t k = 0; ok && k < nstage; k += 2) {
+            // A holds stage k
+            if (k + 1 < nstage) ok = fetch(k + 1, B);
+            finish(A);
+            if (!ok || k + 1 >= nstage) break;
+            // B holds stage k + 1
+            if (k + 2 < nstage) ok = fetch(k + 2, A);
+            finish(B);
+        }
+    } else {
+        SliceRegs<Acc, MAXW> A;
+        for (int64_t k = 0; ok && k < nstage; ++k)
+            if ((ok = fetch(k, A))) finish(A);
+    }
+    if (!ok && lane == 0) atomicOr(&g_dev_error, kDevErrFullWait);
+}
+
+constexpr int kStreamWarps = 8;
+
+// Launch shape of one instantiation on one device: CTAs per SM and pipeline depth.  The
+// most consumer warps per SM wins, provided each CTA still holds enough stages (four for the
+// software-pipelined widths, whose warps hold two stages each; three otherwise).
+struct StreamShape {
+    int dev = -1, sms = 0, ctas = 0, nst = 0;
+};
+
+template <class V, class Acc, class X, bool DIFF, int MAXW>
+static void launch_stream(const StreamArgs& a0, cudaStream_t s) {
+    using L = StreamLayout<V, MAXW, kStreamWarps>;
+    auto kern = sell_stream_kernel<V, Acc, X, DIFF, MAXW, kStreamWarps>;
+    const int threads = (kStreamWarps + 1) * 32;
+    static StreamShape shape;  // per instantiation
+    int dev = 0;
+    FVM_CUDA(cudaGetDevice(&dev));
+    if (shape.dev != dev) {
+        int smem_sm = 0, smem_cta = 0, reserved = 0, sms = 0;
+        FVM_CUDA(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+        FVM_CUDA(cudaDeviceGetAttribute(&smem_cta, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+        FVM_CUDA(cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev));
+        FVM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        FVM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_cta));
+        StreamShape best;
+        for (int ctas = 4; ctas >= 1 && best.ctas == 0; --ctas) {
+            const long budget = std::min<long>(smem_sm / ctas - reserved, smem_cta);
+            const long nst = (budget - (long)L::bytes(0, kSpWindowMax)) / (long)L::kStageBytes;
+            const long need = kStreamPipelined<MAXW> ? 4 : (ctas == 1 ? 2 : 3);
+            if (nst < need) continue;
+            int fit = 0;
+            const int n = (int)std::min<long>(nst, 6);
+            FVM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, kern, threads, L::bytes(n, kSpWindowMax)));
+            if (fit >= ctas) best = {dev, sms, ctas, n};
+        }
+        if (best.ctas == 0) fail(FVM_ERR_CUDA, "streamed operator kernel does not fit on an SM");
+        shape = best;
+    }
+    StreamArgs a = a0;
+    a.nst = shape.nst;
+    // every CTA's range (ceil(nslices / G) slices, at most 3 more window entries after the
+    // alignment rounding) must fit the window
+    const int64_t stages = (a.nslices + kStreamWarps - 1) / kStreamWarps;
+    int64_t grid = std::min<int64_t>((int64_t)shape.ctas * shape.sms, stages);
+    grid = std::max<int64_t>(grid, (a.nslices + (kSpWindowMax - 4) - 1) / (kSpWindowMax - 4));
+    grid = std::max<int64_t>(grid, 1);
+    const int64_t range = (a.nslices + grid - 1) / grid;
+    a.spwin = (int)std::min<int64_t>(kSpWindowMax, ((range + 3) + 15) & ~(int64_t)15);
+    kern<<<(unsigned)grid, threads, L::bytes(a.nst, a.spwin), s>>>(a);
+}
+
 template <class V, class Acc, class X, bool DIFF>
 static void launch_sell(const SellPattern& p, const V* val, const X* xg, const double* x, double* y,
                         const double* rowscale, const double* d, const double* b, const double* q, cudaStream_t s) {
     if (p.nslices == 0) return;
+    if (p.maxw <= 16) {
+        StreamArgs a{p.d_slice_ptr.as<int64_t>(), p.d_col.as<int32_t>(), val, xg, x, y, rowscale, d, b, q,
+                     p.nrows, p.nslices, 0, 0};
+        // exact widths of the common vertex degrees: no predicated-off slot costs an FP64 issue
+        if (p.maxw <= 4)
+            launch_stream<V, Acc, X, DIFF, 4>(a, s);
+        else if (p.maxw <= 6)
+            launch_stream<V, Acc, X, DIFF, 6>(a, s);
+        else if (p.maxw <= 7)
+            launch_stream<V, Acc, X, DIFF, 7>(a, s);
+        else if (p.maxw <= 8)
+            launch_stream<V, Acc, X, DIFF, 8>(a, s);
+        else if (p.maxw <= 12)
+            launch_stream<V, Acc, X, DIFF, 12>(a, s);
+        else
+            launch_stream<V, Acc, X, DIFF, 16>(a, s);
+        return;
+    }
     SellArgs a{p.d_slice_ptr.as<int64_t>(), p.d_width.as<int32_t>(), p.d_col.as<int32_t>(), val, xg, x, y, rowscale,
                d, b, q, p.nrows, p.nslices};
     unsigned grid = grid_for(p.nslices * 32, 256);
-#define FVM_LAUNCH_SELL(W) sell_kernel<V, Acc, X, DIFF, W><<<grid, 256, 0, s>>>(a)
-    FVM_SELL_DISPATCH(p.maxw, FVM_LAUNCH_SELL)
-#undef FVM_LAUNCH_SELL
+    sell_kernel<V, Acc, X, DIFF, 0><<<grid, 256, 0, s>>>(a);
+}
+
+unsigned take_device_error() {
+    unsigned e = 0;
+    FVM_CUDA(cudaMemcpyFromSymbol(&e, g_dev_error, sizeof e));
+    if (e) {
+        const unsigned zero = 0;
+        FVM_CUDA(cudaMemcpyToSymbol(g_dev_error, &zero, sizeof zero));
+    }
+    return e;
 }
 
 void launch_sell_apply64(const SellPattern& p, const double* val, const double* x, double* y, const double* rowscale,

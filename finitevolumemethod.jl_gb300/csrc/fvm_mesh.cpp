@@ -127,7 +127,12 @@ static void finalize_sell(SellPattern& pat, int64_t nrows) {
                 }
             }
         }
-    pat.d_slice_ptr.upload(pat.slice_ptr);
+    {  // two padding entries: the streamed kernel copies its window of offsets in 16-byte units
+        std::vector<int64_t> padded(pat.slice_ptr);
+        padded.push_back(pat.nslots);
+        padded.push_back(pat.nslots);
+        pat.d_slice_ptr.upload(padded);
+    }
     pat.d_width.upload(pat.width);
     pat.d_col.upload(pat.col);
 }

@@ -165,5 +165,33 @@ def sine_diffusion(n=64) -> Spec:
     return Spec(tri, (lambda x, y, t, u, p: 0.0 * x,), ("Dirichlet",), (None,), D=D, u0=u0, tf=1e-4)
 
 
+# ---- a wheel: hub vertices of high degree (slices wider than 16 slots) ----------------------
+def wheel_mesh(nspoke=40, nring=3):
+    """A hub vertex joined to `nspoke` points of the first ring (degree nspoke), then rings of
+    quadrilaterals split into triangles; the outer ring is the boundary."""
+    from fvmgpu.meshes import Triangulation
+
+    pts = [(0.0, 0.0)]
+    for r in range(1, nring + 1):
+        th = 2 * np.pi * np.arange(nspoke) / nspoke + 0.1 * r
+        pts += list(zip(r / nring * np.cos(th), r / nring * np.sin(th)))
+    ring = lambda r, i: 1 + (r - 1) * nspoke + i % nspoke  # noqa: E731
+    tris = [(0, ring(1, i), ring(1, i + 1)) for i in range(nspoke)]
+    for r in range(1, nring):
+        for i in range(nspoke):
+            a, b, c, d = ring(r, i), ring(r, i + 1), ring(r + 1, i), ring(r + 1, i + 1)
+            tris += [(a, c, d), (a, d, b)]
+    boundary = [ring(nring, i) for i in range(nspoke)] + [ring(nring, 0)]
+    return Triangulation(np.array(pts), np.array(tris), [boundary])
+
+
+def wheel_diffusion(nspoke=40) -> Spec:
+    tri = wheel_mesh(nspoke)
+    P = tri.points
+    u0 = np.cos(2 * P[:, 0]) + P[:, 1]
+    return Spec(tri, (lambda x, y, t, u, p: 0.5 * u - x,), ("Neumann",), (None,),
+                D=lambda x, y, t, u, p: 1.0 + x * x + 0.0 * u, S=lambda x, y, t, u, p: 0.3 * u + y, u0=u0, tf=0.1)
+
+
 def disk_poisson_mesh(n_interior=3000, n_boundary=128, seed=0):
     return triangulate_disk(n_interior, n_boundary, seed=seed)

@@ -11,7 +11,7 @@ import pytest
 
 import fvm_oracle as O
 from problems import (api_problem, heat_convection, mixed_annulus, nonlinear_rect, oracle_problem, parity_error,
-                      readme_diffusion, rhs_term_scale, sine_diffusion)
+                      readme_diffusion, rhs_term_scale, sine_diffusion, wheel_diffusion)
 
 pytestmark = pytest.mark.gpu
 
@@ -33,6 +33,7 @@ BUILDERS = {
     "mixed_annulus": mixed_annulus,
     "sine64": lambda: sine_diffusion(64),
     "nonlinear30": lambda: nonlinear_rect(30),
+    "wheel40": lambda: wheel_diffusion(40),  # slices wider than 16 slots: the one-warp-per-slice kernel
 }
 
 
