@@ -28,13 +28,10 @@ struct fvm_batch {
     int precision = FVM_FP64;
     int64_t np = 0, nnz = 0;
     fvm::DBuf d_rowptr, d_col, d_val, d_b, d_q;
-    bool has_b = false, has_q = false;
     fvm::DBuf d_dir_idx, d_dir_val;
     int64_t ndir = 0;
-    fvm::DBuf d_work;  // caller-numbered IO staging: 2 x [np][B]
-    int block = 256, vec = 1;
-    int64_t grid = 0;
-    bool tuned = false;
+    fvm::DBuf d_work;  // caller-numbered IO staging: 3 x [np][B]
+    fvm::BatchOp op;
 };
 
 namespace fvm {
@@ -218,22 +215,20 @@ void tune_cache_store(const TuneKey& k, const TuneVal& v) {
 }
 
 template <class T>
-void launch_op(const fvm_batch* bt, int block, int vec, int64_t grid, const T* u, T* du, cudaStream_t s) {
+void launch_op(const BatchOp& op, int block, int vec, int64_t grid, const T* u, T* du, cudaStream_t s) {
     const int64_t chunk = 32 * (int64_t)vec;
-    const int64_t nchunk = (bt->B + chunk - 1) / chunk;
-    const T* bv = bt->has_b ? bt->d_b.as<T>() : nullptr;
-    const T* qv = bt->has_q ? bt->d_q.as<T>() : nullptr;
-    const int64_t* rp = bt->d_rowptr.as<int64_t>();
-    const int32_t* cl = bt->d_col.as<int32_t>();
-    const T* val = bt->d_val.as<T>();
+    const int64_t nchunk = (op.B + chunk - 1) / chunk;
+    const T* bv = (const T*)op.b;
+    const T* qv = (const T*)op.q;
+    const T* val = (const T*)op.val;
     unsigned g = (unsigned)grid;
     if (vec == 4 && sizeof(T) == 4)
-        batch_op_kernel<T, (sizeof(T) == 4 ? 4 : 2)><<<g, block, 0, s>>>(rp, cl, val, u, du, bv, qv, bt->np, bt->B,
-                                                                      nchunk);
+        batch_op_kernel<T, (sizeof(T) == 4 ? 4 : 2)><<<g, block, 0, s>>>(op.rowptr, op.col, val, u, du, bv, qv, op.np,
+                                                                      op.B, nchunk);
     else if (vec == 2)
-        batch_op_kernel<T, 2><<<g, block, 0, s>>>(rp, cl, val, u, du, bv, qv, bt->np, bt->B, nchunk);
+        batch_op_kernel<T, 2><<<g, block, 0, s>>>(op.rowptr, op.col, val, u, du, bv, qv, op.np, op.B, nchunk);
     else
-        batch_op_kernel<T, 1><<<g, block, 0, s>>>(rp, cl, val, u, du, bv, qv, bt->np, bt->B, nchunk);
+        batch_op_kernel<T, 1><<<g, block, 0, s>>>(op.rowptr, op.col, val, u, du, bv, qv, op.np, op.B, nchunk);
 }
 
 int64_t persistent_grid(int block, int64_t items_warps) {
@@ -257,17 +252,17 @@ int max_vec_for(const void* a, const void* b) {
 
 // Times the candidate shapes on the real buffers (3 launches each) and keeps the fastest.
 template <class T>
-void autotune(fvm_batch* bt, const T* u, T* du, cudaStream_t s) {
-    if (bt->tuned) return;
+void autotune(BatchOp& op, const T* u, T* du, cudaStream_t s) {
+    if (op.tuned) return;
     std::lock_guard<std::mutex> lock(g_tune_mutex);
     tune_cache_load();
-    TuneKey key{bt->np, bt->nnz, bt->B, bt->precision};
+    TuneKey key{op.np, op.nnz, op.B, op.precision};
     auto it = g_tune.find(key);
     if (it != g_tune.end()) {
-        bt->block = it->second.block;
-        bt->vec = it->second.vec;
-        bt->grid = it->second.grid;
-        bt->tuned = true;
+        op.block = it->second.block;
+        op.vec = it->second.vec;
+        op.grid = it->second.grid;
+        op.tuned = true;
         return;
     }
     const int vmax = std::min(sizeof(T) == 4 ? 4 : 2, max_vec_for<T>(u, du));
@@ -277,13 +272,13 @@ void autotune(fvm_batch* bt, const T* u, T* du, cudaStream_t s) {
     float best = 1e30f;
     TuneVal bestv{256, 1, 1};
     for (int vec = 1; vec <= vmax; vec *= 2) {
-        if (bt->B % vec) continue;
+        if (op.B % vec) continue;
         for (int block : {128, 256, 512}) {
-            int64_t nchunk = (bt->B + 32 * vec - 1) / (32 * vec);
-            int64_t grid = persistent_grid(block, bt->np * nchunk);
-            launch_op<T>(bt, block, vec, grid, u, du, s);  // warm
+            int64_t nchunk = (op.B + 32 * vec - 1) / (32 * vec);
+            int64_t grid = persistent_grid(block, op.np * nchunk);
+            launch_op<T>(op, block, vec, grid, u, du, s);  // warm
             FVM_CUDA(cudaEventRecord(e0, s));
-            for (int r = 0; r < 3; ++r) launch_op<T>(bt, block, vec, grid, u, du, s);
+            for (int r = 0; r < 3; ++r) launch_op<T>(op, block, vec, grid, u, du, s);
             FVM_CUDA(cudaEventRecord(e1, s));
             FVM_CUDA(cudaEventSynchronize(e1));
             float ms = 0;
@@ -296,22 +291,17 @@ void autotune(fvm_batch* bt, const T* u, T* du, cudaStream_t s) {
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    bt->block = bestv.block;
-    bt->vec = bestv.vec;
-    bt->grid = bestv.grid;
-    bt->tuned = true;
+    op.block = bestv.block;
+    op.vec = bestv.vec;
+    op.grid = bestv.grid;
+    op.tuned = true;
     g_tune[key] = bestv;
     tune_cache_store(key, bestv);
 }
 
 template <class T>
 void batch_rhs_internal(fvm_batch* bt, const T* u, T* du, cudaStream_t s) {
-    if (((uintptr_t)u | (uintptr_t)du) % sizeof(T))
-        fail(FVM_ERR_INVALID_ARGUMENT, "batched state arrays must be aligned to their element size");
-    autotune<T>(bt, u, du, s);
-    // the grid-stride loop covers every item for any grid, so a narrower vector is always valid
-    const int vec = std::min(bt->vec, max_vec_for<T>(u, du));
-    launch_op<T>(bt, bt->block, vec, bt->grid, u, du, s);
+    batch_op_apply<T>(bt->op, u, du, s);
 }
 
 template <class T>
@@ -381,6 +371,29 @@ void batch_tsit5(fvm_batch* bt, T* u, T* work, int64_t nsteps, double dt, bool u
 }
 
 }  // namespace
+
+template <class T>
+void batch_op_apply(BatchOp& op, const T* u, T* du, cudaStream_t s) {
+    if (((uintptr_t)u | (uintptr_t)du) % sizeof(T))
+        fail(FVM_ERR_INVALID_ARGUMENT, "batched state arrays must be aligned to their element size");
+    autotune<T>(op, u, du, s);
+    // the grid-stride loop covers every item for any grid, so a narrower vector is always valid
+    const int vec = std::min(op.vec, max_vec_for<T>(u, du));
+    launch_op<T>(op, op.block, vec, op.grid, u, du, s);
+}
+template void batch_op_apply<float>(BatchOp&, const float*, float*, cudaStream_t);
+template void batch_op_apply<double>(BatchOp&, const double*, double*, cudaStream_t);
+
+void launch_batch_assemble(const int64_t* mptr, const int32_t* midx, const double* mcoef, const double* cst,
+                           const double* D, void* val, int64_t nnz, int B, int precision, cudaStream_t s) {
+    if (nnz * B == 0) return;
+    const unsigned g = blocks(nnz * B, 256);
+    if (precision == FVM_FP32)
+        batch_assemble_kernel<float><<<g, 256, 0, s>>>(mptr, midx, mcoef, cst, D, (float*)val, nnz, B);
+    else
+        batch_assemble_kernel<double><<<g, 256, 0, s>>>(mptr, midx, mcoef, cst, D, (double*)val, nnz, B);
+}
+
 }  // namespace fvm
 
 using namespace fvm;
@@ -456,22 +469,15 @@ int fvm_batch_create(fvm_problem* p, int32_t batch, const double* dualD, const d
         d_D.upload(Dt);
         size_t es = precision == FVM_FP32 ? 4 : 8;
         bt->d_val.alloc(es * pat.nnz * batch);
-        unsigned g = blocks(pat.nnz * batch, 256);
-        if (precision == FVM_FP32)
-            batch_assemble_kernel<float><<<g, 256>>>(d_mptr.as<int64_t>(), d_midx.as<int32_t>(), d_mcoef.as<double>(),
-                                                     d_cst.as<double>(), d_D.as<double>(), bt->d_val.as<float>(),
-                                                     pat.nnz, batch);
-        else
-            batch_assemble_kernel<double><<<g, 256>>>(d_mptr.as<int64_t>(), d_midx.as<int32_t>(), d_mcoef.as<double>(),
-                                                      d_cst.as<double>(), d_D.as<double>(), bt->d_val.as<double>(),
-                                                      pat.nnz, batch);
+        launch_batch_assemble(d_mptr.as<int64_t>(), d_midx.as<int32_t>(), d_mcoef.as<double>(), d_cst.as<double>(),
+                              d_D.as<double>(), bt->d_val.p, pat.nnz, batch, precision, nullptr);
         FVM_CUDA(cudaGetLastError());
         FVM_CUDA(cudaDeviceSynchronize());
         bt->d_rowptr.upload(pat.rowptr);
         bt->d_col.upload(pat.csr_col);
         auto nz = [](double x) { return x != 0; };
-        bt->has_b = std::any_of(bv.begin(), bv.end(), nz);
-        bt->has_q = std::any_of(qv.begin(), qv.end(), nz);
+        const bool has_b = std::any_of(bv.begin(), bv.end(), nz);
+        const bool has_q = std::any_of(qv.begin(), qv.end(), nz);
         auto upload_t = [&](DBuf& dst, const std::vector<double>& src) {
             if (precision == FVM_FP32) {
                 std::vector<float> f(src.begin(), src.end());
@@ -480,8 +486,18 @@ int fvm_batch_create(fvm_problem* p, int32_t batch, const double* dualD, const d
                 dst.upload(src);
             }
         };
-        if (bt->has_b) upload_t(bt->d_b, bv);
-        if (bt->has_q) upload_t(bt->d_q, qv);
+        if (has_b) upload_t(bt->d_b, bv);
+        if (has_q) upload_t(bt->d_q, qv);
+        BatchOp& op = bt->op;
+        op.np = bt->np;
+        op.nnz = bt->nnz;
+        op.B = batch;
+        op.precision = precision;
+        op.rowptr = bt->d_rowptr.as<int64_t>();
+        op.col = bt->d_col.as<int32_t>();
+        op.val = bt->d_val.p;
+        op.b = has_b ? bt->d_b.p : nullptr;
+        op.q = has_q ? bt->d_q.p : nullptr;
         // Dirichlet list shared by every instance
         std::vector<int32_t> idx;
         std::vector<double> val;
@@ -508,9 +524,9 @@ int fvm_batch_destroy(fvm_batch* b) {
 int fvm_batch_tuning(const fvm_batch* b, int32_t* tune) {
     return guard_call([&] {
         if (!b || !tune) fail(FVM_ERR_INVALID_ARGUMENT, "NULL argument");
-        tune[0] = b->block;
-        tune[1] = b->vec;
-        tune[2] = (int32_t)b->grid;
+        tune[0] = b->op.block;
+        tune[1] = b->op.vec;
+        tune[2] = (int32_t)b->op.grid;
         return FVM_OK;
     });
 }

@@ -190,6 +190,12 @@ using LinearTermSink = std::function<void(int32_t, int32_t, double, int64_t, boo
 void fvm_visit_linear_terms(const fvm_problem* p, const LinearTermSink& emit, std::vector<double>& b,
                             std::vector<double>& q, std::vector<double>& rowscale);
 
+// Terms of a linear template's A and b: emitA(row, col, coef, didx) adds coef * D[didx] (coef
+// alone when didx < 0) to A[row][col]; emitb(row, -1, coef, didx) likewise to b[row].  Rows and
+// columns in the caller's numbering; D[didx] are the dual-edge samples then the boundary
+// quarter-point samples (fvm_template.cpp).
+using TemplateTermSink = std::function<void(int32_t, int32_t, double, int64_t)>;
+void fvm_template_visit_terms(const fvm_template* T, const TemplateTermSink& emitA, const TemplateTermSink& emitb);
 
 namespace fvm {
 // A stream that can be captured: the caller's, or a private one ordered after the legacy
@@ -217,6 +223,27 @@ struct CaptureStream {
         cudaStreamDestroy(own);
     }
 };
+
+// A batched CSR operator on [rows][B] state (instance index fastest) with per-instance values
+// val[k][B]: du[r][b] = sum_k val[k][b] u[col_k][b] + bvec[r] + q[r] u[r][b]^2.  One warp per
+// (row, chunk of instances); the launch shape is tuned on the first application (fvm_batch.cu).
+struct BatchOp {
+    int64_t np = 0, nnz = 0;
+    int B = 0, precision = FVM_FP64;
+    const int64_t* rowptr = nullptr;
+    const int32_t* col = nullptr;
+    const void* val = nullptr;
+    const void* b = nullptr;  // per-row constant shared by the instances, or null
+    const void* q = nullptr;  // per-row quadratic coefficient, or null
+    int block = 256, vec = 1;
+    int64_t grid = 0;
+    bool tuned = false;
+};
+template <class T>
+void batch_op_apply(BatchOp& op, const T* u, T* du, cudaStream_t s);
+// val[k][b] = cst[k] + sum_{m in [mptr[k], mptr[k+1])} mcoef[m] D[midx[m]][b]  (FP64 or FP32 val)
+void launch_batch_assemble(const int64_t* mptr, const int32_t* midx, const double* mcoef, const double* cst,
+                           const double* D, void* val, int64_t nnz, int B, int precision, cudaStream_t s);
 
 // Right-hand side in the internal numbering plus the per-step callback (Dirichlet update).
 struct OdeRhs {

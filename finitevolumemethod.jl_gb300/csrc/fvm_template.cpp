@@ -9,15 +9,18 @@
 
 using namespace fvm;
 
-// A and b in the internal numbering; follows abstract_templates.jl:73-99 (triangles),
-// :149-191 and :237-267 (boundary edges, including the reference's division of row j by
-// V_i at :262), :127-135 (Dudt), :278-309 (Poisson b and steady Dirichlet rows),
-// :317-325 (missing vertices), linear_reaction_diffusion_equations.jl:115-125 and
-// mean_exit_time.jl:84-94.
-static void assemble_template(fvm_template* T) {
+// Terms of A and b, rows and columns in the caller's numbering; follows
+// abstract_templates.jl:73-99 (triangles), :149-191 and :237-267 (boundary edges, including
+// the reference's division of row j by V_i at :262), :127-135 (Dudt), :278-309 (Poisson b and
+// steady Dirichlet rows), :317-325 (missing vertices), linear_reaction_diffusion_equations.jl:
+// 115-125 and mean_exit_time.jl:84-94.  A diffusion term's coefficient multiplies the
+// diffusion sample D[didx] (dual-edge midpoints 3 t + e, then boundary quarter points
+// 3 nt + 2 e + side); a term with didx < 0 is a constant.  Every entry the reference assigns
+// (Dirichlet and missing-vertex rows, Dudt and mean-exit-time b) receives no other term, so
+// all terms add.
+void fvm_template_visit_terms(const fvm_template* T, const TemplateTermSink& emitA, const TemplateTermSink& emitb) {
     const fvm_problem* p = T->prob;
     const fvm_mesh* m = p->mesh;
-    const SellPattern& pat = m->pat;
     const int kind = T->kind;
     if (p->dif_deg != 0) fail(FVM_ERR_UNSUPPORTED_FORM, "template diffusion functions are D(x, y): degree 0");
     bool has_dudt = false;
@@ -25,31 +28,26 @@ static void assemble_template(fvm_template* T) {
     if (has_dudt && kind == FVM_TEMPLATE_POISSON) fail(FVM_ERR_UNSUPPORTED, "PoissonsEquation does not support Dudt nodes.");
     if (has_dudt && kind == FVM_TEMPLATE_MEAN_EXIT_TIME)
         fail(FVM_ERR_UNSUPPORTED, "MeanExitTimeProblem does not support Dudt nodes.");
-    std::vector<double>& A = T->val;
-    std::vector<double>& b = T->b;
-    A.assign(pat.nslots, 0.0);
-    b.assign(m->np, 0.0);
-    auto slot = [&](int32_t r, int32_t c) { return pat.find(m->iperm[r], m->iperm[c]); };
     auto hc = [&](int32_t v) { return p->code[v] == FVM_VERTEX_DIRICHLET || p->code[v] == FVM_VERTEX_DUDT; };
     auto dir = [&](int32_t v) { return p->code[v] == FVM_VERTEX_DIRICHLET; };
     const int ns = p->src_deg + 1, nn = p->neu_deg + 1;
+    const int64_t qbase = 3 * m->nt;
     if (kind == FVM_TEMPLATE_POISSON)  // create_rhs_b
         for (int64_t v = 0; v < m->np; ++v)
-            if (m->has_vertex[v] && !dir((int32_t)v)) b[m->iperm[v]] = p->src.empty() ? 0.0 : p->src[v * ns];
+            if (m->has_vertex[v] && !dir((int32_t)v)) emitb((int32_t)v, -1, p->src.empty() ? 0.0 : p->src[v * ns], -1);
     // triangle_contributions!
     for (int64_t t = 0; t < m->nt; ++t) {
         const int32_t* w = &m->tri[3 * t];
         const double* pr = &m->props[24 * t];
         for (int e = 0; e < 3; ++e) {
             int32_t e1 = w[e], e2 = w[(e + 1) % 3];
-            double D = p->dualD.empty() ? 0.0 : p->dualD[3 * t + e];
-            double Dl = D * pr[21 + e];
+            double l = pr[21 + e];
             double nx = pr[15 + 2 * e], ny = pr[16 + 2 * e];
             bool h1 = hc(e1), h2 = hc(e2);
             for (int v = 0; v < 3; ++v) {
-                double a = Dl * (pr[v] * nx + pr[3 + v] * ny);
-                if (!h1) A[slot(e1, w[v])] += a / m->vol[e1];
-                if (!h2) A[slot(e2, w[v])] -= a / m->vol[e2];
+                double a = l * (pr[v] * nx + pr[3 + v] * ny);
+                if (!h1) emitA(e1, w[v], a / m->vol[e1], 3 * t + e);
+                if (!h2) emitA(e2, w[v], -a / m->vol[e2], 3 * t + e);
             }
         }
     }
@@ -61,13 +59,11 @@ static void assemble_template(fvm_template* T) {
             double nx = (qy - py) / lij, ny = -(qx - px) / lij;
             double mijx = (px + qx) / 2, mijy = (py + qy) / 2;
             double lh = std::sqrt((mijx - px) * (mijx - px) + (mijy - py) * (mijy - py));
-            double Di = p->quarterD.empty() ? 0.0 : p->quarterD[2 * e];
-            double Dj = p->quarterD.empty() ? 0.0 : p->quarterD[2 * e + 1];
             if (p->bneu[e]) {  // neumann_boundary_edge_contributions! (b += D a l / V)
                 double ai = p->quarterN.empty() ? 0.0 : p->quarterN[(2 * e) * nn];
                 double aj = p->quarterN.empty() ? 0.0 : p->quarterN[(2 * e + 1) * nn];
-                if (!hc(i)) b[m->iperm[i]] += Di * ai * lh / m->vol[i];
-                if (!hc(j)) b[m->iperm[j]] += Dj * aj * lh / m->vol[j];
+                if (!hc(i)) emitb(i, -1, ai * lh / m->vol[i], qbase + 2 * e);
+                if (!hc(j)) emitb(j, -1, aj * lh / m->vol[j], qbase + 2 * e + 1);
                 continue;
             }
             int32_t t = m->btri[e];
@@ -75,39 +71,59 @@ static void assemble_template(fvm_template* T) {
             const double* pr = &m->props[24 * t];
             for (int v = 0; v < 3; ++v) {
                 double c = pr[v] * nx + pr[3 + v] * ny;
-                if (!hc(i)) A[slot(i, w[v])] += Di * lh * c / m->vol[i];
-                if (!hc(j)) A[slot(j, w[v])] += Dj * lh * c / m->vol[i];  // V_i, as the reference
+                if (!hc(i)) emitA(i, w[v], lh * c / m->vol[i], qbase + 2 * e);
+                if (!hc(j)) emitA(j, w[v], lh * c / m->vol[i], qbase + 2 * e + 1);  // V_i, as the reference
             }
         }
     }
     if (kind == FVM_TEMPLATE_LINEAR_REACTION_DIFFUSION)  // linear_source_contributions!
         for (int64_t v = 0; v < m->np; ++v)
             if (m->has_vertex[v] && !hc((int32_t)v) && !p->src.empty() && ns > 1)
-                A[slot((int32_t)v, (int32_t)v)] += p->src[v * ns + 1];
+                emitA((int32_t)v, (int32_t)v, p->src[v * ns + 1], -1);
     if (kind == FVM_TEMPLATE_DIFFUSION || kind == FVM_TEMPLATE_LINEAR_REACTION_DIFFUSION) {
         const int nu = p->dudt_deg + 1;
         for (int64_t v = 0; v < m->np; ++v)  // apply_dudt_conditions!
-            if (p->code[v] == FVM_VERTEX_DUDT) b[m->iperm[v]] = p->dudt.empty() ? 0.0 : p->dudt[v * nu];
+            if (p->code[v] == FVM_VERTEX_DUDT) emitb((int32_t)v, -1, p->dudt.empty() ? 0.0 : p->dudt[v * nu], -1);
     }
     if (kind == FVM_TEMPLATE_POISSON)  // apply_steady_dirichlet_conditions!
         for (int64_t v = 0; v < m->np; ++v)
             if (dir((int32_t)v)) {
-                b[m->iperm[v]] = p->dirv.empty() ? 0.0 : p->dirv[v];
-                A[slot((int32_t)v, (int32_t)v)] = 1.0;
+                emitb((int32_t)v, -1, p->dirv.empty() ? 0.0 : p->dirv[v], -1);
+                emitA((int32_t)v, (int32_t)v, 1.0, -1);
             }
     if (kind == FVM_TEMPLATE_MEAN_EXIT_TIME)  // create_met_b!
         for (int64_t v = 0; v < m->np; ++v) {
             if (!m->has_vertex[v]) continue;
             if (!dir((int32_t)v))
-                b[m->iperm[v]] = -1.0;
+                emitb((int32_t)v, -1, -1.0, -1);
             else
-                A[slot((int32_t)v, (int32_t)v)] = 1.0;
+                emitA((int32_t)v, (int32_t)v, 1.0, -1);
         }
-    for (int64_t v = 0; v < m->np; ++v)  // fix_missing_vertices!
-        if (!m->has_vertex[v]) {
-            A[slot((int32_t)v, (int32_t)v)] = 1.0;
-            b[m->iperm[v]] = 0.0;
-        }
+    for (int64_t v = 0; v < m->np; ++v)  // fix_missing_vertices! (b stays 0)
+        if (!m->has_vertex[v]) emitA((int32_t)v, (int32_t)v, 1.0, -1);
+}
+
+// A and b in the internal numbering, from the terms above with the problem's D samples
+static void assemble_template(fvm_template* T) {
+    const fvm_problem* p = T->prob;
+    const fvm_mesh* m = p->mesh;
+    const SellPattern& pat = m->pat;
+    std::vector<double>& A = T->val;
+    std::vector<double>& b = T->b;
+    A.assign(pat.nslots, 0.0);
+    b.assign(m->np, 0.0);
+    const int64_t qbase = 3 * m->nt;
+    auto D = [&](int64_t didx) {
+        if (didx < 0) return 1.0;
+        if (didx < qbase) return p->dualD.empty() ? 0.0 : p->dualD[didx];
+        return p->quarterD.empty() ? 0.0 : p->quarterD[didx - qbase];
+    };
+    fvm_template_visit_terms(
+        T,
+        [&](int32_t r, int32_t c, double coef, int64_t didx) {
+            A[pat.find(m->iperm[r], m->iperm[c])] += D(didx) * coef;
+        },
+        [&](int32_t r, int32_t, double coef, int64_t didx) { b[m->iperm[r]] += D(didx) * coef; });
 }
 
 // FP32 copy of the template values and the FP32 gather buffer (first FP32 use)

@@ -8,7 +8,8 @@ from .meshes import (Triangulation, triangulate_rectangle, triangulate_annulus, 
 from .api import (ConditionType, Neumann, Dudt, Dirichlet, Constrained, ParametrisedFunction, BoundaryConditions,
                   InternalConditions, Conditions, TriangleProperties, FVMGeometry, FVMProblem, fvm_eqs,
                   update_dirichlet_nodes, DiffusionEquation, LinearReactionDiffusionEquation, PoissonsEquation,
-                  MeanExitTimeProblem, Tsit5, KrylovSolver, ODESolution, LinearSolution, solve, BatchedProblem)
+                  MeanExitTimeProblem, Tsit5, KrylovSolver, ODESolution, LinearSolution, solve, BatchedProblem,
+                  AdjointProblem, solve_rrule)
 from ._lib import FVMError, UnsupportedFormError, NotConvergedError
 from ._build import build, lib_path
 
@@ -18,6 +19,6 @@ __all__ = [
     "InternalConditions", "Conditions", "TriangleProperties", "FVMGeometry", "FVMProblem", "fvm_eqs",
     "update_dirichlet_nodes", "DiffusionEquation", "LinearReactionDiffusionEquation", "PoissonsEquation",
     "MeanExitTimeProblem", "Tsit5", "KrylovSolver", "ODESolution", "LinearSolution", "solve", "BatchedProblem",
-    "disjoint_union", "FVMError",
+    "disjoint_union", "AdjointProblem", "solve_rrule", "FVMError",
     "UnsupportedFormError", "NotConvergedError", "build", "lib_path",
 ]

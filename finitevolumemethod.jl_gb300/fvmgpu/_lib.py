@@ -99,6 +99,13 @@ class SolverOptions(C.Structure):
     ]
 
 
+class AdjointStats(C.Structure):
+    _fields_ = [
+        ("steps", C.c_int64), ("checkpoints", C.c_int64), ("rhs_evals", C.c_int64), ("transpose_evals", C.c_int64),
+        ("forward_ms", C.c_double), ("reverse_ms", C.c_double),
+    ]
+
+
 class SolverStats(C.Structure):
     _fields_ = [
         ("iterations", C.c_int64), ("refinements", C.c_int64), ("rel_residual", C.c_double),
@@ -144,6 +151,19 @@ SIGNATURES = {
                                            C.POINTER(OdeStats), C.c_void_p]),
     "fvm_template_steady_solve": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(SolverOptions),
                                             C.POINTER(SolverStats), C.c_int32, C.c_void_p]),
+    "fvm_adjoint_create": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p)]),
+    "fvm_adjoint_destroy": (C.c_int, [C.c_void_p]),
+    "fvm_adjoint_set_log_diffusion": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]),
+    "fvm_adjoint_rhs": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]),
+    "fvm_adjoint_forward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_int64, C.c_void_p, C.c_int32,
+                                      C.c_void_p]),
+    "fvm_adjoint_pullback": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_int64, C.c_int32, C.c_void_p,
+                                       C.c_void_p, C.c_void_p, C.POINTER(AdjointStats), C.c_int32, C.c_void_p]),
+    "fvm_adjoint_loss_grad": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int64, C.c_int32,
+                                        c_double_p, C.c_void_p, C.c_void_p, C.POINTER(AdjointStats), C.c_int32,
+                                        C.c_void_p]),
+    "fvm_adjoint_rhs_vjp": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
+                                      C.c_void_p]),
 }
 
 _LIB = None

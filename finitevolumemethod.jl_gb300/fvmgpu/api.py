@@ -594,6 +594,131 @@ class BatchedProblem:
 
 
 # --------------------------------------------------------------------------------------
+# differentiation: discrete adjoint of the time-dependent templates
+# --------------------------------------------------------------------------------------
+class AdjointProblem:
+    """Differentiable batched solve of a DiffusionEquation or LinearReactionDiffusionEquation
+    template with respect to a per-vertex log-diffusivity field.
+
+    Instance i has D_i(x, y) = the P1 interpolant of exp(theta[:, i]) over the template's mesh,
+    sampled where the reference samples D; conditions, sources and b come from the template (b
+    must not depend on D).  Arrays are (npoints, batch) float64, host numpy arrays or CUDA torch
+    tensors, in the caller's numbering.  Time stepping is fixed-step Tsit5.  What the reference
+    gets by running its solve under ForwardDiff, this gets from a hand-written adjoint:
+    `pullback` is the vector-Jacobian product of theta, u0 -> u(T); `loss_and_grad` the same
+    for loss = sum (u(T) - u_obs)^2; `rhs_vjp` the one of the right-hand side."""
+
+    def __init__(self, template, batch=1):
+        if not isinstance(template, _TimeTemplate):
+            raise TypeError("AdjointProblem takes a DiffusionEquation or LinearReactionDiffusionEquation")
+        self.template, self.B = template, int(batch)
+        self.n = template.mesh.triangulation.num_points
+        h = C.c_void_p()
+        check(load().fvm_adjoint_create(template.handle, self.B, C.byref(h)))
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def _arrays(self, *xs):
+        ptrs, locs = [], set()
+        for x in xs:
+            if x is None:
+                ptrs.append(None)
+                continue
+            if tuple(x.shape) not in ((self.n, self.B),) and not (self.B == 1 and tuple(x.shape) == (self.n,)):
+                raise ValueError(f"arrays must have shape ({self.n}, {self.B})")
+            p, loc = _lib.array_pointer(x)
+            ptrs.append(p)
+            locs.add(loc)
+        if len(locs) != 1:
+            raise TypeError("arrays must all be host arrays or all CUDA tensors")
+        return ptrs, locs.pop()
+
+    def _like(self, x):
+        if isinstance(x, np.ndarray):
+            return np.empty((self.n, self.B))
+        import torch
+
+        return torch.empty((self.n, self.B), dtype=torch.float64, device=x.device)
+
+    @staticmethod
+    def _stream(stream):
+        return stream if stream is not None else _lib.current_stream_handle()
+
+    def set_log_diffusion(self, theta, stream=None):
+        """theta: (npoints, batch) log-diffusivity per vertex and instance."""
+        (tp,), loc = self._arrays(theta)
+        check(load().fvm_adjoint_set_log_diffusion(self._h, tp, loc, self._stream(stream)))
+        return self
+
+    def rhs(self, u, stream=None):
+        """A(theta) u + b for every instance."""
+        du = self._like(u)
+        (up, dp), loc = self._arrays(u, du)
+        check(load().fvm_adjoint_rhs(self._h, up, dp, loc, self._stream(stream)))
+        return du
+
+    def forward(self, u0, dt, nsteps, stream=None):
+        """u(T) after `nsteps` Tsit5 steps of `dt`."""
+        uT = self._like(u0)
+        (up, tp), loc = self._arrays(u0, uT)
+        check(load().fvm_adjoint_forward(self._h, up, float(dt), int(nsteps), tp, loc, self._stream(stream)))
+        return uT
+
+    @staticmethod
+    def _stats(st):
+        return {k: getattr(st, k) for k, _ in _lib.AdjointStats._fields_}
+
+    def pullback(self, u0, dt, nsteps, uT_bar, checkpoint_every=20, stream=None):
+        """(theta_bar, u0_bar, stats) = the vector-Jacobian product of u(T) with uT_bar."""
+        tb, ub = self._like(u0), self._like(u0)
+        (up, bp, tp, ubp), loc = self._arrays(u0, uT_bar, tb, ub)
+        st = _lib.AdjointStats()
+        check(load().fvm_adjoint_pullback(self._h, up, float(dt), int(nsteps), int(checkpoint_every), bp, tp, ubp,
+                                          C.byref(st), loc, self._stream(stream)))
+        return tb, ub, self._stats(st)
+
+    def loss_and_grad(self, u0, u_obs, dt, nsteps, checkpoint_every=20, stream=None):
+        """(loss (batch,), d loss / d theta, d loss / d u0, stats) for
+        loss_i = sum_v (u(T)[v, i] - u_obs[v, i])^2."""
+        tb, ub = self._like(u0), self._like(u0)
+        (up, op, tp, ubp), loc = self._arrays(u0, u_obs, tb, ub)
+        loss = np.empty(self.B)
+        st = _lib.AdjointStats()
+        check(load().fvm_adjoint_loss_grad(self._h, up, op, float(dt), int(nsteps), int(checkpoint_every),
+                                           dptr(loss), tp, ubp, C.byref(st), loc, self._stream(stream)))
+        return loss, tb, ub, self._stats(st)
+
+    def rhs_vjp(self, u, w, stream=None):
+        """(u_bar, theta_bar) = (A^T w, (d f / d theta)^T w) for f(u, theta) = A(theta) u + b."""
+        ub, tb = self._like(u), self._like(u)
+        (up, wp, ubp, tp), loc = self._arrays(u, w, ub, tb)
+        check(load().fvm_adjoint_rhs_vjp(self._h, up, wp, ubp, tp, loc, self._stream(stream)))
+        return ub, tb
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib._LIB is not None:
+            _lib._LIB.fvm_adjoint_destroy(self._h)
+            self._h = None
+
+
+def solve_rrule(adjoint: AdjointProblem, theta, u0, dt, nsteps, checkpoint_every=20):
+    """The rrule of theta, u0 -> u(T) in ChainRulesCore's shape: returns (u(T), pullback) where
+    pullback(uT_bar) -> (theta_bar, u0_bar)."""
+    adjoint.set_log_diffusion(theta)
+    uT = adjoint.forward(u0, dt, nsteps)
+
+    def pullback(uT_bar):
+        adjoint.set_log_diffusion(theta)
+        tb, ub, _ = adjoint.pullback(u0, dt, nsteps, uT_bar, checkpoint_every)
+        return tb, ub
+
+    return uT, pullback
+
+
+# --------------------------------------------------------------------------------------
 # templates (src/specific_problems/)
 # --------------------------------------------------------------------------------------
 class _Template:

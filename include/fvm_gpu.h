@@ -264,6 +264,51 @@ typedef struct fvm_solver_stats {
 int fvm_template_steady_solve(fvm_template* tmpl, double* x, const fvm_solver_options* opt,
                               fvm_solver_stats* stats, int32_t flags, void* stream);
 
+/* ---- differentiation: discrete adjoint of the time-dependent templates ---------------------
+ * The reference differentiates its solves by running them under ForwardDiff (its closures are
+ * generic in the number type) or through SciMLSensitivity; this is the device-side counterpart
+ * for the DiffusionEquation / LinearReactionDiffusionEquation templates.  A batch of instances
+ * shares the template's mesh, conditions and b; instance i has the diffusion field D_i(x, y) =
+ * the P1 interpolant of per-vertex values exp(theta[v][i]) (a log-diffusivity field), sampled
+ * where the reference samples D (dual-edge midpoints, boundary quarter points).  The template's
+ * own D is ignored.  b must not depend on D (no Neumann edges).  Arrays are [npoints][batch]
+ * (batch fastest), FP64, host (FVM_PTR_HOST) or device (FVM_PTR_DEVICE) in the caller's
+ * numbering.  Time stepping is fixed-step Tsit5 (the templates' solve with adaptive = false). */
+typedef struct fvm_adjoint fvm_adjoint;
+typedef struct fvm_adjoint_stats {
+    int64_t steps;            /* time steps of the forward solve */
+    int64_t checkpoints;      /* states kept by the forward pass */
+    int64_t rhs_evals;        /* batched A u + b products (forward pass and recomputation) */
+    int64_t transpose_evals;  /* batched A^T products of the reverse pass */
+    double forward_ms;        /* device time of the forward pass */
+    double reverse_ms;        /* device time of the reverse pass, recomputation included */
+} fvm_adjoint_stats;
+int fvm_adjoint_create(fvm_template* tmpl, int32_t batch, fvm_adjoint** out);
+int fvm_adjoint_destroy(fvm_adjoint* adj);
+/* theta [npoints][batch]: assembles every instance's operator on the device. */
+int fvm_adjoint_set_log_diffusion(fvm_adjoint* adj, const double* theta, int32_t flags, void* stream);
+/* du = A(theta) u + b for every instance. */
+int fvm_adjoint_rhs(fvm_adjoint* adj, const double* u, double* du, int32_t flags, void* stream);
+/* u(T) after nsteps Tsit5 steps of dt from u0. */
+int fvm_adjoint_forward(fvm_adjoint* adj, const double* u0, double dt, int64_t nsteps, double* uT,
+                        int32_t flags, void* stream);
+/* Vector-Jacobian product of the solve: theta_bar = (d uT / d theta)^T uT_bar and
+ * u0_bar = (d uT / d u0)^T uT_bar (u0_bar may be NULL), by the discrete adjoint of the Tsit5
+ * steps; the forward pass keeps u every checkpoint_every steps and the reverse pass recomputes
+ * the states in between. */
+int fvm_adjoint_pullback(fvm_adjoint* adj, const double* u0, double dt, int64_t nsteps, int32_t checkpoint_every,
+                         const double* uT_bar, double* theta_bar, double* u0_bar, fvm_adjoint_stats* stats,
+                         int32_t flags, void* stream);
+/* loss[i] = sum_v (uT[v][i] - u_obs[v][i])^2 (host array [batch]) and its gradients with
+ * respect to theta and u0 (u0_bar may be NULL). */
+int fvm_adjoint_loss_grad(fvm_adjoint* adj, const double* u0, const double* u_obs, double dt, int64_t nsteps,
+                          int32_t checkpoint_every, double* loss, double* theta_bar, double* u0_bar,
+                          fvm_adjoint_stats* stats, int32_t flags, void* stream);
+/* Vector-Jacobian product of the right-hand side f(u, theta) = A(theta) u + b:
+ * u_bar = A^T w (may be NULL), theta_bar = (d f / d theta)^T w. */
+int fvm_adjoint_rhs_vjp(fvm_adjoint* adj, const double* u, const double* w, double* u_bar, double* theta_bar,
+                        int32_t flags, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -754,3 +754,45 @@ def steady_solve(A, b):
     from scipy.sparse.linalg import spsolve
 
     return spsolve(A.tocsc(), b)
+
+
+# --------------------------------------------------------------------------------------
+# fields given by vertex values (the adjoint's log-diffusivity parametrisation)
+# --------------------------------------------------------------------------------------
+def p1_field(tri, values):
+    """The continuous piecewise-linear interpolant of per-vertex `values` over the solid
+    triangles of `tri`, as a closure f(x, y, *ignored) for the template constructors (the
+    reference evaluates D(x, y) at dual-edge midpoints and boundary quarter points).  Each
+    query point is located by its barycentric coordinates; points on a shared edge get the
+    same value from either triangle."""
+    P = np.asarray(tri.points, dtype=np.float64)
+    T = np.asarray(tri.triangles, dtype=np.int64)
+    vals = np.asarray(values, dtype=np.float64)
+
+    def f(x, y, *_):
+        shape = np.broadcast(np.asarray(x), np.asarray(y)).shape
+        xs, ys = (np.broadcast_to(np.asarray(c, dtype=np.float64), shape).ravel() for c in (x, y))
+        out = np.full(xs.shape, np.nan)
+        todo = np.ones(xs.shape, dtype=bool)
+        for a, b, c in T:
+            if not todo.any():
+                break
+            (ax, ay), (bx, by), (cx, cy) = P[a], P[b], P[c]
+            det = (bx - ax) * (cy - ay) - (cx - ax) * (by - ay)
+            la = ((bx - xs) * (cy - ys) - (cx - xs) * (by - ys)) / det
+            lb = ((cx - xs) * (ay - ys) - (ax - xs) * (cy - ys)) / det
+            lc = 1.0 - la - lb
+            tol = -1e-12
+            hit = todo & (la >= tol) & (lb >= tol) & (lc >= tol)
+            out[hit] = la[hit] * vals[a] + lb[hit] * vals[b] + lc[hit] * vals[c]
+            todo &= ~hit
+        if todo.any():
+            raise ValueError("p1_field: a query point lies outside the mesh")
+        return out.reshape(shape) if shape else float(out[0])
+
+    return f
+
+
+def template_ode_solve(A, b, u0, dt, nsteps):
+    """Fixed-step Tsit5 on du/dt = A u + b (the templates' ODEProblem, no callback)."""
+    return tsit5_fixed(None, u0, 0.0, dt, nsteps, rhs=lambda u, t: A @ u + b, dirichlet=False)
