@@ -38,6 +38,9 @@ struct fvm_adjoint {
     bool has_b = false;
     fvm::DBuf d_theta, d_E, d_D, d_val, d_valT;  // per instance
     fvm::BatchOp A, AT;
+    // one instance: A and A^T in the mesh's sliced-ELL layout (the pattern is structurally
+    // symmetric, so A^T has A's slots), applied by the single-instance streamed kernel
+    fvm::DBuf d_slot, d_tslot, d_sell, d_sellT;
     bool theta_set = false;
 };
 
@@ -103,24 +106,43 @@ __global__ void transpose_vals_kernel(const int64_t* __restrict__ tperm, const d
     valT[i] = val[tperm[k] * B + (i - k * B)];
 }
 
-// G[k][b] += sum_{i < ns} kb_i[row(k)][b] * Y_i[col(k)][b]
+// G[k][b] += sum_{i < ns} kb_i[row(k)][b] * Y_i[col(k)][b].  Every (entry, instance) pair is
+// independent: with many instances a warp takes an entry and its lanes the instances (loads
+// coalesced across lanes); with few, a thread takes an entry and loops over the instances.
 struct StagePair {
     const double* kb[6];
     const double* Y[6];
     int ns;
 };
-__global__ void grad_accum_kernel(const int32_t* __restrict__ erow, const int32_t* __restrict__ col,
-                                  StagePair P, double* __restrict__ G, int64_t nnz, int B) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nnz * B) return;
-    int64_t k = i / B;
-    int64_t b = i - k * B;
-    const int64_t r = (int64_t)erow[k] * B + b, c = (int64_t)col[k] * B + b;
-    double acc = G[i];
+__device__ __forceinline__ void grad_accum_one(const StagePair& P, double* G, int64_t k, int64_t r, int64_t c,
+                                               int64_t b, int B) {
+    double acc = G[k * B + b];
 #pragma unroll
     for (int j = 0; j < 6; ++j)
-        if (j < P.ns) acc += P.kb[j][r] * P.Y[j][c];
-    G[i] = acc;
+        if (j < P.ns) acc += P.kb[j][r * B + b] * P.Y[j][c * B + b];
+    G[k * B + b] = acc;
+}
+__global__ void grad_accum_warp_kernel(const int32_t* __restrict__ erow, const int32_t* __restrict__ col, StagePair P,
+                                       double* __restrict__ G, int64_t nnz, int B) {
+    const int64_t k = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (k >= nnz) return;
+    const int64_t r = __ldg(&erow[k]), c = __ldg(&col[k]);
+    for (int64_t b = threadIdx.x & 31; b < B; b += 32) grad_accum_one(P, G, k, r, c, b, B);
+}
+__global__ void grad_accum_thread_kernel(const int32_t* __restrict__ erow, const int32_t* __restrict__ col,
+                                         StagePair P, double* __restrict__ G, int64_t nnz, int B) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nnz) return;
+    const int64_t r = __ldg(&erow[k]), c = __ldg(&col[k]);
+    for (int64_t b = 0; b < B; ++b) grad_accum_one(P, G, k, r, c, b, B);
+}
+void launch_grad_accum(const fvm_adjoint* a, const StagePair& P, double* G, cudaStream_t s) {
+    if (a->B >= 16)
+        grad_accum_warp_kernel<<<blocks(a->nnz * 32, 256), 256, 0, s>>>(a->d_erow.as<int32_t>(), a->d_col.as<int32_t>(),
+                                                                         P, G, a->nnz, a->B);
+    else
+        grad_accum_thread_kernel<<<blocks(a->nnz, 256), 256, 0, s>>>(a->d_erow.as<int32_t>(), a->d_col.as<int32_t>(), P,
+                                                                     G, a->nnz, a->B);
 }
 
 // Dbar[idx][b] = sum coef * G[k][b] over the sample's terms
@@ -147,6 +169,13 @@ __global__ void thetabar_kernel(const int64_t* __restrict__ vptr, const int32_t*
     double acc = 0;
     for (int64_t m = vptr[v]; m < vptr[v + 1]; ++m) acc += vw[m] * Dbar[(int64_t)vsmp[m] * B + b];
     tb[i] = E[i] * acc;
+}
+
+// dst[map[k]] = src[k]
+__global__ void scatter_kernel(const int64_t* __restrict__ map, const double* __restrict__ src, double* __restrict__ dst,
+                               int64_t n) {
+    int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) dst[map[k]] = src[k];
 }
 
 // rows of [n][B]: out[r] = in[perm[r]] (gather) or out[perm[r]] = in[r] (scatter)
@@ -201,7 +230,20 @@ using namespace fvm;
 namespace {
 
 // du = A u + b on the batch (A includes b)
-void adj_rhs(fvm_adjoint* a, const double* u, double* du, cudaStream_t s) { batch_op_apply<double>(a->A, u, du, s); }
+void adj_rhs(fvm_adjoint* a, const double* u, double* du, cudaStream_t s) {
+    if (a->B == 1)
+        launch_sell_apply64(a->T->prob->mesh->pat, a->d_sell.as<double>(), u, du, nullptr,
+                            a->has_b ? a->d_b.as<double>() : nullptr, nullptr, s);
+    else
+        batch_op_apply<double>(a->A, u, du, s);
+}
+// out = A^T w on the batch
+void adj_rhs_t(fvm_adjoint* a, const double* w, double* out, cudaStream_t s) {
+    if (a->B == 1)
+        launch_sell_apply64(a->T->prob->mesh->pat, a->d_sellT.as<double>(), w, out, nullptr, nullptr, nullptr, s);
+    else
+        batch_op_apply<double>(a->AT, w, out, s);
+}
 
 // One Tsit5 step in place: u <- u_{n+1}; k[0] holds f(u_n) on entry and f(u_{n+1}) on exit.
 void fwd_step(fvm_adjoint* a, double* u, double* const* k, double* Y, double h, int64_t n, cudaStream_t s) {
@@ -409,7 +451,7 @@ void pullback_internal(fvm_adjoint* a, const double* u0, double dt, int64_t N, i
                     L.c[L.nv++] = dt * kA[j][i];
                 }
                 lincomb(kb[i], nullptr, L, n, s);
-                batch_op_apply<double>(a->AT, kb[i], Yb[i], s);
+                adj_rhs_t(a, kb[i], Yb[i], s);
                 ++nadj;
             }
             StagePair P{};
@@ -418,8 +460,7 @@ void pullback_internal(fvm_adjoint* a, const double* u0, double dt, int64_t N, i
                 P.kb[i] = kb[i];
                 P.Y[i] = Yi[i];
             }
-            grad_accum_kernel<<<blocks(a->nnz * B, 256), 256, 0, s>>>(a->d_erow.as<int32_t>(), a->d_col.as<int32_t>(),
-                                                                       P, G.as<double>(), a->nnz, B);
+            launch_grad_accum(a, P, G.as<double>(), s);
             LinComb L{};
             L.nv = 6;
             for (int i = 0; i < 6; ++i) {
@@ -586,6 +627,20 @@ int fvm_adjoint_create(fvm_template* T, int32_t batch, fvm_adjoint** out) {
         a->d_vptr.upload(vptr);
         a->d_vsmp.upload(vsmp);
         a->d_vw.upload(vw);
+        if (batch == 1) {
+            std::vector<int64_t> tslot(pat.nnz);
+            for (int64_t k = 0; k < pat.nnz; ++k) {
+                const int64_t t = pat.find(pat.csr_col[k], erow[k]);
+                if (t < 0) fail(FVM_ERR_BAD_MESH, "vertex-neighbour pattern is not structurally symmetric");
+                tslot[k] = t;
+            }
+            a->d_slot.upload(pat.csr_slot);
+            a->d_tslot.upload(tslot);
+            a->d_sell.alloc(8 * pat.nslots);
+            a->d_sellT.alloc(8 * pat.nslots);
+            FVM_CUDA(cudaMemset(a->d_sell.p, 0, a->d_sell.bytes));
+            FVM_CUDA(cudaMemset(a->d_sellT.p, 0, a->d_sellT.bytes));
+        }
         a->has_b = std::any_of(b.begin(), b.end(), [](double x) { return x != 0; });
         if (a->has_b) a->d_b.upload(b);
         const int64_t n = a->np * batch;
@@ -637,6 +692,12 @@ int fvm_adjoint_set_log_diffusion(fvm_adjoint* a, const double* theta, int32_t f
                               a->d_cst.as<double>(), a->d_D.as<double>(), a->d_val.p, a->nnz, B, FVM_FP64, s);
         transpose_vals_kernel<<<blocks(a->nnz * B, 256), 256, 0, s>>>(
             a->d_tperm.as<int64_t>(), a->d_val.as<double>(), a->d_valT.as<double>(), a->nnz, B);
+        if (B == 1) {  // sliced-ELL copies: A's entry (r, c) at slot(r, c) and at A^T's slot(c, r)
+            scatter_kernel<<<blocks(a->nnz, 256), 256, 0, s>>>(a->d_slot.as<int64_t>(), a->d_val.as<double>(),
+                                                                a->d_sell.as<double>(), a->nnz);
+            scatter_kernel<<<blocks(a->nnz, 256), 256, 0, s>>>(a->d_tslot.as<int64_t>(), a->d_val.as<double>(),
+                                                                a->d_sellT.as<double>(), a->nnz);
+        }
         FVM_CUDA(cudaGetLastError());
         a->theta_set = true;
         return FVM_OK;
@@ -758,14 +819,13 @@ int fvm_adjoint_rhs_vjp(fvm_adjoint* a, const double* u, const double* w, double
         double* tb = ui + 3 * n;
         io.in(u, ui);
         io.in(w, wi);
-        if (u_bar) batch_op_apply<double>(a->AT, wi, ub, s);
+        if (u_bar) adj_rhs_t(a, wi, ub, s);
         FVM_CUDA(cudaMemsetAsync(G.p, 0, G.bytes, s));
         StagePair P{};
         P.ns = 1;
         P.kb[0] = wi;
         P.Y[0] = ui;
-        grad_accum_kernel<<<blocks(a->nnz * a->B, 256), 256, 0, s>>>(a->d_erow.as<int32_t>(), a->d_col.as<int32_t>(),
-                                                                       P, G.as<double>(), a->nnz, a->B);
+        launch_grad_accum(a, P, G.as<double>(), s);
         theta_from_G(a, G.as<double>(), tb, s);
         io.out(tb, theta_bar);
         if (u_bar) io.out(ub, u_bar);

@@ -85,7 +85,7 @@ __device__ __forceinline__ void vstore(T* p, const T (&x)[VEC]) {
 }
 
 // du[r][b] = sum_k val[k][b] u[col_k][b] + bvec[r] + q[r] u[r][b]^2 over the chunk of instances
-// of each (row, chunk) work item; grid-stride over items (a persistent grid).
+// of each (row, chunk of 32 * VEC instances) work item; grid-stride over items (a persistent grid).
 template <class T, int VEC>
 __global__ void __launch_bounds__(512) batch_op_kernel(const int64_t* __restrict__ rowptr,
                                                        const int32_t* __restrict__ col, const T* __restrict__ val,
@@ -111,7 +111,10 @@ __global__ void __launch_bounds__(512) batch_op_kernel(const int64_t* __restrict
             vload<T, VEC>(u + (int64_t)c0 * B + b0, x0);
             vload<T, VEC>(u + (int64_t)c1 * B + b0, x1);
 #pragma unroll
-            for (int j = 0; j < VEC; ++j) acc[j] += v0[j] * x0[j] + v1[j] * x1[j];
+            for (int j = 0; j < VEC; ++j) {  // one fused multiply-add per entry (FP64 issue is scarce)
+                acc[j] += v0[j] * x0[j];
+                acc[j] += v1[j] * x1[j];
+            }
         }
         if (k < k1) {
             const int32_t c0 = __ldg(&col[k]);

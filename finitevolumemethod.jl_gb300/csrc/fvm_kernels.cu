@@ -276,11 +276,14 @@ __global__ void __launch_bounds__((NW + 1) * 32, kStreamPipelined<MAXW> ? 2 : 1)
 
 constexpr int kStreamWarps = 8;
 
-// Launch shape of one instantiation on one device: CTAs per SM and pipeline depth.  The
-// most consumer warps per SM wins, provided each CTA still holds enough stages (four for the
-// software-pipelined widths, whose warps hold two stages each; three otherwise).
+// Launch shape of one instantiation on one device: CTAs per SM.  The most consumer warps per
+// SM wins, provided each CTA still holds enough stages with the largest slice-offset window
+// (four for the software-pipelined widths, whose warps hold two stages each; three otherwise).
+// The pipeline depth of a launch then fills the CTA's share of shared memory around its
+// actual window.
 struct StreamShape {
-    int dev = -1, sms = 0, ctas = 0, nst = 0;
+    int dev = -1, sms = 0, ctas = 0;
+    long budget = 0;  // shared memory bytes per CTA
 };
 
 template <class V, class Acc, class X, bool DIFF, int MAXW>
@@ -305,15 +308,13 @@ static void launch_stream(const StreamArgs& a0, cudaStream_t s) {
             const long need = kStreamPipelined<MAXW> ? 4 : (ctas == 1 ? 2 : 3);
             if (nst < need) continue;
             int fit = 0;
-            const int n = (int)std::min<long>(nst, 6);
-            FVM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, kern, threads, L::bytes(n, kSpWindowMax)));
-            if (fit >= ctas) best = {dev, sms, ctas, n};
+            FVM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, kern, threads, (size_t)budget));
+            if (fit >= ctas) best = {dev, sms, ctas, budget};
         }
         if (best.ctas == 0) fail(FVM_ERR_CUDA, "streamed operator kernel does not fit on an SM");
         shape = best;
     }
     StreamArgs a = a0;
-    a.nst = shape.nst;
     // every CTA's range (ceil(nslices / G) slices, at most 3 more window entries after the
     // alignment rounding) must fit the window
     const int64_t stages = (a.nslices + kStreamWarps - 1) / kStreamWarps;
@@ -322,6 +323,7 @@ static void launch_stream(const StreamArgs& a0, cudaStream_t s) {
     grid = std::max<int64_t>(grid, 1);
     const int64_t range = (a.nslices + grid - 1) / grid;
     a.spwin = (int)std::min<int64_t>(kSpWindowMax, ((range + 3) + 15) & ~(int64_t)15);
+    a.nst = (int)std::min<long>(6, (shape.budget - (long)L::bytes(0, a.spwin)) / (long)L::kStageBytes);
     kern<<<(unsigned)grid, threads, L::bytes(a.nst, a.spwin), s>>>(a);
 }
 

@@ -18,6 +18,9 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <limits>
+#include <type_traits>
+#include <utility>
 
 namespace fvm {
 
@@ -26,6 +29,7 @@ constexpr int kRedBlock = 256;
 struct KState {               // device-resident Krylov scalars
     double dot[8];            // reduction results
     double alpha, beta, omega, rho, rz, tol2, rn2;
+    double div2;              // a cycle whose recurrence residual^2 exceeds this has diverged
     int done;
     int breakdown;
     int skip3;                // CG: the update step of this iteration did not run
@@ -98,16 +102,34 @@ struct SpmvArgs {
     int64_t n, nslices;
 };
 
+// (B x)_r of the lane's row.  rowsum == nullptr: explicit values.  Otherwise the difference
+// form sum_j K_rj (x_j - x_r) + rowsum_r x_r, K with a zero diagonal: the FP32 operator.  On a
+// smooth x the explicit FP32 sum cancels to eps32 |B||x| ~ eps32 / h^2 relative (interior rows
+// of a diffusion operator sum to zero); the differences cut that to ~ eps32 / h.
+template <class V, class T>
+__device__ __forceinline__ T spmv_row(const SpmvArgs& A, const V* val, const T* rowsum, const T* x, int64_t s,
+                                      int lane) {
+    if (!rowsum) return sell_row<V, T>(A.slice_ptr, A.width, A.col, val, x, s, lane);
+    const int64_t r = s * kSlice + lane;
+    const int64_t rc = r < A.n ? r : A.n - 1;
+    const T xr = x[rc];
+    const T acc = __ldg(&A.width[s]) <= 8
+                      ? sell_row_product<V, T, T, true, 8>(A.slice_ptr, A.width, A.col, val, x, xr, s, lane)
+                      : sell_row_product<V, T, T, true, 0>(A.slice_ptr, A.width, A.col, val, x, xr, s, lane);
+    return acc + rowsum[rc] * xr;
+}
+
 // CG step 1: Ap = B p; pAp; alpha = rz / pAp
 template <class V, class T>
-__global__ void __launch_bounds__(kRedBlock) cg_spmv_kernel(SpmvArgs A, const V* val, const T* p, T* Ap, double* part,
+__global__ void __launch_bounds__(kRedBlock) cg_spmv_kernel(SpmvArgs A, const V* val, const T* rowsum, const T* p, T* Ap,
+                                                            double* part,
                                                             KState* st) {
     if (st->done) return;
     int64_t s = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
     double v[1] = {0.0};
     if (s < A.nslices) {
-        T y = sell_row<V, T>(A.slice_ptr, A.width, A.col, val, p, s, lane);
+        T y = spmv_row<V, T>(A, val, rowsum, p, s, lane);
         int64_t r = s * kSlice + lane;
         if (r < A.n) {
             Ap[r] = y;
@@ -128,8 +150,10 @@ __global__ void __launch_bounds__(kRedBlock) cg_spmv_kernel(SpmvArgs A, const V*
     }
 }
 
-// CG step 2: x += alpha p; r -= alpha Ap; rz = r . (invD r); rn2 = sum (r invV)^2
-template <class T>
+// CG step 2: x += alpha p; r -= alpha Ap; rn2 = sum (r invV)^2; with the Jacobi
+// preconditioner also rz = r . (invD r) and beta (a polynomial preconditioner computes them
+// after its own pass, cg_rz_kernel)
+template <class T, bool JACOBI>
 __global__ void __launch_bounds__(kRedBlock) cg_update_kernel(T* x, T* r, const T* p, const T* Ap, const T* invD,
                                                               const T* invV, int64_t n, double* part, KState* st) {
     if (st->done) {
@@ -152,12 +176,15 @@ __global__ void __launch_bounds__(kRedBlock) cg_update_kernel(T* x, T* r, const 
     bool last;
     block_reduce_publish<2>(v, part, st, gridDim.x, last);
     if (last && threadIdx.x == 0) {
-        double rz_old = st->rz;
-        st->rz = v[0];
+        if (JACOBI) {
+            double rz_old = st->rz;
+            st->rz = v[0];
+            st->beta = rz_old > 0 ? v[0] / rz_old : 0.0;
+        }
         st->rn2 = v[1];
-        st->beta = rz_old > 0 ? v[0] / rz_old : 0.0;
         st->skip3 = 0;
         if (v[1] <= st->tol2 || !isfinite(v[1])) st->done = 1;
+        if (v[1] > st->div2) st->done = st->breakdown = 1;
     }
 }
 
@@ -168,6 +195,127 @@ __global__ void cg_pupdate_kernel(T* p, const T* r, const T* invD, int64_t n, co
     T beta = (T)st->beta;
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) p[i] = invD[i] * r[i] + beta * p[i];
+}
+
+// ---- Chebyshev polynomial preconditioner -------------------------------------------------
+// z = p(D^-1 B) D^-1 r: `degree` steps of the Chebyshev iteration for D^-1 B y = D^-1 r from
+// y = 0 on an interval [lmin, lmax] that holds the spectrum of D^-1 B (Saad, Iterative Methods
+// for Sparse Linear Systems, 2nd ed., Algorithm 12.1): with theta = (lmax + lmin) / 2,
+// delta = (lmax - lmin) / 2, sigma = theta / delta,
+//     w_0 = D^-1 r, d_0 = w_0 / theta, y_1 = d_0, rho_0 = 1 / sigma,
+//     w_j = w_{j-1} - D^-1 B d_{j-1}, rho_j = 1 / (2 sigma - rho_{j-1}),
+//     d_j = rho_j rho_{j-1} d_{j-1} + (2 rho_j / delta) w_j, y_{j+1} = y_j + d_j.
+// A fixed polynomial in the Jacobi-scaled operator: linear, and symmetric positive definite
+// when B is (the polynomial is positive on (0, lmax]), so CG and BiCGStab take it unchanged.
+constexpr int kChebMax = 16;
+struct ChebPlan {
+    int degree = 0;                       // SpMVs per application: degree - 1
+    double inv_theta = 0;
+    double c1[kChebMax] = {}, c2[kChebMax] = {};
+};
+
+// lmax from Gershgorin on D^-1 B, lmin = lmax / 30 (the low end of the spectrum is left to
+// the Krylov method)
+static ChebPlan cheb_plan(double gershgorin, int degree) {
+    ChebPlan P;
+    P.degree = std::max(1, std::min(degree, kChebMax));
+    const double lmax = 1.05 * gershgorin, lmin = lmax / 30.0;
+    const double theta = 0.5 * (lmax + lmin), delta = 0.5 * (lmax - lmin), sigma = theta / delta;
+    P.inv_theta = 1.0 / theta;
+    double rho_prev = 1.0 / sigma;
+    for (int j = 1; j < P.degree; ++j) {
+        const double rho = 1.0 / (2.0 * sigma - rho_prev);
+        P.c1[j] = rho * rho_prev;
+        P.c2[j] = 2.0 * rho / delta;
+        rho_prev = rho;
+    }
+    return P;
+}
+
+// gate: 0 = skip once the solve is done (BiCGStab, true residual); 1 = skip when this CG
+// iteration's update did not run (the last update before `done` still completes its p)
+__device__ __forceinline__ bool gated(const KState* st, int gate) { return gate ? st->skip3 != 0 : st->done != 0; }
+
+template <class T>
+__global__ void cheb_init_kernel(const T* r, const T* invD, T* w, T* d, T* y, T inv_theta, int64_t n,
+                                 const KState* st, int gate) {
+    if (gated(st, gate)) return;
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        const T wi = invD[i] * r[i];
+        w[i] = wi;
+        const T di = wi * inv_theta;
+        d[i] = di;
+        y[i] = di;
+    }
+}
+
+template <class V, class T>
+__global__ void __launch_bounds__(kRedBlock) cheb_step_kernel(SpmvArgs A, const V* val, const T* rowsum, const T* d_in,
+                                                              const T* invD,
+                                                              T* w, T* d_out, T* y, T c1, T c2, const KState* st,
+                                                              int gate) {
+    if (gated(st, gate)) return;
+    int64_t s = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int lane = threadIdx.x & 31;
+    if (s >= A.nslices) return;
+    const T t = spmv_row<V, T>(A, val, rowsum, d_in, s, lane);
+    int64_t i = s * kSlice + lane;
+    if (i < A.n) {
+        const T wi = w[i] - invD[i] * t;
+        w[i] = wi;
+        const T di = c1 * d_in[i] + c2 * wi;
+        d_out[i] = di;
+        y[i] += di;
+    }
+}
+
+// FP32 evaluation of the polynomial for an FP64 Krylov iteration: w = invD32 (float) r
+__global__ void cheb_init_mixed_kernel(const double* r, const float* invD, float* w, float* d, float* y,
+                                       float inv_theta, int64_t n, const KState* st, int gate) {
+    if (gated(st, gate)) return;
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        const float wi = invD[i] * (float)r[i];
+        w[i] = wi;
+        const float di = wi * inv_theta;
+        d[i] = di;
+        y[i] = di;
+    }
+}
+__global__ void widen_kernel(const float* y, double* out, int64_t n, const KState* st, int gate) {
+    if (gated(st, gate)) return;
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = (double)y[i];
+}
+
+// CG with a polynomial preconditioner: rz = r . z, beta = rz / rz_old; p = z on a restart
+template <class T>
+__global__ void __launch_bounds__(kRedBlock) cg_rz_kernel(const T* r, const T* z, T* p, int set_p, int64_t n,
+                                                          double* part, KState* st, int gate) {
+    if (gated(st, gate)) return;
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    double v[1] = {0.0};
+    if (i < n) {
+        v[0] = (double)(r[i] * z[i]);
+        if (set_p) p[i] = z[i];
+    }
+    bool last;
+    block_reduce_publish<1>(v, part, st, gridDim.x, last);
+    if (last && threadIdx.x == 0) {
+        const double rz_old = st->rz;
+        st->rz = v[0];
+        st->beta = rz_old > 0 ? v[0] / rz_old : 0.0;
+    }
+}
+
+// p = z + beta p (runs whenever the update step of the same iteration ran)
+template <class T>
+__global__ void cg_pupdate_z_kernel(T* p, const T* z, int64_t n, const KState* st) {
+    if (st->skip3) return;
+    T beta = (T)st->beta;
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = z[i] + beta * p[i];
 }
 
 // residual r = rhs - B z (FP64), its FP32 copy, and the scalars that restart / continue CG
@@ -224,14 +372,14 @@ __global__ void bicg_p_kernel(T* p, T* phat, const T* r, const T* v, const T* in
 }
 // v = B phat; alpha = rho / (rhat . v)
 template <class V, class T>
-__global__ void __launch_bounds__(kRedBlock) bicg_v_kernel(SpmvArgs A, const V* val, const T* phat, T* v,
+__global__ void __launch_bounds__(kRedBlock) bicg_v_kernel(SpmvArgs A, const V* val, const T* rowsum, const T* phat, T* v,
                                                            const T* rhat, double* part, KState* st) {
     if (st->done) return;
     int64_t s = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
     double d[1] = {0.0};
     if (s < A.nslices) {
-        T y = sell_row<V, T>(A.slice_ptr, A.width, A.col, val, phat, s, lane);
+        T y = spmv_row<V, T>(A, val, rowsum, phat, s, lane);
         int64_t i = s * kSlice + lane;
         if (i < A.n) {
             v[i] = y;
@@ -263,14 +411,15 @@ __global__ void bicg_s_kernel(T* r, T* shat, const T* v, const T* invD, int64_t 
 }
 // t = B shat; omega = (t . s) / (t . t)
 template <class V, class T>
-__global__ void __launch_bounds__(kRedBlock) bicg_t_kernel(SpmvArgs A, const V* val, const T* shat, T* t, const T* s_vec,
+__global__ void __launch_bounds__(kRedBlock) bicg_t_kernel(SpmvArgs A, const V* val, const T* rowsum, const T* shat, T* t,
+                                                           const T* s_vec,
                                                            double* part, KState* st) {
     if (st->done) return;
     int64_t sl = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
     double d[2] = {0.0, 0.0};
     if (sl < A.nslices) {
-        T y = sell_row<V, T>(A.slice_ptr, A.width, A.col, val, shat, sl, lane);
+        T y = spmv_row<V, T>(A, val, rowsum, shat, sl, lane);
         int64_t i = sl * kSlice + lane;
         if (i < A.n) {
             t[i] = y;
@@ -306,6 +455,7 @@ __global__ void __launch_bounds__(kRedBlock) bicg_x_kernel(T* x, T* r, const T* 
         st->rho = d[0];
         st->rn2 = d[1];
         if (d[1] <= st->tol2 || !isfinite(d[1])) st->done = 1;
+        if (d[1] > st->div2) st->done = st->breakdown = 1;
         if (st->omega == 0.0 || rho_old == 0.0) {
             st->done = 1;
             st->breakdown = 1;
@@ -435,12 +585,31 @@ void fvm_template::build_steady() {
         if (!fixed[r] && !(invD[r] > 0)) fail(FVM_ERR_INVALID_ARGUMENT, "steady operator has a non-positive diagonal");
     }
     symmetric = asym <= 1e-12 * std::max(scale, 1e-300) ? 1 : 0;
+    // Gershgorin bound on the spectrum of D^-1 B (for the Chebyshev preconditioner)
+    cheb_gershgorin = 1.0;
+    for (int64_t r = 0; r < n; ++r) {
+        double row = 0;
+        for (int64_t q = pat.rowptr[r]; q < pat.rowptr[r + 1]; ++q) row += std::fabs(Bv[pat.csr_slot[q]]);
+        cheb_gershgorin = std::max(cheb_gershgorin, row * std::fabs(invD[r]));
+    }
     double bn = 0;
     for (int64_t r = 0; r < n; ++r) bn += b[r] * b[r];
     bnorm = std::sqrt(bn);
-    std::vector<float> Bv32(Bv.size()), invD32(n), invV32(n);
+    // FP32 operator in difference form: off-diagonal values (zero diagonal) and FP64 row sums
+    std::vector<float> Bv32(Bv.size(), 0.0f), rs32(n), invD32(n), invV32(n);
     std::vector<double> invV(n);
-    for (size_t i = 0; i < Bv.size(); ++i) Bv32[i] = (float)Bv[i];
+    for (int64_t s = 0; s < pat.nslices; ++s)
+        for (int lane = 0; lane < kSlice; ++lane) {
+            const int64_t r = s * kSlice + lane;
+            if (r >= n) continue;
+            double rs = 0;
+            for (int64_t q = 0; q < pat.width[s]; ++q) {
+                const int64_t slot = pat.slice_ptr[s] + q * kSlice + lane;
+                rs += Bv[slot];
+                if (pat.col[slot] != r) Bv32[slot] = (float)Bv[slot];
+            }
+            rs32[r] = (float)rs;
+        }
     for (int64_t r = 0; r < n; ++r) {
         invD32[r] = (float)invD[r];
         invV[r] = fixed[r] ? 0.0 : 1.0 / Vr[r];
@@ -448,6 +617,7 @@ void fvm_template::build_steady() {
     }
     d_bval64.upload(Bv);
     d_bval32.upload(Bv32);
+    d_brow32.upload(rs32);
     d_bdiag_inv64.upload(invD);
     d_bdiag_inv32.upload(invD32);
     d_rhs_red.upload(rhs);
@@ -487,7 +657,45 @@ struct Solver {
 template <class T>
 struct Vecs {
     T *x, *r, *p, *Ap, *rhat, *phat, *shat, *t;
+    T *w, *d0, *d1;                    // Chebyshev work vectors
+    float *fw, *fd0, *fd1, *fy;        // FP32 Chebyshev work vectors (FVM_SOLVE_FP32_PRECOND)
 };
+
+constexpr int kWorkVectors = 13;  // 11 vectors of the Krylov type + 4 FP32 vectors (2 doubles' worth)
+
+// y = p(D^-1 B) D^-1 r (Chebyshev preconditioner; see cheb_plan)
+// the same polynomial in FP32 (FP32 values, vectors and accumulation) for an FP64 iteration
+static void cheb_apply_fp32(const Solver& S, const ChebPlan& P, const float* val32, const float* rowsum32,
+                            const float* invD32, const double* r, double* y, Vecs<double>& v, int gate) {
+    cheb_init_mixed_kernel<<<S.nb, kRedBlock, 0, S.s>>>(r, invD32, v.fw, v.fd0, v.fy, (float)P.inv_theta, S.n, S.st,
+                                                        gate);
+    float *din = v.fd0, *dout = v.fd1;
+    for (int j = 1; j < P.degree; ++j) {
+        cheb_step_kernel<float, float><<<S.nbs, kRedBlock, 0, S.s>>>(S.A, val32, rowsum32, din, invD32, v.fw, dout,
+                                                                     v.fy, (float)P.c1[j], (float)P.c2[j], S.st, gate);
+        std::swap(din, dout);
+    }
+    widen_kernel<<<S.nb, kRedBlock, 0, S.s>>>(v.fy, y, S.n, S.st, gate);
+}
+
+template <class V, class T>
+static void cheb_apply(const Solver& S, const ChebPlan& P, const V* val, const T* rowsum, const T* invD, const T* r,
+                       T* y, Vecs<T>& v, int gate) {
+    if constexpr (std::is_same_v<T, double>) {
+        if (v.fw) {  // FP32 polynomial
+            cheb_apply_fp32(S, P, S.T->d_bval32.as<float>(), S.T->d_brow32.as<float>(), S.T->d_bdiag_inv32.as<float>(),
+                            r, y, v, gate);
+            return;
+        }
+    }
+    cheb_init_kernel<T><<<S.nb, kRedBlock, 0, S.s>>>(r, invD, v.w, v.d0, y, (T)P.inv_theta, S.n, S.st, gate);
+    T *din = v.d0, *dout = v.d1;
+    for (int j = 1; j < P.degree; ++j) {
+        cheb_step_kernel<V, T><<<S.nbs, kRedBlock, 0, S.s>>>(S.A, val, rowsum, din, invD, v.w, dout, y, (T)P.c1[j],
+                                                             (T)P.c2[j], S.st, gate);
+        std::swap(din, dout);
+    }
+}
 
 }  // namespace
 
@@ -498,6 +706,7 @@ static void run_krylov(fvm_template* Tm, Solver& S, bool cg, bool mixed, const f
     cudaStream_t s = S.s;
     const V* val = mixed ? (const V*)Tm->d_bval32.p : (const V*)Tm->d_bval64.p;
     const T* invD = mixed ? (const T*)Tm->d_bdiag_inv32.p : (const T*)Tm->d_bdiag_inv64.p;
+    const T* rowsum = mixed ? (const T*)Tm->d_brow32.p : nullptr;  // FP32 products in difference form
     const T* invV = mixed ? (const T*)Tm->d_invV_free32.p : (const T*)Tm->d_invV_free64.p;
     Vecs<T> v;
     T* base = (T*)S.vec;
@@ -509,14 +718,41 @@ static void run_krylov(fvm_template* Tm, Solver& S, bool cg, bool mixed, const f
     v.phat = base + 5 * n;
     v.shat = base + 6 * n;
     v.t = base + 7 * n;
+    v.w = base + 8 * n;
+    v.d0 = base + 9 * n;
+    v.d1 = base + 10 * n;
+    v.fw = v.fd0 = v.fd1 = v.fy = nullptr;
+    if (o.mode == FVM_SOLVE_FP32_PRECOND && !mixed) {
+        float* fb = (float*)(base + 11 * n);
+        v.fw = fb;
+        v.fd0 = fb + n;
+        v.fd1 = fb + 2 * n;
+        v.fy = fb + 3 * n;
+    }
+    const bool cheb = o.precond == FVM_PRECOND_CHEBYSHEV;
+    const ChebPlan plan = cheb ? cheb_plan(Tm->cheb_gershgorin, o.cheb_degree > 0 ? o.cheb_degree : 4) : ChebPlan{};
+    T* zc = v.rhat;  // CG's preconditioned residual (BiCGStab's rhat is unused by CG)
     FVM_CUDA(cudaMemsetAsync(v.x, 0, sizeof(T) * n, s));
     const double tol = o.rtol * Tm->bnorm;
     const double tol2 = tol * tol;
     const int64_t maxit = o.max_iters > 0 ? o.max_iters : 1000000;
-    const double red = o.inner_reduction > 0 && o.inner_reduction < 1 ? o.inner_reduction : 1e-2;
+    // FP32 inner arithmetic (mixed: the whole Krylov iteration; fp32pc: the preconditioner's
+    // polynomial) makes the iteration run in cycles: each cycle reduces the residual by
+    // `inner_reduction` (at most 1e-2 with an FP32 polynomial), then the FP64 true residual is
+    // recomputed.  FP32 rounding makes the preconditioner slightly nonlinear, which BiCGStab's
+    // short recurrences do not tolerate for long: its cycles restart from the FP64 residual.
+    const bool fp32pc = o.mode == FVM_SOLVE_FP32_PRECOND && !mixed;
+    const bool cycles = mixed || fp32pc;
+    double red = o.inner_reduction > 0 && o.inner_reduction < 1 ? o.inner_reduction : 1e-2;
+    if (fp32pc) red = std::min(red, 1e-2);
     KState h{};
     auto set_tol = [&](double t2) {
         FVM_CUDA(cudaMemcpyAsync(&S.st->tol2, &t2, sizeof(double), cudaMemcpyHostToDevice, s));
+    };
+    // cycles with FP32 inner arithmetic stop when their recurrence residual grows 1e4-fold
+    auto set_div = [&](double rn0) {
+        const double d2 = cycles ? 1e8 * rn0 * rn0 : std::numeric_limits<double>::infinity();
+        FVM_CUDA(cudaMemcpyAsync(&S.st->div2, &d2, sizeof(double), cudaMemcpyHostToDevice, s));
     };
     auto read_state = [&]() {
         FVM_CUDA(cudaMemcpyAsync(&h, S.st, sizeof(KState), cudaMemcpyDeviceToHost, s));
@@ -525,9 +761,14 @@ static void run_krylov(fvm_template* Tm, Solver& S, bool cg, bool mixed, const f
     // true residual from z64 (FP64); sets r, optionally p, rz, rn2, done
     auto true_residual = [&](bool set_p) {
         set_tol(tol2);
+        const bool poly_cg = cg && cheb;
         residual_kernel<T><<<S.nbs, kRedBlock, 0, s>>>(S.A, Tm->d_bval64.as<double>(), S.z64, Tm->d_rhs_red.as<double>(),
-                                                      Tm->d_invV_free64.as<double>(), invD, v.r, v.p, set_p ? 1 : 0,
-                                                      S.part, S.st);
+                                                      Tm->d_invV_free64.as<double>(), invD, v.r, v.p,
+                                                      set_p && !poly_cg ? 1 : 0, S.part, S.st);
+        if (poly_cg) {  // rz = r . M^-1 r, and p = M^-1 r on a restart
+            cheb_apply<V, T>(S, plan, val, rowsum, invD, v.r, zc, v, 0);
+            cg_rz_kernel<T><<<S.nb, kRedBlock, 0, s>>>(v.r, zc, v.p, set_p ? 1 : 0, n, S.part, S.st, 0);
+        }
         FVM_CUDA(cudaGetLastError());
         read_state();
         ++stats.refinements;
@@ -543,13 +784,14 @@ static void run_krylov(fvm_template* Tm, Solver& S, bool cg, bool mixed, const f
     static const bool trace = std::getenv("FVM_SOLVER_TRACE") != nullptr;
     // inner target: the FP32 recurrence is trusted down to `red_cur` of the last true residual
     auto inner_tol2 = [&]() {
-        double t = mixed ? std::max(tol, red_cur * rn_last_update) : tol;
+        double t = cycles ? std::max(tol, red_cur * rn_last_update) : tol;
         return t * t;
     };
     bool need_start = !cg;
     while (rn > tol) {
         if (it >= maxit) break;
         set_tol(inner_tol2());
+        set_div(rn);
         if (need_start) {
             // BiCGStab restart from the current residual: rhat = r, p = v = 0, rho = r.r
             bicg_start_kernel<T><<<S.nb, kRedBlock, 0, s>>>(v.rhat, v.r, v.p, v.Ap, n, S.part, S.st);
@@ -557,14 +799,25 @@ static void run_krylov(fvm_template* Tm, Solver& S, bool cg, bool mixed, const f
         }
         for (int c = 0; c < chunk; ++c) {
             if (cg) {
-                cg_spmv_kernel<V, T><<<S.nbs, kRedBlock, 0, s>>>(S.A, val, v.p, v.Ap, S.part, S.st);
-                cg_update_kernel<T><<<S.nb, kRedBlock, 0, s>>>(v.x, v.r, v.p, v.Ap, invD, invV, n, S.part, S.st);
-                cg_pupdate_kernel<T><<<S.nb, kRedBlock, 0, s>>>(v.p, v.r, invD, n, S.st);
+                cg_spmv_kernel<V, T><<<S.nbs, kRedBlock, 0, s>>>(S.A, val, rowsum, v.p, v.Ap, S.part, S.st);
+                if (cheb) {
+                    cg_update_kernel<T, false><<<S.nb, kRedBlock, 0, s>>>(v.x, v.r, v.p, v.Ap, invD, invV, n, S.part,
+                                                                          S.st);
+                    cheb_apply<V, T>(S, plan, val, rowsum, invD, v.r, zc, v, 1);
+                    cg_rz_kernel<T><<<S.nb, kRedBlock, 0, s>>>(v.r, zc, v.p, 0, n, S.part, S.st, 1);
+                    cg_pupdate_z_kernel<T><<<S.nb, kRedBlock, 0, s>>>(v.p, zc, n, S.st);
+                } else {
+                    cg_update_kernel<T, true><<<S.nb, kRedBlock, 0, s>>>(v.x, v.r, v.p, v.Ap, invD, invV, n, S.part,
+                                                                         S.st);
+                    cg_pupdate_kernel<T><<<S.nb, kRedBlock, 0, s>>>(v.p, v.r, invD, n, S.st);
+                }
             } else {
                 bicg_p_kernel<T><<<S.nb, kRedBlock, 0, s>>>(v.p, v.phat, v.r, v.Ap, invD, n, S.st);
-                bicg_v_kernel<V, T><<<S.nbs, kRedBlock, 0, s>>>(S.A, val, v.phat, v.Ap, v.rhat, S.part, S.st);
+                if (cheb) cheb_apply<V, T>(S, plan, val, rowsum, invD, v.p, v.phat, v, 0);  // phat = M^-1 p
+                bicg_v_kernel<V, T><<<S.nbs, kRedBlock, 0, s>>>(S.A, val, rowsum, v.phat, v.Ap, v.rhat, S.part, S.st);
                 bicg_s_kernel<T><<<S.nb, kRedBlock, 0, s>>>(v.r, v.shat, v.Ap, invD, n, S.st);
-                bicg_t_kernel<V, T><<<S.nbs, kRedBlock, 0, s>>>(S.A, val, v.shat, v.t, v.r, S.part, S.st);
+                if (cheb) cheb_apply<V, T>(S, plan, val, rowsum, invD, v.r, v.shat, v, 0);  // shat = M^-1 s
+                bicg_t_kernel<V, T><<<S.nbs, kRedBlock, 0, s>>>(S.A, val, rowsum, v.shat, v.t, v.r, S.part, S.st);
                 bicg_x_kernel<T><<<S.nb, kRedBlock, 0, s>>>(v.x, v.r, v.phat, v.shat, v.t, v.rhat, invV, n, S.part, S.st);
             }
         }
@@ -574,13 +827,14 @@ static void run_krylov(fvm_template* Tm, Solver& S, bool cg, bool mixed, const f
         if (!h.done) continue;
         // reliable update: fold the correction into the FP64 solution, recompute the residual
         accumulate_kernel<T><<<S.nb, kRedBlock, 0, s>>>(S.z64, v.x, 1.0, n);
-        bool restart = h.breakdown != 0;
+        bool restart = h.breakdown != 0 || (cycles && !cg);
         const double rec = std::sqrt(h.rn2);
         const int brk = h.breakdown;
         double rn_new = true_residual(restart);
         if (trace)
             std::fprintf(stderr, "[fvm solver] %s %s it=%lld rn=%.3e (recurrence %.3e) breakdown=%d\n",
-                         cg ? "cg" : "bicgstab", mixed ? "mixed" : "fp64", (long long)it, rn_new / Tm->bnorm,
+                         cg ? "cg" : "bicgstab", mixed ? "mixed" : fp32pc ? "fp32-precond" : "fp64", (long long)it,
+                         rn_new / Tm->bnorm,
                          rec / Tm->bnorm, brk);
         if (!(rn_new < rn)) {
             // the correction raised the true residual (inner-precision drift or breakdown):
@@ -589,7 +843,7 @@ static void run_krylov(fvm_template* Tm, Solver& S, bool cg, bool mixed, const f
             rn_new = true_residual(true);
             restart = true;
             red_cur = std::min(0.5, red_cur * 4);
-            if (++rejects > 6) break;
+            if (++rejects > (fp32pc ? 2 : 6)) break;
         }
         FVM_CUDA(cudaMemsetAsync(v.x, 0, sizeof(T) * n, s));
         rn = rn_new;
@@ -633,16 +887,21 @@ extern "C" int fvm_template_steady_solve(fvm_template* Tm, double* x, const fvm_
         if (loc == FVM_PTR_DEVICE_INTERNAL) fail(FVM_ERR_INVALID_ARGUMENT, "steady solve takes host or device arrays in the caller's numbering");
         fvm_solver_stats st{};
         bool mixed = opt->mode == FVM_SOLVE_MIXED;
+        if (opt->mode == FVM_SOLVE_FP32_PRECOND && opt->precond != FVM_PRECOND_CHEBYSHEV)
+            fail(FVM_ERR_INVALID_ARGUMENT, "the FP32 inner iteration is the Chebyshev preconditioner: set precond");
         bool cg = opt->method == FVM_SOLVER_CG || (opt->method == FVM_SOLVER_AUTO && Tm->symmetric);
         st.method_used = cg ? FVM_SOLVER_CG : FVM_SOLVER_BICGSTAB;
         st.symmetric = Tm->symmetric;
-        if (opt->precond != FVM_PRECOND_JACOBI) fail(FVM_ERR_INVALID_ARGUMENT, "only the Jacobi preconditioner is available");
+        if (opt->precond != FVM_PRECOND_JACOBI && opt->precond != FVM_PRECOND_CHEBYSHEV)
+            fail(FVM_ERR_INVALID_ARGUMENT, "unknown preconditioner");
+        if (opt->precond == FVM_PRECOND_CHEBYSHEV && opt->cheb_degree > kChebMax)
+            fail(FVM_ERR_INVALID_ARGUMENT, "Chebyshev degree above 16");
         Solver S(Tm, s);
         // vectors sized for FP64 even in mixed mode: a stalled mixed solve finishes in FP64
         // (run_krylov<double, double>) on the same workspace
         size_t elem = sizeof(double);
         size_t bytes = sizeof(KState) + sizeof(double) * 8 * (size_t)std::max(S.nb, S.nbs) + sizeof(double) * 3 * n +
-                       elem * 8 * n + 256;
+                       elem * kWorkVectors * n + 256;
         S.ws.alloc(bytes);
         char* w = S.ws.as<char>();
         S.st = (KState*)w;
@@ -677,6 +936,17 @@ extern "C" int fvm_template_steady_solve(fvm_template* Tm, double* x, const fvm_
                     // the FP32 inner iteration stalled: finish in FP64 from the current solution
                     st.fallback_fp64 = 1;
                     run_krylov<double, double>(Tm, S, cg, false, *opt, st);
+                }
+            } else if (opt->mode == FVM_SOLVE_FP32_PRECOND) {
+                try {
+                    run_krylov<double, double>(Tm, S, cg, false, *opt, st);
+                } catch (const Error& e) {
+                    if (e.code != FVM_ERR_NOT_CONVERGED) throw;
+                    // the FP32 polynomial stalled the iteration: finish with the FP64 polynomial
+                    st.fallback_fp64 = 1;
+                    fvm_solver_options o64 = *opt;
+                    o64.mode = FVM_SOLVE_FP64;
+                    run_krylov<double, double>(Tm, S, cg, false, o64, st);
                 }
             } else {
                 run_krylov<double, double>(Tm, S, cg, false, *opt, st);

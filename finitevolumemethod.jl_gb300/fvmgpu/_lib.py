@@ -33,7 +33,7 @@ FVM_TEMPLATE_DIFFUSION, FVM_TEMPLATE_LINEAR_REACTION_DIFFUSION = 0, 1
 FVM_TEMPLATE_POISSON, FVM_TEMPLATE_MEAN_EXIT_TIME = 2, 3
 FVM_SOLVER_AUTO, FVM_SOLVER_CG, FVM_SOLVER_BICGSTAB = 0, 1, 2
 FVM_PRECOND_JACOBI, FVM_PRECOND_CHEBYSHEV = 0, 1
-FVM_SOLVE_FP64, FVM_SOLVE_MIXED = 0, 1
+FVM_SOLVE_FP64, FVM_SOLVE_MIXED, FVM_SOLVE_FP32_PRECOND = 0, 1, 2
 
 
 class FVMError(RuntimeError):

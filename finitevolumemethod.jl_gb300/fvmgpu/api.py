@@ -928,13 +928,18 @@ class Tsit5:
 @dataclass
 class KrylovSolver:
     """GPU steady solver: method "auto" (CG if symmetric, else BiCGStab), "cg", "bicgstab";
-    mode "fp64" or "mixed" (FP32 inner iterations with FP64 reliable updates)."""
+    precond "jacobi" or "chebyshev" (a degree-`cheb_degree` Chebyshev polynomial in the
+    Jacobi-scaled operator); mode "fp64", "mixed" (the Krylov iteration in FP32 with FP64
+    reliable updates of the residual and solution) or "fp32_precond" (the Krylov iteration in
+    FP64, its inner iterations - the Chebyshev polynomial - in FP32)."""
 
     mode: str = "fp64"
     method: str = "auto"
     rtol: float = 1e-10
     max_iters: int = 1_000_000
     inner_reduction: float = 1e-1
+    precond: str = "jacobi"
+    cheb_degree: int = 4
 
 
 @dataclass
@@ -986,17 +991,25 @@ def solve(prob, alg=None, *, saveat=None, dt=None, adaptive=None, abstol=1e-6, r
         so.max_iters = opt.max_iters
         so.method = {"auto": _lib.FVM_SOLVER_AUTO, "cg": _lib.FVM_SOLVER_CG,
                      "bicgstab": _lib.FVM_SOLVER_BICGSTAB}[opt.method]
-        so.precond = _lib.FVM_PRECOND_JACOBI
-        so.mode = _lib.FVM_SOLVE_MIXED if opt.mode == "mixed" else _lib.FVM_SOLVE_FP64
+        so.precond = {"jacobi": _lib.FVM_PRECOND_JACOBI, "chebyshev": _lib.FVM_PRECOND_CHEBYSHEV}[opt.precond]
+        so.cheb_degree = int(opt.cheb_degree)
+        so.mode = {"fp64": _lib.FVM_SOLVE_FP64, "mixed": _lib.FVM_SOLVE_MIXED,
+                   "fp32_precond": _lib.FVM_SOLVE_FP32_PRECOND}[opt.mode]
         so.inner_reduction = opt.inner_reduction
         x = np.zeros(prob.mesh.triangulation.num_points)
         st = _lib.SolverStats()
-        check(lib.fvm_template_steady_solve(prob.handle, C.c_void_p(x.ctypes.data), C.byref(so), C.byref(st),
-                                            _lib.FVM_PTR_HOST, s))
-        return LinearSolution(x, {"iterations": st.iterations, "refinements": st.refinements,
-                                  "rel_residual": st.rel_residual, "elapsed_ms": st.elapsed_ms,
-                                  "method": "cg" if st.method_used == _lib.FVM_SOLVER_CG else "bicgstab",
-                                  "symmetric": bool(st.symmetric), "fallback_fp64": bool(st.fallback_fp64)})
+        status = lib.fvm_template_steady_solve(prob.handle, C.c_void_p(x.ctypes.data), C.byref(so), C.byref(st),
+                                               _lib.FVM_PTR_HOST, s)
+        sol = LinearSolution(x, {"iterations": st.iterations, "refinements": st.refinements,
+                                 "rel_residual": st.rel_residual, "elapsed_ms": st.elapsed_ms,
+                                 "method": "cg" if st.method_used == _lib.FVM_SOLVER_CG else "bicgstab",
+                                 "symmetric": bool(st.symmetric), "fallback_fp64": bool(st.fallback_fp64)})
+        try:
+            check(status)
+        except _lib.NotConvergedError as e:
+            e.solution = sol  # the last iterate and its statistics
+            raise
+        return sol
     if isinstance(prob, _TimeTemplate):
         t0, tf, u0 = prob.initial_time, prob.final_time, prob.u0
     elif isinstance(prob, FVMProblem):

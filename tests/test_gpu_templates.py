@@ -71,24 +71,26 @@ def test_poisson_exact_solution_gpu(gpu_lib):
     prob = F.PoissonsEquation(mesh, BCs, source_function=lambda x, y, p: -np.sin(np.pi * x) * np.sin(np.pi * y))
     P = tri.points
     exact = np.sin(np.pi * P[:, 0]) * np.sin(np.pi * P[:, 1]) / (2 * np.pi**2)
-    for mode in ("fp64", "mixed"):
-        sol = F.solve(prob, F.KrylovSolver(mode=mode))
+    for mode, precond in (("fp64", "jacobi"), ("mixed", "jacobi"), ("fp64", "chebyshev"), ("mixed", "chebyshev")):
+        sol = F.solve(prob, F.KrylovSolver(mode=mode, precond=precond))
         assert sol.stats["rel_residual"] <= 1e-10
         assert np.linalg.norm(sol.u - exact) <= 1e-4 * np.linalg.norm(exact)
 
 
+@pytest.mark.parametrize("precond", ["jacobi", "chebyshev"])
 @pytest.mark.parametrize("mode", ["fp64", "mixed"])
 @pytest.mark.parametrize("jump", [False, True])
-def test_steady_disk_against_direct_solve(gpu_lib, mode, jump):
+def test_steady_disk_against_direct_solve(gpu_lib, mode, jump, precond):
     """Disk Poisson (f = -1) with D = 1 or the 1 / 10 jump at r = 0.5 (non-symmetric operator:
-    BiCGStab), against scipy's direct solve of the oracle's assembled system."""
+    BiCGStab), Jacobi or Chebyshev (degree 4) preconditioning, against scipy's direct solve of
+    the oracle's assembled system."""
     import fvmgpu as F
 
     tri = triangulate_disk(6000, 256, seed=4)
     mesh, BCs = _mesh_bcs(F, tri, [lambda x, y, t, u, p: 0.0 * x], ["Dirichlet"])
     D = (lambda x, y, p: np.where(x * x + y * y < 0.25, 1.0, 10.0)) if jump else (lambda x, y, p: 1.0 + 0.0 * x)
     prob = F.PoissonsEquation(mesh, BCs, diffusion_function=D, source_function=lambda x, y, p: -1.0 + 0.0 * x)
-    sol = F.solve(prob, F.KrylovSolver(mode=mode, rtol=1e-10))
+    sol = F.solve(prob, F.KrylovSolver(mode=mode, rtol=1e-10, precond=precond))
     conds = O.Conditions(tri, [lambda x, y, t, u: 0.0 * x], ["Dirichlet"])
     A, b = O.template_poisson(tri, conds, lambda x, y: D(x, y, None), lambda x, y: -1.0 + 0.0 * x)
     ref = O.steady_solve(A, b)
@@ -96,6 +98,31 @@ def test_steady_disk_against_direct_solve(gpu_lib, mode, jump):
     assert res <= 1e-10, (res, sol.stats)
     assert np.linalg.norm(sol.u - ref) <= 1e-7 * np.linalg.norm(ref)
     assert sol.stats["method"] == ("bicgstab" if jump else "cg")
+    if precond == "chebyshev":  # fewer outer iterations than Jacobi alone
+        jac = F.solve(prob, F.KrylovSolver(mode=mode, rtol=1e-10))
+        assert sol.stats["iterations"] < jac.stats["iterations"], (sol.stats, jac.stats)
+
+
+@pytest.mark.parametrize("jump", [False, True])
+def test_steady_fp32_inner_iterations(gpu_lib, jump):
+    """FP64 Krylov with its inner iterations (the Chebyshev polynomial) in FP32: the same
+    1e-10 FP64 residual, about as many outer iterations as the all-FP64 solve."""
+    import fvmgpu as F
+
+    tri = triangulate_disk(6000, 256, seed=4)
+    mesh, BCs = _mesh_bcs(F, tri, [lambda x, y, t, u, p: 0.0 * x], ["Dirichlet"])
+    D = (lambda x, y, p: np.where(x * x + y * y < 0.25, 1.0, 10.0)) if jump else (lambda x, y, p: 1.0 + 0.0 * x)
+    prob = F.PoissonsEquation(mesh, BCs, diffusion_function=D, source_function=lambda x, y, p: -1.0 + 0.0 * x)
+    sol = F.solve(prob, F.KrylovSolver(mode="fp32_precond", precond="chebyshev", rtol=1e-10))
+    ref64 = F.solve(prob, F.KrylovSolver(mode="fp64", precond="chebyshev", rtol=1e-10))
+    conds = O.Conditions(tri, [lambda x, y, t, u: 0.0 * x], ["Dirichlet"])
+    A, b = O.template_poisson(tri, conds, lambda x, y: D(x, y, None), lambda x, y: -1.0 + 0.0 * x)
+    assert np.linalg.norm(b - A @ sol.u) / np.linalg.norm(b) <= 1e-10
+    assert np.linalg.norm(sol.u - O.steady_solve(A, b)) <= 1e-7 * np.linalg.norm(sol.u)
+    assert not sol.stats["fallback_fp64"]
+    assert sol.stats["iterations"] <= 1.5 * ref64.stats["iterations"] + 16, (sol.stats, ref64.stats)
+    with pytest.raises(F.FVMError):  # the FP32 inner iteration is the Chebyshev polynomial
+        F.solve(prob, F.KrylovSolver(mode="fp32_precond", precond="jacobi"))
 
 
 def test_mean_exit_time_gpu(gpu_lib):
