@@ -107,8 +107,8 @@ __global__ void transpose_vals_kernel(const int64_t* __restrict__ tperm, const d
 }
 
 // G[k][b] += sum_{i < ns} kb_i[row(k)][b] * Y_i[col(k)][b].  Every (entry, instance) pair is
-// independent: with many instances a warp takes an entry and its lanes the instances (loads
-// coalesced across lanes); with few, a thread takes an entry and loops over the instances.
+// independent: with many instances a thread takes a pair (consecutive threads, consecutive
+// instances: coalesced); with few, a thread takes an entry and loops over the instances.
 struct StagePair {
     const double* kb[6];
     const double* Y[6];
@@ -122,12 +122,12 @@ __device__ __forceinline__ void grad_accum_one(const StagePair& P, double* G, in
         if (j < P.ns) acc += P.kb[j][r * B + b] * P.Y[j][c * B + b];
     G[k * B + b] = acc;
 }
-__global__ void grad_accum_warp_kernel(const int32_t* __restrict__ erow, const int32_t* __restrict__ col, StagePair P,
+__global__ void grad_accum_elem_kernel(const int32_t* __restrict__ erow, const int32_t* __restrict__ col, StagePair P,
                                        double* __restrict__ G, int64_t nnz, int B) {
-    const int64_t k = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (k >= nnz) return;
-    const int64_t r = __ldg(&erow[k]), c = __ldg(&col[k]);
-    for (int64_t b = threadIdx.x & 31; b < B; b += 32) grad_accum_one(P, G, k, r, c, b, B);
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nnz * B) return;
+    const int64_t k = i / B;
+    grad_accum_one(P, G, k, __ldg(&erow[k]), __ldg(&col[k]), i - k * B, B);
 }
 __global__ void grad_accum_thread_kernel(const int32_t* __restrict__ erow, const int32_t* __restrict__ col,
                                          StagePair P, double* __restrict__ G, int64_t nnz, int B) {
@@ -138,8 +138,8 @@ __global__ void grad_accum_thread_kernel(const int32_t* __restrict__ erow, const
 }
 void launch_grad_accum(const fvm_adjoint* a, const StagePair& P, double* G, cudaStream_t s) {
     if (a->B >= 16)
-        grad_accum_warp_kernel<<<blocks(a->nnz * 32, 256), 256, 0, s>>>(a->d_erow.as<int32_t>(), a->d_col.as<int32_t>(),
-                                                                         P, G, a->nnz, a->B);
+        grad_accum_elem_kernel<<<blocks(a->nnz * a->B, 256), 256, 0, s>>>(a->d_erow.as<int32_t>(),
+                                                                           a->d_col.as<int32_t>(), P, G, a->nnz, a->B);
     else
         grad_accum_thread_kernel<<<blocks(a->nnz, 256), 256, 0, s>>>(a->d_erow.as<int32_t>(), a->d_col.as<int32_t>(), P,
                                                                      G, a->nnz, a->B);

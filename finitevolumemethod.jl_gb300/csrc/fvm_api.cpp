@@ -275,6 +275,17 @@ static void tsit5_run(OdeRhs& rhs, int64_t n, const double* u0_int, const fvm_od
     }
 }
 
+// Device address of a page-locked host array (cudaHostAlloc / cudaHostRegister), or nullptr
+// for pageable memory.  Kernels read and write such arrays directly over the host link.
+static void* host_mapped(const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 // u/du pointer handling shared by fvm_rhs and fvm_template_apply
 struct IoPlan {
     const double* uin = nullptr;  // internal-order input (device)
@@ -290,8 +301,12 @@ static void rhs_inputs(fvm_problem* p, const double* u, double* du, int32_t loc,
     }
     p->ensure_work();
     if (loc == FVM_PTR_HOST) {
-        FVM_CUDA(cudaMemcpyAsync(p->d_ref.p, u, sizeof(double) * m->np, cudaMemcpyHostToDevice, s));
-        launch_permute_in(m->d_perm.as<int32_t>(), p->d_ref.as<double>(), p->d_u.as<double>(), m->np, s);
+        if (const void* mapped = host_mapped(u)) {  // no staging copy: the permutation reads the host array
+            launch_permute_in_seq(m->d_iperm.as<int32_t>(), (const double*)mapped, p->d_u.as<double>(), m->np, s);
+        } else {
+            FVM_CUDA(cudaMemcpyAsync(p->d_ref.p, u, sizeof(double) * m->np, cudaMemcpyHostToDevice, s));
+            launch_permute_in(m->d_perm.as<int32_t>(), p->d_ref.as<double>(), p->d_u.as<double>(), m->np, s);
+        }
     } else {
         launch_permute_in(m->d_perm.as<int32_t>(), u, p->d_u.as<double>(), m->np, s);
     }
@@ -303,8 +318,12 @@ static void rhs_outputs(fvm_problem* p, double* du, int32_t loc, cudaStream_t s)
     fvm_mesh* m = p->mesh;
     if (loc == FVM_PTR_DEVICE_INTERNAL) return;
     if (loc == FVM_PTR_HOST) {
-        launch_permute_out(m->d_perm.as<int32_t>(), p->d_du.as<double>(), p->d_ref.as<double>(), m->np, s);
-        FVM_CUDA(cudaMemcpyAsync(du, p->d_ref.p, sizeof(double) * m->np, cudaMemcpyDeviceToHost, s));
+        if (void* mapped = host_mapped(du)) {  // the permutation writes the host array
+            launch_permute_out_seq(m->d_iperm.as<int32_t>(), p->d_du.as<double>(), (double*)mapped, m->np, s);
+        } else {
+            launch_permute_out(m->d_perm.as<int32_t>(), p->d_du.as<double>(), p->d_ref.as<double>(), m->np, s);
+            FVM_CUDA(cudaMemcpyAsync(du, p->d_ref.p, sizeof(double) * m->np, cudaMemcpyDeviceToHost, s));
+        }
         FVM_CUDA(cudaStreamSynchronize(s));
         check_device_error();
     } else {

@@ -171,6 +171,9 @@ void launch_to_f32(const double* x, float* y, int64_t n, cudaStream_t s);
 unsigned take_device_error();
 void launch_permute_in(const int32_t* perm, const double* xref, double* xint, int64_t n, cudaStream_t s);
 void launch_permute_out(const int32_t* perm, const double* xint, double* xref, int64_t n, cudaStream_t s);
+// the same with iperm (caller -> internal) and the caller's side in order (host-mapped arrays)
+void launch_permute_in_seq(const int32_t* iperm, const double* xref, double* xint, int64_t n, cudaStream_t s);
+void launch_permute_out_seq(const int32_t* iperm, const double* xint, double* xref, int64_t n, cudaStream_t s);
 void launch_dirichlet(const int32_t* idx, const double* val, double* u, int64_t n, cudaStream_t s);
 void launch_triangle_rhs(const fvm_mesh* m, const fvm_problem* p, const double* u, double* du, cudaStream_t s);
 // Tsit5 stage: y = u + dt * sum_j a[j] * k[j]  (nk vectors)

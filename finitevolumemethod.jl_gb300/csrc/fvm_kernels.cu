@@ -170,6 +170,14 @@ __global__ void __launch_bounds__((NW + 1) * 32, kStreamPipelined<MAXW> ? 2 : 1)
             bulk_copy_g2s(valbuf + (size_t)st * L::kSlots, (const V*)a.val + c0, n * (uint32_t)sizeof(V), &full[st]);
             return true;
         };
+        // the x entries of this CTA's rows into L2: the gathers of the CTA and of its
+        // neighbours in the Hilbert order then hit L2 instead of HBM
+        {  // a hint: the range is shrunk to 16-byte boundaries (x may be any caller's array)
+            const uintptr_t p0 = (uintptr_t)((const X*)a.xg + sb * kSlice);
+            const uintptr_t p1 = (uintptr_t)((const X*)a.xg + min(se * kSlice, a.nrows));
+            const uintptr_t q0 = (p0 + 15) & ~(uintptr_t)15, q1 = p1 & ~(uintptr_t)15;
+            if (q1 > q0) bulk_prefetch_l2((const void*)q0, (uint32_t)(q1 - q0));
+        }
         // stage 0 from two global loads, in parallel with the window copy
         bool ok = issue(0, __ldg(&a.slice_ptr[sb]), __ldg(&a.slice_ptr[min(sb + NW, se)]));
         int64_t issued = ok ? 1 : 0;
@@ -411,6 +419,25 @@ void launch_permute_in(const int32_t* perm, const double* xref, double* xint, in
 }
 void launch_permute_out(const int32_t* perm, const double* xint, double* xref, int64_t n, cudaStream_t s) {
     if (n) permute_out_kernel<<<grid_for(n, 256), 256, 0, s>>>(perm, xint, xref, n);
+}
+
+// The same permutations with the caller-numbered side walked in order: the form for arrays in
+// pinned host memory, read or written by the kernel over the host link in whole lines.
+__global__ void permute_in_seq_kernel(const int32_t* __restrict__ iperm, const double* __restrict__ xref,
+                                      double* __restrict__ xint, int64_t n) {
+    int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < n) xint[__ldg(&iperm[j])] = xref[j];
+}
+__global__ void permute_out_seq_kernel(const int32_t* __restrict__ iperm, const double* __restrict__ xint,
+                                       double* __restrict__ xref, int64_t n) {
+    int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < n) xref[j] = xint[__ldg(&iperm[j])];
+}
+void launch_permute_in_seq(const int32_t* iperm, const double* xref, double* xint, int64_t n, cudaStream_t s) {
+    if (n) permute_in_seq_kernel<<<grid_for(n, 256), 256, 0, s>>>(iperm, xref, xint, n);
+}
+void launch_permute_out_seq(const int32_t* iperm, const double* xint, double* xref, int64_t n, cudaStream_t s) {
+    if (n) permute_out_seq_kernel<<<grid_for(n, 256), 256, 0, s>>>(iperm, xint, xref, n);
 }
 
 // Dirichlet update: u_i <- a(x_i, y_i) on the Dirichlet list (dirichlet.jl:20-26).
