@@ -350,7 +350,7 @@ def run_gpu(args):
 
 
 EXTRA_ROWS = ("rhs_fp32", "rhs_fp64_conservative", "rhs_triangle_fp64", "tsit5_1000_steps", "template_spmv",
-              "batched_c4", "multimesh_c4", "adjoint_c5", "steady")
+              "c1_readme", "batched_c4", "multimesh_c4", "adjoint_c5", "steady")
 
 
 def run_extras(args, F, torch, tri, mesh, prob, flush, perm, u_int, peak):
@@ -416,7 +416,10 @@ def run_selected(args, F, torch, tri, mesh, prob, flush, u_int):
                          "alg_bytes": bb}
         return res
 
-    rows = {"rhs_fp32": rhs_fp32, "rhs_fp64_conservative": rhs_fp64_conservative,
+    def c1_readme():
+        return run_c1(F, torch)
+
+    rows = {"c1_readme": c1_readme, "rhs_fp32": rhs_fp32, "rhs_fp64_conservative": rhs_fp64_conservative,
             "rhs_triangle_fp64": rhs_triangle_fp64, "tsit5_1000_steps": tsit5_1000_steps,
             "template_spmv": template_spmv, "batched_c4": lambda: run_batched(args, F, torch, flush),
             "multimesh_c4": lambda: run_multimesh(args, F, torch), "adjoint_c5": lambda: run_adjoint(args, F, torch),
@@ -429,6 +432,38 @@ def run_selected(args, F, torch, tri, mesh, prob, flush, u_int):
             out[name] = rows[name]()
         except Exception as e:  # noqa: BLE001
             out[name] = {"error": repr(e)}
+    return out
+
+
+def run_c1(F, torch, reps=5):
+    """C1, the README problem (triangulate_rectangle(0, 2, 0, 2, 50, 50, single_boundary=true),
+    zero Dirichlet, D = 1/9, u0 = 50 where y <= 1): adaptive Tsit5 to t = 0.5 as the reference's
+    documentation times it - the DiffusionEquation template with saveat = 0.05 (published
+    5.736 ms, hardware unstated) - and the FVMProblem with saveat = 0.001 (test/README.jl).
+    Wall time of the whole `solve` call, best of `reps` after one warm-up."""
+    from fvmgpu.meshes import triangulate_rectangle
+
+    tri = triangulate_rectangle(0.0, 2.0, 0.0, 2.0, 50, 50, single_boundary=True)
+    mesh = F.FVMGeometry(tri)
+    BCs = F.BoundaryConditions(mesh, zero_bc, F.Dirichlet)
+    u0 = np.where(tri.points[:, 1] <= 1.0, 50.0, 0.0)
+    tmpl = F.DiffusionEquation(mesh, BCs, diffusion_function=lambda x, y, p: 1 / 9 + 0.0 * x, initial_condition=u0,
+                               final_time=0.5)
+    prob = F.FVMProblem(mesh, BCs, diffusion_function=lambda x, y, t, u, p: 1 / 9 + 0.0 * x, initial_condition=u0,
+                        final_time=0.5)
+    out = {}
+    for name, pr, saveat in (("template_saveat_0.05", tmpl, 0.05), ("fvmproblem_saveat_0.001", prob, 0.001)):
+        F.solve(pr, F.Tsit5(), saveat=saveat)
+        best, stats = float("inf"), None
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            sol = F.solve(pr, F.Tsit5(), saveat=saveat)
+            best = min(best, time.perf_counter() - t0)
+            stats = sol.stats
+        out[name] = {"wall_ms": 1e3 * best, "device_ms": stats["elapsed_ms"], "steps": stats["naccept"],
+                     "rejected": stats["nreject"], "saves": len(sol.u)}
+    out["template_saveat_0.05"]["published_reference_ms"] = 5.736
     return out
 
 
