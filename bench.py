@@ -462,7 +462,7 @@ def run_c1(F, torch, reps=5):
             best = min(best, time.perf_counter() - t0)
             stats = sol.stats
         out[name] = {"wall_ms": 1e3 * best, "device_ms": stats["elapsed_ms"], "steps": stats["naccept"],
-                     "rejected": stats["nreject"], "saves": len(sol.u)}
+                     "rejected": stats["nreject"], "saves": len(sol.u), "driver": stats["driver"]}
     out["template_saveat_0.05"]["published_reference_ms"] = 5.736
     return out
 

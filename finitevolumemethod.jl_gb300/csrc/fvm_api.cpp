@@ -85,7 +85,7 @@ static double host_rms(const std::vector<double>& v, const std::vector<double>& 
 static void tsit5_run(OdeRhs& rhs, int64_t n, const double* u0_int, const fvm_ode_options& o, double* out_int,
                       fvm_ode_stats* st, cudaStream_t user_stream) {
     if (!(o.tf > o.t0)) fail(FVM_ERR_INVALID_ARGUMENT, "final time must exceed the initial time");
-    CaptureStream cs(user_stream, !o.adaptive && o.use_graph);
+    CaptureStream cs(user_stream, o.use_graph != 0);
     cudaStream_t s = cs.s;
     std::vector<double> saveat;
     if (o.saveat && o.nsave > 0)
@@ -162,7 +162,105 @@ static void tsit5_run(OdeRhs& rhs, int64_t n, const double* u0_int, const fvm_od
             }
         }
     };
+    // Adaptive steps after the first accepted one run on the device: the step size, the PI
+    // control and the saveat cursor live in device memory.  Small meshes with a sliced-ELL RHS
+    // run the whole loop in one thread-block cluster; otherwise one graph launch loops over
+    // attempted steps with a conditional WHILE node until tf (or an error status) is reached.
+    auto device_loop = [&](bool cluster) {
+        DBuf dstate;
+        const size_t state_bytes = (sizeof(AdaptState) + 15) / 16 * 16;
+        dstate.alloc(state_bytes + sizeof(double) * saveat.size());
+        AdaptState* d_st = dstate.as<AdaptState>();
+        double* d_saveat = reinterpret_cast<double*>(reinterpret_cast<char*>(dstate.p) + state_bytes);
+        AdaptState hs{};
+        hs.t = t;
+        hs.dt = dt;
+        hs.tf = o.tf;
+        hs.qold = qold;
+        hs.tspan = tspan;
+        hs.abstol = o.abstol;
+        hs.reltol = o.reltol;
+        hs.nacc = nacc;
+        hs.nrej = nrej;
+        hs.step = step;
+        hs.max_steps = max_steps;
+        hs.si = (int64_t)si;
+        hs.nsave = (int64_t)saveat.size();
+        FVM_CUDA(cudaMemcpyAsync(d_st, &hs, sizeof hs, cudaMemcpyHostToDevice, s));
+        FVM_CUDA(cudaMemcpyAsync(d_saveat, saveat.data(), sizeof(double) * saveat.size(), cudaMemcpyHostToDevice, s));
+        cudaGraph_t g = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        struct GraphGuard {
+            cudaGraph_t& g;
+            cudaGraphExec_t& e;
+            ~GraphGuard() {
+                if (e) cudaGraphExecDestroy(e);
+                if (g) cudaGraphDestroy(g);
+            }
+        } guard_g{g, exec};
+        DBuf dir;
+        if (cluster) {
+            const double* dirval = nullptr;
+            if (rhs.sell.ndir > 0) {
+                dir.alloc(sizeof(double) * n);
+                launch_fill(dir.as<double>(), std::nan(""), n, s);
+                launch_dirichlet(rhs.sell.dir_idx, rhs.sell.dir_val, dir.as<double>(), rhs.sell.ndir, s);
+                dirval = dir.as<double>();
+            }
+            launch_cluster_tsit5(rhs.sell, dirval, u, k[0], out_int, d_saveat, d_st, kA, kBt, s);
+        } else {
+            FVM_CUDA(cudaGraphCreate(&g, 0));
+            cudaGraphConditionalHandle cond;
+            FVM_CUDA(cudaGraphConditionalHandleCreate(&cond, g, 1, cudaGraphCondAssignDefault));
+            cudaGraphNodeParams cp{};
+            cp.type = cudaGraphNodeTypeConditional;
+            cp.conditional.handle = cond;
+            cp.conditional.type = cudaGraphCondTypeWhile;
+            cp.conditional.size = 1;
+            cudaGraphNode_t node;
+            FVM_CUDA(cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp));
+            cudaGraph_t body = cp.conditional.phGraph_out[0];
+            const int nparts = 304;
+            FVM_CUDA(cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+            launch_adapt_begin(d_st, s);
+            for (int sidx = 1; sidx < 7; ++sidx) {
+                launch_stage_dev(sidx == 6 ? unew : y, u, k, kA[sidx], sidx, d_st, n, s);
+                if (sidx < 6) rhs.f(y, k[sidx], t, s);
+            }
+            rhs.f(unew, k[6], t, s);
+            launch_error_partial_dev(u, unew, k, kBt, d_st, n, d_acc, nparts, s);
+            launch_adaptive_step_tail(d_st, d_acc, nparts, n, cond, out_int, u, unew, k[0], k[6], d_saveat, s);
+            if (rhs.callback) rhs.callback(u, t, s);
+            launch_adaptive_step_end(d_st, out_int, u, d_saveat, n, s);
+            cudaGraph_t captured = nullptr;
+            FVM_CUDA(cudaStreamEndCapture(s, &captured));
+            FVM_CUDA(cudaGraphInstantiate(&exec, g, 0));
+            FVM_CUDA(cudaGraphLaunch(exec, s));
+        }
+        check_launch();
+        FVM_CUDA(cudaMemcpyAsync(&hs, d_st, sizeof hs, cudaMemcpyDeviceToHost, s));
+        FVM_CUDA(cudaStreamSynchronize(s));
+        nrhs += 6 * (hs.step - step);
+        t = hs.t;
+        dt = hs.dt;
+        step = hs.step;
+        nacc = hs.nacc;
+        nrej = hs.nrej;
+        si = (size_t)hs.si;
+        if (hs.status == 1) fail(FVM_ERR_STEP_LIMIT, "Tsit5 reached max_steps before tf");
+        if (hs.status == 2) fail(FVM_ERR_STEP_LIMIT, "Tsit5 step size underflow");
+        if (hs.status == 3) fail(FVM_ERR_STEP_LIMIT, "Tsit5 error estimate is not finite (instability)");
+        if (hs.status == 4) fail(FVM_ERR_STEP_LIMIT, "Tsit5 device loop stopped at its time limit before tf");
+    };
+    int32_t driver = FVM_DRIVER_HOST;
+    const bool use_cluster = o.adaptive && o.use_graph && rhs.sell.pat && rhs.sell.val &&
+                             (rhs.callback == nullptr || rhs.sell.ndir > 0) && cluster_tsit5_available(*rhs.sell.pat);
     while (o.adaptive ? t < o.tf : step < nfixed) {
+        if (o.adaptive && o.use_graph && nacc >= 1) {
+            driver = use_cluster ? FVM_DRIVER_CLUSTER : FVM_DRIVER_DEVICE_LOOP;
+            device_loop(use_cluster);
+            break;
+        }
         if (step >= max_steps) fail(FVM_ERR_STEP_LIMIT, "Tsit5 reached max_steps before tf");
         double h;
         bool last;
@@ -190,6 +288,7 @@ static void tsit5_run(OdeRhs& rhs, int64_t n, const double* u0_int, const fvm_od
             FVM_CUDA(cudaStreamEndCapture(s, &graph));
             FVM_CUDA(cudaGraphInstantiate(&exec, graph, 0));
             int64_t reps = nfixed - 1 - step;
+            driver = FVM_DRIVER_FIXED_GRAPH;
             for (int64_t r = 0; r < reps; ++r) FVM_CUDA(cudaGraphLaunch(exec, s));
             check_launch();
             cudaGraphExecDestroy(exec);
@@ -267,6 +366,7 @@ static void tsit5_run(OdeRhs& rhs, int64_t n, const double* u0_int, const fvm_od
     float ms = 0;
     FVM_CUDA(cudaEventElapsedTime(&ms, ev.a, ev.b));
     if (st) {
+        st->driver = driver;
         st->naccept = nacc;
         st->nreject = nrej;
         st->nrhs = nrhs;
@@ -611,6 +711,15 @@ int fvm_tsit5_solve(fvm_problem* p, const double* u0, const fvm_ode_options* opt
             rhs.callback = [p](double* u, double, cudaStream_t st) {
                 launch_dirichlet(p->d_dir_idx.as<int32_t>(), p->d_dir_val.as<double>(), u, p->ndir, st);
             };
+        if (p->linear && p->precision != FVM_FP32) {  // problem_rhs_internal's explicit FP64 path
+            rhs.sell.pat = &m->pat;
+            rhs.sell.val = p->d_val64.as<double>();
+            rhs.sell.b = p->has_b ? p->d_b.as<double>() : nullptr;
+            rhs.sell.q = p->has_q ? p->d_q.as<double>() : nullptr;
+            rhs.sell.dir_idx = p->d_dir_idx.as<int32_t>();
+            rhs.sell.dir_val = p->d_dir_val.as<double>();
+            rhs.sell.ndir = p->ndir;
+        }
         tsit5_run(rhs, n, d_u0, *opt, d_out.as<double>(), stats, s);
         std::vector<double> h((size_t)n * nsave);
         for (int64_t k = 0; k < nsave; ++k) {

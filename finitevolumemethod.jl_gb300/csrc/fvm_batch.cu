@@ -651,6 +651,7 @@ int fvm_batch_tsit5_solve(fvm_batch* bt, const double* u0, const fvm_ode_options
             st->nrhs = nrhs;
             st->t_final = o->tf;
             st->elapsed_ms = ms;
+            st->driver = o->use_graph ? FVM_DRIVER_FIXED_GRAPH : FVM_DRIVER_HOST;
         }
         return FVM_OK;
     });

@@ -187,6 +187,25 @@ void launch_hermite(double* out, const double* u0, const double* u1, const doubl
 // Krylov helpers
 void launch_fill(double* x, double v, int64_t n, cudaStream_t s);
 
+// Device-side state of the graph-looped adaptive Tsit5 (fvm_kernels.cu, fvm_api.cpp)
+struct AdaptState {
+    double t, dt, h, tf, qold, t_prev, tspan, abstol, reltol;
+    int64_t nacc, nrej, step, max_steps, si, nsave;
+    uint64_t start_ns;             // device clock at the first attempted step (0: not started)
+    int32_t accept, last, status;  // status: 0 running, 1 max_steps, 2 dt underflow, 3 non-finite
+                                   // error, 4 device time limit
+};
+void launch_adapt_begin(AdaptState* st, cudaStream_t s);
+void launch_stage_dev(double* y, const double* u, const double* const* k, const double* a, int nk,
+                      const AdaptState* st, int64_t n, cudaStream_t s);
+void launch_error_partial_dev(const double* u, const double* unew, const double* const* k, const double* bt,
+                              const AdaptState* st, int64_t n, double* part, int nparts, cudaStream_t s);
+void launch_adaptive_step_tail(AdaptState* st, const double* part, int nparts, int64_t n,
+                               cudaGraphConditionalHandle cond, double* out, double* u, const double* unew,
+                               double* k0, const double* k6, const double* saveat, cudaStream_t s);
+void launch_adaptive_step_end(AdaptState* st, double* out, const double* u, const double* saveat, int64_t n,
+                              cudaStream_t s);
+
 }  // namespace fvm
 
 // Linear terms of a problem's RHS: emit(row, col, coef, didx, flux), rows and columns in the
@@ -250,11 +269,32 @@ void batch_op_apply(BatchOp& op, const T* u, T* du, cudaStream_t s);
 void launch_batch_assemble(const int64_t* mptr, const int32_t* midx, const double* mcoef, const double* cst,
                            const double* D, void* val, int64_t nnz, int B, int precision, cudaStream_t s);
 
+// An RHS that is the FP64 explicit sliced-ELL product f(u) = A u + q u^2 + b together with a
+// Dirichlet callback u[dir_idx] = dir_val (both optional parts may be null).  With it, a small
+// mesh's adaptive Tsit5 loop runs inside one thread-block cluster (fvm_cluster.cu).
+struct SellRhsDesc {
+    const SellPattern* pat = nullptr;
+    const double* val = nullptr;
+    const double* b = nullptr;
+    const double* q = nullptr;
+    const int32_t* dir_idx = nullptr;
+    const double* dir_val = nullptr;
+    int64_t ndir = 0;
+};
+
 // Right-hand side in the internal numbering plus the per-step callback (Dirichlet update).
 struct OdeRhs {
     std::function<void(const double*, double*, double, cudaStream_t)> f;
     std::function<void(double*, double, cudaStream_t)> callback;  // may be empty
+    SellRhsDesc sell;  // set when f (and callback) are exactly the described product and update
 };
+
+// the cluster-resident adaptive Tsit5 driver (fvm_cluster.cu); meshes up to kClusterMaxRows
+constexpr int64_t kClusterMaxRows = 8192;
+bool cluster_tsit5_available(const SellPattern& pat);
+void launch_cluster_tsit5(const SellRhsDesc& d, const double* dirval, double* u, double* k0, double* out,
+                          const double* saveat, AdaptState* st, const double (*A)[6], const double* bt,
+                          cudaStream_t s);
 void tsit5_run_internal(OdeRhs& rhs, int64_t n, const double* u0_int, const fvm_ode_options& o, double* out_int,
                         fvm_ode_stats* st, cudaStream_t s);
 int guard_call(const std::function<int()>& f);

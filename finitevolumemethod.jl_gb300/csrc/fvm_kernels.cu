@@ -680,6 +680,184 @@ void launch_hermite(double* out, const double* u0, const double* u1, const doubl
     hermite_kernel<<<grid_for(n, 256), 256, 0, s>>>(out, u0, u1, f0, f1, dt, theta, n);
 }
 
+// ---------------------------------------------------------------------------------------
+// Device-controlled adaptive Tsit5: one attempted step per iteration of a graph WHILE loop.
+// The step size lives in device memory (AdaptState), so the stage, error and output kernels
+// read it there; a one-thread controller applies the PI step control of the host driver and
+// sets the loop condition.  No host round trip per step.
+// ---------------------------------------------------------------------------------------
+__global__ void adapt_begin_kernel(AdaptState* st) {
+    const double t = st->t, dt = st->dt;
+    st->last = t + dt >= st->tf ? 1 : 0;
+    st->h = st->last ? st->tf - t : dt;
+}
+
+__global__ void stage_dev_kernel(double* __restrict__ y, const double* __restrict__ u, StageArgs sa, int nk,
+                                 const AdaptState* __restrict__ st, int64_t n) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double acc = 0.0;
+#pragma unroll
+    for (int j = 0; j < 7; ++j)
+        if (j < nk) acc += sa.a[j] * sa.k[j][i];
+    y[i] = u[i] + st->h * acc;
+}
+void launch_stage_dev(double* y, const double* u, const double* const* k, const double* a, int nk,
+                      const AdaptState* st, int64_t n, cudaStream_t s) {
+    StageArgs sa;
+    for (int j = 0; j < 7; ++j) {
+        sa.k[j] = j < nk ? k[j] : nullptr;
+        sa.a[j] = j < nk ? a[j] : 0.0;
+    }
+    stage_dev_kernel<<<grid_for(n, 256), 256, 0, s>>>(y, u, sa, nk, st, n);
+}
+
+__global__ void error_partial_dev_kernel(const double* __restrict__ u, const double* __restrict__ unew, StageArgs sa,
+                                         const AdaptState* __restrict__ st, int64_t n, double* __restrict__ part) {
+    __shared__ double red[256];
+    const double dt = st->h, abstol = st->abstol, reltol = st->reltol;
+    double acc = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double e = 0.0;
+#pragma unroll
+        for (int j = 0; j < 7; ++j) e += sa.a[j] * sa.k[j][i];
+        e *= dt;
+        double sc = abstol + fmax(fabs(u[i]), fabs(unew[i])) * reltol;
+        double r = e / sc;
+        acc += r * r;
+    }
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+// a graph-looped solve that runs this long stops with status 4 (a runaway step sequence)
+constexpr unsigned long long kDeviceLoopTimeLimitNs = 600ull * 1000000000ull;
+
+// PI control of OrdinaryDiffEq's Tsit5 defaults (the host driver's formulas)
+// (256 threads: the partial sums are reduced in the order of sum_partials_kernel)
+__global__ void adapt_control_kernel(AdaptState* st, const double* __restrict__ part, int nparts, int64_t n,
+                                     cudaGraphConditionalHandle cond) {
+    __shared__ double red[256];
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < nparts; i += blockDim.x) acc += part[i];
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x != 0) return;
+    const double sum = red[0];
+    const double beta1 = 7.0 / 50.0, beta2 = 2.0 / 25.0, qmin = 0.2, qmax = 10.0, gamma = 0.9;
+    const double EEst = sqrt(sum / (double)(n > 1 ? n : 1));
+    const double h = st->h, t = st->t;
+    st->accept = 0;
+    if (!isfinite(EEst)) {
+        st->status = 3;
+        cudaGraphSetConditional(cond, 0);
+        return;
+    }
+    double q11 = 0.0, q;
+    if (EEst == 0.0) {
+        q = 1.0 / qmax;
+    } else {
+        q11 = pow(EEst, beta1);
+        q = q11 / pow(st->qold, beta2);
+        q = fmax(1.0 / qmax, fmin(1.0 / qmin, q / gamma));
+    }
+    st->step += 1;
+    if (EEst > 1.0) {  // reject
+        st->nrej += 1;
+        st->dt = h / fmin(1.0 / qmin, q11 / gamma);
+        if (st->dt < 1e-14 * fmax(1.0, fabs(t))) st->status = 2;
+    } else {
+        st->accept = 1;
+        st->t_prev = t;
+        st->t = st->last ? st->tf : t + h;
+        st->nacc += 1;
+        st->qold = fmax(EEst, 1e-4);
+        st->dt = fmin(h / q, st->tspan);
+    }
+    const bool finished = st->accept && st->last;
+    if (!finished && st->status == 0 && st->step >= st->max_steps) st->status = 1;
+    const unsigned long long now = global_ns();
+    if (st->start_ns == 0) st->start_ns = now;
+    if (!finished && st->status == 0 && now - st->start_ns > kDeviceLoopTimeLimitNs) st->status = 4;
+    cudaGraphSetConditional(cond, (!finished && st->status == 0) ? 1u : 0u);
+}
+
+// saveat points strictly inside the accepted step: cubic Hermite from (u, k0) and (unew, k6)
+__global__ void adapt_save_interp_kernel(double* __restrict__ out, const double* __restrict__ u,
+                                         const double* __restrict__ unew, const double* __restrict__ f0,
+                                         const double* __restrict__ f1, const double* __restrict__ saveat,
+                                         const AdaptState* __restrict__ st, int64_t n) {
+    if (!st->accept) return;
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double h = st->h, t0 = st->t_prev, tn = st->t;
+    for (int64_t j = st->si; j < st->nsave && saveat[j] < tn; ++j) {
+        const double th = (saveat[j] - t0) / h;
+        const double t2 = th * th, t3 = t2 * th;
+        const double h00 = 2 * t3 - 3 * t2 + 1, h10 = t3 - 2 * t2 + th, h01 = -2 * t3 + 3 * t2, h11 = t3 - t2;
+        out[j * n + i] = h00 * u[i] + h10 * h * f0[i] + h01 * unew[i] + h11 * h * f1[i];
+    }
+}
+// accepted step: u <- unew, FSAL k0 <- k6
+__global__ void adapt_commit_kernel(double* __restrict__ u, const double* __restrict__ unew, double* __restrict__ k0,
+                                    const double* __restrict__ k6, const AdaptState* __restrict__ st, int64_t n) {
+    if (!st->accept) return;
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    u[i] = unew[i];
+    k0[i] = k6[i];
+}
+// saveat points at the step's end (after the callback), then the save cursor moves past tn
+__global__ void adapt_save_exact_kernel(double* __restrict__ out, const double* __restrict__ u,
+                                        const double* __restrict__ saveat, const AdaptState* __restrict__ st,
+                                        int64_t n) {
+    if (!st->accept) return;
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double tn = st->t;
+    int64_t j = st->si;
+    while (j < st->nsave && saveat[j] < tn) ++j;
+    for (; j < st->nsave && saveat[j] == tn; ++j) out[j * n + i] = u[i];
+}
+__global__ void adapt_advance_kernel(AdaptState* st, const double* __restrict__ saveat) {
+    if (!st->accept) return;
+    int64_t j = st->si;
+    while (j < st->nsave && saveat[j] <= st->t) ++j;
+    st->si = j;
+}
+
+void launch_adaptive_step_tail(AdaptState* st, const double* part, int nparts, int64_t n,
+                               cudaGraphConditionalHandle cond, double* out, double* u, const double* unew,
+                               double* k0, const double* k6, const double* saveat, cudaStream_t s) {
+    adapt_control_kernel<<<1, 256, 0, s>>>(st, part, nparts, n, cond);
+    adapt_save_interp_kernel<<<grid_for(n, 256), 256, 0, s>>>(out, u, unew, k0, k6, saveat, st, n);
+    adapt_commit_kernel<<<grid_for(n, 256), 256, 0, s>>>(u, unew, k0, k6, st, n);
+}
+void launch_adaptive_step_end(AdaptState* st, double* out, const double* u, const double* saveat, int64_t n,
+                              cudaStream_t s) {
+    adapt_save_exact_kernel<<<grid_for(n, 256), 256, 0, s>>>(out, u, saveat, st, n);
+    adapt_advance_kernel<<<1, 1, 0, s>>>(st, saveat);
+}
+void launch_adapt_begin(AdaptState* st, cudaStream_t s) { adapt_begin_kernel<<<1, 1, 0, s>>>(st); }
+void launch_error_partial_dev(const double* u, const double* unew, const double* const* k, const double* bt,
+                              const AdaptState* st, int64_t n, double* part, int nparts, cudaStream_t s) {
+    StageArgs sa;
+    for (int j = 0; j < 7; ++j) {
+        sa.k[j] = k[j];
+        sa.a[j] = bt[j];
+    }
+    error_partial_dev_kernel<<<nparts, 256, 0, s>>>(u, unew, sa, st, n, part);
+}
+
 __global__ void fill_kernel(double* x, double v, int64_t n) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) x[i] = v;

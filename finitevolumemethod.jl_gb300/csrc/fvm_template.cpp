@@ -262,6 +262,11 @@ int fvm_template_tsit5_solve(fvm_template* T, const double* u0, const fvm_ode_op
             } else
                 launch_sell_apply64(m->pat, T->d_val64.as<double>(), u, du, nullptr, T->d_b.as<double>(), nullptr, st);
         };
+        if (!fp32) {
+            rhs.sell.pat = &m->pat;
+            rhs.sell.val = T->d_val64.as<double>();
+            rhs.sell.b = T->d_b.as<double>();
+        }
         tsit5_run_internal(rhs, n, d_u0, *opt, d_out.as<double>(), stats, s);
         for (int64_t k = 0; k < nsave; ++k) {
             launch_permute_out(m->d_perm.as<int32_t>(), d_out.as<double>() + k * n, d_ref, n, s);

@@ -88,7 +88,7 @@ class OdeOptions(C.Structure):
 class OdeStats(C.Structure):
     _fields_ = [
         ("naccept", C.c_int64), ("nreject", C.c_int64), ("nrhs", C.c_int64),
-        ("t_final", C.c_double), ("elapsed_ms", C.c_double),
+        ("t_final", C.c_double), ("elapsed_ms", C.c_double), ("driver", C.c_int32),
     ]
 
 

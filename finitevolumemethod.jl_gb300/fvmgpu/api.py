@@ -963,6 +963,9 @@ class LinearSolution:
     retcode: str = "Success"
 
 
+_DRIVERS = {0: "host", 1: "fixed_graph", 2: "device_loop", 3: "cluster"}
+
+
 def _saveat_times(saveat, t0, tf):
     if saveat is None:
         return np.array([t0, tf])
@@ -1041,4 +1044,5 @@ def solve(prob, alg=None, *, saveat=None, dt=None, adaptive=None, abstol=1e-6, r
         check(lib.fvm_tsit5_solve(prob.handle, dptr(u0c), C.byref(o), dptr(out), C.byref(st), s))
         us = [row.copy() for row in out]
     return ODESolution(ts, us, {"naccept": st.naccept, "nreject": st.nreject, "nrhs": st.nrhs,
-                                "t_final": st.t_final, "elapsed_ms": st.elapsed_ms})
+                                "t_final": st.t_final, "elapsed_ms": st.elapsed_ms,
+                                "driver": _DRIVERS.get(st.driver, str(st.driver))})

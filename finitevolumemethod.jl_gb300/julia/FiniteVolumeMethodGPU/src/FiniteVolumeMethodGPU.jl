@@ -63,6 +63,7 @@ mutable struct OdeStats
     nrhs::Int64
     t_final::Float64
     elapsed_ms::Float64
+    driver::Int32
 end
 
 function last_error()
@@ -253,7 +254,7 @@ function solve(gp::GPUProblem; saveat, dt = nothing, abstol = 1e-6, reltol = 1e-
     u0 = collect(Float64, prob.initial_condition)
     opt = OdeOptions(t0, tf, dt === nothing ? 0.0 : dt, dt === nothing ? Int32(1) : Int32(0), abstol, reltol,
         max_steps, pointer(ts), length(ts), Int32(1), Int32(0))
-    st = OdeStats(0, 0, 0, 0.0, 0.0)
+    st = OdeStats(0, 0, 0, 0.0, 0.0, Int32(0))
     GC.@preserve ts check(ccall((:fvm_tsit5_solve, libfvmgpu), Cint,
         (Ptr{Cvoid}, Ptr{Float64}, Ref{OdeOptions}, Ptr{Float64}, Ref{OdeStats}, Ptr{Cvoid}),
         gp.handle, u0, opt, out, st, C_NULL))

@@ -175,7 +175,14 @@ typedef struct fvm_ode_stats {
     int64_t naccept, nreject, nrhs;
     double t_final;
     double elapsed_ms;    /* device time of the stepping loop (CUDA events) */
+    int32_t driver;       /* FVM_DRIVER_*: which stepping loop ran after the first step */
 } fvm_ode_stats;
+
+/* stepping loops (fvm_ode_stats.driver) */
+#define FVM_DRIVER_HOST 0          /* host-controlled loop, one launch sequence per step */
+#define FVM_DRIVER_FIXED_GRAPH 1   /* fixed steps replayed as one captured CUDA graph */
+#define FVM_DRIVER_DEVICE_LOOP 2   /* adaptive: CUDA graph with a conditional WHILE node */
+#define FVM_DRIVER_CLUSTER 3       /* adaptive, small sliced-ELL problems: one thread-block cluster */
 
 /* Tsit5 on a generic problem, with the Dirichlet callback after every step
  * (src/solve.jl:133-165).  u0 and out are host arrays in the caller's numbering;

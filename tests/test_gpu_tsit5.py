@@ -31,13 +31,15 @@ def test_fixed_step_tsit5(gpu_lib, use_graph):
     assert sol.stats["naccept"] == st["naccept"] == 20
 
 
-def test_adaptive_readme_saveat(gpu_lib):
-    """README diffusion (test/README.jl): Tsit5 to t = 0.5 with saveat = 0.001."""
+@pytest.mark.parametrize("use_graph", [True, False])
+def test_adaptive_readme_saveat(gpu_lib, use_graph):
+    """README diffusion (test/README.jl): Tsit5 to t = 0.5 with saveat = 0.001.  use_graph runs
+    the steps after the first accepted one as a device-side loop (conditional graph node)."""
     import fvmgpu as F
 
     spec = readme_diffusion(50)
     prob = api_problem(spec)
-    sol = F.solve(prob, F.Tsit5(), saveat=0.001)
+    sol = F.solve(prob, F.Tsit5(), saveat=0.001, use_graph=use_graph)
     assert len(sol.u) == 501 and np.isclose(sol.t[-1], 0.5)
     ref, st = _oracle_run(spec, list(sol.t))
     assert sol.stats["naccept"] == st["naccept"] and sol.stats["nreject"] == st["nreject"]
@@ -47,12 +49,13 @@ def test_adaptive_readme_saveat(gpu_lib):
     assert np.all(np.array(sol.u) <= 50 + 1e-9) and np.all(np.array(sol.u) >= -1e-9)
 
 
-def test_adaptive_mixed_conditions(gpu_lib):
+@pytest.mark.parametrize("use_graph", [True, False])
+def test_adaptive_mixed_conditions(gpu_lib, use_graph):
     import fvmgpu as F
 
     spec = mixed_annulus()
     prob = api_problem(spec)
-    sol = F.solve(prob, F.Tsit5(), saveat=0.02)
+    sol = F.solve(prob, F.Tsit5(), saveat=0.02, use_graph=use_graph)
     ref, st = _oracle_run(spec, list(sol.t))
     err = np.max(np.abs(np.array(sol.u) - ref)) / np.max(np.abs(ref))
     assert err < 1e-8, err
@@ -73,3 +76,43 @@ def test_template_tsit5_matches_oracle(gpu_lib):
     ref, _ = O.tsit5_solve(lambda u, t: A @ u + b, u0, 0.0, 1e-3, [1e-3], dt=5e-5, adaptive=False)
     err = np.max(np.abs(sol.u[-1][:-1] - ref[-1])) / np.max(np.abs(ref[-1]))
     assert err < 1e-10, err
+
+
+@pytest.mark.parametrize("side,driver", [(48, "cluster"), (96, "device_loop")])
+def test_device_loop_matches_host_loop(gpu_lib, side, driver):
+    """The device-side adaptive drivers (one thread-block cluster for the 2304-vertex mesh, the
+    conditional-graph loop for the 9216-vertex one) and the host-controlled loop take the same
+    steps: equal accept/reject counts and solutions equal to rounding, for saveat points that
+    fall inside steps and on step ends (t0 and tf).  With a tiny given initial dt the first
+    error estimates are rounding noise (the stages cancel to ~1e-16), so a last-bit difference
+    between the device and host pow() (or the order of the error-norm sum) moves later step
+    sizes: there the counts still agree and the solutions agree to the integration tolerance
+    (5e-5 of max|u| at reltol 1e-3)."""
+    import fvmgpu as F
+
+    spec = sine_diffusion(side)
+    spec.tf = 0.02
+    prob = api_problem(spec)
+    for kw, tol in (({"saveat": 0.0025}, 1e-12), ({"saveat": [0.0, 0.013, 0.02]}, 1e-12), ({"saveat": None}, 1e-12),
+                    ({"dt": 1e-5, "adaptive": True, "saveat": 0.005}, 5e-5)):
+        a = F.solve(prob, F.Tsit5(), use_graph=True, **kw)
+        b = F.solve(prob, F.Tsit5(), use_graph=False, **kw)
+        assert a.stats["driver"] == driver and b.stats["driver"] == "host"
+        assert a.stats["naccept"] == b.stats["naccept"] and a.stats["nreject"] == b.stats["nreject"]
+        assert a.stats["nrhs"] == b.stats["nrhs"]
+        assert np.array_equal(np.asarray(a.t), np.asarray(b.t))
+        ua, ub = np.array(a.u), np.array(b.u)
+        assert np.max(np.abs(ua - ub)) <= tol * np.max(np.abs(ub)), kw
+
+
+@pytest.mark.parametrize("side,use_graph", [(32, True), (96, True), (32, False)])
+def test_adaptive_step_limit(gpu_lib, side, use_graph):
+    """max_steps counts attempted steps; running out is an error on every driver (cluster,
+    conditional-graph loop, host loop)."""
+    import fvmgpu as F
+
+    spec = sine_diffusion(side)
+    spec.tf = 0.05
+    prob = api_problem(spec)
+    with pytest.raises(F.FVMError, match="max_steps"):
+        F.solve(prob, F.Tsit5(), saveat=0.01, max_steps=5, use_graph=use_graph)
