@@ -158,15 +158,20 @@ def profile_traffic(name):
     return None
 
 
-def timed_steps(fn, K, W, flush, torch):
+def timed_steps(fn, K, W, flush, torch, device_only=True):
     """W untimed warm-up calls, then K calls each bracketed by CUDA events (L2 flushed
-    before each).  Returns per-step milliseconds."""
+    before each).  device_only: a ~50 us device sleep after the flush keeps the GPU busy while
+    the host enqueues the start event and the call, so the events bracket the device work and
+    not the host's launch overhead (end-to-end timings pass False and keep that overhead).
+    Returns per-step milliseconds."""
     for _ in range(W):
         fn()
     torch.cuda.synchronize()
     ev = []
     for _ in range(K):
         flush()
+        if device_only:
+            torch.cuda._sleep(100_000)
         a = torch.cuda.Event(enable_timing=True)
         b = torch.cuda.Event(enable_timing=True)
         a.record()
@@ -307,7 +312,7 @@ def run_gpu(args):
     with ClockSampler(torch.cuda.current_device() if "CUDA_VISIBLE_DEVICES" in os.environ else local) as clk:
         ms = timed_steps(step, K, max(W, 3), flush, torch)
         torch.cuda.synchronize()
-        ms_e2e = timed_steps(e2e_step, K, max(W, 3), flush, torch)
+        ms_e2e = timed_steps(e2e_step, K, max(W, 3), flush, torch, device_only=False)
         torch.cuda.synchronize()
     if dist is not None:
         dist.barrier()

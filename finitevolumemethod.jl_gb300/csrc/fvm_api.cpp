@@ -721,11 +721,7 @@ int fvm_tsit5_solve(fvm_problem* p, const double* u0, const fvm_ode_options* opt
             rhs.sell.ndir = p->ndir;
         }
         tsit5_run(rhs, n, d_u0, *opt, d_out.as<double>(), stats, s);
-        std::vector<double> h((size_t)n * nsave);
-        for (int64_t k = 0; k < nsave; ++k) {
-            launch_permute_out(m->d_perm.as<int32_t>(), d_out.as<double>() + k * n, d_ref, n, s);
-            FVM_CUDA(cudaMemcpyAsync(out + k * n, d_ref, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
-        }
+        snapshots_to_host(m->d_iperm.as<int32_t>(), d_out.as<double>(), out, n, nsave, s);
         FVM_CUDA(cudaStreamSynchronize(s));
         check_launch();
         check_device_error();
@@ -737,6 +733,23 @@ int fvm_tsit5_solve(fvm_problem* p, const double* u0, const fvm_ode_options* opt
 
 // exported for the template / steady-solve translation unit
 namespace fvm {
+void snapshots_to_host(const int32_t* iperm, const double* src, double* out, int64_t n, int64_t nsave,
+                       cudaStream_t s) {
+    if (n == 0 || nsave == 0) return;
+    if (double* mapped = static_cast<double*>(host_mapped(out))) {
+        launch_permute_out_snapshots(iperm, src, mapped, n, nsave, s);
+        return;
+    }
+    const int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(nsave, (int64_t(64) << 20) / (8 * n)));
+    DBuf tmp;
+    tmp.alloc(sizeof(double) * n * chunk);
+    for (int64_t k0 = 0; k0 < nsave; k0 += chunk) {
+        const int64_t kc = std::min(chunk, nsave - k0);
+        launch_permute_out_snapshots(iperm, src + k0 * n, tmp.as<double>(), n, kc, s);
+        FVM_CUDA(cudaMemcpyAsync(out + k0 * n, tmp.p, sizeof(double) * n * kc, cudaMemcpyDeviceToHost, s));
+    }
+}
+
 void tsit5_run_internal(OdeRhs& rhs, int64_t n, const double* u0_int, const fvm_ode_options& o, double* out_int,
                         fvm_ode_stats* st, cudaStream_t s) {
     tsit5_run(rhs, n, u0_int, o, out_int, st, s);

@@ -67,6 +67,10 @@ struct SellPattern {
     std::vector<int32_t> csr_col;    // CSR columns (sorted)
     std::vector<int64_t> csr_slot;   // CSR entry -> SELL slot
     DBuf d_slice_ptr, d_width, d_col;
+    // per-row destination CTAs of the cluster Tsit5 driver (fvm_cluster.cu), for one shape
+    mutable DBuf d_cluster_dest;
+    mutable int cluster_dest_key = -1;
+    mutable int cluster_size = -1, cluster_cap = -1;  // chosen cluster size for the cap in force
     // slot of (row, col), or -1
     int64_t find(int32_t row, int32_t c) const;
     // CSR position of (row, col), or -1
@@ -174,6 +178,8 @@ void launch_permute_out(const int32_t* perm, const double* xint, double* xref, i
 // the same with iperm (caller -> internal) and the caller's side in order (host-mapped arrays)
 void launch_permute_in_seq(const int32_t* iperm, const double* xref, double* xint, int64_t n, cudaStream_t s);
 void launch_permute_out_seq(const int32_t* iperm, const double* xint, double* xref, int64_t n, cudaStream_t s);
+void launch_permute_out_snapshots(const int32_t* iperm, const double* xint, double* xref, int64_t n, int64_t nsave,
+                                  cudaStream_t s);
 void launch_dirichlet(const int32_t* idx, const double* val, double* u, int64_t n, cudaStream_t s);
 void launch_triangle_rhs(const fvm_mesh* m, const fvm_problem* p, const double* u, double* du, cudaStream_t s);
 // Tsit5 stage: y = u + dt * sum_j a[j] * k[j]  (nk vectors)
@@ -295,6 +301,11 @@ bool cluster_tsit5_available(const SellPattern& pat);
 void launch_cluster_tsit5(const SellRhsDesc& d, const double* dirval, double* u, double* k0, double* out,
                           const double* saveat, AdaptState* st, const double (*A)[6], const double* bt,
                           cudaStream_t s);
+// Copies nsave internal-order device snapshots [nsave][n] to the caller's host array in the
+// caller's numbering: written directly when the array is page-locked, else through a device
+// staging buffer in chunks of at most 64 MiB, one copy per chunk.  Does not synchronise.
+void snapshots_to_host(const int32_t* iperm, const double* src, double* out, int64_t n, int64_t nsave,
+                       cudaStream_t s);
 void tsit5_run_internal(OdeRhs& rhs, int64_t n, const double* u0_int, const fvm_ode_options& o, double* out_int,
                         fvm_ode_stats* st, cudaStream_t s);
 int guard_call(const std::function<int()>& f);

@@ -5,6 +5,7 @@
 #include "fvm_tma.cuh"
 
 #include <algorithm>
+#include <vector>
 
 namespace fvm {
 
@@ -92,6 +93,15 @@ struct StreamArgs {
 
 constexpr int kSpWindowMax = 1024;
 
+// First-stage slot range of each CTA, passed with the launch so that the producer issues the
+// first bulk copies without waiting on a global load of the slice offsets (after an L2 flush
+// that load is a DRAM round trip on the start-up path).  n = 0: not provided.
+constexpr int kStage0Max = 640;
+struct Stage0Table {
+    int n;
+    int32_t c0[kStage0Max], c1[kStage0Max];
+};
+
 template <class V, int MAXW, int NW>
 struct StreamLayout {
     static constexpr int kSlots = NW * MAXW * kSlice;  // slots per stage
@@ -123,7 +133,8 @@ template <int MAXW>
 constexpr bool kStreamPipelined = MAXW <= 8;
 
 template <class V, class Acc, class X, bool DIFF, int MAXW, int NW>
-__global__ void __launch_bounds__((NW + 1) * 32, kStreamPipelined<MAXW> ? 2 : 1) sell_stream_kernel(StreamArgs a) {
+__global__ void __launch_bounds__((NW + 1) * 32, kStreamPipelined<MAXW> ? 2 : 1)
+    sell_stream_kernel(StreamArgs a, const __grid_constant__ Stage0Table t0) {
     using L = StreamLayout<V, MAXW, NW>;
     extern __shared__ __align__(128) unsigned char smem[];
     const int nst = a.nst;
@@ -178,8 +189,10 @@ __global__ void __launch_bounds__((NW + 1) * 32, kStreamPipelined<MAXW> ? 2 : 1)
             const uintptr_t q0 = (p0 + 15) & ~(uintptr_t)15, q1 = p1 & ~(uintptr_t)15;
             if (q1 > q0) bulk_prefetch_l2((const void*)q0, (uint32_t)(q1 - q0));
         }
-        // stage 0 from two global loads, in parallel with the window copy
-        bool ok = issue(0, __ldg(&a.slice_ptr[sb]), __ldg(&a.slice_ptr[min(sb + NW, se)]));
+        // stage 0 from the launch's table, else from two global loads, in parallel with the
+        // window copy
+        bool ok = (int)blockIdx.x < t0.n ? issue(0, t0.c0[blockIdx.x], t0.c1[blockIdx.x])
+                                         : issue(0, __ldg(&a.slice_ptr[sb]), __ldg(&a.slice_ptr[min(sb + NW, se)]));
         int64_t issued = ok ? 1 : 0;
         if (ok && !mbar_wait(spbar, 0)) ok = false;
         const int64_t* sp = spw - w0;
@@ -295,7 +308,7 @@ struct StreamShape {
 };
 
 template <class V, class Acc, class X, bool DIFF, int MAXW>
-static void launch_stream(const StreamArgs& a0, cudaStream_t s) {
+static void launch_stream(const StreamArgs& a0, const std::vector<int64_t>& hsp, cudaStream_t s) {
     using L = StreamLayout<V, MAXW, kStreamWarps>;
     auto kern = sell_stream_kernel<V, Acc, X, DIFF, MAXW, kStreamWarps>;
     const int threads = (kStreamWarps + 1) * 32;
@@ -332,7 +345,17 @@ static void launch_stream(const StreamArgs& a0, cudaStream_t s) {
     const int64_t range = (a.nslices + grid - 1) / grid;
     a.spwin = (int)std::min<int64_t>(kSpWindowMax, ((range + 3) + 15) & ~(int64_t)15);
     a.nst = (int)std::min<long>(6, (shape.budget - (long)L::bytes(0, a.spwin)) / (long)L::kStageBytes);
-    kern<<<(unsigned)grid, threads, L::bytes(a.nst, a.spwin), s>>>(a);
+    Stage0Table t0;  // copied into the launch's parameters
+    t0.n = 0;
+    if (grid <= kStage0Max && (int64_t)hsp.size() == a.nslices + 1 && hsp.back() < ((int64_t)1 << 31)) {
+        for (int64_t c = 0; c < grid; ++c) {
+            const int64_t sb = a.nslices * c / grid, se = a.nslices * (c + 1) / grid;
+            t0.c0[c] = (int32_t)hsp[sb];
+            t0.c1[c] = (int32_t)hsp[std::min(sb + kStreamWarps, se)];
+        }
+        t0.n = (int)grid;
+    }
+    kern<<<(unsigned)grid, threads, L::bytes(a.nst, a.spwin), s>>>(a, t0);
 }
 
 template <class V, class Acc, class X, bool DIFF>
@@ -344,17 +367,17 @@ static void launch_sell(const SellPattern& p, const V* val, const X* xg, const d
                      p.nrows, p.nslices, 0, 0};
         // exact widths of the common vertex degrees: no predicated-off slot costs an FP64 issue
         if (p.maxw <= 4)
-            launch_stream<V, Acc, X, DIFF, 4>(a, s);
+            launch_stream<V, Acc, X, DIFF, 4>(a, p.slice_ptr, s);
         else if (p.maxw <= 6)
-            launch_stream<V, Acc, X, DIFF, 6>(a, s);
+            launch_stream<V, Acc, X, DIFF, 6>(a, p.slice_ptr, s);
         else if (p.maxw <= 7)
-            launch_stream<V, Acc, X, DIFF, 7>(a, s);
+            launch_stream<V, Acc, X, DIFF, 7>(a, p.slice_ptr, s);
         else if (p.maxw <= 8)
-            launch_stream<V, Acc, X, DIFF, 8>(a, s);
+            launch_stream<V, Acc, X, DIFF, 8>(a, p.slice_ptr, s);
         else if (p.maxw <= 12)
-            launch_stream<V, Acc, X, DIFF, 12>(a, s);
+            launch_stream<V, Acc, X, DIFF, 12>(a, p.slice_ptr, s);
         else
-            launch_stream<V, Acc, X, DIFF, 16>(a, s);
+            launch_stream<V, Acc, X, DIFF, 16>(a, p.slice_ptr, s);
         return;
     }
     SellArgs a{p.d_slice_ptr.as<int64_t>(), p.d_width.as<int32_t>(), p.d_col.as<int32_t>(), val, xg, x, y, rowscale,
@@ -438,6 +461,22 @@ void launch_permute_in_seq(const int32_t* iperm, const double* xref, double* xin
 }
 void launch_permute_out_seq(const int32_t* iperm, const double* xint, double* xref, int64_t n, cudaStream_t s) {
     if (n) permute_out_seq_kernel<<<grid_for(n, 256), 256, 0, s>>>(iperm, xint, xref, n);
+}
+
+// nsave snapshots at once, caller side in order: xref[k][j] = xint[k][iperm[j]]
+__global__ void permute_out_snapshots_kernel(const int32_t* __restrict__ iperm, const double* __restrict__ xint,
+                                             double* __restrict__ xref, int64_t n, int64_t total) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t k = i / n, j = i - k * n;
+        xref[i] = xint[k * n + __ldg(&iperm[j])];
+    }
+}
+void launch_permute_out_snapshots(const int32_t* iperm, const double* xint, double* xref, int64_t n, int64_t nsave,
+                                  cudaStream_t s) {
+    const int64_t total = n * nsave;
+    if (total == 0) return;
+    const unsigned grid = (unsigned)std::min<int64_t>(grid_for(total, 256), 152 * 16);
+    permute_out_snapshots_kernel<<<grid, 256, 0, s>>>(iperm, xint, xref, n, total);
 }
 
 // Dirichlet update: u_i <- a(x_i, y_i) on the Dirichlet list (dirichlet.jl:20-26).

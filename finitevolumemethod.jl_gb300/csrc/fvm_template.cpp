@@ -268,10 +268,7 @@ int fvm_template_tsit5_solve(fvm_template* T, const double* u0, const fvm_ode_op
             rhs.sell.b = T->d_b.as<double>();
         }
         tsit5_run_internal(rhs, n, d_u0, *opt, d_out.as<double>(), stats, s);
-        for (int64_t k = 0; k < nsave; ++k) {
-            launch_permute_out(m->d_perm.as<int32_t>(), d_out.as<double>() + k * n, d_ref, n, s);
-            FVM_CUDA(cudaMemcpyAsync(out + k * n, d_ref, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
-        }
+        snapshots_to_host(m->d_iperm.as<int32_t>(), d_out.as<double>(), out, n, nsave, s);
         FVM_CUDA(cudaStreamSynchronize(s));
         FVM_CUDA(cudaGetLastError());
         return FVM_OK;
