@@ -331,7 +331,7 @@ def run_gpu(args):
                    "layout": "device-resident u/du in the library's Hilbert numbering",
                    "parallelism": f"replicas x{ws}"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "kernel": "sell_stream_kernel<double,double,double,explicit,7,8>",
+                     "traffic": traffic, "kernel": "sell_stream_kernel<double,double,double,explicit,7,16>",
                      "alg_bytes_per_launch": alg_bytes, "alg_bytes_per_flux_eval": alg_bytes / units,
                      "peak_source": f"{peak_kind} hbm_gbs (burst copy)",
                      "canonical": canonical_roofline(tri, ms.mean(), peak)},

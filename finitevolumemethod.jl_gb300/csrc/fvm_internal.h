@@ -69,6 +69,7 @@ struct SellPattern {
     DBuf d_slice_ptr, d_width, d_col;
     // per-row destination CTAs of the cluster Tsit5 driver (fvm_cluster.cu), for one shape
     mutable DBuf d_cluster_dest;
+    mutable std::vector<uint32_t> cluster_expect;
     mutable int cluster_dest_key = -1;
     mutable int cluster_size = -1, cluster_cap = -1;  // chosen cluster size for the cap in force
     // slot of (row, col), or -1
@@ -296,7 +297,7 @@ struct OdeRhs {
 };
 
 // the cluster-resident adaptive Tsit5 driver (fvm_cluster.cu); meshes up to kClusterMaxRows
-constexpr int64_t kClusterMaxRows = 8192;
+constexpr int64_t kClusterMaxRows = 7680;
 bool cluster_tsit5_available(const SellPattern& pat);
 void launch_cluster_tsit5(const SellRhsDesc& d, const double* dirval, double* u, double* k0, double* out,
                           const double* saveat, AdaptState* st, const double (*A)[6], const double* bt,
