@@ -174,6 +174,7 @@ void launch_sell_diff32(const SellPattern& p, const float* val, const float* x32
 void launch_to_f32(const double* x, float* y, int64_t n, cudaStream_t s);
 // error bits left by a kernel whose bounded wait ran out (0 = none); reading clears them
 unsigned take_device_error();
+unsigned* device_error_word();  // device address of the error word the streamed kernels set
 void launch_permute_in(const int32_t* perm, const double* xref, double* xint, int64_t n, cudaStream_t s);
 void launch_permute_out(const int32_t* perm, const double* xint, double* xref, int64_t n, cudaStream_t s);
 // the same with iperm (caller -> internal) and the caller's side in order (host-mapped arrays)
