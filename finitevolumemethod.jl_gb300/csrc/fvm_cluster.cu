@@ -26,6 +26,7 @@
 #include <vector>
 
 #include "fvm_internal.h"
+#include "fvm_pow.h"
 #include "fvm_tma.cuh"
 
 namespace cg = cooperative_groups;
@@ -68,12 +69,16 @@ struct ClusterCtl {
 
 constexpr int kClusterHermite = 32;  // saveat points per step with shared Hermite weights
 
+__constant__ PowTables c_pow;  // tables of pow_pos, uploaded once per device (launch_cluster_tsit5)
+
 // PI control of OrdinaryDiffEq's Tsit5 defaults, applied by thread 0 of every CTA to the same
 // inputs; sets the next step's h and last.  On GB300 a chain of dependent FP64 operations in
 // one thread costs ~40 ns per operation, so the chain is kept short: EEst^beta1 is taken as
-// (sum / n)^(beta1 / 2) without the square root, qold^beta2 (pq) was computed by another warp
-// during the step's stages, and qold itself (a square root) is left pending for that warp.
-// These change results only in the last bits, like the order of the error-norm sum.
+// (sum / n)^(beta1 / 2) without the square root and through pow_pos (fvm_pow.h, within about
+// one ulp, a third of the dependent operations of the library pow), qold^beta2 (pq) was
+// computed by another warp during the step's stages, and qold itself (a square root) is left
+// pending for that warp.  These change results only in the last bits, like the order of the
+// error-norm sum.
 __device__ void cluster_control(AdaptState& S, ClusterCtl& c, double sum, double flags, double inv_n, double pq,
                                 const double* __restrict__ saveat) {
     const double beta1_half = 7.0 / 100.0, qmin = 0.2, qmax = 10.0, inv_gamma = 1.0 / 0.9, gamma = 0.9;
@@ -91,7 +96,7 @@ __device__ void cluster_control(AdaptState& S, ClusterCtl& c, double sum, double
     if (x == 0.0) {
         qc = 1.0 / qmax;
     } else {
-        q11 = pow(x, beta1_half);
+        q11 = pow_pos(x, beta1_half, c_pow);
         qc = fmax(1.0 / qmax, fmin(1.0 / qmin, (q11 / pq) * inv_gamma));
     }
     S.step += 1;
@@ -203,7 +208,7 @@ __global__ void __launch_bounds__(32 * kClusterWarps, 1) tsit5_cluster_kernel(co
         const double h = ctl.h;
         if (threadIdx.x == pw_thread) {  // read by thread 0 only after the stages
             if (ctl.qold_pending) S.qold = fmax(sqrt(ctl.x_acc), 1e-4);
-            pq_sh = pow(S.qold, 2.0 / 25.0);
+            pq_sh = pow_pos(S.qold, 2.0 / 25.0, c_pow);
         }
         // running stage sums: acc[s] = sum_j a[s][j] k_j over the k_j known so far (slot order
         // j = 0, 1, ... as in the stage kernels), err likewise with the error weights
@@ -477,6 +482,15 @@ void launch_cluster_tsit5(const SellRhsDesc& d, const double* dirval, double* u,
     const SellPattern& p = *d.pat;
     const int cs = cluster_size_for(p);
     if (cs == 0) fail(FVM_ERR_CUDA, "no thread-block cluster is available for the small-mesh Tsit5 driver");
+    static int pow_dev = -1;  // device whose constant bank holds the pow tables
+    int dev = 0;
+    FVM_CUDA(cudaGetDevice(&dev));
+    if (pow_dev != dev) {
+        PowTables T;
+        pow_build_tables(T);
+        FVM_CUDA(cudaMemcpyToSymbol(c_pow, &T, sizeof T));
+        pow_dev = dev;
+    }
     ClusterTsit5Args a{};
     a.slice_ptr = p.d_slice_ptr.as<int64_t>();
     a.width = p.d_width.as<int32_t>();
