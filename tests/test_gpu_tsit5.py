@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 import fvm_oracle as O
-from problems import api_problem, mixed_annulus, oracle_problem, readme_diffusion, sine_diffusion
+from problems import api_problem, mixed_annulus, oracle_problem, readme_diffusion, sine_diffusion, wheel_diffusion
 
 pytestmark = pytest.mark.gpu
 
@@ -123,3 +123,22 @@ def test_adaptive_step_limit(gpu_lib, side, use_graph):
     prob = api_problem(spec)
     with pytest.raises(F.FVMError, match="max_steps"):
         F.solve(prob, F.Tsit5(), saveat=0.01, max_steps=5, use_graph=use_graph)
+
+
+def test_cluster_wide_rows_and_dense_saves(gpu_lib):
+    """The cluster driver on rows wider than 12 slots (a 40-spoke hub: the slot loop re-reads
+    its slots instead of holding them in registers), a Robin boundary and a linear source,
+    with 3001 saveat points (more than the 32 per step whose Hermite weights are shared):
+    the same steps as the host loop, solutions equal to 1e-10 of max|u|."""
+    import fvmgpu as F
+
+    spec = wheel_diffusion(40)
+    prob = api_problem(spec)
+    ts = np.linspace(spec.t0, spec.tf, 3001)
+    a = F.solve(prob, F.Tsit5(), saveat=ts, use_graph=True)
+    b = F.solve(prob, F.Tsit5(), saveat=ts, use_graph=False)
+    assert a.stats["driver"] == "cluster" and b.stats["driver"] == "host"
+    assert a.stats["naccept"] == b.stats["naccept"] and a.stats["nreject"] == b.stats["nreject"]
+    ua, ub = np.array(a.u), np.array(b.u)
+    assert ua.shape == (3001, spec.tri.num_points)
+    assert np.max(np.abs(ua - ub)) <= 1e-10 * np.max(np.abs(ub))
