@@ -154,6 +154,7 @@ struct fvm_template {
     double cheb_gershgorin = 0;                  // Gershgorin bound on the spectrum of D^-1 B
     fvm::DBuf d_bval64, d_bdiag_inv64, d_bdiag_inv32, d_rhs_red;  // reduced operator B (explicit), rhs
     fvm::DBuf d_bval32, d_brow32;                // FP32 B in difference form: off-diagonal values, row sums
+    fvm::DBuf d_bval32x;                         // FP32 B, explicit (the FP32-stored preconditioner operator)
     fvm::DBuf d_xfix, d_invV_free64, d_invV_free32;
     fvm::DBuf d_fixed_mask;                      // 1 on rows fixed by Dirichlet / missing vertex
     void build_steady();

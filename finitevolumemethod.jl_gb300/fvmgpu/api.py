@@ -930,8 +930,9 @@ class KrylovSolver:
     """GPU steady solver: method "auto" (CG if symmetric, else BiCGStab), "cg", "bicgstab";
     precond "jacobi" or "chebyshev" (a degree-`cheb_degree` Chebyshev polynomial in the
     Jacobi-scaled operator); mode "fp64", "mixed" (the Krylov iteration in FP32 with FP64
-    reliable updates of the residual and solution) or "fp32_precond" (the Krylov iteration in
-    FP64, its inner iterations - the Chebyshev polynomial - in FP32)."""
+    reliable updates of the residual and solution) or "fp32_precond" (FP64 Krylov iteration
+    and arithmetic; the Chebyshev preconditioner reads its operator values stored in FP32, a
+    third less operator traffic per preconditioner step)."""
 
     mode: str = "fp64"
     method: str = "auto"

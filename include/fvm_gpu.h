@@ -245,8 +245,8 @@ int fvm_template_tsit5_solve(fvm_template* tmpl, const double* u0, const fvm_ode
 #define FVM_PRECOND_CHEBYSHEV 1
 #define FVM_SOLVE_FP64 0       /* plain FP64 Krylov */
 #define FVM_SOLVE_MIXED 1      /* FP32 inner iterations, FP64 reliable residual / refinement */
-#define FVM_SOLVE_FP32_PRECOND 2 /* FP64 Krylov iteration; its inner iterations (the Chebyshev
-                                  * preconditioner's polynomial) in FP32 values, vectors, sums */
+#define FVM_SOLVE_FP32_PRECOND 2 /* FP64 Krylov iteration and arithmetic; the Chebyshev
+                                  * preconditioner reads its operator values stored in FP32 */
 
 typedef struct fvm_solver_options {
     double rtol;           /* on ||b - A x|| / ||b|| with the reference operator, FP64 */

@@ -104,9 +104,10 @@ def test_steady_disk_against_direct_solve(gpu_lib, mode, jump, precond):
 
 
 @pytest.mark.parametrize("jump", [False, True])
-def test_steady_fp32_inner_iterations(gpu_lib, jump):
-    """FP64 Krylov with its inner iterations (the Chebyshev polynomial) in FP32: the same
-    1e-10 FP64 residual, about as many outer iterations as the all-FP64 solve."""
+def test_steady_fp32_stored_preconditioner(gpu_lib, jump):
+    """FP64 Krylov with a Chebyshev preconditioner on FP32-stored operator values (FP64
+    vectors and arithmetic, so a fixed linear preconditioner): the same 1e-10 FP64 residual
+    without falling back, and about as many iterations as the all-FP64 solve."""
     import fvmgpu as F
 
     tri = triangulate_disk(6000, 256, seed=4)
@@ -121,7 +122,7 @@ def test_steady_fp32_inner_iterations(gpu_lib, jump):
     assert np.linalg.norm(sol.u - O.steady_solve(A, b)) <= 1e-7 * np.linalg.norm(sol.u)
     assert not sol.stats["fallback_fp64"]
     assert sol.stats["iterations"] <= 1.5 * ref64.stats["iterations"] + 16, (sol.stats, ref64.stats)
-    with pytest.raises(F.FVMError):  # the FP32 inner iteration is the Chebyshev polynomial
+    with pytest.raises(F.FVMError):  # the FP32-stored operator is the Chebyshev preconditioner's
         F.solve(prob, F.KrylovSolver(mode="fp32_precond", precond="jacobi"))
 
 
