@@ -95,9 +95,6 @@ struct RhsEpilogue {
         if (b) out += b[r];
         y[r] = out;
     }
-    __device__ void finish(const double*) const {}
-    __device__ double* partials() const { return nullptr; }
-    __device__ unsigned* ticket() const { return nullptr; }
 };
 
 template <class V, class Acc, class X, bool DIFF>

@@ -6,9 +6,8 @@
 //   Pre load(r)                 row r's operands, loaded with the slice's gathers so that
 //                               their latency hides behind the previous slice's sums
 //   row(r, acc, xa, pre, part)  row r's product acc (xa: the row's own x, gathered in the
-//                               difference form or when kOwnX); may add into part[0 .. NP)
-//   finish(tot)                 NP > 0: the grid totals of part, run once by one thread
-//   partials(), ticket()        NP > 0: a [NP][grid] double array and a zeroed counter
+//                               difference form or when kOwnX); part: per-lane scratch
+//                               (NP doubles, zero-initialised)
 #pragma once
 #include <algorithm>
 #include <cstdint>
@@ -194,7 +193,7 @@ __global__ void __launch_bounds__((NW + 1) * 32, kStreamPipelined<MAXW> && NW <=
 
     bool ok = mbar_wait(spbar, 0) && mbar_wait(xbar, 0);
     const int64_t* sp = spw - w0;  // sp[s] for s in [w0, w0 + wcount)
-    double part[Epi::NP > 0 ? Epi::NP : 1] = {};  // this lane's reduction partials
+    double part[Epi::NP > 0 ? Epi::NP : 1] = {};  // per-lane epilogue scratch
 
     // consumers, software-pipelined by one stage: the gathers of stage k + 1 are in flight
     // while the FP64 sums of stage k run.  A warp holds two stages at a time (the one it
@@ -270,49 +269,6 @@ __global__ void __launch_bounds__((NW + 1) * 32, kStreamPipelined<MAXW> && NW <=
             if ((ok = fetch(k, A))) finish(A);
     }
     if (!ok && lane == 0) atomicOr(a.err, kDevErrFullWait);
-    if constexpr (Epi::NP > 0) {
-        // grid reduction of the row partials, in a fixed order: lanes, warps, CTAs.  Only the
-        // consumer warps take part (named barrier 1); the last CTA to finish sums the CTA
-        // partials and hands the totals to the epilogue.
-        __shared__ double wred[NW][Epi::NP];
-        __shared__ bool last;
-#pragma unroll
-        for (int q = 0; q < Epi::NP; ++q) {
-            double x = part[q];
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-            if (lane == 0) wred[warp][q] = x;
-        }
-        asm volatile("bar.sync 1, %0;" ::"r"(NW * 32) : "memory");
-        if (threadIdx.x == 0) {
-            double* gp = e.partials();
-#pragma unroll
-            for (int q = 0; q < Epi::NP; ++q) {
-                double x = 0.0;
-                for (int w = 0; w < NW; ++w) x += wred[w][q];
-                gp[(size_t)q * gridDim.x + blockIdx.x] = x;
-            }
-            __threadfence();
-            last = atomicAdd(e.ticket(), 1u) == gridDim.x - 1;
-        }
-        asm volatile("bar.sync 1, %0;" ::"r"(NW * 32) : "memory");
-        if (!last || warp != 0) return;
-        __threadfence();
-        const double* gp = e.partials();
-        double tot[Epi::NP];
-#pragma unroll
-        for (int q = 0; q < Epi::NP; ++q) {
-            double x = 0.0;
-            for (unsigned c = lane; c < gridDim.x; c += 32) x += __ldcg(&gp[(size_t)q * gridDim.x + c]);
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-            tot[q] = x;
-        }
-        if (lane == 0) {
-            *e.ticket() = 0;
-            e.finish(tot);
-        }
-    }
 }
 
 constexpr int kStreamWarps = 8;
