@@ -73,6 +73,18 @@ def flux_evals(tri):
     return 3 * tri.num_triangles + 2 * tri.num_boundary_edges
 
 
+def read_stream_reference(torch, flush, nbytes, K):
+    """What a plain read of the RHS's compulsory bytes costs on this GPU in one launch of the
+    same size: the sum of an FP32 tensor of `nbytes` (a vectorised, fully occupied streaming
+    reduction), timed like the RHS, L2 flushed before each launch.  The copy benchmark behind
+    the roofline peak streams far more data per launch; this says how close the RHS kernel
+    is to the read rate a launch of its size reaches."""
+    t = torch.ones(nbytes // 4, dtype=torch.float32, device="cuda")
+    ms = timed_steps(lambda: t.sum(), max(K, 20), 5, flush, torch)
+    us = float(ms.mean()) * 1e3
+    return {"bytes": int(t.numel() * 4), "us": us, "gbs": t.numel() * 4 / (us * 1e-6) / 1e9}
+
+
 def canonical_roofline(tri, ms, peak):
     """The RHS against the canonical bytes of the reference's per-triangle layout
     (132 nt + 25 nv + 48 nbe: triangle connectivity, shape coefficients, normals times lengths,
@@ -321,6 +333,7 @@ def run_gpu(args):
     peak, peak_kind = measured_peaks()
     alg_bytes = 12 * info["operator_nonzeros"] + 16 * n
     achieved = alg_bytes / (ms.mean() / 1e3) / 1e9
+    stream = read_stream_reference(torch, flush, alg_bytes, K)
     traffic = profile_traffic("rhs_sell_stream_fp64_1000x1000")
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": max(W, 3),
@@ -334,7 +347,8 @@ def run_gpu(args):
                      "traffic": traffic, "kernel": "sell_stream_kernel<double,double,double,explicit,7,16>",
                      "alg_bytes_per_launch": alg_bytes, "alg_bytes_per_flux_eval": alg_bytes / units,
                      "peak_source": f"{peak_kind} hbm_gbs (burst copy)",
-                     "canonical": canonical_roofline(tri, ms.mean(), peak)},
+                     "canonical": canonical_roofline(tri, ms.mean(), peak),
+                     "read_stream": stream},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n,
                 "ms_per_step": float(ms_e2e.mean()), "path": "fvm_rhs C ABI, pinned host buffers"},
         "clocks": clk.summary(),
