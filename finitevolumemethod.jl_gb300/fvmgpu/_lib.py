@@ -255,6 +255,18 @@ def array_pointer(x, dtype="float64"):
     raise TypeError(f"unsupported array type {type(x)}")
 
 
+def host_empty(shape) -> np.ndarray:
+    """An uninitialised FP64 host array, page-locked when torch with CUDA is available (the
+    library then writes it directly, or copies into it at copy-engine speed)."""
+    try:
+        import torch
+        if torch.cuda.is_available():
+            return torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+    except Exception:  # pragma: no cover
+        pass
+    return np.empty(shape)
+
+
 def current_stream_handle():
     """cudaStream_t of torch's current stream when torch is loaded with CUDA, else NULL."""
     try:

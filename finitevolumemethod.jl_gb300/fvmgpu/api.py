@@ -1022,7 +1022,7 @@ def solve(prob, alg=None, *, saveat=None, dt=None, adaptive=None, abstol=1e-6, r
         raise TypeError(f"cannot solve {type(prob).__name__}")
     ts = _saveat_times(saveat, t0, tf)
     n = prob.mesh.triangulation.num_points
-    out = np.empty((ts.size, n))
+    out = _lib.host_empty((ts.size, n))
     o = _lib.OdeOptions()
     o.t0, o.tf = t0, tf
     if adaptive is None:
@@ -1043,7 +1043,7 @@ def solve(prob, alg=None, *, saveat=None, dt=None, adaptive=None, abstol=1e-6, r
         us = [np.append(row, 1.0) for row in out]  # the augmented component of the MatrixOperator form
     else:
         check(lib.fvm_tsit5_solve(prob.handle, dptr(u0c), C.byref(o), dptr(out), C.byref(st), s))
-        us = [row.copy() for row in out]
+        us = list(out)  # rows of the one output array, not copies
     return ODESolution(ts, us, {"naccept": st.naccept, "nreject": st.nreject, "nrhs": st.nrhs,
                                 "t_final": st.t_final, "elapsed_ms": st.elapsed_ms,
                                 "driver": _DRIVERS.get(st.driver, str(st.driver))})
