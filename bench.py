@@ -337,7 +337,8 @@ def run_gpu(args):
     traffic = profile_traffic("rhs_sell_stream_fp64_1000x1000")
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": max(W, 3),
-        "ms_per_step": float(ms.mean()), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "ms_per_step": float(ms.mean()), "vertex_rhs_per_s": n * ws / tmax * K if tmax else None,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic",
         "config": {"workload": WORKLOAD, "nv": n, "nt": tri.num_triangles, "nbe": tri.num_boundary_edges,
                    "flux_evals_per_step": units, "l2": "flushed between timed steps (256 MiB read)",
