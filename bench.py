@@ -370,7 +370,7 @@ def run_gpu(args):
 
 
 EXTRA_ROWS = ("rhs_fp32", "rhs_fp64_conservative", "rhs_triangle_fp64", "tsit5_1000_steps", "template_spmv",
-              "c1_readme", "batched_c4", "multimesh_c4", "adjoint_c5", "steady")
+              "c1_readme", "batched_c4", "multimesh_c4", "adjoint_c5", "system_gray_scott", "steady")
 
 
 def run_extras(args, F, torch, tri, mesh, prob, flush, perm, u_int, peak):
@@ -443,6 +443,7 @@ def run_selected(args, F, torch, tri, mesh, prob, flush, u_int):
             "rhs_triangle_fp64": rhs_triangle_fp64, "tsit5_1000_steps": tsit5_1000_steps,
             "template_spmv": template_spmv, "batched_c4": lambda: run_batched(args, F, torch, flush),
             "multimesh_c4": lambda: run_multimesh(args, F, torch), "adjoint_c5": lambda: run_adjoint(args, F, torch),
+            "system_gray_scott": lambda: run_system(args, F, torch, flush, mesh),
             "steady": lambda: run_steady(args, F)}
     out = {}
     for name in EXTRA_ROWS:
@@ -645,6 +646,69 @@ def run_batched(args, F, torch, flush):
         "per_instance_loop_ms": B * sol1.stats["elapsed_ms"],
         "speedup_vs_per_instance_loop": B * sol1.stats["elapsed_ms"] / st["elapsed_ms"],
         "fp32_vs_fp64_max_rel_err_8_instances": err}
+    return out
+
+
+def gray_scott_system(F, mesh, centre):
+    """The Gray-Scott tutorial system (docs/src/literate_tutorials/
+    gray_scott_model_turing_patterns_from_a_coupled_reaction_diffusion_system.jl): zero Neumann
+    on the whole boundary, fluxes -eps_c grad u_c (eps = 2e-5, 1e-5), sources b (1 - u) - u v^2
+    and -d v + u v^2 (b = 0.04, d = 0.1), initial bump exp(-80 r^2) about `centre`."""
+    bc = lambda x, y, t, uv, p: 0.0 * x  # noqa: E731
+    P = mesh.triangulation.points
+    r2 = (P[:, 0] - centre[0]) ** 2 + (P[:, 1] - centre[1]) ** 2
+    u0, v0 = 1 - np.exp(-80 * r2), np.exp(-80 * r2)
+    BCs = F.BoundaryConditions(mesh, (bc,) * mesh.triangulation.num_ghost_vertices,
+                               (F.Neumann,) * mesh.triangulation.num_ghost_vertices)
+    up = F.FVMProblem(mesh, BCs, flux_function=lambda x, y, t, a, b, g, e: (-a[0] * e, -b[0] * e), flux_parameters=2e-5,
+                      source_function=lambda x, y, t, uv, b: b * (1 - uv[0]) - uv[0] * uv[1] ** 2,
+                      source_parameters=0.04, initial_condition=u0, final_time=6000.0)
+    vp = F.FVMProblem(mesh, BCs, flux_function=lambda x, y, t, a, b, g, e: (-a[1] * e, -b[1] * e), flux_parameters=1e-5,
+                      source_function=lambda x, y, t, uv, d: -d * uv[1] + uv[0] * uv[1] ** 2,
+                      source_parameters=0.1, initial_condition=v0, final_time=6000.0)
+    return F.FVMSystem(up, vp)
+
+
+def run_system(args, F, torch, flush, c2_mesh):
+    """FVMSystem: the Gray-Scott tutorial system on the tutorial's 200 x 200 mesh of [-1, 1]^2
+    (RHS, and the tutorial's solve to t = 6000 with saveat 10 by adaptive Tsit5) and on the 1000 x 1000 mesh of
+    the headline row (RHS: 2M state values).  Algorithmic bytes of one system RHS: per padded
+    slot a 4-byte column and 8 bytes per coupled flux block, the state read and the result
+    written (16 B per point and component), one mask byte per point."""
+    import time
+
+    from fvmgpu.meshes import triangulate_rectangle
+
+    out = {}
+    K = max(20, min(args.steps, 200))
+    peak = measured_peaks()[0]
+    tri200 = triangulate_rectangle(-1.0, 1.0, -1.0, 1.0, 200, 200, single_boundary=True)
+    for name, mesh, centre in (("gray_scott_200x200", F.FVMGeometry(tri200), (0.0, 0.0)),
+                               ("gray_scott_1000x1000", c2_mesh, (0.5, 0.5))):
+        t0 = time.perf_counter()
+        sys = gray_scott_system(F, mesh, centre)
+        setup_s = time.perf_counter() - t0
+        n, N = mesh.triangulation.num_points, sys.neqs
+        info, minfo = sys.info(), mesh.info()
+        U = torch.from_numpy(np.ascontiguousarray(sys.initial_condition.T)).cuda()
+        dU = torch.empty_like(U)
+        torch.cuda.nvtx.range_push(name)  # lets a profiler select this size's launches
+        ms = timed_steps(lambda: sys.rhs(dU.T, U.T, internal=True), K, 5, flush, torch)
+        torch.cuda.nvtx.range_pop()
+        alg = (4 + 8 * info["flux_blocks"]) * minfo["operator_slots"] + 16 * N * n + n
+        row = {"points": n, "neqs": N, "setup_s": setup_s, "rhs_ms": float(ms.mean()),
+               "point_rhs_per_s": n / (ms.mean() / 1e3), "alg_bytes": alg,
+               "achieved_gbs": alg / (ms.mean() / 1e3) / 1e9, "frac_of_measured_hbm": alg / (ms.mean() / 1e3) / 1e9 / peak,
+               "forms": info}
+        if n <= 50_000:
+            t1 = time.perf_counter()
+            sol = F.solve(sys, F.Tsit5(), saveat=10.0)
+            wall = time.perf_counter() - t1
+            sol = F.solve(sys, F.Tsit5(), saveat=10.0)  # second solve: set-up paid
+            row["tsit5_adaptive_to_t6000"] = {"first_wall_s": wall, "elapsed_ms": sol.stats["elapsed_ms"],
+                                              "steps": sol.stats["naccept"], "rejects": sol.stats["nreject"],
+                                              "driver": sol.stats["driver"], "saves": len(sol.u)}
+        out[name] = row
     return out
 
 

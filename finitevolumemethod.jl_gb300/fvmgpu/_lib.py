@@ -29,6 +29,8 @@ FVM_RHS_FORCE_TRIANGLE = 16
 FVM_RHS_CONSERVATIVE = 32
 FVM_FP64, FVM_FP32 = 0, 1
 FVM_MESH_NO_RENUMBER = 1
+FVM_SYSTEM_MAX_EQ = 8
+FVM_SYSTEM_MAX_TERMS = 64
 FVM_TEMPLATE_DIFFUSION, FVM_TEMPLATE_LINEAR_REACTION_DIFFUSION = 0, 1
 FVM_TEMPLATE_POISSON, FVM_TEMPLATE_MEAN_EXIT_TIME = 2, 3
 FVM_SOLVER_AUTO, FVM_SOLVER_CG, FVM_SOLVER_BICGSTAB = 0, 1, 2
@@ -73,6 +75,22 @@ class ProblemDesc(C.Structure):
         ("dudt", c_double_p),
         ("dirichlet", c_double_p),
         ("precision", C.c_int32),
+    ]
+
+
+class SystemDesc(C.Structure):
+    _fields_ = [
+        ("neq", C.c_int32),
+        ("vertex_code", c_int8_p),
+        ("bedge_neumann", c_int8_p),
+        ("dual_edge_D", c_double_p),
+        ("quarter_D", c_double_p),
+        ("nmono", C.c_int32),
+        ("mono_exp", c_int8_p),
+        ("source", c_double_p),
+        ("dudt", c_double_p),
+        ("quarter_neumann", c_double_p),
+        ("dirichlet", c_double_p),
     ]
 
 
@@ -136,6 +154,13 @@ SIGNATURES = {
     "fvm_dirichlet_apply": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_int32, C.c_void_p]),
     "fvm_tsit5_solve": (C.c_int, [C.c_void_p, c_double_p, C.POINTER(OdeOptions), c_double_p, C.POINTER(OdeStats),
                                   C.c_void_p]),
+    "fvm_system_create": (C.c_int, [C.c_void_p, C.POINTER(SystemDesc), C.POINTER(C.c_void_p)]),
+    "fvm_system_destroy": (C.c_int, [C.c_void_p]),
+    "fvm_system_info": (C.c_int, [C.c_void_p, c_int64_p]),
+    "fvm_system_rhs": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int32, C.c_void_p]),
+    "fvm_system_dirichlet_apply": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_int32, C.c_void_p]),
+    "fvm_system_tsit5_solve": (C.c_int, [C.c_void_p, c_double_p, C.POINTER(OdeOptions), c_double_p,
+                                         C.POINTER(OdeStats), C.c_void_p]),
     "fvm_batch_create": (C.c_int, [C.c_void_p, C.c_int32, c_double_p, c_double_p, C.c_int32,
                                    C.POINTER(C.c_void_p)]),
     "fvm_batch_destroy": (C.c_int, [C.c_void_p]),

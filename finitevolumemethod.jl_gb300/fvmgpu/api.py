@@ -16,7 +16,8 @@ import numpy as np
 from . import _lib
 from ._lib import (FVM_FP32, FVM_FP64, FVM_VERTEX_DIRICHLET, FVM_VERTEX_DUDT, FVM_VERTEX_FREE,
                    FVM_VERTEX_NOT_A_VERTEX, as_f64, as_i8, as_i32, check, dptr, load)
-from .forms import classify_flux, classify_xytu, sample_xy
+from .forms import (classify_flux, classify_system_flux, classify_system_poly, classify_xytu, monomials,
+                    sample_xy)
 from .meshes import Triangulation
 
 
@@ -338,7 +339,10 @@ def _precision(p):
 class FVMProblem:
     """FVMProblem(mesh, boundary_conditions[, internal_conditions]; ...)
     (src/problem.jl:96-163).  The closures are classified into device-coded forms when the
-    problem is created; forms outside the device-coded set raise UnsupportedFormError.
+    problem is first used (`handle`, `fvm_eqs`, `solve`), as the reference evaluates them only
+    when it solves; forms outside the device-coded set raise UnsupportedFormError there.  A
+    problem that is a component of an FVMSystem is never classified on its own: its closures
+    take the tuple of all components.
 
     precision: "fp64" (default) or "fp32" (FP32 flux assembly with FP64 control-volume
     division; linear forms only)."""
@@ -367,7 +371,7 @@ class FVMProblem:
         self.final_time = float(final_time)
         self.precision = _precision(precision)
         self._h = None
-        self._build()
+        self._built = False
 
     # construct_flux_function (src/problem.jl:425-440) happens through the device form:
     # q = -D(x, y, u(x_sigma)) grad u, D a polynomial of degree <= 2 in u.
@@ -442,11 +446,14 @@ class FVMProblem:
 
     @property
     def handle(self):
+        if not self._built:
+            self._build()
+            self._built = True
         return self._h
 
     def info(self) -> Dict[str, int]:
         a = np.zeros(6, dtype=np.int64)
-        check(load().fvm_problem_info(self._h, dptr(a, _lib.c_int64_p)))
+        check(load().fvm_problem_info(self.handle, dptr(a, _lib.c_int64_p)))
         keys = ["linear", "operator_nonzeros", "operator_slots", "has_constant", "has_quadratic", "precision"]
         return dict(zip(keys, (int(v) for v in a)))
 
@@ -454,7 +461,7 @@ class FVMProblem:
         tri = self.mesh.triangulation
         code = np.empty(tri.num_points, dtype=np.int8)
         neu = np.empty(tri.num_boundary_edges, dtype=np.int8)
-        check(load().fvm_problem_export_codes(self._h, dptr(code, _lib.c_int8_p), dptr(neu, _lib.c_int8_p)))
+        check(load().fvm_problem_export_codes(self.handle, dptr(code, _lib.c_int8_p), dptr(neu, _lib.c_int8_p)))
         return code, neu
 
     def __del__(self):
@@ -469,7 +476,7 @@ class FVMProblem:
 
 
 def _prob_of(p):
-    if isinstance(p, (FVMProblem, _Template)):
+    if isinstance(p, (FVMProblem, _Template, FVMSystem)):
         return p
     if isinstance(p, dict):
         return p["prob"]
@@ -485,6 +492,8 @@ def fvm_eqs(du, u, p, t, *, force_triangle=False, conservative=False, internal=F
     prob = _prob_of(p)
     if isinstance(prob, _Template):
         return prob.apply(du, u, stream=stream)
+    if isinstance(prob, FVMSystem):
+        return prob.rhs(du, u, t, internal=internal, stream=stream)
     up, ul = _lib.array_pointer(u)
     dp, dl = _lib.array_pointer(du)
     if ul != dl:
@@ -502,10 +511,217 @@ def fvm_eqs(du, u, p, t, *, force_triangle=False, conservative=False, internal=F
 
 def update_dirichlet_nodes(u, prob, t=0.0, stream=None):
     """update_dirichlet_nodes! (src/equations/dirichlet.jl:78-86), in place."""
+    prob = _prob_of(prob)
+    if isinstance(prob, FVMSystem):
+        return prob.update_dirichlet_nodes(u, t, stream)
     up, ul = _lib.array_pointer(u)
     s = stream if stream is not None else _lib.current_stream_handle()
-    check(load().fvm_dirichlet_apply(_prob_of(prob).handle, up, float(t), ul, s))
+    check(load().fvm_dirichlet_apply(prob.handle, up, float(t), ul, s))
     return u
+
+
+# --------------------------------------------------------------------------------------
+# systems of equations (src/problem.jl:190-365)
+# --------------------------------------------------------------------------------------
+FLUX_ERROR = """
+The flux function errored when evaluated. Please recheck your specification of the function.
+If any of your problems have been defined in terms of a diffusion function D(x, y, t, u, p)
+rather than a flux function, then you need to instead provide a flux function q(x, y, t, alpha, beta, gamma, p),
+recalling the relationship between the two:
+
+    q(x, y, t, alpha, beta, gamma, p) = -D(x, y, t, alpha*x + beta*y + gamma, p) * (alpha, beta)
+
+where p is the same argument for both functions.
+"""
+
+
+class InvalidFluxError(ValueError):
+    """A component of an FVMSystem has no usable flux function (src/problem.jl:277-292)."""
+
+    def __init__(self, detail=""):
+        super().__init__(FLUX_ERROR + (f"\n{detail}" if detail else ""))
+
+
+class FVMSystem:
+    """FVMSystem(prob1, ..., probN) (src/problem.jl:190-365): N coupled equations on one mesh.
+
+    Component i's closures see every component: its flux q(x, y, t, alpha, beta, gamma, p) takes
+    N-tuples alpha, beta, gamma (alpha[c] x + beta[c] y + gamma[c] approximates u_c), its source
+    and condition functions f(x, y, t, u, p) take u = (u_1, ..., u_N).  Each component keeps its
+    own boundary and internal conditions (merge_problem_conditions, :336-365).  Solutions are
+    (N, npoints) arrays whose (j, i) entry is component j at node i.
+
+    Device-coded forms (anything else raises UnsupportedFormError at construction):
+      flux       -sum_c D_c(x, y) (alpha[c], beta[c])  (diagonal or cross diffusion);
+      source     a polynomial of total degree <= 3 in u with (x, y) coefficients;
+      Dudt       the same;
+      Neumann    affine in u with (x, y) coefficients;
+      Dirichlet  a function of (x, y);
+    none may depend on t.  A component defined by a diffusion_function raises InvalidFluxError,
+    as the reference's construction does."""
+
+    def __init__(self, *probs: FVMProblem):
+        if len(probs) == 0:
+            raise ValueError("There must be at least one problem.")
+        if len(probs) > _lib.FVM_SYSTEM_MAX_EQ:
+            raise ValueError(f"at most {_lib.FVM_SYSTEM_MAX_EQ} equations are supported")
+        mesh = probs[0].mesh
+        if not all(p.mesh is mesh for p in probs):
+            raise AssertionError("All problems must have the same mesh.")
+        if not all(p.initial_time == probs[0].initial_time for p in probs):
+            raise AssertionError("All problems must have the same initial time.")
+        if not all(p.final_time == probs[0].final_time for p in probs):
+            raise AssertionError("All problems must have the same final time.")
+        for i, p in enumerate(probs):
+            if p.flux_function is None:
+                raise InvalidFluxError(f"component {i} has no flux_function")
+        self.mesh = mesh
+        self.problems = tuple(probs)
+        self.neqs = len(probs)
+        self.initial_condition = np.stack([p.initial_condition for p in probs])
+        self.initial_time = probs[0].initial_time
+        self.final_time = probs[0].final_time
+        self.conditions = tuple(p.conditions for p in probs)
+        nf = [len(c.functions) for c in self.conditions]
+        self.cnum_fncs = tuple(int(v) for v in np.cumsum([0] + nf[:-1]))
+        self.functions = tuple(f for c in self.conditions for f in c.functions)
+        self.source_functions = tuple(None if p.source_function is None else
+                                      ParametrisedFunction(p.source_function, p.source_parameters) for p in probs)
+        self.flux_functions = tuple(ParametrisedFunction(p.flux_function, p.flux_parameters) for p in probs)
+        self._h = None
+        self._build()
+
+    def map_fidx(self, fidx, var):
+        """Index into `functions` of component var's condition function fidx (problem.jl:295)."""
+        return fidx + self.cnum_fncs[var]
+
+    def _build(self):
+        mesh, tri, N = self.mesh, self.mesh.triangulation, self.neqs
+        t0 = self.initial_time
+        npts, nt, nbe = tri.num_points, tri.num_triangles, tri.num_boundary_edges
+        hv = tri.has_vertex()
+        dual, quarter = mesh.sample_points()
+        dx, dy = dual[..., 0].ravel(), dual[..., 1].ravel()
+        qx, qy = quarter[..., 0].ravel(), quarter[..., 1].ravel()
+        P = tri.points
+        codes = np.zeros((N, npts), dtype=np.int8)
+        neu = np.zeros((N, nbe), dtype=np.int8)
+        Dd = np.zeros((N, N, 3 * nt))
+        Dq = np.zeros((N, N, 2 * nbe))
+        basis = monomials(N)
+        col = {tuple(e): m for m, e in enumerate(basis)}
+        src = np.zeros((N, npts, basis.shape[0]))
+        dudt = np.zeros((N, npts, basis.shape[0]))
+        qneu = np.zeros((N, 2 * nbe, 1 + N))
+        dirv = np.zeros((N, npts))
+        self._codes = codes
+        for r, (cond, q) in enumerate(zip(self.conditions, self.flux_functions)):
+            code, fidx = cond.vertex_tables(hv)
+            nfid = cond.neumann_table(tri.boundary_edges)
+            codes[r], neu[r] = code, nfid >= 0
+            Dd[r] = classify_system_flux(q, dx, dy, t0, N, f"flux_function of component {r}")
+            if nbe:
+                Dq[r] = classify_system_flux(q, qx, qy, t0, N, f"flux_function of component {r}")
+            free = code == FVM_VERTEX_FREE
+            S = self.source_functions[r]
+            if S is not None and np.any(free):
+                e, c = classify_system_poly(S, P[free, 0], P[free, 1], t0, N, f"source_function of component {r}")
+                for k, ek in enumerate(e):
+                    src[r, free, col[tuple(ek)]] = c[:, k]
+            for kind, arr, want in (("Dudt", dudt, FVM_VERTEX_DUDT), ("Dirichlet", None, FVM_VERTEX_DIRICHLET)):
+                f_of = np.where(code == want, fidx, -1)
+                for f in np.unique(f_of[f_of >= 0]):
+                    sel = f_of == f
+                    what = f"{kind} function {int(f)} of component {r}"
+                    e, c = classify_system_poly(cond.functions[int(f)], P[sel, 0], P[sel, 1], t0, N, what,
+                                                max_degree=3 if arr is not None else 0)
+                    for k, ek in enumerate(e):
+                        if arr is not None:
+                            arr[r, sel, col[tuple(ek)]] = c[:, k]
+                        else:
+                            dirv[r, sel] = c[:, k]
+            for f in np.unique(nfid[nfid >= 0]):
+                sel = np.repeat(nfid == f, 2)
+                e, c = classify_system_poly(cond.functions[int(f)], qx[sel], qy[sel], t0, N,
+                                            f"Neumann function {int(f)} of component {r}", max_degree=1)
+                for k, ek in enumerate(e):
+                    qneu[r, sel, 0 if ek.sum() == 0 else 1 + int(np.argmax(ek))] = c[:, k]
+        used = np.nonzero(np.any(src != 0, axis=(0, 1)) | np.any(dudt != 0, axis=(0, 1)))[0]
+        self.monomials = basis[used]
+        d = _Desc()
+        d.c = _lib.SystemDesc()
+        d.c.neq = N
+        d.arr("vertex_code", as_i8(codes), _lib.c_int8_p)
+        d.arr("bedge_neumann", as_i8(neu) if nbe else None, _lib.c_int8_p)
+        d.arr("dual_edge_D", as_f64(Dd))
+        d.arr("quarter_D", as_f64(Dq) if nbe else None)
+        d.c.nmono = int(used.size)
+        d.arr("mono_exp", as_i8(basis[used]) if used.size else None, _lib.c_int8_p)
+        d.arr("source", as_f64(src[:, :, used]) if used.size and np.any(src) else None)
+        d.arr("dudt", as_f64(dudt[:, :, used]) if used.size and np.any(dudt) else None)
+        d.arr("quarter_neumann", as_f64(qneu) if nbe and np.any(qneu) else None)
+        d.arr("dirichlet", as_f64(dirv) if np.any(dirv) else None)
+        h = C.c_void_p()
+        check(load().fvm_system_create(mesh.handle, C.byref(d.c), C.byref(h)))
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def info(self) -> Dict[str, int]:
+        a = np.zeros(6, dtype=np.int64)
+        check(load().fvm_system_info(self._h, dptr(a, _lib.c_int64_p)))
+        keys = ["neqs", "flux_blocks", "terms", "varying_terms", "dirichlet_entries", "has_neumann_constants"]
+        return dict(zip(keys, (int(v) for v in a)))
+
+    def _flat(self, x, name):
+        """(pointer, location, host copy or None) of an (N, npoints) array in the library's
+        [point][component] memory order.  numpy arrays of any layout are staged; a CUDA tensor
+        must already have that memory order (e.g. torch.empty(npoints, N).T)."""
+        N, n = self.neqs, self.mesh.triangulation.num_points
+        if tuple(x.shape) != (N, n):
+            raise ValueError(f"{name} must have shape ({N}, {n})")
+        if isinstance(x, np.ndarray):
+            xt = np.ascontiguousarray(x.T, dtype=np.float64)
+            return C.c_void_p(xt.ctypes.data), _lib.FVM_PTR_HOST, xt
+        p, loc = _lib.array_pointer(x.T)
+        return p, loc, None
+
+    def rhs(self, du, u, t=0.0, internal=False, stream=None):
+        """fvm_eqs!(du, u, p, t) for the system; u, du (N, npoints).  internal=True takes device
+        tensors already in the library's internal point numbering (a device-resident loop's)."""
+        up, ul, _ = self._flat(u, "u")
+        dp, dl, dh = self._flat(du, "du")
+        if ul != dl:
+            raise TypeError("u and du must both be host arrays or both device tensors")
+        if internal:
+            if ul != _lib.FVM_PTR_DEVICE:
+                raise TypeError("internal=True needs device tensors")
+            ul = _lib.FVM_PTR_DEVICE_INTERNAL
+        s = stream if stream is not None else _lib.current_stream_handle()
+        check(load().fvm_system_rhs(self._h, up, dp, float(t), ul, s))
+        if dh is not None:
+            du[...] = dh.T
+        return du
+
+    def update_dirichlet_nodes(self, u, t=0.0, stream=None):
+        """update_dirichlet_nodes! for the system, in place; u (N, npoints)."""
+        up, ul, uh = self._flat(u, "u")
+        s = stream if stream is not None else _lib.current_stream_handle()
+        check(load().fvm_system_dirichlet_apply(self._h, up, float(t), ul, s))
+        if uh is not None:
+            u[...] = uh.T
+        return u
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib._LIB is not None:
+            _lib._LIB.fvm_system_destroy(h)
+            self._h = None
+
+    def __repr__(self):
+        return f"FVMSystem with {self.neqs} equations and time span ({self.initial_time}, {self.final_time})"
 
 
 # --------------------------------------------------------------------------------------
@@ -1018,11 +1234,13 @@ def solve(prob, alg=None, *, saveat=None, dt=None, adaptive=None, abstol=1e-6, r
         t0, tf, u0 = prob.initial_time, prob.final_time, prob.u0
     elif isinstance(prob, FVMProblem):
         t0, tf, u0 = prob.initial_time, prob.final_time, prob.initial_condition
+    elif isinstance(prob, FVMSystem):
+        t0, tf, u0 = prob.initial_time, prob.final_time, prob.initial_condition.T  # [point][component]
     else:
         raise TypeError(f"cannot solve {type(prob).__name__}")
     ts = _saveat_times(saveat, t0, tf)
     n = prob.mesh.triangulation.num_points
-    out = _lib.host_empty((ts.size, n))
+    out = _lib.host_empty((ts.size, n, prob.neqs) if isinstance(prob, FVMSystem) else (ts.size, n))
     o = _lib.OdeOptions()
     o.t0, o.tf = t0, tf
     if adaptive is None:
@@ -1041,6 +1259,9 @@ def solve(prob, alg=None, *, saveat=None, dt=None, adaptive=None, abstol=1e-6, r
     if isinstance(prob, _TimeTemplate):
         check(lib.fvm_template_tsit5_solve(prob.handle, dptr(u0c), C.byref(o), dptr(out), C.byref(st), s))
         us = [np.append(row, 1.0) for row in out]  # the augmented component of the MatrixOperator form
+    elif isinstance(prob, FVMSystem):
+        check(lib.fvm_system_tsit5_solve(prob.handle, dptr(u0c), C.byref(o), dptr(out), C.byref(st), s))
+        us = [row.T for row in out]  # (N, npoints) views: entry (j, i) is component j at node i
     else:
         check(lib.fvm_tsit5_solve(prob.handle, dptr(u0c), C.byref(o), dptr(out), C.byref(st), s))
         us = list(out)  # rows of the one output array, not copies

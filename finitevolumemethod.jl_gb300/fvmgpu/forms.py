@@ -144,3 +144,156 @@ def sample_xy(f, x, y, *extra, what="function"):
     if not np.all(np.isfinite(v)):
         _reject(what, "non-finite values")
     return v
+
+
+# --------------------------------------------------------------------------------------
+# systems (FVMSystem): closures take N-tuples -- alpha, beta, gamma for fluxes, the node's
+# component values u = (u_1, ..., u_N) for sources and conditions
+# --------------------------------------------------------------------------------------
+_SYS_DEGREE = 3
+
+
+def evaluate_tuples(f, x, y, t, *tuples):
+    """Call f(x, y, t, T1, T2, ...) whose Ti are N-tuples of arrays over the points; one call
+    per point, with tuples of floats, when the closure does not accept arrays."""
+    x = np.asarray(x, dtype=np.float64)
+    n = x.shape[0]
+    y = np.broadcast_to(np.asarray(y, dtype=np.float64), (n,))
+    T = [tuple(np.broadcast_to(np.asarray(c, dtype=np.float64), (n,)) for c in tup) for tup in tuples]
+    try:
+        with np.errstate(all="ignore"):
+            out = f(x, y, t, *T)
+        if isinstance(out, tuple):
+            return tuple(np.broadcast_to(np.asarray(o, dtype=np.float64), (n,)).copy() for o in out)
+        return np.broadcast_to(np.asarray(out, dtype=np.float64), (n,)).copy()
+    except (ValueError, TypeError, IndexError):
+        pass
+    res = None
+    for m in range(n):
+        r = f(float(x[m]), float(y[m]), t, *[tuple(float(c[m]) for c in tup) for tup in T])
+        if res is None:
+            res = [np.empty(n) for _ in r] if isinstance(r, tuple) else np.empty(n)
+        if isinstance(r, tuple):
+            for c, v in enumerate(r):
+                res[c][m] = v
+        else:
+            res[m] = r
+    return tuple(res) if isinstance(res, list) else res
+
+
+def _reject_sys(what, why):
+    raise UnsupportedFormError(FVM_ERR_UNSUPPORTED_FORM, f"{what}: {why}; supported system forms are fluxes "
+                               "-sum_c D_c(x, y) (alpha[c], beta[c]), sources and Dudt values that are polynomials "
+                               "of total degree <= 3 in the components with (x, y) coefficients, Neumann values "
+                               "affine in the components, Dirichlet values of (x, y); none may depend on t")
+
+
+def monomials(N, degree=_SYS_DEGREE):
+    """Exponent tuples of the monomials in N variables of total degree <= degree, by degree,
+    then lexicographically from the first variable (int8 array (M, N))."""
+    out = [()]
+    for _ in range(N):
+        out = [e + (k,) for e in out for k in range(degree + 1)]
+    out = [e for e in out if sum(e) <= degree]
+    out.sort(key=lambda e: (sum(e), tuple(-k for k in e)))
+    return np.array(out, dtype=np.int8).reshape(-1, N)
+
+
+def _vandermonde(U, exps):
+    return np.prod(U[:, None, :] ** exps[None, :, :].astype(np.float64), axis=2)
+
+
+def classify_system_flux(q, x, y, t0, N, what="flux_function"):
+    """D (N, npoints) of a component flux q(x, y, t, alpha, beta, gamma) = -sum_c D_c(x, y)
+    (alpha[c], beta[c]), or reject.  Probes alpha, beta, gamma = unit tuples and zero, then
+    verifies one seeded combination at a second time."""
+    x = np.asarray(x, dtype=np.float64)
+    n = x.shape[0]
+    zero = tuple(np.zeros(n) for _ in range(N))
+
+    def unit(c, v=1.0):
+        return tuple(np.full(n, v if k == c else 0.0) for k in range(N))
+
+    def ev(a, b, g, t=t0):
+        try:
+            out = evaluate_tuples(q, x, y, t, a, b, g)
+        except Exception as e:  # noqa: BLE001
+            _reject_sys(what, f"evaluation failed ({e!r})")
+        if not (isinstance(out, tuple) and len(out) == 2):
+            _reject_sys(what, "a flux must return (qx, qy)")
+        return out
+
+    zx, zy = ev(zero, zero, zero)
+    D = np.empty((N, n))
+    ok = True
+    for c in range(N):
+        ax, ay = ev(unit(c), zero, zero)
+        bx, by = ev(zero, unit(c), zero)
+        gx, gy = ev(zero, zero, unit(c))
+        D[c] = -ax
+        sc = np.maximum(np.abs(D[c]), 1e-300)
+        ok = ok and all(np.all(np.abs(v) <= _RTOL * sc) for v in (ay, bx, gx, gy, zx, zy))
+        ok = ok and np.all(np.abs(by + D[c]) <= _RTOL * sc)
+    if ok and np.all(np.isfinite(D)):
+        rng = np.random.default_rng(7)
+        A, B, G = (rng.uniform(-2.0, 2.0, N) for _ in range(3))
+        cx, cy = ev(tuple(np.full(n, v) for v in A), tuple(np.full(n, v) for v in B),
+                    tuple(np.full(n, v) for v in G), t0 + 1.37)
+        sc = np.maximum(np.abs(D).sum(axis=0), 1e-300) * 2.0
+        ok = (np.all(np.abs(cx + (A[:, None] * D).sum(axis=0)) <= _RTOL * sc)
+              and np.all(np.abs(cy + (B[:, None] * D).sum(axis=0)) <= _RTOL * sc))
+    else:
+        ok = False
+    if not ok:
+        _reject_sys(what, "not of the form -sum_c D_c(x, y) (alpha[c], beta[c])")
+    return D
+
+
+def classify_system_poly(f, x, y, t0, N, what, max_degree=_SYS_DEGREE):
+    """(exps (m, N), coefficients (npoints, m)) of f(x, y, t, u) = sum_m c_m(x, y) prod_c
+    u[c]^exps[m][c], a polynomial of total degree <= max_degree in the N-tuple u, or reject.
+
+    The closure is evaluated at seeded sample tuples u (the same at every point), the
+    coefficients fitted by least squares on the full monomial basis, the monomials whose
+    coefficients vanish dropped and the rest refitted; the fit is then verified at fresh
+    tuples and at a second time to a relative tolerance of 1e-10."""
+    x = np.asarray(x, dtype=np.float64)
+    n = x.shape[0]
+    exps = monomials(N, max_degree)
+    M = exps.shape[0]
+    rng = np.random.default_rng(11)
+    U = np.vstack([np.zeros((1, N)), rng.uniform(-1.5, 1.5, size=(M + 5, N))])
+    Uc = rng.uniform(-2.0, 2.0, size=(4, N))
+
+    def ev(u, t=t0):
+        try:
+            v = evaluate_tuples(f, x, y, t, tuple(np.full(n, c) for c in u))
+        except Exception as e:  # noqa: BLE001
+            _reject_sys(what, f"evaluation failed ({e!r})")
+        if isinstance(v, tuple) or not np.all(np.isfinite(v)):
+            _reject_sys(what, "non-finite or non-scalar values")
+        return v
+
+    Fv = np.stack([ev(u) for u in U])  # (K, n)
+    # points with identical samples share one fit, so a coefficient that does not depend on
+    # (x, y) comes out bit-identical at every point
+    Fu, inv = np.unique(Fv, axis=1, return_inverse=True)
+    inv = inv.reshape(-1)
+    coef = np.linalg.lstsq(_vandermonde(U, exps), Fu, rcond=None)[0]  # (M, unique)
+    cmax = np.max(np.abs(coef), axis=1)
+    keep = cmax > 1e-12 * max(np.max(cmax), 1e-300)
+    exps = exps[keep]
+    if exps.shape[0]:
+        coef = np.linalg.lstsq(_vandermonde(U, exps), Fu, rcond=None)[0][:, inv]
+    else:
+        coef = np.zeros((0, n))
+    scale = np.max(np.abs(coef), axis=0) if exps.shape[0] else np.zeros(n)
+    scale = np.maximum(scale, np.max(scale, initial=0.0) * 1e-300 + 1e-300)
+    checks = [(u, t0) for u in Uc] + [(U[1], t0 + 1.37), (Uc[0], t0 + 1.37)]
+    for u, t in checks:
+        pred = (_vandermonde(u[None, :], exps) @ coef)[0] if exps.shape[0] else np.zeros(n)
+        bound = _RTOL * scale * max(1.0, M) * (1.0 + np.max(np.abs(u))) ** max_degree
+        if not np.all(np.abs(ev(u, t) - pred) <= bound):
+            _reject_sys(what, "depends on t" if t != t0 else
+                        f"not a polynomial of total degree <= {max_degree} in the components")
+    return exps, np.ascontiguousarray(coef.T)

@@ -190,6 +190,54 @@ typedef struct fvm_ode_stats {
 int fvm_tsit5_solve(fvm_problem* prob, const double* u0, const fvm_ode_options* opt, double* out,
                     fvm_ode_stats* stats, void* stream);
 
+/* ---- systems of equations (FVMSystem, src/problem.jl:190-365) ---------------------------
+ * N coupled components on one mesh.  State is laid out [npoints][neq] (component fastest),
+ * the memory order of the reference's N x npoints solution matrix (column-major), in the
+ * caller's point numbering.  Each component has its own conditions (vertex codes, Neumann
+ * edges), as merge_problem_conditions keeps them (src/problem.jl:336-365).  Device-coded forms:
+ *   flux of component r   q_r = -sum_c D_rc(x, y) (alpha_c, beta_c)  (linear, cross-diffusion
+ *                         allowed), sampled at the dual-edge midpoints and boundary quarter
+ *                         points;
+ *   source / Dudt of r    a polynomial of total degree <= 3 in the node's component values,
+ *                         sum_m coef_m(x, y) prod_c u_c^exp[m][c];
+ *   Neumann value of r    affine in the quarter-point component values, n0 + sum_c n_c u_c(m);
+ *   Dirichlet value of r  a(x, y).
+ * Arrays are laid out as below; a NULL array means the form is identically zero. */
+#define FVM_SYSTEM_MAX_EQ 8
+#define FVM_SYSTEM_MAX_TERMS 64   /* non-zero (component, monomial) source / Dudt terms */
+typedef struct fvm_system fvm_system;
+typedef struct fvm_system_desc {
+    int32_t neq;                    /* 1 .. FVM_SYSTEM_MAX_EQ */
+    const int8_t* vertex_code;      /* [neq][npoints] FVM_VERTEX_* per component */
+    const int8_t* bedge_neumann;    /* [neq][nbedge] 1 if the edge is Neumann for the component */
+    const double* dual_edge_D;      /* [neq*neq][ntri*3], block (r, c) at r*neq + c */
+    const double* quarter_D;        /* [neq*neq][nbedge*2] */
+    int32_t nmono;                  /* monomials of the polynomial forms */
+    const int8_t* mono_exp;         /* [nmono][neq] exponents, total degree <= 3 */
+    const double* source;           /* [neq][npoints][nmono], used on FREE vertices */
+    const double* dudt;             /* [neq][npoints][nmono], used on DUDT vertices */
+    const double* quarter_neumann;  /* [neq][nbedge*2][1+neq]: n0, n_1 .. n_neq */
+    const double* dirichlet;        /* [neq][npoints] */
+} fvm_system_desc;
+/* Replaces FVMSystem(prob1, ..., probN) (src/problem.jl:318-334) with merge_problem_conditions
+ * (:336-365). */
+int fvm_system_create(fvm_mesh* mesh, const fvm_system_desc* desc, fvm_system** out);
+int fvm_system_destroy(fvm_system* sys);
+/* info[0..5] = neq, coupled (r, c) flux blocks, source / Dudt terms, terms with per-vertex
+ * coefficients, Dirichlet entries, has Neumann constants. */
+int fvm_system_info(const fvm_system* sys, int64_t* info);
+/* Replaces fvm_eqs!(du, u, p, t) on an FVMSystem (src/equations/main_equations.jl:38-44 with
+ * the system methods of shape_functions.jl:12-19, triangle_contributions.jl:18-25,
+ * individual_flux_contributions.jl:35-51, boundary_edge_contributions.jl:15-75,
+ * source_contributions.jl:17-66).  u, du [npoints][neq]; flags FVM_PTR_*. */
+int fvm_system_rhs(fvm_system* sys, const double* u, double* du, double t, int32_t flags, void* stream);
+/* Replaces update_dirichlet_nodes! on an FVMSystem (src/equations/dirichlet.jl:54-61,73-86). */
+int fvm_system_dirichlet_apply(fvm_system* sys, double* u, double t, int32_t flags, void* stream);
+/* Tsit5 on the system with the Dirichlet callback after every step; u0 [npoints][neq] and
+ * out [nsave][npoints][neq] are host arrays in the caller's numbering. */
+int fvm_system_tsit5_solve(fvm_system* sys, const double* u0, const fvm_ode_options* opt, double* out,
+                           fvm_ode_stats* stats, void* stream);
+
 /* ---- batched instances (many parameter sets on one mesh) -------------------------------- */
 /* B instances of one linear problem that differ in their diffusion field D_b(x, y), the
  * batched counterpart of solving B FVMProblems (an EnsembleProblem over D in the reference).

@@ -420,6 +420,153 @@ def update_dirichlet_nodes(prob, u, t):
 
 
 # --------------------------------------------------------------------------------------
+# systems of equations: FVMSystem (src/problem.jl:190-365) and the system branches of
+# src/equations/*.jl.  State u is (N, npoints): u[var, i] is component var at node i.
+# --------------------------------------------------------------------------------------
+def call_system(f, x, y, t, *tuples):
+    """Evaluate a system closure f(x, y, t, T1, T2, ...) whose Ti are N-tuples of arrays (the
+    reference passes tuples for alpha, beta, gamma and u at quarter points, and the column
+    u[:, i] for sources and conditions).  Falls back to one call per point, with tuples of
+    floats, when the closure does not accept arrays.  Returns an array, or a tuple of arrays
+    for a tuple-valued closure (fluxes)."""
+    x = np.asarray(x, dtype=np.float64)
+    n = x.shape[0]
+    T = [tuple(np.broadcast_to(np.asarray(c, dtype=np.float64), (n,)) for c in tup) for tup in tuples]
+    try:
+        with np.errstate(all="ignore"):
+            out = f(x, np.broadcast_to(np.asarray(y, dtype=np.float64), (n,)), t, *T)
+        if isinstance(out, tuple):
+            return tuple(np.broadcast_to(np.asarray(o, dtype=np.float64), (n,)).copy() for o in out)
+        return np.broadcast_to(np.asarray(out, dtype=np.float64), (n,)).copy()
+    except (ValueError, TypeError, IndexError):
+        pass
+    yb = np.broadcast_to(np.asarray(y, dtype=np.float64), (n,))
+    res = None
+    for m in range(n):
+        r = f(float(x[m]), float(yb[m]), t, *[tuple(float(c[m]) for c in tup) for tup in T])
+        if res is None:
+            res = [np.empty(n) for _ in r] if isinstance(r, tuple) else np.empty(n)
+        if isinstance(r, tuple):
+            for c, v in enumerate(r):
+                res[c][m] = v
+        else:
+            res[m] = r
+    return tuple(res) if isinstance(res, list) else res
+
+
+class System:
+    """FVMSystem(prob1, ..., probN) restated (src/problem.jl:233-365).
+
+    Each component keeps its own conditions (merge_problem_conditions, :336-365: the
+    function list of component var is its problem's own, offset by cnum_fncs), flux function
+    q_var(x, y, t, alpha, beta, gamma) with N-tuples alpha, beta, gamma, and source
+    S_var(x, y, t, u) with u the N-tuple of the node's component values."""
+
+    def __init__(self, tri, conds, fluxes, sources=None, u0=None, t0=0.0, tf=1.0):
+        self.N = len(conds)
+        if not (len(fluxes) == self.N and (sources is None or len(sources) == self.N)):
+            raise AssertionError("one flux and one source per component")
+        self.tri = tri
+        self.geo = Geometry(tri.points, tri.triangles)
+        self.conds = list(conds)
+        self.fluxes = list(fluxes)
+        zero = lambda x, y, t, u: 0.0 * x  # noqa: E731
+        self.sources = [zero if s is None else s for s in (sources or [None] * self.N)]
+        self.u0 = None if u0 is None else np.asarray(u0, dtype=np.float64)
+        self.t0, self.tf = t0, tf
+        self.has_vertex = tri.has_vertex()
+        tabs = [c.vertex_tables(tri.num_points, self.has_vertex) for c in self.conds]
+        self.code = np.stack([c for c, _ in tabs])
+        self.fidx = np.stack([f for _, f in tabs])
+        self.neumann_fidx = np.stack([c.edge_tables(tri.boundary_edges) for c in self.conds])
+        be = tri.boundary_edges
+        self.bnd_tri, self.bnd_rot = self.geo.find_triangle(be[:, 0], be[:, 1], tri.boundary_adjacent)
+
+
+def _system_abg(s, u, i, j, k):
+    """get_shape_function_coefficients for a system (src/equations/shape_functions.jl:12-19)."""
+    N = u.shape[0]
+    a = tuple(s[:, 0] * u[l, i] + s[:, 1] * u[l, j] + s[:, 2] * u[l, k] for l in range(N))
+    b = tuple(s[:, 3] * u[l, i] + s[:, 4] * u[l, j] + s[:, 5] * u[l, k] for l in range(N))
+    g = tuple(s[:, 6] * u[l, i] + s[:, 7] * u[l, j] + s[:, 8] * u[l, k] for l in range(N))
+    return a, b, g
+
+
+def system_fvm_eqs(sys, u, t):
+    """serial_fvm_eqs! on an FVMSystem (src/equations/main_equations.jl:38-44) with the system
+    methods of each part:
+    triangles: get_flux for a system (individual_flux_contributions.jl:35-51) and update_du!
+    (triangle_contributions.jl:18-25); boundary edges: get_boundary_fluxes and
+    _get_boundary_fluxes for a system (boundary_edge_contributions.jl:15-39,50-59,67-75);
+    sources: get_source_contribution and fvm_eqs_single_source_contribution! for a system
+    (source_contributions.jl:17-30,49-66).  u and the result are (N, npoints)."""
+    u = np.asarray(u, dtype=np.float64)
+    N, n = u.shape
+    g, tri = sys.geo, sys.tri
+    T = g.triangles
+    du = np.zeros((N, n))
+    a, b, c = _system_abg(g.s, u, T[:, 0], T[:, 1], T[:, 2])
+    Q = np.empty((N, T.shape[0], 3))
+    for e in range(3):
+        x, y = g.mid[:, e, 0], g.mid[:, e, 1]
+        for var in range(N):
+            qx, qy = call_system(sys.fluxes[var], x, y, t, a, b, c)
+            Q[var, :, e] = (qx * g.nrm[:, e, 0] + qy * g.nrm[:, e, 1]) * g.length[:, e]
+    idx = np.stack([T[:, 0], T[:, 1], T[:, 2]], axis=1).ravel()
+    for var in range(N):
+        q = Q[var]
+        np.add.at(du[var], idx, np.stack([q[:, 2] - q[:, 0], q[:, 0] - q[:, 1], q[:, 1] - q[:, 2]], axis=1).ravel())
+    be = tri.boundary_edges
+    if be.shape[0]:
+        i, j = be[:, 0], be[:, 1]
+        Tk = T[sys.bnd_tri]
+        a, b, c = _system_abg(g.s[sys.bnd_tri], u, Tk[:, 0], Tk[:, 1], Tk[:, 2])
+        nx, ny, mix, miy, mjx, mjy, l = boundary_cv_components(tri.points, i, j)
+        for side, (mx, my) in enumerate(((mix, miy), (mjx, mjy))):
+            ushape = tuple(a[v] * mx + b[v] * my + c[v] for v in range(N))
+            for var in range(N):
+                qx, qy = call_system(sys.fluxes[var], mx, my, t, a, b, c)
+                qn = (qx * nx + qy * ny) * l
+                nf = sys.neumann_fidx[var]
+                for f in np.unique(nf[nf >= 0]):
+                    sel = nf == f
+                    qn[sel] = call_system(sys.conds[var].functions[f], mx[sel], my[sel], t,
+                                          tuple(us[sel] for us in ushape)) * l[sel]
+                np.add.at(du[var], be[:, side], -qn)
+    P = tri.points
+    out = du.copy()
+    ucols = tuple(u[v] for v in range(N))
+    for var in range(N):
+        code, fidx = sys.code[var], sys.fidx[var]
+        free = code == FREE
+        if np.any(free):
+            S = call_system(sys.sources[var], P[free, 0], P[free, 1], t, tuple(uc[free] for uc in ucols))
+            out[var, free] = du[var, free] / g.cv_volumes[free] + S
+        out[var, (code == DIRICHLET) | (code == NOT_A_VERTEX)] = 0.0
+        dd = code == DUDT
+        for f in np.unique(fidx[dd]):
+            sel = dd & (fidx == f)
+            out[var, sel] = call_system(sys.conds[var].functions[f], P[sel, 0], P[sel, 1], t,
+                                        tuple(uc[sel] for uc in ucols))
+    return out
+
+
+def system_update_dirichlet_nodes(sys, u, t):
+    """serial_update_dirichlet_nodes! for a system (src/equations/dirichlet.jl:11-18,28-35,54-61):
+    component by component, in place, each node's value from its condition at the node's
+    current column u[:, i] (so a later component sees the earlier components' new values)."""
+    u = np.array(u, dtype=np.float64)
+    P = sys.tri.points
+    for var in range(sys.N):
+        dn = sys.conds[var].dirichlet_nodes
+        for f in set(dn.values()):
+            nodes = np.array([i for i, g in dn.items() if g == f], dtype=np.int64)
+            u[var, nodes] = call_system(sys.conds[var].functions[f], P[nodes, 0], P[nodes, 1], t,
+                                        tuple(u[v, nodes] for v in range(sys.N)))
+    return u
+
+
+# --------------------------------------------------------------------------------------
 # linear templates: src/specific_problems/*.jl, assembled sparse (not dense)
 # --------------------------------------------------------------------------------------
 def _template_A_entries(tri, geo, conds, D, rows, cols, vals):

@@ -160,21 +160,26 @@ def test_dirichlet_update(gpu_lib):
 
 
 def test_unsupported_forms_are_rejected(gpu_lib):
+    """Closures are classified when the problem is first used (as the reference evaluates them
+    only when it solves); an unsupported one raises there, on every use."""
     import fvmgpu as F
 
     spec = readme_diffusion(10)
     spec.D = lambda x, y, t, u, p: 1.0 + np.exp(u)
+    prob = api_problem(spec)
     with pytest.raises(F.UnsupportedFormError):
-        api_problem(spec)
+        prob.handle
+    with pytest.raises(F.UnsupportedFormError):
+        F.fvm_eqs(np.zeros_like(spec.u0), spec.u0, prob, 0.0)
     spec = readme_diffusion(10)
     spec.D = lambda x, y, t, u, p: 1.0 + t + 0.0 * x
     with pytest.raises(F.UnsupportedFormError):
-        api_problem(spec)
+        F.solve(api_problem(spec), F.Tsit5())
     spec = readme_diffusion(10)
     spec.flux = lambda x, y, t, a, b, g, p: (-a + 0.1 * g, -b)
     spec.D = None
     with pytest.raises(F.UnsupportedFormError):
-        api_problem(spec)
+        api_problem(spec).handle
 
 
 def test_full_size_properties(gpu_lib):

@@ -1,0 +1,182 @@
+"""Pins the oracle's FVMSystem restatement (oracle/fvm_oracle.py: System, system_fvm_eqs,
+system_update_dirichlet_nodes) and tests the host classification of system closures
+(fvmgpu/forms.py).  CPU only.
+
+Pins, paths relative to the reference project root:
+* a system of one component equals the single-equation oracle, which the reference's own
+  known-answer tests pin (tests/test_oracle_pins.py);
+* the reference's two-component diffusion system (test/test_functions.jl:318-334) solves like
+  the single diffusion problem it duplicates (test/equations.jl:106-121);
+* the reference's coupled system with an exact solution (test/problem.jl:170-205, the
+  Brusselator-type tutorial docs/src/literate_tutorials/reaction_diffusion_brusselator_system_of_pdes.jl):
+  the RHS at the exact solution converges to its time derivative at second order.
+"""
+import numpy as np
+import pytest
+
+import fvm_oracle as O
+from fvmgpu import forms
+from fvmgpu.meshes import triangulate_rectangle
+from problems import mixed_annulus, oracle_problem, readme_diffusion, rhs_term_scale
+
+
+def _tuple_conditions(spec):
+    """The spec's conditions with closures of the component tuple u = (u_1,)."""
+    wrap = lambda f, p: (lambda x, y, t, u: f(x, y, t, u[0], p))  # noqa: E731
+    return O.Conditions(spec.tri, [wrap(f, p) for f, p in zip(spec.bc_fns, spec.bc_params)], list(spec.bc_types),
+                        [wrap(f, p) for f, p in zip(spec.ic_fns, spec.ic_params)], spec.dirichlet_nodes,
+                        spec.dudt_nodes)
+
+
+def _one_component_system(spec):
+    D, S = spec.D, spec.S
+
+    def q(x, y, t, a, b, g):
+        u = a[0] * x + b[0] * y + g[0]
+        d = D(x, y, t, u, spec.Dp)
+        return (-d * a[0], -d * b[0])
+
+    src = (lambda x, y, t, u: S(x, y, t, u[0], spec.Sp)) if S else None
+    return O.System(spec.tri, [_tuple_conditions(spec)], [q], [src], u0=spec.u0[None, :])
+
+
+def test_system_of_one_component_equals_single_equation_oracle():
+    spec = mixed_annulus()
+    prob = oracle_problem(spec)
+    sys = _one_component_system(spec)
+    rng = np.random.default_rng(3)
+    for t in (0.0, 0.05):
+        u = rng.standard_normal(spec.tri.num_points)
+        ref = O.fvm_eqs(prob, u, t)
+        got = O.system_fvm_eqs(sys, u[None, :], t)[0]
+        scale = rhs_term_scale(prob, u, t)
+        assert np.max(np.abs(got - ref) / (np.abs(ref) + scale + 1e-300)) < 1e-13
+        # the looped restatement of the single equation agrees as well
+        assert np.max(np.abs(O.fvm_eqs_loop(prob, u, t) - got) / (np.abs(ref) + scale + 1e-300)) < 1e-13
+    ud = O.system_update_dirichlet_nodes(sys, u[None, :], 0.1)[0]
+    assert np.array_equal(ud, O.update_dirichlet_nodes(prob, u, 0.1))
+
+
+def reference_diffusion_system():
+    """example_diffusion_problem_system (test/test_functions.jl:318-334): two copies of the 25 x 25
+    diffusion problem with fluxes (-alpha[c]/9, -beta[c]/9)."""
+    spec = readme_diffusion(25)
+    bc = lambda x, y, t, u: 0.0 * u[0] * u[1]  # noqa: E731
+    conds = [O.Conditions(spec.tri, [bc], ["Dirichlet"]) for _ in range(2)]
+    q1 = lambda x, y, t, a, b, g: (-a[0] / 9, -b[0] / 9)  # noqa: E731
+    q2 = lambda x, y, t, a, b, g: (-a[1] / 9, -b[1] / 9)  # noqa: E731
+    sys = O.System(spec.tri, conds, [q1, q2], u0=np.stack([spec.u0, spec.u0]), tf=0.5)
+    return sys, spec
+
+
+def test_reference_diffusion_system_matches_single_problem():
+    sys, spec = reference_diffusion_system()
+    prob = oracle_problem(spec)
+    rng = np.random.default_rng(4)
+    u = rng.standard_normal((2, spec.tri.num_points))
+    du = O.system_fvm_eqs(sys, u, 0.0)
+    for c in range(2):
+        ref = O.fvm_eqs(prob, u[c], 0.0)
+        assert np.linalg.norm(du[c] - ref) <= 1e-13 * np.linalg.norm(ref)
+    # the solutions agree (test/equations.jl:121: every component equals the single problem)
+    ts = np.linspace(0.0, 0.05, 6)
+    f = lambda v, t: O.system_fvm_eqs(sys, v, t)  # noqa: E731
+    cb = lambda v, t: O.system_update_dirichlet_nodes(sys, v, t)  # noqa: E731
+    sol, st = O.tsit5_solve(f, sys.u0, 0.0, 0.05, ts, callback=cb)
+    ref, _ = O.tsit5_solve(lambda v, t: O.fvm_eqs(prob, v, t), spec.u0, 0.0, 0.05, ts,
+                           callback=lambda v, t: O.update_dirichlet_nodes(prob, v, t))
+    for c in range(2):
+        assert np.max(np.abs(sol[:, c] - ref)) <= 1e-3 * np.max(np.abs(ref))
+
+
+def brusselator_system(n):
+    """The coupled system of test/problem.jl:170-205 with its exact solution
+    Phi = exp(-x - y - t/2), Psi = exp(x + y + t/2)."""
+    tri = triangulate_rectangle(0.0, 1.0, 0.0, 1.0, n, n, single_boundary=False)
+    phi_bc = [lambda x, y, t, u: -1 / 4 * np.exp(-x - t / 2), lambda x, y, t, u: 1 / 4 * np.exp(-1 - y - t / 2),
+              lambda x, y, t, u: np.exp(-1 - x - t / 2), lambda x, y, t, u: -1 / 4 * np.exp(-y - t / 2)]
+    psi_bc = [lambda x, y, t, u: np.exp(x + t / 2), lambda x, y, t, u: -1 / 4 * np.exp(1 + y + t / 2),
+              lambda x, y, t, u: -1 / 4 * np.exp(1 + x + t / 2), lambda x, y, t, u: np.exp(y + t / 2)]
+    conds = [O.Conditions(tri, phi_bc, ["Neumann", "Neumann", "Dirichlet", "Neumann"]),
+             O.Conditions(tri, psi_bc, ["Dirichlet", "Neumann", "Neumann", "Dirichlet"])]
+    fluxes = [lambda x, y, t, a, b, g: (-a[0] / 4, -b[0] / 4), lambda x, y, t, a, b, g: (-a[1] / 4, -b[1] / 4)]
+    sources = [lambda x, y, t, u: u[0] ** 2 * u[1] - 2 * u[0], lambda x, y, t, u: -u[0] ** 2 * u[1] + u[0]]
+    P = tri.points
+    u0 = np.stack([np.exp(-P[:, 0] - P[:, 1]), np.exp(P[:, 0] + P[:, 1])])
+    return O.System(tri, conds, fluxes, sources, u0=u0, tf=5.0)
+
+
+def test_brusselator_rhs_converges_to_exact_time_derivative():
+    errs = []
+    for n in (17, 33):
+        sys = brusselator_system(n)
+        du = O.system_fvm_eqs(sys, sys.u0, 0.0)
+        exact = np.stack([-sys.u0[0] / 2, sys.u0[1] / 2])
+        on_boundary = np.zeros(sys.tri.num_points, dtype=bool)
+        on_boundary[sys.tri.boundary_edges.ravel()] = True
+        inner = ~on_boundary
+        errs.append(max(np.max(np.abs(du[c, inner] - exact[c, inner]) / np.abs(exact[c, inner])) for c in range(2)))
+        # Dirichlet nodes carry du = 0; the update writes the exact boundary values
+        ud = O.system_update_dirichlet_nodes(sys, np.zeros_like(sys.u0), 0.0)
+        for c in range(2):
+            nodes = np.array(sorted(sys.conds[c].dirichlet_nodes))
+            assert np.allclose(ud[c, nodes], sys.u0[c, nodes], rtol=1e-14)
+            assert np.all(du[c, nodes] == 0.0)
+    assert errs[0] < 1e-2
+    assert errs[0] / errs[1] > 3.5  # second order on the interior nodes
+
+
+# ---- host classification of system closures ------------------------------------------------
+def test_monomial_basis():
+    for N, M in ((1, 4), (2, 10), (3, 20), (4, 35), (8, 165)):
+        e = forms.monomials(N)
+        assert e.shape == (M, N) and np.all(e.sum(axis=1) <= 3)
+        assert len({tuple(r) for r in e}) == M and not np.any(e[0])
+
+
+def test_classify_system_sources():
+    x = np.linspace(-1, 1, 40)
+    y = np.linspace(0, 2, 40)
+    b, d = 0.04, 0.1
+    e, c = forms.classify_system_poly(lambda x, y, t, u: b * (1 - u[0]) - u[0] * u[1] ** 2, x, y, 0.0, 2, "u_S")
+    got = {tuple(k): c[:, m] for m, k in enumerate(e)}
+    assert set(got) == {(0, 0), (1, 0), (1, 2)}
+    assert np.allclose(got[(0, 0)], b, rtol=1e-13) and np.allclose(got[(1, 0)], -b, rtol=1e-13)
+    assert np.allclose(got[(1, 2)], -1, rtol=1e-13)
+    e, c = forms.classify_system_poly(lambda x, y, t, u: -d * u[1] + u[0] * u[1] ** 2, x, y, 0.0, 2, "v_S")
+    assert {tuple(k) for k in e} == {(0, 1), (1, 2)}
+    e, c = forms.classify_system_poly(lambda x, y, t, u: x * u[0] ** 2 * u[1] - 2 * u[0] + y, x, y, 0.0, 2, "S")
+    got = {tuple(k): c[:, m] for m, k in enumerate(e)}
+    assert np.allclose(got[(2, 1)], x, atol=1e-13) and np.allclose(got[(0, 0)], y, atol=1e-13)
+    e, c = forms.classify_system_poly(lambda x, y, t, u: 0.0 * x, x, y, 0.0, 3, "zero")
+    assert e.shape == (0, 3) and c.shape == (40, 0)
+    # a closure that destructures the tuple, called per point when it does not take arrays
+    e, c = forms.classify_system_poly(lambda x, y, t, uv: (uv[0] if x < 0 else 2.0) * uv[1], x, y, 0.0, 2, "branch")
+    got = {tuple(k): c[:, m] for m, k in enumerate(e)}
+    assert np.allclose(got[(1, 1)], np.where(x < 0, 1.0, 0.0), atol=1e-12)
+    assert np.allclose(got[(0, 1)], np.where(x < 0, 0.0, 2.0), atol=1e-12)
+    for bad in (lambda x, y, t, u: np.exp(u[0]), lambda x, y, t, u: u[0] ** 4, lambda x, y, t, u: t * u[1],
+                lambda x, y, t, u: u[0] * u[1] * u[1] * u[0], lambda x, y, t, u: 1 / (x - x) + u[0]):
+        with pytest.raises(forms.UnsupportedFormError):
+            forms.classify_system_poly(bad, x, y, 0.0, 2, "bad")
+    with pytest.raises(forms.UnsupportedFormError):  # Neumann values must be affine
+        forms.classify_system_poly(lambda x, y, t, u: u[0] * u[1], x, y, 0.0, 2, "Neumann", max_degree=1)
+    with pytest.raises(forms.UnsupportedFormError):  # Dirichlet values are functions of (x, y)
+        forms.classify_system_poly(lambda x, y, t, u: x + u[0], x, y, 0.0, 2, "Dirichlet", max_degree=0)
+
+
+def test_classify_system_fluxes():
+    x = np.linspace(-1, 1, 30)
+    y = np.linspace(0, 1, 30)
+    D = forms.classify_system_flux(lambda x, y, t, a, b, g: (-a[1] * (1 + x), -b[1] * (1 + x)), x, y, 0.0, 2)
+    assert np.allclose(D[1], 1 + x, rtol=1e-15) and not np.any(D[0])
+    q = lambda x, y, t, a, b, g: (-(2 * a[0] - 0.5 * y * a[2]), -(2 * b[0] - 0.5 * y * b[2]))  # noqa: E731
+    D = forms.classify_system_flux(q, x, y, 0.0, 3)
+    assert np.allclose(D[0], 2.0) and np.allclose(D[2], -0.5 * y) and not np.any(D[1])
+    for bad in (lambda x, y, t, a, b, g: (-a[0] * (a[0] * x + g[0]), -b[0]),  # D(u): nonlinear
+                lambda x, y, t, a, b, g: (-a[0], -2 * b[0]),                  # anisotropic
+                lambda x, y, t, a, b, g: (-a[0] + 0.1, -b[0]),                # advection-like constant
+                lambda x, y, t, a, b, g: (-a[0] * (1 + t), -b[0] * (1 + t)),  # time dependent
+                lambda x, y, t, a, b, g: -a[0]):                              # not a pair
+        with pytest.raises(forms.UnsupportedFormError):
+            forms.classify_system_flux(bad, x, y, 0.0, 2)
