@@ -17,12 +17,15 @@ namespace fvm {
 constexpr int kSysMaxEq = FVM_SYSTEM_MAX_EQ;
 constexpr int kSysMaxTerms = FVM_SYSTEM_MAX_TERMS;
 
-// Terms of the polynomial epilogue: term t adds coef_t * prod_c u_c^e_tc to component var_t on
-// the rows whose mask bit var_t is set.  exps packs e_tc in 2 bits per component.
+// Terms of the polynomial epilogue, grouped by monomial: monomial m is u_{f_m0} * ... *
+// u_{f_m(nf_m - 1)} (degree nf_m <= 3, written as its factors) and is evaluated once per row;
+// term[m][r] >= 0 adds coef * monomial to component r on the rows whose mask bit r is set.
 struct SysTerms {
-    int32_t n = 0;
-    uint32_t exps[kSysMaxTerms];
-    int32_t var[kSysMaxTerms];
+    int32_t n = 0;      // terms
+    int32_t nmono = 0;  // distinct monomials
+    uint8_t nf[kSysMaxTerms];
+    uint8_t f[kSysMaxTerms][3];
+    int16_t term[kSysMaxTerms][kSysMaxEq];
     int32_t vary[kSysMaxTerms];  // row of the per-vertex coefficient table, or -1 (coef is uniform)
     double coef[kSysMaxTerms];
 };
@@ -39,11 +42,44 @@ struct SysArgs {
     const double* b;      // [nrows][N] or null (Neumann constants)
     const uint8_t* mask;  // [nrows]: bit r set when component r's row is FREE or DUDT
     const double* vcoef;  // [nvary][nrows]
+    uint32_t cmask;       // shared form: bit c set when some block reads component c
+    double dmat[kSysMaxEq * kSysMaxEq];  // shared form: block (r, c) is dmat[r*N + c] times the one operator
 };
 
-// One warp per 32-row slice, one lane per row.  Each slot gathers the neighbour's N component
-// values (contiguous) once and feeds every stored block of the row.
+// The N component values of point c: 16-byte loads when N is even and u is 16-byte aligned.
+template <int N, bool VEC>
+__device__ __forceinline__ void load_point(const double* __restrict__ u, int64_t c, double (&out)[N]) {
+    if constexpr (VEC && N % 2 == 0) {
+        const double2* p = reinterpret_cast<const double2*>(u + c * N);
+#pragma unroll
+        for (int h = 0; h < N / 2; ++h) {
+            const double2 t = __ldg(p + h);
+            out[2 * h] = t.x;
+            out[2 * h + 1] = t.y;
+        }
+    } else {
+#pragma unroll
+        for (int q = 0; q < N; ++q) out[q] = __ldg(&u[c * N + q]);
+    }
+}
+
+// ui[f] for a warp-uniform runtime f: a chain of selects, no FP64 instruction and no local memory.
 template <int N>
+__device__ __forceinline__ double pick(const double (&ui)[N], int f) {
+    double v = ui[0];
+#pragma unroll
+    for (int q = 1; q < N; ++q) v = f == q ? ui[q] : v;
+    return v;
+}
+
+// One warp per 32-row slice, one lane per row, slices grid-strided.  For a compile-time
+// maximum width MAXW the slot loop is unrolled in three phases -- every column load, then
+// every gather of the neighbours' N component values, then the FMAs of each stored block in
+// slot order -- so a warp waits for one DRAM round trip and one gather round trip per slice
+// instead of two per slot.  MAXW = 0 keeps a rolled loop for wide rows or many components.
+// SH (shared form): the blocks are constant multiples dmat[r][c] of one stored operator G, so
+// each slot reads one value; the row sums S_c = sum_k G_k u_c(col_k) are combined at the end.
+template <int N, int MAXW, bool VEC, bool SH>
 __global__ void __launch_bounds__(256) system_rhs_kernel(const SysArgs a, const SysTerms tm) {
     const int lane = threadIdx.x & 31;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -53,50 +89,124 @@ __global__ void __launch_bounds__(256) system_rhs_kernel(const SysArgs a, const 
         double acc[N];
 #pragma unroll
         for (int r = 0; r < N; ++r) acc[r] = 0.0;
-#pragma unroll 2
-        for (int k = 0; k < w; ++k) {
-            const int64_t slot = base + (int64_t)k * 32;
-            const int64_t c = __ldg(&a.col[slot]);
-            double uc[N];
+        if constexpr (MAXW > 0) {
+            int32_t c[MAXW];
 #pragma unroll
-            for (int q = 0; q < N; ++q) uc[q] = __ldg(&a.u[c * N + q]);
-            const double* v = a.val + slot;
+            for (int k = 0; k < MAXW; ++k)
+                if (k < w) c[k] = __ldg(&a.col[base + (int64_t)k * 32]);
+            double uc[MAXW][N];
+#pragma unroll
+            for (int k = 0; k < MAXW; ++k)
+                if (k < w) load_point<N, VEC>(a.u, c[k], uc[k]);
+            const double* v = a.val + base;
+            if constexpr (SH) {
+                double sc[N];
+#pragma unroll
+                for (int q = 0; q < N; ++q) sc[q] = 0.0;
+#pragma unroll
+                for (int k = 0; k < MAXW; ++k)
+                    if (k < w) {
+                        const double g = __ldg(&v[(int64_t)k * 32]);
+#pragma unroll
+                        for (int q = 0; q < N; ++q)
+                            if ((a.cmask >> q) & 1u) sc[q] = fma(g, uc[k][q], sc[q]);
+                    }
+#pragma unroll
+                for (int r = 0; r < N; ++r)
+#pragma unroll
+                    for (int q = 0; q < N; ++q)
+                        if ((a.blocks >> (r * N + q)) & 1ull) acc[r] = fma(a.dmat[r * N + q], sc[q], acc[r]);
+            } else {
+#pragma unroll
+                for (int r = 0; r < N; ++r)
+#pragma unroll
+                    for (int q = 0; q < N; ++q)
+                        if ((a.blocks >> (r * N + q)) & 1ull) {
+#pragma unroll
+                            for (int k = 0; k < MAXW; ++k)
+                                if (k < w) acc[r] = fma(__ldg(&v[(int64_t)k * 32]), uc[k][q], acc[r]);
+                            v += a.nslots;
+                        }
+            }
+        } else if constexpr (SH) {
+            double sc[N];
+#pragma unroll
+            for (int q = 0; q < N; ++q) sc[q] = 0.0;
+#pragma unroll 2
+            for (int k = 0; k < w; ++k) {
+                const int64_t slot = base + (int64_t)k * 32;
+                double uc[N];
+                load_point<N, VEC>(a.u, __ldg(&a.col[slot]), uc);
+                const double g = __ldg(&a.val[slot]);
+#pragma unroll
+                for (int q = 0; q < N; ++q)
+                    if ((a.cmask >> q) & 1u) sc[q] = fma(g, uc[q], sc[q]);
+            }
 #pragma unroll
             for (int r = 0; r < N; ++r)
 #pragma unroll
                 for (int q = 0; q < N; ++q)
-                    if ((a.blocks >> (r * N + q)) & 1ull) {
-                        acc[r] = fma(__ldg(v), uc[q], acc[r]);
-                        v += a.nslots;
-                    }
+                    if ((a.blocks >> (r * N + q)) & 1ull) acc[r] = fma(a.dmat[r * N + q], sc[q], acc[r]);
+        } else {
+#pragma unroll 2
+            for (int k = 0; k < w; ++k) {
+                const int64_t slot = base + (int64_t)k * 32;
+                double uc[N];
+                load_point<N, VEC>(a.u, __ldg(&a.col[slot]), uc);
+                const double* v = a.val + slot;
+#pragma unroll
+                for (int r = 0; r < N; ++r)
+#pragma unroll
+                    for (int q = 0; q < N; ++q)
+                        if ((a.blocks >> (r * N + q)) & 1ull) {
+                            acc[r] = fma(__ldg(v), uc[q], acc[r]);
+                            v += a.nslots;
+                        }
+            }
         }
         const int64_t row = s * 32 + lane;
         if (row >= a.nrows) continue;
         double ui[N];
-#pragma unroll
-        for (int q = 0; q < N; ++q) ui[q] = a.u[row * N + q];
+        load_point<N, VEC>(a.u, row, ui);
         if (a.b) {
 #pragma unroll
             for (int r = 0; r < N; ++r) acc[r] += a.b[row * N + r];
         }
+        // the source / Dudt polynomials.  Loop bounds and branches are warp-uniform, each
+        // distinct monomial is formed once (degree - 1 multiplications) and each term is one FMA
+        // into the row's running sum, which the row's mask then keeps or drops: FP64 is the
+        // scarce pipe on this GPU.
         const unsigned m = a.mask[row];
-        for (int t = 0; t < tm.n; ++t) {
-            double x = tm.vary[t] < 0 ? tm.coef[t] : __ldg(&a.vcoef[(int64_t)tm.vary[t] * a.nrows + row]);
-            const uint32_t e = tm.exps[t];
+        double p[N];
 #pragma unroll
-            for (int q = 0; q < N; ++q) {
-                const uint32_t eq = (e >> (2 * q)) & 3u;
-                if (eq >= 1) x *= ui[q];
-                if (eq >= 2) x *= ui[q];
-                if (eq >= 3) x *= ui[q];
+        for (int r = 0; r < N; ++r) p[r] = acc[r];
+        for (int mo = 0; mo < tm.nmono; ++mo) {
+            const int nf = tm.nf[mo];
+            double x = 1.0;
+            if (nf > 0) {
+                x = pick<N>(ui, tm.f[mo][0]);
+                for (int k = 1; k < nf; ++k) x *= pick<N>(ui, tm.f[mo][k]);
             }
-            const int rt = tm.var[t];
 #pragma unroll
-            for (int r = 0; r < N; ++r)
-                if (r == rt && ((m >> r) & 1u)) acc[r] += x;
+            for (int r = 0; r < N; ++r) {
+                const int t = tm.term[mo][r];
+                if (t >= 0) {
+                    const double c = tm.vary[t] < 0 ? tm.coef[t] : __ldg(&a.vcoef[(int64_t)tm.vary[t] * a.nrows + row]);
+                    p[r] = fma(c, x, p[r]);
+                }
+            }
         }
 #pragma unroll
-        for (int r = 0; r < N; ++r) a.du[row * N + r] = acc[r];
+        for (int r = 0; r < N; ++r)
+            if ((m >> r) & 1u) acc[r] = p[r];
+        if constexpr (VEC && N % 2 == 0) {
+            double2* o = reinterpret_cast<double2*>(a.du + row * N);
+#pragma unroll
+            for (int h = 0; h < N / 2; ++h) o[h] = make_double2(acc[2 * h], acc[2 * h + 1]);
+        } else {
+#pragma unroll
+            for (int r = 0; r < N; ++r) a.du[row * N + r] = acc[r];
+        }
     }
 }
 
@@ -110,6 +220,9 @@ struct fvm_system {
     int nblocks = 0;
     uint64_t blocks = 0;
     SysTerms terms;
+    bool shared = false;   // every block is dmat[r][c] times the one stored operator
+    uint32_t cmask = 0;
+    double dmat[kSysMaxEq * kSysMaxEq] = {};
     int nvary = 0;
     bool has_b = false;
     int64_t ndir = 0;
@@ -125,6 +238,35 @@ struct fvm_system {
 };
 
 namespace fvm {
+
+// unrolled width for N components and a pattern whose widest slice has maxw slots (0: rolled):
+// exact widths for the common vertex degrees (no predicated-off slot costs an FP64 issue), and
+// at most 32 gathered values per lane in registers
+static int system_bucket(int N, int maxw) {
+    for (int w : {4, 6, 7, 8, 12, 16})
+        if (maxw <= w) return w * N <= 32 ? w : 0;
+    return 0;
+}
+
+template <int N, int MAXW, bool VEC, bool SH>
+static void launch_system_shape(const SysArgs& a, const SysTerms& tm, int64_t nslices, cudaStream_t s) {
+    // 8 warps per block; the grid covers every slice at most once, capped at 8 blocks per SM
+    const unsigned grid = (unsigned)std::min<int64_t>((nslices + 7) / 8, 152 * 8);
+    system_rhs_kernel<N, MAXW, VEC, SH><<<grid, 256, 0, s>>>(a, tm);
+}
+
+template <int N, bool VEC, bool SH>
+static void launch_system_vec(const SysArgs& a, const SysTerms& tm, int64_t nslices, int maxw, cudaStream_t s) {
+    switch (system_bucket(N, maxw)) {
+        case 4: launch_system_shape<N, 4, VEC, SH>(a, tm, nslices, s); break;
+        case 6: if constexpr (N <= 5) launch_system_shape<N, 6, VEC, SH>(a, tm, nslices, s); break;
+        case 7: if constexpr (N <= 4) launch_system_shape<N, 7, VEC, SH>(a, tm, nslices, s); break;
+        case 8: if constexpr (N <= 4) launch_system_shape<N, 8, VEC, SH>(a, tm, nslices, s); break;
+        case 12: if constexpr (N <= 2) launch_system_shape<N, 12, VEC, SH>(a, tm, nslices, s); break;
+        case 16: if constexpr (N <= 2) launch_system_shape<N, 16, VEC, SH>(a, tm, nslices, s); break;
+        default: launch_system_shape<N, 0, VEC, SH>(a, tm, nslices, s); break;
+    }
+}
 
 template <int N>
 static void launch_system(const fvm_system* S, const double* u, double* du, cudaStream_t s) {
@@ -142,10 +284,21 @@ static void launch_system(const fvm_system* S, const double* u, double* du, cuda
               du,
               S->has_b ? S->d_b.as<double>() : nullptr,
               S->d_mask.as<uint8_t>(),
-              S->nvary ? S->d_vcoef.as<double>() : nullptr};
-    // 8 warps per block, at most 8 resident blocks on each of the 152 SMs; slices are grid-strided
-    const unsigned grid = (unsigned)std::min<int64_t>((p.nslices + 7) / 8, 152 * 8);
-    system_rhs_kernel<N><<<grid, 256, 0, s>>>(a, S->terms);
+              S->nvary ? S->d_vcoef.as<double>() : nullptr,
+              S->cmask,
+              {}};
+    std::copy(S->dmat, S->dmat + kSysMaxEq * kSysMaxEq, a.dmat);
+    const bool vec = N % 2 == 0 && ((uintptr_t)u % 16) == 0 && ((uintptr_t)du % 16) == 0;
+    if (S->shared) {
+        if (vec)
+            launch_system_vec<N, true, true>(a, S->terms, p.nslices, p.maxw, s);
+        else
+            launch_system_vec<N, false, true>(a, S->terms, p.nslices, p.maxw, s);
+    } else if (vec) {
+        launch_system_vec<N, true, false>(a, S->terms, p.nslices, p.maxw, s);
+    } else {
+        launch_system_vec<N, false, false>(a, S->terms, p.nslices, p.maxw, s);
+    }
 }
 
 static void system_rhs_internal(const fvm_system* S, const double* u, double* du, cudaStream_t s) {
@@ -215,48 +368,127 @@ static void create_system(fvm_mesh* m, const fvm_system_desc* d, fvm_system** ou
     const SellPattern& pat = m->pat;
     const int64_t q0 = 3 * nt;
 
-    // coupled flux blocks K_rc, and the Neumann constants of each component (from the (r, r) pass)
-    std::vector<double> vals, B((size_t)np * N, 0.0);
-    for (int r = 0; r < N; ++r)
-        for (int c = 0; c < N; ++c) {
-            fvm_problem tp;  // host-side view of component r's flux through u_c
-            tp.mesh = m;
-            tp.code.assign(d->vertex_code + r * np, d->vertex_code + (r + 1) * np);
-            tp.bneu.assign(nbe, 0);
-            for (int64_t e = 0; e < nbe; ++e) tp.bneu[e] = d->bedge_neumann[r * nbe + e] ? 1 : 0;
-            tp.dif_deg = 0;
-            const size_t blk = (size_t)r * N + c;
-            if (d->dual_edge_D) tp.dualD.assign(d->dual_edge_D + blk * 3 * nt, d->dual_edge_D + (blk + 1) * 3 * nt);
-            if (d->quarter_D) tp.quarterD.assign(d->quarter_D + blk * 2 * nbe, d->quarter_D + (blk + 1) * 2 * nbe);
-            tp.neu_deg = 1;
-            if (d->quarter_neumann) {
-                tp.quarterN.assign((size_t)2 * nbe * 2, 0.0);
-                for (int64_t qp = 0; qp < 2 * nbe; ++qp) {
-                    const double* nq = d->quarter_neumann + ((size_t)r * 2 * nbe + qp) * (1 + N);
-                    tp.quarterN[2 * qp] = c == r ? nq[0] : 0.0;
-                    tp.quarterN[2 * qp + 1] = nq[1 + c];
+    // One pass of the linear-term visitor over component r's conditions: the operator of D (dual
+    // samples D3, quarter samples D2; null = 0) plus the Neumann terms n0 + n1 u(m) of the
+    // per-quarter-point pairs NQ ([2*nbe][2], null = none), on the pattern; b gets the constants.
+    auto visit = [&](int r, const double* D3, const double* D2, const std::vector<double>* NQ, std::vector<double>& E,
+                     std::vector<double>& b) {
+        fvm_problem tp;  // host-side view of component r
+        tp.mesh = m;
+        tp.code.assign(d->vertex_code + r * np, d->vertex_code + (r + 1) * np);
+        tp.bneu.assign(nbe, 0);
+        for (int64_t e = 0; e < nbe; ++e) tp.bneu[e] = d->bedge_neumann[r * nbe + e] ? 1 : 0;
+        tp.dif_deg = 0;
+        tp.neu_deg = 1;
+        if (NQ) tp.quarterN = *NQ;
+        E.assign(pat.nslots, 0.0);
+        std::vector<double> qv, rs;
+        fvm_visit_linear_terms(
+            &tp,
+            [&](int32_t row, int32_t col, double coef, int64_t didx, bool) {
+                double v = coef;
+                if (didx >= 0) v *= didx < q0 ? (D3 ? D3[didx] : 0.0) : (D2 ? D2[didx - q0] : 0.0);
+                E[pat.find(m->iperm[row], m->iperm[col])] += v;
+            },
+            b, qv, rs);
+    };
+    // per-quarter-point (n0, n_c) pairs of component r for the block (r, c); n0 only on the diagonal
+    auto neumann_pairs = [&](int r, int c, bool with_n0, bool with_n1) {
+        std::vector<double> nq((size_t)2 * nbe * 2, 0.0);
+        for (int64_t qp = 0; qp < 2 * nbe; ++qp) {
+            const double* a = d->quarter_neumann + ((size_t)r * 2 * nbe + qp) * (1 + N);
+            nq[2 * qp] = with_n0 ? a[0] : 0.0;
+            nq[2 * qp + 1] = with_n1 ? a[1 + c] : 0.0;
+        }
+        return nq;
+    };
+    const double* DD = d->dual_edge_D;
+    const double* DQ = d->quarter_D;
+
+    // Shared form: when every component has the same conditions, no Neumann value depends on u and
+    // every block's D is one constant d_rc at all its samples, block (r, c) is d_rc times the
+    // operator G of those conditions with D = 1, and G is stored once.
+    bool shared = true;
+    for (int r = 1; r < N && shared; ++r)
+        shared = std::equal(d->vertex_code + r * np, d->vertex_code + (r + 1) * np, d->vertex_code) &&
+                 (nbe == 0 || std::equal(d->bedge_neumann + r * nbe, d->bedge_neumann + (r + 1) * nbe, d->bedge_neumann));
+    if (shared && d->quarter_neumann)
+        for (int r = 0; r < N && shared; ++r)
+            for (int64_t qp = 0; qp < 2 * nbe && shared; ++qp)
+                for (int c = 0; c < N && shared; ++c)
+                    shared = d->quarter_neumann[((size_t)r * 2 * nbe + qp) * (1 + N) + 1 + c] == 0.0;
+    std::vector<double> dconst((size_t)N * N, 0.0);
+    for (size_t blk = 0; blk < (size_t)N * N && shared; ++blk) {
+        bool first = true;
+        double v0 = 0.0;
+        auto scan = [&](const double* a, int64_t n) {
+            for (int64_t i = 0; i < n && shared; ++i) {
+                if (first) {
+                    v0 = a[i];
+                    first = false;
+                } else if (a[i] != v0) {
+                    shared = false;
                 }
             }
-            auto Dval = [&](int64_t idx) -> double {
-                if (idx < q0) return tp.dualD.empty() ? 0.0 : tp.dualD[idx];
-                return tp.quarterD.empty() ? 0.0 : tp.quarterD[idx - q0];
-            };
-            std::vector<double> E(pat.nslots, 0.0), b, qv, rs;
-            fvm_visit_linear_terms(
-                &tp,
-                [&](int32_t row, int32_t col, double coef, int64_t didx, bool) {
-                    const double v = didx >= 0 ? coef * Dval(didx) : coef;
-                    E[pat.find(m->iperm[row], m->iperm[col])] += v;
-                },
-                b, qv, rs);
-            if (c == r)
+        };
+        if (DD) scan(DD + blk * 3 * nt, 3 * nt);
+        if (DQ) scan(DQ + blk * 2 * nbe, 2 * nbe);
+        dconst[blk] = (DD || DQ) ? v0 : 0.0;
+    }
+
+    // The shared form reads one value per slot but spends N FP64 FMAs per slot and one per block
+    // and row; the stored blocks spend one per block and slot.  FP64 issue, not DRAM, bounds
+    // these kernels on this GPU, so the shared form is kept only when it issues fewer.
+    if (shared) {
+        int nb = 0;
+        uint32_t cols = 0;
+        for (int r = 0; r < N; ++r)
+            for (int c = 0; c < N; ++c)
+                if (dconst[(size_t)r * N + c] != 0.0) {
+                    ++nb;
+                    cols |= 1u << c;
+                }
+        const double w = pat.nrows ? (double)pat.nslots / (double)pat.nrows : 0.0;
+        shared = (double)__builtin_popcount(cols) * w + nb < (double)nb * w;
+    }
+    std::vector<double> vals, B((size_t)np * N, 0.0), E, b;
+    if (shared) {
+        std::vector<double> ones3(3 * nt, 1.0), ones2(2 * nbe, 1.0);
+        visit(0, ones3.data(), ones2.data(), nullptr, E, b);
+        vals = E;
+        for (int r = 0; r < N; ++r) {
+            if (d->quarter_neumann) {
+                const std::vector<double> nq = neumann_pairs(r, r, true, false);
+                visit(r, nullptr, nullptr, &nq, E, b);
                 for (int64_t i = 0; i < np; ++i) B[(size_t)i * N + r] = b[i];
-            if (std::any_of(E.begin(), E.end(), [](double x) { return x != 0.0; })) {
-                S->blocks |= 1ull << (r * N + c);
-                ++S->nblocks;
-                vals.insert(vals.end(), E.begin(), E.end());
             }
+            for (int c = 0; c < N; ++c)
+                if (dconst[(size_t)r * N + c] != 0.0) {
+                    S->blocks |= 1ull << (r * N + c);
+                    S->cmask |= 1u << c;
+                    S->dmat[r * N + c] = dconst[(size_t)r * N + c];
+                    ++S->nblocks;
+                }
         }
+        S->shared = true;
+    } else {
+        // coupled blocks K_rc, stored one after another; the Neumann constants from the (r, r) pass
+        for (int r = 0; r < N; ++r)
+            for (int c = 0; c < N; ++c) {
+                const size_t blk = (size_t)r * N + c;
+                std::vector<double> nq;
+                if (d->quarter_neumann) nq = neumann_pairs(r, c, c == r, true);
+                visit(r, DD ? DD + blk * 3 * nt : nullptr, DQ ? DQ + blk * 2 * nbe : nullptr,
+                      d->quarter_neumann ? &nq : nullptr, E, b);
+                if (c == r)
+                    for (int64_t i = 0; i < np; ++i) B[(size_t)i * N + r] = b[i];
+                if (std::any_of(E.begin(), E.end(), [](double x) { return x != 0.0; })) {
+                    S->blocks |= 1ull << (r * N + c);
+                    ++S->nblocks;
+                    vals.insert(vals.end(), E.begin(), E.end());
+                }
+            }
+    }
     if (vals.empty()) vals.assign(pat.nslots, 0.0);  // keeps the value pointer valid; no block is read
     S->d_val.upload(vals);
     S->has_b = std::any_of(B.begin(), B.end(), [](double x) { return x != 0.0; });
@@ -271,8 +503,11 @@ static void create_system(fvm_mesh* m, const fvm_system_desc* d, fvm_system** ou
         }
     S->d_mask.upload(mask);
     std::vector<double> vtab, cf(np);
-    for (int r = 0; r < N; ++r)
-        for (int mo = 0; mo < nmono; ++mo) {
+    SysTerms& T = S->terms;
+    for (int mo = 0; mo < nmono; ++mo) {
+        bool used = false;
+        for (int r = 0; r < N; ++r) {
+            T.term[T.nmono][r] = -1;
             bool any = false, uniform = true, first = true;
             double u0 = 0.0;
             for (int64_t v = 0; v < np; ++v) {
@@ -292,13 +527,10 @@ static void create_system(fvm_mesh* m, const fvm_system_desc* d, fvm_system** ou
                 }
             }
             if (!any) continue;
-            SysTerms& T = S->terms;
             if (T.n == kSysMaxTerms)
                 fail(FVM_ERR_UNSUPPORTED_FORM, "more than " + std::to_string(kSysMaxTerms) + " source / Dudt terms");
-            uint32_t e = 0;
-            for (int c = 0; c < N; ++c) e |= (uint32_t)d->mono_exp[mo * N + c] << (2 * c);
-            T.exps[T.n] = e;
-            T.var[T.n] = r;
+            used = true;
+            T.term[T.nmono][r] = (int16_t)T.n;
             if (uniform) {
                 T.vary[T.n] = -1;
                 T.coef[T.n] = u0;
@@ -311,6 +543,14 @@ static void create_system(fvm_mesh* m, const fvm_system_desc* d, fvm_system** ou
             }
             ++T.n;
         }
+        if (!used) continue;
+        int nf = 0;
+        for (int c = 0; c < N; ++c)
+            for (int e = 0; e < d->mono_exp[mo * N + c]; ++e) T.f[T.nmono][nf++] = (uint8_t)c;
+        for (int k = nf; k < 3; ++k) T.f[T.nmono][k] = 0;
+        T.nf[T.nmono] = (uint8_t)nf;
+        ++T.nmono;
+    }
     if (S->nvary) S->d_vcoef.upload(vtab);
 
     // Dirichlet entries on the flat internal state
@@ -362,6 +602,7 @@ int fvm_system_info(const fvm_system* S, int64_t* info) {
         info[3] = S->nvary;
         info[4] = S->ndir;
         info[5] = S->has_b ? 1 : 0;
+        info[6] = S->shared ? 1 : 0;
         return FVM_OK;
     });
 }

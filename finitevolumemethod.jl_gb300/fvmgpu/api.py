@@ -670,9 +670,10 @@ class FVMSystem:
         return self._h
 
     def info(self) -> Dict[str, int]:
-        a = np.zeros(6, dtype=np.int64)
+        a = np.zeros(7, dtype=np.int64)
         check(load().fvm_system_info(self._h, dptr(a, _lib.c_int64_p)))
-        keys = ["neqs", "flux_blocks", "terms", "varying_terms", "dirichlet_entries", "has_neumann_constants"]
+        keys = ["neqs", "flux_blocks", "terms", "varying_terms", "dirichlet_entries", "has_neumann_constants",
+                "shared_operator"]
         return dict(zip(keys, (int(v) for v in a)))
 
     def _flat(self, x, name):

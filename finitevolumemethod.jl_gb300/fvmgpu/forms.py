@@ -274,19 +274,28 @@ def classify_system_poly(f, x, y, t0, N, what, max_degree=_SYS_DEGREE):
             _reject_sys(what, "non-finite or non-scalar values")
         return v
 
-    Fv = np.stack([ev(u) for u in U])  # (K, n)
+    Fv = np.stack([ev(u) for u in U])  # (K, n); U[0] is the zero tuple
     # points with identical samples share one fit, so a coefficient that does not depend on
     # (x, y) comes out bit-identical at every point
     Fu, inv = np.unique(Fv, axis=1, return_inverse=True)
     inv = inv.reshape(-1)
-    coef = np.linalg.lstsq(_vandermonde(U, exps), Fu, rcond=None)[0]  # (M, unique)
-    cmax = np.max(np.abs(coef), axis=1)
-    keep = cmax > 1e-12 * max(np.max(cmax), 1e-300)
-    exps = exps[keep]
-    if exps.shape[0]:
-        coef = np.linalg.lstsq(_vandermonde(U, exps), Fu, rcond=None)[0][:, inv]
+    c0 = Fu[0]  # the constant term is the value at u = 0, exactly (Dirichlet values, constant sources)
+    G = Fu[1:] - c0
+    rest = exps[1:]  # exps[0] is the constant monomial
+    coef = np.linalg.lstsq(_vandermonde(U[1:], rest), G, rcond=None)[0] if rest.shape[0] else np.zeros((0, Fu.shape[1]))
+    cmax = np.max(np.abs(coef), axis=1) if rest.shape[0] else np.zeros(0)
+    keep = cmax > 1e-12 * max(np.max(cmax, initial=0.0), np.max(np.abs(c0)), 1e-300)
+    rest = rest[keep]
+    if rest.shape[0]:
+        coef = np.linalg.lstsq(_vandermonde(U[1:], rest), G, rcond=None)[0]
     else:
-        coef = np.zeros((0, n))
+        coef = np.zeros((0, Fu.shape[1]))
+    if np.any(c0 != 0):
+        exps = np.vstack([exps[:1], rest])
+        coef = np.vstack([c0[None, :], coef])
+    else:
+        exps = rest
+    coef = coef[:, inv]
     scale = np.max(np.abs(coef), axis=0) if exps.shape[0] else np.zeros(n)
     scale = np.maximum(scale, np.max(scale, initial=0.0) * 1e-300 + 1e-300)
     checks = [(u, t0) for u in Uc] + [(U[1], t0 + 1.37), (Uc[0], t0 + 1.37)]

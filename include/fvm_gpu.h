@@ -223,8 +223,10 @@ typedef struct fvm_system_desc {
  * (:336-365). */
 int fvm_system_create(fvm_mesh* mesh, const fvm_system_desc* desc, fvm_system** out);
 int fvm_system_destroy(fvm_system* sys);
-/* info[0..5] = neq, coupled (r, c) flux blocks, source / Dudt terms, terms with per-vertex
- * coefficients, Dirichlet entries, has Neumann constants. */
+/* info[0..6] = neq, coupled (r, c) flux blocks, source / Dudt terms, terms with per-vertex
+ * coefficients, Dirichlet entries, has Neumann constants, shared form (1 when every block is a
+ * constant multiple of one stored operator: equal conditions, constant diffusivities, Neumann
+ * values independent of u). */
 int fvm_system_info(const fvm_system* sys, int64_t* info);
 /* Replaces fvm_eqs!(du, u, p, t) on an FVMSystem (src/equations/main_equations.jl:38-44 with
  * the system methods of shape_functions.jl:12-19, triangle_contributions.jl:18-25,

@@ -74,6 +74,17 @@ def reference_diffusion_system() -> SysSpec:
     return SysSpec(tri, comps, np.stack([u0, u0]), tf=0.5)
 
 
+def cross_diffusion_system() -> SysSpec:
+    """The reference's diffusion system (test/test_functions.jl:318-334) with a constant
+    cross-diffusion matrix [[1/9, 1/20], [1/30, 1/9]]: equal conditions and constant coupled
+    blocks, which the library stores as one shared operator."""
+    spec = reference_diffusion_system()
+    spec.comps[0]["q"] = lambda x, y, t, a, b, g, p: (-(a[0] / 9 + a[1] / 20), -(b[0] / 9 + b[1] / 20))
+    spec.comps[1]["q"] = lambda x, y, t, a, b, g, p: (-(a[0] / 30 + a[1] / 9), -(b[0] / 30 + b[1] / 9))
+    spec.u0 = spec.u0 * np.array([[1.0], [0.5]])
+    return spec
+
+
 def mixed_system(seed=5) -> SysSpec:
     """Three components on an annulus with eight boundary segments: Dirichlet, Dudt (cubic in
     the components), Neumann (affine in the components, cross-coupled) and Constrained edges,
@@ -130,7 +141,7 @@ def _rhs_close(got, ref, tol=1e-12):
         assert np.max(np.abs(got[c] - ref[c])) <= tol * np.max(np.abs(ref[c])), c
 
 
-@pytest.mark.parametrize("make", [gray_scott, reference_diffusion_system, mixed_system])
+@pytest.mark.parametrize("make", [gray_scott, reference_diffusion_system, cross_diffusion_system, mixed_system])
 def test_system_rhs_matches_oracle(gpu_lib, make):
     spec = make()
     osys, sys = spec.oracle(), spec.api()
@@ -147,11 +158,15 @@ def test_system_rhs_matches_oracle(gpu_lib, make):
 def test_system_forms_and_info(gpu_lib):
     sys = gray_scott().api()
     info = sys.info()
+    # diagonal coupling: the two stored blocks issue fewer FP64 FMAs than a shared operator would
     assert info == {"neqs": 2, "flux_blocks": 2, "terms": 5, "varying_terms": 0, "dirichlet_entries": 0,
-                    "has_neumann_constants": 0}
+                    "has_neumann_constants": 0, "shared_operator": 0}
+    ci = cross_diffusion_system().api().info()
+    assert ci["flux_blocks"] == 4 and ci["shared_operator"] == 1 and ci["dirichlet_entries"] > 0
     msys = mixed_system().api()
     mi = msys.info()
-    assert mi["neqs"] == 3 and mi["flux_blocks"] >= 5 and mi["dirichlet_entries"] > 0 and mi["has_neumann_constants"]
+    assert mi["neqs"] == 3 and mi["flux_blocks"] == 8 and mi["dirichlet_entries"] > 0 and mi["has_neumann_constants"]
+    assert not mi["shared_operator"] and mi["terms"] == 13
 
 
 def test_system_dirichlet_update_matches_oracle(gpu_lib):
