@@ -9,7 +9,8 @@ from .api import (ConditionType, Neumann, Dudt, Dirichlet, Constrained, Parametr
                   InternalConditions, Conditions, TriangleProperties, FVMGeometry, FVMProblem, fvm_eqs,
                   update_dirichlet_nodes, DiffusionEquation, LinearReactionDiffusionEquation, PoissonsEquation,
                   MeanExitTimeProblem, Tsit5, KrylovSolver, ODESolution, LinearSolution, solve, BatchedProblem,
-                  AdjointProblem, solve_rrule, FVMSystem, InvalidFluxError)
+                  AdjointProblem, solve_rrule, FVMSystem, InvalidFluxError,
+                  jacobian_sparsity)
 from ._lib import FVMError, UnsupportedFormError, NotConvergedError
 from ._build import build, lib_path
 
@@ -19,6 +20,6 @@ __all__ = [
     "InternalConditions", "Conditions", "TriangleProperties", "FVMGeometry", "FVMProblem", "fvm_eqs",
     "update_dirichlet_nodes", "DiffusionEquation", "LinearReactionDiffusionEquation", "PoissonsEquation",
     "MeanExitTimeProblem", "Tsit5", "KrylovSolver", "ODESolution", "LinearSolution", "solve", "BatchedProblem",
-    "disjoint_union", "AdjointProblem", "solve_rrule", "FVMSystem", "InvalidFluxError", "FVMError",
+    "disjoint_union", "AdjointProblem", "solve_rrule", "FVMSystem", "InvalidFluxError", "jacobian_sparsity", "FVMError",
     "UnsupportedFormError", "NotConvergedError", "build", "lib_path",
 ]

@@ -520,6 +520,35 @@ def update_dirichlet_nodes(u, prob, t=0.0, stream=None):
     return u
 
 
+def jacobian_sparsity(prob, N=None):
+    """jacobian_sparsity(prob) (src/solve.jl:50-131): the Jacobian prototype of fvm_eqs!, a
+    scipy.sparse CSC matrix of ones.  Node i is coupled to itself and, when it is a vertex, to
+    its neighbours in the triangulation.  For an FVMSystem of N equations every coupled node pair
+    becomes an N x N block, with unknowns numbered (node - 1) N + component, the reference's
+    linear indexing of its N x npoints state.  Takes an FVMProblem, an FVMSystem, a template, or
+    a Triangulation (with N for a system) as the reference's methods do."""
+    import scipy.sparse as sp
+
+    if isinstance(prob, Triangulation):
+        tri = prob
+    else:
+        tri = prob.mesh.triangulation
+        if isinstance(prob, FVMSystem):
+            N = prob.neqs
+    n = tri.num_points
+    T = np.asarray(tri.triangles, dtype=np.int64).reshape(-1, 3)
+    diag = np.arange(n, dtype=np.int64)
+    rows = np.concatenate([diag, T[:, 0], T[:, 1], T[:, 1], T[:, 2], T[:, 2], T[:, 0]])
+    cols = np.concatenate([diag, T[:, 1], T[:, 0], T[:, 2], T[:, 1], T[:, 0], T[:, 2]])
+    A = sp.csc_matrix((np.ones(rows.size), (rows, cols)), shape=(n, n))
+    A.sum_duplicates()
+    A.data[:] = 1.0
+    if N is not None:
+        A = sp.kron(A, np.ones((int(N), int(N))), format="csc")
+    A.sort_indices()
+    return A
+
+
 # --------------------------------------------------------------------------------------
 # systems of equations (src/problem.jl:190-365)
 # --------------------------------------------------------------------------------------

@@ -566,6 +566,34 @@ def system_update_dirichlet_nodes(sys, u, t):
     return u
 
 
+def jacobian_sparsity(tri, N=None):
+    """jacobian_sparsity(tri) and jacobian_sparsity(tri, N) (src/solve.jl:60-131), restated as
+    the reference's loops: every point index i gets (i, i); a vertex also gets (i, j) for each
+    neighbour j (get_neighbours, ghost vertices skipped).  With N components, node i's unknowns
+    are i N + l (0-based), and every coupled node pair is a full N x N block.  Returns the set of
+    (row, column) pairs and the dimension."""
+    n = tri.num_points
+    nbrs = [set() for _ in range(n)]
+    for a, b, c in np.asarray(tri.triangles).reshape(-1, 3):
+        for u, v in ((a, b), (b, c), (c, a)):
+            nbrs[int(u)].add(int(v))
+            nbrs[int(v)].add(int(u))
+    has_vertex = tri.has_vertex()
+    K = 1 if N is None else int(N)
+    entries = set()
+    for i in range(n):
+        for l in range(K):
+            for j in range(K):
+                entries.add((i * K + l, i * K + j))
+        if not has_vertex[i]:
+            continue
+        for j in nbrs[i]:
+            for l in range(K):
+                for k in range(K):
+                    entries.add((i * K + l, j * K + k))
+    return entries, n * K
+
+
 # --------------------------------------------------------------------------------------
 # linear templates: src/specific_problems/*.jl, assembled sparse (not dense)
 # --------------------------------------------------------------------------------------

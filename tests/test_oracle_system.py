@@ -180,3 +180,38 @@ def test_classify_system_fluxes():
                 lambda x, y, t, a, b, g: -a[0]):                              # not a pair
         with pytest.raises(forms.UnsupportedFormError):
             forms.classify_system_flux(bad, x, y, 0.0, 2)
+
+
+# ---- Jacobian prototype (src/solve.jl:50-131; test/test_functions.jl:749-793) ---------------
+def _reference_test_matrix(tri, N):
+    """The dense matrix the reference's test_jacobian_sparsity builds (test/test_functions.jl:
+    749-793): for each solid vertex i and each j in (i, neighbours...), all (x, y) with x among
+    i's unknowns and y among j's."""
+    n = tri.num_points
+    A = np.zeros((n * N, n * N))
+    nb = [set() for _ in range(n)]
+    for a, b, c in tri.triangles:
+        for u, v in ((a, b), (b, c), (c, a)):
+            nb[u].add(v)
+            nb[v].add(u)
+    for i in np.nonzero(tri.has_vertex())[0]:
+        for j in [i, *nb[i]]:
+            A[i * N:(i + 1) * N, j * N:(j + 1) * N] = 1.0
+    return A
+
+
+@pytest.mark.parametrize("N", [None, 1, 2, 3])
+def test_jacobian_sparsity_matches_reference(N):
+    import fvmgpu as F
+    from fvmgpu.meshes import triangulate_annulus
+
+    for tri in (triangulate_rectangle(0.0, 1.0, 0.0, 1.0, 7, 9, single_boundary=False),
+                triangulate_annulus(0.5, 1.0, 4, 16, nsegments=4)):
+        J = F.jacobian_sparsity(tri, N)
+        K = 1 if N is None else N
+        assert J.shape == (tri.num_points * K,) * 2 and J.format == "csc"
+        assert np.all(J.data == 1.0)
+        got = set(zip(*J.nonzero()))
+        entries, dim = O.jacobian_sparsity(tri, N)
+        assert dim == J.shape[0] and got == entries
+        assert np.array_equal(J.toarray(), _reference_test_matrix(tri, K))
