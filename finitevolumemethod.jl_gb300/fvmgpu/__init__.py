@@ -10,7 +10,7 @@ from .api import (ConditionType, Neumann, Dudt, Dirichlet, Constrained, Parametr
                   update_dirichlet_nodes, DiffusionEquation, LinearReactionDiffusionEquation, PoissonsEquation,
                   MeanExitTimeProblem, Tsit5, KrylovSolver, ODESolution, LinearSolution, solve, BatchedProblem,
                   AdjointProblem, solve_rrule, FVMSystem, InvalidFluxError,
-                  jacobian_sparsity)
+                  jacobian_sparsity, compute_flux, pl_interpolate, two_point_interpolant)
 from ._lib import FVMError, UnsupportedFormError, NotConvergedError
 from ._build import build, lib_path
 
@@ -20,6 +20,7 @@ __all__ = [
     "InternalConditions", "Conditions", "TriangleProperties", "FVMGeometry", "FVMProblem", "fvm_eqs",
     "update_dirichlet_nodes", "DiffusionEquation", "LinearReactionDiffusionEquation", "PoissonsEquation",
     "MeanExitTimeProblem", "Tsit5", "KrylovSolver", "ODESolution", "LinearSolution", "solve", "BatchedProblem",
-    "disjoint_union", "AdjointProblem", "solve_rrule", "FVMSystem", "InvalidFluxError", "jacobian_sparsity", "FVMError",
+    "disjoint_union", "AdjointProblem", "solve_rrule", "FVMSystem", "InvalidFluxError", "jacobian_sparsity", "compute_flux", "pl_interpolate",
+    "two_point_interpolant", "FVMError",
     "UnsupportedFormError", "NotConvergedError", "build", "lib_path",
 ]

@@ -520,6 +520,91 @@ def update_dirichlet_nodes(u, prob, t=0.0, stream=None):
     return u
 
 
+# --------------------------------------------------------------------------------------
+# output side: fluxes across edges and interpolation (src/problem.jl:447-487, src/utils.jl:23-42)
+# --------------------------------------------------------------------------------------
+def _stored_abg(prob, t, u):
+    """alpha, beta, gamma of the stored triangle t (shape_functions.jl:2-19): scalars for a
+    vector u, N-tuples for an (N, npoints) u."""
+    a, b, c = (int(v) for v in prob.mesh.triangulation.triangles[t])
+    s = prob.mesh.props_array[t, :9]
+    u = np.asarray(u, dtype=np.float64)
+    if u.ndim == 2:
+        return tuple(tuple(s[3 * m] * u[l, a] + s[3 * m + 1] * u[l, b] + s[3 * m + 2] * u[l, c] for l in range(u.shape[0]))
+                     for m in range(3))
+    return tuple(s[3 * m] * u[a] + s[3 * m + 1] * u[b] + s[3 * m + 2] * u[c] for m in range(3))
+
+
+def _flux_closures(prob):
+    """The flux closure(s) q(x, y, t, alpha, beta, gamma) of a problem or system, with the
+    diffusion form q = -D(x, y, t, alpha x + beta y + gamma) (alpha, beta) when the problem was
+    given a diffusion function (construct_flux_function, src/problem.jl:425-440)."""
+    if hasattr(prob, "flux_functions"):  # FVMSystem
+        return list(prob.flux_functions)
+    if prob.flux_function is not None:
+        return ParametrisedFunction(prob.flux_function, prob.flux_parameters)
+    D = ParametrisedFunction(prob.diffusion_function, prob.diffusion_parameters)
+
+    def q(x, y, t, a, b, g):
+        d = D(x, y, t, a * x + b * y + g)
+        return (-d * a, -d * b)
+
+    return q
+
+
+def compute_flux(prob, i, j, u, t):
+    """compute_flux(prob, i, j, u, t) (src/problem.jl:458-487): q . n at the midpoint of edge
+    (i, j), n its unit normal rotated clockwise from (i, j) (pointing to the edge's right), q
+    the flux of the piecewise-linear u on the triangle to the right of the edge, or on the one
+    to its left for a boundary edge with the outside on its right.  For an FVMSystem (u of
+    shape (N, npoints)) a tuple of N values, one per component.  Host-side, like the reference."""
+    tri = prob.mesh.triangulation
+    px, py = tri.points[int(i)]
+    qx, qy = tri.points[int(j)]
+    ex, ey = qx - px, qy - py
+    ell = np.sqrt(ex * ex + ey * ey)
+    nx, ny = ey / ell, -ex / ell
+    T = tri.edge_triangle(j, i)  # the triangle in the direction of the normal
+    if T < 0:
+        T = tri.edge_triangle(i, j)
+    if T < 0:
+        raise ValueError(f"({i}, {j}) is not an edge of the triangulation")
+    a, b, g = _stored_abg(prob, T, u)
+    mx, my = (px + qx) / 2, (py + qy) / 2
+    q = _flux_closures(prob)
+    if isinstance(q, list):
+        out = []
+        for f in q:
+            qvx, qvy = f(mx, my, t, a, b, g)
+            out.append(nx * qvx + ny * qvy)
+        return tuple(out)
+    qvx, qvy = q(mx, my, t, a, b, g)
+    return nx * qvx + ny * qvy
+
+
+def pl_interpolate(prob, T, u, x, y):
+    """pl_interpolate(prob, T, u, x, y) (src/utils.jl:23-27): the piecewise-linear interpolant of
+    u on triangle T = (i, j, k) (any rotation of a solid triangle) at (x, y); for an (N, npoints)
+    u, an array of N values."""
+    t = prob.mesh.triangulation.find_triangle(T)
+    if t < 0:
+        raise ValueError(f"{tuple(T)} is not a solid triangle of the mesh")
+    a, b, g = _stored_abg(prob, t, u)
+    if isinstance(a, tuple):
+        return np.array([a[l] * x + b[l] * y + g[l] for l in range(len(a))])
+    return a * x + b * y + g
+
+
+def two_point_interpolant(mesh, u, i, j, mx, my):
+    """two_point_interpolant(mesh, u, i, j, mx, my) (src/utils.jl:36-42): u on the segment from
+    node i to node j, linear in the distance from node i."""
+    xi, yi = mesh.triangulation.points[int(i)]
+    xj, yj = mesh.triangulation.points[int(j)]
+    ell = np.sqrt((xj - xi) ** 2 + (yj - yi) ** 2)
+    ellp = np.sqrt((mx - xi) ** 2 + (my - yi) ** 2)
+    return u[i] + (u[j] - u[i]) * ellp / ell
+
+
 def jacobian_sparsity(prob, N=None):
     """jacobian_sparsity(prob) (src/solve.jl:50-131): the Jacobian prototype of fvm_eqs!, a
     scipy.sparse CSC matrix of ones.  Node i is coupled to itself and, when it is a vertex, to

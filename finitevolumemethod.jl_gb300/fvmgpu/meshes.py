@@ -79,6 +79,29 @@ class Triangulation:
         m[self.triangles.ravel()] = True
         return m
 
+    def edge_triangle(self, i, j) -> int:
+        """Index of the solid triangle holding the oriented edge (i, j) (its third vertex is
+        get_adjacent(tri, i, j)), or -1 when (i, j) has the outside on its left."""
+        if not hasattr(self, "_edge_keys"):
+            t = self.triangles
+            n = max(self.num_points, 1)
+            keys = np.concatenate([t[:, 0] * n + t[:, 1], t[:, 1] * n + t[:, 2], t[:, 2] * n + t[:, 0]])
+            order = np.argsort(keys, kind="stable")
+            self._edge_keys = keys[order]
+            self._edge_tri = order % max(self.num_triangles, 1)
+        n = max(self.num_points, 1)
+        q = int(i) * n + int(j)
+        pos = int(np.searchsorted(self._edge_keys, q))
+        if pos < self._edge_keys.size and self._edge_keys[pos] == q:
+            return int(self._edge_tri[pos])
+        return -1
+
+    def find_triangle(self, T) -> int:
+        """Index of the stored solid triangle that is (i, j, k) up to rotation, or -1."""
+        i, j, k = (int(v) for v in T)
+        t = self.edge_triangle(i, j)
+        return t if t >= 0 and k in self.triangles[t] else -1
+
     # -- boundary edge map ------------------------------------------------------
     def _build_boundary(self):
         edges, seg = [], []

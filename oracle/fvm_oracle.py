@@ -566,6 +566,63 @@ def system_update_dirichlet_nodes(sys, u, t):
     return u
 
 
+def adjacent(tri, i, j):
+    """get_adjacent(tri, i, j): the third vertex of the solid triangle holding the oriented
+    edge (i, j), or None for an edge with the outside on its left."""
+    if not hasattr(tri, "_oracle_adj"):
+        adj = {}
+        for a, b, c in np.asarray(tri.triangles).reshape(-1, 3):
+            a, b, c = int(a), int(b), int(c)
+            adj[(a, b)], adj[(b, c)], adj[(c, a)] = c, a, b
+        tri._oracle_adj = adj
+    return tri._oracle_adj.get((int(i), int(j)))
+
+
+def _abg_at(prob, T, u):
+    """_safe_get_triangle_props then get_shape_function_coefficients (src/utils.jl:1-11,
+    shape_functions.jl:2-19): the stored rotation of T and its alpha, beta, gamma (N-tuples for
+    an (N, npoints) u)."""
+    g = prob.geo
+    idx, _ = g.find_triangle(np.array([T[0]]), np.array([T[1]]), np.array([T[2]]))
+    t = int(idx[0])
+    a, b, c = (int(v) for v in g.triangles[t])
+    s = g.s[t]
+    u = np.asarray(u, dtype=np.float64)
+    if u.ndim == 2:
+        return tuple(tuple(s[3 * m] * u[l, a] + s[3 * m + 1] * u[l, b] + s[3 * m + 2] * u[l, c]
+                           for l in range(u.shape[0])) for m in range(3))
+    return tuple(s[3 * m] * u[a] + s[3 * m + 1] * u[b] + s[3 * m + 2] * u[c] for m in range(3))
+
+
+def compute_flux(prob, i, j, u, t):
+    """compute_flux(prob, i, j, u, t) (src/problem.jl:458-487) for a Problem or a System."""
+    P = prob.tri.points
+    px, py = P[i]
+    qx, qy = P[j]
+    ex, ey = qx - px, qy - py
+    l = np.sqrt(ex * ex + ey * ey)
+    nx, ny = ey / l, -ex / l
+    k = adjacent(prob.tri, j, i)
+    if k is None:
+        k = adjacent(prob.tri, i, j)
+    else:
+        i, j = j, i
+    a, b, c = _abg_at(prob, (i, j, k), u)
+    mx, my = (px + qx) / 2, (py + qy) / 2
+    if isinstance(prob, System):
+        return tuple(nx * qv[0] + ny * qv[1] for qv in (f(mx, my, t, a, b, c) for f in prob.fluxes))
+    qvx, qvy = prob.flux(mx, my, t, a, b, c)
+    return nx * qvx + ny * qvy
+
+
+def pl_interpolate(prob, T, u, x, y):
+    """pl_interpolate(prob, T, u, x, y) (src/utils.jl:23-27)."""
+    a, b, c = _abg_at(prob, T, u)
+    if isinstance(a, tuple):
+        return np.array([a[l] * x + b[l] * y + c[l] for l in range(len(a))])
+    return a * x + b * y + c
+
+
 def jacobian_sparsity(tri, N=None):
     """jacobian_sparsity(tri) and jacobian_sparsity(tri, N) (src/solve.jl:60-131), restated as
     the reference's loops: every point index i gets (i, i); a vertex also gets (i, j) for each

@@ -215,3 +215,87 @@ def test_jacobian_sparsity_matches_reference(N):
         entries, dim = O.jacobian_sparsity(tri, N)
         assert dim == J.shape[0] and got == entries
         assert np.array_equal(J.toarray(), _reference_test_matrix(tri, K))
+
+
+# ---- output side: compute_flux, pl_interpolate, two_point_interpolant ------------------------
+class _Mesh:
+    """Host stand-in for FVMGeometry: the triangulation and the geometry rows the library
+    exports (s1..s9, dual-edge midpoints, normals, lengths), here from the oracle's geometry."""
+
+    def __init__(self, tri):
+        g = O.Geometry(tri.points, tri.triangles)
+        self.triangulation = tri
+        self.props_array = np.hstack([g.s, g.mid.reshape(-1, 6), g.nrm.reshape(-1, 6), g.length])
+
+
+def _edges(tri):
+    e = set()
+    for a, b, c in tri.triangles:
+        e |= {(int(a), int(b)), (int(b), int(c)), (int(c), int(a))}
+    return sorted(e)
+
+
+def test_compute_flux_and_interpolation_match_oracle():
+    """test/test_functions.jl:660-747: every solid edge's flux q . n at its midpoint, the normal
+    pointing to the edge's right, from the triangle on that side (the other one on the
+    boundary); pl_interpolate reproduces the linear interpolant."""
+    import fvmgpu as F
+
+    spec = mixed_annulus()
+    mesh = _Mesh(spec.tri)
+    types = tuple(getattr(F, t) for t in spec.bc_types)
+    BCs = F.BoundaryConditions(mesh, tuple(spec.bc_fns), types, parameters=tuple(spec.bc_params))
+    prob = F.FVMProblem(mesh, BCs, diffusion_function=spec.D, diffusion_parameters=spec.Dp, initial_condition=spec.u0,
+                        final_time=1.0)
+    oprob = oracle_problem(spec)
+    u = np.random.default_rng(6).standard_normal(spec.tri.num_points)
+    for (i, j) in _edges(spec.tri)[::3]:
+        got = F.compute_flux(prob, i, j, u, 2.5)
+        assert got == O.compute_flux(oprob, i, j, u, 2.5)
+        # the reference test's own construction for interior edges: the triangle (j, i, k)
+        k = O.adjacent(spec.tri, j, i)
+        if k is not None:
+            p, q = spec.tri.points[i], spec.tri.points[j]
+            a, b, c = O._abg_at(oprob, (j, i, k), u)
+            mx, my = (p + q) / 2
+            qv = oprob.flux(mx, my, 2.5, a, b, c)
+            n = np.array([q[1] - p[1], -(q[0] - p[0])]) / np.linalg.norm(q - p)
+            assert np.isclose(got, qv[0] * n[0] + qv[1] * n[1], rtol=1e-12, atol=1e-14)
+    for T in spec.tri.triangles[::7]:
+        x, y = spec.tri.points[T].mean(axis=0)
+        for rot in ((0, 1, 2), (1, 2, 0), (2, 0, 1)):
+            Tr = tuple(int(T[r]) for r in rot)
+            assert F.pl_interpolate(prob, Tr, u, x, y) == O.pl_interpolate(oprob, Tr, u, x, y)
+        # the interpolant reproduces the vertex values (test/geometry.jl:23-75 identities)
+        for v in T:
+            assert np.isclose(F.pl_interpolate(prob, tuple(T), u, *spec.tri.points[v]), u[v], atol=1e-12)
+    i, j = (int(v) for v in spec.tri.triangles[0][:2])
+    pi, pj = spec.tri.points[i], spec.tri.points[j]
+    m = 0.25 * pi + 0.75 * pj
+    assert np.isclose(F.two_point_interpolant(mesh, u, i, j, *m), 0.25 * u[i] + 0.75 * u[j], rtol=1e-13)
+    with pytest.raises(ValueError):
+        F.pl_interpolate(prob, (0, 0, 0), u, 0.0, 0.0)
+
+
+def test_compute_flux_of_a_system():
+    """compute_flux on a system returns one value per component; a component's value equals the
+    single problem's (test/test_functions.jl:703-704)."""
+    import fvmgpu as F
+
+    sys, spec = reference_diffusion_system()
+
+    class _Sys:  # host stand-in: compute_flux reads mesh and flux_functions only
+        mesh = _Mesh(spec.tri)
+        flux_functions = [lambda x, y, t, a, b, g: (-a[0] / 9, -b[0] / 9),
+                          lambda x, y, t, a, b, g: (-a[1] / 9, -b[1] / 9)]
+
+    u = np.random.default_rng(7).standard_normal((2, spec.tri.num_points))
+    oprob = oracle_problem(spec)
+    for (i, j) in _edges(spec.tri)[::11]:
+        got = F.compute_flux(_Sys, i, j, u, 0.0)
+        assert got == O.compute_flux(sys, i, j, u, 0.0)
+        for c in range(2):
+            assert np.isclose(got[c], O.compute_flux(oprob, i, j, u[c], 0.0), rtol=1e-13, atol=1e-15)
+    T = tuple(int(v) for v in spec.tri.triangles[5])
+    x, y = spec.tri.points[list(T)].mean(axis=0)
+    assert np.array_equal(F.pl_interpolate(_Sys, T, u, x, y), O.pl_interpolate(sys, T, u, x, y))
