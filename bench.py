@@ -674,6 +674,34 @@ def gray_scott_system(F, mesh, centre, cross=False):
     return F.FVMSystem(up, vp)
 
 
+def system_cpu_baseline(n_side=200, max_seconds=5.0, max_evals=50):
+    """CPU baseline of the system row: the oracle's numpy restatement of fvm_eqs! on an FVMSystem
+    (vectorised over triangles, edges and points, one process) for the Gray-Scott tutorial
+    system at its own n_side x n_side mesh; a bounded sample of evaluations."""
+    import fvm_oracle as O
+    from fvmgpu.meshes import triangulate_rectangle
+
+    tri = triangulate_rectangle(-1.0, 1.0, -1.0, 1.0, n_side, n_side, single_boundary=True)
+    bc = lambda x, y, t, u: 0.0 * x  # noqa: E731
+    conds = [O.Conditions(tri, [bc], ["Neumann"]) for _ in range(2)]
+    fluxes = [lambda x, y, t, a, b, g: (-a[0] * 2e-5, -b[0] * 2e-5), lambda x, y, t, a, b, g: (-a[1] * 1e-5, -b[1] * 1e-5)]
+    sources = [lambda x, y, t, u: 0.04 * (1 - u[0]) - u[0] * u[1] ** 2, lambda x, y, t, u: -0.1 * u[1] + u[0] * u[1] ** 2]
+    P = tri.points
+    r2 = P[:, 0] ** 2 + P[:, 1] ** 2
+    u = np.stack([1 - np.exp(-80 * r2), np.exp(-80 * r2)])
+    sys_ = O.System(tri, conds, fluxes, sources, u0=u)
+    O.system_fvm_eqs(sys_, u, 0.0)  # warm-up
+    t0 = time.perf_counter()
+    k = 0
+    while k < max_evals and time.perf_counter() - t0 < max_seconds:
+        O.system_fvm_eqs(sys_, u, 0.0)
+        k += 1
+    dt = time.perf_counter() - t0
+    return {"value": tri.num_points * k / dt, "unit": "point-RHS/s", "cores": 1, "kind": "port",
+            "sample": f"{k} evaluations of the {n_side}x{n_side} Gray-Scott system by the numpy oracle ({dt:.2f} s)",
+            "ms_per_eval": 1e3 * dt / k}
+
+
 def run_system(args, F, torch, flush, c2_mesh):
     """FVMSystem: the Gray-Scott tutorial system on the tutorial's 200 x 200 mesh of [-1, 1]^2
     (RHS, and the tutorial's solve to t = 6000 with saveat 10 by adaptive Tsit5) and on the 1000 x 1000 mesh of
@@ -717,6 +745,8 @@ def run_system(args, F, torch, flush, c2_mesh):
                                               "steps": sol.stats["naccept"], "rejects": sol.stats["nreject"],
                                               "driver": sol.stats["driver"], "saves": len(sol.u)}
         out[name] = row
+    if not args.no_cpu_baseline:
+        out["cpu_baseline"] = system_cpu_baseline()
     return out
 
 

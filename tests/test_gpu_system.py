@@ -279,3 +279,35 @@ def test_system_errors(gpu_lib):
                       initial_condition=spec.u0[0], final_time=1.0)
     with pytest.raises(F.UnsupportedFormError):
         F.FVMSystem(p4, p1)
+
+
+@pytest.mark.parametrize("N", [2, 5])
+def test_system_rolled_kernel_on_wide_rows(gpu_lib, N):
+    """A hub vertex of degree 40 (rows wider than 16 slots) and five components take the kernel's
+    rolled slot loop; two components with coupled constant blocks take its shared form."""
+    from problems import wheel_mesh
+
+    tri = wheel_mesh(40)
+    rng = np.random.default_rng(9)
+    P = tri.points
+    if N == 2:  # constant coupled blocks, equal conditions: the shared form
+        q = [lambda x, y, t, a, b, g, p: (-(a[0] + 0.2 * a[1]), -(b[0] + 0.2 * b[1])),
+             lambda x, y, t, a, b, g, p: (-(0.1 * a[0] + 0.5 * a[1]), -(0.1 * b[0] + 0.5 * b[1]))]
+        S = [lambda x, y, t, u, p: u[0] * u[1] - x, lambda x, y, t, u, p: -u[1] ** 3 + 0.0 * x]
+    else:
+        q = [(lambda c: lambda x, y, t, a, b, g, p: (-(1 + x * x) * a[c] - 0.1 * a[(c + 1) % 5],
+                                                   -(1 + x * x) * b[c] - 0.1 * b[(c + 1) % 5]))(c) for c in range(5)]
+        S = [(lambda c: lambda x, y, t, u, p: u[c] * u[(c + 2) % 5] - 0.5 * u[c] + y)(c) for c in range(5)]
+    if N == 2:  # a Neumann value independent of u keeps the blocks shareable
+        bc = lambda x, y, t, u, p: 0.3 - x  # noqa: E731
+    else:
+        bc = lambda x, y, t, u, p: 0.5 * u[0] - x  # noqa: E731
+    comps = [dict(bc=(bc,), bcp=(None,), types=("Neumann",), q=q[c], S=S[c]) for c in range(N)]
+    spec = SysSpec(tri, comps, rng.standard_normal((N, tri.num_points)), tf=0.1)
+    osys, sys = spec.oracle(), spec.api()
+    assert sys.mesh.info()["operator_slots"] > 0
+    assert sys.info()["shared_operator"] == (1 if N == 2 else 0)
+    for u in (spec.u0, rng.standard_normal(spec.u0.shape)):
+        got = np.empty_like(u)
+        sys.rhs(got, u, 0.0)
+        _rhs_close(got, O.system_fvm_eqs(osys, u, 0.0))
