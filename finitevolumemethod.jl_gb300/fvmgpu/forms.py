@@ -254,9 +254,9 @@ def classify_system_poly(f, x, y, t0, N, what, max_degree=_SYS_DEGREE):
     u[c]^exps[m][c], a polynomial of total degree <= max_degree in the N-tuple u, or reject.
 
     The closure is evaluated at seeded sample tuples u (the same at every point), the
-    coefficients fitted by least squares on the full monomial basis, the monomials whose
-    coefficients vanish dropped and the rest refitted; the fit is then verified at fresh
-    tuples and at a second time to a relative tolerance of 1e-10."""
+    coefficients fitted by least squares on the full monomial basis (the constant term exactly,
+    from u = 0), the monomials whose coefficients vanish dropped and the rest refitted; the fit
+    is then verified at fresh tuples and at a second time to a relative tolerance of 1e-10."""
     x = np.asarray(x, dtype=np.float64)
     n = x.shape[0]
     exps = monomials(N, max_degree)
@@ -275,27 +275,36 @@ def classify_system_poly(f, x, y, t0, N, what, max_degree=_SYS_DEGREE):
         return v
 
     Fv = np.stack([ev(u) for u in U])  # (K, n); U[0] is the zero tuple
-    # points with identical samples share one fit, so a coefficient that does not depend on
-    # (x, y) comes out bit-identical at every point
-    Fu, inv = np.unique(Fv, axis=1, return_inverse=True)
-    inv = inv.reshape(-1)
+    # a closure that does not depend on (x, y) gives identical samples at every point: one fit
+    same = n > 0 and bool(np.all(Fv == Fv[:, :1]))
+    Fu = Fv[:, :1] if same else Fv
     c0 = Fu[0]  # the constant term is the value at u = 0, exactly (Dirichlet values, constant sources)
     G = Fu[1:] - c0
     rest = exps[1:]  # exps[0] is the constant monomial
-    coef = np.linalg.lstsq(_vandermonde(U[1:], rest), G, rcond=None)[0] if rest.shape[0] else np.zeros((0, Fu.shape[1]))
+    # least squares through the pseudo-inverse of the small sample matrix: one product for all points
+    coef = np.linalg.pinv(_vandermonde(U[1:], rest)) @ G if rest.shape[0] else np.zeros((0, Fu.shape[1]))
     cmax = np.max(np.abs(coef), axis=1) if rest.shape[0] else np.zeros(0)
-    keep = cmax > 1e-12 * max(np.max(cmax, initial=0.0), np.max(np.abs(c0)), 1e-300)
+    keep = cmax > 1e-12 * max(np.max(cmax, initial=0.0), np.max(np.abs(c0), initial=0.0), 1e-300)
     rest = rest[keep]
     if rest.shape[0]:
-        coef = np.linalg.lstsq(_vandermonde(U[1:], rest), G, rcond=None)[0]
+        coef = np.linalg.pinv(_vandermonde(U[1:], rest)) @ G
     else:
         coef = np.zeros((0, Fu.shape[1]))
+    # a fitted coefficient that is one value up to the fit's rounding at every point (it does
+    # not depend on (x, y) while another coefficient does; measured spreads stay below 1e-13
+    # relative) is set to that one value, so the library can keep it as a scalar
+    for k in range(coef.shape[0]):
+        row = coef[k]
+        lo, hi = row.min(initial=np.inf), row.max(initial=-np.inf)
+        if row.size and hi - lo <= 1e-13 * max(abs(lo), abs(hi)):
+            row[:] = np.median(row)
     if np.any(c0 != 0):
         exps = np.vstack([exps[:1], rest])
         coef = np.vstack([c0[None, :], coef])
     else:
         exps = rest
-    coef = coef[:, inv]
+    if same:
+        coef = np.repeat(coef, n, axis=1)
     scale = np.max(np.abs(coef), axis=0) if exps.shape[0] else np.zeros(n)
     scale = np.maximum(scale, np.max(scale, initial=0.0) * 1e-300 + 1e-300)
     checks = [(u, t0) for u in Uc] + [(U[1], t0 + 1.37), (Uc[0], t0 + 1.37)]
