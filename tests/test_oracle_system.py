@@ -299,3 +299,19 @@ def test_compute_flux_of_a_system():
     T = tuple(int(v) for v in spec.tri.triangles[5])
     x, y = spec.tri.points[list(T)].mean(axis=0)
     assert np.array_equal(F.pl_interpolate(_Sys, T, u, x, y), O.pl_interpolate(sys, T, u, x, y))
+
+
+def test_system_fit_keeps_position_independent_coefficients_exact():
+    """Coefficients that do not depend on (x, y) come out as one value at every point, whether or
+    not another coefficient depends on (x, y); the constant term is the closure's own value."""
+    x = np.linspace(-1, 1, 2000)
+    y = np.linspace(0, 1, 2000)
+    e, c = forms.classify_system_poly(lambda x, y, t, u: 0.04 * (1 - u[0]) - u[0] * u[1] ** 2, x, y, 0.0, 2, "S")
+    assert all(np.unique(c[:, k]).size == 1 for k in range(c.shape[1]))
+    f = lambda x, y, t, u: (1 + x * x) * u[0] * u[1] - 0.3 * u[1] ** 3 + 0.04 * u[0] - y  # noqa: E731
+    e, c = forms.classify_system_poly(f, x, y, 0.0, 2, "S")
+    got = {tuple(k): c[:, m] for m, k in enumerate(e)}
+    assert np.unique(got[(1, 0)]).size == 1 and np.unique(got[(0, 3)]).size == 1
+    assert np.allclose(got[(1, 0)], 0.04, rtol=1e-13) and np.allclose(got[(0, 3)], -0.3, rtol=1e-13)
+    assert np.array_equal(got[(0, 0)], -y)  # the value at u = 0, exactly
+    assert np.allclose(got[(1, 1)], 1 + x * x, rtol=1e-12)
