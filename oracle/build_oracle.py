@@ -28,6 +28,10 @@ class OrcProblem(C.Structure):
     ]
 
 
+class GrayScott(C.Structure):
+    _fields_ = [("eps", C.c_double * 2), ("b", C.c_double), ("d", C.c_double)]
+
+
 def build(force: bool = False) -> Path:
     LIB.parent.mkdir(parents=True, exist_ok=True)
     if force or not LIB.exists() or LIB.stat().st_mtime < SRC.stat().st_mtime:
@@ -52,6 +56,8 @@ def load():
         lib.orc_rhs_threaded.argtypes = [C.POINTER(OrcProblem), C.c_void_p, C.c_void_p, C.c_double, C.c_int,
                                          C.c_void_p]
         lib.orc_max_threads.restype = C.c_int
+        lib.orc_gray_scott_rhs_threaded.argtypes = [C.POINTER(OrcProblem), C.POINTER(GrayScott), C.c_void_p,
+                                                    C.c_void_p, C.c_int, C.c_void_p]
         _lib = lib
     return _lib
 
@@ -96,6 +102,33 @@ class CProblem:
             self._dup = np.empty(self.np * nth)
         du = np.empty(self.np) if du is None else du
         lib.orc_rhs_threaded(C.byref(self.p), u.ctypes.data, du.ctypes.data, t, nth, self._dup.ctypes.data)
+        return du
+
+
+class CGrayScott(CProblem):
+    """The C restatement of the Gray-Scott tutorial FVMSystem (zero Neumann boundary, fluxes
+    -eps_c grad u_c, sources b (1 - u) - u v^2 and -d v + u v^2); state (2, npoints) as the
+    reference's matrix, passed in its [point][component] memory order."""
+
+    def __init__(self, geo, tri, code, bnd_tri, eps=(2e-5, 1e-5), b=0.04, d=0.1):
+        super().__init__(geo, tri, code, D_CONST, (0.0,), bnd_tri)
+        self.g = GrayScott()
+        self.g.eps[0], self.g.eps[1] = eps
+        self.g.b, self.g.d = b, d
+
+    def rhs_threaded(self, u, t=0.0, nthreads=0, du=None):
+        """u, du: (2, npoints) arrays; du is returned."""
+        lib = load()
+        nth = nthreads or lib.orc_max_threads()
+        if self._dup is None or self._dup.size < 2 * self.np * nth:
+            self._dup = np.empty(2 * self.np * nth)
+        ut = np.ascontiguousarray(np.asarray(u, dtype=np.float64).T)
+        dt = np.empty_like(ut)
+        lib.orc_gray_scott_rhs_threaded(C.byref(self.p), C.byref(self.g), ut.ctypes.data, dt.ctypes.data, nth,
+                                        self._dup.ctypes.data)
+        if du is None:
+            return dt.T.copy()
+        du[...] = dt.T
         return du
 
 

@@ -145,6 +145,118 @@ void orc_rhs_threaded(const orc_problem* P, const double* u, double* du, double 
     }
 }
 
+/* ---- FVMSystem: the Gray-Scott tutorial system ------------------------------------------
+ * (docs/src/literate_tutorials/gray_scott_model_turing_patterns_from_a_coupled_reaction_diffusion_system.jl)
+ * evaluated the way the reference evaluates an FVMSystem:
+ *   alpha, beta, gamma tuples per triangle      src/equations/shape_functions.jl:12-19
+ *   every component's flux closure per dual edge individual_flux_contributions.jl:35-51
+ *   update_du! per component                     triangle_contributions.jl:18-25
+ *   boundary edges: all fluxes evaluated, then the (zero) Neumann value replaces them
+ *                                                boundary_edge_contributions.jl:15-75
+ *   sources per component on free vertices       source_contributions.jl:17-30,49-66
+ *   parallel_fvm_eqs! with duplicated du         main_equations.jl:47-81
+ * State [point][component] (the reference's 2 x npoints matrix). */
+typedef struct {
+    double eps[2]; /* u_q = -eps_1 (alpha[1], beta[1]), v_q = -eps_2 (alpha[2], beta[2]) */
+    double b, d;   /* u_S = b (1 - u) - u v^2, v_S = -d v + u v^2 */
+} orc_gray_scott;
+
+static inline void gs_flux(const orc_gray_scott* G, const double* a, const double* b, double q[2][2]) {
+    q[0][0] = -a[0] * G->eps[0];
+    q[0][1] = -b[0] * G->eps[0];
+    q[1][0] = -a[1] * G->eps[1];
+    q[1][1] = -b[1] * G->eps[1];
+}
+
+static inline void gs_triangle(const orc_problem* P, const orc_gray_scott* G, int64_t t, const double* u, double* du) {
+    const int32_t* T = P->tri + 3 * t;
+    const double* pr = P->props + 24 * t;
+    int32_t i = T[0], j = T[1], k = T[2];
+    double a[2], b[2], g[2], Q[2][3];
+    for (int v = 0; v < 2; ++v) {
+        double ui = u[2 * i + v], uj = u[2 * j + v], uk = u[2 * k + v];
+        a[v] = pr[0] * ui + pr[1] * uj + pr[2] * uk;
+        b[v] = pr[3] * ui + pr[4] * uj + pr[5] * uk;
+        g[v] = pr[6] * ui + pr[7] * uj + pr[8] * uk;
+    }
+    (void)g;
+    for (int e = 0; e < 3; ++e) {
+        double q[2][2];
+        gs_flux(G, a, b, q);
+        for (int v = 0; v < 2; ++v) Q[v][e] = (q[v][0] * pr[15 + 2 * e] + q[v][1] * pr[16 + 2 * e]) * pr[21 + e];
+    }
+    for (int v = 0; v < 2; ++v) {
+        du[2 * i + v] = du[2 * i + v] + Q[v][2] - Q[v][0];
+        du[2 * j + v] = du[2 * j + v] + Q[v][0] - Q[v][1];
+        du[2 * k + v] = du[2 * k + v] + Q[v][1] - Q[v][2];
+    }
+}
+
+static inline void gs_bedge(const orc_problem* P, const orc_gray_scott* G, int64_t e, const double* u, double* du) {
+    int32_t i = P->bedge[3 * e], j = P->bedge[3 * e + 1], t = P->bedge[3 * e + 2];
+    const int32_t* T = P->tri + 3 * (int64_t)t;
+    const double* pr = P->props + 24 * (int64_t)t;
+    double a[2], b[2];
+    for (int v = 0; v < 2; ++v) {
+        double u0 = u[2 * T[0] + v], u1 = u[2 * T[1] + v], u2 = u[2 * T[2] + v];
+        a[v] = pr[0] * u0 + pr[1] * u1 + pr[2] * u2;
+        b[v] = pr[3] * u0 + pr[4] * u1 + pr[5] * u2;
+    }
+    double px = P->pts[2 * i], py = P->pts[2 * i + 1], qx = P->pts[2 * j], qy = P->pts[2 * j + 1];
+    double mijx = (px + qx) / 2, mijy = (py + qy) / 2;
+    double l = sqrt((mijx - px) * (mijx - px) + (mijy - py) * (mijy - py));
+    double q[2][2];
+    gs_flux(G, a, b, q); /* at m_i, then replaced by the zero Neumann value */
+    gs_flux(G, a, b, q); /* at m_j */
+    for (int v = 0; v < 2; ++v) {
+        du[2 * i + v] = du[2 * i + v] - 0.0 * l;
+        du[2 * j + v] = du[2 * j + v] - 0.0 * l;
+    }
+}
+
+static inline void gs_source(const orc_problem* P, const orc_gray_scott* G, int64_t i, const double* u, double* du) {
+    if (P->code[i] != 0) {
+        du[2 * i] = du[2 * i + 1] = 0.0;
+        return;
+    }
+    double uu = u[2 * i], vv = u[2 * i + 1];
+    du[2 * i] = du[2 * i] / P->vol[i] + (G->b * (1 - uu) - uu * vv * vv);
+    du[2 * i + 1] = du[2 * i + 1] / P->vol[i] + (-G->d * vv + uu * vv * vv);
+}
+
+void orc_gray_scott_rhs_threaded(const orc_problem* P, const orc_gray_scott* G, const double* u, double* du,
+                                 int nthreads, double* dup) {
+#ifdef _OPENMP
+    if (nthreads <= 0) nthreads = omp_get_max_threads();
+#else
+    nthreads = 1;
+#endif
+    const int64_t n = 2 * P->np;
+    memset(du, 0, sizeof(double) * n);
+#pragma omp parallel num_threads(nthreads)
+    {
+#ifdef _OPENMP
+        int c = omp_get_thread_num();
+        int nth = omp_get_num_threads();
+#else
+        int c = 0, nth = 1;
+#endif
+        double* col = dup + (int64_t)c * n;
+        memset(col, 0, sizeof(double) * n);
+        int64_t t0 = P->nt * c / nth, t1 = P->nt * (c + 1) / nth;
+        for (int64_t q = t0; q < t1; ++q) gs_triangle(P, G, q, u, col);
+        int64_t e0 = P->nbe * c / nth, e1 = P->nbe * (c + 1) / nth;
+        for (int64_t e = e0; e < e1; ++e) gs_bedge(P, G, e, u, col);
+#pragma omp barrier
+        int64_t v0 = P->np * c / nth, v1 = P->np * (c + 1) / nth;
+        for (int w = 0; w < nth; ++w) {
+            const double* cw = dup + (int64_t)w * n;
+            for (int64_t i = 2 * v0; i < 2 * v1; ++i) du[i] += cw[i];
+        }
+        for (int64_t i = v0; i < v1; ++i) gs_source(P, G, i, u, du);
+    }
+}
+
 int orc_max_threads(void) {
 #ifdef _OPENMP
     return omp_get_max_threads();

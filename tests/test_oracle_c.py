@@ -19,3 +19,23 @@ def test_c_oracle_matches_numpy_oracle():
         ref = O.fvm_eqs(prob, u, 0.0)
         for got in (cp.rhs_serial(u), cp.rhs_threaded(u, nthreads=3), cp.rhs_threaded(u, nthreads=1)):
             assert np.linalg.norm(got - ref) <= 1e-13 * np.linalg.norm(ref)
+
+
+def test_c_gray_scott_system_matches_numpy_oracle():
+    """The C restatement of the Gray-Scott FVMSystem (the system row's CPU baseline) agrees with
+    the oracle's system_fvm_eqs."""
+    from fvmgpu.meshes import triangulate_rectangle
+
+    tri = triangulate_rectangle(-1.0, 1.0, -1.0, 1.0, 30, 30, single_boundary=True)
+    bc = lambda x, y, t, u: 0.0 * x  # noqa: E731
+    conds = [O.Conditions(tri, [bc], ["Neumann"]) for _ in range(2)]
+    fluxes = [lambda x, y, t, a, b, g: (-a[0] * 2e-5, -b[0] * 2e-5), lambda x, y, t, a, b, g: (-a[1] * 1e-5, -b[1] * 1e-5)]
+    sources = [lambda x, y, t, u: 0.04 * (1 - u[0]) - u[0] * u[1] ** 2, lambda x, y, t, u: -0.1 * u[1] + u[0] * u[1] ** 2]
+    sys_ = O.System(tri, conds, fluxes, sources)
+    u = np.random.default_rng(1).random((2, tri.num_points))
+    ref = O.system_fvm_eqs(sys_, u, 0.0)
+    cp = B.CGrayScott(sys_.geo, tri, sys_.code[0], sys_.bnd_tri)
+    for nth in (1, 3):
+        got = cp.rhs_threaded(u, nthreads=nth)
+        for c in range(2):
+            assert np.max(np.abs(got[c] - ref[c])) <= 1e-13 * np.max(np.abs(ref[c]))
