@@ -656,6 +656,21 @@ class InvalidFluxError(ValueError):
         super().__init__(FLUX_ERROR + (f"\n{detail}" if detail else ""))
 
 
+def merge_problem_conditions(probs):
+    """merge_problem_conditions (src/problem.jl:336-365): each component keeps its own conditions;
+    the condition functions are concatenated component by component, cnum_fncs[i] being the
+    number of functions of the components before i; sources and fluxes are wrapped with their
+    parameters.  Returns (conditions, cnum_fncs, functions, source_functions, flux_functions)."""
+    conditions = tuple(p.conditions for p in probs)
+    nf = [len(c.functions) for c in conditions]
+    cnum_fncs = tuple(int(v) for v in np.cumsum([0] + nf[:-1]))
+    functions = tuple(f for c in conditions for f in c.functions)
+    source_functions = tuple(None if p.source_function is None else
+                             ParametrisedFunction(p.source_function, p.source_parameters) for p in probs)
+    flux_functions = tuple(ParametrisedFunction(p.flux_function, p.flux_parameters) for p in probs)
+    return conditions, cnum_fncs, functions, source_functions, flux_functions
+
+
 class FVMSystem:
     """FVMSystem(prob1, ..., probN) (src/problem.jl:190-365): N coupled equations on one mesh.
 
@@ -695,13 +710,8 @@ class FVMSystem:
         self.initial_condition = np.stack([p.initial_condition for p in probs])
         self.initial_time = probs[0].initial_time
         self.final_time = probs[0].final_time
-        self.conditions = tuple(p.conditions for p in probs)
-        nf = [len(c.functions) for c in self.conditions]
-        self.cnum_fncs = tuple(int(v) for v in np.cumsum([0] + nf[:-1]))
-        self.functions = tuple(f for c in self.conditions for f in c.functions)
-        self.source_functions = tuple(None if p.source_function is None else
-                                      ParametrisedFunction(p.source_function, p.source_parameters) for p in probs)
-        self.flux_functions = tuple(ParametrisedFunction(p.flux_function, p.flux_parameters) for p in probs)
+        (self.conditions, self.cnum_fncs, self.functions, self.source_functions,
+         self.flux_functions) = merge_problem_conditions(probs)
         self._h = None
         self._build()
 

@@ -104,3 +104,48 @@ def test_saveat_times_follow_julia_ranges():
     assert ts.size == 501 and ts[0] == 0.0 and abs(ts[-1] - 0.5) < 1e-12
     assert np.array_equal(_saveat_times([0.1, 0.2], 0.0, 1.0), [0.1, 0.2])
     assert np.array_equal(_saveat_times(None, 0.0, 1.0), [0.0, 1.0])
+
+
+def test_problems_and_system_conditions_without_a_device():
+    """An FVMProblem is built without touching the device (its closures are classified on first
+    use); the conditions of a system merge as merge_problem_conditions does
+    (test/problem.jl:170-260: cnum_fncs == (0, 4), map_fidx, the merged function list, each
+    component's Neumann / Dirichlet tables)."""
+    import numpy as np
+
+    from fvmgpu import api
+    from fvmgpu.meshes import triangulate_rectangle
+
+    tri = triangulate_rectangle(0.0, 1.0, 0.0, 1.0, 10, 10, single_boundary=False)
+
+    class Mesh:  # a host stand-in: BoundaryConditions and FVMProblem read the triangulation only
+        triangulation = tri
+
+    phi = (lambda x, y, t, u, p: -0.25 * np.exp(-x - t / 2), lambda x, y, t, u, p: 0.25 * np.exp(-1 - y - t / 2),
+           lambda x, y, t, u, p: np.exp(-1 - x - t / 2), lambda x, y, t, u, p: -0.25 * np.exp(-y - t / 2))
+    psi = (lambda x, y, t, u, p: np.exp(x + t / 2), lambda x, y, t, u, p: -0.25 * np.exp(1 + y + t / 2),
+           lambda x, y, t, u, p: -0.25 * np.exp(1 + x + t / 2), lambda x, y, t, u, p: np.exp(y + t / 2))
+    N_, D_ = api.Neumann, api.Dirichlet
+    pbc = api.BoundaryConditions(Mesh, phi, (N_, N_, D_, N_))
+    sbc = api.BoundaryConditions(Mesh, psi, (D_, N_, N_, D_))
+    q1 = lambda x, y, t, a, b, g, p: (-a[0] / 4, -b[0] / 4)  # noqa: E731
+    q2 = lambda x, y, t, a, b, g, p: (-a[1] / 4, -b[1] / 4)  # noqa: E731
+    S1 = lambda x, y, t, u, p: u[0] ** 2 * u[1] - 2 * u[0]  # noqa: E731
+    S2 = lambda x, y, t, u, p: -u[0] ** 2 * u[1] + u[0]  # noqa: E731
+    u0 = np.zeros(tri.num_points)
+    p1 = api.FVMProblem(Mesh, pbc, flux_function=q1, source_function=S1, initial_condition=u0, final_time=5.0)
+    p2 = api.FVMProblem(Mesh, sbc, flux_function=q2, source_function=S2, initial_condition=u0, final_time=5.0)
+    assert p1._h is None and not p1._built  # nothing classified, nothing on the device
+    conds, cnum, fns, srcs, fluxes = api.merge_problem_conditions((p1, p2))
+    assert cnum == (0, 4) and len(fns) == 8
+    assert conds[0] is p1.conditions and conds[1] is p2.conditions
+    for k in range(4):
+        assert fns[k] is p1.conditions.functions[k] and fns[4 + k] is p2.conditions.functions[k]
+    x, y, t = 0.3, 0.7, 0.9
+    for (i, j), f in p2.conditions.neumann_edges.items():
+        assert fns[f + cnum[1]](x, y, t, (1.0, 2.0)) == p2.conditions.functions[f](x, y, t, (1.0, 2.0))
+    assert srcs[0](x, y, t, (2.0, 3.0)) == S1(x, y, t, (2.0, 3.0), None)
+    assert fluxes[1](x, y, t, (1.0, 2.0), (3.0, 4.0), (5.0, 6.0)) == (-0.5, -1.0)
+    # component tables: Phi is Neumann on three sides and Dirichlet on the top, Psi the reverse pattern
+    assert len(conds[0].dirichlet_nodes) == 10 and len(conds[1].dirichlet_nodes) == 19
+    assert len(conds[0].neumann_edges) == 27 and len(conds[1].neumann_edges) == 18
