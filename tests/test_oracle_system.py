@@ -315,3 +315,44 @@ def test_system_fit_keeps_position_independent_coefficients_exact():
     assert np.allclose(got[(1, 0)], 0.04, rtol=1e-13) and np.allclose(got[(0, 3)], -0.3, rtol=1e-13)
     assert np.array_equal(got[(0, 0)], -y)  # the value at u = 0, exactly
     assert np.allclose(got[(1, 1)], 1 + x * x, rtol=1e-12)
+
+
+def test_decoupled_system_equals_its_single_problems():
+    """Two components on one annulus, each with its own conditions (component 0: the mixed
+    Dirichlet / Dudt / Neumann / Constrained layout with internal nodes; component 1: a different
+    layout), diffusion and source, not coupled: each row of the system RHS and of the Dirichlet
+    update equals its own single problem's (merge_problem_conditions keeps conditions per
+    component, src/problem.jl:336-365)."""
+    from problems import Spec
+
+    a = mixed_annulus()
+    types_b = ("Neumann", "Dirichlet", "Dudt", "Neumann", "Constrained", "Neumann", "Dirichlet", "Neumann")
+    b = Spec(a.tri, a.bc_fns[::-1], types_b, a.bc_params[::-1],
+             D=lambda x, y, t, u, p: 2.0 + y * y + 0.0 * u, S=lambda x, y, t, u, p: -u + 0.5 * u * u, u0=a.u0[::-1].copy())
+    specs = (a, b)
+    probs = [oracle_problem(s) for s in specs]
+
+    def comp(s, c):
+        wrap = lambda f, p: (lambda x, y, t, u: f(x, y, t, u[c], p))  # noqa: E731
+        cond = O.Conditions(s.tri, [wrap(f, p) for f, p in zip(s.bc_fns, s.bc_params)], list(s.bc_types),
+                            [wrap(f, p) for f, p in zip(s.ic_fns, s.ic_params)], s.dirichlet_nodes, s.dudt_nodes)
+
+        def q(x, y, t, al, be, ga):
+            d = s.D(x, y, t, al[c] * x + be[c] * y + ga[c], s.Dp)
+            return (-d * al[c], -d * be[c])
+
+        src = lambda x, y, t, u: s.S(x, y, t, u[c], s.Sp)  # noqa: E731
+        return cond, q, src
+
+    parts = [comp(s, c) for c, s in enumerate(specs)]
+    sys = O.System(a.tri, [p[0] for p in parts], [p[1] for p in parts], [p[2] for p in parts])
+    rng = np.random.default_rng(12)
+    u = rng.standard_normal((2, a.tri.num_points))
+    du = O.system_fvm_eqs(sys, u, 0.0)
+    ud = O.system_update_dirichlet_nodes(sys, u, 0.0)
+    for c in range(2):
+        ref = O.fvm_eqs(probs[c], u[c], 0.0)
+        scale = rhs_term_scale(probs[c], u[c], 0.0)
+        assert np.max(np.abs(du[c] - ref) / (np.abs(ref) + scale + 1e-300)) < 1e-13
+        assert np.array_equal(ud[c], O.update_dirichlet_nodes(probs[c], u[c], 0.0))
+        assert np.array_equal(sys.code[c], probs[c].code)
