@@ -751,7 +751,10 @@ def run_system(args, F, torch, flush, c2_mesh):
                                               "driver": sol.stats["driver"], "saves": len(sol.u)}
         out[name] = row
     if not args.no_cpu_baseline:
-        out["cpu_baseline"] = system_cpu_baseline()
+        try:
+            out["cpu_baseline"] = system_cpu_baseline()
+        except Exception as e:  # noqa: BLE001  (the GPU rows above stand on their own)
+            out["cpu_baseline"] = {"value": None, "error": repr(e)}
     return out
 
 
