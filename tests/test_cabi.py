@@ -63,3 +63,50 @@ def test_no_cpu_fallback_without_gpu():
         pytest.skip("a GPU is present")
     with pytest.raises(RuntimeError, match="no CPU fallback"):
         _lib.require_gpu()
+
+
+STRUCTS = {  # C struct in include/fvm_gpu.h -> its ctypes mirror in fvmgpu/_lib.py
+    "fvm_problem_desc": "ProblemDesc",
+    "fvm_system_desc": "SystemDesc",
+    "fvm_ode_options": "OdeOptions",
+    "fvm_ode_stats": "OdeStats",
+    "fvm_solver_options": "SolverOptions",
+    "fvm_solver_stats": "SolverStats",
+    "fvm_adjoint_stats": "AdjointStats",
+}
+
+
+def test_ctypes_structures_match_the_header_layout(tmp_path):
+    """Every field of every C-ABI struct has the same name order, offset and size in the ctypes
+    mirror as the C compiler gives it (a mismatch would pass arguments silently corrupted)."""
+    from fvmgpu import _lib
+
+    lines = ["#include <stdio.h>", "#include <stddef.h>", f'#include "{HEADER}"', "int main(void) {"]
+    for cname, pyname in STRUCTS.items():
+        st = getattr(_lib, pyname)
+        lines.append(f'printf("{cname} sizeof %zu\\n", sizeof({cname}));')
+        for field, _ in st._fields_:
+            lines.append(f'printf("{cname} {field} %zu %zu\\n", offsetof({cname}, {field}), '
+                         f'sizeof((({cname}*)0)->{field}));')
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
+    got = {}
+    for line in filter(None, out):
+        parts = line.split()
+        got[(parts[0], parts[1])] = tuple(int(v) for v in parts[2:])
+    for cname, pyname in STRUCTS.items():
+        st = getattr(_lib, pyname)
+        assert got[(cname, "sizeof")] == (ctypes.sizeof(st),), cname
+        for field, _ in st._fields_:
+            desc = getattr(st, field)
+            assert got[(cname, field)] == (desc.offset, desc.size), (cname, field)
+    # and the ctypes mirrors name every field of the C structs, in order
+    text = re.sub(r"/\*.*?\*/", "", HEADER.read_text(), flags=re.S)
+    for cname, pyname in STRUCTS.items():
+        body = re.search(r"typedef struct " + cname + r" \{(.*?)\}", text, flags=re.S).group(1)
+        names = re.findall(r"(\w+)\s*(?:\[[^\]]*\])?\s*[;,]", body)
+        assert names == [f for f, _ in getattr(_lib, pyname)._fields_], cname
