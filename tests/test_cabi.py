@@ -110,3 +110,35 @@ def test_ctypes_structures_match_the_header_layout(tmp_path):
         body = re.search(r"typedef struct " + cname + r" \{(.*?)\}", text, flags=re.S).group(1)
         names = re.findall(r"(\w+)\s*(?:\[[^\]]*\])?\s*[;,]", body)
         assert names == [f for f, _ in getattr(_lib, pyname)._fields_], cname
+
+
+JULIA = ROOT / "finitevolumemethod.jl_gb300" / "julia" / "FiniteVolumeMethodGPU" / "src" / "FiniteVolumeMethodGPU.jl"
+JULIA_STRUCTS = {"ProblemDesc": "fvm_problem_desc", "SystemDesc": "fvm_system_desc", "OdeOptions": "fvm_ode_options",
+                 "OdeStats": "fvm_ode_stats"}
+JULIA_SIZES = {"Int8": 1, "Int32": 4, "Cint": 4, "Int64": 8, "Float64": 8}
+
+
+def test_julia_binding_structures_match_the_header_layout():
+    """The Julia binding cannot run here (no Julia), but its ccall structures can be checked: laid
+    out with C rules from their field types (isbits structs are C-compatible), each must give
+    the header's field names, offsets and size, the same as the ctypes mirrors do."""
+    from fvmgpu import _lib
+
+    text = JULIA.read_text()
+    for jname, cname in JULIA_STRUCTS.items():
+        body = re.search(r"^(?:mutable )?struct " + jname + r"\n(.*?)^end", text, flags=re.S | re.M).group(1)
+        fields = re.findall(r"^\s*(\w+)::([\w{}]+)\s*$", body, flags=re.M)
+        pyst = getattr(_lib, STRUCTS_BY_C[cname])
+        assert [f for f, _ in fields] == [f for f, _ in pyst._fields_], jname
+        off = 0
+        align = 1
+        for (f, ty), (_, _) in zip(fields, pyst._fields_):
+            size = 8 if ty.startswith("Ptr") else JULIA_SIZES[ty]
+            off = (off + size - 1) // size * size
+            assert off == getattr(pyst, f).offset and size == getattr(pyst, f).size, (jname, f)
+            off += size
+            align = max(align, size)
+        assert (off + align - 1) // align * align == ctypes.sizeof(pyst), jname
+
+
+STRUCTS_BY_C = {c: p for c, p in STRUCTS.items()}
