@@ -142,3 +142,50 @@ def test_julia_binding_structures_match_the_header_layout():
 
 
 STRUCTS_BY_C = {c: p for c, p in STRUCTS.items()}
+
+
+def _c_prototypes():
+    """name -> list of parameter types (whitespace-normalised) of every fvm_* entry point."""
+    text = re.sub(r"/\*.*?\*/", "", HEADER.read_text(), flags=re.S)
+    out = {}
+    for name, params in re.findall(r"\bint\s+(fvm_\w+)\s*\(([^)]*)\)\s*;", text):
+        types = []
+        for p in params.split(","):
+            p = " ".join(p.split())
+            if p in ("void", ""):
+                continue
+            types.append(re.sub(r"\s*\w+$", "", p).replace(" *", "*"))  # drop the parameter name
+        out[name] = types
+    return out
+
+
+def _julia_type(c):
+    """The Julia ccall type a C parameter type takes (by value or through a pointer)."""
+    c = c.replace("const ", "")
+    scalars = {"double": "Float64", "int32_t": "Int32", "int64_t": "Int64", "size_t": "Csize_t", "int": "Cint",
+               "int8_t": "Int8", "char": "UInt8"}
+    if c.endswith("**"):
+        return {"Ref{Ptr{Cvoid}}"}
+    if c.endswith("*"):
+        base = c[:-1]
+        if base in scalars:
+            return {f"Ptr{{{scalars[base]}}}"}
+        if base in ("void", "fvm_mesh", "fvm_problem", "fvm_system", "fvm_template", "fvm_batch", "fvm_adjoint"):
+            return {"Ptr{Cvoid}"}
+        return {"Ref{" + {v: k for k, v in JULIA_STRUCTS.items()}[base] + "}"}  # a struct, passed by reference
+    return {scalars[c]}
+
+
+def test_julia_ccalls_match_the_header_prototypes():
+    """Each ccall of the Julia binding passes as many arguments as the C prototype has, each of a
+    Julia type that the C parameter type takes."""
+    protos = _c_prototypes()
+    text = JULIA.read_text()
+    calls = re.findall(r"ccall\(\(:(fvm_\w+), libfvmgpu\), Cint,\s*\(([^()]*(?:\([^()]*\)[^()]*)*)\)", text)
+    assert len(calls) >= 12
+    for name, types in calls:
+        jt = [t.strip() for t in re.split(r",(?![^{]*\})", types) if t.strip()]
+        ct = protos[name]
+        assert len(jt) == len(ct), (name, jt, ct)
+        for j, c in zip(jt, ct):
+            assert j in _julia_type(c), (name, j, c)
