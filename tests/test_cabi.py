@@ -189,3 +189,32 @@ def test_julia_ccalls_match_the_header_prototypes():
         assert len(jt) == len(ct), (name, jt, ct)
         for j, c in zip(jt, ct):
             assert j in _julia_type(c), (name, j, c)
+
+
+def test_ctypes_signatures_match_the_header_prototypes():
+    """Each ctypes signature has the C prototype's arity, an int result, and an argument type the
+    C parameter type takes (pointers as typed pointers or void pointers)."""
+    from fvmgpu import _lib
+
+    scalars = {"double": ctypes.c_double, "int32_t": ctypes.c_int32, "int64_t": ctypes.c_int64,
+               "size_t": ctypes.c_size_t, "int": ctypes.c_int, "int8_t": ctypes.c_int8, "char": ctypes.c_char}
+    structs = {c: getattr(_lib, p) for c, p in STRUCTS.items()}
+    for name, ctypes_ in _c_prototypes().items():
+        res, args = _lib.SIGNATURES[name]
+        assert res is ctypes.c_int, name
+        assert len(args) == len(ctypes_), name
+        for a, c in zip(args, ctypes_):
+            c = c.replace("const ", "")
+            if c.endswith("**"):
+                ok = a is ctypes.c_void_p or a == ctypes.POINTER(ctypes.c_void_p)
+            elif c.endswith("*"):
+                base = c[:-1]
+                allowed = {ctypes.c_void_p, ctypes.c_char_p}
+                if base in scalars:
+                    allowed.add(ctypes.POINTER(scalars[base]))
+                if base in structs:
+                    allowed.add(ctypes.POINTER(structs[base]))
+                ok = a in allowed
+            else:
+                ok = a is scalars[c]
+            assert ok, (name, a, c)
