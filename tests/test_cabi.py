@@ -218,3 +218,43 @@ def test_ctypes_signatures_match_the_header_prototypes():
             else:
                 ok = a is scalars[c]
             assert ok, (name, a, c)
+
+
+C_CALLER = r"""
+#include <stdio.h>
+#include <string.h>
+#include "fvm_gpu.h"
+/* A plain C11 caller: the header compiles as C and the library links with C linkage. */
+int main(void) {
+    int n = -1;
+    char msg[256];
+    fvm_mesh* mesh = NULL;
+    fvm_system* sys = NULL;
+    fvm_system_desc sd;
+    memset(&sd, 0, sizeof sd);
+    if (fvm_version() < 10000) return 10;
+    if (fvm_device_count(&n) != FVM_OK || n < 0) return 11;
+    if (fvm_mesh_create(NULL, 0, NULL, 0, NULL, NULL, 0, 0, 0, &mesh) != FVM_ERR_INVALID_ARGUMENT) return 12;
+    if (fvm_last_error(msg, sizeof msg) != FVM_OK || msg[0] == 0) return 13;
+    if (fvm_system_create(NULL, &sd, &sys) != FVM_ERR_INVALID_ARGUMENT || sys != NULL) return 14;
+    if (fvm_system_rhs(NULL, NULL, NULL, 0.0, FVM_PTR_HOST, NULL) != FVM_ERR_INVALID_ARGUMENT) return 15;
+    if (fvm_system_destroy(NULL) != FVM_OK) return 16;
+    printf("ok %d\n", n);
+    return 0;
+}
+"""
+
+
+def test_plain_c_caller_compiles_links_and_gets_statuses(tmp_path):
+    """A C11 program that includes only include/fvm_gpu.h links against libfvmgpu.so and gets
+    status codes and messages back, without a GPU (argument checks come before device work)."""
+    from fvmgpu import _build
+
+    lib = _build.build()
+    src = tmp_path / "caller.c"
+    src.write_text(C_CALLER)
+    exe = tmp_path / "caller"
+    subprocess.run(["gcc", "-std=c11", "-Wall", "-Werror", f"-I{HEADER.parent}", str(src), str(lib),
+                    f"-Wl,-rpath,{lib.parent}", "-o", str(exe)], check=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0 and r.stdout.startswith("ok"), (r.returncode, r.stdout, r.stderr)
