@@ -291,12 +291,15 @@ def classify_system_poly(f, x, y, t0, N, what, max_degree=_SYS_DEGREE):
     else:
         coef = np.zeros((0, Fu.shape[1]))
     # a fitted coefficient that is one value up to the fit's rounding at every point (it does
-    # not depend on (x, y) while another coefficient does; measured spreads stay below 1e-13
-    # relative) is set to that one value, so the library can keep it as a scalar
+    # not depend on (x, y) while another coefficient does) is set to that one value, so the
+    # library can keep it as a scalar.  The fit's noise scales with the polynomial's largest
+    # coefficients (measured below 2e-15 of them), so the test is against that scale; the
+    # change is at most 1e-13 of it.
+    big = max(np.max(np.abs(coef), initial=0.0), np.max(np.abs(c0), initial=0.0))
     for k in range(coef.shape[0]):
         row = coef[k]
         lo, hi = row.min(initial=np.inf), row.max(initial=-np.inf)
-        if row.size and hi - lo <= 1e-13 * max(abs(lo), abs(hi)):
+        if row.size and hi - lo <= 1e-13 * big:
             row[:] = np.median(row)
     if np.any(c0 != 0):
         exps = np.vstack([exps[:1], rest])

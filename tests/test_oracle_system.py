@@ -356,3 +356,42 @@ def test_decoupled_system_equals_its_single_problems():
         assert np.max(np.abs(du[c] - ref) / (np.abs(ref) + scale + 1e-300)) < 1e-13
         assert np.array_equal(ud[c], O.update_dirichlet_nodes(probs[c], u[c], 0.0))
         assert np.array_equal(sys.code[c], probs[c].code)
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_classify_recovers_random_polynomials(seed):
+    """Seeded random polynomials of total degree <= 3 in N <= 4 components, some coefficients
+    depending on (x, y), others constant: the classifier returns exactly their monomials, the
+    coefficients to 1e-12, and the constant ones as one value at every point."""
+    rng = np.random.default_rng(100 + seed)
+    N = int(rng.integers(1, 5))
+    basis = forms.monomials(N)
+    pick = rng.choice(basis.shape[0], size=int(rng.integers(1, min(6, basis.shape[0]) + 1)), replace=False)
+    terms = []
+    for k in pick:
+        if rng.random() < 0.5:
+            c0 = float(rng.normal())
+            terms.append((tuple(basis[k]), lambda x, y, c0=c0: c0 + 0.0 * x, True))
+        else:
+            a, b = rng.normal(size=2)
+            terms.append((tuple(basis[k]), lambda x, y, a=a, b=b: a * x + b * y * y + 1.0, False))
+
+    def f(x, y, t, u):
+        out = 0.0 * x
+        for e, c, _ in terms:
+            m = c(x, y)
+            for q, k in enumerate(e):
+                m = m * u[q] ** k
+            out = out + m
+        return out
+
+    x = rng.uniform(-1, 1, 300)
+    y = rng.uniform(-1, 1, 300)
+    e, c = forms.classify_system_poly(f, x, y, 0.0, N, "random")
+    got = {tuple(k): c[:, m] for m, k in enumerate(e)}
+    assert set(got) == {t[0] for t in terms}
+    for ek, cf, const in terms:
+        ref = cf(x, y)
+        assert np.max(np.abs(got[ek] - ref)) <= 1e-12 * max(1.0, np.max(np.abs(ref))), ek
+        if const:
+            assert np.unique(got[ek]).size == 1, ek
