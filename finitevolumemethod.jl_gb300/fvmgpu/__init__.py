@@ -10,7 +10,8 @@ from .api import (ConditionType, Neumann, Dudt, Dirichlet, Constrained, Parametr
                   update_dirichlet_nodes, DiffusionEquation, LinearReactionDiffusionEquation, PoissonsEquation,
                   MeanExitTimeProblem, Tsit5, KrylovSolver, ODESolution, LinearSolution, solve, BatchedProblem,
                   AdjointProblem, solve_rrule, FVMSystem, InvalidFluxError,
-                  jacobian_sparsity, compute_flux, pl_interpolate, two_point_interpolant)
+                  jacobian_sparsity, compute_flux, pl_interpolate, two_point_interpolant,
+                  construct_flux_function)
 from ._lib import FVMError, UnsupportedFormError, NotConvergedError
 from ._build import build, lib_path
 
@@ -21,6 +22,6 @@ __all__ = [
     "update_dirichlet_nodes", "DiffusionEquation", "LinearReactionDiffusionEquation", "PoissonsEquation",
     "MeanExitTimeProblem", "Tsit5", "KrylovSolver", "ODESolution", "LinearSolution", "solve", "BatchedProblem",
     "disjoint_union", "AdjointProblem", "solve_rrule", "FVMSystem", "InvalidFluxError", "jacobian_sparsity", "compute_flux", "pl_interpolate",
-    "two_point_interpolant", "FVMError",
+    "two_point_interpolant", "construct_flux_function", "FVMError",
     "UnsupportedFormError", "NotConvergedError", "build", "lib_path",
 ]

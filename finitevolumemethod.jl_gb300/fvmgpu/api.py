@@ -535,21 +535,28 @@ def _stored_abg(prob, t, u):
     return tuple(s[3 * m] * u[a] + s[3 * m + 1] * u[b] + s[3 * m + 2] * u[c] for m in range(3))
 
 
-def _flux_closures(prob):
-    """The flux closure(s) q(x, y, t, alpha, beta, gamma) of a problem or system, with the
-    diffusion form q = -D(x, y, t, alpha x + beta y + gamma) (alpha, beta) when the problem was
-    given a diffusion function (construct_flux_function, src/problem.jl:425-440)."""
-    if hasattr(prob, "flux_functions"):  # FVMSystem
-        return list(prob.flux_functions)
-    if prob.flux_function is not None:
-        return ParametrisedFunction(prob.flux_function, prob.flux_parameters)
-    D = ParametrisedFunction(prob.diffusion_function, prob.diffusion_parameters)
+def construct_flux_function(q, D, Dp):
+    """construct_flux_function(q, D, Dp) (src/problem.jl:425-440): q itself when given, else the
+    flux of the diffusion function D with parameters Dp,
+    (x, y, t, alpha, beta, gamma, p) -> -D(x, y, t, alpha x + beta y + gamma, Dp) (alpha, beta)."""
+    if q is not None:
+        return q
 
-    def q(x, y, t, a, b, g):
-        d = D(x, y, t, a * x + b * y + g)
+    def flux(x, y, t, a, b, g, p):
+        u = a * x + b * y + g
+        d = D(x, y, t, u, Dp)
         return (-d * a, -d * b)
 
-    return q
+    return flux
+
+
+def _flux_closures(prob):
+    """The flux closure(s) q(x, y, t, alpha, beta, gamma) of a problem (construct_flux_function
+    with its parameters bound) or a list of them for a system."""
+    if hasattr(prob, "flux_functions"):  # FVMSystem
+        return list(prob.flux_functions)
+    q = construct_flux_function(prob.flux_function, prob.diffusion_function, prob.diffusion_parameters)
+    return ParametrisedFunction(q, prob.flux_parameters)
 
 
 def compute_flux(prob, i, j, u, t):

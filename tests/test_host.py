@@ -149,3 +149,20 @@ def test_problems_and_system_conditions_without_a_device():
     # component tables: Phi is Neumann on three sides and Dirichlet on the top, Psi the reverse pattern
     assert len(conds[0].dirichlet_nodes) == 10 and len(conds[1].dirichlet_nodes) == 19
     assert len(conds[0].neumann_edges) == 27 and len(conds[1].neumann_edges) == 18
+
+
+def test_construct_flux_function():
+    """test/problem.jl:152-160: a given flux is returned as it is; otherwise the diffusion flux
+    -D(x, y, t, alpha x + beta y + gamma, Dp) (alpha, beta)."""
+    import numpy as np
+
+    import fvmgpu as F
+
+    q = lambda x, y, t, a, b, g, p: (a, b)  # noqa: E731
+    assert F.construct_flux_function(q, None, None) is q
+    D = lambda x, y, t, u, p: x + y + t + u + p[1]  # noqa: E731
+    Dp = (0.2, 5.73)
+    _q = F.construct_flux_function(None, D, Dp)
+    x, y, t, a, b, g = np.random.default_rng(3).random(6)
+    u = a * x + b * y + g
+    assert _q(x, y, t, a, b, g, None) == (-a * D(x, y, t, u, Dp), -b * D(x, y, t, u, Dp))
