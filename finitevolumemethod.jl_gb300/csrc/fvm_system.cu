@@ -250,7 +250,8 @@ static int system_bucket(int N, int maxw) {
 
 template <int N, int MAXW, bool VEC, bool SH>
 static void launch_system_shape(const SysArgs& a, const SysTerms& tm, int64_t nslices, cudaStream_t s) {
-    // 8 warps per block; the grid covers every slice at most once, capped at 8 blocks per SM
+    // 8 warps per block, one warp per slice up to 8 blocks for each of the 152 SMs; beyond that
+    // the warps stride over the slices
     const unsigned grid = (unsigned)std::min<int64_t>((nslices + 7) / 8, 152 * 8);
     system_rhs_kernel<N, MAXW, VEC, SH><<<grid, 256, 0, s>>>(a, tm);
 }
