@@ -154,20 +154,28 @@ _SYS_DEGREE = 3
 
 
 def evaluate_tuples(f, x, y, t, *tuples):
-    """Call f(x, y, t, T1, T2, ...) whose Ti are N-tuples of arrays over the points; one call
-    per point, with tuples of floats, when the closure does not accept arrays."""
+    """Call f(x, y, t, T1, T2, ...) whose Ti are N-tuples of values (scalars, the same at every
+    point, or arrays over the points).  Scalars are passed as scalars first, so work that does
+    not depend on the point is done once; a closure that needs arrays gets them broadcast; one
+    that takes neither is called once per point with tuples of floats."""
     x = np.asarray(x, dtype=np.float64)
     n = x.shape[0]
     y = np.broadcast_to(np.asarray(y, dtype=np.float64), (n,))
     T = [tuple(np.broadcast_to(np.asarray(c, dtype=np.float64), (n,)) for c in tup) for tup in tuples]
-    try:
-        with np.errstate(all="ignore"):
-            out = f(x, y, t, *T)
-        if isinstance(out, tuple):
-            return tuple(np.broadcast_to(np.asarray(o, dtype=np.float64), (n,)).copy() for o in out)
-        return np.broadcast_to(np.asarray(out, dtype=np.float64), (n,)).copy()
-    except (ValueError, TypeError, IndexError):
-        pass
+    attempts = []
+    if any(np.ndim(c) == 0 for tup in tuples for c in tup):
+        attempts.append([tuple(np.float64(c) if np.ndim(c) == 0 else Tc for c, Tc in zip(tup, Ttup))
+                         for tup, Ttup in zip(tuples, T)])
+    attempts.append(T)
+    for args in attempts:
+        try:
+            with np.errstate(all="ignore"):
+                out = f(x, y, t, *args)
+            if isinstance(out, tuple):
+                return tuple(np.broadcast_to(np.asarray(o, dtype=np.float64), (n,)).copy() for o in out)
+            return np.broadcast_to(np.asarray(out, dtype=np.float64), (n,)).copy()
+        except (ValueError, TypeError, IndexError):
+            pass
     res = None
     for m in range(n):
         r = f(float(x[m]), float(y[m]), t, *[tuple(float(c[m]) for c in tup) for tup in T])
@@ -209,10 +217,10 @@ def classify_system_flux(q, x, y, t0, N, what="flux_function"):
     verifies one seeded combination at a second time."""
     x = np.asarray(x, dtype=np.float64)
     n = x.shape[0]
-    zero = tuple(np.zeros(n) for _ in range(N))
+    zero = (0.0,) * N
 
     def unit(c, v=1.0):
-        return tuple(np.full(n, v if k == c else 0.0) for k in range(N))
+        return tuple(v if k == c else 0.0 for k in range(N))
 
     def ev(a, b, g, t=t0):
         try:
@@ -231,14 +239,15 @@ def classify_system_flux(q, x, y, t0, N, what="flux_function"):
         bx, by = ev(zero, unit(c), zero)
         gx, gy = ev(zero, zero, unit(c))
         D[c] = -ax
-        sc = np.maximum(np.abs(D[c]), 1e-300)
-        ok = ok and all(np.all(np.abs(v) <= _RTOL * sc) for v in (ay, bx, gx, gy, zx, zy))
-        ok = ok and np.all(np.abs(by + D[c]) <= _RTOL * sc)
+        # every probe output that must vanish, and by + D, against the one tolerance
+        worst = np.abs(by + D[c])
+        for v in (ay, bx, gx, gy, zx, zy):
+            np.maximum(worst, np.abs(v), out=worst)
+        ok = ok and bool(np.all(worst <= _RTOL * np.maximum(np.abs(D[c]), 1e-300)))
     if ok and np.all(np.isfinite(D)):
         rng = np.random.default_rng(7)
         A, B, G = (rng.uniform(-2.0, 2.0, N) for _ in range(3))
-        cx, cy = ev(tuple(np.full(n, v) for v in A), tuple(np.full(n, v) for v in B),
-                    tuple(np.full(n, v) for v in G), t0 + 1.37)
+        cx, cy = ev(tuple(float(v) for v in A), tuple(float(v) for v in B), tuple(float(v) for v in G), t0 + 1.37)
         sc = np.maximum(np.abs(D).sum(axis=0), 1e-300) * 2.0
         ok = (np.all(np.abs(cx + (A[:, None] * D).sum(axis=0)) <= _RTOL * sc)
               and np.all(np.abs(cy + (B[:, None] * D).sum(axis=0)) <= _RTOL * sc))
@@ -267,7 +276,7 @@ def classify_system_poly(f, x, y, t0, N, what, max_degree=_SYS_DEGREE):
 
     def ev(u, t=t0):
         try:
-            v = evaluate_tuples(f, x, y, t, tuple(np.full(n, c) for c in u))
+            v = evaluate_tuples(f, x, y, t, tuple(float(c) for c in u))
         except Exception as e:  # noqa: BLE001
             _reject_sys(what, f"evaluation failed ({e!r})")
         if isinstance(v, tuple) or not np.all(np.isfinite(v)):
