@@ -1,4 +1,5 @@
-"""Generates tests/golden/c1_readme.npz: frozen oracle outputs for the README diffusion problem
+"""Generates tests/golden/c1_readme.npz (and system_gray_scott.npz, see compute_system): frozen
+oracle outputs for the README diffusion problem
 (test/README.jl:4-15 of the reference: triangulate_rectangle(0, 2, 0, 2, 50, 50,
 single_boundary=true), zero Dirichlet, D = 1/9, u0 = 50 where y <= 1 else 0).
 
@@ -24,7 +25,7 @@ sys.path[:0] = [os.path.join(ROOT, "oracle"), os.path.join(ROOT, "tests"),
                 os.path.join(ROOT, "finitevolumemethod.jl_gb300")]
 
 import fvm_oracle as O  # noqa: E402
-from problems import oracle_problem, readme_diffusion  # noqa: E402
+from problems import gray_scott_oracle, oracle_problem, readme_diffusion  # noqa: E402
 
 T_SAVE = [0.01, 0.1, 0.25, 0.5]
 
@@ -41,5 +42,20 @@ def compute():
             "u_save": np.array(snaps), "naccept": np.array(st["naccept"]), "nreject": np.array(st["nreject"])}
 
 
+def compute_system():
+    """tests/golden/system_gray_scott.npz: the Gray-Scott tutorial FVMSystem (tests/problems.py:
+    gray_scott_oracle) on 30 x 30.  u_rand (seed 21) and system fvm_eqs! of it; du_u0 of the
+    initial condition; u_save at t_save from fixed-step Tsit5 (dt = 1) started at u0."""
+    sys_ = gray_scott_oracle(30)
+    u_rand = np.random.default_rng(21).random(sys_.u0.shape)
+    t_save = np.array([0.0, 5.0, 20.0])
+    snaps, _ = O.tsit5_solve(lambda u, t: O.system_fvm_eqs(sys_, u, t), sys_.u0, 0.0, 20.0, list(t_save), dt=1.0,
+                             adaptive=False)
+    return {"u_rand": u_rand, "du_rand": O.system_fvm_eqs(sys_, u_rand, 0.0),
+            "du_u0": O.system_fvm_eqs(sys_, sys_.u0, 0.0), "t_save": t_save, "u_save": np.array(snaps)}
+
+
 if __name__ == "__main__":
-    np.savez_compressed(os.path.join(os.path.dirname(os.path.abspath(__file__)), "c1_readme.npz"), **compute())
+    here = os.path.dirname(os.path.abspath(__file__))
+    np.savez_compressed(os.path.join(here, "c1_readme.npz"), **compute())
+    np.savez_compressed(os.path.join(here, "system_gray_scott.npz"), **compute_system())

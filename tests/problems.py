@@ -195,3 +195,19 @@ def wheel_diffusion(nspoke=40) -> Spec:
 
 def disk_poisson_mesh(n_interior=3000, n_boundary=128, seed=0):
     return triangulate_disk(n_interior, n_boundary, seed=seed)
+
+
+# ---- Gray-Scott tutorial system (docs/src/literate_tutorials/gray_scott_model_turing_patterns_...) ----
+def gray_scott_oracle(n=30):
+    """The tutorial's FVMSystem for the oracle on an n x n mesh of [-1, 1]^2: zero Neumann on the
+    whole boundary, fluxes -eps_c grad u_c (eps = 2e-5, 1e-5), sources b (1 - u) - u v^2 and
+    -d v + u v^2 (b = 0.04, d = 0.1), initial bump exp(-80 r^2)."""
+    tri = triangulate_rectangle(-1.0, 1.0, -1.0, 1.0, n, n, single_boundary=True)
+    bc = lambda x, y, t, u: 0.0 * x  # noqa: E731
+    conds = [O.Conditions(tri, [bc], ["Neumann"]) for _ in range(2)]
+    fluxes = [lambda x, y, t, a, b, g: (-a[0] * 2e-5, -b[0] * 2e-5), lambda x, y, t, a, b, g: (-a[1] * 1e-5, -b[1] * 1e-5)]
+    sources = [lambda x, y, t, u: 0.04 * (1 - u[0]) - u[0] * u[1] ** 2, lambda x, y, t, u: -0.1 * u[1] + u[0] * u[1] ** 2]
+    P = tri.points
+    r2 = P[:, 0] ** 2 + P[:, 1] ** 2
+    u0 = np.stack([1 - np.exp(-80 * r2), np.exp(-80 * r2)])
+    return O.System(tri, conds, fluxes, sources, u0=u0, tf=6000.0)

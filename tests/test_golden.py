@@ -42,3 +42,40 @@ def test_gpu_matches_fixture(gpu_lib):
     sol = F.solve(prob, F.Tsit5(), saveat=list(g["t_save"]))
     assert sol.stats["naccept"] == int(g["naccept"]) and sol.stats["nreject"] == int(g["nreject"])
     assert np.max(np.abs(np.array(sol.u) - g["u_save"])) <= 1e-8 * 50.0
+
+
+SYSTEM_GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "system_gray_scott.npz")
+
+
+def test_oracle_reproduces_system_fixture():
+    """tests/golden/system_gray_scott.npz (the Gray-Scott tutorial FVMSystem on 30 x 30): the
+    oracle's system restatement still gives the frozen RHS values and fixed-step solution."""
+    from problems import gray_scott_oracle
+
+    g = np.load(SYSTEM_GOLDEN)
+    sys_ = gray_scott_oracle(30)
+    for u, du in ((g["u_rand"], g["du_rand"]), (sys_.u0, g["du_u0"])):
+        got = O.system_fvm_eqs(sys_, u, 0.0)
+        for c in range(2):
+            assert np.max(np.abs(got[c] - du[c])) <= 1e-14 * np.max(np.abs(du[c]))
+    snaps, _ = O.tsit5_solve(lambda u, t: O.system_fvm_eqs(sys_, u, t), sys_.u0, 0.0, 20.0, list(g["t_save"]),
+                             dt=1.0, adaptive=False)
+    assert np.max(np.abs(np.array(snaps) - g["u_save"])) <= 1e-14
+
+
+@pytest.mark.gpu
+def test_gpu_matches_system_fixture(gpu_lib):
+    import fvmgpu as F
+    from test_gpu_system import gray_scott
+
+    g = np.load(SYSTEM_GOLDEN)
+    spec = gray_scott(30)
+    spec.tf = 20.0  # the fixture's end time
+    sys_ = spec.api()
+    for u, du in ((g["u_rand"], g["du_rand"]), (spec.u0, g["du_u0"])):
+        got = np.empty_like(u)
+        sys_.rhs(got, np.ascontiguousarray(u), 0.0)
+        for c in range(2):
+            assert np.max(np.abs(got[c] - du[c])) <= 1e-12 * np.max(np.abs(du[c]))
+    sol = F.solve(sys_, F.Tsit5(), saveat=list(g["t_save"]), dt=1.0, adaptive=False)
+    assert np.max(np.abs(np.array(sol.u) - g["u_save"])) <= 1e-11
