@@ -56,6 +56,8 @@ def load():
         lib.orc_rhs_threaded.argtypes = [C.POINTER(OrcProblem), C.c_void_p, C.c_void_p, C.c_double, C.c_int,
                                          C.c_void_p]
         lib.orc_max_threads.restype = C.c_int
+        lib.orc_steady_bicgstab.argtypes = [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                            C.c_double, C.c_int64, C.c_int, C.c_void_p, C.c_void_p]
         lib.orc_gray_scott_rhs_threaded.argtypes = [C.POINTER(OrcProblem), C.POINTER(GrayScott), C.c_void_p,
                                                     C.c_void_p, C.c_int, C.c_void_p]
         _lib = lib
@@ -130,6 +132,31 @@ class CGrayScott(CProblem):
             return dt.T.copy()
         du[...] = dt.T
         return du
+
+
+def steady_bicgstab(A, b, rtol=1e-10, maxit=200_000, nthreads=0):
+    """Jacobi-preconditioned FP64 BiCGStab on the host threads for the CSR matrix A (the CPU
+    baseline of the steady templates); returns (x, {"iterations", "rel_residual", "converged",
+    "seconds", "threads"})."""
+    import time
+
+    lib = load()
+    A = A.tocsr()
+    n = A.shape[0]
+    rp = np.ascontiguousarray(A.indptr, dtype=np.int64)
+    ci = np.ascontiguousarray(A.indices, dtype=np.int32)
+    va = np.ascontiguousarray(A.data, dtype=np.float64)
+    bb = np.ascontiguousarray(b, dtype=np.float64)
+    x = np.zeros(n)
+    work = np.empty(8 * n)
+    st = np.zeros(3)
+    nth = nthreads or lib.orc_max_threads()
+    t0 = time.perf_counter()
+    lib.orc_steady_bicgstab(n, rp.ctypes.data, ci.ctypes.data, va.ctypes.data, bb.ctypes.data, x.ctypes.data,
+                            float(rtol), int(maxit), int(nth), work.ctypes.data, st.ctypes.data)
+    dt = time.perf_counter() - t0
+    return x, {"iterations": int(st[0]), "rel_residual": float(st[1]), "converged": bool(st[2]), "seconds": dt,
+               "threads": nth}
 
 
 def max_threads() -> int:

@@ -807,13 +807,23 @@ def template_mean_exit_time(tri, conds, D):
 
 
 def _set_diag(A, idx, value):
-    """A[i, i] = value for i in idx (assignment, not accumulation)."""
-    if len(idx) == 0:
+    """A[i, i] = value for i in idx (assignment, not accumulation).  Stored diagonal entries of
+    those rows are overwritten and missing ones are added, so the result is exactly `value`
+    whatever was accumulated there before."""
+    from scipy.sparse import coo_matrix
+
+    idx = np.unique(np.asarray(idx, dtype=np.int64))
+    if idx.size == 0:
         return A
-    A = A.tolil()
-    for i in idx:
-        A[i, i] = value
-    return A.tocsr()
+    M = A.tocoo()
+    on = (M.row == M.col) & np.isin(M.row, idx)
+    data = M.data.copy()
+    data[on] = value
+    missing = np.setdiff1d(idx, M.row[on])
+    r = np.concatenate([M.row, missing])
+    c = np.concatenate([M.col, missing])
+    v = np.concatenate([data, np.full(missing.size, float(value))])
+    return coo_matrix((v, (r, c)), shape=A.shape).tocsr()
 
 
 # --------------------------------------------------------------------------------------

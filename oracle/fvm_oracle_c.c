@@ -257,6 +257,127 @@ void orc_gray_scott_rhs_threaded(const orc_problem* P, const orc_gray_scott* G, 
     }
 }
 
+/* ---- steady linear solve on the host cores (CPU baseline of the steady templates) --------
+ * The reference solves PoissonsEquation / MeanExitTimeProblem as LinearProblem(A, b)
+ * (src/specific_problems/poissons_equation.jl:81, mean_exit_time.jl:76) with a sparse direct
+ * method.  This baseline is a threaded FP64 BiCGStab with a Jacobi preconditioner (right
+ * preconditioning, van der Vorst 1992) on the CSR matrix A, stopped when the true residual
+ * ||b - A x|| / ||b|| reaches rtol: the same method and stopping test as the GPU's plain FP64
+ * solve, on all host threads.  stats = {iterations, relative residual, converged}. */
+static void csr_mv(int64_t n, const int64_t* rp, const int32_t* ci, const double* va, const double* x, double* y) {
+#pragma omp for schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+        double s = 0.0;
+        for (int64_t q = rp[i]; q < rp[i + 1]; ++q) s += va[q] * x[ci[q]];
+        y[i] = s;
+    }
+}
+
+void orc_steady_bicgstab(int64_t n, const int64_t* rp, const int32_t* ci, const double* va, const double* b, double* x,
+                         double rtol, int64_t maxit, int nthreads, double* work, double* stats) {
+#ifdef _OPENMP
+    if (nthreads <= 0) nthreads = omp_get_max_threads();
+#endif
+    double *r = work, *rh = work + n, *p = work + 2 * n, *v = work + 3 * n, *ph = work + 4 * n, *sh = work + 5 * n,
+           *t = work + 6 * n, *dinv = work + 7 * n;
+    double bn2 = 0.0;
+    for (int64_t i = 0; i < n; ++i) bn2 += b[i] * b[i];
+    const double tol = rtol * sqrt(bn2);
+    for (int64_t i = 0; i < n; ++i) {
+        double d = 0.0;
+        for (int64_t q = rp[i]; q < rp[i + 1]; ++q)
+            if (ci[q] == i) d = va[q];
+        dinv[i] = d != 0.0 ? 1.0 / d : 1.0;
+    }
+    int64_t it = 0;
+    double rn = 0.0;
+    int converged = 0;
+    /* shared scalars, written by one thread between barriers */
+    double rho = 1.0, alpha = 1.0, omega = 1.0, dot1 = 0.0, dot2 = 0.0, dot3 = 0.0;
+    int restart = 1, stop = 0;
+#pragma omp parallel num_threads(nthreads)
+    {
+        while (!stop) {
+            if (restart) {
+                csr_mv(n, rp, ci, va, x, t);
+#pragma omp single
+                dot1 = 0.0;
+#pragma omp for reduction(+ : dot1) schedule(static)
+                for (int64_t i = 0; i < n; ++i) {
+                    r[i] = b[i] - t[i];
+                    rh[i] = r[i];
+                    p[i] = v[i] = 0.0;
+                    dot1 += r[i] * r[i];
+                }
+#pragma omp single
+                {
+                    rn = sqrt(dot1);
+                    rho = alpha = omega = 1.0;
+                    restart = 0;
+                    if (rn <= tol) {
+                        converged = 1;
+                        stop = 1;
+                    } else if (it >= maxit) {
+                        stop = 1;
+                    }
+                }
+                if (stop) break;
+            }
+#pragma omp single
+            dot1 = 0.0;
+#pragma omp for reduction(+ : dot1) schedule(static)
+            for (int64_t i = 0; i < n; ++i) dot1 += rh[i] * r[i];
+            const double rho_new = dot1;
+            const double beta = (rho_new / rho) * (alpha / omega);
+#pragma omp for schedule(static)
+            for (int64_t i = 0; i < n; ++i) {
+                p[i] = r[i] + beta * (p[i] - omega * v[i]);
+                ph[i] = dinv[i] * p[i];
+            }
+            csr_mv(n, rp, ci, va, ph, v);
+#pragma omp single
+            dot2 = 0.0;
+#pragma omp for reduction(+ : dot2) schedule(static)
+            for (int64_t i = 0; i < n; ++i) dot2 += rh[i] * v[i];
+            const double al = rho_new / dot2;
+#pragma omp for schedule(static)
+            for (int64_t i = 0; i < n; ++i) {
+                r[i] = r[i] - al * v[i]; /* s */
+                sh[i] = dinv[i] * r[i];
+            }
+            csr_mv(n, rp, ci, va, sh, t);
+#pragma omp single
+            dot1 = dot2 = 0.0;
+#pragma omp for reduction(+ : dot1, dot2) schedule(static)
+            for (int64_t i = 0; i < n; ++i) {
+                dot1 += t[i] * r[i];
+                dot2 += t[i] * t[i];
+            }
+            const double om = dot2 > 0.0 ? dot1 / dot2 : 0.0;
+#pragma omp single
+            dot3 = 0.0;
+#pragma omp for reduction(+ : dot3) schedule(static)
+            for (int64_t i = 0; i < n; ++i) {
+                x[i] += al * ph[i] + om * sh[i];
+                r[i] = r[i] - om * t[i];
+                dot3 += r[i] * r[i];
+            }
+#pragma omp single
+            {
+                rho = rho_new;
+                alpha = al;
+                omega = om;
+                ++it;
+                /* recurrence converged (or broke down): confirm with the true residual */
+                if (sqrt(dot3) <= tol || !(om != 0.0) || !isfinite(dot3) || it >= maxit) restart = 1;
+            }
+        }
+    }
+    stats[0] = (double)it;
+    stats[1] = bn2 > 0 ? rn / sqrt(bn2) : rn;
+    stats[2] = (double)converged;
+}
+
 int orc_max_threads(void) {
 #ifdef _OPENMP
     return omp_get_max_threads();

@@ -211,3 +211,34 @@ def gray_scott_oracle(n=30):
     r2 = P[:, 0] ** 2 + P[:, 1] ** 2
     u0 = np.stack([1 - np.exp(-80 * r2), np.exp(-80 * r2)])
     return O.System(tri, conds, fluxes, sources, u0=u0, tf=6000.0)
+
+
+# ---- the benchmarked configurations at full size --------------------------------------------
+def c2_diffusion(n=1000) -> Spec:
+    """The 1000 x 1000 DiffusionEquation workload in FVMProblem form: triangulate_rectangle(0, 1,
+    0, 1, n, n) with its four boundary segments, zero Dirichlet on each, D = 1 + 0.5 sin(2 pi x)
+    sin(2 pi y), u0 = exp(-50 ((x - 0.5)^2 + (y - 0.5)^2))."""
+    tri = triangulate_rectangle(0.0, 1.0, 0.0, 1.0, n, n, single_boundary=False)
+    P = tri.points
+    u0 = np.exp(-50 * ((P[:, 0] - 0.5) ** 2 + (P[:, 1] - 0.5) ** 2))
+    D = lambda x, y, t, u, p: 1 + 0.5 * np.sin(2 * np.pi * x) * np.sin(2 * np.pi * y) + 0.0 * u  # noqa: E731
+    z = lambda x, y, t, u, p: 0.0 * x  # noqa: E731
+    return Spec(tri, (z,) * 4, ("Dirichlet",) * 4, (None,) * 4, D=D, u0=u0, tf=1e-4)
+
+
+def fourier_logfield(seed, sigma=0.5, modes=16):
+    """log D(x, y) = sigma sum_m a_m cos(2 pi k_m . x + phi_m) / sqrt(modes / 2) with a_m ~ N(0, 1),
+    k_m integer in [1, 4]^2, phi_m ~ U[0, 2 pi), drawn in that order from default_rng(seed): the
+    log-normal diffusivity of the batched workload, as a closure of (x, y)."""
+    rng = np.random.default_rng(seed)
+    a = rng.standard_normal(modes)
+    k = rng.integers(1, 5, size=(modes, 2))
+    ph = rng.uniform(0, 2 * np.pi, modes)
+
+    def logD(x, y):
+        x, y = np.asarray(x, dtype=np.float64), np.asarray(y, dtype=np.float64)
+        s = np.zeros(np.broadcast(x, y).shape)
+        for m in range(modes):
+            s = s + a[m] * np.cos(2 * np.pi * (k[m, 0] * x + k[m, 1] * y) + ph[m])
+        return sigma * s / np.sqrt(modes / 2)
+    return logD

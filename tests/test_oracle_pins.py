@@ -371,3 +371,18 @@ def test_nonlinear_and_mixed_oracle_consistency():
         prob = oracle_problem(spec)
         u = spec.u0
         assert isapprox(O.fvm_eqs(prob, u, 0.3), O.fvm_eqs_loop(prob, u, 0.3), 1e-13)
+
+
+def test_set_diag_assigns_like_a_dense_matrix():
+    """The oracle's A[i, i] = value on a sparse matrix equals the assignment on the dense
+    matrix, for rows with and without a stored diagonal entry."""
+    from scipy.sparse import random as sprandom
+
+    A = sprandom(60, 60, density=0.1, format="csr", random_state=3)
+    A.setdiag(np.where(np.arange(60) % 3 == 0, 0.0, 2.5))
+    A.eliminate_zeros()
+    idx = np.array([0, 3, 4, 5, 17, 18, 59, 4])
+    ref = A.toarray()
+    ref[idx, idx] = 1.0
+    got = O._set_diag(A, idx, 1.0)
+    assert np.array_equal(got.toarray(), ref)
