@@ -56,6 +56,7 @@ struct DBuf {
 
 // ---- sliced-ELL operator (slice height 32, one warp per slice, column-major slots) ----
 constexpr int kSlice = 32;
+constexpr int kSteadyWindow = 1024;  // rows sorted by length within windows of this many rows
 
 struct SellPattern {
     int64_t nrows = 0, nslices = 0, nslots = 0, nnz = 0;
@@ -147,20 +148,29 @@ struct fvm_template {
     int kind = 0;
     fvm::DBuf d_val64, d_val32, d_b, d_u32;
     std::vector<double> val, b;                 // SELL values (internal), b internal
-    // steady solve (reduced SPD-like system on free rows)
+    // steady solve: the reduced system B z = rhs on the free rows (fixed rows are identity
+    // rows), on its own row order: the mesh order with rows sorted by length (longest first)
+    // within windows of kSteadyWindow rows, and entries that vanish (eliminated columns)
+    // dropped, so slices are nearly full and mostly take the unrolled eight-slot path
     bool steady_ready = false;
     int symmetric = 0;
     double bnorm = 0;
     double cheb_gershgorin = 0;                  // Gershgorin bound on the spectrum of D^-1 B
-    fvm::DBuf d_bval64, d_bdiag_inv64, d_bdiag_inv32, d_rhs_red;  // reduced operator B (explicit), rhs
-    fvm::DBuf d_bval32, d_brow32;                // FP32 B in difference form: off-diagonal values, row sums
-    fvm::DBuf d_bval32x;                         // FP32 B, explicit (the FP32-stored preconditioner operator)
+    fvm::SellPattern spat;                       // pattern of B, solver order
+    std::vector<int32_t> sperm;                  // solver row -> caller index
+    fvm::DBuf d_sperm;
+    fvm::DBuf d_bval64, d_bval32;                // B explicit (FP64, FP32)
+    fvm::DBuf d_brow64, d_brow32;                // row sums of B, compensated, for the difference form
+    fvm::DBuf d_bdiag_inv64, d_bdiag_inv32, d_rhs_red;
     fvm::DBuf d_xfix, d_invV_free64, d_invV_free32;
     fvm::DBuf d_fixed_mask;                      // 1 on rows fixed by Dirichlet / missing vertex
     void build_steady();
 };
 
 namespace fvm {
+// Sliced ELL from a pattern's CSR view (rowptr, csr_col): slices of 32 rows, width = longest
+// row of the slice, slots column-major, padding slots pointing at the row itself (fvm_mesh.cpp)
+void finalize_sell(SellPattern& pat, int64_t nrows);
 // kernels (fvm_kernels.cu)
 void launch_sell_apply64(const SellPattern& p, const double* val, const double* x, double* y,
                          const double* rowscale, const double* b, const double* q, cudaStream_t s);

@@ -96,7 +96,7 @@ static inline uint64_t edge_key(int64_t a, int64_t b) { return ((uint64_t)(uint3
 
 // Sliced ELL from the CSR view (rowptr, csr_col): slices of 32 rows, width = longest row in the
 // slice, slots column-major; padding slots point at the row itself with value 0.
-static void finalize_sell(SellPattern& pat, int64_t nrows) {
+void fvm::finalize_sell(SellPattern& pat, int64_t nrows) {
     pat.nnz = (int64_t)pat.csr_col.size();
     pat.nslices = (nrows + kSlice - 1) / kSlice;
     pat.slice_ptr.assign(pat.nslices + 1, 0);

@@ -1277,16 +1277,19 @@ class Tsit5:
 class KrylovSolver:
     """GPU steady solver: method "auto" (CG if symmetric, else BiCGStab), "cg", "bicgstab";
     precond "jacobi" or "chebyshev" (a degree-`cheb_degree` Chebyshev polynomial in the
-    Jacobi-scaled operator); mode "fp64", "mixed" (the Krylov iteration in FP32 with FP64
-    reliable updates of the residual and solution) or "fp32_precond" (FP64 Krylov iteration
-    and arithmetic; the Chebyshev preconditioner reads its operator values stored in FP32, a
-    third less operator traffic per preconditioner step)."""
+    Jacobi-scaled operator); mode "fp64", "mixed" or "fp32_precond".  "mixed" with the
+    Chebyshev preconditioner runs the Krylov iteration in FP64 and evaluates the polynomial in
+    FP32 (values, vectors, difference-form products); with Jacobi it runs FP32 Krylov cycles,
+    each reducing the residual by `inner_reduction`, folded into the FP64 solution.
+    "fp32_precond": FP64 iteration and arithmetic, the polynomial reading FP32-stored values.
+    The stopping test is ||b - A x|| / ||b|| <= rtol for the FP64 solution, evaluated in FP64
+    in difference form with compensated row sums."""
 
     mode: str = "fp64"
     method: str = "auto"
     rtol: float = 1e-10
     max_iters: int = 1_000_000
-    inner_reduction: float = 1e-1
+    inner_reduction: float = 1e-3
     precond: str = "jacobi"
     cheb_degree: int = 4
 
