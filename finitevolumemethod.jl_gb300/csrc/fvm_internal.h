@@ -96,6 +96,7 @@ struct Tiles {
 
 struct fvm_mesh {
     int64_t np = 0, nt = 0, nbe = 0, nv = 0;   // points, triangles, boundary edges, vertices
+    int device = -1;                            // device current at creation (holds the arrays)
     std::vector<double> pts;                    // [2*np] caller order
     std::vector<int32_t> tri;                   // [3*nt]
     std::vector<int32_t> be;                    // [2*nbe]

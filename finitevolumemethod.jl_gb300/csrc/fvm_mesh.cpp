@@ -146,6 +146,7 @@ extern "C" int fvm_mesh_create_impl(const double* points, int64_t npoints, const
     if (!points || !triangles || (nbedge > 0 && !boundary_edges)) fail(FVM_ERR_INVALID_ARGUMENT, "NULL mesh array");
     if (npoints >= (int64_t)INT32_MAX || ntri >= (int64_t)INT32_MAX) fail(FVM_ERR_INVALID_ARGUMENT, "mesh too large for 32-bit indices");
     std::unique_ptr<fvm_mesh> m(new fvm_mesh());
+    FVM_CUDA(cudaGetDevice(&m->device));
     m->np = npoints;
     m->nt = ntri;
     m->nbe = nbedge;

@@ -2,11 +2,11 @@
 //
 // fvm_rhs with device arrays in the caller's numbering stages u and du through two work
 // vectors in the library's internal numbering, and allocates them with cudaMalloc the first
-// time.  Some callers cannot let that happen: code running while a CUDA graph is being
-// captured (cudaMalloc is not a capturable operation), real-time loops whose allocator is
-// frozen after start-up, and hosts that hand all device memory to their own pool.  This
-// entry point uses a fixed scratch area compiled into the library instead, so a call makes no
-// cudaMalloc, cudaFree or other allocating call.
+// time.  Some callers cannot let that happen: real-time loops whose allocator is frozen after
+// start-up, and hosts that hand all device memory to their own pool, where a cudaMalloc
+// behind the pool's back fails or fragments it.  This entry point uses a fixed scratch area
+// compiled into the library instead, so a call makes no cudaMalloc, cudaFree or other
+// allocating call.
 //
 // The scratch lives in a file-scope __device__ array sized for FVM_NOALLOC_MAX_POINTS points
 // (2 x 262,144 doubles = 4 MiB).  Every GPU that loads the library holds it until the
@@ -50,6 +50,12 @@ extern "C" int fvm_rhs_noalloc(fvm_problem* p, const double* u, double* du, doub
         if (!p || !u || !du) fvm::fail(FVM_ERR_INVALID_ARGUMENT, "NULL argument");
         (void)t;  // device-coded forms are time independent
         const fvm_mesh* m = p->mesh;
+        int dev = -1;
+        FVM_CUDA(cudaGetDevice(&dev));
+        if (dev != m->device)
+            fvm::fail(FVM_ERR_INVALID_ARGUMENT, "fvm_rhs_noalloc: the mesh was created on device " +
+                                               std::to_string(m->device) + ", the current device is " +
+                                               std::to_string(dev));
         if (m->np > FVM_NOALLOC_MAX_POINTS)
             fvm::fail(FVM_ERR_INVALID_ARGUMENT, "fvm_rhs_noalloc handles at most " +
                                                     std::to_string(FVM_NOALLOC_MAX_POINTS) + " points; this mesh has " +

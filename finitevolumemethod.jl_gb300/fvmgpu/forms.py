@@ -265,7 +265,9 @@ def classify_system_poly(f, x, y, t0, N, what, max_degree=_SYS_DEGREE):
     The closure is evaluated at seeded sample tuples u (the same at every point), the
     coefficients fitted by least squares on the full monomial basis (the constant term exactly,
     from u = 0), the monomials whose coefficients vanish dropped and the rest refitted; the fit
-    is then verified at fresh tuples and at a second time to a relative tolerance of 1e-10."""
+    is then verified at fresh tuples and at a second time to a tolerance of 1e-10 relative to
+    sum_m |c_m| |u^e_m| at each point (plus 1e-13 of the largest coefficient per monomial, the
+    fit's rounding): a t-dependence or non-polynomial part larger than that is rejected."""
     x = np.asarray(x, dtype=np.float64)
     n = x.shape[0]
     exps = monomials(N, max_degree)
@@ -299,16 +301,15 @@ def classify_system_poly(f, x, y, t0, N, what, max_degree=_SYS_DEGREE):
         coef = np.linalg.pinv(_vandermonde(U[1:], rest)) @ G
     else:
         coef = np.zeros((0, Fu.shape[1]))
-    # a fitted coefficient that is one value up to the fit's rounding at every point (it does
-    # not depend on (x, y) while another coefficient does) is set to that one value, so the
-    # library can keep it as a scalar.  The fit's noise scales with the polynomial's largest
-    # coefficients (measured below 2e-15 of them), so the test is against that scale; the
-    # change is at most 1e-13 of it.
-    big = max(np.max(np.abs(coef), initial=0.0), np.max(np.abs(c0), initial=0.0))
+    # a fitted coefficient that is one value up to rounding at every point (it does not depend
+    # on (x, y) while another coefficient does) is set to that one value, so the library can
+    # keep it as a scalar.  The test is against the coefficient's own size (a spread within
+    # 1e-13 of its largest magnitude): a coefficient that really varies is never flattened,
+    # however small it is next to the others.
     for k in range(coef.shape[0]):
         row = coef[k]
         lo, hi = row.min(initial=np.inf), row.max(initial=-np.inf)
-        if row.size and hi - lo <= 1e-13 * big:
+        if row.size and hi - lo <= 1e-13 * max(abs(lo), abs(hi)):
             row[:] = np.median(row)
     if np.any(c0 != 0):
         exps = np.vstack([exps[:1], rest])
@@ -322,7 +323,10 @@ def classify_system_poly(f, x, y, t0, N, what, max_degree=_SYS_DEGREE):
     checks = [(u, t0) for u in Uc] + [(U[1], t0 + 1.37), (Uc[0], t0 + 1.37)]
     for u, t in checks:
         pred = (_vandermonde(u[None, :], exps) @ coef)[0] if exps.shape[0] else np.zeros(n)
-        bound = _RTOL * scale * max(1.0, M) * (1.0 + np.max(np.abs(u))) ** max_degree
+        # relative to the size of what is summed: sum_m |c_m| |u^e_m| at each point, plus a
+        # floor at the fit's rounding (a few ulps of the largest coefficient per monomial)
+        terms = (_vandermonde(np.abs(u)[None, :], exps) @ np.abs(coef))[0] if exps.shape[0] else np.zeros(n)
+        bound = _RTOL * terms + 1e-13 * scale * exps.shape[0] * (1.0 + np.max(np.abs(u))) ** max_degree
         if not np.all(np.abs(ev(u, t) - pred) <= bound):
             _reject_sys(what, "depends on t" if t != t0 else
                         f"not a polynomial of total degree <= {max_degree} in the components")

@@ -139,9 +139,9 @@ int fvm_problem_export_codes(const fvm_problem* prob, int8_t* vertex_code, int8_
  * boundary-edge fluxes and per-vertex source / condition finalisation.  stream is a
  * cudaStream_t (NULL = default stream).  flags: FVM_PTR_* | FVM_RHS_FORCE_TRIANGLE. */
 int fvm_rhs(fvm_problem* prob, const double* u, double* du, double t, int32_t flags, void* stream);
-/* fvm_rhs for callers that cannot call cudaMalloc.  That includes code running inside an open
- * CUDA graph capture, real-time loops whose allocator is frozen after start-up, and hosts that
- * hand all device memory to their own pool.  This entry point has no counterpart in the
+/* fvm_rhs for callers that cannot call cudaMalloc: real-time loops whose allocator is frozen
+ * after start-up, and hosts that hand all device memory to their own pool (where a cudaMalloc
+ * behind the pool's back fails or fragments it).  This entry point has no counterpart in the
  * reference, which has no GPU path.
  *   u, du: device arrays in the caller's numbering.
  *   The mesh may have at most FVM_NOALLOC_MAX_POINTS points; larger meshes are rejected with
@@ -152,7 +152,9 @@ int fvm_rhs(fvm_problem* prob, const double* u, double* du, double t, int32_t fl
  *   The first call on each device looks up the array's device address (no allocation).  Make
  *   that first call before any stream capture.
  *   A nonlinear problem's per-triangle data is prepared by its first fvm_rhs call, so make one
- *   fvm_rhs call before using this entry point on such a problem. */
+ *   fvm_rhs call before using this entry point on such a problem (otherwise
+ *   FVM_ERR_INVALID_ARGUMENT).  Call it with the device that was current when the mesh was
+ *   created (otherwise FVM_ERR_INVALID_ARGUMENT). */
 #define FVM_NOALLOC_MAX_POINTS 262144
 int fvm_rhs_noalloc(fvm_problem* prob, const double* u, double* du, double t, void* stream);
 /* Replaces update_dirichlet_nodes! (src/equations/dirichlet.jl:78-86). */

@@ -395,3 +395,19 @@ def test_classify_recovers_random_polynomials(seed):
         assert np.max(np.abs(got[ek] - ref)) <= 1e-12 * max(1.0, np.max(np.abs(ref))), ek
         if const:
             assert np.unique(got[ek]).size == 1, ek
+
+
+def test_system_fit_rejects_small_t_dependence_and_keeps_small_varying_coefficients():
+    """The fit's acceptance is relative to the size of the evaluated terms: a t-dependence of
+    1e-9 of the value is rejected.  Snapping to one value is relative to each coefficient's own
+    size: a coefficient that varies with (x, y) stays varying however small it is next to the
+    others."""
+    x = np.linspace(-1, 1, 500)
+    y = np.linspace(0, 1, 500)
+    with pytest.raises(forms.UnsupportedFormError):
+        forms.classify_system_poly(lambda x, y, t, u: u[0] * (1 + 1e-9 * t) + 0.0 * x, x, y, 0.0, 2, "S")
+    e, c = forms.classify_system_poly(lambda x, y, t, u: 5.0 * u[0] ** 2 + 1e-9 * (1 + x) * u[1], x, y, 0.0, 2, "S")
+    got = {tuple(k): c[:, m] for m, k in enumerate(e)}
+    assert np.unique(got[(0, 1)]).size > 1  # not flattened
+    assert np.allclose(got[(0, 1)], 1e-9 * (1 + x), rtol=1e-6, atol=1e-14)  # fit noise ~1e-16 of 5
+    assert np.unique(got[(2, 0)]).size == 1

@@ -1,7 +1,7 @@
 """fvm_rhs_noalloc: the RHS entry point for callers that cannot allocate device memory.
 
-Such callers include code inside an open CUDA graph capture, real-time loops with a frozen
-allocator, and hosts that give all device memory to their own pool.  The test calls the
+Such callers include real-time loops with a frozen allocator and hosts that give all device
+memory to their own pool, where a cudaMalloc behind the pool's back fails or fragments it.  The test calls the
 entry point through the C ABI, twice in a row with different inputs, and checks each result
 against the allocating entry point fvm_rhs.  It uses the same FP64 tolerance as the other RHS
 tests (1e-12 relative); both paths run the same kernels, so the results are identical.  The
@@ -67,3 +67,23 @@ def test_noalloc_rejects_meshes_above_the_limit(gpu_lib):
     st = lib.fvm_rhs_noalloc(prob.handle, ctypes.c_void_p(u.data_ptr()), ctypes.c_void_p(du.data_ptr()), 0.0, None)
     assert st == gpu_lib.FVM_ERR_INVALID_ARGUMENT
     assert "262144" in gpu_lib.last_error()
+
+
+def test_noalloc_refuses_a_fresh_nonlinear_problem(gpu_lib):
+    """A nonlinear problem's per-triangle data is built by its first fvm_rhs call; before that
+    the no-allocation entry point refuses it (it never allocates lazily), and after one
+    fvm_rhs call it runs."""
+    import torch
+
+    lib = gpu_lib.load()
+    spec = nonlinear_rect(20)
+    prob = api_problem(spec)
+    u = torch.tensor(spec.u0, device="cuda")
+    st, _ = _rhs(lib, prob, u, noalloc=True)
+    assert st == gpu_lib.FVM_ERR_INVALID_ARGUMENT
+    assert "fvm_rhs" in gpu_lib.last_error()
+    st_ref, ref = _rhs(lib, prob, u, noalloc=False)
+    assert st_ref == 0, gpu_lib.last_error()
+    st, got = _rhs(lib, prob, u, noalloc=True)
+    assert st == 0, gpu_lib.last_error()
+    assert np.linalg.norm(got - ref) <= 1e-12 * np.linalg.norm(ref)
