@@ -229,7 +229,7 @@ static void tsit5_run(OdeRhs& rhs, int64_t n, const double* u0_int, const fvm_od
             }
             rhs.f(unew, k[6], t, s);
             launch_error_partial_dev(u, unew, k, kBt, d_st, n, d_acc, nparts, s);
-            launch_adaptive_step_tail(d_st, d_acc, nparts, n, cond, out_int, u, unew, k[0], k[6], d_saveat, s);
+            launch_adaptive_step_tail(d_st, d_acc, nparts, n, cond, out_int, u, unew, k, d_saveat, s);
             if (rhs.callback) rhs.callback(u, t, s);
             launch_adaptive_step_end(d_st, out_int, u, d_saveat, n, s);
             cudaGraph_t captured = nullptr;
@@ -332,7 +332,7 @@ static void tsit5_run(OdeRhs& rhs, int64_t n, const double* u0_int, const fvm_od
         double tn = last ? o.tf : (o.adaptive ? t + h : o.t0 + (double)(step + 1) * dt);
         while (si < saveat.size() && saveat[si] < tn) {
             double th = (saveat[si] - t) / h;
-            launch_hermite(out_int + si * n, u, unew, k[0], k[6], h, th, n, s);
+            launch_tsit5_interp(out_int + si * n, u, k, h, th, n, s);
             ++si;
         }
         std::swap(u, unew);

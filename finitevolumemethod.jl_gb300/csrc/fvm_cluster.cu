@@ -57,6 +57,7 @@ struct ClusterTsit5Args {
     uint32_t expect_bytes[kClusterMax];  // per CTA: bytes of row values it receives per stage
     double a[7][6];
     double bt[7];
+    double bi[7][4];  // continuous extension: w_i(theta) = sum_p bi[i][p] theta^(p+1)
 };
 
 // Step decision of one CTA's thread 0, read by the CTA's other threads after a __syncthreads.
@@ -67,7 +68,7 @@ struct ClusterCtl {
     int32_t last, accept, stop, qold_pending;
 };
 
-constexpr int kClusterHermite = 32;  // saveat points per step with shared Hermite weights
+constexpr int kClusterInterp = 32;  // saveat points per step whose theta is shared
 
 __constant__ PowTables c_pow;  // tables of pow_pos, uploaded once per device (launch_cluster_tsit5)
 
@@ -151,7 +152,7 @@ __global__ void __launch_bounds__(32 * kClusterWarps, 1) tsit5_cluster_kernel(co
     __shared__ ClusterCtl ctl;
     __shared__ double wsum[kClusterWarps];
     __shared__ double pq_sh;
-    __shared__ double hw[kClusterHermite][4];  // Hermite weights h00, h10 h, h01, h11 h per save
+    __shared__ double thsh[kClusterInterp];  // theta of the step's interior saves
     __shared__ __align__(8) uint64_t ybar[3];
     __shared__ __align__(8) uint64_t pbar[2];
     cg::cluster_group cl = cg::this_cluster();
@@ -216,6 +217,10 @@ __global__ void __launch_bounds__(32 * kClusterWarps, 1) tsit5_cluster_kernel(co
 #pragma unroll
         for (int s = 1; s <= 6; ++s) acc[s] = a.a[s][0] * k0;
         err = a.bt[0] * k0;
+        // running sums of the continuous extension, m[p] = sum_i bi[i][p] k_i
+        double m[4];
+#pragma unroll
+        for (int p = 0; p < 4; ++p) m[p] = a.bi[0][p] * k0;
         double unew = 0.0, inv_sc = 0.0;
 #pragma unroll
         for (int s = 1; s <= 6; ++s) {
@@ -261,6 +266,8 @@ __global__ void __launch_bounds__(32 * kClusterWarps, 1) tsit5_cluster_kernel(co
 #pragma unroll
                 for (int s2 = s + 1; s2 <= 6; ++s2) acc[s2] += a.a[s2][s] * f;
                 err += a.bt[s] * f;
+#pragma unroll
+                for (int p = 0; p < 4; ++p) m[p] += a.bi[s][p] * f;
                 if (s == 6) k6 = f;
             }
             ++g;
@@ -322,34 +329,15 @@ __global__ void __launch_bounds__(32 * kClusterWarps, 1) tsit5_cluster_kernel(co
         __syncthreads();
         if (ctl.accept) {
             const int64_t nint = ctl.j1 - ctl.si;
-            if (nint > 0) {  // Hermite weights of the step's interior saves, one lane each
-                if (threadIdx.x < kClusterHermite && threadIdx.x < nint) {
-                    const double th = (__ldg(&a.saveat[ctl.si + threadIdx.x]) - ctl.t0) / h;
-                    const double t2 = th * th, t3 = t2 * th;
-                    hw[threadIdx.x][0] = 2 * t3 - 3 * t2 + 1;
-                    hw[threadIdx.x][1] = (t3 - 2 * t2 + th) * h;
-                    hw[threadIdx.x][2] = -2 * t3 + 3 * t2;
-                    hw[threadIdx.x][3] = (t3 - t2) * h;
-                }
+            if (nint > 0) {  // the step's interior saves from the continuous extension
+                if (threadIdx.x < kClusterInterp && threadIdx.x < nint)
+                    thsh[threadIdx.x] = (__ldg(&a.saveat[ctl.si + threadIdx.x]) - ctl.t0) / h;
                 __syncthreads();
                 if (own) {
                     for (int64_t j = ctl.si; j < ctl.j1; ++j) {
                         const int64_t jj = j - ctl.si;
-                        double w0, w1, w2, w3;
-                        if (jj < kClusterHermite) {
-                            w0 = hw[jj][0];
-                            w1 = hw[jj][1];
-                            w2 = hw[jj][2];
-                            w3 = hw[jj][3];
-                        } else {
-                            const double th = (__ldg(&a.saveat[j]) - ctl.t0) / h;
-                            const double t2 = th * th, t3 = t2 * th;
-                            w0 = 2 * t3 - 3 * t2 + 1;
-                            w1 = (t3 - 2 * t2 + th) * h;
-                            w2 = -2 * t3 + 3 * t2;
-                            w3 = (t3 - t2) * h;
-                        }
-                        a.out[j * n + r] = w0 * u + w1 * k0 + w2 * unew + w3 * k6;
+                        const double th = jj < kClusterInterp ? thsh[jj] : (__ldg(&a.saveat[j]) - ctl.t0) / h;
+                        a.out[j * n + r] = u + h * (th * (m[0] + th * (m[1] + th * (m[2] + th * m[3]))));
                     }
                 }
             }
@@ -513,6 +501,7 @@ void launch_cluster_tsit5(const SellRhsDesc& d, const double* dirval, double* u,
         for (int j = 0; j < 6; ++j) a.a[i][j] = A[i][j];
         a.bt[i] = bt[i];
     }
+    tsit5_interp_poly(a.bi);
     cudaLaunchConfig_t cfg{};
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;

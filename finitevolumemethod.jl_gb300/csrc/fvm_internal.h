@@ -168,7 +168,30 @@ struct fvm_template {
     void build_steady();
 };
 
+#ifdef __CUDACC__
+#define FVM_HD __host__ __device__
+#else
+#define FVM_HD
+#endif
+
 namespace fvm {
+// Tsit5's free 4th-order continuous extension (Tsitouras 2011, Comput. Math. Appl. 62:770-775),
+// the dense output OrdinaryDiffEq's Tsit5 interpolates saveat with:
+//     u(t_n + theta h) = u_n + h sum_i w_i(theta) k_i
+// over the seven stage derivatives, k_7 = f(u_{n+1}).  w_i(1) are the step's weights.
+FVM_HD inline void tsit5_interp_weights(double t, double w[7]) {
+    w[0] = -1.0530884977290216 * t * (t - 1.3299890189751412) * (t * t - 1.4364028541716351 * t + 0.7139816917074209);
+    w[1] = 0.1017 * t * t * (t * t - 2.1966568338249754 * t + 1.2949852507374631);
+    w[2] = 2.490627285651252793 * t * t * (t * t - 2.38535645472061657 * t + 1.57803468208092486);
+    w[3] = -16.54810288924490272 * (t - 1.21712927295533244) * (t - 0.61620406037800089) * t * t;
+    w[4] = 47.37952196281928122 * (t - 1.203071208372362603) * (t - 0.658047292653547382) * t * t;
+    w[5] = -34.87065786149660974 * (t - 1.2) * (t - 0.666666666666666667) * t * t;
+    w[6] = 2.5 * (t - 1) * (t - 0.6) * t * t;
+}
+// The same weights as polynomials: w_i(theta) = sum_{p=1..4} beta[i][p-1] theta^p (the
+// products above multiplied out), for drivers that keep running sums sum_i beta[i][p] k_i.
+void tsit5_interp_poly(double beta[7][4]);
+
 // Sliced ELL from a pattern's CSR view (rowptr, csr_col): slices of 32 rows, width = longest
 // row of the slice, slots column-major, padding slots pointing at the row itself (fvm_mesh.cpp)
 void finalize_sell(SellPattern& pat, int64_t nrows);
@@ -202,8 +225,9 @@ void launch_stage(double* y, const double* u, const double* const* k, const doub
 // err_i = dt * sum_j bt[j] k[j]; accumulates sum((err_i / (abstol + max(|u|,|unew|) reltol))^2)
 void launch_error_norm(const double* u, const double* unew, const double* const* k, const double* bt,
                        double dt, double abstol, double reltol, int64_t n, double* d_acc, cudaStream_t s);
-void launch_hermite(double* out, const double* u0, const double* u1, const double* f0, const double* f1,
-                    double dt, double theta, int64_t n, cudaStream_t s);
+// saveat value inside a step: out = u + h sum_j w_j(theta) k_j (seven stage derivatives)
+void launch_tsit5_interp(double* out, const double* u, const double* const* k, double h, double theta, int64_t n,
+                         cudaStream_t s);
 // Krylov helpers
 void launch_fill(double* x, double v, int64_t n, cudaStream_t s);
 
@@ -222,7 +246,7 @@ void launch_error_partial_dev(const double* u, const double* unew, const double*
                               const AdaptState* st, int64_t n, double* part, int nparts, cudaStream_t s);
 void launch_adaptive_step_tail(AdaptState* st, const double* part, int nparts, int64_t n,
                                cudaGraphConditionalHandle cond, double* out, double* u, const double* unew,
-                               double* k0, const double* k6, const double* saveat, cudaStream_t s);
+                               double* const* k, const double* saveat, cudaStream_t s);
 void launch_adaptive_step_end(AdaptState* st, double* out, const double* u, const double* saveat, int64_t n,
                               cudaStream_t s);
 

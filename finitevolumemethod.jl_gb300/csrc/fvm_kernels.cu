@@ -444,19 +444,41 @@ void launch_error_norm(const double* u, const double* unew, const double* const*
     sum_partials_kernel<<<1, 256, 0, s>>>(d_acc + 1, kErrBlocks, d_acc);
 }
 
-// cubic Hermite on [t_n, t_n + dt] from (u0, f0) and (u1, f1) at theta in [0, 1]
-__global__ void hermite_kernel(double* __restrict__ out, const double* __restrict__ u0, const double* __restrict__ u1,
-                               const double* __restrict__ f0, const double* __restrict__ f1, double dt, double th,
-                               int64_t n) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    double t2 = th * th, t3 = t2 * th;
-    double h00 = 2 * t3 - 3 * t2 + 1, h10 = t3 - 2 * t2 + th, h01 = -2 * t3 + 3 * t2, h11 = t3 - t2;
-    out[i] = h00 * u0[i] + h10 * dt * f0[i] + h01 * u1[i] + h11 * dt * f1[i];
+// saveat value inside a step from Tsit5's continuous extension: a stage combination with the
+// weights w_j(theta)
+void launch_tsit5_interp(double* out, const double* u, const double* const* k, double h, double theta, int64_t n,
+                         cudaStream_t s) {
+    double w[7];
+    tsit5_interp_weights(theta, w);
+    launch_stage(out, u, k, w, 7, h, n, s);
 }
-void launch_hermite(double* out, const double* u0, const double* u1, const double* f0, const double* f1, double dt,
-                    double theta, int64_t n, cudaStream_t s) {
-    hermite_kernel<<<grid_for(n, 256), 256, 0, s>>>(out, u0, u1, f0, f1, dt, theta, n);
+
+// w_i(theta) multiplied out: each is a constant times linear or quadratic factors times theta
+// or theta^2
+void tsit5_interp_poly(double beta[7][4]) {
+    // coefficients of theta^0.. of a polynomial held as a vector, multiplied factor by factor
+    auto mul = [](std::vector<double> p, std::initializer_list<double> f) {
+        std::vector<double> r(p.size() + f.size() - 1, 0.0);
+        size_t j = 0;
+        for (double fj : f) {
+            for (size_t i = 0; i < p.size(); ++i) r[i + j] += p[i] * fj;
+            ++j;
+        }
+        return r;
+    };
+    std::vector<std::vector<double>> P(7);
+    P[0] = mul(mul(mul({-1.0530884977290216}, {0.0, 1.0}), {-1.3299890189751412, 1.0}),
+               {0.7139816917074209, -1.4364028541716351, 1.0});
+    P[1] = mul(mul({0.1017}, {0.0, 0.0, 1.0}), {1.2949852507374631, -2.1966568338249754, 1.0});
+    P[2] = mul(mul({2.490627285651252793}, {0.0, 0.0, 1.0}), {1.57803468208092486, -2.38535645472061657, 1.0});
+    P[3] = mul(mul(mul({-16.54810288924490272}, {-1.21712927295533244, 1.0}), {-0.61620406037800089, 1.0}),
+               {0.0, 0.0, 1.0});
+    P[4] = mul(mul(mul({47.37952196281928122}, {-1.203071208372362603, 1.0}), {-0.658047292653547382, 1.0}),
+               {0.0, 0.0, 1.0});
+    P[5] = mul(mul(mul({-34.87065786149660974}, {-1.2, 1.0}), {-0.666666666666666667, 1.0}), {0.0, 0.0, 1.0});
+    P[6] = mul(mul(mul({2.5}, {-1.0, 1.0}), {-0.6, 1.0}), {0.0, 0.0, 1.0});
+    for (int i = 0; i < 7; ++i)
+        for (int p = 0; p < 4; ++p) beta[i][p] = p + 1 < (int)P[i].size() ? P[i][p + 1] : 0.0;
 }
 
 // ---------------------------------------------------------------------------------------
@@ -570,20 +592,26 @@ __global__ void adapt_control_kernel(AdaptState* st, const double* __restrict__ 
     cudaGraphSetConditional(cond, (!finished && st->status == 0) ? 1u : 0u);
 }
 
-// saveat points strictly inside the accepted step: cubic Hermite from (u, k0) and (unew, k6)
-__global__ void adapt_save_interp_kernel(double* __restrict__ out, const double* __restrict__ u,
-                                         const double* __restrict__ unew, const double* __restrict__ f0,
-                                         const double* __restrict__ f1, const double* __restrict__ saveat,
-                                         const AdaptState* __restrict__ st, int64_t n) {
+// saveat points strictly inside the accepted step: Tsit5's continuous extension of the step
+// (the seven stage derivatives; the weights are the same for every row of a save)
+__global__ void adapt_save_interp_kernel(double* __restrict__ out, const double* __restrict__ u, StageArgs sk,
+                                         const double* __restrict__ saveat, const AdaptState* __restrict__ st,
+                                         int64_t n) {
     if (!st->accept) return;
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double h = st->h, t0 = st->t_prev, tn = st->t;
+    double kv[7];
+#pragma unroll
+    for (int j = 0; j < 7; ++j) kv[j] = sk.k[j][i];
+    const double ui = u[i];
     for (int64_t j = st->si; j < st->nsave && saveat[j] < tn; ++j) {
-        const double th = (saveat[j] - t0) / h;
-        const double t2 = th * th, t3 = t2 * th;
-        const double h00 = 2 * t3 - 3 * t2 + 1, h10 = t3 - 2 * t2 + th, h01 = -2 * t3 + 3 * t2, h11 = t3 - t2;
-        out[j * n + i] = h00 * u[i] + h10 * h * f0[i] + h01 * unew[i] + h11 * h * f1[i];
+        double w[7];
+        tsit5_interp_weights((saveat[j] - t0) / h, w);
+        double acc = 0.0;
+#pragma unroll
+        for (int q = 0; q < 7; ++q) acc += w[q] * kv[q];
+        out[j * n + i] = ui + h * acc;
     }
 }
 // accepted step: u <- unew, FSAL k0 <- k6
@@ -616,10 +644,15 @@ __global__ void adapt_advance_kernel(AdaptState* st, const double* __restrict__ 
 
 void launch_adaptive_step_tail(AdaptState* st, const double* part, int nparts, int64_t n,
                                cudaGraphConditionalHandle cond, double* out, double* u, const double* unew,
-                               double* k0, const double* k6, const double* saveat, cudaStream_t s) {
+                               double* const* k, const double* saveat, cudaStream_t s) {
+    StageArgs sk;
+    for (int j = 0; j < 7; ++j) {
+        sk.k[j] = k[j];
+        sk.a[j] = 0.0;
+    }
     adapt_control_kernel<<<1, 256, 0, s>>>(st, part, nparts, n, cond);
-    adapt_save_interp_kernel<<<grid_for(n, 256), 256, 0, s>>>(out, u, unew, k0, k6, saveat, st, n);
-    adapt_commit_kernel<<<grid_for(n, 256), 256, 0, s>>>(u, unew, k0, k6, st, n);
+    adapt_save_interp_kernel<<<grid_for(n, 256), 256, 0, s>>>(out, u, sk, saveat, st, n);
+    adapt_commit_kernel<<<grid_for(n, 256), 256, 0, s>>>(u, unew, k[0], k[6], st, n);
 }
 void launch_adaptive_step_end(AdaptState* st, double* out, const double* u, const double* saveat, int64_t n,
                               cudaStream_t s) {

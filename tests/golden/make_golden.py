@@ -9,6 +9,9 @@ Arrays (caller numbering, 2500 points):
   t_save, u_save    adaptive Tsit5 (abstol 1e-6, reltol 1e-3, the Dirichlet callback after
                     every step) at t = 0.01, 0.1, 0.25, 0.5
   naccept, nreject  the step counts of that run
+  k_dense, u_dense  24 of the 501 saves of the README's saveat = 0.001 run (t = 0.001 k_dense;
+                    the steps do not depend on saveat, so any subset of the grid gives the same
+                    values), interpolated inside the steps by Tsit5's continuous extension
 
 The reference itself cannot run here (pure Julia, no Julia on any machine), so the fixture
 freezes the oracle, which is pinned by the reference's known-answer tests; it guards the
@@ -38,8 +41,13 @@ def compute():
     du_u0 = O.fvm_eqs(prob, spec.u0, 0.0)
     cb = lambda u, t: O.update_dirichlet_nodes(prob, u, t)  # noqa: E731
     snaps, st = O.tsit5_solve(lambda u, t: O.fvm_eqs(prob, u, t), spec.u0, 0.0, 0.5, T_SAVE, callback=cb)
+    k_dense = np.sort(np.random.default_rng(22).choice(501, size=24, replace=False))
+    dense, st2 = O.tsit5_solve(lambda u, t: O.fvm_eqs(prob, u, t), spec.u0, 0.0, 0.5, list(0.001 * k_dense),
+                               callback=cb)
+    assert st2["naccept"] == st["naccept"] and st2["nreject"] == st["nreject"]
     return {"u_rand": u_rand, "du_rand": du_rand, "du_u0": du_u0, "t_save": np.array(T_SAVE),
-            "u_save": np.array(snaps), "naccept": np.array(st["naccept"]), "nreject": np.array(st["nreject"])}
+            "u_save": np.array(snaps), "naccept": np.array(st["naccept"]), "nreject": np.array(st["nreject"]),
+            "k_dense": k_dense, "u_dense": np.array(dense)}
 
 
 def compute_system():

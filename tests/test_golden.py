@@ -44,6 +44,34 @@ def test_gpu_matches_fixture(gpu_lib):
     assert np.max(np.abs(np.array(sol.u) - g["u_save"])) <= 1e-8 * 50.0
 
 
+@pytest.mark.gpu
+def test_gpu_matches_dense_saveat_fixture(gpu_lib):
+    """The README's own run, saveat = 0.001 (501 saves, test/README.jl:4-15): the saves inside
+    steps come from Tsit5's continuous extension on the GPU as in the oracle; 24 of them are
+    frozen in the fixture.  Same step counts; within the adaptive-run tolerance, 1e-8 of
+    max|u| = 50 (the step control's rounding differs in the last bits between the drivers)."""
+    import fvmgpu as F
+
+    g = _golden()
+    spec = readme_diffusion(50)
+    prob = api_problem(spec)
+    sol = F.solve(prob, F.Tsit5(), saveat=0.001)
+    assert len(sol.u) == 501
+    assert sol.stats["naccept"] == int(g["naccept"]) and sol.stats["nreject"] == int(g["nreject"])
+    got = np.array(sol.u)[g["k_dense"]]
+    assert np.max(np.abs(got - g["u_dense"])) <= 1e-8 * 50.0
+
+
+def test_oracle_reproduces_dense_saveat_fixture():
+    g = _golden()
+    spec = readme_diffusion(50)
+    prob = oracle_problem(spec)
+    cb = lambda u, t: O.update_dirichlet_nodes(prob, u, t)  # noqa: E731
+    snaps, _ = O.tsit5_solve(lambda u, t: O.fvm_eqs(prob, u, t), spec.u0, 0.0, 0.5, list(0.001 * g["k_dense"]),
+                             callback=cb)
+    assert np.max(np.abs(np.array(snaps) - g["u_dense"])) <= 1e-12 * 50.0
+
+
 SYSTEM_GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "system_gray_scott.npz")
 
 

@@ -32,6 +32,21 @@ def test_fixed_step_tsit5(gpu_lib, use_graph):
     assert sol.stats["naccept"] == st["naccept"] == 20
 
 
+def test_fixed_step_dense_output(gpu_lib):
+    """saveat points inside fixed steps (dt = 3.7e-4, saves every 1e-3): Tsit5's continuous
+    extension on the GPU against the oracle's, 1e-10 of max|u|."""
+    import fvmgpu as F
+
+    spec = readme_diffusion(50)
+    spec.tf = 0.05
+    prob = api_problem(spec)
+    sol = F.solve(prob, F.Tsit5(), dt=3.7e-4, adaptive=False, saveat=0.001)
+    ref, st = _oracle_run(spec, list(sol.t), dt=3.7e-4, adaptive=False)
+    assert len(sol.u) == 51 and sol.stats["naccept"] == st["naccept"]
+    err = np.max(np.abs(np.array(sol.u) - ref)) / 50.0
+    assert err < 1e-10, err
+
+
 @pytest.mark.parametrize("use_graph", [True, False])
 def test_adaptive_readme_saveat(gpu_lib, use_graph):
     """README diffusion (test/README.jl): Tsit5 to t = 0.5 with saveat = 0.001.  use_graph runs
@@ -129,7 +144,7 @@ def test_adaptive_step_limit(gpu_lib, side, use_graph):
 def test_cluster_wide_rows_and_dense_saves(gpu_lib):
     """The cluster driver on rows wider than 12 slots (a 40-spoke hub: the slot loop re-reads
     its slots instead of holding them in registers), a Robin boundary and a linear source,
-    with 3001 saveat points (more than the 32 per step whose Hermite weights are shared):
+    with 3001 saveat points (more than the 32 per step whose theta is shared):
     the same steps as the host loop, solutions equal to 1e-10 of max|u|."""
     import fvmgpu as F
 

@@ -386,3 +386,40 @@ def test_set_diag_assigns_like_a_dense_matrix():
     ref[idx, idx] = 1.0
     got = O._set_diag(A, idx, 1.0)
     assert np.array_equal(got.toarray(), ref)
+
+
+def test_tsit5_continuous_extension_order_conditions():
+    """Tsit5's dense output (Tsitouras 2011): at theta = 1 the weights are the step's, and for
+    every theta the order-4 conditions of a continuous extension hold,
+    sum b = theta, b.c = theta^2/2, b.c^2 = theta^3/3, b.Ac = theta^3/6, b.c^3 = theta^4/4,
+    b.(c*Ac) = theta^4/8, b.Ac^2 = theta^4/12, b.AAc = theta^4/24."""
+    c = O.TSIT5_C
+    A = np.zeros((7, 7))
+    for i in range(1, 7):
+        for j, a in enumerate(O.TSIT5_A[i]):
+            A[i, j] = a
+    assert np.max(np.abs(O.tsit5_interp_weights(1.0) - O.TSIT5_B)) <= 1e-14
+    assert np.max(np.abs(O.tsit5_interp_weights(0.0))) == 0.0
+    for th in np.linspace(0.05, 1.0, 12):
+        w = O.tsit5_interp_weights(th)
+        conds = [w.sum() - th, w @ c - th ** 2 / 2, w @ c ** 2 - th ** 3 / 3, w @ (A @ c) - th ** 3 / 6,
+                 w @ c ** 3 - th ** 4 / 4, w @ (c * (A @ c)) - th ** 4 / 8, w @ (A @ c ** 2) - th ** 4 / 12,
+                 w @ (A @ (A @ c)) - th ** 4 / 24]
+        assert np.max(np.abs(conds)) <= 1e-14, th
+
+
+def test_tsit5_dense_output_is_fourth_order():
+    """On u' = -u the interpolated values inside one step of size h have error O(h^5): halving
+    h divides the error by about 32 (at least 20 here)."""
+    f = lambda u, t: -u  # noqa: E731
+    errs = []
+    for h in (0.2, 0.1):
+        k = [f(np.array([1.0]), 0.0)]
+        for s_ in range(1, 7):
+            y = np.array([1.0])
+            for j, a in enumerate(O.TSIT5_A[s_]):
+                y = y + h * a * k[j]
+            k.append(f(y, 0.0))
+        th = 0.4
+        errs.append(abs(O.tsit5_interpolate(np.array([1.0]), k, h, th)[0] - np.exp(-th * h)))
+    assert errs[0] / errs[1] > 20
