@@ -6,6 +6,7 @@
 #include "fvm_tma.cuh"
 
 #include <algorithm>
+#include <atomic>
 #include <vector>
 
 namespace fvm {
@@ -65,6 +66,29 @@ __global__ void __launch_bounds__(256) sell_kernel(SellArgs a) {
 // ---------------------------------------------------------------------------------------
 __device__ unsigned g_dev_error = 0;
 
+// Consumer stage-wait limit and producer delay of the streamed kernels (fault-path testing;
+// fvm_test_set_stream_waits).  0 = the defaults: kWaitLimitNs and no delay.
+static std::atomic<unsigned long long> g_stream_wait_ns{0}, g_producer_delay_ns{0};
+static unsigned long long stream_wait_ns() {
+    const unsigned long long w = g_stream_wait_ns.load();
+    return w ? w : kWaitLimitNs;
+}
+}  // namespace fvm
+
+extern "C" int fvm_test_set_stream_waits(int64_t consumer_wait_ns, int64_t producer_delay_ns) {
+    // bounded: a delay never exceeds 10 ms, a wait limit never goes below 100 ns
+    if (producer_delay_ns < 0 || producer_delay_ns > 10000000 || consumer_wait_ns < 0 ||
+        (consumer_wait_ns != 0 && consumer_wait_ns < 100)) {
+        fvm::set_last_error("fvm_test_set_stream_waits: delay outside [0, 10 ms] or wait limit below 100 ns");
+        return FVM_ERR_INVALID_ARGUMENT;
+    }
+    fvm::g_stream_wait_ns.store((unsigned long long)consumer_wait_ns);
+    fvm::g_producer_delay_ns.store((unsigned long long)producer_delay_ns);
+    return FVM_OK;
+}
+
+namespace fvm {
+
 unsigned* device_error_word() {
     static unsigned* p = nullptr;
     if (!p) FVM_CUDA(cudaGetSymbolAddress((void**)&p, g_dev_error));
@@ -103,7 +127,7 @@ static void launch_sell(const SellPattern& p, const V* val, const X* xg, const d
     if (p.nslices == 0) return;
     if (p.maxw <= 16) {
         StreamArgs a{p.d_slice_ptr.as<int64_t>(), p.d_col.as<int32_t>(), val, xg, device_error_word(),
-                     p.nrows, p.nslices, 0, 0, 0};
+                     p.nrows, p.nslices, 0, 0, 0, stream_wait_ns(), g_producer_delay_ns.load()};
         const RhsEpilogue e{x, y, rowscale, d, b, q};
         // exact widths of the common vertex degrees: no predicated-off slot costs an FP64 issue
         if (p.maxw <= 4)

@@ -48,6 +48,10 @@ struct StreamArgs {
     int nst;    // pipeline stages held in shared memory
     int spwin;  // slice offsets held per CTA: its range plus alignment slack, a multiple of 16
     int xb;     // bytes of shared memory holding the CTA's own rows of x (0: gathers via L1/L2)
+    // limit of a consumer's wait for a stage to land (kWaitLimitNs), and a delay of the producer
+    // before its second stage (0): the fault-path test shortens the one and sets the other so
+    // that the wait runs out, the CTA stops and the error word reports it
+    unsigned long long wait_ns, producer_delay_ns;
 };
 
 constexpr int kSpWindowMax = 1024;
@@ -108,6 +112,7 @@ __global__ void __launch_bounds__((NW + 1) * 32, kStreamPipelined<MAXW> && NW <=
     uint64_t* empty = full + nst;
     uint64_t* spbar = empty + nst;
     uint64_t* xbar = spbar + 1;
+    __shared__ volatile int abort_flag;  // a consumer gave up: the producer stops issuing stages
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t G = gridDim.x;
     const int64_t sb = a.nslices * (int64_t)blockIdx.x / G, se = a.nslices * ((int64_t)blockIdx.x + 1) / G;
@@ -128,6 +133,7 @@ __global__ void __launch_bounds__((NW + 1) * 32, kStreamPipelined<MAXW> && NW <=
     }
     const uint64_t xcnt = xbytes / sizeof(X);
     if (threadIdx.x == 0) {
+        abort_flag = 0;
         for (int i = 0; i < nst; ++i) {
             mbar_init(&full[i], 1);
             mbar_init(&empty[i], NW);
@@ -151,7 +157,9 @@ __global__ void __launch_bounds__((NW + 1) * 32, kStreamPipelined<MAXW> && NW <=
         // streams stage k (slots [c0, c1)) into its buffer once the buffer is free
         auto issue = [&](int64_t k, int64_t c0, int64_t c1) -> bool {
             const int st = (int)(k % nst);
-            if (k >= nst && !mbar_wait(&empty[st], (uint32_t)((k / nst - 1) & 1))) return false;
+            if (abort_flag) return false;
+            if (k >= nst && !mbar_wait_for(&empty[st], (uint32_t)((k / nst - 1) & 1), kWaitLimitNs, &abort_flag))
+                return false;
             const uint32_t n = (uint32_t)(c1 - c0);  // <= kSlots: NW slices of at most MAXW slots
             if (n == 0) {  // slices without slots: nothing to copy
                 mbar_arrive(&full[st]);
@@ -176,13 +184,18 @@ __global__ void __launch_bounds__((NW + 1) * 32, kStreamPipelined<MAXW> && NW <=
                                          : issue(0, __ldg(&a.slice_ptr[sb]), __ldg(&a.slice_ptr[min(sb + NW, se)]));
         int64_t issued = ok ? 1 : 0;
         if (ok && !mbar_wait(spbar, 0)) ok = false;
+        if (a.producer_delay_ns) {  // fault-path test only: hold back the second stage
+            const unsigned long long d0 = global_ns();
+            while (global_ns() - d0 < a.producer_delay_ns) {
+            }
+        }
         const int64_t* sp = spw - w0;
         for (int64_t k = 1; ok && k < nstage; ++k) {
             const int64_t s0 = sb + k * NW;
             if ((ok = issue(k, sp[s0], sp[min(s0 + NW, se)]))) issued = k + 1;
         }
-        if (!ok) {
-            atomicOr(a.err, kDevErrEmptyWait);
+        if (!ok || abort_flag) {  // a wait ran out here or in a consumer
+            if (!ok && !abort_flag) atomicOr(a.err, kDevErrEmptyWait);
             // wait (bounded) for the copies already issued into the stages still in flight
             for (int64_t j = (issued > nst ? issued - nst : 0); j < issued; ++j)
                 mbar_wait(&full[j % nst], (uint32_t)((j / nst) & 1));
@@ -215,7 +228,10 @@ __global__ void __launch_bounds__((NW + 1) * 32, kStreamPipelined<MAXW> && NW <=
         R.cw = 0;
         R.xa = 0;
         if ((DIFF || Epi::kOwnX) && R.have) R.xa = gather(R.r < a.nrows ? R.r : a.nrows - 1);
-        if (!mbar_wait(&full[R.st], (uint32_t)((k / nst) & 1))) return false;
+        if (!mbar_wait_for(&full[R.st], (uint32_t)((k / nst) & 1), a.wait_ns, &abort_flag)) {
+            abort_flag = 1;
+            return false;
+        }
         if (R.have) {
             const int64_t cb = sp[s];
             R.cw = (int)((sp[s + 1] - cb) / kSlice);

@@ -60,6 +60,18 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
     }
 }
 
+// Waits like mbar_wait with the given limit; gives up early once *abort is set (another warp
+// of the CTA has given up and will not release the stages this wait depends on).
+__device__ __forceinline__ bool mbar_wait_for(uint64_t* bar, uint32_t parity, unsigned long long limit_ns,
+                                              const volatile int* abort) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const unsigned long long t0 = global_ns();
+    for (;;) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if (*abort || global_ns() - t0 > limit_ns) return false;
+    }
+}
+
 // ---- distributed shared memory (thread-block clusters) ----------------------------------
 
 // shared::cluster address of the same shared-memory location in CTA `rank` of the cluster

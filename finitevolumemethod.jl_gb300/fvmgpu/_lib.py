@@ -151,6 +151,7 @@ SIGNATURES = {
     "fvm_problem_export_codes": (C.c_int, [C.c_void_p, c_int8_p, c_int8_p]),
     "fvm_rhs": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int32, C.c_void_p]),
     "fvm_rhs_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_void_p]),
+    "fvm_test_set_stream_waits": (C.c_int, [C.c_int64, C.c_int64]),
     "fvm_dirichlet_apply": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_int32, C.c_void_p]),
     "fvm_tsit5_solve": (C.c_int, [C.c_void_p, c_double_p, C.POINTER(OdeOptions), c_double_p, C.POINTER(OdeStats),
                                   C.c_void_p]),

@@ -157,6 +157,14 @@ int fvm_rhs(fvm_problem* prob, const double* u, double* du, double t, int32_t fl
  *   created (otherwise FVM_ERR_INVALID_ARGUMENT). */
 #define FVM_NOALLOC_MAX_POINTS 262144
 int fvm_rhs_noalloc(fvm_problem* prob, const double* u, double* du, double t, void* stream);
+/* Fault-path testing of the streamed operator kernel (no counterpart in the reference).  Every
+ * wait of the library's kernels is bounded; a wait that runs out sets a bit in a device error
+ * word, the kernel drains its copies in flight and returns, and the next synchronising call
+ * returns FVM_ERR_CUDA.  This sets, for all later launches of the streamed kernel, the limit of
+ * a consumer's wait for a stage (consumer_wait_ns, at least 100; 0 = the default 2 s) and a
+ * delay of the producer before its second stage (producer_delay_ns, at most 10 ms; 0 = none),
+ * so that a test can make the wait run out.  Not for production use; reset with (0, 0). */
+int fvm_test_set_stream_waits(int64_t consumer_wait_ns, int64_t producer_delay_ns);
 /* Replaces update_dirichlet_nodes! (src/equations/dirichlet.jl:78-86). */
 int fvm_dirichlet_apply(fvm_problem* prob, double* u, double t, int32_t flags, void* stream);
 
