@@ -57,7 +57,8 @@ def load():
                                          C.c_void_p]
         lib.orc_max_threads.restype = C.c_int
         lib.orc_steady_bicgstab.argtypes = [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
-                                            C.c_double, C.c_int64, C.c_int, C.c_void_p, C.c_void_p]
+                                            C.c_double, C.c_void_p, C.c_double, C.c_int64, C.c_double, C.c_int,
+                                            C.c_void_p, C.c_void_p]
         lib.orc_gray_scott_rhs_threaded.argtypes = [C.POINTER(OrcProblem), C.POINTER(GrayScott), C.c_void_p,
                                                     C.c_void_p, C.c_int, C.c_void_p]
         _lib = lib
@@ -134,29 +135,61 @@ class CGrayScott(CProblem):
         return du
 
 
-def steady_bicgstab(A, b, rtol=1e-10, maxit=200_000, nthreads=0):
-    """Jacobi-preconditioned FP64 BiCGStab on the host threads for the CSR matrix A (the CPU
-    baseline of the steady templates); returns (x, {"iterations", "rel_residual", "converged",
-    "seconds", "threads"})."""
+def reduced_system(A, b, V):
+    """The steady template's system A x = b as the GPU solver takes it: rows fixed by a
+    Dirichlet condition or a missing vertex (identity rows of A) stay identity rows with a zero
+    right-hand side, their columns move into the right-hand side of the free rows, and free rows
+    are scaled by -V.  Returns (B, rhs, xfix, w) with x = z + xfix for B z = rhs, and
+    (b - A x)_i = -(rhs - B z)_i / V_i on free rows (w = 1 / V there, 0 on fixed rows)."""
+    from scipy.sparse import csr_matrix, diags
+
+    A = A.tocsr()
+    n = A.shape[0]
+    nnz_row = np.diff(A.indptr)
+    fixed = (nnz_row == 1) & np.isclose(A.diagonal(), 1.0) & (np.asarray(abs(A).sum(axis=1)).ravel() == 1.0)
+    xfix = np.where(fixed, b, 0.0)
+    M = A.tocoo()
+    keep = ~fixed[M.row] & ~fixed[M.col]
+    Bf = csr_matrix((M.data[keep], (M.row[keep], M.col[keep])), shape=A.shape)
+    rhs_free = b - A @ xfix
+    sc = np.where(fixed, 1.0, -V)
+    B = (diags(sc) @ Bf).tocsr() + diags(np.where(fixed, 1.0, 0.0))
+    rhs = np.where(fixed, 0.0, sc * rhs_free)
+    w = np.where(fixed, 0.0, 1.0 / np.where(fixed, 1.0, V))
+    return B.tocsr(), rhs, xfix, w
+
+
+def steady_bicgstab(A, b, rtol=1e-10, maxit=200_000, nthreads=0, max_seconds=1e9, V=None):
+    """Jacobi-preconditioned FP64 BiCGStab on the host threads (the CPU baseline of the steady
+    templates), stopped at ||b - A x|| / ||b|| <= rtol, maxit or max_seconds.  With the control
+    volumes V it solves the GPU solver's reduced system (reduced_system) instead of A x = b
+    directly.  Returns (x, {"iterations", "rel_residual", "converged", "seconds", "threads"})."""
     import time
 
     lib = load()
     A = A.tocsr()
     n = A.shape[0]
-    rp = np.ascontiguousarray(A.indptr, dtype=np.int64)
-    ci = np.ascontiguousarray(A.indices, dtype=np.int32)
-    va = np.ascontiguousarray(A.data, dtype=np.float64)
-    bb = np.ascontiguousarray(b, dtype=np.float64)
-    x = np.zeros(n)
+    bnorm = float(np.linalg.norm(b))
+    if V is not None:
+        M, rhs, xfix, w = reduced_system(A, b, V)
+    else:
+        M, rhs, xfix, w = A, np.asarray(b, dtype=np.float64), np.zeros(n), None
+    rp = np.ascontiguousarray(M.indptr, dtype=np.int64)
+    ci = np.ascontiguousarray(M.indices, dtype=np.int32)
+    va = np.ascontiguousarray(M.data, dtype=np.float64)
+    bb = np.ascontiguousarray(rhs, dtype=np.float64)
+    wp = None if w is None else np.ascontiguousarray(w, dtype=np.float64)
+    z = np.zeros(n)
     work = np.empty(8 * n)
     st = np.zeros(3)
     nth = nthreads or lib.orc_max_threads()
     t0 = time.perf_counter()
-    lib.orc_steady_bicgstab(n, rp.ctypes.data, ci.ctypes.data, va.ctypes.data, bb.ctypes.data, x.ctypes.data,
-                            float(rtol), int(maxit), int(nth), work.ctypes.data, st.ctypes.data)
+    lib.orc_steady_bicgstab(n, rp.ctypes.data, ci.ctypes.data, va.ctypes.data, bb.ctypes.data,
+                            None if wp is None else wp.ctypes.data, bnorm, z.ctypes.data, float(rtol), int(maxit),
+                            float(max_seconds), int(nth), work.ctypes.data, st.ctypes.data)
     dt = time.perf_counter() - t0
-    return x, {"iterations": int(st[0]), "rel_residual": float(st[1]), "converged": bool(st[2]), "seconds": dt,
-               "threads": nth}
+    return z + xfix, {"iterations": int(st[0]), "rel_residual": float(st[1]), "converged": bool(st[2]),
+                      "seconds": dt, "threads": nth}
 
 
 def max_threads() -> int:

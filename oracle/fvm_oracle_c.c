@@ -262,27 +262,36 @@ void orc_gray_scott_rhs_threaded(const orc_problem* P, const orc_gray_scott* G, 
  * (src/specific_problems/poissons_equation.jl:81, mean_exit_time.jl:76) with a sparse direct
  * method.  This baseline is a threaded FP64 BiCGStab with a Jacobi preconditioner (right
  * preconditioning, van der Vorst 1992) on the CSR matrix A, stopped when the true residual
- * ||b - A x|| / ||b|| reaches rtol: the same method and stopping test as the GPU's plain FP64
- * solve, on all host threads.  stats = {iterations, relative residual, converged}. */
-static void csr_mv(int64_t n, const int64_t* rp, const int32_t* ci, const double* va, const double* x, double* y) {
-#pragma omp for schedule(static)
-    for (int64_t i = 0; i < n; ++i) {
-        double s = 0.0;
-        for (int64_t q = rp[i]; q < rp[i + 1]; ++q) s += va[q] * x[ci[q]];
-        y[i] = s;
-    }
+ * ||b - A x|| / ||b|| reaches rtol (or after max_seconds): the same method and stopping test as
+ * the GPU's plain FP64 solve, on all host threads, with the inner products summed in a fixed
+ * order.  stats = {iterations, relative residual, converged}. */
+
+/* Sum of the threads' partials in thread order (deterministic for a given thread count,
+ * unlike an OpenMP reduction clause, whose combination order is unspecified). */
+static double ordered_sum(const double* part, int nth, int q) {
+    double s = 0.0;
+    for (int c = 0; c < nth; ++c) s += part[4 * c + q];
+    return s;
 }
 
-void orc_steady_bicgstab(int64_t n, const int64_t* rp, const int32_t* ci, const double* va, const double* b, double* x,
-                         double rtol, int64_t maxit, int nthreads, double* work, double* stats) {
+void orc_steady_bicgstab(int64_t n, const int64_t* rp, const int32_t* ci, const double* va, const double* b,
+                         const double* w, double bnorm, double* x, double rtol, int64_t maxit, double max_seconds,
+                         int nthreads, double* work, double* stats) {
 #ifdef _OPENMP
     if (nthreads <= 0) nthreads = omp_get_max_threads();
+#else
+    nthreads = 1;
 #endif
     double *r = work, *rh = work + n, *p = work + 2 * n, *v = work + 3 * n, *ph = work + 4 * n, *sh = work + 5 * n,
            *t = work + 6 * n, *dinv = work + 7 * n;
+    double part[4 * 512];
+    if (nthreads > 512) nthreads = 512;
+    /* the stopping norm ||w (b - A x)|| against rtol * bnorm (w = NULL: the plain 2-norm and
+     * bnorm = ||b||) */
     double bn2 = 0.0;
-    for (int64_t i = 0; i < n; ++i) bn2 += b[i] * b[i];
-    const double tol = rtol * sqrt(bn2);
+    for (int64_t i = 0; i < n; ++i) bn2 += (w ? w[i] * b[i] : b[i]) * (w ? w[i] * b[i] : b[i]);
+    if (!(bnorm > 0)) bnorm = sqrt(bn2);
+    const double tol = rtol * bnorm;
     for (int64_t i = 0; i < n; ++i) {
         double d = 0.0;
         for (int64_t q = rp[i]; q < rp[i + 1]; ++q)
@@ -292,26 +301,38 @@ void orc_steady_bicgstab(int64_t n, const int64_t* rp, const int32_t* ci, const 
     int64_t it = 0;
     double rn = 0.0;
     int converged = 0;
-    /* shared scalars, written by one thread between barriers */
-    double rho = 1.0, alpha = 1.0, omega = 1.0, dot1 = 0.0, dot2 = 0.0, dot3 = 0.0;
+    double rho = 1.0, alpha = 1.0, omega = 1.0;
     int restart = 1, stop = 0;
+#ifdef _OPENMP
+    const double t_start = omp_get_wtime();
+#endif
 #pragma omp parallel num_threads(nthreads)
     {
+#ifdef _OPENMP
+        const int c = omp_get_thread_num(), nth = omp_get_num_threads();
+#else
+        const int c = 0, nth = 1;
+#endif
+        /* each thread owns the contiguous rows [i0, i1) in every loop */
+        const int64_t i0 = n * c / nth, i1 = n * (c + 1) / nth;
+        double* my = part + 4 * c;
         while (!stop) {
             if (restart) {
-                csr_mv(n, rp, ci, va, x, t);
-#pragma omp single
-                dot1 = 0.0;
-#pragma omp for reduction(+ : dot1) schedule(static)
-                for (int64_t i = 0; i < n; ++i) {
-                    r[i] = b[i] - t[i];
+                double a0 = 0.0;
+                for (int64_t i = i0; i < i1; ++i) {
+                    double sacc = 0.0;
+                    for (int64_t q = rp[i]; q < rp[i + 1]; ++q) sacc += va[q] * x[ci[q]];
+                    r[i] = b[i] - sacc;
                     rh[i] = r[i];
                     p[i] = v[i] = 0.0;
-                    dot1 += r[i] * r[i];
+                    const double wr = w ? w[i] * r[i] : r[i];
+                    a0 += wr * wr;
                 }
+                my[0] = a0;
+#pragma omp barrier
 #pragma omp single
                 {
-                    rn = sqrt(dot1);
+                    rn = sqrt(ordered_sum(part, nth, 0));
                     rho = alpha = omega = 1.0;
                     restart = 0;
                     if (rn <= tol) {
@@ -320,61 +341,82 @@ void orc_steady_bicgstab(int64_t n, const int64_t* rp, const int32_t* ci, const 
                     } else if (it >= maxit) {
                         stop = 1;
                     }
+#ifdef _OPENMP
+                    if (omp_get_wtime() - t_start > max_seconds) stop = 1;
+#endif
                 }
                 if (stop) break;
             }
-#pragma omp single
-            dot1 = 0.0;
-#pragma omp for reduction(+ : dot1) schedule(static)
-            for (int64_t i = 0; i < n; ++i) dot1 += rh[i] * r[i];
-            const double rho_new = dot1;
+            double a0 = 0.0;
+            for (int64_t i = i0; i < i1; ++i) a0 += rh[i] * r[i];
+            my[0] = a0;
+#pragma omp barrier
+            const double rho_new = ordered_sum(part, nth, 0);
             const double beta = (rho_new / rho) * (alpha / omega);
-#pragma omp for schedule(static)
-            for (int64_t i = 0; i < n; ++i) {
+            for (int64_t i = i0; i < i1; ++i) {
                 p[i] = r[i] + beta * (p[i] - omega * v[i]);
                 ph[i] = dinv[i] * p[i];
             }
-            csr_mv(n, rp, ci, va, ph, v);
-#pragma omp single
-            dot2 = 0.0;
-#pragma omp for reduction(+ : dot2) schedule(static)
-            for (int64_t i = 0; i < n; ++i) dot2 += rh[i] * v[i];
-            const double al = rho_new / dot2;
-#pragma omp for schedule(static)
-            for (int64_t i = 0; i < n; ++i) {
+#pragma omp barrier
+            a0 = 0.0;
+            for (int64_t i = i0; i < i1; ++i) {
+                double sacc = 0.0;
+                for (int64_t q = rp[i]; q < rp[i + 1]; ++q) sacc += va[q] * ph[ci[q]];
+                v[i] = sacc;
+                a0 += rh[i] * sacc;
+            }
+            my[1] = a0;
+#pragma omp barrier
+            const double al = rho_new / ordered_sum(part, nth, 1);
+            for (int64_t i = i0; i < i1; ++i) {
                 r[i] = r[i] - al * v[i]; /* s */
                 sh[i] = dinv[i] * r[i];
             }
-            csr_mv(n, rp, ci, va, sh, t);
-#pragma omp single
-            dot1 = dot2 = 0.0;
-#pragma omp for reduction(+ : dot1, dot2) schedule(static)
-            for (int64_t i = 0; i < n; ++i) {
-                dot1 += t[i] * r[i];
-                dot2 += t[i] * t[i];
+#pragma omp barrier
+            double a1 = 0.0, a2 = 0.0;
+            for (int64_t i = i0; i < i1; ++i) {
+                double sacc = 0.0;
+                for (int64_t q = rp[i]; q < rp[i + 1]; ++q) sacc += va[q] * sh[ci[q]];
+                t[i] = sacc;
+                a1 += sacc * r[i];
+                a2 += sacc * sacc;
             }
-            const double om = dot2 > 0.0 ? dot1 / dot2 : 0.0;
-#pragma omp single
-            dot3 = 0.0;
-#pragma omp for reduction(+ : dot3) schedule(static)
-            for (int64_t i = 0; i < n; ++i) {
-                x[i] += al * ph[i] + om * sh[i];
-                r[i] = r[i] - om * t[i];
-                dot3 += r[i] * r[i];
-            }
+            my[2] = a1;
+            my[3] = a2;
+#pragma omp barrier
+            const double tt = ordered_sum(part, nth, 3);
+            const double om = tt > 0.0 ? ordered_sum(part, nth, 2) / tt : 0.0;
+            /* a breakdown (non-finite step) leaves x as it is and restarts from its residual */
+            const int good = isfinite(al) && isfinite(om);
+            double a3 = 0.0;
+            if (good)
+                for (int64_t i = i0; i < i1; ++i) {
+                    x[i] += al * ph[i] + om * sh[i];
+                    r[i] = r[i] - om * t[i];
+                    const double wr = w ? w[i] * r[i] : r[i];
+                    a3 += wr * wr;
+                }
+            else
+                a3 = NAN;
+            my[0] = a3;
+#pragma omp barrier
 #pragma omp single
             {
+                const double rr = ordered_sum(part, nth, 0);
                 rho = rho_new;
                 alpha = al;
                 omega = om;
                 ++it;
                 /* recurrence converged (or broke down): confirm with the true residual */
-                if (sqrt(dot3) <= tol || !(om != 0.0) || !isfinite(dot3) || it >= maxit) restart = 1;
+                if (sqrt(rr) <= tol || !(om != 0.0) || !isfinite(rr) || it >= maxit) restart = 1;
+#ifdef _OPENMP
+                if (it % 64 == 0 && omp_get_wtime() - t_start > max_seconds) restart = 1;
+#endif
             }
         }
     }
     stats[0] = (double)it;
-    stats[1] = bn2 > 0 ? rn / sqrt(bn2) : rn;
+    stats[1] = bnorm > 0 ? rn / bnorm : rn;
     stats[2] = (double)converged;
 }
 

@@ -51,8 +51,12 @@ def test_threaded_steady_bicgstab_matches_direct_solve():
     conds = O.Conditions(tri, [lambda x, y, t, u: 0.0 * x], ["Dirichlet"])
     A, b = O.template_poisson(tri, conds, lambda x, y: np.where(x * x + y * y < 0.25, 1.0, 10.0),
                               lambda x, y: -1.0 + 0.0 * x)
-    x, st = B.steady_bicgstab(A, b, rtol=1e-10, nthreads=2)
-    assert st["converged"] and st["rel_residual"] <= 1e-10
-    assert np.linalg.norm(b - A @ x) <= 1e-10 * np.linalg.norm(b)
     ref = O.steady_solve(A, b)
-    assert np.linalg.norm(x - ref) <= 1e-8 * np.linalg.norm(ref)
+    V = O.Geometry(tri.points, tri.triangles).cv_volumes
+    for v in (None, V):  # A x = b directly, and the GPU solver's reduced system
+        x, st = B.steady_bicgstab(A, b, rtol=1e-10, nthreads=2, V=v)
+        assert st["converged"] and st["rel_residual"] <= 1e-10
+        assert np.linalg.norm(b - A @ x) <= 1.5e-10 * np.linalg.norm(b)
+        assert np.linalg.norm(x - ref) <= 1e-8 * np.linalg.norm(ref)
+        x2, st2 = B.steady_bicgstab(A, b, rtol=1e-10, nthreads=2, V=v)
+        assert np.array_equal(x, x2) and st2["iterations"] == st["iterations"]  # fixed summation order
