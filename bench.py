@@ -583,7 +583,8 @@ def run_steady(args, F):
                 r["fl_xstar_residual"] = STEADY_FLOOR[label]
             modes = [("fp64", "chebyshev", 4), ("mixed", "chebyshev", 4), ("fp64", "chebyshev", 8),
                      ("mixed", "chebyshev", 8)]
-            modes += [("fp64", "chebyshev", 16), ("mixed", "chebyshev", 16)] if dkind == "const" else [("fp64", "jacobi", 0)]
+            if dkind != "const":
+                modes += [("fp64", "jacobi", 0)]
             for mode, precond, deg in modes:
                 key = f"{mode}_{precond}{deg or ''}"
                 try:
@@ -594,7 +595,7 @@ def run_steady(args, F):
                 st = sol.stats
                 r[key] = {"ms": st["elapsed_ms"], "it": st["iterations"], "res": st["rel_residual"], "conv": conv,
                           "method": st["method"], **({"fallback_fp64": True} if st["fallback_fp64"] else {})}
-            for deg in (4, 8, 16):
+            for deg in (4, 8):
                 a_, b_ = r.get(f"fp64_chebyshev{deg}"), r.get(f"mixed_chebyshev{deg}")
                 if a_ and b_ and a_["conv"] and b_["conv"]:
                     r[f"speedup_mixed_vs_fp64_chebyshev{deg}"] = a_["ms"] / b_["ms"]
