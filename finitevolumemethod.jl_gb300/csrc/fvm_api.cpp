@@ -148,7 +148,8 @@ static void tsit5_run(OdeRhs& rhs, int64_t n, const double* u0_int, const fvm_od
     const double beta1 = 7.0 / 50.0, beta2 = 2.0 / 25.0, qmin = 0.2, qmax = 10.0, gamma = 0.9;
     double qold = 1e-4;
     // fixed steps with nothing to save before tf run as a captured CUDA graph
-    bool graph_ok = !o.adaptive && o.use_graph && si + 1 == saveat.size() && saveat.back() == o.tf;
+    bool graph_ok = !o.adaptive && o.use_graph && si + 1 == saveat.size() && saveat.back() == o.tf &&
+                    !rhs.time_dependent;
     int64_t nfixed = o.adaptive ? 0 : (int64_t)std::ceil(tspan / dt - 1e-9);
     if (!o.adaptive && nfixed > max_steps) fail(FVM_ERR_STEP_LIMIT, "fixed-step Tsit5 needs more than max_steps steps");
     int64_t step = 0;
@@ -256,7 +257,7 @@ static void tsit5_run(OdeRhs& rhs, int64_t n, const double* u0_int, const fvm_od
     const bool use_cluster = o.adaptive && o.use_graph && rhs.sell.pat && rhs.sell.val &&
                              (rhs.callback == nullptr || rhs.sell.ndir > 0) && cluster_tsit5_available(*rhs.sell.pat);
     while (o.adaptive ? t < o.tf : step < nfixed) {
-        if (o.adaptive && o.use_graph && nacc >= 1) {
+        if (o.adaptive && o.use_graph && nacc >= 1 && !rhs.time_dependent) {
             driver = use_cluster ? FVM_DRIVER_CLUSTER : FVM_DRIVER_DEVICE_LOOP;
             device_loop(use_cluster);
             break;
@@ -342,7 +343,8 @@ static void tsit5_run(OdeRhs& rhs, int64_t n, const double* u0_int, const fvm_od
         bool reeval = false;
         if (rhs.callback) {
             rhs.callback(u, t, s);
-            reeval = first_callback;  // later updates rewrite the same constant values
+            // later updates rewrite the same values unless they depend on t
+            reeval = first_callback || rhs.callback_varies;
             first_callback = false;
         }
         while (si < saveat.size() && saveat[si] == t) save_copy(u);
@@ -431,13 +433,33 @@ static void rhs_outputs(fvm_problem* p, double* du, int32_t loc, cudaStream_t s)
     }
 }
 
+static TimeTaus time_taus(const fvm_problem* p, double t) {
+    TimeTaus tt{};
+    for (int g = 0; g < p->ntime; ++g) tt.tau[g] = time_factor_value(&p->tfac[4 * g], t);
+    return tt;
+}
+
+void problem_dirichlet_internal(const fvm_problem* p, double* u, double t, cudaStream_t s) {
+    if (p->ntime > 0)
+        launch_dirichlet_time(p->d_dir_idx.as<int32_t>(), p->d_dir_val.as<double>(), p->d_tdir.as<double>(),
+                              time_taus(p, t), p->ntime, u, p->ndir, s);
+    else
+        launch_dirichlet(p->d_dir_idx.as<int32_t>(), p->d_dir_val.as<double>(), u, p->ndir, s);
+}
+
 // fvm_eqs! in the internal numbering
 void problem_rhs_internal(fvm_problem* p, const double* u, double* du, bool force_triangle, cudaStream_t s,
-                          bool conservative) {
+                          bool conservative, double t) {
     fvm_mesh* m = p->mesh;
+    if (p->ntime > 0 && force_triangle)
+        fail(FVM_ERR_UNSUPPORTED, "time-dependent values run on the operator path only (no force_triangle)");
     if (p->linear && !force_triangle) {
         const double* dg = p->has_d ? p->d_d.as<double>() : nullptr;
         const double* b = p->has_b ? p->d_b.as<double>() : nullptr;
+        if (p->ntime > 0) {  // b(t) = b + sum_g tau_g(t) b_g
+            launch_time_b(b, p->d_tb.as<double>(), time_taus(p, t), p->ntime, p->d_beff.as<double>(), m->np, s);
+            b = p->d_beff.as<double>();
+        }
         const double* q = p->has_q ? p->d_q.as<double>() : nullptr;
         if (p->precision == FVM_FP32) {
             launch_to_f32(u, p->d_u32.as<float>(), m->np, s);
@@ -651,11 +673,10 @@ int fvm_rhs(fvm_problem* p, const double* u, double* du, double t, int32_t flags
         cudaStream_t s = (cudaStream_t)stream;
         int32_t loc = flags & 3;
         if (loc > FVM_PTR_DEVICE_INTERNAL) fail(FVM_ERR_INVALID_ARGUMENT, "bad pointer-location flag");
-        (void)t;  // device-coded forms are time independent
         IoPlan io;
         rhs_inputs(p, u, du, loc, io, s);
         problem_rhs_internal(p, io.uin, io.dout, (flags & FVM_RHS_FORCE_TRIANGLE) != 0, s,
-                             (flags & FVM_RHS_CONSERVATIVE) != 0);
+                             (flags & FVM_RHS_CONSERVATIVE) != 0, t);
         check_launch();
         rhs_outputs(p, du, loc, s);
         return FVM_OK;
@@ -665,19 +686,18 @@ int fvm_rhs(fvm_problem* p, const double* u, double* du, double t, int32_t flags
 int fvm_dirichlet_apply(fvm_problem* p, double* u, double t, int32_t flags, void* stream) {
     return guard([&] {
         if (!p || !u) fail(FVM_ERR_INVALID_ARGUMENT, "NULL argument");
-        (void)t;
         cudaStream_t s = (cudaStream_t)stream;
         fvm_mesh* m = p->mesh;
         int32_t loc = flags & 3;
         if (loc == FVM_PTR_DEVICE_INTERNAL) {
-            launch_dirichlet(p->d_dir_idx.as<int32_t>(), p->d_dir_val.as<double>(), u, p->ndir, s);
+            problem_dirichlet_internal(p, u, t, s);
         } else {
             p->ensure_work();
             if (loc == FVM_PTR_HOST)
                 FVM_CUDA(cudaMemcpyAsync(p->d_ref.p, u, sizeof(double) * m->np, cudaMemcpyHostToDevice, s));
             const double* src = loc == FVM_PTR_HOST ? p->d_ref.as<double>() : u;
             launch_permute_in(m->d_perm.as<int32_t>(), src, p->d_u.as<double>(), m->np, s);
-            launch_dirichlet(p->d_dir_idx.as<int32_t>(), p->d_dir_val.as<double>(), p->d_u.as<double>(), p->ndir, s);
+            problem_dirichlet_internal(p, p->d_u.as<double>(), t, s);
             double* dst = loc == FVM_PTR_HOST ? p->d_ref.as<double>() : u;
             launch_permute_out(m->d_perm.as<int32_t>(), p->d_u.as<double>(), dst, m->np, s);
             if (loc == FVM_PTR_HOST) {
@@ -706,12 +726,14 @@ int fvm_tsit5_solve(fvm_problem* p, const double* u0, const fvm_ode_options* opt
         FVM_CUDA(cudaMemcpyAsync(d_ref, u0, sizeof(double) * n, cudaMemcpyHostToDevice, s));
         launch_permute_in(m->d_perm.as<int32_t>(), d_ref, d_u0, n, s);
         OdeRhs rhs;
-        rhs.f = [p](const double* u, double* du, double, cudaStream_t st) { problem_rhs_internal(p, u, du, false, st); };
+        rhs.f = [p](const double* u, double* du, double t, cudaStream_t st) {
+            problem_rhs_internal(p, u, du, false, st, false, t);
+        };
         if (p->ndir > 0)
-            rhs.callback = [p](double* u, double, cudaStream_t st) {
-                launch_dirichlet(p->d_dir_idx.as<int32_t>(), p->d_dir_val.as<double>(), u, p->ndir, st);
-            };
-        if (p->linear && p->precision != FVM_FP32) {  // problem_rhs_internal's explicit FP64 path
+            rhs.callback = [p](double* u, double t, cudaStream_t st) { problem_dirichlet_internal(p, u, t, st); };
+        rhs.time_dependent = p->ntime > 0;
+        rhs.callback_varies = p->tdir_varies;
+        if (p->linear && p->precision != FVM_FP32 && p->ntime == 0) {  // problem_rhs_internal's explicit FP64 path
             rhs.sell.pat = &m->pat;
             rhs.sell.val = p->d_val64.as<double>();
             rhs.sell.b = p->has_b ? p->d_b.as<double>() : nullptr;

@@ -1,6 +1,7 @@
 // Internal declarations of libfvmgpu: handles, device buffers, kernel launchers.
 #pragma once
 #include <cuda_runtime.h>
+#include <cmath>
 #include <cstdint>
 #include <cstddef>
 #include <string>
@@ -122,6 +123,13 @@ struct fvm_problem {
     std::vector<int8_t> code;                   // [np] caller order
     std::vector<int8_t> bneu;                   // [nbe]
     std::vector<double> dualD, quarterD, quarterN, src, dudt, dirv;  // copies of the descriptor arrays
+    std::vector<double> dualM, quarterM;        // a linear flux q = M (alpha, beta, gamma), 6 per point
+    bool flux_linear = false;
+    // time factors: b(t) = b + sum_g tau_g(t) b_g, Dirichlet values val + sum_g tau_g(t) val_g
+    int ntime = 0;
+    bool tdir_varies = false;                   // some time-dependent Dirichlet value is nonzero
+    std::vector<double> tfac;                   // [ntime][4] kind, t_ref, a, b
+    fvm::DBuf d_tb, d_tdir, d_beff;             // [ntime][np] internal, [ntime][ndir], [np]
     // linear operator path, explicit form on the pattern with the diagonal (default):
     //   du_i = rowscale_i * sum_j A_ij u_j + b_i + q_i u_i^2
     // and difference form on the off-diagonal pattern (FVM_RHS_CONSERVATIVE):
@@ -331,6 +339,11 @@ struct OdeRhs {
     std::function<void(const double*, double*, double, cudaStream_t)> f;
     std::function<void(double*, double, cudaStream_t)> callback;  // may be empty
     SellRhsDesc sell;  // set when f (and callback) are exactly the described product and update
+    // f depends on t: every step runs on the host-controlled loop (captured steps replay fixed t)
+    bool time_dependent = false;
+    // the callback's values depend on t: it changes u after every step, so the first-same-as-
+    // last derivative is evaluated again after it (as after the first callback otherwise)
+    bool callback_varies = false;
 };
 
 // the cluster-resident adaptive Tsit5 driver (fvm_cluster.cu); meshes up to kClusterMaxRows
@@ -348,5 +361,21 @@ void tsit5_run_internal(OdeRhs& rhs, int64_t n, const double* u0_int, const fvm_
                         fvm_ode_stats* st, cudaStream_t s);
 int guard_call(const std::function<int()>& f);
 void problem_rhs_internal(fvm_problem* p, const double* u, double* du, bool force_triangle, cudaStream_t s,
-                          bool conservative = false);
+                          bool conservative = false, double t = 0.0);
+// the problem's Dirichlet update u_i = a(x_i, y_i, t) in the internal numbering
+void problem_dirichlet_internal(const fvm_problem* p, double* u, double t, cudaStream_t s);
+// tau(t) of a time factor {kind, t_ref, a, b}
+inline double time_factor_value(const double* f, double t) {
+    const double d = t - f[1];
+    return f[0] == 1.0 ? std::exp(f[2] * d) : 1.0 + d * (f[2] + d * f[3]);
+}
+constexpr int kMaxTime = FVM_MAX_TIME_FACTORS;
+struct TimeTaus {
+    double tau[kMaxTime];
+};
+// out = b + sum_g tau_g tb[g] (b may be null); u[idx[k]] = val[k] + sum_g tau_g tval[g][k]
+void launch_time_b(const double* b, const double* tb, const TimeTaus& tt, int ntime, double* out, int64_t n,
+                   cudaStream_t s);
+void launch_dirichlet_time(const int32_t* idx, const double* val, const double* tval, const TimeTaus& tt, int ntime,
+                           double* u, int64_t n, cudaStream_t s);
 }  // namespace fvm

@@ -253,6 +253,34 @@ void launch_dirichlet(const int32_t* idx, const double* val, double* u, int64_t 
     if (n) dirichlet_kernel<<<grid_for(n, 256), 256, 0, s>>>(idx, val, u, n);
 }
 
+// Time-dependent values: v = v_static + sum_g tau_g(t) v_g, the tau_g evaluated on the host.
+__global__ void time_b_kernel(const double* __restrict__ b, const double* __restrict__ tb, TimeTaus tt, int ntime,
+                              double* __restrict__ out, int64_t n) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double v = b ? b[i] : 0.0;
+    for (int g = 0; g < ntime; ++g) v = fma(tt.tau[g], tb[g * n + i], v);
+    out[i] = v;
+}
+void launch_time_b(const double* b, const double* tb, const TimeTaus& tt, int ntime, double* out, int64_t n,
+                   cudaStream_t s) {
+    if (n) time_b_kernel<<<grid_for(n, 256), 256, 0, s>>>(b, tb, tt, ntime, out, n);
+}
+
+__global__ void dirichlet_time_kernel(const int32_t* __restrict__ idx, const double* __restrict__ val,
+                                      const double* __restrict__ tval, TimeTaus tt, int ntime, double* __restrict__ u,
+                                      int64_t n) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double v = val[i];
+    for (int g = 0; g < ntime; ++g) v = fma(tt.tau[g], tval[g * n + i], v);
+    u[idx[i]] = v;
+}
+void launch_dirichlet_time(const int32_t* idx, const double* val, const double* tval, const TimeTaus& tt, int ntime,
+                           double* u, int64_t n, cudaStream_t s) {
+    if (n) dirichlet_time_kernel<<<grid_for(n, 256), 256, 0, s>>>(idx, val, tval, tt, ntime, u, n);
+}
+
 // ---------------------------------------------------------------------------------------
 // Per-triangle flux kernel (generic fvm_eqs! for any device-coded form).
 // One CTA per vertex tile; the CTA walks every triangle touching the tile (coalesced SoA

@@ -48,7 +48,6 @@ double* scratch_for_current_device() {
 extern "C" int fvm_rhs_noalloc(fvm_problem* p, const double* u, double* du, double t, void* stream) {
     return fvm::guard_call([&] {
         if (!p || !u || !du) fvm::fail(FVM_ERR_INVALID_ARGUMENT, "NULL argument");
-        (void)t;  // device-coded forms are time independent
         const fvm_mesh* m = p->mesh;
         int dev = -1;
         FVM_CUDA(cudaGetDevice(&dev));
@@ -71,7 +70,7 @@ extern "C" int fvm_rhs_noalloc(fvm_problem* p, const double* u, double* du, doub
         // every entry of both halves is written before it is read, so stale contents from an
         // earlier call never leak into this one
         fvm::launch_permute_in(m->d_perm.as<int32_t>(), u, u_int, m->np, s);
-        fvm::problem_rhs_internal(p, u_int, du_int, false, s);
+        fvm::problem_rhs_internal(p, u_int, du_int, false, s, false, t);
         fvm::launch_permute_out(m->d_perm.as<int32_t>(), du_int, du, m->np, s);
         FVM_CUDA(cudaGetLastError());
         return FVM_OK;

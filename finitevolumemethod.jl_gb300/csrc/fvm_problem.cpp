@@ -23,6 +23,10 @@ void fvm_problem::ensure_work() {
 //   triangle dual edge e of T = (a, b, c): Q_e = -D_e l_e (alpha n_x + beta n_y)
 //   boundary half edge (non-Neumann):      Q_h = -D_h l_h (alpha n_x + beta n_y)
 //   boundary half edge (Neumann, a = n0 + n1 u(m)): Q_h = l_h (n0 + n1 u(m)).
+// With a linear flux q = M (alpha, beta, gamma) the dual-edge and half-edge fluxes are
+//   Q = l ((n_x M0 + n_y M3) alpha + (n_x M1 + n_y M4) beta + (n_x M2 + n_y M5) gamma),
+// alpha, beta, gamma being s1..s9 combinations of the triangle's values (shape_functions.jl:2-9);
+// the alpha, beta part sums to zero along a row (a flux term), the gamma part does not.
 // The visitor reports each coefficient as emit(row, col, coef, didx, flux) (caller numbering):
 // the contribution to A_row,col is coef * D[didx] when didx >= 0 (D indexed over the dual edges,
 // 3 per triangle, then the boundary quarter points, 2 per edge), coef otherwise.  `flux` marks
@@ -34,6 +38,12 @@ void fvm_visit_linear_terms(const fvm_problem* p, const LinearTermSink& emit, st
     b.assign(m->np, 0.0);
     q.assign(m->np, 0.0);
     rowscale.assign(m->np, 0.0);
+    // l (n . q) per unit alpha, beta, gamma of a linear flux sampled as M[6] at the point
+    auto nq = [](const double* M, double nx, double ny, double g[3]) {
+        g[0] = nx * M[0] + ny * M[3];
+        g[1] = nx * M[1] + ny * M[4];
+        g[2] = nx * M[2] + ny * M[5];
+    };
     for (int64_t t = 0; t < m->nt; ++t) {
         const int32_t* w = &m->tri[3 * t];
         const double* pr = &m->props[24 * t];
@@ -41,6 +51,22 @@ void fvm_visit_linear_terms(const fvm_problem* p, const LinearTermSink& emit, st
             int32_t e1 = w[e], e2 = w[(e + 1) % 3];
             double l = pr[21 + e], nx = pr[15 + 2 * e], ny = pr[16 + 2 * e];
             bool f1 = p->code[e1] == FVM_VERTEX_FREE, f2 = p->code[e2] == FVM_VERTEX_FREE;
+            if (p->flux_linear) {  // e1 loses Q_e, e2 gains it
+                double g[3];
+                nq(&p->dualM[6 * (3 * t + e)], nx, ny, g);
+                for (int v = 0; v < 3; ++v) {
+                    const double cg = l * (g[0] * pr[v] + g[1] * pr[3 + v]), cz = l * g[2] * pr[6 + v];
+                    if (f1) {
+                        emit(e1, w[v], -cg / m->vol[e1], -1, true);
+                        if (cz != 0) emit(e1, w[v], -cz / m->vol[e1], -1, false);
+                    }
+                    if (f2) {
+                        emit(e2, w[v], cg / m->vol[e2], -1, true);
+                        if (cz != 0) emit(e2, w[v], cz / m->vol[e2], -1, false);
+                    }
+                }
+                continue;
+            }
             for (int v = 0; v < 3; ++v) {
                 double a = l * (pr[v] * nx + pr[3 + v] * ny);
                 if (f1) emit(e1, w[v], a / m->vol[e1], 3 * t + e, true);
@@ -82,6 +108,22 @@ void fvm_visit_linear_terms(const fvm_problem* p, const LinearTermSink& emit, st
         int32_t t = m->btri[e];
         const int32_t* w = &m->tri[3 * t];
         const double* pr = &m->props[24 * t];
+        if (p->flux_linear) {  // du_i -= Q(m_i), du_j -= Q(m_j)
+            double gi[3], gj[3];
+            nq(&p->quarterM[6 * (2 * e)], nx, ny, gi);
+            nq(&p->quarterM[6 * (2 * e + 1)], nx, ny, gj);
+            for (int v = 0; v < 3; ++v) {
+                if (fi) {
+                    emit(i, w[v], -lh * (gi[0] * pr[v] + gi[1] * pr[3 + v]) / m->vol[i], -1, true);
+                    if (gi[2] != 0) emit(i, w[v], -lh * gi[2] * pr[6 + v] / m->vol[i], -1, false);
+                }
+                if (fj) {
+                    emit(j, w[v], -lh * (gj[0] * pr[v] + gj[1] * pr[3 + v]) / m->vol[j], -1, true);
+                    if (gj[2] != 0) emit(j, w[v], -lh * gj[2] * pr[6 + v] / m->vol[j], -1, false);
+                }
+            }
+            continue;
+        }
         for (int v = 0; v < 3; ++v) {
             double c = lh * (pr[v] * nx + pr[3 + v] * ny);
             if (fi) emit(i, w[v], c / m->vol[i], q0 + 2 * e, true);
@@ -108,6 +150,29 @@ void fvm_visit_linear_terms(const fvm_problem* p, const LinearTermSink& emit, st
             }
         }
     }
+}
+
+// Constant terms of one time factor's values (time_neumann, time_source, time_dudt of the
+// descriptor), in the internal numbering: the parts of fvm_visit_linear_terms that reach b.
+static std::vector<double> time_constant_terms(const fvm_problem* p, const double* neu, const double* src,
+                                               const double* dudt) {
+    const fvm_mesh* m = p->mesh;
+    std::vector<double> b(m->np, 0.0);
+    if (neu)
+        for (int64_t e = 0; e < m->nbe; ++e) {
+            if (!p->bneu[e]) continue;
+            int32_t i = m->be[2 * e], j = m->be[2 * e + 1];
+            double px = m->pts[2 * i], py = m->pts[2 * i + 1], qx = m->pts[2 * j], qy = m->pts[2 * j + 1];
+            double mijx = (px + qx) / 2, mijy = (py + qy) / 2;
+            double lh = std::sqrt((mijx - px) * (mijx - px) + (mijy - py) * (mijy - py));
+            if (p->code[i] == FVM_VERTEX_FREE) b[m->iperm[i]] -= lh * neu[2 * e] / m->vol[i];
+            if (p->code[j] == FVM_VERTEX_FREE) b[m->iperm[j]] -= lh * neu[2 * e + 1] / m->vol[j];
+        }
+    for (int64_t v = 0; v < m->np; ++v) {
+        if (p->code[v] == FVM_VERTEX_FREE && src) b[m->iperm[v]] += src[v];
+        if (p->code[v] == FVM_VERTEX_DUDT && dudt) b[m->iperm[v]] = dudt[v];
+    }
+    return b;
 }
 
 // Two equivalent storages are produced from the same contributions:
@@ -181,7 +246,16 @@ extern "C" int fvm_problem_create_impl(fvm_mesh* mesh, const fvm_problem_desc* d
     copy(d->source, (size_t)m->np * (p->src_deg + 1), p->src);
     copy(d->dudt, (size_t)m->np * (p->dudt_deg + 1), p->dudt);
     copy(d->dirichlet, (size_t)m->np, p->dirv);
-    for (const auto* arr : {&p->dualD, &p->quarterD, &p->quarterN, &p->src, &p->dudt, &p->dirv})
+    if (d->dual_edge_flux) {  // a flux linear in (alpha, beta, gamma): no diffusivity samples
+        if (m->nbe > 0 && !d->quarter_flux) fail(FVM_ERR_INVALID_ARGUMENT, "quarter_flux is required with dual_edge_flux");
+        p->flux_linear = true;
+        p->dif_deg = 0;
+        p->dualD.clear();
+        p->quarterD.clear();
+        copy(d->dual_edge_flux, (size_t)m->nt * 3 * 6, p->dualM);
+        copy(d->quarter_flux, (size_t)m->nbe * 2 * 6, p->quarterM);
+    }
+    for (const auto* arr : {&p->dualD, &p->quarterD, &p->quarterN, &p->src, &p->dudt, &p->dirv, &p->dualM, &p->quarterM})
         for (double x : *arr)
             if (!std::isfinite(x)) fail(FVM_ERR_INVALID_ARGUMENT, "sampled closure values must be finite");
     // a form is linear when it is affine in u, except a u^2 term on a vertex's own value
@@ -210,6 +284,49 @@ extern "C" int fvm_problem_create_impl(fvm_mesh* mesh, const fvm_problem_desc* d
         p->ndir = (int64_t)idx.size();
         p->d_dir_idx.upload(idx);
         p->d_dir_val.upload(val);
+        if (d->ntime < 0 || d->ntime > FVM_MAX_TIME_FACTORS)
+            fail(FVM_ERR_INVALID_ARGUMENT, "ntime must lie in [0, FVM_MAX_TIME_FACTORS]");
+        if (d->ntime > 0) {
+            if (!p->linear)
+                fail(FVM_ERR_UNSUPPORTED_FORM, "time-dependent values are supported for linear problems only");
+            if (!d->time_factor) fail(FVM_ERR_INVALID_ARGUMENT, "time_factor is required when ntime > 0");
+            p->ntime = d->ntime;
+            p->tfac.assign(d->time_factor, d->time_factor + 4 * p->ntime);
+            for (int g = 0; g < p->ntime; ++g) {
+                const double* f = &p->tfac[4 * g];
+                if (f[0] != 1.0 && f[0] != 2.0) fail(FVM_ERR_INVALID_ARGUMENT, "time_factor kind must be 1 or 2");
+                if (!std::isfinite(f[1]) || !std::isfinite(f[2]) || !std::isfinite(f[3]))
+                    fail(FVM_ERR_INVALID_ARGUMENT, "time_factor values must be finite");
+            }
+            auto finite = [](const double* a, size_t n) {
+                for (size_t i = 0; a && i < n; ++i)
+                    if (!std::isfinite(a[i])) fail(FVM_ERR_INVALID_ARGUMENT, "time-dependent values must be finite");
+            };
+            std::vector<double> tb((size_t)p->ntime * m->np), tdir((size_t)p->ntime * std::max<int64_t>(p->ndir, 1), 0.0);
+            for (int g = 0; g < p->ntime; ++g) {
+                const double* neu = d->time_neumann ? d->time_neumann + (size_t)g * 2 * m->nbe : nullptr;
+                const double* src = d->time_source ? d->time_source + (size_t)g * m->np : nullptr;
+                const double* dud = d->time_dudt ? d->time_dudt + (size_t)g * m->np : nullptr;
+                finite(neu, 2 * m->nbe);
+                finite(src, m->np);
+                finite(dud, m->np);
+                std::vector<double> bg = time_constant_terms(p.get(), neu, src, dud);
+                std::copy(bg.begin(), bg.end(), tb.begin() + (size_t)g * m->np);
+                if (d->time_dirichlet) {
+                    const double* dv = d->time_dirichlet + (size_t)g * m->np;
+                    finite(dv, m->np);
+                    int64_t k = 0;
+                    for (int64_t v = 0; v < m->np; ++v)
+                        if (p->code[v] == FVM_VERTEX_DIRICHLET) {
+                            p->tdir_varies |= dv[v] != 0.0;
+                            tdir[(size_t)g * p->ndir + k++] = dv[v];
+                        }
+                }
+            }
+            p->d_tb.upload(tb);
+            p->d_tdir.upload(tdir);
+            p->d_beff.alloc(sizeof(double) * m->np);
+        }
     }
     if (p->linear) {
         std::vector<double> E, A, dg, b, q, rs;
@@ -253,6 +370,11 @@ extern "C" int fvm_problem_create_impl(fvm_mesh* mesh, const fvm_problem_desc* d
 // Per-element data of the per-triangle flux kernel (used for nonlinear forms, or on request).
 void fvm_problem::build_triangle_path() {
     if (tri_ready) return;
+    if (ntime > 0)
+        fail(FVM_ERR_UNSUPPORTED, "time-dependent values run on the operator path only (no force_triangle)");
+    if (flux_linear)
+        fail(FVM_ERR_UNSUPPORTED, "a flux linear in (alpha, beta, gamma) other than -D grad u runs on the operator "
+                                  "path only: it needs affine Neumann, source and Dudt forms and no force_triangle");
     fvm_mesh* m = mesh;
     m->build_tiles();
     const Tiles& T = m->tiles;

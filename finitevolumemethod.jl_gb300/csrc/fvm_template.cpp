@@ -143,6 +143,7 @@ int fvm_template_create(fvm_problem* prob, int32_t kind, fvm_template** out) {
         if (!prob || !out) fail(FVM_ERR_INVALID_ARGUMENT, "NULL argument");
         if (kind < FVM_TEMPLATE_DIFFUSION || kind > FVM_TEMPLATE_MEAN_EXIT_TIME)
             fail(FVM_ERR_INVALID_ARGUMENT, "unknown template kind");
+        if (prob->ntime > 0) fail(FVM_ERR_UNSUPPORTED_FORM, "templates take time-independent conditions");
         *out = nullptr;
         std::unique_ptr<fvm_template> T(new fvm_template());
         T->prob = prob;

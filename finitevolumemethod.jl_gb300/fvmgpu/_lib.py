@@ -24,6 +24,7 @@ FVM_ERR_UNSUPPORTED = 7
 FVM_ERR_STEP_LIMIT = 8
 
 FVM_VERTEX_FREE, FVM_VERTEX_DIRICHLET, FVM_VERTEX_DUDT, FVM_VERTEX_NOT_A_VERTEX = 0, 1, 2, 3
+FVM_MAX_TIME_FACTORS = 8
 FVM_PTR_HOST, FVM_PTR_DEVICE, FVM_PTR_DEVICE_INTERNAL = 0, 1, 2
 FVM_RHS_FORCE_TRIANGLE = 16
 FVM_RHS_CONSERVATIVE = 32
@@ -75,6 +76,14 @@ class ProblemDesc(C.Structure):
         ("dudt", c_double_p),
         ("dirichlet", c_double_p),
         ("precision", C.c_int32),
+        ("dual_edge_flux", c_double_p),
+        ("quarter_flux", c_double_p),
+        ("ntime", C.c_int32),
+        ("time_factor", c_double_p),
+        ("time_dirichlet", c_double_p),
+        ("time_neumann", c_double_p),
+        ("time_source", c_double_p),
+        ("time_dudt", c_double_p),
     ]
 
 

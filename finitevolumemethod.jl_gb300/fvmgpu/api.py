@@ -15,8 +15,8 @@ import numpy as np
 
 from . import _lib
 from ._lib import (FVM_FP32, FVM_FP64, FVM_VERTEX_DIRICHLET, FVM_VERTEX_DUDT, FVM_VERTEX_FREE,
-                   FVM_VERTEX_NOT_A_VERTEX, as_f64, as_i8, as_i32, check, dptr, load)
-from .forms import (classify_flux, classify_system_flux, classify_system_poly, classify_xytu, monomials,
+                   FVM_VERTEX_NOT_A_VERTEX, UnsupportedFormError, as_f64, as_i8, as_i32, check, dptr, load)
+from .forms import (classify_flux, classify_linear_flux, classify_system_flux, classify_system_poly, classify_xytu, monomials,
                     sample_xy)
 from .meshes import Triangulation
 
@@ -308,16 +308,62 @@ class _Desc:
         setattr(self.c, name, a.ctypes.data_as(ctype))
 
 
-def _group_eval(points_by_entity, fidx_by_entity, functions, t0, what, max_degree):
+class _TimeParts:
+    """The time factors of a problem's values and, per factor, the B arrays of each kind
+    (descriptor fields time_factor, time_dirichlet, time_neumann, time_source, time_dudt)."""
+
+    def __init__(self, sizes):
+        self.factors = []
+        self.sizes = sizes  # kind -> length of one factor's array
+        self.values = {kind: [] for kind in sizes}
+
+    def add(self, kind, tau, sel, B):
+        for g, f in enumerate(self.factors):
+            if f.close_to(tau):
+                break
+        else:
+            if len(self.factors) == _lib.FVM_MAX_TIME_FACTORS:
+                raise UnsupportedFormError(_lib.FVM_ERR_UNSUPPORTED_FORM, f"more than {_lib.FVM_MAX_TIME_FACTORS} "
+                                           "distinct time factors")
+            self.factors.append(tau)
+            for kd in self.values:
+                self.values[kd].append(None)
+            g = len(self.factors) - 1
+        if self.values[kind][g] is None:
+            self.values[kind][g] = np.zeros(self.sizes[kind])
+        self.values[kind][g][sel] += B
+
+    def fill(self, d):
+        d.c.ntime = len(self.factors)
+        if not self.factors:
+            return
+        d.arr("time_factor", as_f64(np.array(self.factors, dtype=np.float64)))
+        for kind, vals in self.values.items():
+            if all(v is None for v in vals):
+                d.arr(kind, None)
+            else:
+                d.arr(kind, as_f64(np.stack([np.zeros(self.sizes[kind]) if v is None else v for v in vals])))
+
+
+def _group_eval(points_by_entity, fidx_by_entity, functions, t0, what, max_degree, time=None):
     """Classify condition functions per function index over the entities that use them.
-    points_by_entity: (n, k, 2); returns coefficients (n, k, deg+1) and deg."""
+    points_by_entity: (n, k, 2); returns coefficients (n, k, deg+1) and deg.  time =
+    (tf, _TimeParts, kind) allows a time factor on the constant term, recorded in the parts
+    (entities flattened to n * k)."""
     n, k = points_by_entity.shape[:2]
     results = {}
     deg = 0
     for f in np.unique(fidx_by_entity[fidx_by_entity >= 0]):
         sel = fidx_by_entity == f
         P = points_by_entity[sel].reshape(-1, 2)
-        c, d = classify_xytu(functions[int(f)], P[:, 0], P[:, 1], t0, f"{what} function {int(f)}", max_degree)
+        name = f"{what} function {int(f)}"
+        if time is None:
+            c, d = classify_xytu(functions[int(f)], P[:, 0], P[:, 1], t0, name, max_degree)
+        else:
+            tf, parts, kind = time
+            c, d, tp = classify_xytu(functions[int(f)], P[:, 0], P[:, 1], t0, name, max_degree, tf=tf, time=True)
+            if tp is not None:
+                parts.add(kind, tp[0], np.repeat(sel, k), tp[1])
         results[int(f)] = (sel, c)
         deg = max(deg, d)
     out = np.zeros((n, k, deg + 1))
@@ -383,14 +429,25 @@ class FVMProblem:
         neu = conds.neumann_table(tri.boundary_edges)
         dual, quarter = mesh.sample_points()
         d = _Desc()
+        tf = self.final_time
+        parts = _TimeParts({"time_dirichlet": tri.num_points, "time_neumann": 2 * tri.num_boundary_edges,
+                            "time_source": tri.num_points, "time_dudt": tri.num_points})
         self._code, self._fidx, self._neu = code, fidx, neu
         d.arr("vertex_code", as_i8(code), _lib.c_int8_p)
         d.arr("bedge_neumann", as_i8(neu >= 0), _lib.c_int8_p)
+        dual_M = quarter_M = None
         if self.flux_function is not None:
             q = ParametrisedFunction(self.flux_function, self.flux_parameters)
-            Dd = classify_flux(q, dual[..., 0].ravel(), dual[..., 1].ravel(), t0)
-            Dq = classify_flux(q, quarter[..., 0].ravel(), quarter[..., 1].ravel(), t0) if tri.num_boundary_edges else np.zeros(0)
-            ddeg, dual_c, quarter_c = 0, Dd.reshape(-1, 1), Dq.reshape(-1, 1)
+            try:  # the diffusion form -D(x, y) grad u
+                Dd = classify_flux(q, dual[..., 0].ravel(), dual[..., 1].ravel(), t0)
+                Dq = (classify_flux(q, quarter[..., 0].ravel(), quarter[..., 1].ravel(), t0) if tri.num_boundary_edges
+                      else np.zeros(0))
+                ddeg, dual_c, quarter_c = 0, Dd.reshape(-1, 1), Dq.reshape(-1, 1)
+            except UnsupportedFormError:  # else any flux linear in (alpha, beta, gamma), e.g. advection
+                dual_M = classify_linear_flux(q, dual[..., 0].ravel(), dual[..., 1].ravel(), t0)
+                quarter_M = (classify_linear_flux(q, quarter[..., 0].ravel(), quarter[..., 1].ravel(), t0)
+                             if tri.num_boundary_edges else np.zeros((0, 6)))
+                ddeg, dual_c, quarter_c = 0, np.zeros((0, 1)), np.zeros((0, 1))
         else:
             Df = ParametrisedFunction(self.diffusion_function, self.diffusion_parameters)
             allp = np.concatenate([dual.reshape(-1, 2), quarter.reshape(-1, 2)])
@@ -398,11 +455,13 @@ class FVMProblem:
             nd = dual.reshape(-1, 2).shape[0]
             dual_c, quarter_c = c[:nd], c[nd:]
         d.c.diffusion_degree = ddeg
-        d.arr("dual_edge_D", as_f64(dual_c))
+        d.arr("dual_edge_D", as_f64(dual_c) if dual_c.size else None)
         d.arr("quarter_D", as_f64(quarter_c) if quarter_c.size else None)
+        d.arr("dual_edge_flux", as_f64(dual_M) if dual_M is not None else None)
+        d.arr("quarter_flux", as_f64(quarter_M) if quarter_M is not None and quarter_M.size else None)
         # Neumann q.n = a(x, y, t, u) at the quarter points of each Neumann edge
         if np.any(neu >= 0):
-            nc, ndeg = _group_eval(quarter, neu, conds.functions, t0, "Neumann", 2)
+            nc, ndeg = _group_eval(quarter, neu, conds.functions, t0, "Neumann", 2, (tf, parts, "time_neumann"))
             d.c.neumann_degree = ndeg
             d.arr("quarter_neumann", as_f64(nc.reshape(-1, ndeg + 1)))
         else:
@@ -413,7 +472,9 @@ class FVMProblem:
         free = code == FVM_VERTEX_FREE
         if self.source_function is not None and np.any(free):
             S = ParametrisedFunction(self.source_function, self.source_parameters)
-            c, sdeg = classify_xytu(S, P[free, 0], P[free, 1], t0, "source_function")
+            c, sdeg, tp = classify_xytu(S, P[free, 0], P[free, 1], t0, "source_function", tf=tf, time=True)
+            if tp is not None:
+                parts.add("time_source", tp[0], free, tp[1])
             src = np.zeros((tri.num_points, sdeg + 1))
             src[free] = c
             d.c.source_degree = sdeg
@@ -425,7 +486,7 @@ class FVMProblem:
         pts3 = P.reshape(-1, 1, 2)
         dfidx = np.where(code == FVM_VERTEX_DUDT, fidx, -1)
         if np.any(dfidx >= 0):
-            dc, udeg = _group_eval(pts3, dfidx, conds.functions, t0, "Dudt", 2)
+            dc, udeg = _group_eval(pts3, dfidx, conds.functions, t0, "Dudt", 2, (tf, parts, "time_dudt"))
             d.c.dudt_degree = udeg
             d.arr("dudt", as_f64(dc.reshape(-1, udeg + 1)))
         else:
@@ -433,10 +494,12 @@ class FVMProblem:
             d.arr("dudt", None)
         rfidx = np.where(code == FVM_VERTEX_DIRICHLET, fidx, -1)
         if np.any(rfidx >= 0):
-            rc, _ = _group_eval(pts3, rfidx, conds.functions, t0, "Dirichlet", 0)
+            rc, _ = _group_eval(pts3, rfidx, conds.functions, t0, "Dirichlet", 0, (tf, parts, "time_dirichlet"))
             d.arr("dirichlet", as_f64(rc.reshape(-1)))
         else:
             d.arr("dirichlet", None)
+        parts.fill(d)
+        self.time_factors = list(parts.factors)
         d.c.precision = self.precision
         h = C.c_void_p()
         check(load().fvm_problem_create(mesh.handle, C.byref(d.c), C.byref(h)))

@@ -7,12 +7,16 @@ quarter points) and classifies it:
 * a closure of (x, y) alone is sampled into a per-point array;
 * a closure that is a polynomial of degree <= 2 in u with (x, y)-dependent coefficients
   becomes the coefficient arrays c0, c1, c2 (f = c0 + c1 u + c2 u^2);
-* anything else (t dependence, non-polynomial u dependence, non-finite values) is rejected
-  with `UnsupportedFormError`: never guessed.
+* where the caller allows it (conditions and sources of linear problems), the constant term
+  c0 may depend on t through one factor of a fixed set: c0(x, y, t) = A(x, y) + tau(t) B(x, y)
+  with tau(t) = exp(a (t - t0)) or 1 + a (t - t0) + b (t - t0)^2 (`TimeFactor`);
+* anything else (other t dependence, non-polynomial u dependence, non-finite values) is
+  rejected with `UnsupportedFormError`: never guessed.
 
 Classification probes the closure at u in {0, 1, -1} and t in {t0, t0 + 1.37}, fits the
 quadratic, and verifies it at u in {2, -0.5, 3.25} and at the second time, to a relative
-tolerance of 1e-10.
+tolerance of 1e-10.  A time factor is fitted from c0 at six equally spaced times across
+[t0, tf] and verified at three other times, to the same tolerance.
 """
 from __future__ import annotations
 
@@ -58,11 +62,88 @@ def evaluate(f, *args):
 
 def _reject(what, why):
     raise UnsupportedFormError(FVM_ERR_UNSUPPORTED_FORM, f"{what}: {why}; supported forms are closures of (x, y) "
-                               "and polynomials of degree <= 2 in u with (x, y) coefficients, independent of t")
+                               "and polynomials of degree <= 2 in u with (x, y) coefficients, independent of t "
+                               "except for a constant term A(x, y) + tau(t) B(x, y), tau(t) = exp(a (t - t0)) or "
+                               "1 + a (t - t0) + b (t - t0)^2, in the conditions and source of a linear problem")
 
 
-def classify_xytu(f, x, y, t0, what, max_degree=2):
-    """Coefficients (c0, c1, c2)[:deg+1] and degree of g(x, y, t, u) = f(x, y, t, u) at points."""
+class TimeFactor(tuple):
+    """(kind, t_ref, a, b): kind 1 is tau(t) = exp(a (t - t_ref)), kind 2 is
+    tau(t) = 1 + a (t - t_ref) + b (t - t_ref)^2 (the descriptor's time_factor rows)."""
+
+    def __new__(cls, kind, t_ref, a, b=0.0):
+        return super().__new__(cls, (float(kind), float(t_ref), float(a), float(b)))
+
+    def __call__(self, t):
+        d = np.asarray(t, dtype=np.float64) - self[1]
+        return np.exp(self[2] * d) if self[0] == 1.0 else 1.0 + d * (self[2] + d * self[3])
+
+    def close_to(self, other, rtol=1e-11):
+        return (self[0] == other[0] and self[1] == other[1]
+                and all(abs(p - q) <= rtol * max(abs(p), abs(q), 1e-300) for p, q in zip(self[2:], other[2:])))
+
+
+def fit_time_factor(c0_at, t0, tf, what):
+    """Fit c0(t) = A + tau(t) B (arrays over points) for tau in the device set, from c0 at six
+    equally spaced times across [t0, tf]; verify at three other times.  Returns
+    (A, TimeFactor, B), or None when c0 does not depend on t.  Rejects other t dependence."""
+    t0 = float(t0)
+    span = float(tf) - t0 if tf is not None and float(tf) > t0 else 1.0
+    h = span / 5
+    C = [np.asarray(c0_at(t0 + k * h), dtype=np.float64) for k in range(6)]
+    scale = max(float(np.max(np.abs(c))) if c.size else 0.0 for c in C)
+    tol = _RTOL * max(scale, 1e-300)
+    for c in C:
+        if not np.all(np.isfinite(c)):
+            _reject(what, "non-finite values")
+    D = [c - C[0] for c in C]
+    if all(np.all(np.abs(d) <= tol) for d in D):
+        return None
+    w = max(D[1:], key=lambda d: float(np.max(np.abs(d))))
+    ww = float(np.dot(w, w))
+    s = np.array([float(np.dot(d, w)) / ww for d in D])  # D_k = s_k w
+    if not all(np.all(np.abs(d - sk * w) <= tol) for d, sk in zip(D, s)):
+        _reject(what, "depends on t other than through one factor tau(t)")
+    smax = float(np.max(np.abs(s)))
+    fits = []
+    # exponential: differences of s form a geometric sequence with ratio exp(a h)
+    if abs(s[1]) > 1e-8 * smax:
+        rho = (s[2] - s[1]) / s[1]
+        if rho > 0 and abs(rho - 1) > 1e-6:
+            a = np.log(rho) / h
+            cexp = s[1] / (rho - 1)
+            pred = cexp * (np.exp(a * h * np.arange(6)) - 1)
+            if np.all(np.abs(pred - s) <= 1e-10 * smax):
+                fits.append((TimeFactor(1, t0, a), cexp))
+    if not fits:  # polynomial: s_k = alpha k + beta k^2
+        k = np.arange(6, dtype=np.float64)
+        M = np.stack([k, k * k], axis=1)
+        (al, be), *_ = np.linalg.lstsq(M, s, rcond=None)
+        # a coefficient at the rounding level of the other is zero (so equal factors compare equal)
+        if abs(be) <= 1e-12 * abs(al):
+            be = 0.0
+        elif abs(al) <= 1e-12 * abs(be):
+            al = 0.0
+        if np.all(np.abs(M @ np.array([al, be]) - s) <= 1e-10 * smax):
+            fits.append((TimeFactor(2, t0, al / h, be / (h * h)), 1.0))
+    if not fits:
+        _reject(what, "depends on t other than through exp(a (t - t0)) or a quadratic in t - t0")
+    tau, cs = fits[0]
+    B = cs * w
+    A = C[0] - B
+    for frac in (0.31, 2.77, 4.43):
+        t = t0 + frac * h
+        if not np.all(np.abs(np.asarray(c0_at(t)) - (A + tau(t) * B)) <= tol):
+            _reject(what, "depends on t other than through exp(a (t - t0)) or a quadratic in t - t0")
+    return A, tau, B
+
+
+def classify_xytu(f, x, y, t0, what, max_degree=2, tf=None, time=False):
+    """Coefficients (c0, c1, c2)[:deg+1] and degree of g(x, y, t, u) = f(x, y, t, u) at points.
+
+    time=True allows c0 to depend on t through one factor (`fit_time_factor` over [t0, tf]);
+    then returns (coeffs, deg, tpart) with coeffs[..., 0] the static part A and tpart
+    (TimeFactor, B) or None."""
     x = np.asarray(x, dtype=np.float64)
     y = np.asarray(y, dtype=np.float64)
     t1 = float(t0)
@@ -84,10 +165,18 @@ def classify_xytu(f, x, y, t0, what, max_degree=2):
         pred = c0 + u * (c1 + u * c2)
         if not np.all(np.abs(gu - pred) <= _RTOL * (scale * (1 + abs(u)) ** 2)):
             _reject(what, "not a polynomial of degree <= 2 in u")
+    tpart = None
+    gt = {u: evaluate(f, x, y, t2, np.full(x.shape, u)) for u in _FIT_U}
+    if time:
+        fit = fit_time_factor(lambda t: evaluate(f, x, y, t, np.zeros(x.shape)), t1, tf, what)
+        if fit is not None:
+            c0, tau, B = fit
+            tpart = (tau, B)
+            # only c0 may vary: the u-dependent part at the second time is the first's
+            gt = {u: gt[u] - gt[0.0] + g[0.0] for u in _FIT_U}
     for u in _FIT_U:
-        gt = evaluate(f, x, y, t2, np.full(x.shape, u))
-        if not np.all(np.abs(gt - g[u]) <= _RTOL * (scale * (1 + abs(u)) ** 2)):
-            _reject(what, "depends on t")
+        if not np.all(np.abs(gt[u] - g[u]) <= _RTOL * (scale * (1 + abs(u)) ** 2)):
+            _reject(what, "depends on t" + (" in its u-dependent terms" if time else ""))
     tiny = 1e-14 * np.max(scale) if scale.size else 0.0
     if np.all(np.abs(c2) <= tiny):
         c2 = np.zeros_like(c2)
@@ -97,6 +186,8 @@ def classify_xytu(f, x, y, t0, what, max_degree=2):
     if deg > max_degree:
         _reject(what, f"degree {deg} in u exceeds {max_degree}")
     coeffs = np.stack([c0, c1, c2][: deg + 1], axis=-1)
+    if time:
+        return coeffs, deg, tpart
     return coeffs, deg
 
 
@@ -133,6 +224,44 @@ def classify_flux(q, x, y, t0, what="flux_function"):
     if not ok or not np.all(np.isfinite(D)):
         _reject(what, "not of the form -D(x, y) (alpha, beta)")
     return D
+
+
+def classify_linear_flux(q, x, y, t0, what="flux_function"):
+    """M (npoints, 6) of a flux linear in (alpha, beta, gamma),
+    q(x, y, t, alpha, beta, gamma) = (M0 alpha + M1 beta + M2 gamma, M3 alpha + M4 beta + M5 gamma),
+    with M depending on (x, y) only (e.g. the advection-diffusion flux nu u - D grad u with
+    u = alpha x + beta y + gamma), or reject.  Probes the unit vectors and zero, and verifies
+    linearity at (2, -3, 5) and at a second time, relative to the size of the summed terms."""
+    x = np.asarray(x, dtype=np.float64)
+    y = np.asarray(y, dtype=np.float64)
+    ones = np.ones(x.shape)
+
+    def ev(a, b, c, t=t0):
+        try:
+            qx, qy = evaluate(q, x, y, t, a * ones, b * ones, c * ones)
+        except Exception as e:  # noqa: BLE001
+            _reject(what, f"evaluation failed ({e!r})")
+        return np.asarray(qx, dtype=np.float64) * ones, np.asarray(qy, dtype=np.float64) * ones
+
+    zx, zy = ev(0.0, 0.0, 0.0)
+    cols = [ev(1.0, 0.0, 0.0), ev(0.0, 1.0, 0.0), ev(0.0, 0.0, 1.0)]
+    M = np.stack([cols[0][0] - zx, cols[1][0] - zx, cols[2][0] - zx,
+                  cols[0][1] - zy, cols[1][1] - zy, cols[2][1] - zy], axis=1)
+    if not np.all(np.isfinite(M)):
+        _reject(what, "non-finite values")
+    big = np.max(np.abs(M), axis=1)
+    ok = np.all(np.abs(zx) <= _RTOL * big) and np.all(np.abs(zy) <= _RTOL * big)
+    if ok:
+        a, b, c = 2.0, -3.0, 5.0
+        cx, cy = ev(a, b, c, t0 + 1.37)
+        px = M[:, 0] * a + M[:, 1] * b + M[:, 2] * c
+        py = M[:, 3] * a + M[:, 4] * b + M[:, 5] * c
+        tx = np.abs(M[:, 0] * a) + np.abs(M[:, 1] * b) + np.abs(M[:, 2] * c)
+        ty = np.abs(M[:, 3] * a) + np.abs(M[:, 4] * b) + np.abs(M[:, 5] * c)
+        ok = np.all(np.abs(cx - px) <= _RTOL * tx + 1e-300) and np.all(np.abs(cy - py) <= _RTOL * ty + 1e-300)
+    if not ok:
+        _reject(what, "not linear in (alpha, beta, gamma) with coefficients of (x, y)")
+    return np.ascontiguousarray(M)
 
 
 def sample_xy(f, x, y, *extra, what="function"):

@@ -43,6 +43,14 @@ struct ProblemDesc
     dudt::Ptr{Float64}
     dirichlet::Ptr{Float64}
     precision::Int32
+    dual_edge_flux::Ptr{Float64}
+    quarter_flux::Ptr{Float64}
+    ntime::Int32
+    time_factor::Ptr{Float64}
+    time_dirichlet::Ptr{Float64}
+    time_neumann::Ptr{Float64}
+    time_source::Ptr{Float64}
+    time_dudt::Ptr{Float64}
 end
 
 struct OdeOptions
@@ -219,7 +227,9 @@ function GPUProblem(prob::FVM.FVMProblem; precision = :fp64)
     keep = Any[code, neu, dualD, quarterD, quarterN, Sc, dudt, dir]
     desc = ProblemDesc(pointer(code), pointer(neu), Int32(ddeg), pointer(dualD), pointer(quarterD), Int32(ndeg),
         isempty(quarterN) ? Ptr{Float64}(C_NULL) : pointer(quarterN), Int32(sdeg), pointer(Sc), Int32(udeg),
-        pointer(dudt), pointer(dir), precision == :fp32 ? Int32(1) : Int32(0))
+        pointer(dudt), pointer(dir), precision == :fp32 ? Int32(1) : Int32(0), Ptr{Float64}(C_NULL),
+        Ptr{Float64}(C_NULL), Int32(0), Ptr{Float64}(C_NULL), Ptr{Float64}(C_NULL), Ptr{Float64}(C_NULL),
+        Ptr{Float64}(C_NULL), Ptr{Float64}(C_NULL))
     h = Ref{Ptr{Cvoid}}(C_NULL)
     GC.@preserve keep check(ccall((:fvm_problem_create, libfvmgpu), Cint,
         (Ptr{Cvoid}, Ref{ProblemDesc}, Ref{Ptr{Cvoid}}), m.handle, desc, h))

@@ -123,7 +123,27 @@ typedef struct fvm_problem_desc {
     /* Dirichlet u = a(x, y) at vertices with code DIRICHLET (dirichlet.jl:2-8) */
     const double* dirichlet;        /* [npoints] */
     int32_t precision;              /* FVM_FP64 or FVM_FP32 */
+    /* A flux linear in (alpha, beta, gamma) (src/problem.jl:118-163, e.g. the advection-diffusion
+     * q = nu u - D grad u with u = alpha x + beta y + gamma):
+     *     q = (M0 alpha + M1 beta + M2 gamma, M3 alpha + M4 beta + M5 gamma)
+     * with M sampled at the dual-edge midpoints and boundary quarter points.  When given,
+     * dual_edge_D / quarter_D and diffusion_degree are ignored.  NULL: the diffusion form. */
+    const double* dual_edge_flux;   /* [ntri*3][6] */
+    const double* quarter_flux;     /* [nbedge*2][6] */
+    /* Values that depend on t through a factor (src/conditions.jl:237-251 conditions a(x, y, t, u, p)
+     * and source S(x, y, t, u, p) independent of u): value(x, y, t) = tau_g(t) v_g(x, y) for a time
+     * factor from a fixed set, time_factor[g] = {kind, t_ref, a, b}:
+     *   kind 1: tau(t) = exp(a (t - t_ref));  kind 2: tau(t) = 1 + a (t - t_ref) + b (t - t_ref)^2.
+     * The v_g are added to the static values above (which hold 0 where a value is time-dependent).
+     * Linear problems only.  ntime = 0: no time dependence (the arrays may be NULL). */
+    int32_t ntime;                  /* at most FVM_MAX_TIME_FACTORS */
+    const double* time_factor;      /* [ntime][4] */
+    const double* time_dirichlet;   /* [ntime][npoints] Dirichlet values */
+    const double* time_neumann;     /* [ntime][nbedge*2] Neumann values q.n at the quarter points */
+    const double* time_source;      /* [ntime][npoints] source values on free vertices */
+    const double* time_dudt;        /* [ntime][npoints] Dudt values */
 } fvm_problem_desc;
+#define FVM_MAX_TIME_FACTORS 8
 
 /* Replaces FVMProblem(mesh, BCs, ICs; ...) (src/problem.jl:118-163) together with
  * Conditions(mesh, BCs, ICs) (src/conditions.jl:546-552). */

@@ -988,8 +988,13 @@ def tsit5_solve(f, u0, t0, tf, saveat, dt=None, adaptive=True, abstol=1e-6, relt
         step += 1
         reeval = False
         if callback is not None:
-            u = callback(u, t)
-            reeval = first_cb
+            # OrdinaryDiffEq evaluates the first-same-as-last derivative again after a callback
+            # that modifies u; one that rewrites the values u already holds changes nothing
+            # (Dirichlet rows have du = 0, so after the first update a time-independent value
+            # is already in place and f(u) is the step's last stage)
+            ucb = callback(u, t)
+            reeval = first_cb or not np.array_equal(ucb, u)
+            u = ucb
             first_cb = False
         while si < len(saveat) and saveat[si] == t:
             out.append(u.copy())

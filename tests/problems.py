@@ -242,3 +242,71 @@ def fourier_logfield(seed, sigma=0.5, modes=16):
             s = s + a[m] * np.cos(2 * np.pi * (k[m, 0] * x + k[m, 1] * y) + ph[m])
         return sigma * s / np.sqrt(modes / 2)
     return logD
+
+
+# ---- advection-diffusion (docs/src/literate_tutorials/piecewise_linear_and_natural_neighbour_
+# interpolation_for_an_advection_diffusion_equation.jl): q = nu u - D grad u, nu = (0.05, 0),
+# D = 0.02, zero Dirichlet, u0 = exp(-(x^2 + y^2) / eps^2) / (eps^2 pi), eps = 1/10.  The tutorial
+# refines a 2 x 2 rectangle of [-30, 30]^2 with DelaunayTriangulation's refine!, which has no
+# restatement here: a uniform n x n grid of the same square stands in for it.
+def advection_diffusion(n=121) -> Spec:
+    tri = triangulate_rectangle(-30.0, 30.0, -30.0, 30.0, n, n, single_boundary=True)
+    P = tri.points
+    eps = 0.1
+    u0 = np.exp(-(P[:, 0] ** 2 + P[:, 1] ** 2) / eps ** 2) / (eps ** 2 * np.pi)
+
+    def flux(x, y, t, a, b, g, p):
+        u = a * x + b * y + g
+        return p["nu"] * u - p["D"] * a, -p["D"] * b
+    return Spec(tri, (lambda x, y, t, u, p: 0.0 * x,), ("Dirichlet",), (None,), flux=flux,
+                fluxp={"D": 0.02, "nu": 0.05}, u0=u0, tf=250.0)
+
+
+# ---- diffusion on an annulus with a time-dependent inner Dirichlet value -------------------
+# (docs/src/literate_tutorials/diffusion_equation_on_an_annulus.jl:34-67): radii 0.2 and 1,
+# q . n = 0 on the outer circle, u = 50 (1 - exp(-t/2)) on the inner one, D = 1, the
+# tutorial's three-Gaussian initial condition, final time 2, saveat 0.2.  The tutorial refines
+# a Delaunay mesh of the annulus; a polar lattice of the same annulus stands in for it.
+def annulus_time_dirichlet(nr=24, ntheta=96) -> Spec:
+    tri = triangulate_annulus(0.2, 1.0, nr, ntheta, nsegments=1)
+    x, y = tri.points[:, 0], tri.points[:, 1]
+    u0 = (10 * np.exp(-25 * ((x + 0.5) ** 2 + (y + 0.5) ** 2)) - 5 * np.exp(-50 * ((x + 0.3) ** 2 + (y + 0.5) ** 2))
+          - 10 * np.exp(-45 * ((x - 0.5) ** 2 + (y - 0.5) ** 2)))
+    fns = (lambda x, y, t, u, p: 0.0 * x, lambda x, y, t, u, p: 50 * (1 - np.exp(-t / 2)) + 0.0 * x)
+    return Spec(tri, fns, ("Neumann", "Dirichlet"), (None, None), D=lambda x, y, t, u, p: 1.0 + 0.0 * x, u0=u0,
+                tf=2.0)
+
+
+# ---- the Brusselator's first component with its coupling replaced by -u --------------------
+# (docs/src/literate_tutorials/reaction_diffusion_brusselator_system_of_pdes.jl:60-124): on the
+# unit square, q = -grad(u)/4, S = -u, and the tutorial's boundary values for Phi
+# (q . n = -exp(-x - t/2)/4 below, exp(-1 - y - t/2)/4 right, -exp(-y - t/2)/4 left,
+# u = exp(-1 - x - t/2) on top).  u = exp(-x - y - t/2) solves it exactly.
+def brusselator_phi(n=40) -> Spec:
+    tri = triangulate_rectangle(0.0, 1.0, 0.0, 1.0, n, n, single_boundary=False)
+    P = tri.points
+    fns = (lambda x, y, t, u, p: -0.25 * np.exp(-x - t / 2),
+           lambda x, y, t, u, p: 0.25 * np.exp(-1 - y - t / 2),
+           lambda x, y, t, u, p: np.exp(-1 - x - t / 2),
+           lambda x, y, t, u, p: -0.25 * np.exp(-y - t / 2))
+    return Spec(tri, fns, ("Neumann", "Neumann", "Dirichlet", "Neumann"), (None,) * 4,
+                flux=lambda x, y, t, a, b, g, p: (-a / 4, -b / 4), S=lambda x, y, t, u, p: -u,
+                u0=np.exp(-P[:, 0] - P[:, 1]), tf=1.0)
+
+
+def brusselator_phi_exact(x, y, t):
+    return np.exp(-x - y - t / 2)
+
+
+# ---- every kind of time-dependent value, with polynomial and exponential factors ----------
+def time_forms_rect(n=30, seed=3) -> Spec:
+    tri = triangulate_rectangle(0.0, 1.0, 0.0, 1.0, n, n, single_boundary=False)
+    rng = np.random.default_rng(seed)
+    fns = (lambda x, y, t, u, p: (2.0 - t) * x,                       # Dirichlet, linear in t
+           lambda x, y, t, u, p: 0.1 * t * y + 0.2 * u,               # Neumann, Robin part + t
+           lambda x, y, t, u, p: -0.5 * u + np.exp(0.7 * t) * y,      # Dudt, exponential
+           lambda x, y, t, u, p: p + 0.0 * x)                         # Neumann, constant
+    return Spec(tri, fns, ("Dirichlet", "Neumann", "Dudt", "Neumann"), (None, None, None, 0.3),
+                D=lambda x, y, t, u, p: 1.0 + x + 0.0 * u,
+                S=lambda x, y, t, u, p: 0.5 * u + (1 + 0.3 * t + 0.2 * t * t) * np.sin(3 * x),
+                u0=rng.random(tri.num_points), t0=0.5, tf=1.5)

@@ -161,7 +161,8 @@ def test_dirichlet_update(gpu_lib):
 
 def test_unsupported_forms_are_rejected(gpu_lib):
     """Closures are classified when the problem is first used (as the reference evaluates them
-    only when it solves); an unsupported one raises there, on every use."""
+    only when it solves); an unsupported one raises there, on every use.  A flux linear in
+    (alpha, beta, gamma) is a device form (advection); a flux nonlinear in them is not."""
     import fvmgpu as F
 
     spec = readme_diffusion(10)
@@ -178,6 +179,8 @@ def test_unsupported_forms_are_rejected(gpu_lib):
     spec = readme_diffusion(10)
     spec.flux = lambda x, y, t, a, b, g, p: (-a + 0.1 * g, -b)
     spec.D = None
+    assert api_problem(spec).info()["linear"] == 1
+    spec.flux = lambda x, y, t, a, b, g, p: (-a + 0.1 * g * g, -b)
     with pytest.raises(F.UnsupportedFormError):
         api_problem(spec).handle
 

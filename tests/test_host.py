@@ -166,3 +166,77 @@ def test_construct_flux_function():
     x, y, t, a, b, g = np.random.default_rng(3).random(6)
     u = a * x + b * y + g
     assert _q(x, y, t, a, b, g, None) == (-a * D(x, y, t, u, Dp), -b * D(x, y, t, u, Dp))
+
+
+def test_classify_linear_flux_advection_and_rejections():
+    """The advection-diffusion flux of the reference's tutorial, q = nu u - D grad u with
+    u = alpha x + beta y + gamma, is linear in (alpha, beta, gamma): M = (nu_x x - D, nu_x y, nu_x,
+    nu_y x, nu_y y - D, nu_y).  Non-linear or t-dependent fluxes are rejected."""
+    from fvmgpu import forms
+
+    x = np.linspace(-1, 1, 50)
+    y = np.linspace(0, 2, 50)
+    D, nu = 0.02, 0.05
+
+    def q(x, y, t, a, b, g, p=None):
+        u = a * x + b * y + g
+        return nu * u - D * a, -D * b
+
+    M = forms.classify_linear_flux(q, x, y, 0.0)
+    ref = np.stack([nu * x - D, nu * y, nu + 0 * x, 0 * x, 0 * x - D, 0 * x], axis=1)
+    assert np.allclose(M, ref, rtol=1e-13, atol=1e-15)
+    for bad in (lambda x, y, t, a, b, g: (a * a, b), lambda x, y, t, a, b, g: (a * (1 + t), b),
+                lambda x, y, t, a, b, g: (a + 1.0, b)):
+        with pytest.raises(forms.UnsupportedFormError):
+            forms.classify_linear_flux(bad, x, y, 0.0)
+
+
+def test_time_factor_fit_recovers_the_device_set():
+    """Constant terms A(x, y) + tau(t) B(x, y) with tau = exp(a (t - t0)) or a quadratic in
+    t - t0 are fitted to within rounding (the annulus tutorial's 50 (1 - exp(-t/2)), the
+    Brusselator's exp(-x - t/2)); other t dependence, or t in the u-dependent terms, is rejected."""
+    from fvmgpu import forms
+
+    x = np.linspace(0, 1, 40)
+    y = np.cos(3 * x)
+    cases = [(lambda x, y, t, u: 50 * (1 - np.exp(-t / 2)) + 0 * x, 0.0, 2.0, 1.0, -0.5),
+             (lambda x, y, t, u: -0.25 * np.exp(-x - t / 2), 0.0, 1.0, 1.0, -0.5),
+             (lambda x, y, t, u: (2 - t) * x + 0.3 * u, 0.5, 1.5, 2.0, None),
+             (lambda x, y, t, u: (1 + 0.3 * t + 0.2 * t * t) * np.sin(3 * x) - u * u, 0.5, 1.5, 2.0, None),
+             (lambda x, y, t, u: np.exp(0.7 * t) * y, 0.0, 5.0, 1.0, 0.7)]
+    for f, t0, tf, kind, a in cases:
+        c, deg, tp = forms.classify_xytu(f, x, y, t0, "f", tf=tf, time=True)
+        tau, B = tp
+        assert tau[0] == kind and tau[1] == t0
+        if a is not None:
+            assert abs(tau[2] - a) <= 1e-12 * abs(a)
+        for t in np.linspace(t0, tf + 1, 7):
+            want = f(x, y, t, 0.0)
+            assert np.max(np.abs(c[:, 0] + tau(t) * B - want)) <= 1e-13 * max(1.0, np.max(np.abs(want)))
+    c, deg, tp = forms.classify_xytu(lambda x, y, t, u: x + 2 * u, x, y, 0.0, "f", tf=1.0, time=True)
+    assert tp is None and deg == 1
+    for bad in (lambda x, y, t, u: np.sin(t) * x, lambda x, y, t, u: t * u, lambda x, y, t, u: np.exp(-t) * x + t * y):
+        with pytest.raises(forms.UnsupportedFormError):
+            forms.classify_xytu(bad, x, y, 0.0, "g", tf=1.0, time=True)
+    with pytest.raises(forms.UnsupportedFormError, match="depends on t"):
+        forms.classify_xytu(lambda x, y, t, u: np.exp(-t) * x, x, y, 0.0, "g")  # time not allowed here
+
+
+def test_time_factors_merge_across_closures():
+    """Closures with the same factor share one descriptor row (the Brusselator's three
+    exp(-t/2) sides), each kind of value in its own array; more than eight factors are refused."""
+    from fvmgpu import forms
+    from fvmgpu.api import _TimeParts
+
+    parts = _TimeParts({"time_dirichlet": 5, "time_neumann": 4, "time_source": 5, "time_dudt": 5})
+    x = np.linspace(0, 1, 2)
+    for k, f in enumerate((lambda x, y, t, u: np.exp(-x - t / 2), lambda x, y, t, u: -np.exp(-1 - x - t / 2))):
+        _, _, (tau, B) = forms.classify_xytu(f, x, x, 0.0, "f", tf=1.0, time=True)
+        sel = np.zeros(4, dtype=bool)
+        sel[2 * k:2 * k + 2] = True
+        parts.add("time_neumann", tau, sel, B)
+    assert len(parts.factors) == 1 and np.all(parts.values["time_neumann"][0] != 0)
+    for g in range(7):
+        parts.add("time_source", forms.TimeFactor(2, 0.0, g + 1.0), np.ones(5, dtype=bool), np.ones(5))
+    with pytest.raises(forms.UnsupportedFormError, match="time factors"):
+        parts.add("time_source", forms.TimeFactor(2, 0.0, 99.0), np.ones(5, dtype=bool), np.ones(5))
