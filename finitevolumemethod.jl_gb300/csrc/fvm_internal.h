@@ -265,6 +265,10 @@ void launch_adaptive_step_end(AdaptState* st, double* out, const double* u, cons
 using LinearTermSink = std::function<void(int32_t, int32_t, double, int64_t, bool)>;
 void fvm_visit_linear_terms(const fvm_problem* p, const LinearTermSink& emit, std::vector<double>& b,
                             std::vector<double>& q, std::vector<double>& rowscale);
+// The constant terms that values neu [nbedge*2] (Neumann q.n), src [npoints] (source on FREE
+// vertices) and dudt [npoints] (Dudt vertices) add to the RHS, internal numbering (any may be null).
+std::vector<double> fvm_time_constant_terms(const fvm_problem* p, const double* neu, const double* src,
+                                            const double* dudt);
 
 // Terms of a linear template's A and b: emitA(row, col, coef, didx) adds coef * D[didx] (coef
 // alone when didx < 0) to A[row][col]; emitb(row, -1, coef, didx) likewise to b[row].  Rows and

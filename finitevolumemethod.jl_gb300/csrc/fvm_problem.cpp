@@ -154,8 +154,8 @@ void fvm_visit_linear_terms(const fvm_problem* p, const LinearTermSink& emit, st
 
 // Constant terms of one time factor's values (time_neumann, time_source, time_dudt of the
 // descriptor), in the internal numbering: the parts of fvm_visit_linear_terms that reach b.
-static std::vector<double> time_constant_terms(const fvm_problem* p, const double* neu, const double* src,
-                                               const double* dudt) {
+std::vector<double> fvm_time_constant_terms(const fvm_problem* p, const double* neu, const double* src,
+                                            const double* dudt) {
     const fvm_mesh* m = p->mesh;
     std::vector<double> b(m->np, 0.0);
     if (neu)
@@ -310,7 +310,7 @@ extern "C" int fvm_problem_create_impl(fvm_mesh* mesh, const fvm_problem_desc* d
                 finite(neu, 2 * m->nbe);
                 finite(src, m->np);
                 finite(dud, m->np);
-                std::vector<double> bg = time_constant_terms(p.get(), neu, src, dud);
+                std::vector<double> bg = fvm_time_constant_terms(p.get(), neu, src, dud);
                 std::copy(bg.begin(), bg.end(), tb.begin() + (size_t)g * m->np);
                 if (d->time_dirichlet) {
                     const double* dv = d->time_dirichlet + (size_t)g * m->np;

@@ -227,6 +227,11 @@ struct fvm_system {
     bool has_b = false;
     int64_t ndir = 0;
     DBuf d_val, d_b, d_mask, d_vcoef, d_dir_idx, d_dir_val;
+    // time factors: b(t) = b + sum_g tau_g(t) b_g, Dirichlet values val + sum_g tau_g(t) val_g
+    int ntime = 0;
+    bool tdir_varies = false;
+    std::vector<double> tfac;  // [ntime][4]
+    DBuf d_tb, d_tdir, d_beff; // [ntime][np][N] internal, [ntime][ndir], [np][N]
     DBuf d_perm, d_iperm;  // flat [point][component] permutations: internal -> caller, caller -> internal
     DBuf d_u, d_du, d_ref;
     int64_t n() const { return (int64_t)neq * mesh->np; }
@@ -270,7 +275,7 @@ static void launch_system_vec(const SysArgs& a, const SysTerms& tm, int64_t nsli
 }
 
 template <int N>
-static void launch_system(const fvm_system* S, const double* u, double* du, cudaStream_t s) {
+static void launch_system(const fvm_system* S, const double* u, double* du, const double* b, cudaStream_t s) {
     const SellPattern& p = S->mesh->pat;
     if (p.nslices == 0) return;
     SysArgs a{p.d_slice_ptr.as<int64_t>(),
@@ -283,7 +288,7 @@ static void launch_system(const fvm_system* S, const double* u, double* du, cuda
               S->blocks,
               u,
               du,
-              S->has_b ? S->d_b.as<double>() : nullptr,
+              b,
               S->d_mask.as<uint8_t>(),
               S->nvary ? S->d_vcoef.as<double>() : nullptr,
               S->cmask,
@@ -302,23 +307,39 @@ static void launch_system(const fvm_system* S, const double* u, double* du, cuda
     }
 }
 
-static void system_rhs_internal(const fvm_system* S, const double* u, double* du, cudaStream_t s) {
+static TimeTaus system_taus(const fvm_system* S, double t) {
+    TimeTaus tt{};
+    for (int g = 0; g < S->ntime; ++g) tt.tau[g] = time_factor_value(&S->tfac[4 * g], t);
+    return tt;
+}
+
+static void system_rhs_internal(const fvm_system* S, const double* u, double* du, cudaStream_t s, double t) {
+    const double* b = S->has_b ? S->d_b.as<double>() : nullptr;
+    if (S->ntime > 0) {  // b(t) = b + sum_g tau_g(t) b_g
+        launch_time_b(b, S->d_tb.as<double>(), system_taus(S, t), S->ntime, S->d_beff.as<double>(), S->n(), s);
+        b = S->d_beff.as<double>();
+    }
     switch (S->neq) {
-        case 1: launch_system<1>(S, u, du, s); break;
-        case 2: launch_system<2>(S, u, du, s); break;
-        case 3: launch_system<3>(S, u, du, s); break;
-        case 4: launch_system<4>(S, u, du, s); break;
-        case 5: launch_system<5>(S, u, du, s); break;
-        case 6: launch_system<6>(S, u, du, s); break;
-        case 7: launch_system<7>(S, u, du, s); break;
-        case 8: launch_system<8>(S, u, du, s); break;
+        case 1: launch_system<1>(S, u, du, b, s); break;
+        case 2: launch_system<2>(S, u, du, b, s); break;
+        case 3: launch_system<3>(S, u, du, b, s); break;
+        case 4: launch_system<4>(S, u, du, b, s); break;
+        case 5: launch_system<5>(S, u, du, b, s); break;
+        case 6: launch_system<6>(S, u, du, b, s); break;
+        case 7: launch_system<7>(S, u, du, b, s); break;
+        case 8: launch_system<8>(S, u, du, b, s); break;
         default: fail(FVM_ERR_INVALID_ARGUMENT, "neq out of range");
     }
     FVM_CUDA(cudaGetLastError());
 }
 
-static void system_dirichlet_internal(const fvm_system* S, double* u, cudaStream_t s) {
-    if (S->ndir) launch_dirichlet(S->d_dir_idx.as<int32_t>(), S->d_dir_val.as<double>(), u, S->ndir, s);
+static void system_dirichlet_internal(const fvm_system* S, double* u, cudaStream_t s, double t) {
+    if (!S->ndir) return;
+    if (S->ntime > 0)
+        launch_dirichlet_time(S->d_dir_idx.as<int32_t>(), S->d_dir_val.as<double>(), S->d_tdir.as<double>(),
+                              system_taus(S, t), S->ntime, u, S->ndir, s);
+    else
+        launch_dirichlet(S->d_dir_idx.as<int32_t>(), S->d_dir_val.as<double>(), u, S->ndir, s);
 }
 
 static void create_system(fvm_mesh* m, const fvm_system_desc* d, fvm_system** out) {
@@ -567,6 +588,55 @@ static void create_system(fvm_mesh* m, const fvm_system_desc* d, fvm_system** ou
     S->d_dir_idx.upload(idx);
     S->d_dir_val.upload(dval);
 
+    // time factors: per factor, the constant terms of each component (as the Neumann constants
+    // above) and the Dirichlet values in the order of idx
+    if (d->ntime < 0 || d->ntime > FVM_MAX_TIME_FACTORS)
+        fail(FVM_ERR_INVALID_ARGUMENT, "ntime must lie in [0, FVM_MAX_TIME_FACTORS]");
+    if (d->ntime > 0) {
+        if (!d->time_factor) fail(FVM_ERR_INVALID_ARGUMENT, "time_factor is required when ntime > 0");
+        S->ntime = d->ntime;
+        S->tfac.assign(d->time_factor, d->time_factor + 4 * S->ntime);
+        for (int g = 0; g < S->ntime; ++g) {
+            const double* f = &S->tfac[4 * g];
+            if (f[0] != 1.0 && f[0] != 2.0) fail(FVM_ERR_INVALID_ARGUMENT, "time_factor kind must be 1 or 2");
+            if (!std::isfinite(f[1]) || !std::isfinite(f[2]) || !std::isfinite(f[3]))
+                fail(FVM_ERR_INVALID_ARGUMENT, "time_factor values must be finite");
+        }
+        const size_t G = (size_t)S->ntime;
+        finite(d->time_dirichlet, G * N * np, "time_dirichlet");
+        finite(d->time_neumann, G * N * 2 * nbe, "time_neumann");
+        finite(d->time_source, G * N * np, "time_source");
+        finite(d->time_dudt, G * N * np, "time_dudt");
+        std::vector<double> tb(G * np * N, 0.0), tdir(G * std::max<int64_t>(S->ndir, 1), 0.0);
+        for (int g = 0; g < S->ntime; ++g) {
+            for (int r = 0; r < N; ++r) {
+                fvm_problem tp;  // host-side view of component r
+                tp.mesh = m;
+                tp.code.assign(d->vertex_code + r * np, d->vertex_code + (r + 1) * np);
+                tp.bneu.assign(nbe, 0);
+                for (int64_t e = 0; e < nbe; ++e) tp.bneu[e] = d->bedge_neumann[r * nbe + e] ? 1 : 0;
+                const size_t gr = (size_t)g * N + r;
+                std::vector<double> bg = fvm_time_constant_terms(
+                    &tp, d->time_neumann ? d->time_neumann + gr * 2 * nbe : nullptr,
+                    d->time_source ? d->time_source + gr * np : nullptr, d->time_dudt ? d->time_dudt + gr * np : nullptr);
+                for (int64_t i = 0; i < np; ++i) tb[((size_t)g * np + i) * N + r] = bg[i];
+            }
+            if (d->time_dirichlet) {
+                int64_t k = 0;
+                for (int r = 0; r < N; ++r)
+                    for (int64_t v = 0; v < np; ++v)
+                        if (d->vertex_code[r * np + v] == FVM_VERTEX_DIRICHLET) {
+                            const double x = d->time_dirichlet[((size_t)g * N + r) * np + v];
+                            S->tdir_varies |= x != 0.0;
+                            tdir[(size_t)g * S->ndir + k++] = x;
+                        }
+            }
+        }
+        S->d_tb.upload(tb);
+        S->d_tdir.upload(tdir);
+        S->d_beff.alloc(sizeof(double) * np * N);
+    }
+
     std::vector<int32_t> perm((size_t)np * N), iperm((size_t)np * N);
     for (int64_t i = 0; i < np; ++i)
         for (int r = 0; r < N; ++r) {
@@ -611,12 +681,11 @@ int fvm_system_info(const fvm_system* S, int64_t* info) {
 int fvm_system_rhs(fvm_system* S, const double* u, double* du, double t, int32_t flags, void* stream) {
     return guard_call([&] {
         if (!S || !u || !du) fail(FVM_ERR_INVALID_ARGUMENT, "NULL argument");
-        (void)t;  // device-coded forms are time independent
         cudaStream_t s = (cudaStream_t)stream;
         const int32_t loc = flags & 3;
         if (loc > FVM_PTR_DEVICE_INTERNAL) fail(FVM_ERR_INVALID_ARGUMENT, "bad pointer-location flag");
         if (loc == FVM_PTR_DEVICE_INTERNAL) {
-            system_rhs_internal(S, u, du, s);
+            system_rhs_internal(S, u, du, s, t);
             return FVM_OK;
         }
         S->ensure_work();
@@ -628,7 +697,7 @@ int fvm_system_rhs(fvm_system* S, const double* u, double* du, double t, int32_t
         } else {
             launch_permute_in(perm, u, S->d_u.as<double>(), n, s);
         }
-        system_rhs_internal(S, S->d_u.as<double>(), S->d_du.as<double>(), s);
+        system_rhs_internal(S, S->d_u.as<double>(), S->d_du.as<double>(), s, t);
         if (loc == FVM_PTR_HOST) {
             launch_permute_out(perm, S->d_du.as<double>(), S->d_ref.as<double>(), n, s);
             FVM_CUDA(cudaMemcpyAsync(du, S->d_ref.p, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
@@ -644,12 +713,11 @@ int fvm_system_rhs(fvm_system* S, const double* u, double* du, double t, int32_t
 int fvm_system_dirichlet_apply(fvm_system* S, double* u, double t, int32_t flags, void* stream) {
     return guard_call([&] {
         if (!S || !u) fail(FVM_ERR_INVALID_ARGUMENT, "NULL argument");
-        (void)t;
         cudaStream_t s = (cudaStream_t)stream;
         const int32_t loc = flags & 3;
         if (loc > FVM_PTR_DEVICE_INTERNAL) fail(FVM_ERR_INVALID_ARGUMENT, "bad pointer-location flag");
         if (loc == FVM_PTR_DEVICE_INTERNAL) {
-            system_dirichlet_internal(S, u, s);
+            system_dirichlet_internal(S, u, s, t);
         } else {
             S->ensure_work();
             const int64_t n = S->n();
@@ -657,7 +725,7 @@ int fvm_system_dirichlet_apply(fvm_system* S, double* u, double t, int32_t flags
             if (loc == FVM_PTR_HOST)
                 FVM_CUDA(cudaMemcpyAsync(S->d_ref.p, u, sizeof(double) * n, cudaMemcpyHostToDevice, s));
             launch_permute_in(perm, loc == FVM_PTR_HOST ? S->d_ref.as<double>() : u, S->d_u.as<double>(), n, s);
-            system_dirichlet_internal(S, S->d_u.as<double>(), s);
+            system_dirichlet_internal(S, S->d_u.as<double>(), s, t);
             launch_permute_out(perm, S->d_u.as<double>(), loc == FVM_PTR_HOST ? S->d_ref.as<double>() : u, n, s);
             if (loc == FVM_PTR_HOST) {
                 FVM_CUDA(cudaMemcpyAsync(u, S->d_ref.p, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
@@ -684,8 +752,11 @@ int fvm_system_tsit5_solve(fvm_system* S, const double* u0, const fvm_ode_option
         FVM_CUDA(cudaMemcpyAsync(d_ref, u0, sizeof(double) * n, cudaMemcpyHostToDevice, s));
         launch_permute_in(S->d_perm.as<int32_t>(), d_ref, d_u0, n, s);
         OdeRhs rhs;
-        rhs.f = [S](const double* u, double* du, double, cudaStream_t st) { system_rhs_internal(S, u, du, st); };
-        if (S->ndir > 0) rhs.callback = [S](double* u, double, cudaStream_t st) { system_dirichlet_internal(S, u, st); };
+        rhs.f = [S](const double* u, double* du, double t, cudaStream_t st) { system_rhs_internal(S, u, du, st, t); };
+        if (S->ndir > 0)
+            rhs.callback = [S](double* u, double t, cudaStream_t st) { system_dirichlet_internal(S, u, st, t); };
+        rhs.time_dependent = S->ntime > 0;
+        rhs.callback_varies = S->tdir_varies;
         tsit5_run_internal(rhs, n, d_u0, *opt, d_out.as<double>(), stats, s);
         snapshots_to_host(S->d_iperm.as<int32_t>(), d_out.as<double>(), out, n, nsave, s);
         FVM_CUDA(cudaStreamSynchronize(s));

@@ -100,6 +100,12 @@ class SystemDesc(C.Structure):
         ("dudt", c_double_p),
         ("quarter_neumann", c_double_p),
         ("dirichlet", c_double_p),
+        ("ntime", C.c_int32),
+        ("time_factor", c_double_p),
+        ("time_dirichlet", c_double_p),
+        ("time_neumann", c_double_p),
+        ("time_source", c_double_p),
+        ("time_dudt", c_double_p),
     ]
 
 

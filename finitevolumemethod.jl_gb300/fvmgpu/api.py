@@ -808,6 +808,14 @@ class FVMSystem:
         dudt = np.zeros((N, npts, basis.shape[0]))
         qneu = np.zeros((N, 2 * nbe, 1 + N))
         dirv = np.zeros((N, npts))
+        tf = self.final_time
+        parts = _TimeParts({"time_dirichlet": N * npts, "time_neumann": N * 2 * nbe, "time_source": N * npts,
+                            "time_dudt": N * npts})
+
+        def flat(r, sel, size):  # component r's entries of a [N][size] array
+            m = np.zeros(N * size, dtype=bool)
+            m[r * size:(r + 1) * size] = sel
+            return m
         self._codes = codes
         for r, (cond, q) in enumerate(zip(self.conditions, self.flux_functions)):
             code, fidx = cond.vertex_tables(hv)
@@ -819,7 +827,10 @@ class FVMSystem:
             free = code == FVM_VERTEX_FREE
             S = self.source_functions[r]
             if S is not None and np.any(free):
-                e, c = classify_system_poly(S, P[free, 0], P[free, 1], t0, N, f"source_function of component {r}")
+                e, c, tp = classify_system_poly(S, P[free, 0], P[free, 1], t0, N, f"source_function of component {r}",
+                                                tf=tf, time=True)
+                if tp is not None:
+                    parts.add("time_source", tp[0], flat(r, free, npts), tp[1])
                 for k, ek in enumerate(e):
                     src[r, free, col[tuple(ek)]] = c[:, k]
             for kind, arr, want in (("Dudt", dudt, FVM_VERTEX_DUDT), ("Dirichlet", None, FVM_VERTEX_DIRICHLET)):
@@ -827,8 +838,11 @@ class FVMSystem:
                 for f in np.unique(f_of[f_of >= 0]):
                     sel = f_of == f
                     what = f"{kind} function {int(f)} of component {r}"
-                    e, c = classify_system_poly(cond.functions[int(f)], P[sel, 0], P[sel, 1], t0, N, what,
-                                                max_degree=3 if arr is not None else 0)
+                    e, c, tp = classify_system_poly(cond.functions[int(f)], P[sel, 0], P[sel, 1], t0, N, what,
+                                                    max_degree=3 if arr is not None else 0, tf=tf, time=True)
+                    if tp is not None:
+                        parts.add("time_dudt" if arr is not None else "time_dirichlet", tp[0], flat(r, sel, npts),
+                                  tp[1])
                     for k, ek in enumerate(e):
                         if arr is not None:
                             arr[r, sel, col[tuple(ek)]] = c[:, k]
@@ -836,8 +850,11 @@ class FVMSystem:
                             dirv[r, sel] = c[:, k]
             for f in np.unique(nfid[nfid >= 0]):
                 sel = np.repeat(nfid == f, 2)
-                e, c = classify_system_poly(cond.functions[int(f)], qx[sel], qy[sel], t0, N,
-                                            f"Neumann function {int(f)} of component {r}", max_degree=1)
+                e, c, tp = classify_system_poly(cond.functions[int(f)], qx[sel], qy[sel], t0, N,
+                                                f"Neumann function {int(f)} of component {r}", max_degree=1, tf=tf,
+                                                time=True)
+                if tp is not None:
+                    parts.add("time_neumann", tp[0], flat(r, sel, 2 * nbe), tp[1])
                 for k, ek in enumerate(e):
                     qneu[r, sel, 0 if ek.sum() == 0 else 1 + int(np.argmax(ek))] = c[:, k]
         used = np.nonzero(np.any(src != 0, axis=(0, 1)) | np.any(dudt != 0, axis=(0, 1)))[0]
@@ -855,6 +872,8 @@ class FVMSystem:
         d.arr("dudt", as_f64(dudt[:, :, used]) if used.size and np.any(dudt) else None)
         d.arr("quarter_neumann", as_f64(qneu) if nbe and np.any(qneu) else None)
         d.arr("dirichlet", as_f64(dirv) if np.any(dirv) else None)
+        parts.fill(d)
+        self.time_factors = list(parts.factors)
         h = C.c_void_p()
         check(load().fvm_system_create(mesh.handle, C.byref(d.c), C.byref(h)))
         self._h = h

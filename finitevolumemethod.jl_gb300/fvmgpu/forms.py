@@ -322,7 +322,9 @@ def _reject_sys(what, why):
     raise UnsupportedFormError(FVM_ERR_UNSUPPORTED_FORM, f"{what}: {why}; supported system forms are fluxes "
                                "-sum_c D_c(x, y) (alpha[c], beta[c]), sources and Dudt values that are polynomials "
                                "of total degree <= 3 in the components with (x, y) coefficients, Neumann values "
-                               "affine in the components, Dirichlet values of (x, y); none may depend on t")
+                               "affine in the components, Dirichlet values of (x, y); none may depend on t except for a "
+                               "constant term A(x, y) + tau(t) B(x, y), tau(t) = exp(a (t - t0)) or "
+                               "1 + a (t - t0) + b (t - t0)^2")
 
 
 def monomials(N, degree=_SYS_DEGREE):
@@ -387,9 +389,12 @@ def classify_system_flux(q, x, y, t0, N, what="flux_function"):
     return D
 
 
-def classify_system_poly(f, x, y, t0, N, what, max_degree=_SYS_DEGREE):
+def classify_system_poly(f, x, y, t0, N, what, max_degree=_SYS_DEGREE, tf=None, time=False):
     """(exps (m, N), coefficients (npoints, m)) of f(x, y, t, u) = sum_m c_m(x, y) prod_c
     u[c]^exps[m][c], a polynomial of total degree <= max_degree in the N-tuple u, or reject.
+    time=True allows the constant term to depend on t through one factor (`fit_time_factor`
+    over [t0, tf]): then the constant coefficient is the static part A and the result has a
+    third item, (TimeFactor, B) or None.
 
     The closure is evaluated at seeded sample tuples u (the same at every point), the
     coefficients fitted by least squares on the full monomial basis (the constant term exactly,
@@ -414,6 +419,7 @@ def classify_system_poly(f, x, y, t0, N, what, max_degree=_SYS_DEGREE):
             _reject_sys(what, "non-finite or non-scalar values")
         return v
 
+    tfit = fit_time_factor(lambda t: ev(np.zeros(N), t), t0, tf, what) if time else None
     Fv = np.stack([ev(u) for u in U])  # (K, n); U[0] is the zero tuple
     # a closure that does not depend on (x, y) gives identical samples at every point: one fit
     same = n > 0 and bool(np.all(Fv == Fv[:, :1]))
@@ -447,16 +453,35 @@ def classify_system_poly(f, x, y, t0, N, what, max_degree=_SYS_DEGREE):
         exps = rest
     if same:
         coef = np.repeat(coef, n, axis=1)
+    tB = np.zeros(n)
+    tau = None
+    if tfit is not None:  # constant term A + tau(t) B: the constant coefficient becomes A
+        A, tau, tB = tfit
+        A = np.where(np.abs(A) <= 1e-13 * np.max(np.abs(tB)), 0.0, A)
+        if exps.shape[0] and not np.any(exps[0]):
+            coef[0] = A
+        else:
+            exps = np.vstack([np.zeros((1, N), dtype=exps.dtype), exps])
+            coef = np.vstack([A[None, :], coef])
+        if not np.any(coef[0]):
+            exps, coef = exps[1:], coef[1:]
     scale = np.max(np.abs(coef), axis=0) if exps.shape[0] else np.zeros(n)
     scale = np.maximum(scale, np.max(scale, initial=0.0) * 1e-300 + 1e-300)
     checks = [(u, t0) for u in Uc] + [(U[1], t0 + 1.37), (Uc[0], t0 + 1.37)]
+    if tau is not None:
+        scale = np.maximum(scale, np.abs(tB))
     for u, t in checks:
         pred = (_vandermonde(u[None, :], exps) @ coef)[0] if exps.shape[0] else np.zeros(n)
         # relative to the size of what is summed: sum_m |c_m| |u^e_m| at each point, plus a
         # floor at the fit's rounding (a few ulps of the largest coefficient per monomial)
         terms = (_vandermonde(np.abs(u)[None, :], exps) @ np.abs(coef))[0] if exps.shape[0] else np.zeros(n)
-        bound = _RTOL * terms + 1e-13 * scale * exps.shape[0] * (1.0 + np.max(np.abs(u))) ** max_degree
+        if tau is not None:
+            pred = pred + tau(t) * tB
+            terms = terms + np.abs(tau(t) * tB)
+        bound = _RTOL * terms + 1e-13 * scale * (exps.shape[0] + (tau is not None)) * (1.0 + np.max(np.abs(u))) ** max_degree
         if not np.all(np.abs(ev(u, t) - pred) <= bound):
             _reject_sys(what, "depends on t" if t != t0 else
                         f"not a polynomial of total degree <= {max_degree} in the components")
+    if time:
+        return exps, np.ascontiguousarray(coef.T), (None if tau is None else (tau, tB))
     return exps, np.ascontiguousarray(coef.T)

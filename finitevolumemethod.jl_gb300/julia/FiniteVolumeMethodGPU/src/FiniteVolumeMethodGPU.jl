@@ -286,6 +286,12 @@ struct SystemDesc
     dudt::Ptr{Float64}
     quarter_neumann::Ptr{Float64}
     dirichlet::Ptr{Float64}
+    ntime::Int32
+    time_factor::Ptr{Float64}
+    time_dirichlet::Ptr{Float64}
+    time_neumann::Ptr{Float64}
+    time_source::Ptr{Float64}
+    time_dudt::Ptr{Float64}
 end
 
 # exponent vectors of the monomials in N variables of total degree <= 3, by degree
@@ -448,7 +454,8 @@ function GPUSystem(sys::FVM.FVMSystem{N}) where {N}
     desc = SystemDesc(Int32(N), pointer(code), nbe > 0 ? pointer(neu) : Ptr{Int8}(C_NULL), pointer(Dd),
         ptrf(Dq, nbe > 0), Int32(length(used)), isempty(used) ? Ptr{Int8}(C_NULL) : pointer(mexp),
         ptrf(srcu, !isempty(used) && any(!iszero, srcu)), ptrf(dudu, !isempty(used) && any(!iszero, dudu)),
-        ptrf(qn, nbe > 0 && any(!iszero, qn)), ptrf(dir, any(!iszero, dir)))
+        ptrf(qn, nbe > 0 && any(!iszero, qn)), ptrf(dir, any(!iszero, dir)), Int32(0), Ptr{Float64}(C_NULL),
+        Ptr{Float64}(C_NULL), Ptr{Float64}(C_NULL), Ptr{Float64}(C_NULL), Ptr{Float64}(C_NULL))
     h = Ref{Ptr{Cvoid}}(C_NULL)
     GC.@preserve keep check(ccall((:fvm_system_create, libfvmgpu), Cint,
         (Ptr{Cvoid}, Ref{SystemDesc}, Ref{Ptr{Cvoid}}), m.handle, desc, h))

@@ -248,6 +248,14 @@ typedef struct fvm_system_desc {
     const double* dudt;             /* [neq][npoints][nmono], used on DUDT vertices */
     const double* quarter_neumann;  /* [neq][nbedge*2][1+neq]: n0, n_1 .. n_neq */
     const double* dirichlet;        /* [neq][npoints] */
+    /* Time factors as in fvm_problem_desc, per component: the values v_g are added to the
+     * constant terms (Dirichlet values, Neumann n0, the source's and Dudt's constant monomial). */
+    int32_t ntime;                  /* at most FVM_MAX_TIME_FACTORS */
+    const double* time_factor;      /* [ntime][4] */
+    const double* time_dirichlet;   /* [ntime][neq][npoints] */
+    const double* time_neumann;     /* [ntime][neq][nbedge*2] */
+    const double* time_source;      /* [ntime][neq][npoints] */
+    const double* time_dudt;        /* [ntime][neq][npoints] */
 } fvm_system_desc;
 /* Replaces FVMSystem(prob1, ..., probN) (src/problem.jl:318-334) with merge_problem_conditions
  * (:336-365). */

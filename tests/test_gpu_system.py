@@ -136,6 +136,31 @@ def mixed_system(seed=5) -> SysSpec:
     return SysSpec(tri, comps, u0, tf=0.1)
 
 
+def brusselator(n=100, tf=5.0) -> SysSpec:
+    """The Brusselator tutorial (docs/src/literate_tutorials/reaction_diffusion_brusselator_system_of_pdes.jl:84-124):
+    unit square, fluxes -grad(Phi)/4 and -grad(Psi)/4, sources Phi^2 Psi - 2 Phi and
+    -Phi^2 Psi + Phi, boundary values with factors exp(-t/2) and exp(t/2).  Its exact solution
+    is Phi = exp(-x - y - t/2), Psi = exp(x + y + t/2)."""
+    tri = triangulate_rectangle(0.0, 1.0, 0.0, 1.0, n, n, single_boundary=False)
+    phi_bc = (lambda x, y, t, u, p: -1 / 4 * np.exp(-x - t / 2), lambda x, y, t, u, p: 1 / 4 * np.exp(-1 - y - t / 2),
+              lambda x, y, t, u, p: np.exp(-1 - x - t / 2), lambda x, y, t, u, p: -1 / 4 * np.exp(-y - t / 2))
+    psi_bc = (lambda x, y, t, u, p: np.exp(x + t / 2), lambda x, y, t, u, p: -1 / 4 * np.exp(1 + y + t / 2),
+              lambda x, y, t, u, p: -1 / 4 * np.exp(1 + x + t / 2), lambda x, y, t, u, p: np.exp(y + t / 2))
+    P = tri.points
+    comps = [dict(bc=phi_bc, bcp=(None,) * 4, types=("Neumann", "Neumann", "Dirichlet", "Neumann"),
+                  q=lambda x, y, t, a, b, g, p: (-a[0] / 4, -b[0] / 4),
+                  S=lambda x, y, t, u, p: u[0] ** 2 * u[1] - 2 * u[0]),
+             dict(bc=psi_bc, bcp=(None,) * 4, types=("Dirichlet", "Neumann", "Neumann", "Dirichlet"),
+                  q=lambda x, y, t, a, b, g, p: (-a[1] / 4, -b[1] / 4),
+                  S=lambda x, y, t, u, p: -u[0] ** 2 * u[1] + u[0])]
+    u0 = np.stack([np.exp(-P[:, 0] - P[:, 1]), np.exp(P[:, 0] + P[:, 1])])
+    return SysSpec(tri, comps, u0, tf=tf)
+
+
+def brusselator_exact(P, t):
+    return np.stack([np.exp(-P[:, 0] - P[:, 1] - t / 2), np.exp(P[:, 0] + P[:, 1] + t / 2)])
+
+
 def _rhs_close(got, ref, tol=1e-12):
     for c in range(ref.shape[0]):
         assert np.max(np.abs(got[c] - ref[c])) <= tol * np.max(np.abs(ref[c])), c
@@ -271,7 +296,8 @@ def test_system_errors(gpu_lib):
         F.FVMSystem(p1, p2)
     with pytest.raises(ValueError):
         F.FVMSystem()
-    tdep = F.BoundaryConditions(mesh, (lambda x, y, t, u, p: np.exp(-x - t / 2),), (F.Neumann,))
+    # exp(-x - t/2) is a device form (a time factor); sin(3t) is not
+    tdep = F.BoundaryConditions(mesh, (lambda x, y, t, u, p: np.sin(3 * t) * np.exp(-x),), (F.Neumann,))
     p3 = F.FVMProblem(mesh, tdep, flux_function=q, initial_condition=spec.u0[0], final_time=1.0)
     with pytest.raises(F.UnsupportedFormError):
         F.FVMSystem(p3, p1)
@@ -311,3 +337,57 @@ def test_system_rolled_kernel_on_wide_rows(gpu_lib, N):
         got = np.empty_like(u)
         sys.rhs(got, u, 0.0)
         _rhs_close(got, O.system_fvm_eqs(osys, u, 0.0))
+
+
+def test_brusselator_rhs_and_dirichlet_at_any_t(gpu_lib):
+    """The Brusselator's time-dependent boundary values (two factors, exp(-t/2) and exp(t/2),
+    on Neumann and Dirichlet edges of both components): RHS and Dirichlet update against the
+    oracle at times inside and beyond the time span."""
+    import fvmgpu as F
+
+    spec = brusselator(30)
+    osys, sys = spec.oracle(), spec.api()
+    assert sorted(round(f[2], 9) for f in sys.time_factors) == [-0.5, 0.5]
+    rng = np.random.default_rng(4)
+    u = spec.u0 * (1 + 0.1 * rng.standard_normal(spec.u0.shape))
+    for t in (0.0, 0.7, 5.0, 7.5):
+        got = np.empty_like(u)
+        sys.rhs(got, u, t)
+        _rhs_close(got, O.system_fvm_eqs(osys, u, t))
+        v = u.copy()
+        F.update_dirichlet_nodes(v, sys, t)
+        w = O.system_update_dirichlet_nodes(osys, u, t)
+        assert np.max(np.abs(v - w)) <= 1e-14 * np.max(np.abs(w)), t
+
+
+def test_brusselator_solve_matches_oracle(gpu_lib):
+    """Adaptive Tsit5 on a 16 x 16 Brusselator to t = 0.3 against the oracle's driver: the
+    host-controlled loop, the same steps, snapshots within 1e-8 of max|u|."""
+    import fvmgpu as F
+
+    spec = brusselator(16, tf=0.3)
+    osys, sys = spec.oracle(), spec.api()
+    ts = np.linspace(0.0, 0.3, 7)
+    sol = F.solve(sys, F.Tsit5(), saveat=ts, abstol=1e-8, reltol=1e-6)
+    ref, st = O.tsit5_solve(lambda v, t: O.system_fvm_eqs(osys, v, t), spec.u0, 0.0, 0.3, ts, abstol=1e-8,
+                            reltol=1e-6, callback=lambda v, t: O.system_update_dirichlet_nodes(osys, v, t))
+    assert sol.stats["driver"] == "host"
+    assert sol.stats["naccept"] == st["naccept"] and sol.stats["nreject"] == st["nreject"]
+    assert sol.stats["nrhs"] == st["nrhs"]
+    got = np.array(sol.u)
+    assert np.max(np.abs(got - ref)) <= 1e-8 * np.max(np.abs(ref))
+
+
+def test_brusselator_tutorial_mesh_converges_to_exact_solution(gpu_lib):
+    """The tutorial's 100 x 100 mesh (and 50 x 50) to t = 1: the GPU solution is within the
+    discretisation error of the exact solution, which falls with h."""
+    import fvmgpu as F
+
+    errs = []
+    for n in (50, 100):
+        spec = brusselator(n, tf=1.0)
+        sys = spec.api()
+        sol = F.solve(sys, F.Tsit5(), saveat=[1.0], abstol=1e-9, reltol=1e-9)
+        ex = brusselator_exact(spec.tri.points, 1.0)
+        errs.append(max(np.max(np.abs(sol.u[-1][c] - ex[c])) / np.max(ex[c]) for c in range(2)))
+    assert errs[1] < 1e-3 and errs[1] < 0.5 * errs[0], errs

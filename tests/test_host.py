@@ -240,3 +240,23 @@ def test_time_factors_merge_across_closures():
         parts.add("time_source", forms.TimeFactor(2, 0.0, g + 1.0), np.ones(5, dtype=bool), np.ones(5))
     with pytest.raises(forms.UnsupportedFormError, match="time factors"):
         parts.add("time_source", forms.TimeFactor(2, 0.0, 99.0), np.ones(5, dtype=bool), np.ones(5))
+
+
+def test_system_time_factor_fit():
+    """System closures (the Brusselator's boundary values): the constant term's factor is fitted
+    and the remaining polynomial is the static part; t in a component-dependent term is refused."""
+    from fvmgpu import forms
+
+    x = np.linspace(0, 1, 12)
+    y = x[::-1].copy()
+    f = lambda x, y, t, u: -0.25 * np.exp(1 + y + t / 2) + 0.3 * u[0]  # noqa: E731
+    e, c, (tau, B) = forms.classify_system_poly(f, x, y, 0.0, 2, "f", max_degree=1, tf=5.0, time=True)
+    assert e.tolist() == [[1, 0]] and np.allclose(c[:, 0], 0.3, rtol=1e-13)
+    assert tau[0] == 1.0 and abs(tau[2] - 0.5) <= 1e-12
+    for t in (0.0, 1.3, 5.0):
+        assert np.allclose(tau(t) * B, -0.25 * np.exp(1 + y + t / 2), rtol=1e-13, atol=0)
+    e, c, tp = forms.classify_system_poly(lambda x, y, t, u: u[0] ** 2 * u[1] - 2 * u[0], x, y, 0.0, 2, "S",
+                                          tf=5.0, time=True)
+    assert tp is None and e.tolist() == [[1, 0], [2, 1]]
+    with pytest.raises(forms.UnsupportedFormError):
+        forms.classify_system_poly(lambda x, y, t, u: np.exp(-t) * u[0] + x, x, y, 0.0, 2, "g", tf=1.0, time=True)
