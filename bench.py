@@ -346,9 +346,13 @@ def run_gpu(args):
     _lib.require_gpu()
     t_setup = time.perf_counter()
     tri = c2_triangulation()
+    t_mesh = time.perf_counter()
     mesh = F.FVMGeometry(tri)
+    t_prob = time.perf_counter()
     prob = c2_problem(mesh)
     info = prob.info()
+    setup = {"triangulate_rectangle_s": t_mesh - t_setup, "fvm_geometry_s": t_prob - t_mesh,
+             "fvm_problem_s": time.perf_counter() - t_prob}
     n = tri.num_points
     units = flux_evals(tri)
     log(f"[bench] setup {time.perf_counter() - t_setup:.1f} s; operator nonzeros {info['operator_nonzeros']}, "
@@ -405,6 +409,7 @@ def run_gpu(args):
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n,
                 "ms_per_step": float(ms_e2e.mean()), "path": "fvm_rhs C ABI, pinned host buffers"},
         "clocks": clk.summary(),
+        "setup": _round(setup),
     }
     if per_step is not None and per_e2e is not None:
         # value's K steps plus e2e's K steps, each counted by the activity profiler
@@ -577,8 +582,12 @@ def run_steady(args, F):
             t0 = time.perf_counter()
             if npts not in meshes:
                 meshes = {npts: F.triangulate_disk(npts, 4096, seed=0)}
+            t1 = time.perf_counter()
             pois, A, b = c3_poisson(F, meshes[npts], dkind)
-            r = {"nv": int(A.shape[0]), "nnz": int(A.nnz), "rtol": rtol, "setup_s": time.perf_counter() - t0}
+            # mesh_gen_s: the disk mesh generator standing in for DelaunayTriangulation;
+            # setup_s: FVMGeometry, PoissonsEquation (conditions, sampling, assembly) and the host export
+            r = {"nv": int(A.shape[0]), "nnz": int(A.nnz), "rtol": rtol, "mesh_gen_s": t1 - t0,
+                 "setup_s": time.perf_counter() - t1}
             if label in STEADY_FLOOR:
                 r["fl_xstar_residual"] = STEADY_FLOOR[label]
             modes = [("fp64", "chebyshev", 4), ("mixed", "chebyshev", 4), ("fp64", "chebyshev", 8),

@@ -451,6 +451,8 @@ void problem_dirichlet_internal(const fvm_problem* p, double* u, double t, cudaS
 void problem_rhs_internal(fvm_problem* p, const double* u, double* du, bool force_triangle, cudaStream_t s,
                           bool conservative, double t) {
     fvm_mesh* m = p->mesh;
+    if (p->conditions_only)
+        fail(FVM_ERR_INVALID_ARGUMENT, "this problem carries a template's conditions only (FVM_PROBLEM_CONDITIONS_ONLY)");
     if (p->ntime > 0 && force_triangle)
         fail(FVM_ERR_UNSUPPORTED, "time-dependent values run on the operator path only (no force_triangle)");
     if (p->linear && !force_triangle) {
@@ -714,6 +716,7 @@ int fvm_tsit5_solve(fvm_problem* p, const double* u0, const fvm_ode_options* opt
                     void* stream) {
     return guard([&] {
         if (!p || !u0 || !opt || !out) fail(FVM_ERR_INVALID_ARGUMENT, "NULL argument");
+        if (p->conditions_only) fail(FVM_ERR_INVALID_ARGUMENT, "this problem carries a template's conditions only");
         cudaStream_t s = (cudaStream_t)stream;
         fvm_mesh* m = p->mesh;
         const int64_t n = m->np;

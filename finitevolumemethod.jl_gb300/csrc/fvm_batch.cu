@@ -409,6 +409,7 @@ int fvm_batch_create(fvm_problem* p, int32_t batch, const double* dualD, const d
         if (!p || !dualD || !out) fail(FVM_ERR_INVALID_ARGUMENT, "NULL argument");
         if (batch < 1) fail(FVM_ERR_INVALID_ARGUMENT, "batch must be positive");
         if (precision != FVM_FP64 && precision != FVM_FP32) fail(FVM_ERR_INVALID_ARGUMENT, "bad precision");
+        if (p->conditions_only) fail(FVM_ERR_INVALID_ARGUMENT, "this problem carries a template's conditions only");
         if (p->dif_deg != 0 || !p->linear || p->flux_linear || p->ntime > 0)
             fail(FVM_ERR_UNSUPPORTED_FORM, "batched instances need a linear, time-independent problem with a diffusion "
                                            "flux -D(x, y) grad u");

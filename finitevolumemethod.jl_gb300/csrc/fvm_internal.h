@@ -9,6 +9,9 @@
 #include <memory>
 #include <stdexcept>
 #include <functional>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
 #include "../../include/fvm_gpu.h"
 
 namespace fvm {
@@ -23,6 +26,23 @@ void set_last_error(const std::string& msg);
 void cuda_check(cudaError_t e, const char* what);
 #define FVM_CUDA(x) ::fvm::cuda_check((x), #x)
 
+// Set-up phase timing on stderr when FVM_SETUP_TRACE is set: mark("phase") prints the time
+// since the previous mark (or construction).
+struct SetupTrace {
+    const char* scope;
+    bool on;
+    std::chrono::steady_clock::time_point t0;
+    explicit SetupTrace(const char* s) : scope(s), on(std::getenv("FVM_SETUP_TRACE") != nullptr),
+                                         t0(std::chrono::steady_clock::now()) {}
+    void mark(const char* phase) {
+        if (!on) return;
+        auto t1 = std::chrono::steady_clock::now();
+        std::fprintf(stderr, "[fvm setup] %s %s %.1f ms\n", scope, phase,
+                     std::chrono::duration<double, std::milli>(t1 - t0).count());
+        t0 = t1;
+    }
+};
+
 // ---- device buffer (RAII) ------------------------------------------------------------
 struct DBuf {
     void* p = nullptr;
@@ -30,6 +50,20 @@ struct DBuf {
     DBuf() = default;
     DBuf(const DBuf&) = delete;
     DBuf& operator=(const DBuf&) = delete;
+    DBuf(DBuf&& o) noexcept : p(o.p), bytes(o.bytes) {
+        o.p = nullptr;
+        o.bytes = 0;
+    }
+    DBuf& operator=(DBuf&& o) noexcept {
+        if (this != &o) {
+            release();
+            p = o.p;
+            bytes = o.bytes;
+            o.p = nullptr;
+            o.bytes = 0;
+        }
+        return *this;
+    }
     ~DBuf() { release(); }
     void release() {
         if (p) cudaFree(p);
@@ -120,6 +154,7 @@ struct fvm_problem {
     int precision = FVM_FP64;
     int dif_deg = 0, neu_deg = 0, src_deg = 0, dudt_deg = 0;
     bool linear = true;                         // every form is affine in u (quadratic only on the diagonal)
+    bool conditions_only = false;               // a template's conditions: no operator assembled
     std::vector<int8_t> code;                   // [np] caller order
     std::vector<int8_t> bneu;                   // [nbe]
     std::vector<double> dualD, quarterD, quarterN, src, dudt, dirv;  // copies of the descriptor arrays
@@ -259,6 +294,13 @@ void launch_adaptive_step_end(AdaptState* st, double* out, const double* u, cons
                               cudaStream_t s);
 
 }  // namespace fvm
+
+// The mesh build of fvm_mesh_create on the device (fvm_mesh_dev.cu): geometry, control volumes,
+// boundary-edge triangles, Hilbert order and the vertex-neighbour pattern, identical to the host
+// build; fills the host copies the set-up code reads.
+namespace fvm {
+void mesh_ingest_device(fvm_mesh* m, const int32_t* boundary_adjacent, bool renumber);
+}
 
 // Linear terms of a problem's RHS: emit(row, col, coef, didx, flux), rows and columns in the
 // caller's numbering; the coefficient multiplies D[didx] when didx >= 0 (fvm_problem.cpp).

@@ -2,6 +2,7 @@
 // operator pattern (sliced ELL) and the vertex tiles of the per-triangle flux kernel.
 // Compiled with -ffp-contract=off so the geometry arithmetic rounds like the reference.
 #include "fvm_internal.h"
+#include "fvm_geometry.h"
 #include <algorithm>
 #include <cmath>
 #include <numeric>
@@ -12,6 +13,11 @@ namespace fvm {
 int64_t SellPattern::find_csr(int32_t row, int32_t c) const {
     int64_t lo = rowptr[row], hi = rowptr[row + 1];
     const int32_t* b = csr_col.data();
+    if (hi - lo <= 16) {  // the usual vertex degree: a short sorted scan
+        for (int64_t q = lo; q < hi && b[q] <= c; ++q)
+            if (b[q] == c) return q;
+        return -1;
+    }
     const int32_t* it = std::lower_bound(b + lo, b + hi, c);
     if (it == b + hi || *it != c) return -1;
     return it - b;
@@ -22,75 +28,9 @@ int64_t SellPattern::find(int32_t row, int32_t c) const {
     return q < 0 ? -1 : csr_slot[q];
 }
 
-// Hilbert index of (x, y) on a 2^16 x 2^16 grid (the standard rotate-and-reflect walk).
-static uint64_t hilbert_index(uint32_t x, uint32_t y) {
-    const uint32_t n = 1u << 16;
-    uint64_t d = 0;
-    for (uint32_t s = n / 2; s > 0; s /= 2) {
-        uint32_t rx = (x & s) ? 1u : 0u;
-        uint32_t ry = (y & s) ? 1u : 0u;
-        d += (uint64_t)s * s * ((3u * rx) ^ ry);
-        if (ry == 0) {
-            if (rx == 1) {
-                x = s - 1 - (x & (s - 1));
-                y = s - 1 - (y & (s - 1));
-            } else {
-                x &= (s - 1);
-                y &= (s - 1);
-            }
-            std::swap(x, y);
-        } else {
-            x &= (s - 1);
-            y &= (s - 1);
-        }
-    }
-    return d;
-}
-
 }  // namespace fvm
 
 using namespace fvm;
-
-// Geometry of one triangle, in the operation order of src/geometry.jl:107-161.
-static void triangle_geometry(const double* P, int32_t i, int32_t j, int32_t k, double* props, double S[3]) {
-    double px = P[2 * i], py = P[2 * i + 1];
-    double qx = P[2 * j], qy = P[2 * j + 1];
-    double rx = P[2 * k], ry = P[2 * k + 1];
-    // DelaunayTriangulation statistics: centroid and edge midpoints
-    double cx = (px + qx + rx) / 3, cy = (py + qy + ry) / 3;
-    double m1x = (px + qx) / 2, m1y = (py + qy) / 2;
-    double m2x = (qx + rx) / 2, m2y = (qy + ry) / 2;
-    double m3x = (rx + px) / 2, m3y = (ry + py) / 2;
-    double pcx = cx - px, pcy = cy - py;
-    double qcx = cx - qx, qcy = cy - qy;
-    double rcx = cx - rx, rcy = cy - ry;
-    double m13x = m1x - m3x, m13y = m1y - m3y;
-    double m21x = m2x - m1x, m21y = m2y - m1y;
-    double m32x = m3x - m2x, m32y = m3y - m2y;
-    S[0] = 0.5 * std::fabs(pcx * m13y - pcy * m13x);
-    S[1] = 0.5 * std::fabs(qcx * m21y - qcy * m21x);
-    S[2] = 0.5 * std::fabs(rcx * m32y - rcy * m32x);
-    double D = qx * ry - qy * rx - px * ry + rx * py + px * qy - qx * py;
-    props[0] = (qy - ry) / D;
-    props[1] = (ry - py) / D;
-    props[2] = (py - qy) / D;
-    props[3] = (rx - qx) / D;
-    props[4] = (px - rx) / D;
-    props[5] = (qx - px) / D;
-    props[6] = (qx * ry - rx * qy) / D;
-    props[7] = (rx * py - px * ry) / D;
-    props[8] = (px * qy - qx * py) / D;
-    double mx[3] = {m1x, m2x, m3x}, my[3] = {m1y, m2y, m3y};
-    for (int e = 0; e < 3; ++e) {
-        props[9 + 2 * e] = (mx[e] + cx) / 2;
-        props[10 + 2 * e] = (my[e] + cy) / 2;
-        double ex = cx - mx[e], ey = cy - my[e];
-        double l = std::sqrt(ex * ex + ey * ey);  // LinearAlgebra.norm of a 2-tuple, no rescaling needed
-        props[15 + 2 * e] = ey / l;
-        props[16 + 2 * e] = -ex / l;
-        props[21 + e] = l;
-    }
-}
 
 static inline uint64_t edge_key(int64_t a, int64_t b) { return ((uint64_t)(uint32_t)a << 32) | (uint32_t)b; }
 
@@ -145,6 +85,7 @@ extern "C" int fvm_mesh_create_impl(const double* points, int64_t npoints, const
     if (npoints <= 0 || ntri <= 0 || nbedge < 0) fail(FVM_ERR_INVALID_ARGUMENT, "mesh sizes must be positive");
     if (!points || !triangles || (nbedge > 0 && !boundary_edges)) fail(FVM_ERR_INVALID_ARGUMENT, "NULL mesh array");
     if (npoints >= (int64_t)INT32_MAX || ntri >= (int64_t)INT32_MAX) fail(FVM_ERR_INVALID_ARGUMENT, "mesh too large for 32-bit indices");
+    SetupTrace tr("mesh");
     std::unique_ptr<fvm_mesh> m(new fvm_mesh());
     FVM_CUDA(cudaGetDevice(&m->device));
     m->np = npoints;
@@ -160,6 +101,12 @@ extern "C" int fvm_mesh_create_impl(const double* points, int64_t npoints, const
     for (int64_t e = 0; e < 2 * nbedge; ++e)
         if (m->be[e] < 0 || m->be[e] >= npoints)
             fail(FVM_ERR_BAD_MESH, "boundary edge " + std::to_string(e / 2) + " has a vertex index out of range");
+    tr.mark("copy");
+    if (!(flags & FVM_MESH_HOST_INGEST)) {
+        mesh_ingest_device(m.get(), boundary_adjacent, !(flags & FVM_MESH_NO_RENUMBER));
+        *out = m.release();
+        return FVM_OK;
+    }
 
     // geometry (src/geometry.jl:99-169), triangles in the caller's order
     m->vol.assign(npoints, 0.0);
@@ -182,6 +129,7 @@ extern "C" int fvm_mesh_create_impl(const double* points, int64_t npoints, const
     }
     m->nv = 0;
     for (int64_t v = 0; v < npoints; ++v) m->nv += m->has_vertex[v];
+    tr.mark("geometry");
 
     // boundary edge -> triangle (get_adjacent + _safe_get_triangle_props, src/utils.jl:1-11)
     {
@@ -213,6 +161,7 @@ extern "C" int fvm_mesh_create_impl(const double* points, int64_t npoints, const
         }
     }
 
+    tr.mark("boundary triangles");
     // Hilbert renumbering of vertices; points that are not vertices go last
     m->perm.resize(npoints);
     m->iperm.resize(npoints);
@@ -230,9 +179,7 @@ extern "C" int fvm_mesh_create_impl(const double* points, int64_t npoints, const
         if (!(span > 0)) span = 1.0;
         std::vector<std::pair<uint64_t, int32_t>> key(npoints);
         for (int64_t v = 0; v < npoints; ++v) {
-            uint32_t hx = (uint32_t)std::min(65535.0, std::floor((P[2 * v] - xmin) / span * 65535.0));
-            uint32_t hy = (uint32_t)std::min(65535.0, std::floor((P[2 * v + 1] - ymin) / span * 65535.0));
-            uint64_t h = hilbert_index(hx, hy);
+            uint64_t h = point_hilbert_key(P[2 * v], P[2 * v + 1], xmin, ymin, span);
             if (!m->has_vertex[v]) h = ~0ull;
             key[v] = {h, (int32_t)v};
         }
@@ -241,6 +188,7 @@ extern "C" int fvm_mesh_create_impl(const double* points, int64_t npoints, const
     }
     for (int64_t v = 0; v < npoints; ++v) m->iperm[m->perm[v]] = (int32_t)v;
 
+    tr.mark("hilbert");
     // vertex-neighbour pattern (internal numbering): diagonal + every pair within a triangle
     {
         SellPattern& pat = m->pat;
@@ -287,6 +235,7 @@ extern "C" int fvm_mesh_create_impl(const double* points, int64_t npoints, const
         finalize_sell(off, npoints);
     }
 
+    tr.mark("pattern");
     // device-side vertex data
     m->d_perm.upload(m->perm);
     m->d_iperm.upload(m->iperm);
@@ -298,6 +247,7 @@ extern "C" int fvm_mesh_create_impl(const double* points, int64_t npoints, const
         }
         m->d_invV.upload(invV);
     }
+    tr.mark("upload");
     *out = m.release();
     return FVM_OK;
 }

@@ -59,6 +59,8 @@ extern "C" int fvm_rhs_noalloc(fvm_problem* p, const double* u, double* du, doub
             fvm::fail(FVM_ERR_INVALID_ARGUMENT, "fvm_rhs_noalloc handles at most " +
                                                     std::to_string(FVM_NOALLOC_MAX_POINTS) + " points; this mesh has " +
                                                     std::to_string(m->np) + " (use fvm_rhs)");
+        if (p->conditions_only)
+            fvm::fail(FVM_ERR_INVALID_ARGUMENT, "this problem carries a template's conditions only");
         if (!p->linear && !p->tri_ready)
             fvm::fail(FVM_ERR_INVALID_ARGUMENT,
                       "fvm_rhs_noalloc: this problem's per-triangle data is prepared by its first fvm_rhs call; "

@@ -30,6 +30,10 @@ def cuda_home() -> Path:
     return Path("/usr/local/cuda")
 
 
+# the device mesh build rounds like the host one (-ffp-contract=off there): no FMA contraction
+NVCC_FILE_FLAGS = {"fvm_mesh_dev.cu": ["-fmad=false"]}
+
+
 def sources():
     return sorted(CSRC.glob("*.cpp")), sorted(CSRC.glob("*.cu"))
 
@@ -65,7 +69,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     for src in cu:
         obj = objdir / (src.stem + ".cu.o")
         jobs.append([nvcc, "-std=c++17", "-O3", ARCH, "-lineinfo", "-Xcompiler", "-fPIC", *inc,
-                     "-c", str(src), "-o", str(obj)])
+                     *NVCC_FILE_FLAGS.get(src.name, []), "-c", str(src), "-o", str(obj)])
 
     def run(cmd):
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -25,11 +25,13 @@ FVM_ERR_STEP_LIMIT = 8
 
 FVM_VERTEX_FREE, FVM_VERTEX_DIRICHLET, FVM_VERTEX_DUDT, FVM_VERTEX_NOT_A_VERTEX = 0, 1, 2, 3
 FVM_MAX_TIME_FACTORS = 8
+FVM_PROBLEM_CONDITIONS_ONLY = 1
 FVM_PTR_HOST, FVM_PTR_DEVICE, FVM_PTR_DEVICE_INTERNAL = 0, 1, 2
 FVM_RHS_FORCE_TRIANGLE = 16
 FVM_RHS_CONSERVATIVE = 32
 FVM_FP64, FVM_FP32 = 0, 1
 FVM_MESH_NO_RENUMBER = 1
+FVM_MESH_HOST_INGEST = 2
 FVM_SYSTEM_MAX_EQ = 8
 FVM_SYSTEM_MAX_TERMS = 64
 FVM_TEMPLATE_DIFFUSION, FVM_TEMPLATE_LINEAR_REACTION_DIFFUSION = 0, 1
@@ -84,6 +86,7 @@ class ProblemDesc(C.Structure):
         ("time_neumann", c_double_p),
         ("time_source", c_double_p),
         ("time_dudt", c_double_p),
+        ("options", C.c_int32),
     ]
 
 

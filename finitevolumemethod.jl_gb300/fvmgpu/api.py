@@ -211,9 +211,11 @@ class TriangleProperties:
 class FVMGeometry:
     """FVMGeometry(tri) (src/geometry.jl:44-49,99-169): the mesh flattened once into
     Hilbert-ordered device arrays by libfvmgpu.  `cv_volumes` and `triangle_props` keep the
-    reference's meaning (caller numbering)."""
+    reference's meaning (caller numbering).  The geometry, the Hilbert order and the operator
+    pattern are computed on the device; host_ingest=True computes them on the host instead
+    (the two give identical meshes)."""
 
-    def __init__(self, tri: Triangulation, tile_vertices: int = 0, renumber: bool = True):
+    def __init__(self, tri: Triangulation, tile_vertices: int = 0, renumber: bool = True, host_ingest: bool = False):
         lib = load()
         _lib.require_gpu()
         self.triangulation = tri
@@ -224,7 +226,8 @@ class FVMGeometry:
         h = C.c_void_p()
         check(lib.fvm_mesh_create(dptr(pts), tri.num_points, dptr(tris, _lib.c_int32_p), tri.num_triangles,
                                   dptr(be, _lib.c_int32_p), dptr(badj, _lib.c_int32_p), tri.num_boundary_edges,
-                                  int(tile_vertices), 0 if renumber else _lib.FVM_MESH_NO_RENUMBER, C.byref(h)))
+                                  int(tile_vertices), (0 if renumber else _lib.FVM_MESH_NO_RENUMBER)
+                                  | (_lib.FVM_MESH_HOST_INGEST if host_ingest else 0), C.byref(h)))
         self._h = h
         self.cv_volumes = np.empty(tri.num_points)
         self._props = np.empty((tri.num_triangles, 24))
@@ -1201,6 +1204,7 @@ class _Template:
                 d.c.source_degree = 0
                 d.arr("source", as_f64(sv))
         d.c.precision = FVM_FP64
+        d.c.options = _lib.FVM_PROBLEM_CONDITIONS_ONLY  # the template assembles its own operator
         self._code = code
         hp = C.c_void_p()
         check(load().fvm_problem_create(mesh.handle, C.byref(d.c), C.byref(hp)))

@@ -15,7 +15,7 @@ quarter points) and classifies it:
 
 Classification probes the closure at u in {0, 1, -1} and t in {t0, t0 + 1.37}, fits the
 quadratic, and verifies it at u in {2, -0.5, 3.25} and at the second time, to a relative
-tolerance of 1e-10.  A time factor is fitted from c0 at six equally spaced times across
+tolerance of 1e-10 (two verifications at every point, the rest on a subsample).  A time factor is fitted from c0 at six equally spaced times across
 [t0, tf] and verified at three other times, to the same tolerance.
 """
 from __future__ import annotations
@@ -141,17 +141,29 @@ def fit_time_factor(c0_at, t0, tf, what):
 def classify_xytu(f, x, y, t0, what, max_degree=2, tf=None, time=False):
     """Coefficients (c0, c1, c2)[:deg+1] and degree of g(x, y, t, u) = f(x, y, t, u) at points.
 
+    The closure is evaluated at every point five times: the fit at u = 0, 1, -1, and two
+    verifications, u = 2 at t0 and u = -0.5 at the second time, which catch a part that is not
+    quadratic in u, or that depends on t, at any point.  The other probes (u = -0.5 and 3.25 at
+    t0, the fit values at the second time) run on a subsample of about 4096 points.
+
     time=True allows c0 to depend on t through one factor (`fit_time_factor` over [t0, tf]);
     then returns (coeffs, deg, tpart) with coeffs[..., 0] the static part A and tpart
     (TimeFactor, B) or None."""
     x = np.asarray(x, dtype=np.float64)
     y = np.asarray(y, dtype=np.float64)
+    n = x.shape[0] if x.ndim else 1
     t1 = float(t0)
     t2 = t1 + 1.37
-    try:
-        g = {u: evaluate(f, x, y, t1, np.full(x.shape, u)) for u in _FIT_U}
-    except Exception as e:  # noqa: BLE001
-        _reject(what, f"evaluation failed ({e!r})")
+    sub = slice(None, None, max(1, n // 4096)) if x.ndim else slice(None)
+
+    def ev(t, u, at=slice(None)):
+        xs, ys = (x[at], y[at]) if x.ndim else (x, y)
+        try:
+            return evaluate(f, xs, ys, t, np.full(xs.shape, u))
+        except Exception as e:  # noqa: BLE001
+            _reject(what, f"evaluation failed ({e!r})")
+
+    g = {u: ev(t1, u) for u in _FIT_U}
     for v in g.values():
         if not np.all(np.isfinite(v)):
             _reject(what, "non-finite values")
@@ -160,23 +172,42 @@ def classify_xytu(f, x, y, t0, what, max_degree=2, tf=None, time=False):
     c2 = (g[1.0] + g[-1.0]) / 2 - c0
     scale = np.maximum(np.maximum(np.abs(c0), np.abs(c1)), np.abs(c2))
     scale = np.maximum(scale, np.max(scale) * 1e-300 + 1e-300)
-    for u in _CHECK_U:
-        gu = evaluate(f, x, y, t1, np.full(x.shape, u))
-        pred = c0 + u * (c1 + u * c2)
-        if not np.all(np.abs(gu - pred) <= _RTOL * (scale * (1 + abs(u)) ** 2)):
-            _reject(what, "not a polynomial of degree <= 2 in u")
-    tpart = None
-    gt = {u: evaluate(f, x, y, t2, np.full(x.shape, u)) for u in _FIT_U}
-    if time:
-        fit = fit_time_factor(lambda t: evaluate(f, x, y, t, np.zeros(x.shape)), t1, tf, what)
-        if fit is not None:
-            c0, tau, B = fit
-            tpart = (tau, B)
-            # only c0 may vary: the u-dependent part at the second time is the first's
-            gt = {u: gt[u] - gt[0.0] + g[0.0] for u in _FIT_U}
+    B = np.zeros_like(c0)
+    tau = None
+
+    def fit_time(at):
+        return fit_time_factor(lambda t: ev(t, 0.0, at), t1, tf, what)
+
+    if time and fit_time(sub) is not None:  # the factor, fitted at every point
+        _, tau, B = fit_time(slice(None))
+
+    def check(t, u, at, why):
+        got = ev(t, u, at)
+        dt = 0.0 if tau is None else tau(t) - 1.0
+        pred = c0[at] + dt * B[at] + u * (c1[at] + u * c2[at])
+        sc = np.maximum(scale[at], np.abs(dt * B[at]))
+        if not np.all(np.abs(got - pred) <= _RTOL * (sc * (1 + abs(u)) ** 2)):
+            _reject(what, why)
+
+    poly = "not a polynomial of degree <= 2 in u"
+    tdep = "depends on t" + (" in its u-dependent terms" if time else "")
+    check(t1, 2.0, slice(None), poly)
+    if time and tau is None:
+        # a t dependence the subsample missed: fit it at every point before the full check
+        try:
+            check(t2, -0.5, slice(None), tdep)
+        except UnsupportedFormError:
+            fit = fit_time(slice(None))
+            if fit is None:
+                raise
+            _, tau, B = fit
+    check(t2, -0.5, slice(None), tdep)
+    for u in _CHECK_U[1:]:
+        check(t1, u, sub, poly)
     for u in _FIT_U:
-        if not np.all(np.abs(gt[u] - g[u]) <= _RTOL * (scale * (1 + abs(u)) ** 2)):
-            _reject(what, "depends on t" + (" in its u-dependent terms" if time else ""))
+        check(t2, u, sub, tdep)
+    if tau is not None:
+        c0 = c0 - B
     tiny = 1e-14 * np.max(scale) if scale.size else 0.0
     if np.all(np.abs(c2) <= tiny):
         c2 = np.zeros_like(c2)
@@ -187,7 +218,7 @@ def classify_xytu(f, x, y, t0, what, max_degree=2, tf=None, time=False):
         _reject(what, f"degree {deg} in u exceeds {max_degree}")
     coeffs = np.stack([c0, c1, c2][: deg + 1], axis=-1)
     if time:
-        return coeffs, deg, tpart
+        return coeffs, deg, (None if tau is None else (tau, B))
     return coeffs, deg
 
 

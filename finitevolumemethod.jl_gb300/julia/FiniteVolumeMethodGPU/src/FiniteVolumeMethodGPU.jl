@@ -51,6 +51,7 @@ struct ProblemDesc
     time_neumann::Ptr{Float64}
     time_source::Ptr{Float64}
     time_dudt::Ptr{Float64}
+    options::Int32
 end
 
 struct OdeOptions
@@ -229,7 +230,7 @@ function GPUProblem(prob::FVM.FVMProblem; precision = :fp64)
         isempty(quarterN) ? Ptr{Float64}(C_NULL) : pointer(quarterN), Int32(sdeg), pointer(Sc), Int32(udeg),
         pointer(dudt), pointer(dir), precision == :fp32 ? Int32(1) : Int32(0), Ptr{Float64}(C_NULL),
         Ptr{Float64}(C_NULL), Int32(0), Ptr{Float64}(C_NULL), Ptr{Float64}(C_NULL), Ptr{Float64}(C_NULL),
-        Ptr{Float64}(C_NULL), Ptr{Float64}(C_NULL))
+        Ptr{Float64}(C_NULL), Ptr{Float64}(C_NULL), Int32(0))
     h = Ref{Ptr{Cvoid}}(C_NULL)
     GC.@preserve keep check(ccall((:fvm_problem_create, libfvmgpu), Cint,
         (Ptr{Cvoid}, Ref{ProblemDesc}, Ref{Ptr{Cvoid}}), m.handle, desc, h))

@@ -72,8 +72,12 @@ int fvm_device_count(int* count);
  *   boundary_edges    [2*nbedge]    (i, j) with the domain on the left
  *   boundary_adjacent [nbedge]      k = get_adjacent(tri, i, j), or NULL to look it up
  *   tile_vertices     vertices per tile of the triangle kernel (0 = default)
- *   flags             FVM_MESH_NO_RENUMBER keeps the caller's numbering internally */
+ *   flags             FVM_MESH_NO_RENUMBER keeps the caller's numbering internally;
+ *                     FVM_MESH_HOST_INGEST builds the mesh data on the host */
 #define FVM_MESH_NO_RENUMBER 1
+/* FVM_MESH_HOST_INGEST builds the geometry, Hilbert order and operator pattern on the host
+ * (by default they are built on the device; both builds give identical meshes) */
+#define FVM_MESH_HOST_INGEST 2
 int fvm_mesh_create(const double* points, int64_t npoints, const int32_t* triangles, int64_t ntri,
                     const int32_t* boundary_edges, const int32_t* boundary_adjacent, int64_t nbedge,
                     int32_t tile_vertices, int32_t flags, fvm_mesh** out);
@@ -142,7 +146,11 @@ typedef struct fvm_problem_desc {
     const double* time_neumann;     /* [ntime][nbedge*2] Neumann values q.n at the quarter points */
     const double* time_source;      /* [ntime][npoints] source values on free vertices */
     const double* time_dudt;        /* [ntime][npoints] Dudt values */
+    int32_t options;                /* FVM_PROBLEM_* bits */
 } fvm_problem_desc;
+/* The problem only carries a template's conditions and samples (fvm_template_create): no
+ * operator is assembled, and the RHS and time-stepping calls refuse it. */
+#define FVM_PROBLEM_CONDITIONS_ONLY 1
 #define FVM_MAX_TIME_FACTORS 8
 
 /* Replaces FVMProblem(mesh, BCs, ICs; ...) (src/problem.jl:118-163) together with

@@ -260,3 +260,24 @@ def test_system_time_factor_fit():
     assert tp is None and e.tolist() == [[1, 0], [2, 1]]
     with pytest.raises(forms.UnsupportedFormError):
         forms.classify_system_poly(lambda x, y, t, u: np.exp(-t) * u[0] + x, x, y, 0.0, 2, "g", tf=1.0, time=True)
+
+
+def test_classification_checks_every_point():
+    """Only two of the verification probes run at every point; they still catch a t dependence
+    or a non-polynomial u dependence confined to one point off the subsample, and a time factor
+    there is fitted at every point."""
+    from fvmgpu import forms
+
+    n = 40_000
+    x = np.linspace(0.0, 1.0, n)
+    y = np.zeros(n)
+    x5 = x[5]  # the subsample takes every 9th point: 0, 9, 18, ...
+    odd = lambda x: np.where(x == x5, 1.0, 0.0)  # noqa: E731
+    with pytest.raises(forms.UnsupportedFormError, match="depends on t"):
+        forms.classify_xytu(lambda x, y, t, u: x + odd(x) * t, x, y, 0.0, "f")
+    with pytest.raises(forms.UnsupportedFormError, match="polynomial"):
+        forms.classify_xytu(lambda x, y, t, u: x + odd(x) * np.exp(u), x, y, 0.0, "f")
+    c, deg, (tau, B) = forms.classify_xytu(lambda x, y, t, u: x + odd(x) * np.exp(-t), x, y, 0.0, "f", tf=1.0,
+                                           time=True)
+    assert deg == 0 and tau[0] == 1.0 and abs(tau[2] + 1.0) < 1e-12
+    assert abs(B[5] - 1.0) < 1e-12 and np.all(B[np.arange(n) != 5] == 0)
