@@ -115,6 +115,17 @@ struct SellPattern {
 };
 
 // ---- mesh ----------------------------------------------------------------------------
+// Point location and interpolation data (fvm_post.cu), built on first use: a uniform grid
+// over the bounding box, each cell listing (in ascending order) the triangles whose bounding
+// box meets it; the points, triangles and shape coefficients in the caller's numbering.
+struct Locator {
+    bool ready = false;
+    double xmin = 0, ymin = 0, h = 1;
+    int64_t gx = 1, gy = 1;
+    DBuf d_cell_start, d_cell_tri;  // [gx*gy+1], [pairs]
+    DBuf d_pts, d_tri, d_shape;     // [np][2], [nt][3], [nt][9]
+};
+
 struct Tiles {
     bool built = false;
     int tile_vertices = 0;
@@ -144,6 +155,7 @@ struct fvm_mesh {
     fvm::SellPattern pat;                       // vertex-neighbour pattern with the diagonal (templates)
     fvm::SellPattern pat_off;                   // off-diagonal neighbours only (difference-form RHS)
     fvm::Tiles tiles;
+    fvm::Locator loc;
     fvm::DBuf d_perm, d_iperm, d_invV;          // d_invV internal order
     int tile_vertices_req = 0;
     void build_tiles();

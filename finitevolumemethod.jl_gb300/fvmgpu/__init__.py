@@ -10,7 +10,7 @@ from .api import (ConditionType, Neumann, Dudt, Dirichlet, Constrained, Parametr
                   update_dirichlet_nodes, DiffusionEquation, LinearReactionDiffusionEquation, PoissonsEquation,
                   MeanExitTimeProblem, Tsit5, KrylovSolver, ODESolution, LinearSolution, solve, BatchedProblem,
                   AdjointProblem, solve_rrule, FVMSystem, InvalidFluxError,
-                  jacobian_sparsity, compute_flux, pl_interpolate, two_point_interpolant,
+                  jacobian_sparsity, compute_flux, pl_interpolate, interpolate, two_point_interpolant,
                   construct_flux_function)
 from ._lib import FVMError, UnsupportedFormError, NotConvergedError
 from ._build import build, lib_path
@@ -21,7 +21,7 @@ __all__ = [
     "InternalConditions", "Conditions", "TriangleProperties", "FVMGeometry", "FVMProblem", "fvm_eqs",
     "update_dirichlet_nodes", "DiffusionEquation", "LinearReactionDiffusionEquation", "PoissonsEquation",
     "MeanExitTimeProblem", "Tsit5", "KrylovSolver", "ODESolution", "LinearSolution", "solve", "BatchedProblem",
-    "disjoint_union", "AdjointProblem", "solve_rrule", "FVMSystem", "InvalidFluxError", "jacobian_sparsity", "compute_flux", "pl_interpolate",
+    "disjoint_union", "AdjointProblem", "solve_rrule", "FVMSystem", "InvalidFluxError", "jacobian_sparsity", "compute_flux", "pl_interpolate", "interpolate",
     "two_point_interpolant", "construct_flux_function", "FVMError",
     "UnsupportedFormError", "NotConvergedError", "build", "lib_path",
 ]

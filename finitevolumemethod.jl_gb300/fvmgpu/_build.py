@@ -31,7 +31,7 @@ def cuda_home() -> Path:
 
 
 # the device mesh build rounds like the host one (-ffp-contract=off there): no FMA contraction
-NVCC_FILE_FLAGS = {"fvm_mesh_dev.cu": ["-fmad=false"]}
+NVCC_FILE_FLAGS = {"fvm_mesh_dev.cu": ["-fmad=false"], "fvm_post.cu": ["-fmad=false"]}
 
 
 def sources():

@@ -162,6 +162,9 @@ SIGNATURES = {
     "fvm_mesh_geometry": (C.c_int, [C.c_void_p, c_double_p, c_double_p]),
     "fvm_mesh_sample_points": (C.c_int, [C.c_void_p, c_double_p, c_double_p]),
     "fvm_mesh_permutation": (C.c_int, [C.c_void_p, c_int32_p]),
+    "fvm_mesh_locate": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]),
+    "fvm_pl_interpolate": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int64, C.c_void_p, C.c_void_p,
+                                     C.c_void_p, C.c_int32, C.c_void_p]),
     "fvm_mesh_export_connectivity": (C.c_int, [C.c_void_p, c_int32_p, c_int32_p]),
     "fvm_problem_create": (C.c_int, [C.c_void_p, C.POINTER(ProblemDesc), C.POINTER(C.c_void_p)]),
     "fvm_problem_destroy": (C.c_int, [C.c_void_p]),

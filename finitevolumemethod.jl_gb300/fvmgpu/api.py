@@ -275,6 +275,19 @@ class FVMGeometry:
         check(load().fvm_mesh_permutation(self._h, dptr(p, _lib.c_int32_p)))
         return p
 
+    def locate(self, x, y=None, stream=None):
+        """Triangle holding each query point, on the device (fvm_mesh_locate): the caller index
+        of a solid triangle containing (x[q], y[q]) (the lowest such index for points on shared
+        edges), -1 outside the mesh.  x, y: host arrays (or x an (nq, 2) array and y None), or an
+        (nq, 2) CUDA float64 tensor as x; returns int64 of the same kind."""
+        xy = _query_points(x, y)
+        p, loc = _lib.array_pointer(xy)
+        out = _like(xy, (xy.shape[0],), "int64")
+        op, _ = _lib.array_pointer(out, "int64")
+        s = stream if stream is not None else _lib.current_stream_handle()
+        check(load().fvm_mesh_locate(self._h, xy.shape[0], p, op, loc, s))
+        return out
+
     def export_connectivity(self):
         tri = self.triangulation
         t = np.empty((tri.num_triangles, 3), dtype=np.int32)
@@ -653,6 +666,57 @@ def compute_flux(prob, i, j, u, t):
         return tuple(out)
     qvx, qvy = q(mx, my, t, a, b, g)
     return nx * qvx + ny * qvy
+
+
+def _query_points(x, y):
+    if y is None:
+        xy = x
+    else:
+        xy = np.stack([np.asarray(x, dtype=np.float64).ravel(), np.asarray(y, dtype=np.float64).ravel()], axis=1)
+    if isinstance(xy, np.ndarray):
+        return np.ascontiguousarray(xy, dtype=np.float64).reshape(-1, 2)
+    return xy.reshape(-1, 2).contiguous()
+
+
+def _like(ref, shape, dtype):
+    if isinstance(ref, np.ndarray):
+        return np.empty(shape, dtype=dtype)
+    import torch
+
+    return torch.empty(shape, dtype=getattr(torch, dtype), device=ref.device)
+
+
+def interpolate(prob, u, x, y=None, T=None, stream=None):
+    """pl_interpolate(prob, T, u, x, y) (src/utils.jl:23-27) for many points at once, on the
+    device: each point is located (FVMGeometry.locate, the step the reference's tutorials take
+    with jump_and_march) unless the triangles T (caller indices) are given, and u's
+    piecewise-linear interpolant is evaluated there; NaN outside the mesh.  `prob` is a problem,
+    system, template or FVMGeometry; u (npoints,) or (N, npoints), x, y host arrays (or x an
+    (nq, 2) array), or CUDA tensors.  Returns (nq,) or (N, nq) values of u's kind."""
+    mesh = prob if isinstance(prob, FVMGeometry) else prob.mesh
+    xy = _query_points(x, y)
+    nq = xy.shape[0]
+    host = isinstance(xy, np.ndarray)
+    tri = mesh.locate(xy, stream=stream) if T is None else T
+    if host:
+        tri = np.ascontiguousarray(tri, dtype=np.int64).reshape(-1)
+        uu = np.asarray(u, dtype=np.float64)
+        ncomp = 1 if uu.ndim == 1 else uu.shape[0]
+        uflat = np.ascontiguousarray(uu.T if uu.ndim == 2 else uu)
+    else:
+        tri = tri.reshape(-1).to(dtype=getattr(__import__("torch"), "int64")).contiguous()
+        ncomp = 1 if u.dim() == 1 else u.shape[0]
+        uflat = (u.T if u.dim() == 2 else u).contiguous()
+    if tri.shape[0] != nq:
+        raise ValueError("T must give one triangle per query point")
+    out = _like(xy, (nq, ncomp), "float64")
+    up, loc = _lib.array_pointer(uflat)
+    tp, _ = _lib.array_pointer(tri, "int64")
+    xp, _ = _lib.array_pointer(xy)
+    op, _ = _lib.array_pointer(out)
+    s = stream if stream is not None else _lib.current_stream_handle()
+    check(load().fvm_pl_interpolate(mesh.handle, up, ncomp, nq, tp, xp, op, loc, s))
+    return out[:, 0] if ncomp == 1 and (u.ndim if host else u.dim()) == 1 else out.T
 
 
 def pl_interpolate(prob, T, u, x, y):

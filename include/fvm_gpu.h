@@ -196,6 +196,21 @@ int fvm_test_set_stream_waits(int64_t consumer_wait_ns, int64_t producer_delay_n
 /* Replaces update_dirichlet_nodes! (src/equations/dirichlet.jl:78-86). */
 int fvm_dirichlet_apply(fvm_problem* prob, double* u, double t, int32_t flags, void* stream);
 
+/* ---- post-processing on the device ------------------------------------------------------ */
+/* Point location, the step the reference's tutorials take with DelaunayTriangulation's
+ * jump_and_march before pl_interpolate: tri_out[q] = the caller index of a solid triangle that
+ * holds point (xy[2q], xy[2q+1]) -- the lowest such index, for points on shared edges -- or -1
+ * outside the mesh.  xy [nq][2] and tri_out [nq] are host or device arrays (flags FVM_PTR_HOST
+ * or FVM_PTR_DEVICE).  The first call builds a uniform grid of the triangles on the device. */
+int fvm_mesh_locate(fvm_mesh* mesh, int64_t nq, const double* xy, int64_t* tri_out, int32_t flags, void* stream);
+/* Replaces pl_interpolate(prob, T, u, x, y) (src/utils.jl:23-27) for nq points at once:
+ * out[q][c] = alpha_c x + beta_c y + gamma_c, the shape-function coefficients of component c of
+ * u on triangle tri[q] (a caller index; -1 gives NaN).  u [npoints][ncomp]; u, tri, xy and out
+ * are host or device arrays per flags (FVM_PTR_HOST, FVM_PTR_DEVICE; FVM_PTR_DEVICE_INTERNAL
+ * takes u in the internal numbering, the other arrays on the device). */
+int fvm_pl_interpolate(fvm_mesh* mesh, const double* u, int32_t ncomp, int64_t nq, const int64_t* tri,
+                       const double* xy, double* out, int32_t flags, void* stream);
+
 /* ---- time stepping (solve(prob, Tsit5(); saveat), src/solve.jl:167-208) ---------------- */
 typedef struct fvm_ode_options {
     double t0, tf;
