@@ -12,6 +12,15 @@ same for an `FVMSystem`, whose sources and conditions may be polynomials of tota
 in the component tuple and whose fluxes may couple the components linearly.
 Indices passed to the C ABI are 0-based.
 
+Also bound: the four templates (`GPUTemplate`: `DiffusionEquation`,
+`LinearReactionDiffusionEquation`, `PoissonsEquation`, `MeanExitTimeProblem`, with time stepping
+or the steady Krylov solve), batched instances (`GPUBatch`), the discrete adjoint of the time
+templates (`GPUAdjoint`, with a `ChainRulesCore.rrule` for `adjoint_solve`) and device point
+location / interpolation (`locate`, `interpolate`).  With OrdinaryDiffEqTsit5 loaded, the package
+extension adds `CommonSolve.solve(prob, Tsit5(); saveat, ...)` methods for `FVMProblem`,
+`FVMSystem`, `DiffusionEquation` and `LinearReactionDiffusionEquation`, so scripts written for
+the reference run unchanged, and `CommonSolve.solve(tmpl, GPUKrylov())` for the steady templates.
+
 This layer has not been executed: Julia is not installed on the machines this build was
 developed and measured on.
 """
@@ -19,15 +28,27 @@ module FiniteVolumeMethodGPU
 
 using FiniteVolumeMethod
 using DelaunayTriangulation
+using ChainRulesCore
+import CommonSolve
 const FVM = FiniteVolumeMethod
 const DT = DelaunayTriangulation
+
+export GPUProblem, GPUSystem, GPUTemplate, GPUBatch, GPUAdjoint, GPUKrylov, adjoint_solve, adjoint_pullback,
+    set_log_diffusion!, locate, interpolate, steady_solve
 
 const libfvmgpu = get(ENV, "FVMGPU_LIB", joinpath(@__DIR__, "..", "..", "..", "fvmgpu", "_lib", "libfvmgpu.so"))
 
 const FVM_OK = Cint(0)
 const FVM_PTR_HOST = Cint(0)
 const FVM_PTR_DEVICE = Cint(1)
+const FVM_PTR_DEVICE_INTERNAL = Cint(2)
 const FVM_VERTEX_FREE, FVM_VERTEX_DIRICHLET, FVM_VERTEX_DUDT, FVM_VERTEX_NOT_A_VERTEX = Int8(0), Int8(1), Int8(2), Int8(3)
+const FVM_PROBLEM_CONDITIONS_ONLY = Int32(1)
+const FVM_TEMPLATE_DIFFUSION, FVM_TEMPLATE_LINEAR_REACTION_DIFFUSION, FVM_TEMPLATE_POISSON, FVM_TEMPLATE_MEAN_EXIT_TIME =
+    Int32(0), Int32(1), Int32(2), Int32(3)
+const FVM_SOLVER_AUTO, FVM_SOLVER_CG, FVM_SOLVER_BICGSTAB = Int32(0), Int32(1), Int32(2)
+const FVM_PRECOND_JACOBI, FVM_PRECOND_CHEBYSHEV = Int32(0), Int32(1)
+const FVM_SOLVE_FP64, FVM_SOLVE_MIXED, FVM_SOLVE_FP32_PRECOND = Int32(0), Int32(1), Int32(2)
 
 struct ProblemDesc
     vertex_code::Ptr{Int8}
@@ -160,6 +181,25 @@ function classify(f, xs, ys, t0; maxdeg = 2, what = "function")
     return permutedims(hcat(c0, c1, c2)[:, 1:deg+1]), deg
 end
 
+# FVM_VERTEX_* per point (Dirichlet before Dudt: source_contributions.jl:5-11) and the
+# Neumann flag of each boundary edge, from the merged Conditions
+function vertex_codes(tri, conds, np)
+    code = fill(FVM_VERTEX_FREE, np)
+    for i in 1:np
+        if !DT.has_vertex(tri, i)
+            code[i] = FVM_VERTEX_NOT_A_VERTEX
+        elseif FVM.is_dirichlet_node(conds, i)
+            code[i] = FVM_VERTEX_DIRICHLET
+        elseif FVM.is_dudt_node(conds, i)
+            code[i] = FVM_VERTEX_DUDT
+        end
+    end
+    return code
+end
+
+neumann_flags(conds, m::GPUMesh) =
+    Int8[FVM.is_neumann_edge(conds, m.bedges[1, e] + 1, m.bedges[2, e] + 1) for e in 1:size(m.bedges, 2)]
+
 # ---- problem: FVMProblem(mesh, BCs, ICs; ...) (src/problem.jl:118-163) ---------------------
 mutable struct GPUProblem{P}
     prob::P
@@ -174,17 +214,8 @@ function GPUProblem(prob::FVM.FVMProblem; precision = :fp64)
     conds = prob.conditions
     np = m.npoints
     t0 = prob.initial_time
-    code = fill(FVM_VERTEX_FREE, np)
-    for i in 1:np
-        if !DT.has_vertex(tri, i)
-            code[i] = FVM_VERTEX_NOT_A_VERTEX
-        elseif FVM.is_dirichlet_node(conds, i)
-            code[i] = FVM_VERTEX_DIRICHLET
-        elseif FVM.is_dudt_node(conds, i)
-            code[i] = FVM_VERTEX_DUDT
-        end
-    end
-    neu = Int8[FVM.is_neumann_edge(conds, m.bedges[1, e] + 1, m.bedges[2, e] + 1) for e in 1:size(m.bedges, 2)]
+    code = vertex_codes(tri, conds, np)
+    neu = neumann_flags(conds, m)
     dual, quarter = sample_points(m)
     # q(x, y, t, alpha, beta, gamma) = -D(x, y, u) (alpha, beta): D is recovered as -q_x(1, 0, 0)
     q = (x, y, t, u) -> -prob.flux_function(x, y, t, 1.0, 0.0, u, prob.flux_parameters)[1]
@@ -200,8 +231,8 @@ function GPUProblem(prob::FVM.FVMProblem; precision = :fp64)
             neu[e] == 1 || continue
             fidx = FVM.get_neumann_fidx(conds, m.bedges[1, e] + 1, m.bedges[2, e] + 1)
             f = (x, y, t, u) -> FVM.eval_condition_fnc(conds, fidx, x, y, t, u)
-            c, d = classify(f, quarter[1, 2e-1:2e], quarter[2, 2e-1:2e], t0; what = "Neumann function $(fidx)")
-            qN[1:d+1, 2e-1:2e] .= c
+            c, d = classify(f, quarter[1, (2*e-1):(2*e)], quarter[2, (2*e-1):(2*e)], t0; what = "Neumann function $(fidx)")
+            qN[1:d+1, (2*e-1):(2*e)] .= c
             ndeg = max(ndeg, d)
         end
         quarterN = vec(qN[1:ndeg+1, :])
@@ -438,11 +469,11 @@ function GPUSystem(sys::FVM.FVMSystem{N}) where {N}
             i, j = m.bedges[1, e] + 1, m.bedges[2, e] + 1
             fidx = FVM.get_neumann_fidx(sys, i, j, r)
             f = (x, y, t, u) -> FVM.eval_condition_fnc(sys, fidx, r, x, y, t, u)
-            es, cs = classify_system(f, quarter[1, 2e-1:2e], quarter[2, 2e-1:2e], t0, N; maxdeg = 1,
+            es, cs = classify_system(f, quarter[1, (2*e-1):(2*e)], quarter[2, (2*e-1):(2*e)], t0, N; maxdeg = 1,
                 what = "Neumann function $(fidx) of component $(r)")
             for (k, ek) in enumerate(es)
                 slot = sum(ek) == 0 ? 1 : 1 + findfirst(!iszero, ek)
-                qn[slot, 2e-1:2e, r] .= cs[k, :]
+                qn[slot, (2*e-1):(2*e), r] .= cs[k, :]
             end
         end
     end
@@ -499,6 +530,411 @@ function solve(gs::GPUSystem; saveat, dt = nothing, abstol = 1e-6, reltol = 1e-3
         (Ptr{Cvoid}, Ptr{Float64}, Ref{OdeOptions}, Ptr{Float64}, Ref{OdeStats}, Ptr{Cvoid}),
         gs.handle, u0, opt, out, st, C_NULL))
     return ts, [out[:, :, k] for k in eachindex(ts)]
+end
+
+# ---- templates (src/specific_problems/) ----------------------------------------------------
+mutable struct GPUTemplate{T}
+    tmpl::T
+    mesh::GPUMesh
+    problem::Ptr{Cvoid}   # the conditions carrier (FVM_PROBLEM_CONDITIONS_ONLY)
+    handle::Ptr{Cvoid}
+    keep::Vector{Any}
+end
+
+template_kind(::FVM.DiffusionEquation) = FVM_TEMPLATE_DIFFUSION
+template_kind(::FVM.LinearReactionDiffusionEquation) = FVM_TEMPLATE_LINEAR_REACTION_DIFFUSION
+template_kind(::FVM.PoissonsEquation) = FVM_TEMPLATE_POISSON
+template_kind(::FVM.MeanExitTimeProblem) = FVM_TEMPLATE_MEAN_EXIT_TIME
+
+"""
+    GPUTemplate(tmpl)
+
+A `DiffusionEquation`, `LinearReactionDiffusionEquation`, `PoissonsEquation` or
+`MeanExitTimeProblem` assembled on the device (`fvm_template_create`): D(x, y, p) sampled at the
+dual-edge midpoints and boundary quarter points, the conditions evaluated with t = u = nothing
+(src/specific_problems/abstract_templates.jl), the source (Poisson's f, the reaction
+coefficient) at the vertices.
+"""
+function GPUTemplate(tmpl::FVM.AbstractFVMTemplate)
+    m = GPUMesh(tmpl.mesh)
+    tri = tmpl.mesh.triangulation
+    conds = tmpl.conditions
+    np = m.npoints
+    kind = template_kind(tmpl)
+    code = vertex_codes(tri, conds, np)
+    neu = neumann_flags(conds, m)
+    dual, quarter = sample_points(m)
+    D, Dp = tmpl.diffusion_function, tmpl.diffusion_parameters
+    dualD = Float64[D(dual[1, k], dual[2, k], Dp) for k in axes(dual, 2)]
+    quarterD = Float64[D(quarter[1, k], quarter[2, k], Dp) for k in axes(quarter, 2)]
+    qn = zeros(size(quarter, 2))
+    for e in 1:size(m.bedges, 2)
+        neu[e] == 1 || continue
+        fidx = FVM.get_neumann_fidx(conds, m.bedges[1, e] + 1, m.bedges[2, e] + 1)
+        for k in (2 * e - 1, 2 * e)
+            qn[k] = Float64(FVM.eval_condition_fnc(conds, fidx, quarter[1, k], quarter[2, k], nothing, nothing))
+        end
+    end
+    dudt = zeros(np)
+    dir = zeros(np)
+    for i in 1:np
+        (code[i] == FVM_VERTEX_DUDT || code[i] == FVM_VERTEX_DIRICHLET) || continue
+        x, y = DT.getxy(DT.get_point(tri, i))
+        isdudt = code[i] == FVM_VERTEX_DUDT
+        fidx = isdudt ? FVM.get_dudt_fidx(conds, i) : FVM.get_dirichlet_fidx(conds, i)
+        v = Float64(FVM.eval_condition_fnc(conds, fidx, x, y, nothing, nothing))
+        isdudt ? (dudt[i] = v) : (dir[i] = v)
+    end
+    src = zeros(0)
+    sdeg = Int32(0)
+    if kind == FVM_TEMPLATE_POISSON || kind == FVM_TEMPLATE_LINEAR_REACTION_DIFFUSION
+        S, Sp = tmpl.source_function, tmpl.source_parameters
+        sv = Float64[S(DT.getxy(DT.get_point(tri, i))..., Sp) for i in 1:np]
+        if kind == FVM_TEMPLATE_LINEAR_REACTION_DIFFUSION  # the reaction coefficient: source c1 u
+            src = vec(permutedims(hcat(zeros(np), sv)))
+            sdeg = Int32(1)
+        else
+            src = sv
+        end
+    end
+    keep = Any[code, neu, dualD, quarterD, qn, src, dudt, dir]
+    nbe = size(m.bedges, 2)
+    pf(a, use) = use ? pointer(a) : Ptr{Float64}(C_NULL)
+    desc = ProblemDesc(pointer(code), nbe > 0 ? pointer(neu) : Ptr{Int8}(C_NULL), Int32(0), pointer(dualD),
+        pf(quarterD, nbe > 0), Int32(0), pf(qn, any(==(1), neu)), sdeg, pf(src, !isempty(src)), Int32(0), pointer(dudt),
+        pointer(dir), Int32(0), Ptr{Float64}(C_NULL), Ptr{Float64}(C_NULL), Int32(0), Ptr{Float64}(C_NULL),
+        Ptr{Float64}(C_NULL), Ptr{Float64}(C_NULL), Ptr{Float64}(C_NULL), Ptr{Float64}(C_NULL),
+        FVM_PROBLEM_CONDITIONS_ONLY)
+    hp = Ref{Ptr{Cvoid}}(C_NULL)
+    GC.@preserve keep check(ccall((:fvm_problem_create, libfvmgpu), Cint,
+        (Ptr{Cvoid}, Ref{ProblemDesc}, Ref{Ptr{Cvoid}}), m.handle, desc, hp))
+    ht = Ref{Ptr{Cvoid}}(C_NULL)
+    st = ccall((:fvm_template_create, libfvmgpu), Cint, (Ptr{Cvoid}, Int32, Ref{Ptr{Cvoid}}), hp[], kind, ht)
+    if st != FVM_OK
+        msg = last_error()
+        ccall((:fvm_problem_destroy, libfvmgpu), Cint, (Ptr{Cvoid},), hp[])
+        error("libfvmgpu status $(st): $(msg)")
+    end
+    gt = GPUTemplate(tmpl, m, hp[], ht[], keep)
+    finalizer(gt) do x
+        ccall((:fvm_template_destroy, libfvmgpu), Cint, (Ptr{Cvoid},), x.handle)
+        ccall((:fvm_problem_destroy, libfvmgpu), Cint, (Ptr{Cvoid},), x.problem)
+    end
+    return gt
+end
+
+"""
+    apply!(du, u, gt::GPUTemplate; precision = :fp64)
+
+du = A u + b, the template's MatrixOperator product (diffusion_equation.jl:93-94); vectors of
+length npoints.
+"""
+function apply!(du::Vector{Float64}, u::Vector{Float64}, gt::GPUTemplate; precision = :fp64)
+    check(ccall((:fvm_template_apply, libfvmgpu), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Int32, Int32, Ptr{Cvoid}),
+        gt.handle, u, du, precision == :fp32 ? Int32(1) : Int32(0), FVM_PTR_HOST, C_NULL))
+    return du
+end
+
+"""
+    export_operator(gt::GPUTemplate) -> (A::SparseMatrixCSC-ready (rowptr, col, val), b)
+
+A in CSR (0-based, caller numbering, sorted columns) and b, as assembled on the device.
+"""
+function export_operator(gt::GPUTemplate)
+    nnz = Ref{Int64}(0)
+    check(ccall((:fvm_template_export, libfvmgpu), Cint,
+        (Ptr{Cvoid}, Ref{Int64}, Ptr{Int32}, Ptr{Int32}, Ptr{Float64}, Ptr{Float64}),
+        gt.handle, nnz, C_NULL, C_NULL, C_NULL, C_NULL))
+    np = gt.mesh.npoints
+    rowptr = Vector{Int32}(undef, np + 1)
+    col = Vector{Int32}(undef, nnz[])
+    val = Vector{Float64}(undef, nnz[])
+    b = Vector{Float64}(undef, np)
+    check(ccall((:fvm_template_export, libfvmgpu), Cint,
+        (Ptr{Cvoid}, Ref{Int64}, Ptr{Int32}, Ptr{Int32}, Ptr{Float64}, Ptr{Float64}),
+        gt.handle, nnz, rowptr, col, val, b))
+    return (rowptr, col, val), b
+end
+
+"""
+    solve(gt::GPUTemplate; saveat, dt = nothing, abstol = 1e-6, reltol = 1e-3)
+
+Tsit5 on du/dt = A u + b of a `DiffusionEquation` / `LinearReactionDiffusionEquation`.  Returns
+`(t, u)` with `u[k]` of length npoints + 1, the reference's augmented state (last entry 1).
+"""
+function solve(gt::GPUTemplate; saveat, dt = nothing, abstol = 1e-6, reltol = 1e-3, max_steps = 0)
+    tmpl = gt.tmpl
+    t0, tf = tmpl.initial_time, tmpl.final_time
+    ts = saveat isa Number ? collect(t0:saveat:tf) : collect(Float64, saveat)
+    np = gt.mesh.npoints
+    out = Vector{Float64}(undef, np * length(ts))
+    u0 = collect(Float64, tmpl.initial_condition)[1:np]
+    opt = OdeOptions(t0, tf, dt === nothing ? 0.0 : dt, dt === nothing ? Int32(1) : Int32(0), abstol, reltol,
+        max_steps, pointer(ts), length(ts), Int32(1), Int32(0))
+    st = OdeStats(0, 0, 0, 0.0, 0.0, Int32(0))
+    GC.@preserve ts check(ccall((:fvm_template_tsit5_solve, libfvmgpu), Cint,
+        (Ptr{Cvoid}, Ptr{Float64}, Ref{OdeOptions}, Ptr{Float64}, Ref{OdeStats}, Ptr{Cvoid}),
+        gt.handle, u0, opt, out, st, C_NULL))
+    return ts, [vcat(out[(k-1)*np+1:k*np], 1.0) for k in eachindex(ts)]
+end
+
+# ---- steady solve (LinearProblem(A, b), poissons_equation.jl:81, mean_exit_time.jl:76) -----
+struct SolverOptions
+    rtol::Float64
+    max_iters::Int64
+    method::Int32
+    precond::Int32
+    cheb_degree::Int32
+    mode::Int32
+    inner_reduction::Float64
+end
+
+mutable struct SolverStats
+    iterations::Int64
+    refinements::Int64
+    rel_residual::Float64
+    elapsed_ms::Float64
+    method_used::Int32
+    symmetric::Int32
+    fallback_fp64::Int32
+end
+
+"""
+    GPUKrylov(; rtol = 1e-10, method = :auto, precond = :jacobi, cheb_degree = 4, mode = :fp64,
+              max_iters = 1_000_000, inner_reduction = 1e-3)
+
+The device steady solver, an algorithm for `solve(tmpl, GPUKrylov())` on a `PoissonsEquation` or
+`MeanExitTimeProblem` in place of a LinearSolve factorisation: CG (symmetric reduced operator)
+or BiCGStab, Jacobi or Chebyshev preconditioning, FP64 or mixed precision, stopped on the FP64
+residual ||b - A x|| / ||b|| <= rtol.
+"""
+Base.@kwdef struct GPUKrylov
+    rtol::Float64 = 1e-10
+    method::Symbol = :auto
+    precond::Symbol = :jacobi
+    cheb_degree::Int = 4
+    mode::Symbol = :fp64
+    max_iters::Int = 1_000_000
+    inner_reduction::Float64 = 1e-3
+end
+
+"""
+    steady_solve(gt::GPUTemplate, alg::GPUKrylov = GPUKrylov(); u0 = zeros) -> (x, stats)
+
+Solves A x = b of a Poisson or mean-exit-time template on the device.
+"""
+function steady_solve(gt::GPUTemplate, alg::GPUKrylov = GPUKrylov(); u0 = nothing)
+    np = gt.mesh.npoints
+    x = u0 === nothing ? zeros(np) : collect(Float64, u0)[1:np]
+    method = Dict(:auto => FVM_SOLVER_AUTO, :cg => FVM_SOLVER_CG, :bicgstab => FVM_SOLVER_BICGSTAB)[alg.method]
+    precond = Dict(:jacobi => FVM_PRECOND_JACOBI, :chebyshev => FVM_PRECOND_CHEBYSHEV)[alg.precond]
+    mode = Dict(:fp64 => FVM_SOLVE_FP64, :mixed => FVM_SOLVE_MIXED, :fp32_precond => FVM_SOLVE_FP32_PRECOND)[alg.mode]
+    opt = SolverOptions(alg.rtol, alg.max_iters, method, precond, Int32(alg.cheb_degree), mode, alg.inner_reduction)
+    st = SolverStats(0, 0, 0.0, 0.0, Int32(0), Int32(0), Int32(0))
+    status = ccall((:fvm_template_steady_solve, libfvmgpu), Cint,
+        (Ptr{Cvoid}, Ptr{Float64}, Ref{SolverOptions}, Ref{SolverStats}, Int32, Ptr{Cvoid}),
+        gt.handle, x, opt, st, FVM_PTR_HOST, C_NULL)
+    status == Cint(6) && @warn "steady solve stopped before rtol" st.rel_residual st.iterations
+    status == Cint(6) || check(status)
+    return x, st
+end
+
+"""
+    solve(tmpl::Union{PoissonsEquation, MeanExitTimeProblem}, alg::GPUKrylov)
+
+The steady template solved on the device in place of `solve(tmpl, KLUFactorization())`
+(src/specific_problems/abstract_templates.jl:58-60): a named tuple with `u` (the solution) and
+`stats`.
+"""
+function CommonSolve.solve(tmpl::Union{FVM.PoissonsEquation, FVM.MeanExitTimeProblem}, alg::GPUKrylov; kwargs...)
+    x, st = steady_solve(gpu_object(tmpl), alg)
+    return (u = x, stats = st)
+end
+
+# ---- batched instances (an EnsembleProblem over D on one mesh) ------------------------------
+mutable struct GPUBatch
+    gp::GPUProblem
+    handle::Ptr{Cvoid}
+    batch::Int
+end
+
+"""
+    GPUBatch(gp::GPUProblem, dualD::Matrix, quarterD::Matrix; precision = :fp64)
+
+`batch` instances of the linear problem `gp` that differ in their diffusion field: `dualD` is
+batch x (3 ntri) (the field at the dual-edge midpoints, `sample_points` order), `quarterD`
+batch x (2 nbedge) (or empty without boundary samples).  States are batch x npoints matrices
+(the library's [point][instance] memory).
+"""
+function GPUBatch(gp::GPUProblem, dualD::Matrix{Float64}, quarterD::Matrix{Float64}; precision = :fp64)
+    B = size(dualD, 1)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    dT = permutedims(dualD)   # [instance][sample] rows, each instance contiguous
+    qT = permutedims(quarterD)
+    GC.@preserve dT qT check(ccall((:fvm_batch_create, libfvmgpu), Cint,
+        (Ptr{Cvoid}, Int32, Ptr{Float64}, Ptr{Float64}, Int32, Ref{Ptr{Cvoid}}),
+        gp.handle, Int32(B), dT, isempty(qT) ? Ptr{Float64}(C_NULL) : pointer(qT),
+        precision == :fp32 ? Int32(1) : Int32(0), h))
+    gb = GPUBatch(gp, h[], B)
+    finalizer(gb) do x
+        ccall((:fvm_batch_destroy, libfvmgpu), Cint, (Ptr{Cvoid},), x.handle)
+    end
+    return gb
+end
+
+function fvm_eqs!(du::Matrix{Float64}, u::Matrix{Float64}, gb::GPUBatch, t)
+    check(ccall((:fvm_batch_rhs, libfvmgpu), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Float64, Int32, Ptr{Cvoid}),
+        gb.handle, u, du, t, FVM_PTR_HOST, C_NULL))
+    return du
+end
+
+"""
+    solve(gb::GPUBatch, u0::Matrix; dt, saveat)
+
+Fixed-step Tsit5 on every instance (u0 batch x npoints).  Returns `(t, u)`, `u[k]` batch x npoints.
+"""
+function solve(gb::GPUBatch, u0::Matrix{Float64}; dt, saveat)
+    prob = gb.gp.prob
+    t0, tf = prob.initial_time, prob.final_time
+    ts = saveat isa Number ? collect(t0:saveat:tf) : collect(Float64, saveat)
+    B, np = size(u0)
+    out = Array{Float64}(undef, B, np, length(ts))
+    opt = OdeOptions(t0, tf, dt, Int32(0), 1e-6, 1e-3, 0, pointer(ts), length(ts), Int32(1), Int32(0))
+    st = OdeStats(0, 0, 0, 0.0, 0.0, Int32(0))
+    GC.@preserve ts check(ccall((:fvm_batch_tsit5_solve, libfvmgpu), Cint,
+        (Ptr{Cvoid}, Ptr{Float64}, Ref{OdeOptions}, Ptr{Float64}, Ref{OdeStats}, Ptr{Cvoid}),
+        gb.handle, u0, opt, out, st, C_NULL))
+    return ts, [out[:, :, k] for k in eachindex(ts)]
+end
+
+# ---- discrete adjoint of the time templates ----------------------------------------------
+mutable struct AdjointStats
+    steps::Int64
+    checkpoints::Int64
+    rhs_evals::Int64
+    transpose_evals::Int64
+    forward_ms::Float64
+    reverse_ms::Float64
+end
+
+mutable struct GPUAdjoint
+    gt::GPUTemplate
+    handle::Ptr{Cvoid}
+    batch::Int
+end
+
+"""
+    GPUAdjoint(gt::GPUTemplate, batch)
+
+`batch` instances of a `DiffusionEquation` / `LinearReactionDiffusionEquation` template whose
+diffusion field is exp(theta) interpolated from per-vertex values theta (batch x npoints), for
+gradients of fixed-step Tsit5 solves by the discrete adjoint (`adjoint_solve` and its rrule).
+"""
+function GPUAdjoint(gt::GPUTemplate, batch::Integer)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:fvm_adjoint_create, libfvmgpu), Cint, (Ptr{Cvoid}, Int32, Ref{Ptr{Cvoid}}), gt.handle, Int32(batch), h))
+    ga = GPUAdjoint(gt, h[], Int(batch))
+    finalizer(ga) do x
+        ccall((:fvm_adjoint_destroy, libfvmgpu), Cint, (Ptr{Cvoid},), x.handle)
+    end
+    return ga
+end
+
+function set_log_diffusion!(ga::GPUAdjoint, theta::Matrix{Float64})
+    check(ccall((:fvm_adjoint_set_log_diffusion, libfvmgpu), Cint, (Ptr{Cvoid}, Ptr{Float64}, Int32, Ptr{Cvoid}),
+        ga.handle, theta, FVM_PTR_HOST, C_NULL))
+    return ga
+end
+
+"""
+    adjoint_solve(ga::GPUAdjoint, theta, u0, dt, nsteps) -> uT
+
+u(T) of every instance after `nsteps` Tsit5 steps of `dt` (theta, u0, uT: batch x npoints).
+Differentiable: `ChainRulesCore.rrule` runs the discrete adjoint on the device.
+"""
+function adjoint_solve(ga::GPUAdjoint, theta::Matrix{Float64}, u0::Matrix{Float64}, dt::Real, nsteps::Integer)
+    set_log_diffusion!(ga, theta)
+    uT = similar(u0)
+    check(ccall((:fvm_adjoint_forward, libfvmgpu), Cint,
+        (Ptr{Cvoid}, Ptr{Float64}, Float64, Int64, Ptr{Float64}, Int32, Ptr{Cvoid}),
+        ga.handle, u0, Float64(dt), Int64(nsteps), uT, FVM_PTR_HOST, C_NULL))
+    return uT
+end
+
+"""
+    adjoint_pullback(ga, theta, u0, dt, nsteps, uT_bar; checkpoint_every = 20) -> (theta_bar, u0_bar, stats)
+"""
+function adjoint_pullback(ga::GPUAdjoint, theta::Matrix{Float64}, u0::Matrix{Float64}, dt::Real, nsteps::Integer,
+                          uT_bar::AbstractMatrix; checkpoint_every::Integer = 20)
+    set_log_diffusion!(ga, theta)
+    tb = similar(theta)
+    ub = similar(u0)
+    ubar = Matrix{Float64}(uT_bar)
+    st = AdjointStats(0, 0, 0, 0, 0.0, 0.0)
+    check(ccall((:fvm_adjoint_pullback, libfvmgpu), Cint,
+        (Ptr{Cvoid}, Ptr{Float64}, Float64, Int64, Int32, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ref{AdjointStats},
+         Int32, Ptr{Cvoid}),
+        ga.handle, u0, Float64(dt), Int64(nsteps), Int32(checkpoint_every), ubar, tb, ub, st, FVM_PTR_HOST, C_NULL))
+    return tb, ub, st
+end
+
+function ChainRulesCore.rrule(::typeof(adjoint_solve), ga::GPUAdjoint, theta::Matrix{Float64}, u0::Matrix{Float64},
+                              dt::Real, nsteps::Integer)
+    uT = adjoint_solve(ga, theta, u0, dt, nsteps)
+    function adjoint_solve_pullback(uT_bar)
+        tb, ub, _ = adjoint_pullback(ga, theta, u0, dt, nsteps, ChainRulesCore.unthunk(uT_bar))
+        return ChainRulesCore.NoTangent(), ChainRulesCore.NoTangent(), tb, ub, ChainRulesCore.NoTangent(),
+               ChainRulesCore.NoTangent()
+    end
+    return uT, adjoint_solve_pullback
+end
+
+# ---- post-processing: point location and pl_interpolate for many points -------------------
+"""
+    locate(m::GPUMesh, xs, ys) -> Vector{Int}
+
+The (1-based) index, in `each_solid_triangle` order, of a triangle holding each point, 0 outside
+the mesh; the device counterpart of the tutorials' jump_and_march.
+"""
+function locate(m::GPUMesh, xs::AbstractVector, ys::AbstractVector)
+    xy = Vector{Float64}(undef, 2length(xs))
+    for q in eachindex(xs)
+        xy[2q-1], xy[2q] = xs[q], ys[q]
+    end
+    out = Vector{Int64}(undef, length(xs))
+    check(ccall((:fvm_mesh_locate, libfvmgpu), Cint, (Ptr{Cvoid}, Int64, Ptr{Float64}, Ptr{Int64}, Int32, Ptr{Cvoid}),
+        m.handle, Int64(length(xs)), xy, out, FVM_PTR_HOST, C_NULL))
+    return out .+ 1
+end
+
+"""
+    interpolate(m::GPUMesh, u, xs, ys) -> Vector{Float64}
+
+pl_interpolate (src/utils.jl:23-27) of the nodal values u at every point, NaN outside the mesh.
+"""
+function interpolate(m::GPUMesh, u::AbstractVector, xs::AbstractVector, ys::AbstractVector)
+    tri = locate(m, xs, ys) .- 1
+    xy = Vector{Float64}(undef, 2length(xs))
+    for q in eachindex(xs)
+        xy[2q-1], xy[2q] = xs[q], ys[q]
+    end
+    uu = collect(Float64, u)
+    out = Vector{Float64}(undef, length(xs))
+    check(ccall((:fvm_pl_interpolate, libfvmgpu), Cint,
+        (Ptr{Cvoid}, Ptr{Float64}, Int32, Int64, Ptr{Int64}, Ptr{Float64}, Ptr{Float64}, Int32, Ptr{Cvoid}),
+        m.handle, uu, Int32(1), Int64(length(xs)), tri, xy, out, FVM_PTR_HOST, C_NULL))
+    return out
+end
+
+# GPU objects of the reference's problems, built once per problem object (CommonSolve methods)
+const _CACHE = IdDict{Any, Any}()
+gpu_object(prob::FVM.FVMProblem) = get!(() -> GPUProblem(prob), _CACHE, prob)
+gpu_object(sys::FVM.FVMSystem) = get!(() -> GPUSystem(sys), _CACHE, sys)
+gpu_object(tmpl::FVM.AbstractFVMTemplate) = get!(() -> GPUTemplate(tmpl), _CACHE, tmpl)
+clear_gpu_cache!() = empty!(_CACHE)
+
+function __init__()
+    isfile(libfvmgpu) || @warn "libfvmgpu.so not found at $(libfvmgpu); build it (python -c 'import fvmgpu; fvmgpu.build()') or set FVMGPU_LIB"
 end
 
 end # module

@@ -114,7 +114,8 @@ def test_ctypes_structures_match_the_header_layout(tmp_path):
 
 JULIA = ROOT / "finitevolumemethod.jl_gb300" / "julia" / "FiniteVolumeMethodGPU" / "src" / "FiniteVolumeMethodGPU.jl"
 JULIA_STRUCTS = {"ProblemDesc": "fvm_problem_desc", "SystemDesc": "fvm_system_desc", "OdeOptions": "fvm_ode_options",
-                 "OdeStats": "fvm_ode_stats"}
+                 "OdeStats": "fvm_ode_stats", "SolverOptions": "fvm_solver_options", "SolverStats": "fvm_solver_stats",
+                 "AdjointStats": "fvm_adjoint_stats"}
 JULIA_SIZES = {"Int8": 1, "Int32": 4, "Cint": 4, "Int64": 8, "Float64": 8}
 
 
@@ -168,8 +169,8 @@ def _julia_type(c):
         return {"Ref{Ptr{Cvoid}}"}
     if c.endswith("*"):
         base = c[:-1]
-        if base in scalars:
-            return {f"Ptr{{{scalars[base]}}}"}
+        if base in scalars:  # an array, or one value written back through a Ref
+            return {f"Ptr{{{scalars[base]}}}", f"Ref{{{scalars[base]}}}"}
         if base in ("void", "fvm_mesh", "fvm_problem", "fvm_system", "fvm_template", "fvm_batch", "fvm_adjoint"):
             return {"Ptr{Cvoid}"}
         return {"Ref{" + {v: k for k, v in JULIA_STRUCTS.items()}[base] + "}"}  # a struct, passed by reference
@@ -182,7 +183,13 @@ def test_julia_ccalls_match_the_header_prototypes():
     protos = _c_prototypes()
     text = JULIA.read_text()
     calls = re.findall(r"ccall\(\(:(fvm_\w+), libfvmgpu\), Cint,\s*\(([^()]*(?:\([^()]*\)[^()]*)*)\)", text)
-    assert len(calls) >= 12
+    assert len(calls) >= 30
+    # every entry point a user of the reference needs is bound
+    bound = {name for name, _ in calls}
+    for name in ("fvm_template_create", "fvm_template_tsit5_solve", "fvm_template_steady_solve", "fvm_batch_create",
+                 "fvm_batch_tsit5_solve", "fvm_adjoint_forward", "fvm_adjoint_pullback", "fvm_mesh_locate",
+                 "fvm_pl_interpolate", "fvm_system_tsit5_solve", "fvm_tsit5_solve"):
+        assert name in bound, name
     for name, types in calls:
         jt = [t.strip() for t in re.split(r",(?![^{]*\})", types) if t.strip()]
         ct = protos[name]
