@@ -884,9 +884,11 @@ def run_adjoint(args, F, torch):
     adj.set_log_diffusion(theta)
     adj.loss_and_grad(u0, obs, dt, N, checkpoint_every=K)  # warm-up (autotune, first-touch)
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    _, _, _, st = adj.loss_and_grad(u0, obs, dt, N, checkpoint_every=K)
-    wall_b = time.perf_counter() - t0
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        t0 = time.perf_counter()
+        _, _, _, st = adj.loss_and_grad(u0, obs, dt, N, checkpoint_every=K)
+        wall_b = time.perf_counter() - t0
+    clocks = clk.summary()
     dev_b = st["forward_ms"] + st["reverse_ms"]
     one = F.AdjointProblem(tmpl, batch=1)
     one.set_log_diffusion(theta[:, :1].copy())
@@ -899,12 +901,41 @@ def run_adjoint(args, F, torch):
         wall_1 += time.perf_counter() - t0
         dev_1 += s1["forward_ms"] + s1["reverse_ms"]
     loop_dev = dev_1 / 4 * B
+    nnz = mesh.info()["operator_nnz"]
+    # FP64 issue ceiling: 2 DFMA per clock per SM at the sampled median SM clock
+    mhz = clocks["sm_mhz"] or 2070.0
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    ceiling = 2.0 * sms * mhz * 1e6
+    dfma_b = adjoint_dfma(tri.num_points, nnz, B, N, K)
+    dfma_1 = adjoint_dfma(tri.num_points, nnz, 1, N, K)
     return {"instances": B, "steps": N, "checkpoint_every": K, "checkpoints": st["checkpoints"],
             "rhs_evals": st["rhs_evals"], "transpose_evals": st["transpose_evals"],
             "batched_device_ms": dev_b, "batched_wall_ms": 1e3 * wall_b,
             "gradients_per_s": B / (dev_b / 1e3),
             "per_instance_loop_device_ms": loop_dev, "per_instance_loop_wall_ms": 1e3 * wall_1 / 4 * B,
-            "speedup_vs_per_instance_loop": loop_dev / dev_b}
+            "speedup_vs_per_instance_loop": loop_dev / dev_b,
+            "fp64_roofline": {"dfma_per_gradient_batch": dfma_b, "batched_dfma_per_s": dfma_b / (dev_b / 1e3),
+                              "batched_frac": dfma_b / (dev_b / 1e3) / ceiling,
+                              "loop_dfma_per_s": dfma_1 * B / (loop_dev / 1e3),
+                              "loop_frac": dfma_1 * B / (loop_dev / 1e3) / ceiling,
+                              "ceiling_dfma_per_s": ceiling, "sm_mhz": mhz, "sms": sms,
+                              "ceiling": "2 DFMA / clock / SM x SMs x median sampled SM clock"},
+            "clocks": clocks}
+
+
+def adjoint_dfma(npts, nnz, B, N, K):
+    """FP64 fused multiply-adds of one loss-and-gradient call (forward, checkpointed reverse):
+    one per operator entry and instance per product, one per term and element of each Tsit5
+    stage, cotangent and lambda combination, six per entry and instance for the gradient
+    accumulation G += sum_i kb_i (x) Y_i."""
+    n, E = npts * B, nnz * B
+    step_fwd = 6 * E + 21 * n  # six products; stage combinations 1 + 2 + 3 + 4 + 5 + 6 terms
+    fwd = E + n + N * step_fwd
+    recompute = sum(E + n + (min(N, s0 + K) - s0 - 1) * step_fwd for s0 in range(0, N, K) if min(N, s0 + K) - s0 > 1)
+    # per reverse step: 5 stage products + 15 stage terms; kb_5 (1 term); 6 transpose products;
+    # kb_4 .. kb_0 (2 + 3 + 4 + 5 + 6 terms); lambda (6 terms); gradient accumulation
+    step_rev = 5 * E + 15 * n + n + 6 * E + 20 * n + 6 * n + 6 * E
+    return int(fwd + recompute + N * step_rev)
 
 
 def main():

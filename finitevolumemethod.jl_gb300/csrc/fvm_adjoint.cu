@@ -245,26 +245,64 @@ void adj_rhs_t(fvm_adjoint* a, const double* w, double* out, cudaStream_t s) {
         batch_op_apply<double>(a->AT, w, out, s);
 }
 
-// One Tsit5 step in place: u <- u_{n+1}; k[0] holds f(u_n) on entry and f(u_{n+1}) on exit.
-void fwd_step(fvm_adjoint* a, double* u, double* const* k, double* Y, double h, int64_t n, cudaStream_t s) {
-    for (int i = 1; i < 6; ++i) {
-        LinComb L{};
-        L.nv = i;
-        for (int j = 0; j < i; ++j) {
-            L.v[j] = k[j];
-            L.c[j] = h * kA[i][j];
+// prod = A x (+ b), or A^T x (transpose), then z = x0 + sum_t c_t v_t with null v_t standing for
+// prod: on a batch one fused pass (the combination in the product's row epilogue, run while the
+// FP64 pipe works on the product), else the single-instance product and a separate pass.
+void op_then(fvm_adjoint* a, bool transpose, const double* x, double* prod, double* z, const double* x0,
+             const LinComb& L, int64_t n, cudaStream_t s) {
+    if (a->B > 1) {
+        BatchEpi<double> E;
+        E.z = z;
+        E.x0 = x0;
+        E.nv = L.nv;
+        for (int t = 0; t < L.nv; ++t) {
+            E.v[t] = L.v[t];
+            E.c[t] = L.c[t];
         }
-        lincomb(Y, u, L, n, s);
-        adj_rhs(a, Y, k[i], s);
+        batch_op_apply_epi<double>(transpose ? a->AT : a->A, x, prod, E, s);
+        return;
+    }
+    if (transpose)
+        adj_rhs_t(a, x, prod, s);
+    else
+        adj_rhs(a, x, prod, s);
+    LinComb M = L;
+    for (int t = 0; t < M.nv; ++t)
+        if (!M.v[t]) M.v[t] = prod;
+    lincomb(z, x0, M, n, s);
+}
+
+// Y_1 = u + h a_21 k_0, the first stage combination of a Tsit5 step
+void first_stage(double* Y1, const double* u, const double* k0, double h, int64_t n, cudaStream_t s) {
+    LinComb L{};
+    L.nv = 1;
+    L.v[0] = k0;
+    L.c[0] = h * kA[1][0];
+    lincomb(Y1, u, L, n, s);
+}
+
+// One Tsit5 step in place: u <- u_{n+1}.  On entry k[0] = f(u_n) and Y[0] = u_n + h a_21 k_0
+// (first_stage); on exit k[0] = f(u_{n+1}) and Y[0] = the next step's first stage.  Each stage
+// combination is formed in the epilogue of the product before it (Y alternates between Y[0]
+// and Y[1], as a product's input and its epilogue's output must differ).
+void fwd_step(fvm_adjoint* a, double* u, double* const* k, double* const* Y, double h, int64_t n, cudaStream_t s) {
+    for (int i = 1; i < 6; ++i) {
+        // k_i = f(Y_i); then Y_{i+1} = u + sum_{j<=i} h a_{i+1,j} k_j, or u_{n+1} after k_5
+        const int row = i + 1 < 6 ? i + 1 : 6;
+        LinComb L{};
+        L.nv = i + 1;
+        for (int j = 0; j <= i; ++j) {
+            L.v[j] = j < i ? k[j] : nullptr;
+            L.c[j] = h * kA[row][j];
+        }
+        double* z = i < 5 ? Y[i % 2] : u;
+        op_then(a, false, Y[(i - 1) % 2], k[i], z, u, L, n, s);
     }
     LinComb L{};
-    L.nv = 6;
-    for (int j = 0; j < 6; ++j) {
-        L.v[j] = k[j];
-        L.c[j] = h * kA[6][j];
-    }
-    lincomb(u, u, L, n, s);
-    adj_rhs(a, u, k[0], s);
+    L.nv = 1;
+    L.v[0] = nullptr;
+    L.c[0] = h * kA[1][0];
+    op_then(a, false, u, k[0], Y[0], u, L, n, s);  // FSAL k_0 = f(u_{n+1}), the next first stage
 }
 
 struct Timer {
@@ -348,7 +386,7 @@ void pullback_internal(fvm_adjoint* a, const double* u0, double dt, int64_t N, i
     const int64_t ncp = (N + K - 1) / K;
     const int64_t seglen = std::min<int64_t>(K, N);
     // workspace: u, k[7], Y, checkpoints, segment states, stage values/derivatives/cotangents, lambda, G
-    const int64_t nvec = 1 + 7 + 1 + ncp + seglen + 5 + 6 + 6 + 6 + 1;
+    const int64_t nvec = 1 + 7 + 2 + ncp + seglen + 5 + 6 + 6 + 6 + 1;
     DBuf ws, G;
     ws.alloc(8 * n * nvec);
     G.alloc(8 * a->nnz * B);
@@ -361,7 +399,9 @@ void pullback_internal(fvm_adjoint* a, const double* u0, double dt, int64_t N, i
     double* u = take(1);
     double* k[7];
     for (int j = 0; j < 7; ++j) k[j] = take(1);
-    double* Y = take(1);
+    double* Y[2];
+    Y[0] = take(1);
+    Y[1] = take(1);
     double* cps = take(ncp);
     double* seg = take(seglen);
     double* Ys[6];
@@ -379,6 +419,7 @@ void pullback_internal(fvm_adjoint* a, const double* u0, double dt, int64_t N, i
     FVM_CUDA(cudaEventRecord(tf.e0, s));
     FVM_CUDA(cudaMemcpyAsync(u, u0, 8 * n, cudaMemcpyDeviceToDevice, s));
     adj_rhs(a, u, k[0], s);
+    first_stage(Y[0], u, k[0], dt, n, s);
     ++nrhs;
     for (int64_t step = 0; step < N; ++step) {
         if (step % K == 0) FVM_CUDA(cudaMemcpyAsync(cps + (step / K) * n, u, 8 * n, cudaMemcpyDeviceToDevice, s));
@@ -415,6 +456,7 @@ void pullback_internal(fvm_adjoint* a, const double* u0, double dt, int64_t N, i
         FVM_CUDA(cudaMemcpyAsync(seg, cps + sg * n, 8 * n, cudaMemcpyDeviceToDevice, s));
         if (s1 - s0 > 1) {
             adj_rhs(a, seg, k[0], s);
+            first_stage(Y[0], seg, k[0], dt, n, s);
             ++nrhs;
         }
         for (int64_t j = 1; j < s1 - s0; ++j) {
@@ -424,34 +466,48 @@ void pullback_internal(fvm_adjoint* a, const double* u0, double dt, int64_t N, i
         }
         for (int64_t step = s1 - 1; step >= s0; --step) {
             const double* un = seg + (step - s0) * n;
-            // stages of this step: Y_1 = u_n, Y_i = u_n + h sum_{j<i} a_ij k_j, k_i = A Y_i + b
+            // stages of this step: Y_1 = u_n, Y_i = u_n + h sum_{j<i} a_ij k_j, k_i = A Y_i + b;
+            // each Y_{i+1} is formed in the epilogue of k_i's product (k_6 forms no later stage)
             const double* Yi[6];
             Yi[0] = un;
-            adj_rhs(a, un, ks[0], s);
-            for (int i = 1; i < 6; ++i) {
+            for (int i = 0; i < 5; ++i) {
                 LinComb L{};
-                L.nv = i;
-                for (int j = 0; j < i; ++j) {
-                    L.v[j] = ks[j];
-                    L.c[j] = dt * kA[i][j];
+                L.nv = i + 1;
+                for (int j = 0; j <= i; ++j) {
+                    L.v[j] = j < i ? ks[j] : nullptr;
+                    L.c[j] = dt * kA[i + 1][j];
                 }
-                lincomb(Ys[i], un, L, n, s);
-                Yi[i] = Ys[i];
-                if (i < 5) adj_rhs(a, Ys[i], ks[i], s);  // k_6 itself forms no later stage
+                op_then(a, false, Yi[i], ks[i], Ys[i + 1], un, L, n, s);
+                Yi[i + 1] = Ys[i + 1];
             }
             nrhs += 5;
-            // reverse through the stages
+            // reverse through the stages: kb_i = h b_i lambda + sum_{j>i} h a_ji Yb_j, Yb_i = A^T kb_i;
+            // kb_{i-1} is formed in the epilogue of Yb_i's product, and lambda += sum_i Yb_i in Yb_0's
+            {
+                LinComb L{};
+                L.nv = 1;
+                L.v[0] = lam;
+                L.c[0] = dt * kA[6][5];
+                lincomb(kb[5], nullptr, L, n, s);
+            }
             for (int i = 5; i >= 0; --i) {
                 LinComb L{};
-                L.nv = 0;
-                L.v[L.nv] = lam;
-                L.c[L.nv++] = dt * kA[6][i];
-                for (int j = i + 1; j < 6; ++j) {
-                    L.v[L.nv] = Yb[j];
-                    L.c[L.nv++] = dt * kA[j][i];
+                if (i > 0) {
+                    const int m = i - 1;
+                    L.v[L.nv] = lam;
+                    L.c[L.nv++] = dt * kA[6][m];
+                    for (int j = m + 1; j < 6; ++j) {
+                        L.v[L.nv] = j == i ? nullptr : Yb[j];
+                        L.c[L.nv++] = dt * kA[j][m];
+                    }
+                    op_then(a, true, kb[i], Yb[i], kb[m], nullptr, L, n, s);
+                } else {
+                    for (int j = 0; j < 6; ++j) {
+                        L.v[L.nv] = j == 0 ? nullptr : Yb[j];
+                        L.c[L.nv++] = 1.0;
+                    }
+                    op_then(a, true, kb[0], Yb[0], lam, lam, L, n, s);
                 }
-                lincomb(kb[i], nullptr, L, n, s);
-                adj_rhs_t(a, kb[i], Yb[i], s);
                 ++nadj;
             }
             StagePair P{};
@@ -461,13 +517,6 @@ void pullback_internal(fvm_adjoint* a, const double* u0, double dt, int64_t N, i
                 P.Y[i] = Yi[i];
             }
             launch_grad_accum(a, P, G.as<double>(), s);
-            LinComb L{};
-            L.nv = 6;
-            for (int i = 0; i < 6; ++i) {
-                L.v[i] = Yb[i];
-                L.c[i] = 1.0;
-            }
-            lincomb(lam, lam, L, n, s);
         }
     }
     FVM_CUDA(cudaGetLastError());
@@ -731,13 +780,14 @@ int fvm_adjoint_forward(fvm_adjoint* a, const double* u0, double dt, int64_t nst
         Io io(a, flags, s);
         const int64_t n = io.n;
         DBuf w;
-        w.alloc(8 * n * 9);
+        w.alloc(8 * n * 10);
         double* u = w.as<double>();
         double* k[7];
         for (int j = 0; j < 7; ++j) k[j] = u + (1 + j) * n;
-        double* Y = u + 8 * n;
+        double* Y[2] = {u + 8 * n, u + 9 * n};
         io.in(u0, u);
         adj_rhs(a, u, k[0], s);
+        first_stage(Y[0], u, k[0], dt, n, s);
         for (int64_t step = 0; step < nsteps; ++step) fwd_step(a, u, k, Y, dt, n, s);
         io.out(u, uT);
         FVM_CUDA(cudaStreamSynchronize(s));

@@ -86,12 +86,14 @@ __device__ __forceinline__ void vstore(T* p, const T (&x)[VEC]) {
 
 // du[r][b] = sum_k val[k][b] u[col_k][b] + bvec[r] + q[r] u[r][b]^2 over the chunk of instances
 // of each (row, chunk of 32 * VEC instances) work item; grid-stride over items (a persistent grid).
-template <class T, int VEC>
+// EPI: the row's linear combination E (BatchEpi) is formed from the fresh product in the same
+// pass; du may then be null (the product is not stored).
+template <class T, int VEC, bool EPI = false>
 __global__ void __launch_bounds__(512) batch_op_kernel(const int64_t* __restrict__ rowptr,
                                                        const int32_t* __restrict__ col, const T* __restrict__ val,
                                                        const T* __restrict__ u, T* __restrict__ du,
                                                        const T* __restrict__ bvec, const T* __restrict__ q, int64_t n,
-                                                       int B, int64_t nchunk) {
+                                                       int B, int64_t nchunk, BatchEpi<T> E = {}) {
     const int lane = threadIdx.x & 31;
     const int64_t nwarp = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t item = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; item < n * nchunk; item += nwarp) {
@@ -136,7 +138,29 @@ __global__ void __launch_bounds__(512) batch_op_kernel(const int64_t* __restrict
 #pragma unroll
             for (int j = 0; j < VEC; ++j) acc[j] += qq * ur[j] * ur[j];
         }
-        vstore<T, VEC>(du + r * B + b0, acc);
+        if (!EPI || du) vstore<T, VEC>(du + r * B + b0, acc);
+        if constexpr (EPI) {  // z = x0 + sum_t c_t v_t in list order, the fresh product where v_t is null
+            T z[VEC];
+            if (E.x0) {
+                vload<T, VEC>(E.x0 + r * B + b0, z);
+            } else {
+#pragma unroll
+                for (int j = 0; j < VEC; ++j) z[j] = 0;
+            }
+            for (int t = 0; t < E.nv; ++t) {
+                T v[VEC];
+                if (E.v[t]) {
+                    vload<T, VEC>(E.v[t] + r * B + b0, v);
+                } else {
+#pragma unroll
+                    for (int j = 0; j < VEC; ++j) v[j] = acc[j];
+                }
+                const T c = (T)E.c[t];
+#pragma unroll
+                for (int j = 0; j < VEC; ++j) z[j] += c * v[j];
+            }
+            vstore<T, VEC>(E.z + r * B + b0, z);
+        }
     }
 }
 
@@ -374,6 +398,28 @@ void batch_tsit5(fvm_batch* bt, T* u, T* work, int64_t nsteps, double dt, bool u
 }
 
 }  // namespace
+
+template <class T>
+void batch_op_apply_epi(BatchOp& op, const T* u, T* du, const BatchEpi<T>& E, cudaStream_t s) {
+    if (((uintptr_t)u | (uintptr_t)du | (uintptr_t)E.z) % sizeof(T))
+        fail(FVM_ERR_INVALID_ARGUMENT, "batched state arrays must be aligned to their element size");
+    if (!E.z || E.nv > 8) fail(FVM_ERR_INVALID_ARGUMENT, "bad batched epilogue");
+    autotune<T>(op, u, du ? du : E.z, s);
+    uintptr_t addr = (uintptr_t)u | (uintptr_t)E.z | (uintptr_t)E.x0 | (uintptr_t)du;
+    for (int t = 0; t < E.nv; ++t) addr |= (uintptr_t)E.v[t];
+    const int vec = std::min(op.vec, max_vec_for<T>((const void*)addr, (const void*)addr));
+    const int64_t chunk = 32 * (int64_t)vec;
+    const int64_t nchunk = (op.B + chunk - 1) / chunk;
+    const unsigned g = (unsigned)op.grid;
+    const T* val = (const T*)op.val;
+    const T* bv = (const T*)op.b;
+    const T* qv = (const T*)op.q;
+    if (vec == 2)
+        batch_op_kernel<T, 2, true><<<g, op.block, 0, s>>>(op.rowptr, op.col, val, u, du, bv, qv, op.np, op.B, nchunk, E);
+    else
+        batch_op_kernel<T, 1, true><<<g, op.block, 0, s>>>(op.rowptr, op.col, val, u, du, bv, qv, op.np, op.B, nchunk, E);
+}
+template void batch_op_apply_epi<double>(BatchOp&, const double*, double*, const BatchEpi<double>&, cudaStream_t);
 
 template <class T>
 void batch_op_apply(BatchOp& op, const T* u, T* du, cudaStream_t s) {

@@ -375,6 +375,20 @@ struct BatchOp {
 };
 template <class T>
 void batch_op_apply(BatchOp& op, const T* u, T* du, cudaStream_t s);
+// A row epilogue of the batched product: z = x0 + sum_t c_t v_t over [np][B] arrays, in list
+// order, where a null v_t stands for the product just formed (x0 may be null; z may alias x0
+// but not the product's input).
+template <class T>
+struct BatchEpi {
+    T* z = nullptr;
+    const T* x0 = nullptr;
+    const T* v[8] = {};
+    double c[8] = {};
+    int nv = 0;
+};
+// du = A u (+ b), and the epilogue E formed in the same pass (du may be null)
+template <class T>
+void batch_op_apply_epi(BatchOp& op, const T* u, T* du, const BatchEpi<T>& E, cudaStream_t s);
 // val[k][b] = cst[k] + sum_{m in [mptr[k], mptr[k+1])} mcoef[m] D[midx[m]][b]  (FP64 or FP32 val)
 void launch_batch_assemble(const int64_t* mptr, const int32_t* midx, const double* mcoef, const double* cst,
                            const double* D, void* val, int64_t nnz, int B, int precision, cudaStream_t s);
