@@ -1,0 +1,584 @@
+// Implicit time stepping on the device: the Jacobian-vector product of fvm_eqs! and TR-BDF2
+// with simplified Newton and matrix-free BiCGStab.
+//
+// The reference hands its ODEProblem, with jac_prototype = jacobian_sparsity(prob)
+// (src/solve.jl:50-131,167-183), to OrdinaryDiffEq's implicit solvers; its tutorials use TRBDF2
+// (docs/src/literate_tutorials/diffusion_equation_on_an_annulus.jl:64,
+// docs/src/tutorials/diffusion_equation_on_a_square_plate.md).  Here the Jacobian is never
+// formed: J(u) v is one launch (the operator itself on the linear path, the derivative of the
+// per-triangle kernel otherwise, fvm_kernels.cu), and each TR-BDF2 stage solves its Newton
+// systems W d = r, W = I - d h J(u_n), with BiCGStab preconditioned by diag(W).
+//
+// TR-BDF2 as in Hosea & Shampine, "Analysis and implementation of TR-BDF2", Appl. Numer. Math.
+// 20 (1996): gamma = 2 - sqrt 2, d = gamma / 2, w = sqrt 2 / 4, z = h f:
+//   trapezoidal stage to t + gamma h:  z_g = h f(u_n + d z_n + d z_g)
+//   BDF2 stage to t + h:              z_1 = h f(u_n + w z_n + w z_g + d z_1),
+//                                     u_{n+1} = u_n + w z_n + w z_g + d z_1
+//   error estimate (filtered by W):   est = W^-1 ((1 - sqrt 2)/3 z_n + 1/3 z_g + (sqrt 2 - 2)/3 z_1)
+// Step control: accept when RMS(est / (abstol + reltol max(|u_n|, |u_{n+1}|))) <= 1, and
+// h <- h min(10, max(0.2, 0.9 err^(-1/3))).  A stage whose Newton iteration does not converge
+// in 10 iterations (or diverges) retries the step with h / 4.  saveat values inside a step
+// are the cubic Hermite interpolant of (u_n, f_n), (u_{n+1}, f_{n+1}).  The Dirichlet update
+// runs after every accepted step, as with Tsit5.
+#include "fvm_internal.h"
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+namespace fvm {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kParts = 304;  // blocks of the reductions (2 per SM): partials summed on the host in order
+
+inline unsigned blocks_for(int64_t n) { return (unsigned)std::max<int64_t>(1, (n + kThreads - 1) / kThreads); }
+
+// out = c0 x0 + c1 x1 + c2 x2 + c3 x3 (null terms skipped); out may alias an input
+struct Lin {
+    const double* x[4];
+    double c[4];
+};
+__global__ void lin_kernel(double* out, Lin L, int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double acc = 0.0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+        if (L.x[j]) acc += L.c[j] * L.x[j][i];
+    out[i] = acc;
+}
+void lin(double* out, const Lin& L, int64_t n, cudaStream_t s) {
+    lin_kernel<<<blocks_for(n), kThreads, 0, s>>>(out, L, n);
+}
+Lin lin2(const double* a, double ca, const double* b, double cb) {
+    Lin L{};
+    L.x[0] = a;
+    L.c[0] = ca;
+    L.x[1] = b;
+    L.c[1] = cb;
+    return L;
+}
+
+// two dot products per pass, partials per block: part[2 * b + k]
+__global__ void dot2_kernel(const double* a0, const double* b0, const double* a1, const double* b1, int64_t n,
+                            double* part) {
+    __shared__ double red[2][kThreads];
+    double s0 = 0.0, s1 = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        s0 += a0[i] * b0[i];
+        if (a1) s1 += a1[i] * b1[i];
+    }
+    red[0][threadIdx.x] = s0;
+    red[1][threadIdx.x] = s1;
+    __syncthreads();
+    for (int w = kThreads / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) {
+            red[0][threadIdx.x] += red[0][threadIdx.x + w];
+            red[1][threadIdx.x] += red[1][threadIdx.x + w];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        part[2 * blockIdx.x] = red[0][0];
+        part[2 * blockIdx.x + 1] = red[1][0];
+    }
+}
+
+// sum of (x / (abstol + reltol max(|a|, |b|)))^2, partials per block (b may be null)
+__global__ void wnorm_kernel(const double* x, const double* a, const double* b, double abstol, double reltol,
+                             int64_t n, double* part) {
+    __shared__ double red[kThreads];
+    double s = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double sc = abstol + reltol * (b ? fmax(fabs(a[i]), fabs(b[i])) : fabs(a[i]));
+        const double r = x[i] / sc;
+        s += r * r;
+    }
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = kThreads / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+// y = x / dw (Jacobi), dw = 1 - c diagJ
+__global__ void jacobi_kernel(const double* x, const double* dw, double* y, int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = x[i] / dw[i];
+}
+__global__ void wdiag_kernel(const double* dj, double c, double* dw, int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dw[i] = 1.0 - c * dj[i];
+}
+// the diagonal of a sliced-ELL operator: padding slots name the row itself with value 0
+template <class V>
+__global__ void sell_diag_kernel(const int64_t* slice_ptr, const int32_t* width, const int32_t* col, const V* val,
+                                 const double* rowscale, int64_t nrows, double* diag) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nrows) return;
+    const int64_t s = r / kSlice;
+    const int lane = (int)(r - s * kSlice);
+    double d = 0.0;
+    for (int k = 0; k < width[s]; ++k) {
+        const int64_t slot = slice_ptr[s] + (int64_t)k * kSlice + lane;
+        if (col[slot] == r) d += (double)val[slot];
+    }
+    diag[r] = rowscale ? d * rowscale[r] : d;
+}
+
+// Hermite interpolation of a saved value inside a step
+__global__ void hermite_kernel(double* out, const double* u0, const double* f0, const double* u1, const double* f1,
+                               double h, double th, int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double t2 = th * th, t3 = t2 * th;
+    const double h00 = 2 * t3 - 3 * t2 + 1, h10 = t3 - 2 * t2 + th, h01 = -2 * t3 + 3 * t2, h11 = t3 - t2;
+    out[i] = h00 * u0[i] + h10 * h * f0[i] + h01 * u1[i] + h11 * h * f1[i];
+}
+
+struct Reducer {
+    DBuf part;
+    std::vector<double> host;
+    Reducer() {
+        part.alloc(sizeof(double) * 2 * kParts);
+        host.resize(2 * kParts);
+    }
+    void fetch(int count, cudaStream_t s) {
+        FVM_CUDA(cudaMemcpyAsync(host.data(), part.p, sizeof(double) * count, cudaMemcpyDeviceToHost, s));
+        FVM_CUDA(cudaStreamSynchronize(s));
+    }
+    void dot2(const double* a0, const double* b0, const double* a1, const double* b1, int64_t n, double& r0,
+              double& r1, cudaStream_t s) {
+        dot2_kernel<<<kParts, kThreads, 0, s>>>(a0, b0, a1, b1, n, part.as<double>());
+        fetch(2 * kParts, s);
+        r0 = r1 = 0.0;
+        for (int b = 0; b < kParts; ++b) {
+            r0 += host[2 * b];
+            r1 += host[2 * b + 1];
+        }
+    }
+    double dot(const double* a, const double* b, int64_t n, cudaStream_t s) {
+        double r0, r1;
+        dot2(a, b, nullptr, nullptr, n, r0, r1, s);
+        return r0;
+    }
+    // RMS of x / (abstol + reltol max(|a|, |b|))
+    double wrms(const double* x, const double* a, const double* b, double abstol, double reltol, int64_t n,
+                cudaStream_t s) {
+        wnorm_kernel<<<kParts, kThreads, 0, s>>>(x, a, b, abstol, reltol, n, part.as<double>());
+        fetch(kParts, s);
+        double r = 0.0;
+        for (int k = 0; k < kParts; ++k) r += host[k];
+        return std::sqrt(r / (double)std::max<int64_t>(1, n));
+    }
+};
+
+}  // namespace
+
+// J(u) v in the internal numbering (the linear path: A v + 2 q u v; otherwise the derivative of
+// the per-triangle kernel)
+void problem_jvp_internal(fvm_problem* p, const double* u, const double* v, double* jv, cudaStream_t s) {
+    fvm_mesh* m = p->mesh;
+    if (p->conditions_only) fail(FVM_ERR_INVALID_ARGUMENT, "this problem carries a template's conditions only");
+    if (p->linear) {
+        if (p->precision == FVM_FP32) {
+            launch_to_f32(v, p->d_u32.as<float>(), m->np, s);
+            launch_sell_apply32(m->pat, p->d_val32.as<float>(), p->d_u32.as<float>(), v, jv,
+                                p->d_rowscale.as<double>(), nullptr, nullptr, s);
+        } else {
+            launch_sell_apply64(m->pat, p->d_val64.as<double>(), v, jv, nullptr, nullptr, nullptr, s);
+        }
+        if (p->has_q) launch_quad_jvp(p->d_q.as<double>(), u, v, nullptr, jv, m->np, s);
+    } else {
+        p->build_triangle_path();
+        launch_triangle_jvp(m, p, u, v, jv, false, s);
+    }
+}
+
+// diag J(u) in the internal numbering
+void problem_jacobian_diagonal_internal(fvm_problem* p, const double* u, double* dj, cudaStream_t s) {
+    fvm_mesh* m = p->mesh;
+    if (p->conditions_only) fail(FVM_ERR_INVALID_ARGUMENT, "this problem carries a template's conditions only");
+    if (p->linear) {
+        const SellPattern& pat = m->pat;
+        if (p->precision == FVM_FP32)
+            sell_diag_kernel<float><<<blocks_for(m->np), kThreads, 0, s>>>(
+                pat.d_slice_ptr.as<int64_t>(), pat.d_width.as<int32_t>(), pat.d_col.as<int32_t>(),
+                p->d_val32.as<float>(), p->d_rowscale.as<double>(), m->np, dj);
+        else
+            sell_diag_kernel<double><<<blocks_for(m->np), kThreads, 0, s>>>(
+                pat.d_slice_ptr.as<int64_t>(), pat.d_width.as<int32_t>(), pat.d_col.as<int32_t>(),
+                p->d_val64.as<double>(), nullptr, m->np, dj);
+        if (p->has_q) launch_quad_jvp(p->d_q.as<double>(), u, nullptr, dj, dj, m->np, s);
+    } else {
+        p->build_triangle_path();
+        launch_triangle_jvp(m, p, u, nullptr, dj, true, s);
+    }
+}
+
+namespace {
+
+constexpr double kSqrt2 = 1.4142135623730951;
+constexpr double kGamma = 2.0 - kSqrt2;
+constexpr double kD = kGamma / 2.0;
+constexpr double kW = kSqrt2 / 4.0;
+
+struct Trbdf2 {
+    fvm_problem* p;
+    int64_t n;
+    cudaStream_t s;
+    double abstol, reltol;
+    Reducer red;
+    DBuf buf;
+    double *u, *un, *fn, *f1, *zn, *zg, *z1, *base, *tmp, *dj, *dw, *est;
+    double *r, *rhat, *pv, *ph, *v, *sv, *sh, *t, *x;  // BiCGStab
+    int64_t nrhs = 0, newton = 0, krylov = 0, jvps = 0, newton_fail = 0;
+    double wd = 0;  // d h of the current W
+    const double* wu = nullptr;  // J's point
+
+    Trbdf2(fvm_problem* p_, int64_t n_, cudaStream_t s_, double at, double rt)
+        : p(p_), n(n_), s(s_), abstol(at), reltol(rt) {
+        constexpr int nv = 21;
+        buf.alloc(sizeof(double) * n * nv);
+        double* q = buf.as<double>();
+        double** slots[nv] = {&u, &un, &fn, &f1, &zn, &zg, &z1, &base, &tmp, &dj, &dw, &est,
+                              &r, &rhat, &pv, &ph, &v, &sv, &sh, &t, &x};
+        for (int k = 0; k < nv; ++k) *slots[k] = q + (int64_t)k * n;
+    }
+    void rhs(const double* y, double* out, double tt) {
+        problem_rhs_internal(p, y, out, false, s, false, tt);
+        ++nrhs;
+    }
+    void wmul(const double* xin, double* out) {  // out = xin - d h J(wu) xin
+        problem_jvp_internal(p, wu, xin, out, s);
+        ++jvps;
+        lin(out, lin2(xin, 1.0, out, -wd), n, s);
+    }
+    // W at u_n with d h: its diagonal for the preconditioner
+    void set_w(const double* at, double dh) {
+        wu = at;
+        wd = dh;
+        problem_jacobian_diagonal_internal(p, at, dj, s);
+        wdiag_kernel<<<blocks_for(n), kThreads, 0, s>>>(dj, dh, dw, n);
+    }
+    // x = W^-1 b by right-preconditioned BiCGStab to ||b - W x|| <= rtol ||b||; x starts at 0
+    bool solve(const double* b, double* xo, double rtol, int maxit) {
+        FVM_CUDA(cudaMemsetAsync(xo, 0, sizeof(double) * n, s));
+        FVM_CUDA(cudaMemcpyAsync(r, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+        FVM_CUDA(cudaMemcpyAsync(rhat, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+        FVM_CUDA(cudaMemsetAsync(pv, 0, sizeof(double) * n, s));
+        FVM_CUDA(cudaMemsetAsync(v, 0, sizeof(double) * n, s));
+        double rho, bb;
+        red.dot2(rhat, r, b, b, n, rho, bb, s);
+        const double bnorm = std::sqrt(bb);
+        if (!(bnorm > 0)) return true;
+        double alpha = 1.0, omega = 1.0, rho_prev = 1.0;
+        for (int it = 0; it < maxit; ++it) {
+            ++krylov;
+            if (it > 0) {
+                if (!(rho != 0.0) || !std::isfinite(rho)) return false;
+                const double beta = (rho / rho_prev) * (alpha / omega);
+                // p = r + beta (p - omega v)
+                Lin L{};
+                L.x[0] = r;
+                L.c[0] = 1.0;
+                L.x[1] = pv;
+                L.c[1] = beta;
+                L.x[2] = v;
+                L.c[2] = -beta * omega;
+                lin(pv, L, n, s);
+            } else {
+                FVM_CUDA(cudaMemcpyAsync(pv, r, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+            }
+            jacobi_kernel<<<blocks_for(n), kThreads, 0, s>>>(pv, dw, ph, n);
+            wmul(ph, v);
+            const double rv = red.dot(rhat, v, n, s);
+            if (!(rv != 0.0) || !std::isfinite(rv)) return false;
+            alpha = rho / rv;
+            lin(sv, lin2(r, 1.0, v, -alpha), n, s);  // s = r - alpha v
+            jacobi_kernel<<<blocks_for(n), kThreads, 0, s>>>(sv, dw, sh, n);
+            wmul(sh, t);
+            double ts, tt;
+            red.dot2(t, sv, t, t, n, ts, tt, s);
+            omega = tt > 0 ? ts / tt : 0.0;
+            // x += alpha ph + omega sh; r = s - omega t
+            Lin L{};
+            L.x[0] = xo;
+            L.c[0] = 1.0;
+            L.x[1] = ph;
+            L.c[1] = alpha;
+            L.x[2] = sh;
+            L.c[2] = omega;
+            lin(xo, L, n, s);
+            lin(r, lin2(sv, 1.0, t, -omega), n, s);
+            double rr;
+            rho_prev = rho;
+            red.dot2(rhat, r, r, r, n, rho, rr, s);
+            if (!std::isfinite(rr)) return false;
+            if (std::sqrt(rr) <= rtol * bnorm) return true;
+            if (!(omega != 0.0)) return false;
+        }
+        return false;
+    }
+    // z = h f(base + d z) by simplified Newton from the predictor already in z; exact_linear: one
+    // iteration solves an affine f to the Krylov tolerance
+    bool stage(double* z, double tt, double h, bool exact_linear) {
+        double prev = 0.0;
+        for (int it = 0; it < 10; ++it) {
+            ++newton;
+            lin(tmp, lin2(base, 1.0, z, kD), n, s);  // the stage's state
+            rhs(tmp, r, tt);
+            lin(r, lin2(r, h, z, -1.0), n, s);  // residual h f - z
+            FVM_CUDA(cudaMemcpyAsync(est, r, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+            if (!solve(est, x, 1e-10, 1000)) return false;
+            lin(z, lin2(z, 1.0, x, 1.0), n, s);
+            if (exact_linear) return true;
+            const double dn = red.wrms(x, u, nullptr, abstol, reltol, n, s);
+            if (!std::isfinite(dn)) return false;
+            if (dn <= 1e-10) return true;
+            if (it > 0) {
+                const double theta = dn / prev;
+                if (theta >= 1.0) return false;
+                if (theta / (1.0 - theta) * dn <= 1e-2) return true;
+            }
+            prev = dn;
+        }
+        return false;
+    }
+};
+
+}  // namespace
+}  // namespace fvm
+
+using namespace fvm;
+
+extern "C" {
+
+int fvm_jvp(fvm_problem* p, const double* u, const double* v, double* jv, double t, int32_t flags, void* stream) {
+    return guard_call([&] {
+        if (!p || !u || !v || !jv) fail(FVM_ERR_INVALID_ARGUMENT, "NULL argument");
+        (void)t;  // time factors enter constant terms only: J does not depend on t
+        const int32_t loc = flags & 3;
+        if (loc > FVM_PTR_DEVICE_INTERNAL) fail(FVM_ERR_INVALID_ARGUMENT, "bad pointer-location flag");
+        cudaStream_t s = (cudaStream_t)stream;
+        fvm_mesh* m = p->mesh;
+        const int64_t n = m->np;
+        if (loc == FVM_PTR_DEVICE_INTERNAL) {
+            problem_jvp_internal(p, u, v, jv, s);
+            FVM_CUDA(cudaGetLastError());
+            return FVM_OK;
+        }
+        DBuf w;
+        w.alloc(sizeof(double) * 4 * n);
+        double *ui = w.as<double>(), *vi = ui + n, *ji = ui + 2 * n, *st = ui + 3 * n;
+        auto in = [&](const double* src, double* dst) {
+            const double* from = src;
+            if (loc == FVM_PTR_HOST) {
+                FVM_CUDA(cudaMemcpyAsync(st, src, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+                from = st;
+            }
+            launch_permute_in(m->d_perm.as<int32_t>(), from, dst, n, s);
+        };
+        in(u, ui);
+        in(v, vi);
+        problem_jvp_internal(p, ui, vi, ji, s);
+        double* dst = loc == FVM_PTR_HOST ? st : jv;
+        launch_permute_out(m->d_perm.as<int32_t>(), ji, dst, n, s);
+        if (loc == FVM_PTR_HOST) FVM_CUDA(cudaMemcpyAsync(jv, st, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+        FVM_CUDA(cudaStreamSynchronize(s));
+        FVM_CUDA(cudaGetLastError());
+        return FVM_OK;
+    });
+}
+
+int fvm_jacobian_diagonal(fvm_problem* p, const double* u, double* diag, double t, int32_t flags, void* stream) {
+    return guard_call([&] {
+        if (!p || !u || !diag) fail(FVM_ERR_INVALID_ARGUMENT, "NULL argument");
+        (void)t;
+        const int32_t loc = flags & 3;
+        if (loc > FVM_PTR_DEVICE_INTERNAL) fail(FVM_ERR_INVALID_ARGUMENT, "bad pointer-location flag");
+        cudaStream_t s = (cudaStream_t)stream;
+        fvm_mesh* m = p->mesh;
+        const int64_t n = m->np;
+        if (loc == FVM_PTR_DEVICE_INTERNAL) {
+            problem_jacobian_diagonal_internal(p, u, diag, s);
+            FVM_CUDA(cudaGetLastError());
+            return FVM_OK;
+        }
+        DBuf w;
+        w.alloc(sizeof(double) * 3 * n);
+        double *ui = w.as<double>(), *di = ui + n, *st = ui + 2 * n;
+        const double* from = u;
+        if (loc == FVM_PTR_HOST) {
+            FVM_CUDA(cudaMemcpyAsync(st, u, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+            from = st;
+        }
+        launch_permute_in(m->d_perm.as<int32_t>(), from, ui, n, s);
+        problem_jacobian_diagonal_internal(p, ui, di, s);
+        double* dst = loc == FVM_PTR_HOST ? st : diag;
+        launch_permute_out(m->d_perm.as<int32_t>(), di, dst, n, s);
+        if (loc == FVM_PTR_HOST) FVM_CUDA(cudaMemcpyAsync(diag, st, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+        FVM_CUDA(cudaStreamSynchronize(s));
+        FVM_CUDA(cudaGetLastError());
+        return FVM_OK;
+    });
+}
+
+int fvm_trbdf2_solve(fvm_problem* p, const double* u0, const fvm_ode_options* o, double* out, fvm_ode_stats* st,
+                     fvm_implicit_stats* ist, void* stream) {
+    return guard_call([&] {
+        if (!p || !u0 || !o || !out) fail(FVM_ERR_INVALID_ARGUMENT, "NULL argument");
+        if (p->conditions_only) fail(FVM_ERR_INVALID_ARGUMENT, "this problem carries a template's conditions only");
+        if (!(o->tf > o->t0)) fail(FVM_ERR_INVALID_ARGUMENT, "final time must exceed the initial time");
+        if (!o->adaptive && !(o->dt > 0)) fail(FVM_ERR_INVALID_ARGUMENT, "dt must be positive for fixed steps");
+        cudaStream_t s = (cudaStream_t)stream;
+        fvm_mesh* m = p->mesh;
+        const int64_t n = m->np;
+        std::vector<double> saveat;
+        if (o->saveat && o->nsave > 0)
+            saveat.assign(o->saveat, o->saveat + o->nsave);
+        else
+            saveat.push_back(o->tf);
+        for (size_t i = 0; i < saveat.size(); ++i) {
+            if (saveat[i] < o->t0 || saveat[i] > o->tf) fail(FVM_ERR_INVALID_ARGUMENT, "saveat times must lie in [t0, tf]");
+            if (i && saveat[i] < saveat[i - 1]) fail(FVM_ERR_INVALID_ARGUMENT, "saveat must be sorted");
+        }
+        Trbdf2 M(p, n, s, o->abstol, o->reltol);
+        DBuf d_in, d_out;
+        d_in.alloc(sizeof(double) * n);
+        d_out.alloc(sizeof(double) * n * saveat.size());
+        FVM_CUDA(cudaMemcpyAsync(d_in.p, u0, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+        launch_permute_in(m->d_perm.as<int32_t>(), d_in.as<double>(), M.u, n, s);
+        double* outi = d_out.as<double>();
+        size_t si = 0;
+        auto save = [&](const double* src) {
+            FVM_CUDA(cudaMemcpyAsync(outi + si * n, src, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+            ++si;
+        };
+        double t = o->t0;
+        while (si < saveat.size() && saveat[si] == t) save(M.u);
+        cudaEvent_t e0, e1;
+        FVM_CUDA(cudaEventCreate(&e0));
+        FVM_CUDA(cudaEventCreate(&e1));
+        FVM_CUDA(cudaEventRecord(e0, s));
+        M.rhs(M.u, M.fn, t);
+        const double tspan = o->tf - o->t0;
+        // affine f with an exact product: one Newton iteration solves each stage
+        const bool exact_linear = p->linear && !p->has_q && p->precision != FVM_FP32;
+        double h = o->dt;
+        if (o->adaptive && !(h > 0)) {  // order-2 version of the Hairer-Wanner initial step
+            const double d0 = M.red.wrms(M.u, M.u, nullptr, o->abstol, o->reltol, n, s);
+            const double d1 = M.red.wrms(M.fn, M.u, nullptr, o->abstol, o->reltol, n, s);
+            const double h0 = (d0 < 1e-5 || d1 < 1e-5) ? 1e-6 : 0.01 * d0 / d1;
+            h = std::min(h0, tspan);
+        }
+        const int64_t max_steps = o->max_steps > 0 ? o->max_steps : 100000000;
+        int64_t nacc = 0, nrej = 0, step = 0;
+        bool first_cb = true;
+        while (t < o->tf) {
+            if (step >= max_steps) fail(FVM_ERR_STEP_LIMIT, "TRBDF2 reached max_steps before tf");
+            const bool last = t + h >= o->tf - 1e-12 * tspan;
+            const double hh = last ? o->tf - t : h;
+            ++step;
+            // z_n = h f_n; W = I - d h J(u_n)
+            lin(M.zn, lin2(M.fn, hh, nullptr, 0.0), n, s);
+            M.set_w(M.u, kD * hh);
+            // trapezoidal stage: base = u_n + d z_n, predictor z_g = z_n
+            lin(M.base, lin2(M.u, 1.0, M.zn, kD), n, s);
+            FVM_CUDA(cudaMemcpyAsync(M.zg, M.zn, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+            bool ok = M.stage(M.zg, t + kGamma * hh, hh, exact_linear);
+            if (ok) {  // BDF2 stage: base = u_n + w z_n + w z_g, predictor z_1 = z_g
+                Lin L{};
+                L.x[0] = M.u;
+                L.c[0] = 1.0;
+                L.x[1] = M.zn;
+                L.c[1] = kW;
+                L.x[2] = M.zg;
+                L.c[2] = kW;
+                lin(M.base, L, n, s);
+                FVM_CUDA(cudaMemcpyAsync(M.z1, M.zg, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+                ok = M.stage(M.z1, t + hh, hh, exact_linear);
+            }
+            if (!ok) {
+                ++M.newton_fail;
+                if (!o->adaptive) fail(FVM_ERR_STEP_LIMIT, "TRBDF2: the Newton iteration did not converge at the fixed dt");
+                h = hh / 4;
+                if (h < 1e-14 * std::max(1.0, std::fabs(t))) fail(FVM_ERR_STEP_LIMIT, "TRBDF2 step size underflow");
+                continue;
+            }
+            lin(M.un, lin2(M.base, 1.0, M.z1, kD), n, s);  // u_{n+1}
+            double err = 0.0;
+            if (o->adaptive) {
+                Lin L{};
+                L.x[0] = M.zn;
+                L.c[0] = (1.0 - kSqrt2) / 3.0;
+                L.x[1] = M.zg;
+                L.c[1] = 1.0 / 3.0;
+                L.x[2] = M.z1;
+                L.c[2] = (kSqrt2 - 2.0) / 3.0;
+                lin(M.tmp, L, n, s);
+                if (!M.solve(M.tmp, M.est, 1e-10, 1000)) fail(FVM_ERR_STEP_LIMIT, "TRBDF2: the error estimate's solve failed");
+                err = M.red.wrms(M.est, M.u, M.un, o->abstol, o->reltol, n, s);
+                if (!std::isfinite(err)) fail(FVM_ERR_STEP_LIMIT, "TRBDF2 error estimate is not finite");
+                if (err > 1.0) {
+                    ++nrej;
+                    h = hh * std::min(10.0, std::max(0.2, 0.9 * std::pow(err, -1.0 / 3.0)));
+                    if (h < 1e-14 * std::max(1.0, std::fabs(t))) fail(FVM_ERR_STEP_LIMIT, "TRBDF2 step size underflow");
+                    continue;
+                }
+            }
+            const double tn = last ? o->tf : t + hh;
+            // f at u_{n+1} (before the Dirichlet update) for the interpolant
+            M.rhs(M.un, M.f1, tn);
+            while (si < saveat.size() && saveat[si] < tn) {
+                const double th = (saveat[si] - t) / hh;
+                hermite_kernel<<<blocks_for(n), kThreads, 0, s>>>(outi + si * n, M.u, M.fn, M.un, M.f1, hh, th, n);
+                ++si;
+            }
+            std::swap(M.u, M.un);
+            std::swap(M.fn, M.f1);
+            t = tn;
+            ++nacc;
+            if (p->ndir > 0) {
+                problem_dirichlet_internal(p, M.u, t, s);
+                if (first_cb || p->tdir_varies) M.rhs(M.u, M.fn, t);
+                first_cb = false;
+            }
+            while (si < saveat.size() && saveat[si] == t) save(M.u);
+            if (o->adaptive) {
+                const double q = err > 0 ? 0.9 * std::pow(err, -1.0 / 3.0) : 10.0;
+                h = std::min(tspan, hh * std::min(10.0, std::max(0.2, q)));
+            }
+            if (last) break;
+        }
+        while (si < saveat.size()) save(M.u);
+        FVM_CUDA(cudaEventRecord(e1, s));
+        FVM_CUDA(cudaEventSynchronize(e1));
+        float ms = 0;
+        FVM_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        snapshots_to_host(m->d_iperm.as<int32_t>(), outi, out, n, (int64_t)saveat.size(), s);
+        FVM_CUDA(cudaStreamSynchronize(s));
+        FVM_CUDA(cudaGetLastError());
+        if (st) {
+            st->naccept = nacc;
+            st->nreject = nrej;
+            st->nrhs = M.nrhs;
+            st->t_final = t;
+            st->elapsed_ms = ms;
+            st->driver = FVM_DRIVER_HOST;
+        }
+        if (ist) {
+            ist->newton_iters = M.newton;
+            ist->krylov_iters = M.krylov;
+            ist->jvps = M.jvps;
+            ist->newton_failures = M.newton_fail;
+        }
+        return FVM_OK;
+    });
+}
+
+}  // extern "C"

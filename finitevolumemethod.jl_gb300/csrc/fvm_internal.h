@@ -295,6 +295,12 @@ struct AdaptState {
                                    // error, 4 device time limit
 };
 void launch_adapt_begin(AdaptState* st, cudaStream_t s);
+// Jacobian of fvm_eqs!: J(u) v on the per-triangle path (diag: diag J(u), v unused)
+void launch_triangle_jvp(const fvm_mesh* m, const fvm_problem* p, const double* u, const double* v, double* jv,
+                         bool diag, cudaStream_t s);
+// y += 2 q u v, or (diag non-null) y = diag + 2 q u
+void launch_quad_jvp(const double* q, const double* u, const double* v, const double* diag, double* y, int64_t n,
+                     cudaStream_t s);
 void launch_stage_dev(double* y, const double* u, const double* const* k, const double* a, int nk,
                       const AdaptState* st, int64_t n, cudaStream_t s);
 void launch_error_partial_dev(const double* u, const double* unew, const double* const* k, const double* bt,

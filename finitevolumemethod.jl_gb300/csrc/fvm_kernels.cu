@@ -392,6 +392,128 @@ __global__ void __launch_bounds__(256) triangle_rhs_kernel(TriArgs a) {
     }
 }
 
+// Derivative of a D polynomial c0 + c1 x + c2 x^2 at x.
+template <int DDEG>
+__device__ __forceinline__ double dpoly_prime(const double* c, int64_t stride, int64_t e, double x) {
+    if (DDEG == 0) return 0.0;
+    double r = __ldg(&c[stride + e]);
+    if (DDEG >= 2) r += 2.0 * x * __ldg(&c[2 * stride + e]);
+    return r;
+}
+
+// The derivative of fvm_eqs! on the per-triangle path.  JVP (DIAG false): du = J(u) v, with
+// each dual-edge flux Q = D(u_s) G(u) giving dQ = D'(u_s) (s . v) G(u) + D(u_s) G(v), u_s the
+// dual-edge midpoint value; the boundary and source terms likewise.  DIAG: du = diag J(u), the
+// derivative of each vertex's row with respect to its own value.  Same tiles and order as
+// triangle_rhs_kernel.
+template <int DDEG, bool DIAG>
+__global__ void __launch_bounds__(256) triangle_jvp_kernel(TriArgs a, const double* __restrict__ v) {
+    extern __shared__ double acc[];
+    const int64_t tile = blockIdx.x;
+    const int64_t v0 = tile * a.tv;
+    for (int i = threadIdx.x; i < a.tv; i += blockDim.x) acc[i] = 0.0;
+    __syncthreads();
+    const int64_t N = a.nelem;
+    const int64_t e0 = a.off[tile], e1 = a.off[tile + 1];
+    // dual-edge midpoint weights (in twelfths) of the corners a, b, c for edges 0, 1, 2
+    const double W[3][3] = {{5.0, 5.0, 2.0}, {2.0, 5.0, 5.0}, {5.0, 2.0, 5.0}};
+    for (int64_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+        const int32_t va = __ldg(&a.ev[e]), vb = __ldg(&a.ev[N + e]), vc = __ldg(&a.ev[2 * N + e]);
+        const double ua = __ldg(&a.u[va]), ub = __ldg(&a.u[vb]), uc = __ldg(&a.u[vc]);
+        double xa = 0, xb = 0, xc = 0;
+        if (!DIAG) {
+            xa = __ldg(&v[va]);
+            xb = __ldg(&v[vb]);
+            xc = __ldg(&v[vc]);
+        }
+        // dQ[d] (JVP), or dQ[d][corner] = dQ_d / du_corner (DIAG)
+        double dQ[3][3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const double* gc = DDEG == 0 ? a.ec : a.g;
+            const double g0 = __ldg(&gc[(2 * d) * N + e]), g1 = __ldg(&gc[(2 * d + 1) * N + e]);
+            const double dG[3] = {g0, g1, -g0 - g1};  // dG / d(ua, ub, uc)
+            if (DDEG == 0) {
+                if (DIAG) {
+                    for (int k = 0; k < 3; ++k) dQ[d][k] = dG[k];
+                } else {
+                    dQ[d][0] = g0 * (xa - xc) + g1 * (xb - xc);
+                }
+            } else {
+                const double G = g0 * (ua - uc) + g1 * (ub - uc);
+                const double us = (W[d][0] * ua + W[d][1] * ub + W[d][2] * uc) / 12.0;
+                const double* cd = a.ec + (int64_t)(d * (DDEG + 1)) * N;
+                const double D = dpoly<DDEG>(cd, N, e, us), Dp = dpoly_prime<DDEG>(cd, N, e, us);
+                if (DIAG) {
+                    for (int k = 0; k < 3; ++k) dQ[d][k] = Dp * (W[d][k] / 12.0) * G + D * dG[k];
+                } else {
+                    const double sv = (W[d][0] * xa + W[d][1] * xb + W[d][2] * xc) / 12.0;
+                    dQ[d][0] = Dp * sv * G + D * (g0 * (xa - xc) + g1 * (xb - xc));
+                }
+            }
+        }
+        const uint64_t la = (uint64_t)(va - v0), lb = (uint64_t)(vb - v0), lc = (uint64_t)(vc - v0);
+        if (DIAG) {  // row a gets Q2 - Q0, row b Q0 - Q1, row c Q1 - Q2
+            if (la < (uint64_t)a.tv) atomicAdd(&acc[la], dQ[2][0] - dQ[0][0]);
+            if (lb < (uint64_t)a.tv) atomicAdd(&acc[lb], dQ[0][1] - dQ[1][1]);
+            if (lc < (uint64_t)a.tv) atomicAdd(&acc[lc], dQ[1][2] - dQ[2][2]);
+        } else {
+            if (la < (uint64_t)a.tv) atomicAdd(&acc[la], dQ[2][0] - dQ[0][0]);
+            if (lb < (uint64_t)a.tv) atomicAdd(&acc[lb], dQ[0][0] - dQ[1][0]);
+            if (lc < (uint64_t)a.tv) atomicAdd(&acc[lc], dQ[1][0] - dQ[2][0]);
+        }
+    }
+    const int64_t NB = a.nbelem;
+    const int nd = DDEG + 1;
+    const int64_t b0 = a.boff[tile], b1 = a.boff[tile + 1];
+    for (int64_t e = b0 + threadIdx.x; e < b1; e += blockDim.x) {
+        const int32_t vi = a.bv[e], vj = a.bv[NB + e], vk = a.bv[2 * NB + e];
+        const double ui = a.u[vi], uj = a.u[vj], uk = a.u[vk];
+        const double umi = (3.0 * ui + uj) / 4.0, umj = (ui + 3.0 * uj) / 4.0;
+        const double lh = a.bg[2 * NB + e];
+        double xi = 0, xj = 0, xk = 0;
+        if (!DIAG) {
+            xi = v[vi];
+            xj = v[vj];
+            xk = v[vk];
+        }
+        const double dmi = DIAG ? 0.75 : (3.0 * xi + xj) / 4.0, dmj = DIAG ? 0.75 : (xi + 3.0 * xj) / 4.0;
+        double dQi, dQj;
+        if (a.bc[e] != 0.0) {  // Neumann q.n = n0 + n1 u(m) + n2 u(m)^2
+            const double* n = a.bc + (int64_t)(1 + 2 * nd) * NB;
+            dQi = (n[NB + e] + 2.0 * umi * n[2 * NB + e]) * dmi * lh;
+            dQj = (n[4 * NB + e] + 2.0 * umj * n[5 * NB + e]) * dmj * lh;
+        } else {
+            const double bg0 = a.bg[e], bg1 = a.bg[NB + e];
+            const double G = bg0 * (ui - uk) + bg1 * (uj - uk);
+            const double Gi = DIAG ? bg0 : bg0 * (xi - xk) + bg1 * (xj - xk);
+            const double Gj = DIAG ? bg1 : Gi;
+            dQi = dpoly_prime<DDEG>(a.bc + NB, NB, e, umi) * dmi * G + dpoly<DDEG>(a.bc + NB, NB, e, umi) * Gi;
+            dQj = dpoly_prime<DDEG>(a.bc + (int64_t)(1 + nd) * NB, NB, e, umj) * dmj * G +
+                  dpoly<DDEG>(a.bc + (int64_t)(1 + nd) * NB, NB, e, umj) * Gj;
+        }
+        const uint64_t li = (uint64_t)(vi - v0), lj = (uint64_t)(vj - v0);
+        if (li < (uint64_t)a.tv) atomicAdd(&acc[li], -dQi);
+        if (lj < (uint64_t)a.tv) atomicAdd(&acc[lj], -dQj);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < a.tv; i += blockDim.x) {
+        const int64_t vv = v0 + i;
+        if (vv >= a.np) break;
+        const int c = a.code[vv];
+        const double uu = a.u[vv];
+        const double xv = DIAG ? 1.0 : v[vv];
+        double r = 0.0;
+        if (c == FVM_VERTEX_FREE) {
+            r = acc[i] * a.invV[vv];
+            if (a.vsrc) r += (a.vsrc[a.np + vv] + 2.0 * uu * a.vsrc[2 * a.np + vv]) * xv;
+        } else if (c == FVM_VERTEX_DUDT) {
+            if (a.vdudt) r = (a.vdudt[a.np + vv] + 2.0 * uu * a.vdudt[2 * a.np + vv]) * xv;
+        }
+        a.du[vv] = r;
+    }
+}
+
 void launch_triangle_rhs(const fvm_mesh* m, const fvm_problem* p, const double* u, double* du, cudaStream_t s) {
     const Tiles& T = m->tiles;
     TriArgs a;
@@ -419,6 +541,62 @@ void launch_triangle_rhs(const fvm_mesh* m, const fvm_problem* p, const double* 
         case 1: triangle_rhs_kernel<1><<<(unsigned)T.ntiles, 256, smem, s>>>(a); break;
         default: triangle_rhs_kernel<2><<<(unsigned)T.ntiles, 256, smem, s>>>(a); break;
     }
+}
+
+void launch_triangle_jvp(const fvm_mesh* m, const fvm_problem* p, const double* u, const double* v, double* jv,
+                         bool diag, cudaStream_t s) {
+    const Tiles& T = m->tiles;
+    TriArgs a;
+    a.off = T.d_off.as<int64_t>();
+    a.boff = T.d_boff.as<int64_t>();
+    a.ev = T.d_ev.as<int32_t>();
+    a.g = T.d_g.as<double>();
+    a.ec = p->d_ec.as<double>();
+    a.bv = T.d_bv.as<int32_t>();
+    a.bg = T.d_bg.as<double>();
+    a.bc = p->d_bc.as<double>();
+    a.code = p->d_code.as<int8_t>();
+    a.invV = m->d_invV.as<double>();
+    a.vsrc = p->src.empty() ? nullptr : p->d_vsrc.as<double>();
+    a.vdudt = p->dudt.empty() ? nullptr : p->d_vdudt.as<double>();
+    a.u = u;
+    a.du = jv;
+    a.nelem = T.nelem;
+    a.nbelem = T.nbelem;
+    a.np = m->np;
+    a.tv = T.tile_vertices;
+    const size_t smem = sizeof(double) * T.tile_vertices;
+    const unsigned g = (unsigned)T.ntiles;
+    if (diag) {
+        switch (p->dif_deg) {
+            case 0: triangle_jvp_kernel<0, true><<<g, 256, smem, s>>>(a, v); break;
+            case 1: triangle_jvp_kernel<1, true><<<g, 256, smem, s>>>(a, v); break;
+            default: triangle_jvp_kernel<2, true><<<g, 256, smem, s>>>(a, v); break;
+        }
+    } else {
+        switch (p->dif_deg) {
+            case 0: triangle_jvp_kernel<0, false><<<g, 256, smem, s>>>(a, v); break;
+            case 1: triangle_jvp_kernel<1, false><<<g, 256, smem, s>>>(a, v); break;
+            default: triangle_jvp_kernel<2, false><<<g, 256, smem, s>>>(a, v); break;
+        }
+    }
+}
+
+// y += 2 q u v (the derivative of a quadratic diagonal term q u^2), or y = diag + 2 q u (DIAG)
+__global__ void quad_jvp_kernel(const double* __restrict__ q, const double* __restrict__ u,
+                                const double* __restrict__ v, const double* __restrict__ diag, double* __restrict__ y,
+                                int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double qq = q ? q[i] : 0.0;
+    if (diag)
+        y[i] = diag[i] + 2.0 * qq * u[i];
+    else
+        y[i] += 2.0 * qq * u[i] * v[i];
+}
+void launch_quad_jvp(const double* q, const double* u, const double* v, const double* diag, double* y, int64_t n,
+                     cudaStream_t s) {
+    if (n) quad_jvp_kernel<<<grid_for(n, 256), 256, 0, s>>>(q, u, v, diag, y, n);
 }
 
 // ---------------------------------------------------------------------------------------

@@ -128,6 +128,13 @@ class OdeStats(C.Structure):
     ]
 
 
+class ImplicitStats(C.Structure):
+    _fields_ = [
+        ("newton_iters", C.c_int64), ("krylov_iters", C.c_int64), ("jvps", C.c_int64),
+        ("newton_failures", C.c_int64),
+    ]
+
+
 class SolverOptions(C.Structure):
     _fields_ = [
         ("rtol", C.c_double), ("max_iters", C.c_int64), ("method", C.c_int32), ("precond", C.c_int32),
@@ -174,6 +181,10 @@ SIGNATURES = {
     "fvm_rhs_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_void_p]),
     "fvm_test_set_stream_waits": (C.c_int, [C.c_int64, C.c_int64]),
     "fvm_dirichlet_apply": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_int32, C.c_void_p]),
+    "fvm_jvp": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int32, C.c_void_p]),
+    "fvm_jacobian_diagonal": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int32, C.c_void_p]),
+    "fvm_trbdf2_solve": (C.c_int, [C.c_void_p, c_double_p, C.POINTER(OdeOptions), c_double_p, C.POINTER(OdeStats),
+                                   C.POINTER(ImplicitStats), C.c_void_p]),
     "fvm_tsit5_solve": (C.c_int, [C.c_void_p, c_double_p, C.POINTER(OdeOptions), c_double_p, C.POINTER(OdeStats),
                                   C.c_void_p]),
     "fvm_system_create": (C.c_int, [C.c_void_p, C.POINTER(SystemDesc), C.POINTER(C.c_void_p)]),

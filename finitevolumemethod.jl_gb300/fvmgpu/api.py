@@ -1423,6 +1423,42 @@ class Tsit5:
         return "Tsit5()"
 
 
+class TRBDF2:
+    """TR-BDF2 (the implicit method of the reference's tutorials), on the device: simplified
+    Newton per stage, matrix-free BiCGStab on W = I - d h J with the exact Jacobian-vector
+    product of fvm_eqs!, diag(W) as preconditioner; adaptive with TR-BDF2's error estimate
+    (dt given with adaptive=False: fixed steps).  FVMProblem only."""
+
+    def __repr__(self):
+        return "TRBDF2()"
+
+
+def jvp(prob, u, v, t=0.0, stream=None):
+    """J(u) v, the Jacobian-vector product of fvm_eqs! (exact for every device-coded form).
+    u, v host float64 arrays or CUDA tensors (caller numbering); returns J(u) v of their kind."""
+    prob = _prob_of(prob)
+    out = np.empty_like(u) if isinstance(u, np.ndarray) else u.new_empty(u.shape)
+    up, ul = _lib.array_pointer(u)
+    vp, vl = _lib.array_pointer(v)
+    op, ol = _lib.array_pointer(out)
+    if not (ul == vl == ol):
+        raise TypeError("u and v must both be host arrays or both device tensors")
+    s = stream if stream is not None else _lib.current_stream_handle()
+    check(load().fvm_jvp(prob.handle, up, vp, op, float(t), ul, s))
+    return out
+
+
+def jacobian_diagonal(prob, u, t=0.0, stream=None):
+    """diag J(u) of fvm_eqs! (the Jacobi preconditioner of a Newton-Krylov solve)."""
+    prob = _prob_of(prob)
+    out = np.empty_like(u) if isinstance(u, np.ndarray) else u.new_empty(u.shape)
+    up, ul = _lib.array_pointer(u)
+    op, _ = _lib.array_pointer(out)
+    s = stream if stream is not None else _lib.current_stream_handle()
+    check(load().fvm_jacobian_diagonal(prob.handle, up, op, float(t), ul, s))
+    return out
+
+
 @dataclass
 class KrylovSolver:
     """GPU steady solver: method "auto" (CG if symmetric, else BiCGStab), "cg", "bicgstab";
@@ -1547,6 +1583,16 @@ def solve(prob, alg=None, *, saveat=None, dt=None, adaptive=None, abstol=1e-6, r
     elif isinstance(prob, FVMSystem):
         check(lib.fvm_system_tsit5_solve(prob.handle, dptr(u0c), C.byref(o), dptr(out), C.byref(st), s))
         us = [row.T for row in out]  # (N, npoints) views: entry (j, i) is component j at node i
+    elif isinstance(alg, TRBDF2):
+        if not isinstance(prob, FVMProblem):
+            raise TypeError("TRBDF2 runs on an FVMProblem")
+        ist = _lib.ImplicitStats()
+        check(lib.fvm_trbdf2_solve(prob.handle, dptr(u0c), C.byref(o), dptr(out), C.byref(st), C.byref(ist), s))
+        us = list(out)
+        return ODESolution(ts, us, {"naccept": st.naccept, "nreject": st.nreject, "nrhs": st.nrhs,
+                                    "t_final": st.t_final, "elapsed_ms": st.elapsed_ms, "driver": "host",
+                                    "newton_iters": ist.newton_iters, "krylov_iters": ist.krylov_iters,
+                                    "jvps": ist.jvps, "newton_failures": ist.newton_failures})
     else:
         check(lib.fvm_tsit5_solve(prob.handle, dptr(u0c), C.byref(o), dptr(out), C.byref(st), s))
         us = list(out)  # rows of the one output array, not copies

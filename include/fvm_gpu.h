@@ -243,6 +243,28 @@ typedef struct fvm_ode_stats {
 int fvm_tsit5_solve(fvm_problem* prob, const double* u0, const fvm_ode_options* opt, double* out,
                     fvm_ode_stats* stats, void* stream);
 
+/* ---- implicit stepping (solve(prob, TRBDF2()), the solver of the reference's tutorials) --- */
+/* Jacobian-vector product of fvm_eqs! (the derivative that a Newton-Krylov solve of the
+ * reference's implicit methods needs, src/solve.jl:50-131 gives its sparsity): jv = J(u) v,
+ * exact for every device-coded form.  u, v, jv per flags (FVM_PTR_*). */
+int fvm_jvp(fvm_problem* prob, const double* u, const double* v, double* jv, double t, int32_t flags, void* stream);
+/* diag J(u), per flags (FVM_PTR_*). */
+int fvm_jacobian_diagonal(fvm_problem* prob, const double* u, double* diag, double t, int32_t flags, void* stream);
+typedef struct fvm_implicit_stats {
+    int64_t newton_iters;     /* simplified-Newton iterations over all stages */
+    int64_t krylov_iters;     /* BiCGStab iterations */
+    int64_t jvps;             /* Jacobian-vector products */
+    int64_t newton_failures;  /* steps retried with a quarter of the step after a Newton failure */
+} fvm_implicit_stats;
+/* TR-BDF2 (Hosea & Shampine 1996) on the problem, the Dirichlet update after every step:
+ * simplified Newton per stage with W = I - d h J(u_n) applied by fvm_jvp and solved by
+ * BiCGStab with the diagonal of W as preconditioner; adaptive with TR-BDF2's error estimate,
+ * or fixed dt.  Options, u0 and out as fvm_tsit5_solve (use_graph is ignored); istats may be
+ * NULL. */
+int fvm_trbdf2_solve(fvm_problem* prob, const double* u0, const fvm_ode_options* opt, double* out,
+                     fvm_ode_stats* stats, fvm_implicit_stats* istats, void* stream);
+
+
 /* ---- systems of equations (FVMSystem, src/problem.jl:190-365) ---------------------------
  * N coupled components on one mesh.  State is laid out [npoints][neq] (component fastest),
  * the memory order of the reference's N x npoints solution matrix (column-major), in the

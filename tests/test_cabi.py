@@ -73,6 +73,7 @@ STRUCTS = {  # C struct in include/fvm_gpu.h -> its ctypes mirror in fvmgpu/_lib
     "fvm_solver_options": "SolverOptions",
     "fvm_solver_stats": "SolverStats",
     "fvm_adjoint_stats": "AdjointStats",
+    "fvm_implicit_stats": "ImplicitStats",
 }
 
 

@@ -470,3 +470,24 @@ def test_oracle_system_time_dependent_values_converge_to_exact_solution():
         ex = np.stack([np.exp(-P[:, 0] - P[:, 1] - 0.15), np.exp(P[:, 0] + P[:, 1] + 0.15)])
         errs.append(max(np.max(np.abs(ref[-1][c] - ex[c])) / np.max(ex[c]) for c in range(2)))
     assert errs[1] < 0.5 * errs[0] < 1e-2, errs
+
+
+def test_oracle_trbdf2_is_second_order():
+    """The oracle's TR-BDF2 with fixed steps on a linear problem: halving dt divides the error
+    at t = 0.05 (against a tight Tsit5 solution) by about 4."""
+    from problems import oracle_problem, sine_diffusion
+
+    spec = sine_diffusion(12)
+    prob = oracle_problem(spec)
+    f = lambda u, t: O.fvm_eqs(prob, u, t)  # noqa: E731
+    ent, n = O.jacobian_sparsity(spec.tri)
+    J = O.colored_jacobian(f, spec.u0, 0.0, ent, n, affine=True)
+    cb = lambda u, t: O.update_dirichlet_nodes(prob, u, t)  # noqa: E731
+    ref, _ = O.tsit5_solve(f, spec.u0, 0.0, 0.05, [0.05], abstol=1e-12, reltol=1e-12, callback=cb)
+    errs = []
+    for dt in (5e-3, 2.5e-3, 1.25e-3):
+        sol, st = O.trbdf2_solve(f, lambda u, t: J, spec.u0, 0.0, 0.05, [0.05], dt=dt, adaptive=False,
+                                 callback=cb, affine=True)
+        errs.append(np.max(np.abs(sol[-1] - ref[-1])))
+    r1, r2 = errs[0] / errs[1], errs[1] / errs[2]
+    assert 3.5 < r1 < 4.5 and 3.5 < r2 < 4.5, (errs, r1, r2)
