@@ -427,7 +427,7 @@ def run_gpu(args):
 
 
 EXTRA_ROWS = ("rhs_fp32", "rhs_fp64_conservative", "rhs_triangle_fp64", "tsit5_1000_steps", "template_spmv",
-              "c1_readme", "batched_c4", "multimesh_c4", "adjoint_c5", "system_gray_scott", "steady")
+              "c1_readme", "batched_c4", "multimesh_c4", "adjoint_c5", "system_gray_scott", "steady", "implicit")
 
 
 def _kernel_row(F, torch, fn, K, flush, units, alg_bytes, peak, profile=None):
@@ -509,7 +509,7 @@ def run_selected(args, F, torch, tri, mesh, prob, flush, u_int, peak):
             "template_spmv": template_spmv, "batched_c4": lambda: run_batched(args, F, torch, flush, peak),
             "multimesh_c4": lambda: run_multimesh(args, F, torch), "adjoint_c5": lambda: run_adjoint(args, F, torch),
             "system_gray_scott": lambda: run_system(args, F, torch, flush, mesh),
-            "steady": lambda: run_steady(args, F)}
+            "steady": lambda: run_steady(args, F), "implicit": lambda: run_implicit(F, prob)}
     for name in EXTRA_ROWS:
         if name not in want:
             continue
@@ -518,7 +518,7 @@ def run_selected(args, F, torch, tri, mesh, prob, flush, u_int, peak):
         except Exception as e:  # noqa: BLE001
             out = {"error": repr(e)[:300]}
         log(f"[bench] {name}: {json.dumps(out)}")
-        if name in ("system_gray_scott", "steady", "batched_c4") and "error" not in out:
+        if name in ("system_gray_scott", "steady", "batched_c4", "implicit") and "error" not in out:
             for sub, d in out.items():
                 emit_row(f"{name}.{sub}", d)
         else:
@@ -921,6 +921,46 @@ def run_adjoint(args, F, torch):
                               "ceiling_dfma_per_s": ceiling, "sm_mhz": mhz, "sms": sms,
                               "ceiling": "2 DFMA / clock / SM x SMs x median sampled SM clock"},
             "clocks": clocks}
+
+
+def run_implicit(F, c2_prob):
+    """Implicit stepping (TR-BDF2 with the device JVP and matrix-free BiCGStab).  (1) The annulus
+    tutorial (polar lattice stand-in, 2,304 vertices, time-dependent inner value, to t = 2,
+    saveat 0.2) at the default tolerances: TR-BDF2 against Tsit5, which steps at its stability
+    limit there.  (2) C2 (the 1M-vertex FVMProblem): 10 fixed TR-BDF2 steps of 1e-5, 100 times
+    the 1000-step Tsit5 row's dt."""
+    out = {}
+    tri = F.triangulate_annulus(0.2, 1.0, 24, 96, nsegments=1)
+    x, y = tri.points[:, 0], tri.points[:, 1]
+    u0 = (10 * np.exp(-25 * ((x + 0.5) ** 2 + (y + 0.5) ** 2)) - 5 * np.exp(-50 * ((x + 0.3) ** 2 + (y + 0.5) ** 2))
+          - 10 * np.exp(-45 * ((x - 0.5) ** 2 + (y - 0.5) ** 2)))
+    mesh = F.FVMGeometry(tri)
+    BCs = F.BoundaryConditions(mesh, (lambda x, y, t, u, p: 0.0 * x, lambda x, y, t, u, p: 50 * (1 - np.exp(-t / 2)) + 0.0 * x),
+                               (F.Neumann, F.Dirichlet))
+    prob = F.FVMProblem(mesh, BCs, diffusion_function=lambda x, y, t, u, p: 1.0 + 0.0 * x, initial_condition=u0,
+                        final_time=2.0)
+    F.solve(prob, F.TRBDF2(), saveat=0.2)  # warm-up
+    t0 = time.perf_counter()
+    imp = F.solve(prob, F.TRBDF2(), saveat=0.2)
+    wall_i = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    exp_ = F.solve(prob, F.Tsit5(), saveat=0.2)
+    wall_e = time.perf_counter() - t0
+    out["annulus_tutorial"] = {"vertices": tri.num_points, "trbdf2_steps": imp.stats["naccept"],
+                               "trbdf2_rejected": imp.stats["nreject"], "newton_iters": imp.stats["newton_iters"],
+                               "krylov_iters": imp.stats["krylov_iters"], "trbdf2_wall_ms": 1e3 * wall_i,
+                               "trbdf2_device_ms": imp.stats["elapsed_ms"], "tsit5_steps": exp_.stats["naccept"],
+                               "tsit5_wall_ms": 1e3 * wall_e, "tsit5_device_ms": exp_.stats["elapsed_ms"],
+                               "max_rel_diff": float(np.max(np.abs(np.array(imp.u) - np.array(exp_.u)))
+                                                     / np.max(np.abs(exp_.u)))}
+    p = c2_prob  # final time 1e-4: ten steps of 1e-5
+    sol = F.solve(p, F.TRBDF2(), dt=1e-5, adaptive=False, saveat=[p.final_time])
+    out["c2_fixed_dt_1e-5"] = {"steps": sol.stats["naccept"], "device_ms": sol.stats["elapsed_ms"],
+                               "ms_per_step": sol.stats["elapsed_ms"] / max(1, sol.stats["naccept"]),
+                               "newton_iters": sol.stats["newton_iters"], "krylov_iters": sol.stats["krylov_iters"],
+                               "jvps": sol.stats["jvps"],
+                               "krylov_iters_per_stage": sol.stats["krylov_iters"] / max(1, sol.stats["newton_iters"])}
+    return out
 
 
 def adjoint_dfma(npts, nnz, B, N, K):

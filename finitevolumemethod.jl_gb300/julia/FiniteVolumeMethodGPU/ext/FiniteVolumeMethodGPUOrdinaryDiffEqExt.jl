@@ -1,5 +1,5 @@
 """
-The reference's `solve(prob, Tsit5(); saveat, ...)` (src/solve.jl:197-220;
+The reference's `solve(prob, Tsit5(); saveat, ...)` and `solve(prob, TRBDF2(...))` (src/solve.jl:197-220;
 src/specific_problems/abstract_templates.jl:58-60) on the GPU: methods of `CommonSolve.solve`
 for an `FVMProblem`, an `FVMSystem` and the time-dependent templates with OrdinaryDiffEq's
 `Tsit5`, more specific than the reference's own, so an unchanged script that loads
@@ -12,7 +12,7 @@ module FiniteVolumeMethodGPUOrdinaryDiffEqExt
 
 using FiniteVolumeMethodGPU
 using FiniteVolumeMethod
-using OrdinaryDiffEq: Tsit5
+using OrdinaryDiffEq: Tsit5, TRBDF2
 import CommonSolve
 import SciMLBase
 
@@ -37,6 +37,16 @@ function gpu_tsit5(prob, alg; saveat = nothing, dt = nothing, adaptive = true, a
 end
 
 CommonSolve.solve(prob::FVM.FVMProblem, alg::Tsit5; kwargs...) = gpu_tsit5(prob, alg; kwargs...)
+
+# TRBDF2 (the tutorials' implicit method, whatever linsolve it names): the device's TR-BDF2
+function CommonSolve.solve(prob::FVM.FVMProblem, alg::TRBDF2; saveat = nothing, dt = nothing, adaptive = true,
+                           abstol = 1e-6, reltol = 1e-3, maxiters = 0, kwargs...)
+    g = G.gpu_object(prob)
+    fixed = dt !== nothing && !adaptive
+    ts, us, _ = G.solve_trbdf2(g; saveat = save_times(prob, saveat), dt = fixed ? dt : nothing, abstol, reltol,
+                               max_steps = maxiters)
+    return gpu_solution(alg, ts, us)
+end
 CommonSolve.solve(sys::FVM.FVMSystem, alg::Tsit5; kwargs...) = gpu_tsit5(sys, alg; kwargs...)
 CommonSolve.solve(tmpl::FVM.DiffusionEquation, alg::Tsit5; kwargs...) = gpu_tsit5(tmpl, alg; kwargs...)
 CommonSolve.solve(tmpl::FVM.LinearReactionDiffusionEquation, alg::Tsit5; kwargs...) = gpu_tsit5(tmpl, alg; kwargs...)

@@ -34,7 +34,7 @@ const FVM = FiniteVolumeMethod
 const DT = DelaunayTriangulation
 
 export GPUProblem, GPUSystem, GPUTemplate, GPUBatch, GPUAdjoint, GPUKrylov, adjoint_solve, adjoint_pullback,
-    set_log_diffusion!, locate, interpolate, steady_solve
+    set_log_diffusion!, locate, interpolate, steady_solve, jvp!, solve_trbdf2
 
 const libfvmgpu = get(ENV, "FVMGPU_LIB", joinpath(@__DIR__, "..", "..", "..", "fvmgpu", "_lib", "libfvmgpu.so"))
 
@@ -303,6 +303,51 @@ function solve(gp::GPUProblem; saveat, dt = nothing, abstol = 1e-6, reltol = 1e-
         (Ptr{Cvoid}, Ptr{Float64}, Ref{OdeOptions}, Ptr{Float64}, Ref{OdeStats}, Ptr{Cvoid}),
         gp.handle, u0, opt, out, st, C_NULL))
     return ts, [out[(k-1)*np+1:k*np] for k in eachindex(ts)]
+end
+
+# ---- implicit stepping: TR-BDF2 with the device Jacobian-vector product ---------------------
+mutable struct ImplicitStats
+    newton_iters::Int64
+    krylov_iters::Int64
+    jvps::Int64
+    newton_failures::Int64
+end
+
+"""
+    jvp!(jv, u, v, gp::GPUProblem, t)
+
+J(u) v, the Jacobian-vector product of `fvm_eqs!` (exact for every device-coded form): what a
+Newton-Krylov solve of the reference's implicit methods needs (src/solve.jl:50-131 gives J's
+sparsity).
+"""
+function jvp!(jv::Vector{Float64}, u::Vector{Float64}, v::Vector{Float64}, gp::GPUProblem, t)
+    check(ccall((:fvm_jvp, libfvmgpu), Cint,
+        (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Float64, Int32, Ptr{Cvoid}),
+        gp.handle, u, v, jv, t, FVM_PTR_HOST, C_NULL))
+    return jv
+end
+
+"""
+    solve_trbdf2(gp::GPUProblem; saveat, dt = nothing, abstol = 1e-6, reltol = 1e-3)
+
+TR-BDF2 on the device (simplified Newton, matrix-free BiCGStab on I - d h J): the reference
+tutorials' `solve(prob, TRBDF2(linsolve = KLUFactorization()))`.  Returns `(t, u, stats)`.
+"""
+function solve_trbdf2(gp::GPUProblem; saveat, dt = nothing, abstol = 1e-6, reltol = 1e-3, max_steps = 0)
+    prob = gp.prob
+    t0, tf = prob.initial_time, prob.final_time
+    ts = saveat isa Number ? collect(t0:saveat:tf) : collect(Float64, saveat)
+    np = gp.mesh.npoints
+    out = Vector{Float64}(undef, np * length(ts))
+    u0 = collect(Float64, prob.initial_condition)
+    opt = OdeOptions(t0, tf, dt === nothing ? 0.0 : dt, dt === nothing ? Int32(1) : Int32(0), abstol, reltol,
+        max_steps, pointer(ts), length(ts), Int32(0), Int32(0))
+    st = OdeStats(0, 0, 0, 0.0, 0.0, Int32(0))
+    ist = ImplicitStats(0, 0, 0, 0)
+    GC.@preserve ts check(ccall((:fvm_trbdf2_solve, libfvmgpu), Cint,
+        (Ptr{Cvoid}, Ptr{Float64}, Ref{OdeOptions}, Ptr{Float64}, Ref{OdeStats}, Ref{ImplicitStats}, Ptr{Cvoid}),
+        gp.handle, u0, opt, out, st, ist, C_NULL))
+    return ts, [out[(k-1)*np+1:k*np] for k in eachindex(ts)], ist
 end
 
 # ---- systems: FVMSystem(prob1, ..., probN) (src/problem.jl:190-365) -----------------------
