@@ -128,6 +128,107 @@ __global__ void sell_diag_kernel(const int64_t* slice_ptr, const int32_t* width,
     diag[r] = rowscale ? d * rowscale[r] : d;
 }
 
+// BiCGStab with its scalars in device memory: each dot product's block partials are summed in a
+// fixed order by one finalize kernel, which also updates the scalars; the vector kernels read
+// them, and every kernel does nothing once `status` is set (1 converged, 2 breakdown), so the
+// host checks only every few iterations.
+struct KDev {
+    double rho, rho_prev, alpha, omega, bb, tol2, rr;
+    int32_t status, it;
+};
+// the two sums of the partials part[2 b + k] over the blocks, by a fixed tree over one block of
+// kFin threads (deterministic); valid in thread 0
+constexpr int kFin = 512;
+static_assert(kParts <= kFin, "one finalize thread per partial");
+__device__ void sum_parts2(const double* part, double& s0, double& s1) {
+    __shared__ double a[kFin], b[kFin];
+    const int t = threadIdx.x;
+    a[t] = t < kParts ? part[2 * t] : 0.0;
+    b[t] = t < kParts ? part[2 * t + 1] : 0.0;
+    __syncthreads();
+    for (int w = kFin / 2; w > 0; w >>= 1) {
+        if (t < w) {
+            a[t] += a[t + w];
+            b[t] += b[t + w];
+        }
+        __syncthreads();
+    }
+    s0 = a[0];
+    s1 = b[0];
+}
+__global__ void kd_init_kernel(KDev* kd, const double* part, double tol2) {
+    double s0, s1;
+    sum_parts2(part, s0, s1);
+    if (threadIdx.x) return;
+    kd->rho = s0;
+    kd->bb = s1;
+    kd->tol2 = tol2;
+    kd->rho_prev = kd->alpha = kd->omega = 1.0;
+    kd->rr = kd->bb;
+    kd->it = 0;
+    kd->status = kd->bb > 0.0 ? 0 : 1;
+}
+// p = r (first iteration) or p = r + beta (p - omega v), beta = (rho / rho_prev)(alpha / omega)
+__global__ void kd_p_kernel(const KDev* kd, const double* r, double* p, const double* v, int64_t n) {
+    if (kd->status) return;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (kd->it == 0) {
+        p[i] = r[i];
+    } else {
+        const double beta = (kd->rho / kd->rho_prev) * (kd->alpha / kd->omega);
+        p[i] = r[i] + beta * (p[i] - kd->omega * v[i]);
+    }
+}
+__global__ void kd_alpha_kernel(KDev* kd, const double* part) {
+    if (kd->status) return;  // uniform over the block: status changes only after the sums
+    double rv, unused;
+    sum_parts2(part, rv, unused);
+    if (threadIdx.x) return;
+    if (!(rv != 0.0) || !isfinite(rv)) {
+        kd->status = 2;
+        return;
+    }
+    kd->alpha = kd->rho / rv;
+}
+__global__ void kd_s_kernel(const KDev* kd, const double* r, const double* v, double* s, int64_t n) {
+    if (kd->status) return;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) s[i] = r[i] - kd->alpha * v[i];
+}
+__global__ void kd_omega_kernel(KDev* kd, const double* part) {
+    if (kd->status) return;
+    double ts, tt;
+    sum_parts2(part, ts, tt);
+    if (threadIdx.x) return;
+    kd->omega = tt > 0.0 ? ts / tt : 0.0;
+}
+// x += alpha ph + omega sh; r = s - omega t
+__global__ void kd_xr_kernel(const KDev* kd, double* x, const double* ph, const double* sh, const double* s,
+                             const double* t, double* r, int64_t n) {
+    if (kd->status) return;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    x[i] = x[i] + kd->alpha * ph[i] + kd->omega * sh[i];
+    r[i] = s[i] - kd->omega * t[i];
+}
+__global__ void kd_rho_kernel(KDev* kd, const double* part) {
+    if (kd->status) return;
+    double rho, rr;
+    sum_parts2(part, rho, rr);
+    if (threadIdx.x) return;
+    kd->rho_prev = kd->rho;
+    kd->rho = rho;
+    kd->rr = rr;
+    kd->it += 1;
+    if (!isfinite(kd->rr))
+        kd->status = 2;
+    else if (kd->rr <= kd->tol2 * kd->bb)
+        kd->status = 1;
+    else if (!(kd->omega != 0.0) || !(kd->rho != 0.0))
+        kd->status = 2;
+}
+
 // Hermite interpolation of a saved value inside a step
 __global__ void hermite_kernel(double* out, const double* u0, const double* f0, const double* u1, const double* f1,
                                double h, double th, int64_t n) {
@@ -246,82 +347,98 @@ struct Trbdf2 {
         double** slots[nv] = {&u, &un, &fn, &f1, &zn, &zg, &z1, &base, &tmp, &dj, &dw, &est,
                               &r, &rhat, &pv, &ph, &v, &sv, &sh, &t, &x};
         for (int k = 0; k < nv; ++k) *slots[k] = q + (int64_t)k * n;
+        kdev.alloc(sizeof(KDev));
     }
     void rhs(const double* y, double* out, double tt) {
         problem_rhs_internal(p, y, out, false, s, false, tt);
         ++nrhs;
     }
-    void wmul(const double* xin, double* out) {  // out = xin - d h J(wu) xin
+    void wmul(const double* xin, double* out) {  // out = xin - d h J(wu) xin (two per BiCGStab iteration)
         problem_jvp_internal(p, wu, xin, out, s);
-        ++jvps;
         lin(out, lin2(xin, 1.0, out, -wd), n, s);
     }
-    // W at u_n with d h: its diagonal for the preconditioner
+    // W at u_n with d h: its diagonal for the preconditioner; the captured iteration chunk of
+    // the previous W is dropped
     void set_w(const double* at, double dh) {
+        drop_chunk();
         wu = at;
         wd = dh;
         problem_jacobian_diagonal_internal(p, at, dj, s);
         wdiag_kernel<<<blocks_for(n), kThreads, 0, s>>>(dj, dh, dw, n);
     }
-    // x = W^-1 b by right-preconditioned BiCGStab to ||b - W x|| <= rtol ||b||; x starts at 0
+    // x = W^-1 b by right-preconditioned BiCGStab to ||b - W x|| <= rtol ||b||; x starts at 0.
+    // The iterations run without host round trips; the host reads the scalars every kCheck.
+    static constexpr int kCheck = 8;
     bool solve(const double* b, double* xo, double rtol, int maxit) {
         FVM_CUDA(cudaMemsetAsync(xo, 0, sizeof(double) * n, s));
         FVM_CUDA(cudaMemcpyAsync(r, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
         FVM_CUDA(cudaMemcpyAsync(rhat, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
         FVM_CUDA(cudaMemsetAsync(pv, 0, sizeof(double) * n, s));
         FVM_CUDA(cudaMemsetAsync(v, 0, sizeof(double) * n, s));
-        double rho, bb;
-        red.dot2(rhat, r, b, b, n, rho, bb, s);
-        const double bnorm = std::sqrt(bb);
-        if (!(bnorm > 0)) return true;
-        double alpha = 1.0, omega = 1.0, rho_prev = 1.0;
-        for (int it = 0; it < maxit; ++it) {
-            ++krylov;
-            if (it > 0) {
-                if (!(rho != 0.0) || !std::isfinite(rho)) return false;
-                const double beta = (rho / rho_prev) * (alpha / omega);
-                // p = r + beta (p - omega v)
-                Lin L{};
-                L.x[0] = r;
-                L.c[0] = 1.0;
-                L.x[1] = pv;
-                L.c[1] = beta;
-                L.x[2] = v;
-                L.c[2] = -beta * omega;
-                lin(pv, L, n, s);
-            } else {
-                FVM_CUDA(cudaMemcpyAsync(pv, r, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+        KDev* kd = kdev.as<KDev>();
+        double* part = red.part.as<double>();
+        dot2_kernel<<<kParts, kThreads, 0, s>>>(rhat, r, b, b, n, part);
+        kd_init_kernel<<<1, kFin, 0, s>>>(kd, part, rtol * rtol);
+        if (xo != x) fail(FVM_ERR_INVALID_ARGUMENT, "the captured Krylov chunk writes the solver's x");
+        if (!chunk) capture_chunk();
+        for (int done = 0; done < maxit; done += kCheck) {
+            FVM_CUDA(cudaGraphLaunch(chunk, s));
+            KDev h{};
+            FVM_CUDA(cudaMemcpyAsync(&h, kd, sizeof h, cudaMemcpyDeviceToHost, s));
+            FVM_CUDA(cudaStreamSynchronize(s));
+            krylov += h.it - (int64_t)done_its;
+            jvps += 2 * (h.it - (int64_t)done_its);
+            done_its = h.it;
+            if (h.status == 1) {
+                done_its = 0;
+                return true;
             }
-            jacobi_kernel<<<blocks_for(n), kThreads, 0, s>>>(pv, dw, ph, n);
-            wmul(ph, v);
-            const double rv = red.dot(rhat, v, n, s);
-            if (!(rv != 0.0) || !std::isfinite(rv)) return false;
-            alpha = rho / rv;
-            lin(sv, lin2(r, 1.0, v, -alpha), n, s);  // s = r - alpha v
-            jacobi_kernel<<<blocks_for(n), kThreads, 0, s>>>(sv, dw, sh, n);
-            wmul(sh, t);
-            double ts, tt;
-            red.dot2(t, sv, t, t, n, ts, tt, s);
-            omega = tt > 0 ? ts / tt : 0.0;
-            // x += alpha ph + omega sh; r = s - omega t
-            Lin L{};
-            L.x[0] = xo;
-            L.c[0] = 1.0;
-            L.x[1] = ph;
-            L.c[1] = alpha;
-            L.x[2] = sh;
-            L.c[2] = omega;
-            lin(xo, L, n, s);
-            lin(r, lin2(sv, 1.0, t, -omega), n, s);
-            double rr;
-            rho_prev = rho;
-            red.dot2(rhat, r, r, r, n, rho, rr, s);
-            if (!std::isfinite(rr)) return false;
-            if (std::sqrt(rr) <= rtol * bnorm) return true;
-            if (!(omega != 0.0)) return false;
+            if (h.status == 2) {
+                done_its = 0;
+                return false;
+            }
         }
+        done_its = 0;
         return false;
     }
+    int64_t done_its = 0;
+    DBuf kdev;
+    // kCheck BiCGStab iterations on the current W, captured once per W and replayed
+    cudaGraphExec_t chunk = nullptr;
+    void iterations() {
+        KDev* kd = kdev.as<KDev>();
+        double* part = red.part.as<double>();
+        const unsigned g = blocks_for(n);
+        for (int j = 0; j < kCheck; ++j) {
+            kd_p_kernel<<<g, kThreads, 0, s>>>(kd, r, pv, v, n);
+            jacobi_kernel<<<g, kThreads, 0, s>>>(pv, dw, ph, n);
+            wmul(ph, v);
+            dot2_kernel<<<kParts, kThreads, 0, s>>>(rhat, v, nullptr, nullptr, n, part);
+            kd_alpha_kernel<<<1, kFin, 0, s>>>(kd, part);
+            kd_s_kernel<<<g, kThreads, 0, s>>>(kd, r, v, sv, n);
+            jacobi_kernel<<<g, kThreads, 0, s>>>(sv, dw, sh, n);
+            wmul(sh, t);
+            dot2_kernel<<<kParts, kThreads, 0, s>>>(t, sv, t, t, n, part);
+            kd_omega_kernel<<<1, kFin, 0, s>>>(kd, part);
+            kd_xr_kernel<<<g, kThreads, 0, s>>>(kd, x, ph, sh, sv, t, r, n);
+            dot2_kernel<<<kParts, kThreads, 0, s>>>(rhat, r, r, r, n, part);
+            kd_rho_kernel<<<1, kFin, 0, s>>>(kd, part);
+        }
+    }
+    void capture_chunk() {
+        cudaGraph_t graph = nullptr;
+        FVM_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        iterations();
+        FVM_CUDA(cudaStreamEndCapture(s, &graph));
+        const cudaError_t e = cudaGraphInstantiate(&chunk, graph, 0);
+        cudaGraphDestroy(graph);
+        FVM_CUDA(e);
+    }
+    void drop_chunk() {
+        if (chunk) cudaGraphExecDestroy(chunk);
+        chunk = nullptr;
+    }
+    ~Trbdf2() { drop_chunk(); }
     // z = h f(base + d z) by simplified Newton from the predictor already in z; exact_linear: one
     // iteration solves an affine f to the Krylov tolerance
     bool stage(double* z, double tt, double h, bool exact_linear) {
@@ -433,7 +550,23 @@ int fvm_trbdf2_solve(fvm_problem* p, const double* u0, const fvm_ode_options* o,
         if (p->conditions_only) fail(FVM_ERR_INVALID_ARGUMENT, "this problem carries a template's conditions only");
         if (!(o->tf > o->t0)) fail(FVM_ERR_INVALID_ARGUMENT, "final time must exceed the initial time");
         if (!o->adaptive && !(o->dt > 0)) fail(FVM_ERR_INVALID_ARGUMENT, "dt must be positive for fixed steps");
+        // a stream that can be captured (the legacy default stream cannot): the caller's, or one
+        // of ours ordered after the default stream's earlier work
         cudaStream_t s = (cudaStream_t)stream;
+        struct OwnStream {
+            cudaStream_t s = nullptr;
+            ~OwnStream() {
+                if (s) {
+                    cudaStreamSynchronize(s);
+                    cudaStreamDestroy(s);
+                }
+            }
+        } own;
+        if (!s || s == cudaStreamLegacy || s == cudaStreamPerThread) {
+            FVM_CUDA(cudaDeviceSynchronize());
+            FVM_CUDA(cudaStreamCreateWithFlags(&own.s, cudaStreamNonBlocking));
+            s = own.s;
+        }
         fvm_mesh* m = p->mesh;
         const int64_t n = m->np;
         std::vector<double> saveat;
@@ -519,8 +652,8 @@ int fvm_trbdf2_solve(fvm_problem* p, const double* u0, const fvm_ode_options* o,
                 L.x[2] = M.z1;
                 L.c[2] = (kSqrt2 - 2.0) / 3.0;
                 lin(M.tmp, L, n, s);
-                if (!M.solve(M.tmp, M.est, 1e-10, 1000)) fail(FVM_ERR_STEP_LIMIT, "TRBDF2: the error estimate's solve failed");
-                err = M.red.wrms(M.est, M.u, M.un, o->abstol, o->reltol, n, s);
+                if (!M.solve(M.tmp, M.x, 1e-10, 1000)) fail(FVM_ERR_STEP_LIMIT, "TRBDF2: the error estimate's solve failed");
+                err = M.red.wrms(M.x, M.u, M.un, o->abstol, o->reltol, n, s);
                 if (!std::isfinite(err)) fail(FVM_ERR_STEP_LIMIT, "TRBDF2 error estimate is not finite");
                 if (err > 1.0) {
                     ++nrej;
