@@ -326,8 +326,25 @@ constexpr double kGamma = 2.0 - kSqrt2;
 constexpr double kD = kGamma / 2.0;
 constexpr double kW = kSqrt2 / 4.0;
 
+}  // namespace
+
+// What the integrator needs of a right-hand side, in the internal numbering: f(y, t), J(u) v,
+// diag J(u), and the Dirichlet update after a step (optional).  callback_varies: the update
+// changes u at every step (time-dependent values).  affine: f is affine in u with an exact J,
+// so one Newton iteration solves a stage.
+struct ImplicitRhs {
+    std::function<void(const double*, double*, double, cudaStream_t)> f;
+    std::function<void(const double*, const double*, double*, cudaStream_t)> jvp;
+    std::function<void(const double*, double*, cudaStream_t)> diag;
+    std::function<void(double*, double, cudaStream_t)> callback;
+    bool callback_varies = false;
+    bool affine = false;
+};
+
+namespace {
+
 struct Trbdf2 {
-    fvm_problem* p;
+    ImplicitRhs* R;
     int64_t n;
     cudaStream_t s;
     double abstol, reltol;
@@ -339,8 +356,8 @@ struct Trbdf2 {
     double wd = 0;  // d h of the current W
     const double* wu = nullptr;  // J's point
 
-    Trbdf2(fvm_problem* p_, int64_t n_, cudaStream_t s_, double at, double rt)
-        : p(p_), n(n_), s(s_), abstol(at), reltol(rt) {
+    Trbdf2(ImplicitRhs* R_, int64_t n_, cudaStream_t s_, double at, double rt)
+        : R(R_), n(n_), s(s_), abstol(at), reltol(rt) {
         constexpr int nv = 21;
         buf.alloc(sizeof(double) * n * nv);
         double* q = buf.as<double>();
@@ -350,11 +367,11 @@ struct Trbdf2 {
         kdev.alloc(sizeof(KDev));
     }
     void rhs(const double* y, double* out, double tt) {
-        problem_rhs_internal(p, y, out, false, s, false, tt);
+        R->f(y, out, tt, s);
         ++nrhs;
     }
     void wmul(const double* xin, double* out) {  // out = xin - d h J(wu) xin (two per BiCGStab iteration)
-        problem_jvp_internal(p, wu, xin, out, s);
+        R->jvp(wu, xin, out, s);
         lin(out, lin2(xin, 1.0, out, -wd), n, s);
     }
     // W at u_n with d h: its diagonal for the preconditioner; the captured iteration chunk of
@@ -363,7 +380,7 @@ struct Trbdf2 {
         drop_chunk();
         wu = at;
         wd = dh;
-        problem_jacobian_diagonal_internal(p, at, dj, s);
+        R->diag(at, dj, s);
         wdiag_kernel<<<blocks_for(n), kThreads, 0, s>>>(dj, dh, dw, n);
     }
     // x = W^-1 b by right-preconditioned BiCGStab to ||b - W x|| <= rtol ||b||; x starts at 0.
@@ -471,6 +488,176 @@ struct Trbdf2 {
 
 using namespace fvm;
 
+// TR-BDF2 on R over a mesh's points: u0 and out are host arrays in the caller's numbering.
+static int trbdf2_run(ImplicitRhs& R, fvm_mesh* m, const double* u0, const fvm_ode_options* o, double* out,
+                      fvm_ode_stats* st, fvm_implicit_stats* ist, void* stream) {
+    {
+        if (!u0 || !o || !out) fail(FVM_ERR_INVALID_ARGUMENT, "NULL argument");
+        if (!(o->tf > o->t0)) fail(FVM_ERR_INVALID_ARGUMENT, "final time must exceed the initial time");
+        if (!o->adaptive && !(o->dt > 0)) fail(FVM_ERR_INVALID_ARGUMENT, "dt must be positive for fixed steps");
+        // a stream that can be captured (the legacy default stream cannot): the caller's, or one
+        // of ours ordered after the default stream's earlier work
+        cudaStream_t s = (cudaStream_t)stream;
+        struct OwnStream {
+            cudaStream_t s = nullptr;
+            ~OwnStream() {
+                if (s) {
+                    cudaStreamSynchronize(s);
+                    cudaStreamDestroy(s);
+                }
+            }
+        } own;
+        if (!s || s == cudaStreamLegacy || s == cudaStreamPerThread) {
+            FVM_CUDA(cudaDeviceSynchronize());
+            FVM_CUDA(cudaStreamCreateWithFlags(&own.s, cudaStreamNonBlocking));
+            s = own.s;
+        }
+        const int64_t n = m->np;
+        std::vector<double> saveat;
+        if (o->saveat && o->nsave > 0)
+            saveat.assign(o->saveat, o->saveat + o->nsave);
+        else
+            saveat.push_back(o->tf);
+        for (size_t i = 0; i < saveat.size(); ++i) {
+            if (saveat[i] < o->t0 || saveat[i] > o->tf) fail(FVM_ERR_INVALID_ARGUMENT, "saveat times must lie in [t0, tf]");
+            if (i && saveat[i] < saveat[i - 1]) fail(FVM_ERR_INVALID_ARGUMENT, "saveat must be sorted");
+        }
+        Trbdf2 M(&R, n, s, o->abstol, o->reltol);
+        DBuf d_in, d_out;
+        d_in.alloc(sizeof(double) * n);
+        d_out.alloc(sizeof(double) * n * saveat.size());
+        FVM_CUDA(cudaMemcpyAsync(d_in.p, u0, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+        launch_permute_in(m->d_perm.as<int32_t>(), d_in.as<double>(), M.u, n, s);
+        double* outi = d_out.as<double>();
+        size_t si = 0;
+        auto save = [&](const double* src) {
+            FVM_CUDA(cudaMemcpyAsync(outi + si * n, src, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+            ++si;
+        };
+        double t = o->t0;
+        while (si < saveat.size() && saveat[si] == t) save(M.u);
+        cudaEvent_t e0, e1;
+        FVM_CUDA(cudaEventCreate(&e0));
+        FVM_CUDA(cudaEventCreate(&e1));
+        FVM_CUDA(cudaEventRecord(e0, s));
+        M.rhs(M.u, M.fn, t);
+        const double tspan = o->tf - o->t0;
+        // affine f with an exact product: one Newton iteration solves each stage
+        const bool exact_linear = R.affine;
+        double h = o->dt;
+        if (o->adaptive && !(h > 0)) {  // order-2 version of the Hairer-Wanner initial step
+            const double d0 = M.red.wrms(M.u, M.u, nullptr, o->abstol, o->reltol, n, s);
+            const double d1 = M.red.wrms(M.fn, M.u, nullptr, o->abstol, o->reltol, n, s);
+            const double h0 = (d0 < 1e-5 || d1 < 1e-5) ? 1e-6 : 0.01 * d0 / d1;
+            h = std::min(h0, tspan);
+        }
+        const int64_t max_steps = o->max_steps > 0 ? o->max_steps : 100000000;
+        int64_t nacc = 0, nrej = 0, step = 0;
+        bool first_cb = true;
+        while (t < o->tf) {
+            if (step >= max_steps) fail(FVM_ERR_STEP_LIMIT, "TRBDF2 reached max_steps before tf");
+            const bool last = t + h >= o->tf - 1e-12 * tspan;
+            const double hh = last ? o->tf - t : h;
+            ++step;
+            // z_n = h f_n; W = I - d h J(u_n)
+            lin(M.zn, lin2(M.fn, hh, nullptr, 0.0), n, s);
+            M.set_w(M.u, kD * hh);
+            // trapezoidal stage: base = u_n + d z_n, predictor z_g = z_n
+            lin(M.base, lin2(M.u, 1.0, M.zn, kD), n, s);
+            FVM_CUDA(cudaMemcpyAsync(M.zg, M.zn, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+            bool ok = M.stage(M.zg, t + kGamma * hh, hh, exact_linear);
+            if (ok) {  // BDF2 stage: base = u_n + w z_n + w z_g, predictor z_1 = z_g
+                Lin L{};
+                L.x[0] = M.u;
+                L.c[0] = 1.0;
+                L.x[1] = M.zn;
+                L.c[1] = kW;
+                L.x[2] = M.zg;
+                L.c[2] = kW;
+                lin(M.base, L, n, s);
+                FVM_CUDA(cudaMemcpyAsync(M.z1, M.zg, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+                ok = M.stage(M.z1, t + hh, hh, exact_linear);
+            }
+            if (!ok) {
+                ++M.newton_fail;
+                if (!o->adaptive) fail(FVM_ERR_STEP_LIMIT, "TRBDF2: the Newton iteration did not converge at the fixed dt");
+                h = hh / 4;
+                if (h < 1e-14 * std::max(1.0, std::fabs(t))) fail(FVM_ERR_STEP_LIMIT, "TRBDF2 step size underflow");
+                continue;
+            }
+            lin(M.un, lin2(M.base, 1.0, M.z1, kD), n, s);  // u_{n+1}
+            double err = 0.0;
+            if (o->adaptive) {
+                Lin L{};
+                L.x[0] = M.zn;
+                L.c[0] = (1.0 - kSqrt2) / 3.0;
+                L.x[1] = M.zg;
+                L.c[1] = 1.0 / 3.0;
+                L.x[2] = M.z1;
+                L.c[2] = (kSqrt2 - 2.0) / 3.0;
+                lin(M.tmp, L, n, s);
+                if (!M.solve(M.tmp, M.x, 1e-10, 1000)) fail(FVM_ERR_STEP_LIMIT, "TRBDF2: the error estimate's solve failed");
+                err = M.red.wrms(M.x, M.u, M.un, o->abstol, o->reltol, n, s);
+                if (!std::isfinite(err)) fail(FVM_ERR_STEP_LIMIT, "TRBDF2 error estimate is not finite");
+                if (err > 1.0) {
+                    ++nrej;
+                    h = hh * std::min(10.0, std::max(0.2, 0.9 * std::pow(err, -1.0 / 3.0)));
+                    if (h < 1e-14 * std::max(1.0, std::fabs(t))) fail(FVM_ERR_STEP_LIMIT, "TRBDF2 step size underflow");
+                    continue;
+                }
+            }
+            const double tn = last ? o->tf : t + hh;
+            // f at u_{n+1} (before the Dirichlet update) for the interpolant
+            M.rhs(M.un, M.f1, tn);
+            while (si < saveat.size() && saveat[si] < tn) {
+                const double th = (saveat[si] - t) / hh;
+                hermite_kernel<<<blocks_for(n), kThreads, 0, s>>>(outi + si * n, M.u, M.fn, M.un, M.f1, hh, th, n);
+                ++si;
+            }
+            std::swap(M.u, M.un);
+            std::swap(M.fn, M.f1);
+            t = tn;
+            ++nacc;
+            if (R.callback) {
+                R.callback(M.u, t, s);
+                if (first_cb || R.callback_varies) M.rhs(M.u, M.fn, t);
+                first_cb = false;
+            }
+            while (si < saveat.size() && saveat[si] == t) save(M.u);
+            if (o->adaptive) {
+                const double q = err > 0 ? 0.9 * std::pow(err, -1.0 / 3.0) : 10.0;
+                h = std::min(tspan, hh * std::min(10.0, std::max(0.2, q)));
+            }
+            if (last) break;
+        }
+        while (si < saveat.size()) save(M.u);
+        FVM_CUDA(cudaEventRecord(e1, s));
+        FVM_CUDA(cudaEventSynchronize(e1));
+        float ms = 0;
+        FVM_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        snapshots_to_host(m->d_iperm.as<int32_t>(), outi, out, n, (int64_t)saveat.size(), s);
+        FVM_CUDA(cudaStreamSynchronize(s));
+        FVM_CUDA(cudaGetLastError());
+        if (st) {
+            st->naccept = nacc;
+            st->nreject = nrej;
+            st->nrhs = M.nrhs;
+            st->t_final = t;
+            st->elapsed_ms = ms;
+            st->driver = FVM_DRIVER_HOST;
+        }
+        if (ist) {
+            ist->newton_iters = M.newton;
+            ist->krylov_iters = M.krylov;
+            ist->jvps = M.jvps;
+            ist->newton_failures = M.newton_fail;
+        }
+        return FVM_OK;
+    }
+}
+
 extern "C" {
 
 int fvm_jvp(fvm_problem* p, const double* u, const double* v, double* jv, double t, int32_t flags, void* stream) {
@@ -546,171 +733,46 @@ int fvm_jacobian_diagonal(fvm_problem* p, const double* u, double* diag, double 
 int fvm_trbdf2_solve(fvm_problem* p, const double* u0, const fvm_ode_options* o, double* out, fvm_ode_stats* st,
                      fvm_implicit_stats* ist, void* stream) {
     return guard_call([&] {
-        if (!p || !u0 || !o || !out) fail(FVM_ERR_INVALID_ARGUMENT, "NULL argument");
+        if (!p) fail(FVM_ERR_INVALID_ARGUMENT, "NULL argument");
         if (p->conditions_only) fail(FVM_ERR_INVALID_ARGUMENT, "this problem carries a template's conditions only");
-        if (!(o->tf > o->t0)) fail(FVM_ERR_INVALID_ARGUMENT, "final time must exceed the initial time");
-        if (!o->adaptive && !(o->dt > 0)) fail(FVM_ERR_INVALID_ARGUMENT, "dt must be positive for fixed steps");
-        // a stream that can be captured (the legacy default stream cannot): the caller's, or one
-        // of ours ordered after the default stream's earlier work
-        cudaStream_t s = (cudaStream_t)stream;
-        struct OwnStream {
-            cudaStream_t s = nullptr;
-            ~OwnStream() {
-                if (s) {
-                    cudaStreamSynchronize(s);
-                    cudaStreamDestroy(s);
-                }
-            }
-        } own;
-        if (!s || s == cudaStreamLegacy || s == cudaStreamPerThread) {
-            FVM_CUDA(cudaDeviceSynchronize());
-            FVM_CUDA(cudaStreamCreateWithFlags(&own.s, cudaStreamNonBlocking));
-            s = own.s;
-        }
-        fvm_mesh* m = p->mesh;
-        const int64_t n = m->np;
-        std::vector<double> saveat;
-        if (o->saveat && o->nsave > 0)
-            saveat.assign(o->saveat, o->saveat + o->nsave);
-        else
-            saveat.push_back(o->tf);
-        for (size_t i = 0; i < saveat.size(); ++i) {
-            if (saveat[i] < o->t0 || saveat[i] > o->tf) fail(FVM_ERR_INVALID_ARGUMENT, "saveat times must lie in [t0, tf]");
-            if (i && saveat[i] < saveat[i - 1]) fail(FVM_ERR_INVALID_ARGUMENT, "saveat must be sorted");
-        }
-        Trbdf2 M(p, n, s, o->abstol, o->reltol);
-        DBuf d_in, d_out;
-        d_in.alloc(sizeof(double) * n);
-        d_out.alloc(sizeof(double) * n * saveat.size());
-        FVM_CUDA(cudaMemcpyAsync(d_in.p, u0, sizeof(double) * n, cudaMemcpyHostToDevice, s));
-        launch_permute_in(m->d_perm.as<int32_t>(), d_in.as<double>(), M.u, n, s);
-        double* outi = d_out.as<double>();
-        size_t si = 0;
-        auto save = [&](const double* src) {
-            FVM_CUDA(cudaMemcpyAsync(outi + si * n, src, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
-            ++si;
+        ImplicitRhs R;
+        R.f = [p](const double* y, double* du, double t, cudaStream_t s) {
+            problem_rhs_internal(p, y, du, false, s, false, t);
         };
-        double t = o->t0;
-        while (si < saveat.size() && saveat[si] == t) save(M.u);
-        cudaEvent_t e0, e1;
-        FVM_CUDA(cudaEventCreate(&e0));
-        FVM_CUDA(cudaEventCreate(&e1));
-        FVM_CUDA(cudaEventRecord(e0, s));
-        M.rhs(M.u, M.fn, t);
-        const double tspan = o->tf - o->t0;
-        // affine f with an exact product: one Newton iteration solves each stage
-        const bool exact_linear = p->linear && !p->has_q && p->precision != FVM_FP32;
-        double h = o->dt;
-        if (o->adaptive && !(h > 0)) {  // order-2 version of the Hairer-Wanner initial step
-            const double d0 = M.red.wrms(M.u, M.u, nullptr, o->abstol, o->reltol, n, s);
-            const double d1 = M.red.wrms(M.fn, M.u, nullptr, o->abstol, o->reltol, n, s);
-            const double h0 = (d0 < 1e-5 || d1 < 1e-5) ? 1e-6 : 0.01 * d0 / d1;
-            h = std::min(h0, tspan);
-        }
-        const int64_t max_steps = o->max_steps > 0 ? o->max_steps : 100000000;
-        int64_t nacc = 0, nrej = 0, step = 0;
-        bool first_cb = true;
-        while (t < o->tf) {
-            if (step >= max_steps) fail(FVM_ERR_STEP_LIMIT, "TRBDF2 reached max_steps before tf");
-            const bool last = t + h >= o->tf - 1e-12 * tspan;
-            const double hh = last ? o->tf - t : h;
-            ++step;
-            // z_n = h f_n; W = I - d h J(u_n)
-            lin(M.zn, lin2(M.fn, hh, nullptr, 0.0), n, s);
-            M.set_w(M.u, kD * hh);
-            // trapezoidal stage: base = u_n + d z_n, predictor z_g = z_n
-            lin(M.base, lin2(M.u, 1.0, M.zn, kD), n, s);
-            FVM_CUDA(cudaMemcpyAsync(M.zg, M.zn, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
-            bool ok = M.stage(M.zg, t + kGamma * hh, hh, exact_linear);
-            if (ok) {  // BDF2 stage: base = u_n + w z_n + w z_g, predictor z_1 = z_g
-                Lin L{};
-                L.x[0] = M.u;
-                L.c[0] = 1.0;
-                L.x[1] = M.zn;
-                L.c[1] = kW;
-                L.x[2] = M.zg;
-                L.c[2] = kW;
-                lin(M.base, L, n, s);
-                FVM_CUDA(cudaMemcpyAsync(M.z1, M.zg, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
-                ok = M.stage(M.z1, t + hh, hh, exact_linear);
-            }
-            if (!ok) {
-                ++M.newton_fail;
-                if (!o->adaptive) fail(FVM_ERR_STEP_LIMIT, "TRBDF2: the Newton iteration did not converge at the fixed dt");
-                h = hh / 4;
-                if (h < 1e-14 * std::max(1.0, std::fabs(t))) fail(FVM_ERR_STEP_LIMIT, "TRBDF2 step size underflow");
-                continue;
-            }
-            lin(M.un, lin2(M.base, 1.0, M.z1, kD), n, s);  // u_{n+1}
-            double err = 0.0;
-            if (o->adaptive) {
-                Lin L{};
-                L.x[0] = M.zn;
-                L.c[0] = (1.0 - kSqrt2) / 3.0;
-                L.x[1] = M.zg;
-                L.c[1] = 1.0 / 3.0;
-                L.x[2] = M.z1;
-                L.c[2] = (kSqrt2 - 2.0) / 3.0;
-                lin(M.tmp, L, n, s);
-                if (!M.solve(M.tmp, M.x, 1e-10, 1000)) fail(FVM_ERR_STEP_LIMIT, "TRBDF2: the error estimate's solve failed");
-                err = M.red.wrms(M.x, M.u, M.un, o->abstol, o->reltol, n, s);
-                if (!std::isfinite(err)) fail(FVM_ERR_STEP_LIMIT, "TRBDF2 error estimate is not finite");
-                if (err > 1.0) {
-                    ++nrej;
-                    h = hh * std::min(10.0, std::max(0.2, 0.9 * std::pow(err, -1.0 / 3.0)));
-                    if (h < 1e-14 * std::max(1.0, std::fabs(t))) fail(FVM_ERR_STEP_LIMIT, "TRBDF2 step size underflow");
-                    continue;
-                }
-            }
-            const double tn = last ? o->tf : t + hh;
-            // f at u_{n+1} (before the Dirichlet update) for the interpolant
-            M.rhs(M.un, M.f1, tn);
-            while (si < saveat.size() && saveat[si] < tn) {
-                const double th = (saveat[si] - t) / hh;
-                hermite_kernel<<<blocks_for(n), kThreads, 0, s>>>(outi + si * n, M.u, M.fn, M.un, M.f1, hh, th, n);
-                ++si;
-            }
-            std::swap(M.u, M.un);
-            std::swap(M.fn, M.f1);
-            t = tn;
-            ++nacc;
-            if (p->ndir > 0) {
-                problem_dirichlet_internal(p, M.u, t, s);
-                if (first_cb || p->tdir_varies) M.rhs(M.u, M.fn, t);
-                first_cb = false;
-            }
-            while (si < saveat.size() && saveat[si] == t) save(M.u);
-            if (o->adaptive) {
-                const double q = err > 0 ? 0.9 * std::pow(err, -1.0 / 3.0) : 10.0;
-                h = std::min(tspan, hh * std::min(10.0, std::max(0.2, q)));
-            }
-            if (last) break;
-        }
-        while (si < saveat.size()) save(M.u);
-        FVM_CUDA(cudaEventRecord(e1, s));
-        FVM_CUDA(cudaEventSynchronize(e1));
-        float ms = 0;
-        FVM_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
-        snapshots_to_host(m->d_iperm.as<int32_t>(), outi, out, n, (int64_t)saveat.size(), s);
-        FVM_CUDA(cudaStreamSynchronize(s));
-        FVM_CUDA(cudaGetLastError());
-        if (st) {
-            st->naccept = nacc;
-            st->nreject = nrej;
-            st->nrhs = M.nrhs;
-            st->t_final = t;
-            st->elapsed_ms = ms;
-            st->driver = FVM_DRIVER_HOST;
-        }
-        if (ist) {
-            ist->newton_iters = M.newton;
-            ist->krylov_iters = M.krylov;
-            ist->jvps = M.jvps;
-            ist->newton_failures = M.newton_fail;
-        }
-        return FVM_OK;
+        R.jvp = [p](const double* u, const double* v, double* jv, cudaStream_t s) { problem_jvp_internal(p, u, v, jv, s); };
+        R.diag = [p](const double* u, double* d, cudaStream_t s) { problem_jacobian_diagonal_internal(p, u, d, s); };
+        if (p->ndir > 0)
+            R.callback = [p](double* u, double t, cudaStream_t s) { problem_dirichlet_internal(p, u, t, s); };
+        R.callback_varies = p->tdir_varies;
+        R.affine = p->linear && !p->has_q && p->precision != FVM_FP32;
+        return trbdf2_run(R, p->mesh, u0, o, out, st, ist, stream);
+    });
+}
+
+int fvm_template_trbdf2_solve(fvm_template* T, const double* u0, const fvm_ode_options* o, double* out,
+                              fvm_ode_stats* st, fvm_implicit_stats* ist, void* stream) {
+    return guard_call([&] {
+        if (!T) fail(FVM_ERR_INVALID_ARGUMENT, "NULL argument");
+        if (T->kind != FVM_TEMPLATE_DIFFUSION && T->kind != FVM_TEMPLATE_LINEAR_REACTION_DIFFUSION)
+            fail(FVM_ERR_INVALID_ARGUMENT, "only time-dependent templates can be stepped");
+        fvm_mesh* m = T->prob->mesh;
+        // du/dt = A u + b: J = A, the template's operator itself (its rows of Dirichlet and missing
+        // vertices are zero, so those values stay as given)
+        ImplicitRhs R;
+        R.f = [T, m](const double* y, double* du, double, cudaStream_t s) {
+            launch_sell_apply64(m->pat, T->d_val64.as<double>(), y, du, nullptr, T->d_b.as<double>(), nullptr, s);
+        };
+        R.jvp = [T, m](const double*, const double* v, double* jv, cudaStream_t s) {
+            launch_sell_apply64(m->pat, T->d_val64.as<double>(), v, jv, nullptr, nullptr, nullptr, s);
+        };
+        R.diag = [T, m](const double*, double* d, cudaStream_t s) {
+            const SellPattern& pat = m->pat;
+            sell_diag_kernel<double><<<blocks_for(m->np), kThreads, 0, s>>>(
+                pat.d_slice_ptr.as<int64_t>(), pat.d_width.as<int32_t>(), pat.d_col.as<int32_t>(),
+                T->d_val64.as<double>(), nullptr, m->np, d);
+        };
+        R.affine = true;
+        return trbdf2_run(R, m, u0, o, out, st, ist, stream);
     });
 }
 

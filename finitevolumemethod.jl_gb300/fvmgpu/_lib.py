@@ -185,6 +185,8 @@ SIGNATURES = {
     "fvm_jacobian_diagonal": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int32, C.c_void_p]),
     "fvm_trbdf2_solve": (C.c_int, [C.c_void_p, c_double_p, C.POINTER(OdeOptions), c_double_p, C.POINTER(OdeStats),
                                    C.POINTER(ImplicitStats), C.c_void_p]),
+    "fvm_template_trbdf2_solve": (C.c_int, [C.c_void_p, c_double_p, C.POINTER(OdeOptions), c_double_p,
+                                            C.POINTER(OdeStats), C.POINTER(ImplicitStats), C.c_void_p]),
     "fvm_tsit5_solve": (C.c_int, [C.c_void_p, c_double_p, C.POINTER(OdeOptions), c_double_p, C.POINTER(OdeStats),
                                   C.c_void_p]),
     "fvm_system_create": (C.c_int, [C.c_void_p, C.POINTER(SystemDesc), C.POINTER(C.c_void_p)]),

@@ -1427,7 +1427,8 @@ class TRBDF2:
     """TR-BDF2 (the implicit method of the reference's tutorials), on the device: simplified
     Newton per stage, matrix-free BiCGStab on W = I - d h J with the exact Jacobian-vector
     product of fvm_eqs!, diag(W) as preconditioner; adaptive with TR-BDF2's error estimate
-    (dt given with adaptive=False: fixed steps).  FVMProblem only."""
+    (dt given with adaptive=False: fixed steps).  FVMProblem, DiffusionEquation and
+    LinearReactionDiffusionEquation (J = A)."""
 
     def __repr__(self):
         return "TRBDF2()"
@@ -1577,6 +1578,15 @@ def solve(prob, alg=None, *, saveat=None, dt=None, adaptive=None, abstol=1e-6, r
     o.precision = _precision(precision)
     st = _lib.OdeStats()
     u0c = as_f64(u0)
+    if isinstance(prob, _TimeTemplate) and isinstance(alg, TRBDF2):
+        ist = _lib.ImplicitStats()
+        check(lib.fvm_template_trbdf2_solve(prob.handle, dptr(u0c), C.byref(o), dptr(out), C.byref(st), C.byref(ist),
+                                            s))
+        us = [np.append(row, 1.0) for row in out]
+        return ODESolution(ts, us, {"naccept": st.naccept, "nreject": st.nreject, "nrhs": st.nrhs,
+                                    "t_final": st.t_final, "elapsed_ms": st.elapsed_ms, "driver": "host",
+                                    "newton_iters": ist.newton_iters, "krylov_iters": ist.krylov_iters,
+                                    "jvps": ist.jvps, "newton_failures": ist.newton_failures})
     if isinstance(prob, _TimeTemplate):
         check(lib.fvm_template_tsit5_solve(prob.handle, dptr(u0c), C.byref(o), dptr(out), C.byref(st), s))
         us = [np.append(row, 1.0) for row in out]  # the augmented component of the MatrixOperator form
@@ -1585,7 +1595,7 @@ def solve(prob, alg=None, *, saveat=None, dt=None, adaptive=None, abstol=1e-6, r
         us = [row.T for row in out]  # (N, npoints) views: entry (j, i) is component j at node i
     elif isinstance(alg, TRBDF2):
         if not isinstance(prob, FVMProblem):
-            raise TypeError("TRBDF2 runs on an FVMProblem")
+            raise TypeError("TRBDF2 runs on an FVMProblem or a time-dependent template")
         ist = _lib.ImplicitStats()
         check(lib.fvm_trbdf2_solve(prob.handle, dptr(u0c), C.byref(o), dptr(out), C.byref(st), C.byref(ist), s))
         us = list(out)

@@ -39,14 +39,17 @@ end
 CommonSolve.solve(prob::FVM.FVMProblem, alg::Tsit5; kwargs...) = gpu_tsit5(prob, alg; kwargs...)
 
 # TRBDF2 (the tutorials' implicit method, whatever linsolve it names): the device's TR-BDF2
-function CommonSolve.solve(prob::FVM.FVMProblem, alg::TRBDF2; saveat = nothing, dt = nothing, adaptive = true,
-                           abstol = 1e-6, reltol = 1e-3, maxiters = 0, kwargs...)
+function gpu_trbdf2(prob, alg; saveat = nothing, dt = nothing, adaptive = true, abstol = 1e-6, reltol = 1e-3,
+                    maxiters = 0, kwargs...)
     g = G.gpu_object(prob)
     fixed = dt !== nothing && !adaptive
     ts, us, _ = G.solve_trbdf2(g; saveat = save_times(prob, saveat), dt = fixed ? dt : nothing, abstol, reltol,
                                max_steps = maxiters)
     return gpu_solution(alg, ts, us)
 end
+CommonSolve.solve(prob::FVM.FVMProblem, alg::TRBDF2; kwargs...) = gpu_trbdf2(prob, alg; kwargs...)
+CommonSolve.solve(tmpl::FVM.DiffusionEquation, alg::TRBDF2; kwargs...) = gpu_trbdf2(tmpl, alg; kwargs...)
+CommonSolve.solve(tmpl::FVM.LinearReactionDiffusionEquation, alg::TRBDF2; kwargs...) = gpu_trbdf2(tmpl, alg; kwargs...)
 CommonSolve.solve(sys::FVM.FVMSystem, alg::Tsit5; kwargs...) = gpu_tsit5(sys, alg; kwargs...)
 CommonSolve.solve(tmpl::FVM.DiffusionEquation, alg::Tsit5; kwargs...) = gpu_tsit5(tmpl, alg; kwargs...)
 CommonSolve.solve(tmpl::FVM.LinearReactionDiffusionEquation, alg::Tsit5; kwargs...) = gpu_tsit5(tmpl, alg; kwargs...)

@@ -350,6 +350,8 @@ function solve_trbdf2(gp::GPUProblem; saveat, dt = nothing, abstol = 1e-6, relto
     return ts, [out[(k-1)*np+1:k*np] for k in eachindex(ts)], ist
 end
 
+
+
 # ---- systems: FVMSystem(prob1, ..., probN) (src/problem.jl:190-365) -----------------------
 struct SystemDesc
     neq::Int32
@@ -721,6 +723,29 @@ function solve(gt::GPUTemplate; saveat, dt = nothing, abstol = 1e-6, reltol = 1e
         (Ptr{Cvoid}, Ptr{Float64}, Ref{OdeOptions}, Ptr{Float64}, Ref{OdeStats}, Ptr{Cvoid}),
         gt.handle, u0, opt, out, st, C_NULL))
     return ts, [vcat(out[(k-1)*np+1:k*np], 1.0) for k in eachindex(ts)]
+end
+
+"""
+    solve_trbdf2(gt::GPUTemplate; saveat, dt = nothing, abstol = 1e-6, reltol = 1e-3)
+
+TR-BDF2 on a time-dependent template (J = A).  Returns `(t, u, stats)`, `u[k]` of length
+npoints + 1 (the reference's augmented state).
+"""
+function solve_trbdf2(gt::GPUTemplate; saveat, dt = nothing, abstol = 1e-6, reltol = 1e-3, max_steps = 0)
+    tmpl = gt.tmpl
+    t0, tf = tmpl.initial_time, tmpl.final_time
+    ts = saveat isa Number ? collect(t0:saveat:tf) : collect(Float64, saveat)
+    np = gt.mesh.npoints
+    out = Vector{Float64}(undef, np * length(ts))
+    u0 = collect(Float64, tmpl.initial_condition)[1:np]
+    opt = OdeOptions(t0, tf, dt === nothing ? 0.0 : dt, dt === nothing ? Int32(1) : Int32(0), abstol, reltol,
+        max_steps, pointer(ts), length(ts), Int32(0), Int32(0))
+    st = OdeStats(0, 0, 0, 0.0, 0.0, Int32(0))
+    ist = ImplicitStats(0, 0, 0, 0)
+    GC.@preserve ts check(ccall((:fvm_template_trbdf2_solve, libfvmgpu), Cint,
+        (Ptr{Cvoid}, Ptr{Float64}, Ref{OdeOptions}, Ptr{Float64}, Ref{OdeStats}, Ref{ImplicitStats}, Ptr{Cvoid}),
+        gt.handle, u0, opt, out, st, ist, C_NULL))
+    return ts, [vcat(out[(k-1)*np+1:k*np], 1.0) for k in eachindex(ts)], ist
 end
 
 # ---- steady solve (LinearProblem(A, b), poissons_equation.jl:81, mean_exit_time.jl:76) -----

@@ -263,6 +263,10 @@ typedef struct fvm_implicit_stats {
  * NULL. */
 int fvm_trbdf2_solve(fvm_problem* prob, const double* u0, const fvm_ode_options* opt, double* out,
                      fvm_ode_stats* stats, fvm_implicit_stats* istats, void* stream);
+/* TR-BDF2 on a DiffusionEquation / LinearReactionDiffusionEquation template, du/dt = A u + b
+ * (J = A): solve(template, TRBDF2()) (abstract_templates.jl:58-60). */
+int fvm_template_trbdf2_solve(fvm_template* tmpl, const double* u0, const fvm_ode_options* opt, double* out,
+                              fvm_ode_stats* stats, fvm_implicit_stats* istats, void* stream);
 
 
 /* ---- systems of equations (FVMSystem, src/problem.jl:190-365) ---------------------------

@@ -189,7 +189,7 @@ def test_julia_ccalls_match_the_header_prototypes():
     bound = {name for name, _ in calls}
     for name in ("fvm_template_create", "fvm_template_tsit5_solve", "fvm_template_steady_solve", "fvm_batch_create",
                  "fvm_batch_tsit5_solve", "fvm_adjoint_forward", "fvm_adjoint_pullback", "fvm_mesh_locate",
-                 "fvm_pl_interpolate", "fvm_system_tsit5_solve", "fvm_tsit5_solve", "fvm_jvp", "fvm_trbdf2_solve"):
+                 "fvm_pl_interpolate", "fvm_system_tsit5_solve", "fvm_tsit5_solve", "fvm_jvp", "fvm_trbdf2_solve", "fvm_template_trbdf2_solve"):
         assert name in bound, name
     for name, types in calls:
         jt = [t.strip() for t in re.split(r",(?![^{]*\})", types) if t.strip()]

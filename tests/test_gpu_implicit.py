@@ -122,3 +122,24 @@ def test_trbdf2_takes_large_steps_on_a_stiff_problem(gpu_lib):
     assert err < 1e-2, err
     inner = np.linalg.norm(spec.tri.points, axis=1) < 0.2 + 1e-9
     assert np.allclose(imp.u[-1][inner], 50 * (1 - np.exp(-1.0)), rtol=1e-13)
+
+
+def test_trbdf2_on_a_template_matches_oracle(gpu_lib):
+    """DiffusionEquation with TR-BDF2 (J = A): the oracle's TR-BDF2 on its own sparse assembly of
+    A and b, the same steps, 1e-8 of max|u|."""
+    import fvmgpu as F
+
+    spec = sine_diffusion(30)
+    mesh = F.FVMGeometry(spec.tri)
+    BCs = F.BoundaryConditions(mesh, spec.bc_fns[0], F.Dirichlet)
+    D = lambda x, y, p: spec.D(x, y, 0, 0, None)  # noqa: E731
+    tmpl = F.DiffusionEquation(mesh, BCs, diffusion_function=D, initial_condition=spec.u0, final_time=0.02)
+    saveat = [0.0, 0.01, 0.02]
+    sol = F.solve(tmpl, F.TRBDF2(), saveat=saveat)
+    conds = O.Conditions(spec.tri, [lambda x, y, t, u: 0.0 * x], ["Dirichlet"])
+    A, b, u0 = O.template_diffusion(spec.tri, conds, lambda x, y: D(x, y, None), spec.u0)
+    ref, st = O.trbdf2_solve(lambda u, t: A @ u + b, lambda u, t: A, u0, 0.0, 0.02, saveat, affine=True)
+    assert sol.stats["naccept"] == st["naccept"] and sol.stats["nreject"] == st["nreject"]
+    got = np.array([row[:-1] for row in sol.u])
+    err = np.max(np.abs(got - ref)) / np.max(np.abs(ref))
+    assert err < 1e-8, err
