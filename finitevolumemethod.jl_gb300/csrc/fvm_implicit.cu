@@ -326,23 +326,6 @@ constexpr double kGamma = 2.0 - kSqrt2;
 constexpr double kD = kGamma / 2.0;
 constexpr double kW = kSqrt2 / 4.0;
 
-}  // namespace
-
-// What the integrator needs of a right-hand side, in the internal numbering: f(y, t), J(u) v,
-// diag J(u), and the Dirichlet update after a step (optional).  callback_varies: the update
-// changes u at every step (time-dependent values).  affine: f is affine in u with an exact J,
-// so one Newton iteration solves a stage.
-struct ImplicitRhs {
-    std::function<void(const double*, double*, double, cudaStream_t)> f;
-    std::function<void(const double*, const double*, double*, cudaStream_t)> jvp;
-    std::function<void(const double*, double*, cudaStream_t)> diag;
-    std::function<void(double*, double, cudaStream_t)> callback;
-    bool callback_varies = false;
-    bool affine = false;
-};
-
-namespace {
-
 struct Trbdf2 {
     ImplicitRhs* R;
     int64_t n;
@@ -488,9 +471,10 @@ struct Trbdf2 {
 
 using namespace fvm;
 
-// TR-BDF2 on R over a mesh's points: u0 and out are host arrays in the caller's numbering.
-static int trbdf2_run(ImplicitRhs& R, fvm_mesh* m, const double* u0, const fvm_ode_options* o, double* out,
-                      fvm_ode_stats* st, fvm_implicit_stats* ist, void* stream) {
+// TR-BDF2 on R over n unknowns: u0 and out are host arrays in the caller's numbering, perm /
+// iperm the device permutations between it and the internal one.
+int fvm::trbdf2_run(ImplicitRhs& R, const int32_t* perm, const int32_t* iperm, int64_t n, const double* u0,
+                    const fvm_ode_options* o, double* out, fvm_ode_stats* st, fvm_implicit_stats* ist, void* stream) {
     {
         if (!u0 || !o || !out) fail(FVM_ERR_INVALID_ARGUMENT, "NULL argument");
         if (!(o->tf > o->t0)) fail(FVM_ERR_INVALID_ARGUMENT, "final time must exceed the initial time");
@@ -512,7 +496,6 @@ static int trbdf2_run(ImplicitRhs& R, fvm_mesh* m, const double* u0, const fvm_o
             FVM_CUDA(cudaStreamCreateWithFlags(&own.s, cudaStreamNonBlocking));
             s = own.s;
         }
-        const int64_t n = m->np;
         std::vector<double> saveat;
         if (o->saveat && o->nsave > 0)
             saveat.assign(o->saveat, o->saveat + o->nsave);
@@ -527,7 +510,7 @@ static int trbdf2_run(ImplicitRhs& R, fvm_mesh* m, const double* u0, const fvm_o
         d_in.alloc(sizeof(double) * n);
         d_out.alloc(sizeof(double) * n * saveat.size());
         FVM_CUDA(cudaMemcpyAsync(d_in.p, u0, sizeof(double) * n, cudaMemcpyHostToDevice, s));
-        launch_permute_in(m->d_perm.as<int32_t>(), d_in.as<double>(), M.u, n, s);
+        launch_permute_in(perm, d_in.as<double>(), M.u, n, s);
         double* outi = d_out.as<double>();
         size_t si = 0;
         auto save = [&](const double* src) {
@@ -637,7 +620,7 @@ static int trbdf2_run(ImplicitRhs& R, fvm_mesh* m, const double* u0, const fvm_o
         FVM_CUDA(cudaEventElapsedTime(&ms, e0, e1));
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
-        snapshots_to_host(m->d_iperm.as<int32_t>(), outi, out, n, (int64_t)saveat.size(), s);
+        snapshots_to_host(iperm, outi, out, n, (int64_t)saveat.size(), s);
         FVM_CUDA(cudaStreamSynchronize(s));
         FVM_CUDA(cudaGetLastError());
         if (st) {
@@ -745,7 +728,8 @@ int fvm_trbdf2_solve(fvm_problem* p, const double* u0, const fvm_ode_options* o,
             R.callback = [p](double* u, double t, cudaStream_t s) { problem_dirichlet_internal(p, u, t, s); };
         R.callback_varies = p->tdir_varies;
         R.affine = p->linear && !p->has_q && p->precision != FVM_FP32;
-        return trbdf2_run(R, p->mesh, u0, o, out, st, ist, stream);
+        fvm_mesh* m = p->mesh;
+        return trbdf2_run(R, m->d_perm.as<int32_t>(), m->d_iperm.as<int32_t>(), m->np, u0, o, out, st, ist, stream);
     });
 }
 
@@ -772,7 +756,7 @@ int fvm_template_trbdf2_solve(fvm_template* T, const double* u0, const fvm_ode_o
                 T->d_val64.as<double>(), nullptr, m->np, d);
         };
         R.affine = true;
-        return trbdf2_run(R, m, u0, o, out, st, ist, stream);
+        return trbdf2_run(R, m->d_perm.as<int32_t>(), m->d_iperm.as<int32_t>(), m->np, u0, o, out, st, ist, stream);
     });
 }
 

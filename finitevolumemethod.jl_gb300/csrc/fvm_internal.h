@@ -456,4 +456,21 @@ void launch_time_b(const double* b, const double* tb, const TimeTaus& tt, int nt
                    cudaStream_t s);
 void launch_dirichlet_time(const int32_t* idx, const double* val, const double* tval, const TimeTaus& tt, int ntime,
                            double* u, int64_t n, cudaStream_t s);
+
+// What the implicit integrator needs of a right-hand side, in the internal numbering: f(y, t),
+// J(u) v, diag J(u), and the Dirichlet update after a step (optional).  callback_varies: the
+// update changes u at every step (time-dependent values).  affine: f is affine in u with an
+// exact J, so one Newton iteration solves a stage.
+struct ImplicitRhs {
+    std::function<void(const double*, double*, double, cudaStream_t)> f;
+    std::function<void(const double*, const double*, double*, cudaStream_t)> jvp;
+    std::function<void(const double*, double*, cudaStream_t)> diag;
+    std::function<void(double*, double, cudaStream_t)> callback;
+    bool callback_varies = false;
+    bool affine = false;
+};
+// TR-BDF2 on R over n unknowns; u0 and out are host arrays in the caller's numbering, perm (internal
+// -> caller) and iperm (caller -> internal) device index arrays.  Throws on error.
+int trbdf2_run(ImplicitRhs& R, const int32_t* perm, const int32_t* iperm, int64_t n, const double* u0,
+               const fvm_ode_options* o, double* out, fvm_ode_stats* st, fvm_implicit_stats* ist, void* stream);
 }  // namespace fvm

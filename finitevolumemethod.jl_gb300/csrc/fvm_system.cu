@@ -210,6 +210,87 @@ __global__ void __launch_bounds__(256) system_rhs_kernel(const SysArgs a, const 
     }
 }
 
+// The polynomial epilogue's share of the Jacobian, one thread per row.  With v: y += P'(u) v,
+// each monomial's derivative along v being sum_k v_{f_k} prod_{j != k} u_{f_j}.  Without v:
+// y[r] += dP_r/du_r, the diagonal.  Rows and components outside the mask get nothing, as in
+// the right-hand side.
+template <int N>
+__global__ void system_poly_jacobian_kernel(const double* __restrict__ u, const double* __restrict__ v,
+                                            double* __restrict__ y, const uint8_t* __restrict__ mask,
+                                            const double* __restrict__ vcoef, int64_t nrows, const SysTerms tm) {
+    const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= nrows) return;
+    double ui[N], vi[N], acc[N];
+    load_point<N, false>(u, row, ui);
+    if (v) load_point<N, false>(v, row, vi);
+#pragma unroll
+    for (int r = 0; r < N; ++r) acc[r] = 0.0;
+    for (int mo = 0; mo < tm.nmono; ++mo) {
+        const int nf = tm.nf[mo];
+        if (nf == 0) continue;  // a constant
+        // prod_{j != k} u_{f_j} for each factor k
+        double rest[3];
+        for (int k = 0; k < nf; ++k) {
+            double x = 1.0;
+            for (int j = 0; j < nf; ++j)
+                if (j != k) x *= pick<N>(ui, tm.f[mo][j]);
+            rest[k] = x;
+        }
+        double dv = 0.0;
+        if (v)
+            for (int k = 0; k < nf; ++k) dv = fma(pick<N>(vi, tm.f[mo][k]), rest[k], dv);
+#pragma unroll
+        for (int r = 0; r < N; ++r) {
+            const int t = tm.term[mo][r];
+            if (t < 0) continue;
+            double d = dv;
+            if (!v) {
+                d = 0.0;
+                for (int k = 0; k < nf; ++k)
+                    if (tm.f[mo][k] == r) d += rest[k];
+            }
+            const double c = tm.vary[t] < 0 ? tm.coef[t] : vcoef[(int64_t)tm.vary[t] * nrows + row];
+            acc[r] = fma(c, d, acc[r]);
+        }
+    }
+    const unsigned m = mask[row];
+#pragma unroll
+    for (int r = 0; r < N; ++r)
+        if ((m >> r) & 1u) y[row * N + r] += acc[r];
+}
+
+// the shared form's diagonal multipliers dmat[r][r]
+struct SysDiagMat {
+    double d[kSysMaxEq];
+};
+
+// diag[i][r] = K_rr[i][i], the diagonal blocks' diagonal entries, one thread per row
+__global__ void system_block_diag_kernel(const int64_t* slice_ptr, const int32_t* width, const int32_t* col,
+                                         const double* val, int64_t nslots, uint64_t blocks, int N, bool shared,
+                                         const SysDiagMat dm, int64_t nrows, double* diag) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nrows) return;
+    const int64_t s = i / 32;
+    const int lane = (int)(i - s * 32);
+    double g[kSysMaxEq];
+    for (int r = 0; r < N; ++r) g[r] = 0.0;
+    for (int k = 0; k < width[s]; ++k) {
+        const int64_t slot = slice_ptr[s] + (int64_t)k * 32 + lane;
+        if (col[slot] != i) continue;
+        for (int r = 0; r < N; ++r) {
+            const int bit = r * N + r;
+            if (!((blocks >> bit) & 1ull)) continue;
+            if (shared) {
+                g[r] += dm.d[r] * val[slot];
+            } else {
+                const int idx = __popcll(blocks & ((1ull << bit) - 1));  // rank among the stored blocks
+                g[r] += val[(int64_t)idx * nslots + slot];
+            }
+        }
+    }
+    for (int r = 0; r < N; ++r) diag[i * N + r] = g[r];
+}
+
 }  // namespace fvm
 
 using namespace fvm;
@@ -275,7 +356,9 @@ static void launch_system_vec(const SysArgs& a, const SysTerms& tm, int64_t nsli
 }
 
 template <int N>
-static void launch_system(const fvm_system* S, const double* u, double* du, const double* b, cudaStream_t s) {
+static void launch_system(const fvm_system* S, const double* u, double* du, const double* b, cudaStream_t s,
+                          const SysTerms* terms = nullptr) {
+    const SysTerms& tm = terms ? *terms : S->terms;
     const SellPattern& p = S->mesh->pat;
     if (p.nslices == 0) return;
     SysArgs a{p.d_slice_ptr.as<int64_t>(),
@@ -297,13 +380,13 @@ static void launch_system(const fvm_system* S, const double* u, double* du, cons
     const bool vec = N % 2 == 0 && ((uintptr_t)u % 16) == 0 && ((uintptr_t)du % 16) == 0;
     if (S->shared) {
         if (vec)
-            launch_system_vec<N, true, true>(a, S->terms, p.nslices, p.maxw, s);
+            launch_system_vec<N, true, true>(a, tm, p.nslices, p.maxw, s);
         else
-            launch_system_vec<N, false, true>(a, S->terms, p.nslices, p.maxw, s);
+            launch_system_vec<N, false, true>(a, tm, p.nslices, p.maxw, s);
     } else if (vec) {
-        launch_system_vec<N, true, false>(a, S->terms, p.nslices, p.maxw, s);
+        launch_system_vec<N, true, false>(a, tm, p.nslices, p.maxw, s);
     } else {
-        launch_system_vec<N, false, false>(a, S->terms, p.nslices, p.maxw, s);
+        launch_system_vec<N, false, false>(a, tm, p.nslices, p.maxw, s);
     }
 }
 
@@ -340,6 +423,43 @@ static void system_dirichlet_internal(const fvm_system* S, double* u, cudaStream
                               system_taus(S, t), S->ntime, u, S->ndir, s);
     else
         launch_dirichlet(S->d_dir_idx.as<int32_t>(), S->d_dir_val.as<double>(), u, S->ndir, s);
+}
+
+// J(u) v = K v + P'(u) v: the block operator on v with no constants and no polynomial terms, then
+// the polynomials' derivatives (time factors enter the constants only: J does not depend on t)
+template <int N>
+static void system_jacobian_n(const fvm_system* S, const double* u, const double* v, double* y, cudaStream_t s) {
+    const int64_t np = S->mesh->np;
+    const unsigned grid = (unsigned)((np + 255) / 256);
+    if (v) {
+        const SysTerms none{};
+        launch_system<N>(S, v, y, nullptr, s, &none);
+    } else {
+        const SellPattern& p = S->mesh->pat;
+        SysDiagMat dm{};
+        for (int r = 0; r < N; ++r) dm.d[r] = S->dmat[r * N + r];
+        system_block_diag_kernel<<<grid, 256, 0, s>>>(p.d_slice_ptr.as<int64_t>(), p.d_width.as<int32_t>(),
+                                                      p.d_col.as<int32_t>(), S->d_val.as<double>(), p.nslots,
+                                                      S->blocks, N, S->shared, dm, np, y);
+    }
+    if (S->terms.nmono > 0)
+        system_poly_jacobian_kernel<N><<<grid, 256, 0, s>>>(u, v, y, S->d_mask.as<uint8_t>(),
+                                                            S->nvary ? S->d_vcoef.as<double>() : nullptr, np, S->terms);
+}
+
+// v non-null: y = J(u) v; v null: y = diag J(u)
+static void system_jacobian_internal(const fvm_system* S, const double* u, const double* v, double* y, cudaStream_t s) {
+    switch (S->neq) {
+        case 1: system_jacobian_n<1>(S, u, v, y, s); break;
+        case 2: system_jacobian_n<2>(S, u, v, y, s); break;
+        case 3: system_jacobian_n<3>(S, u, v, y, s); break;
+        case 4: system_jacobian_n<4>(S, u, v, y, s); break;
+        case 5: system_jacobian_n<5>(S, u, v, y, s); break;
+        case 6: system_jacobian_n<6>(S, u, v, y, s); break;
+        case 7: system_jacobian_n<7>(S, u, v, y, s); break;
+        case 8: system_jacobian_n<8>(S, u, v, y, s); break;
+        default: fail(FVM_ERR_INVALID_ARGUMENT, "neq out of range");
+    }
 }
 
 static void create_system(fvm_mesh* m, const fvm_system_desc* d, fvm_system** out) {
@@ -762,6 +882,88 @@ int fvm_system_tsit5_solve(fvm_system* S, const double* u0, const fvm_ode_option
         FVM_CUDA(cudaStreamSynchronize(s));
         FVM_CUDA(cudaGetLastError());
         return FVM_OK;
+    });
+}
+
+}  // extern "C"
+
+namespace {
+
+// y = J(u) v (v non-null) or diag J(u), with u, v, y per the pointer-location flag
+void system_jacobian_entry(fvm_system* S, const double* u, const double* v, double* y, int32_t flags,
+                           cudaStream_t s) {
+    const int32_t loc = flags & 3;
+    if (loc > FVM_PTR_DEVICE_INTERNAL) fail(FVM_ERR_INVALID_ARGUMENT, "bad pointer-location flag");
+    if (loc == FVM_PTR_DEVICE_INTERNAL) {
+        system_jacobian_internal(S, u, v, y, s);
+        FVM_CUDA(cudaGetLastError());
+        return;
+    }
+    const int64_t n = S->n();
+    const int32_t* perm = S->d_perm.as<int32_t>();
+    DBuf w;
+    w.alloc(sizeof(double) * 4 * n);
+    double *ui = w.as<double>(), *vi = ui + n, *yi = ui + 2 * n, *st = ui + 3 * n;
+    auto in = [&](const double* src, double* dst) {
+        const double* from = src;
+        if (loc == FVM_PTR_HOST) {
+            FVM_CUDA(cudaMemcpyAsync(st, src, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+            from = st;
+        }
+        launch_permute_in(perm, from, dst, n, s);
+    };
+    in(u, ui);
+    if (v) in(v, vi);
+    system_jacobian_internal(S, ui, v ? vi : nullptr, yi, s);
+    double* dst = loc == FVM_PTR_HOST ? st : y;
+    launch_permute_out(perm, yi, dst, n, s);
+    if (loc == FVM_PTR_HOST) FVM_CUDA(cudaMemcpyAsync(y, st, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+    FVM_CUDA(cudaStreamSynchronize(s));
+    FVM_CUDA(cudaGetLastError());
+}
+
+}  // namespace
+
+extern "C" {
+
+int fvm_system_jvp(fvm_system* S, const double* u, const double* v, double* jv, double t, int32_t flags,
+                   void* stream) {
+    return guard_call([&] {
+        if (!S || !u || !v || !jv) fail(FVM_ERR_INVALID_ARGUMENT, "NULL argument");
+        (void)t;  // time factors enter the constants only
+        system_jacobian_entry(S, u, v, jv, flags, (cudaStream_t)stream);
+        return FVM_OK;
+    });
+}
+
+int fvm_system_jacobian_diagonal(fvm_system* S, const double* u, double* diag, double t, int32_t flags,
+                                 void* stream) {
+    return guard_call([&] {
+        if (!S || !u || !diag) fail(FVM_ERR_INVALID_ARGUMENT, "NULL argument");
+        (void)t;
+        system_jacobian_entry(S, u, nullptr, diag, flags, (cudaStream_t)stream);
+        return FVM_OK;
+    });
+}
+
+int fvm_system_trbdf2_solve(fvm_system* S, const double* u0, const fvm_ode_options* opt, double* out,
+                            fvm_ode_stats* stats, fvm_implicit_stats* istats, void* stream) {
+    return guard_call([&] {
+        if (!S) fail(FVM_ERR_INVALID_ARGUMENT, "NULL argument");
+        ImplicitRhs R;
+        R.f = [S](const double* y, double* du, double t, cudaStream_t s) { system_rhs_internal(S, y, du, s, t); };
+        R.jvp = [S](const double* u, const double* v, double* jv, cudaStream_t s) {
+            system_jacobian_internal(S, u, v, jv, s);
+        };
+        R.diag = [S](const double* u, double* d, cudaStream_t s) { system_jacobian_internal(S, u, nullptr, d, s); };
+        if (S->ndir > 0)
+            R.callback = [S](double* u, double t, cudaStream_t s) { system_dirichlet_internal(S, u, s, t); };
+        R.callback_varies = S->tdir_varies;
+        bool affine = true;  // no monomial of degree two or more
+        for (int mo = 0; mo < S->terms.nmono; ++mo) affine = affine && S->terms.nf[mo] <= 1;
+        R.affine = affine;
+        return trbdf2_run(R, S->d_perm.as<int32_t>(), S->d_iperm.as<int32_t>(), S->n(), u0, opt, out, stats, istats,
+                          stream);
     });
 }
 

@@ -196,6 +196,11 @@ SIGNATURES = {
     "fvm_system_dirichlet_apply": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_int32, C.c_void_p]),
     "fvm_system_tsit5_solve": (C.c_int, [C.c_void_p, c_double_p, C.POINTER(OdeOptions), c_double_p,
                                          C.POINTER(OdeStats), C.c_void_p]),
+    "fvm_system_jvp": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int32, C.c_void_p]),
+    "fvm_system_jacobian_diagonal": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int32,
+                                               C.c_void_p]),
+    "fvm_system_trbdf2_solve": (C.c_int, [C.c_void_p, c_double_p, C.POINTER(OdeOptions), c_double_p,
+                                          C.POINTER(OdeStats), C.POINTER(ImplicitStats), C.c_void_p]),
     "fvm_batch_create": (C.c_int, [C.c_void_p, C.c_int32, c_double_p, c_double_p, C.c_int32,
                                    C.POINTER(C.c_void_p)]),
     "fvm_batch_destroy": (C.c_int, [C.c_void_p]),

@@ -972,7 +972,7 @@ class FVMSystem:
     def rhs(self, du, u, t=0.0, internal=False, stream=None):
         """fvm_eqs!(du, u, p, t) for the system; u, du (N, npoints).  internal=True takes device
         tensors already in the library's internal point numbering (a device-resident loop's)."""
-        up, ul, _ = self._flat(u, "u")
+        up, ul, uh = self._flat(u, "u")  # uh keeps the staged copy alive
         dp, dl, dh = self._flat(du, "du")
         if ul != dl:
             raise TypeError("u and du must both be host arrays or both device tensors")
@@ -985,6 +985,31 @@ class FVMSystem:
         if dh is not None:
             du[...] = dh.T
         return du
+
+    def jvp(self, u, v, t=0.0, stream=None):
+        """J(u) v of the system's fvm_eqs! (exact); u, v (N, npoints), returned alike."""
+        out = np.empty_like(u) if isinstance(u, np.ndarray) else u.new_empty((u.shape[1], u.shape[0])).T
+        up, ul, uh = self._flat(u, "u")  # the staged host copies must outlive the call
+        vp, vl, vh = self._flat(v, "v")
+        op, ol, oh = self._flat(out, "jv")
+        if not (ul == vl == ol):
+            raise TypeError("u and v must both be host arrays or both device tensors")
+        s = stream if stream is not None else _lib.current_stream_handle()
+        check(load().fvm_system_jvp(self._h, up, vp, op, float(t), ul, s))
+        if oh is not None:
+            out[...] = oh.T
+        return out
+
+    def jacobian_diagonal(self, u, t=0.0, stream=None):
+        """diag J(u) of the system's fvm_eqs!, (N, npoints)."""
+        out = np.empty_like(u) if isinstance(u, np.ndarray) else u.new_empty((u.shape[1], u.shape[0])).T
+        up, ul, uh = self._flat(u, "u")
+        op, _, oh = self._flat(out, "diag")
+        s = stream if stream is not None else _lib.current_stream_handle()
+        check(load().fvm_system_jacobian_diagonal(self._h, up, op, float(t), ul, s))
+        if oh is not None:
+            out[...] = oh.T
+        return out
 
     def update_dirichlet_nodes(self, u, t=0.0, stream=None):
         """update_dirichlet_nodes! for the system, in place; u (N, npoints)."""
@@ -1427,7 +1452,7 @@ class TRBDF2:
     """TR-BDF2 (the implicit method of the reference's tutorials), on the device: simplified
     Newton per stage, matrix-free BiCGStab on W = I - d h J with the exact Jacobian-vector
     product of fvm_eqs!, diag(W) as preconditioner; adaptive with TR-BDF2's error estimate
-    (dt given with adaptive=False: fixed steps).  FVMProblem, DiffusionEquation and
+    (dt given with adaptive=False: fixed steps).  FVMProblem, FVMSystem, DiffusionEquation and
     LinearReactionDiffusionEquation (J = A)."""
 
     def __repr__(self):
@@ -1438,6 +1463,8 @@ def jvp(prob, u, v, t=0.0, stream=None):
     """J(u) v, the Jacobian-vector product of fvm_eqs! (exact for every device-coded form).
     u, v host float64 arrays or CUDA tensors (caller numbering); returns J(u) v of their kind."""
     prob = _prob_of(prob)
+    if isinstance(prob, FVMSystem):
+        return prob.jvp(u, v, t, stream)
     out = np.empty_like(u) if isinstance(u, np.ndarray) else u.new_empty(u.shape)
     up, ul = _lib.array_pointer(u)
     vp, vl = _lib.array_pointer(v)
@@ -1452,6 +1479,8 @@ def jvp(prob, u, v, t=0.0, stream=None):
 def jacobian_diagonal(prob, u, t=0.0, stream=None):
     """diag J(u) of fvm_eqs! (the Jacobi preconditioner of a Newton-Krylov solve)."""
     prob = _prob_of(prob)
+    if isinstance(prob, FVMSystem):
+        return prob.jacobian_diagonal(u, t, stream)
     out = np.empty_like(u) if isinstance(u, np.ndarray) else u.new_empty(u.shape)
     up, ul = _lib.array_pointer(u)
     op, _ = _lib.array_pointer(out)
@@ -1590,12 +1619,21 @@ def solve(prob, alg=None, *, saveat=None, dt=None, adaptive=None, abstol=1e-6, r
     if isinstance(prob, _TimeTemplate):
         check(lib.fvm_template_tsit5_solve(prob.handle, dptr(u0c), C.byref(o), dptr(out), C.byref(st), s))
         us = [np.append(row, 1.0) for row in out]  # the augmented component of the MatrixOperator form
+    elif isinstance(prob, FVMSystem) and isinstance(alg, TRBDF2):
+        ist = _lib.ImplicitStats()
+        check(lib.fvm_system_trbdf2_solve(prob.handle, dptr(u0c), C.byref(o), dptr(out), C.byref(st), C.byref(ist),
+                                          s))
+        return ODESolution(ts, [row.T for row in out],
+                           {"naccept": st.naccept, "nreject": st.nreject, "nrhs": st.nrhs, "t_final": st.t_final,
+                            "elapsed_ms": st.elapsed_ms, "driver": "host", "newton_iters": ist.newton_iters,
+                            "krylov_iters": ist.krylov_iters, "jvps": ist.jvps,
+                            "newton_failures": ist.newton_failures})
     elif isinstance(prob, FVMSystem):
         check(lib.fvm_system_tsit5_solve(prob.handle, dptr(u0c), C.byref(o), dptr(out), C.byref(st), s))
         us = [row.T for row in out]  # (N, npoints) views: entry (j, i) is component j at node i
     elif isinstance(alg, TRBDF2):
         if not isinstance(prob, FVMProblem):
-            raise TypeError("TRBDF2 runs on an FVMProblem or a time-dependent template")
+            raise TypeError("TRBDF2 runs on an FVMProblem, an FVMSystem or a time-dependent template")
         ist = _lib.ImplicitStats()
         check(lib.fvm_trbdf2_solve(prob.handle, dptr(u0c), C.byref(o), dptr(out), C.byref(st), C.byref(ist), s))
         us = list(out)

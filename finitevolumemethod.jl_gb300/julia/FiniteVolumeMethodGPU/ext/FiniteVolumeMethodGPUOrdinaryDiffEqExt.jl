@@ -48,6 +48,7 @@ function gpu_trbdf2(prob, alg; saveat = nothing, dt = nothing, adaptive = true, 
     return gpu_solution(alg, ts, us)
 end
 CommonSolve.solve(prob::FVM.FVMProblem, alg::TRBDF2; kwargs...) = gpu_trbdf2(prob, alg; kwargs...)
+CommonSolve.solve(sys::FVM.FVMSystem, alg::TRBDF2; kwargs...) = gpu_trbdf2(sys, alg; kwargs...)
 CommonSolve.solve(tmpl::FVM.DiffusionEquation, alg::TRBDF2; kwargs...) = gpu_trbdf2(tmpl, alg; kwargs...)
 CommonSolve.solve(tmpl::FVM.LinearReactionDiffusionEquation, alg::TRBDF2; kwargs...) = gpu_trbdf2(tmpl, alg; kwargs...)
 CommonSolve.solve(sys::FVM.FVMSystem, alg::Tsit5; kwargs...) = gpu_tsit5(sys, alg; kwargs...)

@@ -579,6 +579,41 @@ function solve(gs::GPUSystem; saveat, dt = nothing, abstol = 1e-6, reltol = 1e-3
     return ts, [out[:, :, k] for k in eachindex(ts)]
 end
 
+"""
+    jvp!(jv, u, v, gs::GPUSystem, t)
+
+`jv = J(u) v` for the system's `fvm_eqs!` (N x npoints matrices), exact.
+"""
+function jvp!(jv::Matrix{Float64}, u::Matrix{Float64}, v::Matrix{Float64}, gs::GPUSystem, t)
+    check(ccall((:fvm_system_jvp, libfvmgpu), Cint,
+        (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Float64, Int32, Ptr{Cvoid}),
+        gs.handle, u, v, jv, t, FVM_PTR_HOST, C_NULL))
+    return jv
+end
+
+"""
+    solve_trbdf2(gs::GPUSystem; saveat, dt = nothing, abstol = 1e-6, reltol = 1e-3)
+
+TR-BDF2 on the system (the Brusselator and Gray-Scott tutorials' `solve(system, TRBDF2(...))`).
+Returns `(t, u, stats)` with `u[k]` the N x npoints state at `t[k]`.
+"""
+function solve_trbdf2(gs::GPUSystem; saveat, dt = nothing, abstol = 1e-6, reltol = 1e-3, max_steps = 0)
+    sys = gs.sys
+    t0, tf = sys.initial_time, sys.final_time
+    ts = saveat isa Number ? collect(t0:saveat:tf) : collect(Float64, saveat)
+    N, np = size(sys.initial_condition)
+    out = Array{Float64}(undef, N, np, length(ts))
+    u0 = Matrix{Float64}(sys.initial_condition)
+    opt = OdeOptions(t0, tf, dt === nothing ? 0.0 : dt, dt === nothing ? Int32(1) : Int32(0), abstol, reltol,
+        max_steps, pointer(ts), length(ts), Int32(0), Int32(0))
+    st = OdeStats(0, 0, 0, 0.0, 0.0, Int32(0))
+    ist = ImplicitStats(0, 0, 0, 0)
+    GC.@preserve ts check(ccall((:fvm_system_trbdf2_solve, libfvmgpu), Cint,
+        (Ptr{Cvoid}, Ptr{Float64}, Ref{OdeOptions}, Ptr{Float64}, Ref{OdeStats}, Ref{ImplicitStats}, Ptr{Cvoid}),
+        gs.handle, u0, opt, out, st, ist, C_NULL))
+    return ts, [out[:, :, k] for k in eachindex(ts)], ist
+end
+
 # ---- templates (src/specific_problems/) ----------------------------------------------------
 mutable struct GPUTemplate{T}
     tmpl::T

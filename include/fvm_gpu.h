@@ -326,6 +326,18 @@ int fvm_system_dirichlet_apply(fvm_system* sys, double* u, double t, int32_t fla
  * out [nsave][npoints][neq] are host arrays in the caller's numbering. */
 int fvm_system_tsit5_solve(fvm_system* sys, const double* u0, const fvm_ode_options* opt, double* out,
                            fvm_ode_stats* stats, void* stream);
+/* Jacobian-vector product of the system's fvm_eqs!: jv = J(u) v, exact (block operator plus the
+ * derivatives of the source / Dudt polynomials).  u, v, jv [npoints][neq] per flags (FVM_PTR_*). */
+int fvm_system_jvp(fvm_system* sys, const double* u, const double* v, double* jv, double t, int32_t flags,
+                   void* stream);
+/* diag J(u), [npoints][neq] per flags (FVM_PTR_*). */
+int fvm_system_jacobian_diagonal(fvm_system* sys, const double* u, double* diag, double t, int32_t flags,
+                                 void* stream);
+/* TR-BDF2 on the system (solve(prob::FVMSystem, TRBDF2()), the integrator of the reference's
+ * reaction-diffusion system tutorials), as fvm_trbdf2_solve; u0 [npoints][neq] and out
+ * [nsave][npoints][neq] host arrays in the caller's numbering. */
+int fvm_system_trbdf2_solve(fvm_system* sys, const double* u0, const fvm_ode_options* opt, double* out,
+                            fvm_ode_stats* stats, fvm_implicit_stats* istats, void* stream);
 
 /* ---- batched instances (many parameter sets on one mesh) -------------------------------- */
 /* B instances of one linear problem that differ in their diffusion field D_b(x, y), the

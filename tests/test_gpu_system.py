@@ -391,3 +391,119 @@ def test_brusselator_tutorial_mesh_converges_to_exact_solution(gpu_lib):
         ex = brusselator_exact(spec.tri.points, 1.0)
         errs.append(max(np.max(np.abs(sol.u[-1][c] - ex[c])) / np.max(ex[c]) for c in range(2)))
     assert errs[1] < 1e-3 and errs[1] < 0.5 * errs[0], errs
+
+
+def _flat_oracle(osys, N):
+    """The oracle's system fvm_eqs! on states flattened [point][component] (the numbering of
+    jacobian_sparsity(tri, N): node i's unknowns i N + l)."""
+    return lambda x, t: O.system_fvm_eqs(osys, x.reshape(-1, N).T, t).T.ravel()
+
+
+@pytest.mark.parametrize("make", [lambda: gray_scott(12), mixed_system, lambda: brusselator(10),
+                                  cross_diffusion_system])
+def test_system_jvp_and_diagonal_against_oracle(gpu_lib, make):
+    """J(u) v of the system (block operator plus the polynomial derivatives, stored and shared
+    block forms) against central differences of the oracle's system fvm_eqs!, and diag J
+    against the oracle's coloured finite-difference Jacobian."""
+    import torch
+
+    import fvmgpu as F
+
+    spec = make()
+    osys, sys = spec.oracle(), spec.api()
+    N, n = spec.u0.shape
+    rng = np.random.default_rng(11)
+    u = spec.u0 + 0.1 * rng.standard_normal(spec.u0.shape)
+    v = rng.standard_normal(spec.u0.shape)
+    t = 0.3
+    got = F.jvp(sys, u, v, t)
+    eps = 1e-5
+    fd = (O.system_fvm_eqs(osys, u + eps * v, t) - O.system_fvm_eqs(osys, u - eps * v, t)) / (2 * eps)
+    assert np.max(np.abs(got - fd)) <= 1e-7 * np.max(np.abs(fd))
+    dev = lambda a: torch.tensor(np.ascontiguousarray(a.T), device="cuda").T  # noqa: E731
+    got_d = F.jvp(sys, dev(u), dev(v), t)
+    assert np.array_equal(got_d.cpu().numpy(), got)
+    ent, nn = O.jacobian_sparsity(spec.tri, N)
+    J = O.colored_jacobian(_flat_oracle(osys, N), u.T.ravel(), t, ent, nn)
+    want = J.diagonal().reshape(n, N).T
+    diag = F.jacobian_diagonal(sys, u, t)
+    assert np.max(np.abs(diag - want)) <= 1e-6 * np.max(np.abs(want))
+
+
+def _oracle_system_trbdf2(spec, saveat, **kw):
+    osys = spec.oracle()
+    N = spec.u0.shape[0]
+    f = _flat_oracle(osys, N)
+    ent, nn = O.jacobian_sparsity(spec.tri, N)
+    jac = lambda x, t: O.colored_jacobian(f, x, t, ent, nn)  # noqa: E731
+    cb = lambda x, t: O.system_update_dirichlet_nodes(osys, x.reshape(-1, N).T, t).T.ravel()  # noqa: E731
+    ref, st = O.trbdf2_solve(f, jac, spec.u0.T.ravel(), spec.t0, spec.tf, saveat, callback=cb, **kw)
+    return np.array([r.reshape(-1, N).T for r in ref]), st
+
+
+def test_system_trbdf2_matches_oracle(gpu_lib):
+    """TR-BDF2 on a 12 x 12 Brusselator (nonlinear sources, time-dependent Dirichlet and Neumann
+    values) to t = 0.2 at tight tolerances: Newton with the exact device JVP against the
+    oracle's with a finite-difference Jacobian and exact sparse solves."""
+    import fvmgpu as F
+
+    spec = brusselator(12, tf=0.2)
+    sys = spec.api()
+    saveat = [0.0, 0.1, 0.2]
+    sol = F.solve(sys, F.TRBDF2(), saveat=saveat, abstol=1e-8, reltol=1e-8)
+    ref, st = _oracle_system_trbdf2(spec, saveat, abstol=1e-8, reltol=1e-8)
+    assert abs(sol.stats["naccept"] - st["naccept"]) <= 2
+    got = np.array(sol.u)
+    assert np.max(np.abs(got - ref)) <= 1e-6 * np.max(np.abs(ref))
+
+
+def test_system_trbdf2_mixed_forms_fixed_step(gpu_lib):
+    """Fixed-step TR-BDF2 on the three-component system with every device-coded form (Dudt
+    and Neumann boundaries coupled across components, internal Dirichlet and Dudt nodes, cubic
+    sources): the oracle's steps, 1e-7 of max|u|."""
+    import fvmgpu as F
+
+    spec = mixed_system()
+    spec.tf = 0.01
+    sys = spec.api()
+    saveat = [0.0, 0.005, 0.01]
+    sol = F.solve(sys, F.TRBDF2(), saveat=saveat, dt=1e-3, adaptive=False)
+    ref, st = _oracle_system_trbdf2(spec, saveat, dt=1e-3, adaptive=False)
+    assert sol.stats["naccept"] == st["naccept"] == 10
+    got = np.array(sol.u)
+    assert np.max(np.abs(got - ref)) <= 1e-7 * np.max(np.abs(ref))
+
+
+def test_system_trbdf2_affine_takes_one_newton_iteration(gpu_lib):
+    """A system with no product of components (the cross-diffusion system) is affine: one
+    Newton iteration per stage, and the oracle's steps."""
+    import fvmgpu as F
+
+    spec = cross_diffusion_system()
+    spec.tf = 0.05
+    sys = spec.api()
+    saveat = [0.0, 0.05]
+    sol = F.solve(sys, F.TRBDF2(), saveat=saveat)
+    ref, st = _oracle_system_trbdf2(spec, saveat, affine=True)
+    assert sol.stats["naccept"] == st["naccept"]
+    assert sol.stats["newton_iters"] == 2 * (sol.stats["naccept"] + sol.stats["nreject"])
+    got = np.array(sol.u)
+    assert np.max(np.abs(got - ref)) <= 1e-8 * np.max(np.abs(ref))
+
+
+def test_brusselator_tutorial_trbdf2(gpu_lib):
+    """The tutorial's call, solve(system, TRBDF2(), saveat = 1.0) on the 100 x 100 mesh to t = 5:
+    A-stable steps set by accuracy, not the diffusion limit (measured 363 against Tsit5's
+    28,988), and the exact solution within the integration tolerance (largest relative error
+    over the saves measured 9.7e-3; default-tolerance Tsit5 on the same mesh: 2.8e-2)."""
+    import fvmgpu as F
+
+    spec = brusselator(100, tf=5.0)
+    sys = spec.api()
+    saveat = np.arange(0.0, 5.0 + 1e-12, 1.0)
+    sol = F.solve(sys, F.TRBDF2(), saveat=saveat)
+    assert sol.stats["naccept"] < 500
+    for k, t in enumerate(saveat):
+        ex = brusselator_exact(spec.tri.points, t)
+        err = max(np.max(np.abs(sol.u[k][c] - ex[c])) / np.max(ex[c]) for c in range(2))
+        assert err < 2e-2, (t, err)
