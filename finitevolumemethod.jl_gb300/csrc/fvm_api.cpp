@@ -85,6 +85,7 @@ static double host_rms(const std::vector<double>& v, const std::vector<double>& 
 static void tsit5_run(OdeRhs& rhs, int64_t n, const double* u0_int, const fvm_ode_options& o, double* out_int,
                       fvm_ode_stats* st, cudaStream_t user_stream) {
     if (!(o.tf > o.t0)) fail(FVM_ERR_INVALID_ARGUMENT, "final time must exceed the initial time");
+    if (!std::isfinite(o.tf)) fail(FVM_ERR_INVALID_ARGUMENT, "the final time must be finite (a steady problem is solved by fvm_steady_solve)");
     CaptureStream cs(user_stream, o.use_graph != 0);
     cudaStream_t s = cs.s;
     std::vector<double> saveat;

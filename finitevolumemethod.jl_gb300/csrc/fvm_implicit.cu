@@ -112,6 +112,41 @@ __global__ void wdiag_kernel(const double* dj, double c, double* dw, int64_t n) 
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) dw[i] = 1.0 - c * dj[i];
 }
+// W = F - c J with F = diag(mask) (steady Newton): out = mask x - c out, out holding J x
+__global__ void wmask_kernel(double* out, const double* x, const double* mask, double c, int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = mask[i] * x[i] - c * out[i];
+}
+// its diagonal mask - c diagJ; a zero (a row that does not depend on its own value) taken as 1
+__global__ void wdiag_mask_kernel(const double* dj, const double* mask, double c, double* dw, int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double d = mask[i] - c * dj[i];
+    dw[i] = d != 0.0 ? d : 1.0;
+}
+// max|f| and max|f + u|, partials per block: part[2 b], part[2 b + 1]
+__global__ void maxabs2_kernel(const double* f, const double* u, int64_t n, double* part) {
+    __shared__ double red[2][kThreads];
+    double m0 = 0.0, m1 = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        m0 = fmax(m0, fabs(f[i]));
+        m1 = fmax(m1, fabs(f[i] + u[i]));
+    }
+    red[0][threadIdx.x] = m0;
+    red[1][threadIdx.x] = m1;
+    __syncthreads();
+    for (int w = kThreads / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) {
+            red[0][threadIdx.x] = fmax(red[0][threadIdx.x], red[0][threadIdx.x + w]);
+            red[1][threadIdx.x] = fmax(red[1][threadIdx.x], red[1][threadIdx.x + w]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        part[2 * blockIdx.x] = red[0][0];
+        part[2 * blockIdx.x + 1] = red[1][0];
+    }
+}
 // the diagonal of a sliced-ELL operator: padding slots name the row itself with value 0
 template <class V>
 __global__ void sell_diag_kernel(const int64_t* slice_ptr, const int32_t* width, const int32_t* col, const V* val,
@@ -265,6 +300,16 @@ struct Reducer {
         dot2(a, b, nullptr, nullptr, n, r0, r1, s);
         return r0;
     }
+    // max|f| and max|f + u| (NaN propagates as a failed test: fmax drops it, so check finiteness)
+    void maxabs2(const double* f, const double* u, int64_t n, double& m0, double& m1, cudaStream_t s) {
+        maxabs2_kernel<<<kParts, kThreads, 0, s>>>(f, u, n, part.as<double>());
+        fetch(2 * kParts, s);
+        m0 = m1 = 0.0;
+        for (int b = 0; b < kParts; ++b) {
+            m0 = std::max(m0, host[2 * b]);
+            m1 = std::max(m1, host[2 * b + 1]);
+        }
+    }
     // RMS of x / (abstol + reltol max(|a|, |b|))
     double wrms(const double* x, const double* a, const double* b, double abstol, double reltol, int64_t n,
                 cudaStream_t s) {
@@ -338,6 +383,7 @@ struct Trbdf2 {
     int64_t nrhs = 0, newton = 0, krylov = 0, jvps = 0, newton_fail = 0;
     double wd = 0;  // d h of the current W
     const double* wu = nullptr;  // J's point
+    const double* wmask = nullptr;  // null: W = I - wd J; else W = diag(wmask) - wd J
 
     Trbdf2(ImplicitRhs* R_, int64_t n_, cudaStream_t s_, double at, double rt)
         : R(R_), n(n_), s(s_), abstol(at), reltol(rt) {
@@ -355,7 +401,10 @@ struct Trbdf2 {
     }
     void wmul(const double* xin, double* out) {  // out = xin - d h J(wu) xin (two per BiCGStab iteration)
         R->jvp(wu, xin, out, s);
-        lin(out, lin2(xin, 1.0, out, -wd), n, s);
+        if (wmask)
+            wmask_kernel<<<blocks_for(n), kThreads, 0, s>>>(out, xin, wmask, wd, n);
+        else
+            lin(out, lin2(xin, 1.0, out, -wd), n, s);
     }
     // W at u_n with d h: its diagonal for the preconditioner; the captured iteration chunk of
     // the previous W is dropped
@@ -364,7 +413,10 @@ struct Trbdf2 {
         wu = at;
         wd = dh;
         R->diag(at, dj, s);
-        wdiag_kernel<<<blocks_for(n), kThreads, 0, s>>>(dj, dh, dw, n);
+        if (wmask)
+            wdiag_mask_kernel<<<blocks_for(n), kThreads, 0, s>>>(dj, wmask, dh, dw, n);
+        else
+            wdiag_kernel<<<blocks_for(n), kThreads, 0, s>>>(dj, dh, dw, n);
     }
     // x = W^-1 b by right-preconditioned BiCGStab to ||b - W x|| <= rtol ||b||; x starts at 0.
     // The iterations run without host round trips; the host reads the scalars every kCheck.
@@ -466,6 +518,27 @@ struct Trbdf2 {
     }
 };
 
+// a stream that can be captured (the legacy default stream cannot): the caller's, or one of ours
+// ordered after the default stream's earlier work
+struct CapturableStream {
+    cudaStream_t s = nullptr, own = nullptr;
+    explicit CapturableStream(void* stream) : s((cudaStream_t)stream) {
+        if (!s || s == cudaStreamLegacy || s == cudaStreamPerThread) {
+            FVM_CUDA(cudaDeviceSynchronize());
+            FVM_CUDA(cudaStreamCreateWithFlags(&own, cudaStreamNonBlocking));
+            s = own;
+        }
+    }
+    CapturableStream(const CapturableStream&) = delete;
+    CapturableStream& operator=(const CapturableStream&) = delete;
+    ~CapturableStream() {
+        if (own) {
+            cudaStreamSynchronize(own);
+            cudaStreamDestroy(own);
+        }
+    }
+};
+
 }  // namespace
 }  // namespace fvm
 
@@ -474,34 +547,23 @@ using namespace fvm;
 // TR-BDF2 on R over n unknowns: u0 and out are host arrays in the caller's numbering, perm /
 // iperm the device permutations between it and the internal one.
 int fvm::trbdf2_run(ImplicitRhs& R, const int32_t* perm, const int32_t* iperm, int64_t n, const double* u0,
-                    const fvm_ode_options* o, double* out, fvm_ode_stats* st, fvm_implicit_stats* ist, void* stream) {
+                    const fvm_ode_options* o, double* out, fvm_ode_stats* st, fvm_implicit_stats* ist, void* stream,
+                    SteadyStop* stop) {
     {
         if (!u0 || !o || !out) fail(FVM_ERR_INVALID_ARGUMENT, "NULL argument");
         if (!(o->tf > o->t0)) fail(FVM_ERR_INVALID_ARGUMENT, "final time must exceed the initial time");
+        if (!stop && !std::isfinite(o->tf)) fail(FVM_ERR_INVALID_ARGUMENT, "the final time must be finite");
         if (!o->adaptive && !(o->dt > 0)) fail(FVM_ERR_INVALID_ARGUMENT, "dt must be positive for fixed steps");
-        // a stream that can be captured (the legacy default stream cannot): the caller's, or one
-        // of ours ordered after the default stream's earlier work
-        cudaStream_t s = (cudaStream_t)stream;
-        struct OwnStream {
-            cudaStream_t s = nullptr;
-            ~OwnStream() {
-                if (s) {
-                    cudaStreamSynchronize(s);
-                    cudaStreamDestroy(s);
-                }
-            }
-        } own;
-        if (!s || s == cudaStreamLegacy || s == cudaStreamPerThread) {
-            FVM_CUDA(cudaDeviceSynchronize());
-            FVM_CUDA(cudaStreamCreateWithFlags(&own.s, cudaStreamNonBlocking));
-            s = own.s;
-        }
+        CapturableStream cs(stream);
+        cudaStream_t s = cs.s;
         std::vector<double> saveat;
-        if (o->saveat && o->nsave > 0)
+        if (stop)
+            saveat.push_back(INFINITY);  // one output, the u that passes the test (saved at the end)
+        else if (o->saveat && o->nsave > 0)
             saveat.assign(o->saveat, o->saveat + o->nsave);
         else
             saveat.push_back(o->tf);
-        for (size_t i = 0; i < saveat.size(); ++i) {
+        for (size_t i = 0; i < saveat.size() && !stop; ++i) {
             if (saveat[i] < o->t0 || saveat[i] > o->tf) fail(FVM_ERR_INVALID_ARGUMENT, "saveat times must lie in [t0, tf]");
             if (i && saveat[i] < saveat[i - 1]) fail(FVM_ERR_INVALID_ARGUMENT, "saveat must be sorted");
         }
@@ -538,8 +600,11 @@ int fvm::trbdf2_run(ImplicitRhs& R, const int32_t* perm, const int32_t* iperm, i
         int64_t nacc = 0, nrej = 0, step = 0;
         bool first_cb = true;
         while (t < o->tf) {
-            if (step >= max_steps) fail(FVM_ERR_STEP_LIMIT, "TRBDF2 reached max_steps before tf");
-            const bool last = t + h >= o->tf - 1e-12 * tspan;
+            if (step >= max_steps) {
+                if (stop) break;  // not converged: the caller reports it
+                fail(FVM_ERR_STEP_LIMIT, "TRBDF2 reached max_steps before tf");
+            }
+            const bool last = std::isfinite(o->tf) && t + h >= o->tf - 1e-12 * tspan;
             const double hh = last ? o->tf - t : h;
             ++step;
             // z_n = h f_n; W = I - d h J(u_n)
@@ -607,6 +672,15 @@ int fvm::trbdf2_run(ImplicitRhs& R, const int32_t* perm, const int32_t* iperm, i
                 first_cb = false;
             }
             while (si < saveat.size() && saveat[si] == t) save(M.u);
+            if (stop) {  // f_n is f at the updated u
+                double m0, m1;
+                M.red.maxabs2(M.fn, M.u, n, m0, m1, s);
+                stop->residual = m0;
+                if (m0 <= stop->abstol || m0 <= stop->reltol * m1) {
+                    stop->converged = true;
+                    break;
+                }
+            }
             if (o->adaptive) {
                 const double q = err > 0 ? 0.9 * std::pow(err, -1.0 / 3.0) : 10.0;
                 h = std::min(tspan, hh * std::min(10.0, std::max(0.2, q)));
@@ -639,6 +713,105 @@ int fvm::trbdf2_run(ImplicitRhs& R, const int32_t* perm, const int32_t* iperm, i
         }
         return FVM_OK;
     }
+}
+
+// NewtonRaphson on f(u, t) = 0: (F - J(u)) du = f(u) by the Krylov solver of the stages, F the
+// identity on the fixed rows (R.fixed), until the steady test passes
+static void newton_run(ImplicitRhs& R, const int32_t* perm, const int32_t* iperm, int64_t n, const double* u0,
+                       const fvm_steady_options* o, double* out, fvm_steady_stats* st, bool& converged,
+                       void* stream) {
+    CapturableStream cs(stream);
+    cudaStream_t s = cs.s;
+    if (!R.fixed) fail(FVM_ERR_INVALID_ARGUMENT, "Newton needs the fixed-row mask");
+    Trbdf2 M(&R, n, s, 1.0, 0.0);
+    M.wmask = R.fixed;
+    DBuf d_in;
+    d_in.alloc(sizeof(double) * n);
+    FVM_CUDA(cudaMemcpyAsync(d_in.p, u0, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    launch_permute_in(perm, d_in.as<double>(), M.u, n, s);
+    cudaEvent_t e0, e1;
+    FVM_CUDA(cudaEventCreate(&e0));
+    FVM_CUDA(cudaEventCreate(&e1));
+    FVM_CUDA(cudaEventRecord(e0, s));
+    if (R.callback) R.callback(M.u, o->t, s);
+    const int64_t max_it = o->max_iters > 0 ? o->max_iters : 50;
+    int64_t it = 0;
+    double res = INFINITY;
+    converged = false;
+    for (;; ++it) {
+        M.rhs(M.u, M.fn, o->t);
+        double m1;
+        M.red.maxabs2(M.fn, M.u, n, res, m1, s);
+        if (!std::isfinite(res)) break;
+        if (res <= o->abstol || res <= o->reltol * m1) {
+            converged = true;
+            break;
+        }
+        if (it >= max_it) break;
+        ++M.newton;
+        M.set_w(M.u, 1.0);  // W = F - J(u)
+        FVM_CUDA(cudaMemcpyAsync(M.est, M.fn, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+        if (!M.solve(M.est, M.x, 1e-10, 20000)) break;
+        lin(M.u, lin2(M.u, 1.0, M.x, 1.0), n, s);
+    }
+    FVM_CUDA(cudaEventRecord(e1, s));
+    FVM_CUDA(cudaEventSynchronize(e1));
+    float ms = 0;
+    FVM_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    snapshots_to_host(iperm, M.u, out, n, 1, s);
+    FVM_CUDA(cudaStreamSynchronize(s));
+    FVM_CUDA(cudaGetLastError());
+    if (st) {
+        st->iterations = M.newton;
+        st->krylov_iters = M.krylov;
+        st->jvps = M.jvps;
+        st->nrhs = M.nrhs;
+        st->residual = res;
+        st->t_final = o->t;
+        st->elapsed_ms = ms;
+    }
+}
+
+void fvm::steady_run(ImplicitRhs& R, const int32_t* perm, const int32_t* iperm, int64_t n, const double* u0,
+                     const fvm_steady_options* o, double* out, fvm_steady_stats* st, void* stream) {
+    if (!u0 || !o || !out) fail(FVM_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (!(o->abstol >= 0) || !(o->reltol >= 0)) fail(FVM_ERR_INVALID_ARGUMENT, "tolerances must be non-negative");
+    if (st) *st = fvm_steady_stats{};
+    bool converged = false;
+    if (o->method == FVM_STEADY_NEWTON) {
+        newton_run(R, perm, iperm, n, u0, o, out, st, converged, stream);
+    } else if (o->method == FVM_STEADY_DYNAMIC) {
+        if (!(o->tmax > o->t)) fail(FVM_ERR_INVALID_ARGUMENT, "tmax must exceed t");
+        fvm_ode_options od{};
+        od.t0 = o->t;
+        od.tf = o->tmax;
+        od.adaptive = 1;
+        od.abstol = o->ode_abstol > 0 ? o->ode_abstol : 1e-6;
+        od.reltol = o->ode_reltol > 0 ? o->ode_reltol : 1e-3;
+        od.max_steps = o->max_iters > 0 ? o->max_iters : 100000;
+        SteadyStop stop;
+        stop.abstol = o->abstol;
+        stop.reltol = o->reltol;
+        stop.residual = INFINITY;
+        fvm_ode_stats os{};
+        fvm_implicit_stats is{};
+        trbdf2_run(R, perm, iperm, n, u0, &od, out, &os, &is, stream, &stop);
+        converged = stop.converged;
+        if (st) {
+            st->iterations = os.naccept;
+            st->krylov_iters = is.krylov_iters;
+            st->jvps = is.jvps;
+            st->nrhs = os.nrhs;
+            st->residual = stop.residual;
+            st->t_final = os.t_final;
+            st->elapsed_ms = os.elapsed_ms;
+        }
+    } else {
+        fail(FVM_ERR_INVALID_ARGUMENT, "unknown steady method");
+    }
+    if (!converged) fail(FVM_ERR_NOT_CONVERGED, "the steady-state test was not met");
 }
 
 extern "C" {
@@ -757,6 +930,34 @@ int fvm_template_trbdf2_solve(fvm_template* T, const double* u0, const fvm_ode_o
         };
         R.affine = true;
         return trbdf2_run(R, m->d_perm.as<int32_t>(), m->d_iperm.as<int32_t>(), m->np, u0, o, out, st, ist, stream);
+    });
+}
+
+int fvm_steady_solve(fvm_problem* p, const double* u0, const fvm_steady_options* o, double* out,
+                     fvm_steady_stats* st, void* stream) {
+    return guard_call([&] {
+        if (!p) fail(FVM_ERR_INVALID_ARGUMENT, "NULL argument");
+        if (p->conditions_only) fail(FVM_ERR_INVALID_ARGUMENT, "this problem carries a template's conditions only");
+        fvm_mesh* m = p->mesh;
+        // the rows the problem fixes: Dirichlet points and points in no triangle (du = 0 there)
+        std::vector<double> fixed((size_t)m->np, 0.0);
+        for (int64_t v = 0; v < m->np; ++v)
+            if (p->code[v] == FVM_VERTEX_DIRICHLET || p->code[v] == FVM_VERTEX_NOT_A_VERTEX) fixed[m->iperm[v]] = 1.0;
+        DBuf d_fixed;
+        d_fixed.upload(fixed);
+        ImplicitRhs R;
+        R.f = [p](const double* y, double* du, double t, cudaStream_t s) {
+            problem_rhs_internal(p, y, du, false, s, false, t);
+        };
+        R.jvp = [p](const double* u, const double* v, double* jv, cudaStream_t s) { problem_jvp_internal(p, u, v, jv, s); };
+        R.diag = [p](const double* u, double* d, cudaStream_t s) { problem_jacobian_diagonal_internal(p, u, d, s); };
+        if (p->ndir > 0)
+            R.callback = [p](double* u, double t, cudaStream_t s) { problem_dirichlet_internal(p, u, t, s); };
+        R.callback_varies = p->tdir_varies;
+        R.affine = p->linear && !p->has_q && p->precision != FVM_FP32;
+        R.fixed = d_fixed.as<double>();
+        steady_run(R, m->d_perm.as<int32_t>(), m->d_iperm.as<int32_t>(), m->np, u0, o, out, st, stream);
+        return FVM_OK;
     });
 }
 

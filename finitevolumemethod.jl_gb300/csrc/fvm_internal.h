@@ -468,9 +468,22 @@ struct ImplicitRhs {
     std::function<void(double*, double, cudaStream_t)> callback;
     bool callback_varies = false;
     bool affine = false;
+    const double* fixed = nullptr;  // steady Newton: 1 on the rows the problem fixes, else 0 (internal)
+};
+// DynamicSS's stopping test on a TR-BDF2 run: after each accepted step, max|f(u)| <= abstol or
+// <= reltol max|f(u) + u| ends the run with u as its one output
+struct SteadyStop {
+    double abstol = 0, reltol = 0;
+    bool converged = false;
+    double residual = 0;
 };
 // TR-BDF2 on R over n unknowns; u0 and out are host arrays in the caller's numbering, perm (internal
 // -> caller) and iperm (caller -> internal) device index arrays.  Throws on error.
 int trbdf2_run(ImplicitRhs& R, const int32_t* perm, const int32_t* iperm, int64_t n, const double* u0,
-               const fvm_ode_options* o, double* out, fvm_ode_stats* st, fvm_implicit_stats* ist, void* stream);
+               const fvm_ode_options* o, double* out, fvm_ode_stats* st, fvm_implicit_stats* ist, void* stream,
+               SteadyStop* stop = nullptr);
+// fvm_steady_solve on R (either method); fills out and st, then throws FVM_ERR_NOT_CONVERGED if the
+// test was not met
+void steady_run(ImplicitRhs& R, const int32_t* perm, const int32_t* iperm, int64_t n, const double* u0,
+                const fvm_steady_options* o, double* out, fvm_steady_stats* st, void* stream);
 }  // namespace fvm

@@ -259,6 +259,15 @@ __global__ void system_poly_jacobian_kernel(const double* __restrict__ u, const 
         if ((m >> r) & 1u) y[row * N + r] += acc[r];
 }
 
+// 1 on the [point][component] rows the system fixes (mask bit clear: Dirichlet, no triangle), else 0
+__global__ void system_fixed_kernel(const uint8_t* mask, int N, int64_t n, double* fixed) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int64_t row = i / N;
+    const int r = (int)(i - row * N);
+    fixed[i] = ((mask[row] >> r) & 1u) ? 0.0 : 1.0;
+}
+
 // the shared form's diagonal multipliers dmat[r][r]
 struct SysDiagMat {
     double d[kSysMaxEq];
@@ -964,6 +973,35 @@ int fvm_system_trbdf2_solve(fvm_system* S, const double* u0, const fvm_ode_optio
         R.affine = affine;
         return trbdf2_run(R, S->d_perm.as<int32_t>(), S->d_iperm.as<int32_t>(), S->n(), u0, opt, out, stats, istats,
                           stream);
+    });
+}
+
+int fvm_system_steady_solve(fvm_system* S, const double* u0, const fvm_steady_options* opt, double* out,
+                            fvm_steady_stats* stats, void* stream) {
+    return guard_call([&] {
+        if (!S) fail(FVM_ERR_INVALID_ARGUMENT, "NULL argument");
+        const int64_t n = S->n();
+        DBuf d_fixed;
+        d_fixed.alloc(sizeof(double) * n);
+        system_fixed_kernel<<<(unsigned)((n + 255) / 256), 256>>>(S->d_mask.as<uint8_t>(), S->neq, n,
+                                                                  d_fixed.as<double>());
+        FVM_CUDA(cudaGetLastError());
+        FVM_CUDA(cudaDeviceSynchronize());
+        ImplicitRhs R;
+        R.f = [S](const double* y, double* du, double t, cudaStream_t s) { system_rhs_internal(S, y, du, s, t); };
+        R.jvp = [S](const double* u, const double* v, double* jv, cudaStream_t s) {
+            system_jacobian_internal(S, u, v, jv, s);
+        };
+        R.diag = [S](const double* u, double* d, cudaStream_t s) { system_jacobian_internal(S, u, nullptr, d, s); };
+        if (S->ndir > 0)
+            R.callback = [S](double* u, double t, cudaStream_t s) { system_dirichlet_internal(S, u, s, t); };
+        R.callback_varies = S->tdir_varies;
+        bool affine = true;
+        for (int mo = 0; mo < S->terms.nmono; ++mo) affine = affine && S->terms.nf[mo] <= 1;
+        R.affine = affine;
+        R.fixed = d_fixed.as<double>();
+        steady_run(R, S->d_perm.as<int32_t>(), S->d_iperm.as<int32_t>(), n, u0, opt, out, stats, stream);
+        return FVM_OK;
     });
 }
 

@@ -26,6 +26,7 @@ FVM_ERR_STEP_LIMIT = 8
 FVM_VERTEX_FREE, FVM_VERTEX_DIRICHLET, FVM_VERTEX_DUDT, FVM_VERTEX_NOT_A_VERTEX = 0, 1, 2, 3
 FVM_MAX_TIME_FACTORS = 8
 FVM_PROBLEM_CONDITIONS_ONLY = 1
+FVM_STEADY_DYNAMIC, FVM_STEADY_NEWTON = 0, 1
 FVM_PTR_HOST, FVM_PTR_DEVICE, FVM_PTR_DEVICE_INTERNAL = 0, 1, 2
 FVM_RHS_FORCE_TRIANGLE = 16
 FVM_RHS_CONSERVATIVE = 32
@@ -135,6 +136,20 @@ class ImplicitStats(C.Structure):
     ]
 
 
+class SteadyOptions(C.Structure):
+    _fields_ = [
+        ("method", C.c_int32), ("abstol", C.c_double), ("reltol", C.c_double), ("t", C.c_double),
+        ("tmax", C.c_double), ("ode_abstol", C.c_double), ("ode_reltol", C.c_double), ("max_iters", C.c_int64),
+    ]
+
+
+class SteadyStats(C.Structure):
+    _fields_ = [
+        ("iterations", C.c_int64), ("krylov_iters", C.c_int64), ("jvps", C.c_int64), ("nrhs", C.c_int64),
+        ("residual", C.c_double), ("t_final", C.c_double), ("elapsed_ms", C.c_double),
+    ]
+
+
 class SolverOptions(C.Structure):
     _fields_ = [
         ("rtol", C.c_double), ("max_iters", C.c_int64), ("method", C.c_int32), ("precond", C.c_int32),
@@ -196,6 +211,10 @@ SIGNATURES = {
     "fvm_system_dirichlet_apply": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_int32, C.c_void_p]),
     "fvm_system_tsit5_solve": (C.c_int, [C.c_void_p, c_double_p, C.POINTER(OdeOptions), c_double_p,
                                          C.POINTER(OdeStats), C.c_void_p]),
+    "fvm_steady_solve": (C.c_int, [C.c_void_p, c_double_p, C.POINTER(SteadyOptions), c_double_p,
+                                   C.POINTER(SteadyStats), C.c_void_p]),
+    "fvm_system_steady_solve": (C.c_int, [C.c_void_p, c_double_p, C.POINTER(SteadyOptions), c_double_p,
+                                          C.POINTER(SteadyStats), C.c_void_p]),
     "fvm_system_jvp": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int32, C.c_void_p]),
     "fvm_system_jacobian_diagonal": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int32,
                                                C.c_void_p]),

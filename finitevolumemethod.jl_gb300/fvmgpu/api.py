@@ -1459,6 +1459,108 @@ class TRBDF2:
         return "TRBDF2()"
 
 
+class SteadyFVMProblem:
+    """SteadyFVMProblem(prob) (src/problem.jl:166-180): an FVMProblem or FVMSystem to be solved for
+    du/dt = 0.  The problem's initial condition is the initial guess, and its final time is
+    conventionally Inf.  solve(steady, DynamicSS(...)) or solve(steady, NewtonRaphson())."""
+
+    def __init__(self, prob):
+        if not isinstance(prob, (FVMProblem, FVMSystem)):
+            raise TypeError("SteadyFVMProblem wraps an FVMProblem or an FVMSystem")
+        self.problem = prob
+        self.mesh = prob.mesh
+
+    def __repr__(self):
+        nv = int(self.mesh.triangulation.has_vertex().sum())
+        if isinstance(self.problem, FVMSystem):
+            return f"SteadyFVMProblem with {nv} nodes and {self.problem.neqs} equations"
+        return f"SteadyFVMProblem with {nv} nodes"
+
+
+@dataclass
+class DynamicSS:
+    """DynamicSS(alg; abstol = 1e-8, reltol = 1e-6, tspan = Inf) of SteadyStateDiffEq: step the
+    ODE in pseudo-time from the initial guess, the Dirichlet update after every step, until
+    max|du/dt| <= abstol or max|du/dt| <= reltol max|du/dt + u|.  The device integrator is
+    TR-BDF2 whichever implicit method `alg` names (the tutorials use TRBDF2 and Rosenbrock23):
+    the steady state is the same, the path to it differs.  ode_abstol / ode_reltol are the
+    integrator's step tolerances."""
+
+    alg: Any = None
+    abstol: float = 1e-8
+    reltol: float = 1e-6
+    tspan: float = float("inf")
+    ode_abstol: float = 1e-6
+    ode_reltol: float = 1e-3
+    max_steps: int = 0
+
+
+@dataclass
+class NewtonRaphson:
+    """NewtonRaphson() of NonlinearSolve on f(u) = 0, on the device: each iteration solves
+    (F - J(u)) du = f(u) by matrix-free BiCGStab with the exact JVP, F the identity on the rows
+    the problem fixes (Dirichlet nodes, points outside the mesh), which keep their values (the
+    Dirichlet values at the initial time are applied to the guess first).  Stops when
+    max|f(u)| <= abstol or <= reltol max|f(u) + u|."""
+
+    abstol: float = 1e-10
+    reltol: float = 1e-10
+    max_iters: int = 50
+
+
+@dataclass
+class SteadyStateSolution:
+    """The steady state: u (vector, or N x npoints matrix for a system), stats, retcode."""
+
+    u: np.ndarray
+    stats: Dict[str, Any] = field(default_factory=dict)
+    retcode: str = "Success"
+
+
+def _solve_steady(sp, alg, abstol, reltol, stream):
+    """solve(::SteadyFVMProblem, alg) (src/solve.jl:184-196) on the device."""
+    prob = sp.problem
+    alg = alg if alg is not None else DynamicSS(TRBDF2())
+    o = _lib.SteadyOptions()
+    if isinstance(alg, NewtonRaphson):
+        o.method = _lib.FVM_STEADY_NEWTON
+        o.max_iters = int(alg.max_iters)
+        method = "newton"
+    elif isinstance(alg, DynamicSS):
+        o.method = _lib.FVM_STEADY_DYNAMIC
+        o.tmax = prob.initial_time + float(alg.tspan)
+        o.ode_abstol, o.ode_reltol = alg.ode_abstol, alg.ode_reltol
+        o.max_iters = int(alg.max_steps)
+        method = "dynamic"
+    else:
+        raise TypeError("a SteadyFVMProblem is solved with DynamicSS(...) or NewtonRaphson()")
+    o.abstol = float(alg.abstol if abstol is None else abstol)
+    o.reltol = float(alg.reltol if reltol is None else reltol)
+    o.t = prob.initial_time
+    st = _lib.SteadyStats()
+    lib = load()
+    if isinstance(prob, FVMSystem):
+        u0 = as_f64(prob.initial_condition.T)  # [point][component]
+        out = _lib.host_empty(u0.shape)
+        status = lib.fvm_system_steady_solve(prob.handle, dptr(u0), C.byref(o), dptr(out), C.byref(st), stream)
+        u = out.T
+    else:
+        u0 = as_f64(prob.initial_condition)
+        out = _lib.host_empty(u0.shape)
+        status = lib.fvm_steady_solve(prob.handle, dptr(u0), C.byref(o), dptr(out), C.byref(st), stream)
+        u = out
+    stats = {"method": method, "iterations": st.iterations, "krylov_iters": st.krylov_iters, "jvps": st.jvps,
+             "nrhs": st.nrhs, "residual": st.residual, "t_final": st.t_final, "elapsed_ms": st.elapsed_ms}
+    sol = SteadyStateSolution(u, stats)
+    try:
+        check(status)
+    except _lib.NotConvergedError as e:
+        sol.retcode = "Failure"
+        e.solution = sol  # the last iterate and its statistics
+        raise
+    return sol
+
+
 def jvp(prob, u, v, t=0.0, stream=None):
     """J(u) v, the Jacobian-vector product of fvm_eqs! (exact for every device-coded form).
     u, v host float64 arrays or CUDA tensors (caller numbering); returns J(u) v of their kind."""
@@ -1547,14 +1649,22 @@ def _saveat_times(saveat, t0, tf):
     return np.asarray(saveat, dtype=np.float64)
 
 
-def solve(prob, alg=None, *, saveat=None, dt=None, adaptive=None, abstol=1e-6, reltol=1e-3, max_steps=0,
+def solve(prob, alg=None, *, saveat=None, dt=None, adaptive=None, abstol=None, reltol=None, max_steps=0,
           use_graph=True, parallel=True, precision="fp64", stream=None, **kwargs):
-    """solve(prob, alg; saveat, ...) (src/solve.jl:197-220; abstract_templates.jl:58-60).
+    """solve(prob, alg; saveat, ...) (src/solve.jl:184-220; abstract_templates.jl:58-60).
 
-    Time-dependent problems step with Tsit5 (adaptive unless `dt` is given with
-    adaptive=False); steady templates solve A u = b with the GPU Krylov solver."""
+    Time-dependent problems step with Tsit5 or TRBDF2 (adaptive unless `dt` is given with
+    adaptive=False; abstol 1e-6, reltol 1e-3 by default); steady templates solve A u = b with the
+    GPU Krylov solver; a SteadyFVMProblem takes DynamicSS or NewtonRaphson (abstol / reltol
+    then override the method's own)."""
     lib = load()
     s = stream if stream is not None else _lib.current_stream_handle()
+    if isinstance(prob, SteadyFVMProblem):
+        return _solve_steady(prob, alg, abstol, reltol, s)
+    abstol = 1e-6 if abstol is None else abstol
+    reltol = 1e-3 if reltol is None else reltol
+    if isinstance(prob, (FVMProblem, FVMSystem)) and not np.isfinite(prob.final_time):
+        raise ValueError("the final time is not finite: wrap the problem in SteadyFVMProblem for its steady state")
     if isinstance(prob, _Template) and prob.steady:
         opt = alg if isinstance(alg, KrylovSolver) else KrylovSolver()
         so = _lib.SolverOptions()

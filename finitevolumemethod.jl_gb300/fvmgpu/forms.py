@@ -88,7 +88,7 @@ def fit_time_factor(c0_at, t0, tf, what):
     equally spaced times across [t0, tf]; verify at three other times.  Returns
     (A, TimeFactor, B), or None when c0 does not depend on t.  Rejects other t dependence."""
     t0 = float(t0)
-    span = float(tf) - t0 if tf is not None and float(tf) > t0 else 1.0
+    span = float(tf) - t0 if tf is not None and np.isfinite(float(tf)) and float(tf) > t0 else 1.0
     h = span / 5
     C = [np.asarray(c0_at(t0 + k * h), dtype=np.float64) for k in range(6)]
     scale = max(float(np.max(np.abs(c))) if c.size else 0.0 for c in C)

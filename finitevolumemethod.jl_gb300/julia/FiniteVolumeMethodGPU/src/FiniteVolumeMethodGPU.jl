@@ -33,7 +33,8 @@ import CommonSolve
 const FVM = FiniteVolumeMethod
 const DT = DelaunayTriangulation
 
-export GPUProblem, GPUSystem, GPUTemplate, GPUBatch, GPUAdjoint, GPUKrylov, adjoint_solve, adjoint_pullback,
+export GPUProblem, GPUSystem, GPUTemplate, GPUBatch, GPUAdjoint, GPUKrylov, GPUSteady, steady_state, adjoint_solve,
+    adjoint_pullback,
     set_log_diffusion!, locate, interpolate, steady_solve, jvp!, solve_trbdf2
 
 const libfvmgpu = get(ENV, "FVMGPU_LIB", joinpath(@__DIR__, "..", "..", "..", "fvmgpu", "_lib", "libfvmgpu.so"))
@@ -854,6 +855,101 @@ The steady template solved on the device in place of `solve(tmpl, KLUFactorizati
 function CommonSolve.solve(tmpl::Union{FVM.PoissonsEquation, FVM.MeanExitTimeProblem}, alg::GPUKrylov; kwargs...)
     x, st = steady_solve(gpu_object(tmpl), alg)
     return (u = x, stats = st)
+end
+
+# ---- steady states: SteadyFVMProblem (src/problem.jl:166-180, src/solve.jl:184-196) ----------
+struct SteadyOptions
+    method::Int32
+    abstol::Float64
+    reltol::Float64
+    t::Float64
+    tmax::Float64
+    ode_abstol::Float64
+    ode_reltol::Float64
+    max_iters::Int64
+end
+
+mutable struct SteadyStats
+    iterations::Int64
+    krylov_iters::Int64
+    jvps::Int64
+    nrhs::Int64
+    residual::Float64
+    t_final::Float64
+    elapsed_ms::Float64
+end
+
+"""
+    GPUSteady(method = :dynamic; abstol, reltol, tspan = Inf, ode_abstol = 1e-6, ode_reltol = 1e-3,
+              max_iters = 0)
+
+The device steady solver for `solve(SteadyFVMProblem(prob), GPUSteady(...))`, in place of the
+tutorials' `DynamicSS(TRBDF2(...))` / `DynamicSS(Rosenbrock23())` (`method = :dynamic`: TR-BDF2 in
+pseudo-time until max|du/dt| <= abstol or <= reltol max|du/dt + u|; abstol 1e-8, reltol 1e-6 by
+default) or `NewtonRaphson()` (`method = :newton`: Newton-Krylov with the exact device JVP, the
+rows the problem fixes held; abstol = reltol = 1e-10 by default).
+"""
+struct GPUSteady
+    method::Symbol
+    abstol::Float64
+    reltol::Float64
+    tspan::Float64
+    ode_abstol::Float64
+    ode_reltol::Float64
+    max_iters::Int
+end
+function GPUSteady(method::Symbol = :dynamic; abstol = method === :newton ? 1e-10 : 1e-8,
+                   reltol = method === :newton ? 1e-10 : 1e-6, tspan = Inf, ode_abstol = 1e-6, ode_reltol = 1e-3,
+                   max_iters = 0)
+    method in (:dynamic, :newton) || throw(ArgumentError("GPUSteady method is :dynamic or :newton"))
+    return GPUSteady(method, abstol, reltol, tspan, ode_abstol, ode_reltol, max_iters)
+end
+
+steady_options(alg::GPUSteady, t0) = SteadyOptions(alg.method === :newton ? Int32(1) : Int32(0), alg.abstol,
+    alg.reltol, t0, t0 + alg.tspan, alg.ode_abstol, alg.ode_reltol, alg.max_iters)
+
+"""
+    steady_state(g::Union{GPUProblem, GPUSystem}, alg::GPUSteady = GPUSteady()) -> (u, stats)
+
+The steady state from the problem's initial condition (the initial guess), on the device
+(`fvm_steady_solve` / `fvm_system_steady_solve`).  Not converged: a warning, and the last iterate.
+"""
+function steady_state(gp::GPUProblem, alg::GPUSteady = GPUSteady())
+    prob = gp.prob
+    u0 = collect(Float64, prob.initial_condition)
+    out = similar(u0)
+    opt = steady_options(alg, prob.initial_time)
+    st = SteadyStats(0, 0, 0, 0, 0.0, 0.0, 0.0)
+    status = ccall((:fvm_steady_solve, libfvmgpu), Cint,
+        (Ptr{Cvoid}, Ptr{Float64}, Ref{SteadyOptions}, Ptr{Float64}, Ref{SteadyStats}, Ptr{Cvoid}),
+        gp.handle, u0, opt, out, st, C_NULL)
+    status == Cint(6) && @warn "steady state not reached" st.residual st.iterations
+    status == Cint(6) || check(status)
+    return out, st
+end
+function steady_state(gs::GPUSystem, alg::GPUSteady = GPUSteady())
+    sys = gs.sys
+    u0 = Matrix{Float64}(sys.initial_condition)
+    out = similar(u0)
+    opt = steady_options(alg, sys.initial_time)
+    st = SteadyStats(0, 0, 0, 0, 0.0, 0.0, 0.0)
+    status = ccall((:fvm_system_steady_solve, libfvmgpu), Cint,
+        (Ptr{Cvoid}, Ptr{Float64}, Ref{SteadyOptions}, Ptr{Float64}, Ref{SteadyStats}, Ptr{Cvoid}),
+        gs.handle, u0, opt, out, st, C_NULL)
+    status == Cint(6) && @warn "steady state not reached" st.residual st.iterations
+    status == Cint(6) || check(status)
+    return out, st
+end
+
+"""
+    solve(prob::SteadyFVMProblem, alg::GPUSteady)
+
+The steady state on the device: a named tuple with `u` (vector, or N x npoints matrix for a
+system) and `stats`.
+"""
+function CommonSolve.solve(prob::FVM.SteadyFVMProblem, alg::GPUSteady; kwargs...)
+    u, st = steady_state(gpu_object(prob.problem), alg)
+    return (u = u, stats = st)
 end
 
 # ---- batched instances (an EnsembleProblem over D on one mesh) ------------------------------

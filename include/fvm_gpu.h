@@ -339,6 +339,41 @@ int fvm_system_jacobian_diagonal(fvm_system* sys, const double* u, double* diag,
 int fvm_system_trbdf2_solve(fvm_system* sys, const double* u0, const fvm_ode_options* opt, double* out,
                             fvm_ode_stats* stats, fvm_implicit_stats* istats, void* stream);
 
+/* ---- steady states (SteadyFVMProblem, src/problem.jl:166-180; solve, src/solve.jl:184-196) --
+ * The reference wraps the problem's ODE right-hand side in a SteadyStateProblem and hands it to
+ * SteadyStateDiffEq (DynamicSS(alg): integrate in pseudo-time until du/dt vanishes) or to
+ * NonlinearSolve (NewtonRaphson: Newton on f(u) = 0).  Both run here on the device:
+ *   FVM_STEADY_DYNAMIC  TR-BDF2 (as fvm_trbdf2_solve) from t, the Dirichlet update after every
+ *                       step, stopped after the first accepted step whose u passes the test
+ *   FVM_STEADY_NEWTON   Newton-Krylov on f(u, t) = 0: (F - J(u)) du = f(u) by BiCGStab with the
+ *                       Jacobi preconditioner, F the identity on the rows the problem fixes
+ *                       (Dirichlet, points outside the mesh), so those rows keep their values;
+ *                       the Dirichlet update at t is applied to the initial guess first
+ * Test on the returned u: max|f(u)| <= abstol, or max|f(u)| <= reltol max|f(u) + u|.  u0 and out
+ * are host arrays in the caller's numbering (systems: [npoints][neq]).  Not converged within
+ * max_iters (or tmax): FVM_ERR_NOT_CONVERGED, with the last iterate in out and stats filled. */
+#define FVM_STEADY_DYNAMIC 0
+#define FVM_STEADY_NEWTON 1
+typedef struct fvm_steady_options {
+    int32_t method;                 /* FVM_STEADY_* */
+    double abstol, reltol;          /* the test above */
+    double t;                       /* Newton: the time f is evaluated at; DynamicSS: the pseudo-time start */
+    double tmax;                    /* DynamicSS: pseudo-time limit (INFINITY allowed) */
+    double ode_abstol, ode_reltol;  /* DynamicSS: the TR-BDF2 step tolerances */
+    int64_t max_iters;              /* Newton iterations or DynamicSS steps; 0: 50 or 100000 */
+} fvm_steady_options;
+typedef struct fvm_steady_stats {
+    int64_t iterations;             /* Newton iterations, or accepted TR-BDF2 steps */
+    int64_t krylov_iters, jvps, nrhs;
+    double residual;                /* max|f(u)| at the returned u */
+    double t_final;                 /* DynamicSS: the pseudo-time reached */
+    double elapsed_ms;              /* device time (CUDA events) */
+} fvm_steady_stats;
+int fvm_steady_solve(fvm_problem* prob, const double* u0, const fvm_steady_options* opt, double* out,
+                     fvm_steady_stats* stats, void* stream);
+int fvm_system_steady_solve(fvm_system* sys, const double* u0, const fvm_steady_options* opt, double* out,
+                            fvm_steady_stats* stats, void* stream);
+
 /* ---- batched instances (many parameter sets on one mesh) -------------------------------- */
 /* B instances of one linear problem that differ in their diffusion field D_b(x, y), the
  * batched counterpart of solving B FVMProblems (an EnsembleProblem over D in the reference).

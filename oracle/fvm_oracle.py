@@ -834,6 +834,44 @@ def trbdf2_solve(f, jac, u0, t0, tf, saveat, dt=None, adaptive=True, abstol=1e-6
                            "failures": failures}
 
 
+def fixed_rows(tri, conds_list):
+    """The rows a steady solve holds at their values, over states flattened [point][component]:
+    a component's Dirichlet nodes and every point in no triangle (du/dt = 0 there, and the
+    Jacobian row is zero).  Test infrastructure for the steady solvers."""
+    N = len(conds_list)
+    fixed = np.zeros((tri.num_points, N))
+    hv = tri.has_vertex()
+    for r, c in enumerate(conds_list):
+        fixed[list(c.dirichlet_nodes.keys()), r] = 1.0
+        fixed[~hv, r] = 1.0
+    return fixed.ravel()
+
+
+def steady_newton(f, jac, u0, t, fixed, abstol=1e-10, reltol=1e-10, max_iters=50, callback=None):
+    """A steady state of du/dt = f(u, t) (SteadyFVMProblem, src/problem.jl:166-180, solved with
+    NonlinearSolve's NewtonRaphson, src/solve.jl:184-196), restated with exact sparse solves:
+    the Dirichlet update at t (`callback`) on the guess, then u <- u + du with
+    (F - J(u)) du = f(u), F = diag(fixed) (the fixed rows keep their values, where J's rows
+    vanish), until max|f(u)| <= abstol or <= reltol max|f(u) + u|.  Test infrastructure.
+    Returns (u, Newton iterations, max|f(u)|)."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spl
+
+    u = np.array(u0, dtype=np.float64)
+    if callback is not None:
+        u = callback(u, t)
+    F = sp.diags(np.asarray(fixed, dtype=np.float64))
+    for it in range(max_iters + 1):
+        r = f(u, t)
+        res = float(np.max(np.abs(r)))
+        if res <= abstol or res <= reltol * float(np.max(np.abs(r + u))):
+            return u, it, res
+        if it == max_iters:
+            break
+        u = u + spl.spsolve((F - jac(u, t)).tocsc(), r)
+    raise RuntimeError("steady_newton did not converge")
+
+
 # --------------------------------------------------------------------------------------
 # linear templates: src/specific_problems/*.jl, assembled sparse (not dense)
 # --------------------------------------------------------------------------------------

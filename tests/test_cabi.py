@@ -74,6 +74,8 @@ STRUCTS = {  # C struct in include/fvm_gpu.h -> its ctypes mirror in fvmgpu/_lib
     "fvm_solver_stats": "SolverStats",
     "fvm_adjoint_stats": "AdjointStats",
     "fvm_implicit_stats": "ImplicitStats",
+    "fvm_steady_options": "SteadyOptions",
+    "fvm_steady_stats": "SteadyStats",
 }
 
 
@@ -116,7 +118,8 @@ def test_ctypes_structures_match_the_header_layout(tmp_path):
 JULIA = ROOT / "finitevolumemethod.jl_gb300" / "julia" / "FiniteVolumeMethodGPU" / "src" / "FiniteVolumeMethodGPU.jl"
 JULIA_STRUCTS = {"ProblemDesc": "fvm_problem_desc", "SystemDesc": "fvm_system_desc", "OdeOptions": "fvm_ode_options",
                  "OdeStats": "fvm_ode_stats", "SolverOptions": "fvm_solver_options", "SolverStats": "fvm_solver_stats",
-                 "AdjointStats": "fvm_adjoint_stats", "ImplicitStats": "fvm_implicit_stats"}
+                 "AdjointStats": "fvm_adjoint_stats", "ImplicitStats": "fvm_implicit_stats",
+                 "SteadyOptions": "fvm_steady_options", "SteadyStats": "fvm_steady_stats"}
 JULIA_SIZES = {"Int8": 1, "Int32": 4, "Cint": 4, "Int64": 8, "Float64": 8}
 
 

@@ -491,3 +491,46 @@ def test_oracle_trbdf2_is_second_order():
         errs.append(np.max(np.abs(sol[-1] - ref[-1])))
     r1, r2 = errs[0] / errs[1], errs[1] / errs[2]
     assert 3.5 < r1 < 4.5 and 3.5 < r2 < 4.5, (errs, r1, r2)
+
+
+def _steady_oracle_problem(tri, bc_fns, bc_types, D=None, S=None, dirichlet_nodes=None):
+    conds = O.Conditions(tri, list(bc_fns), list(bc_types), [lambda x, y, t, u: 0.0 * x] if dirichlet_nodes else [],
+                         dirichlet_nodes or {})
+    prob = O.Problem(tri, conds, D=D, source=S, u0=np.zeros(tri.num_points), t0=0.0, tf=np.inf)
+    f = lambda u, t: O.fvm_eqs(prob, u, t)  # noqa: E731
+    ent, n = O.jacobian_sparsity(tri)
+    jac = lambda u, t: O.colored_jacobian(f, u, t, ent, n)  # noqa: E731
+    cb = lambda u, t: O.update_dirichlet_nodes(prob, u, t)  # noqa: E731
+    return prob, f, jac, cb, O.fixed_rows(tri, [conds])
+
+
+def test_oracle_steady_newton_reproduces_a_linear_solution():
+    """The steady state of the Laplace tutorial's boundary values (0, 100y, 100, 100y on a
+    rectangle) without its internal line is u = 100y, which the vertex-centred scheme reproduces
+    exactly: the oracle's Newton steady solve returns it to rounding."""
+    tri = triangulate_rectangle(0.0, 1.0, 0.0, 1.0, 21, 21, single_boundary=False)
+    bcs = (lambda x, y, t, u: 0.0 * x, lambda x, y, t, u: 100 * y, lambda x, y, t, u: 100.0 + 0.0 * x,
+           lambda x, y, t, u: 100 * y)
+    _, f, jac, cb, fixed = _steady_oracle_problem(tri, bcs, ["Dirichlet"] * 4, D=lambda x, y, t, u: 1.0 + 0.0 * x)
+    u, it, res = O.steady_newton(f, jac, np.zeros(tri.num_points), 0.0, fixed, callback=cb)
+    assert np.max(np.abs(u - 100 * tri.points[:, 1])) <= 1e-9 * 100
+    assert it <= 2 and res <= 1e-6
+
+
+def test_oracle_steady_newton_mean_exit_time_disk():
+    """du/dt = div grad u + 1 with u = 0 on the unit disk's boundary: the steady state is the mean
+    exit time (1 - r^2)/4, and it matches the oracle's MeanExitTimeProblem assembly solved
+    directly."""
+    from fvmgpu.meshes import triangulate_disk
+
+    tri = triangulate_disk(1500, 96, seed=3)
+    _, f, jac, cb, fixed = _steady_oracle_problem(tri, [lambda x, y, t, u: 0.0 * x], ["Dirichlet"],
+                                                  D=lambda x, y, t, u: 1.0 + 0.0 * x,
+                                                  S=lambda x, y, t, u: 1.0 + 0.0 * x)
+    u, it, _ = O.steady_newton(f, jac, np.zeros(tri.num_points), 0.0, fixed, callback=cb)
+    r2 = (tri.points**2).sum(axis=1)
+    assert isapprox(u, (1 - r2) / 4, 5e-3)
+    conds = O.Conditions(tri, [lambda x, y, t, u: 0.0 * x], ["Dirichlet"])
+    A, b = O.template_mean_exit_time(tri, conds, lambda x, y: 1.0 + 0.0 * x)
+    T = O.steady_solve(A, b)
+    assert np.max(np.abs(u - T)) <= 1e-9 * np.max(np.abs(T))
