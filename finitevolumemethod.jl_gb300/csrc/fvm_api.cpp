@@ -41,8 +41,8 @@ static void check_launch() { FVM_CUDA(cudaGetLastError()); }
 // after a stream synchronisation: reports a kernel whose bounded wait ran out
 static void check_device_error() {
     if (unsigned e = take_device_error())
-        fail(FVM_ERR_CUDA, "a streamed kernel timed out waiting for its copies (device error bits " +
-                               std::to_string(e) + ")");
+        fail(FVM_ERR_CUDA, "a kernel timed out in a bounded wait (device error bits " + std::to_string(e) +
+                               "; 1, 2: the streamed kernel's stages; 4: the host-array RHS's work items)");
 }
 
 // Tsit5 tableau (Tsitouras 2011, as published).
@@ -434,11 +434,12 @@ static void rhs_outputs(fvm_problem* p, double* du, int32_t loc, cudaStream_t s)
     }
 }
 
-static TimeTaus time_taus(const fvm_problem* p, double t) {
+TimeTaus problem_time_taus(const fvm_problem* p, double t) {
     TimeTaus tt{};
     for (int g = 0; g < p->ntime; ++g) tt.tau[g] = time_factor_value(&p->tfac[4 * g], t);
     return tt;
 }
+static TimeTaus time_taus(const fvm_problem* p, double t) { return problem_time_taus(p, t); }
 
 void problem_dirichlet_internal(const fvm_problem* p, double* u, double t, cudaStream_t s) {
     if (p->ntime > 0)
@@ -676,6 +677,16 @@ int fvm_rhs(fvm_problem* p, const double* u, double* du, double t, int32_t flags
         cudaStream_t s = (cudaStream_t)stream;
         int32_t loc = flags & 3;
         if (loc > FVM_PTR_DEVICE_INTERNAL) fail(FVM_ERR_INVALID_ARGUMENT, "bad pointer-location flag");
+        if (loc == FVM_PTR_HOST && !(flags & (FVM_RHS_FORCE_TRIANGLE | FVM_RHS_CONSERVATIVE))) {
+            // page-locked host arrays: one launch overlaps the link transfers with the product
+            const void* mu = host_mapped(u);
+            void* md = mu ? host_mapped(du) : nullptr;
+            if (md && problem_rhs_host_fused(p, (const double*)mu, (double*)md, t, s)) {
+                FVM_CUDA(cudaStreamSynchronize(s));
+                check_device_error();
+                return FVM_OK;
+            }
+        }
         IoPlan io;
         rhs_inputs(p, u, du, loc, io, s);
         problem_rhs_internal(p, io.uin, io.dout, (flags & FVM_RHS_FORCE_TRIANGLE) != 0, s,

@@ -1,5 +1,6 @@
 // Internal declarations of libfvmgpu: handles, device buffers, kernel launchers.
 #pragma once
+struct fvm_mesh;
 #include <cuda_runtime.h>
 #include <cmath>
 #include <cstdint>
@@ -126,6 +127,18 @@ struct Locator {
     DBuf d_pts, d_tri, d_shape;     // [np][2], [nt][3], [nt][9]
 };
 
+// The work queue of the fused host-array RHS (fvm_e2e.cu) for one mesh: A items read caller
+// chunks of u from the host, B items compute blocks of slices, C items write caller chunks of
+// du; each lists the items it waits for.
+struct E2ePlan {
+    bool built = false;
+    int nA = 0, nB = 0, nC = 0, nitems = 0;
+    int chunk = 0, spi = 0;  // caller points per A / C item, slices per B item
+    DBuf d_order, d_dep_ptr, d_dep, d_flags, d_counter;
+    unsigned epoch = 0;      // flags equal to the current call's epoch are done
+    void build(const ::fvm_mesh* m);
+};
+
 struct Tiles {
     bool built = false;
     int tile_vertices = 0;
@@ -156,6 +169,7 @@ struct fvm_mesh {
     fvm::SellPattern pat_off;                   // off-diagonal neighbours only (difference-form RHS)
     fvm::Tiles tiles;
     fvm::Locator loc;
+    fvm::E2ePlan e2e;
     fvm::DBuf d_perm, d_iperm, d_invV;          // d_invV internal order
     int tile_vertices_req = 0;
     void build_tiles();
@@ -456,6 +470,12 @@ void launch_time_b(const double* b, const double* tb, const TimeTaus& tt, int nt
                    cudaStream_t s);
 void launch_dirichlet_time(const int32_t* idx, const double* val, const double* tval, const TimeTaus& tt, int ntime,
                            double* u, int64_t n, cudaStream_t s);
+// tau_g(t) of the problem's time factors
+TimeTaus problem_time_taus(const fvm_problem* p, double t);
+// fvm_eqs! from a page-locked host u into a page-locked host du (device addresses of both), one
+// launch overlapping the link transfers with the product (fvm_e2e.cu); false when the problem
+// is not on the FP64 operator path (the caller then takes the general path)
+bool problem_rhs_host_fused(fvm_problem* p, const double* uh, double* dh, double t, cudaStream_t s);
 
 // What the implicit integrator needs of a right-hand side, in the internal numbering: f(y, t),
 // J(u) v, diag J(u), and the Dirichlet update after a step (optional).  callback_varies: the

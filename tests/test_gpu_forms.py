@@ -68,6 +68,11 @@ def test_time_dependent_rhs_and_dirichlet(gpu_lib, make):
         for cons in (False, True):
             du = F.fvm_eqs(np.zeros_like(u), u.copy(), prob, t, conservative=cons)
             assert parity_error(du, ref, scale) <= 1e-12, (t, cons)
+            if not cons:  # page-locked host arrays: the one-launch path, b(t) formed first
+                u_pin, du_pin = F._lib.host_empty(u.shape), F._lib.host_empty(u.shape)
+                u_pin[:] = u
+                F.fvm_eqs(du_pin, u_pin, prob, t)
+                assert np.array_equal(du_pin, du), t
         if oprob.conds.dirichlet_nodes:
             got = F.update_dirichlet_nodes(u.copy(), prob, t)
             want = O.update_dirichlet_nodes(oprob, u, t)

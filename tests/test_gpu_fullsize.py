@@ -54,6 +54,31 @@ def test_c2_rhs_every_path_against_oracle(gpu_lib, c2):
             assert e2 <= FP64_RTOL and einf <= FP64_RTOL, (name, force, cons, e2, einf)
 
 
+def test_c2_rhs_page_locked_host_arrays_against_oracle(gpu_lib, c2):
+    """The headline's end-to-end call: page-locked host u and du take the one-launch path that
+    overlaps the link transfers with the product.  Against the oracle at 1e-12, and bit-identical
+    to the device-array path, over repeated calls."""
+    import torch
+
+    import fvmgpu as F
+
+    spec, oprob, fields, refs = c2
+    prob = api_problem(spec)
+    n = spec.tri.num_points
+    u_pin = torch.empty(n, dtype=torch.float64, pin_memory=True)
+    du_pin = torch.empty(n, dtype=torch.float64, pin_memory=True)
+    for name, u in fields.items():
+        ref, scale = refs[name]
+        u_pin.numpy()[:] = u
+        dev = F.fvm_eqs(torch.zeros(n, dtype=torch.float64, device="cuda"), u_pin.cuda(), prob, 0.0).cpu().numpy()
+        for _ in range(3):
+            du_pin.numpy()[:] = np.nan
+            F.fvm_eqs(du_pin.numpy(), u_pin.numpy(), prob, 0.0)
+            assert np.array_equal(du_pin.numpy(), dev), name
+        e2, einf = _errs(du_pin.numpy(), ref, scale)
+        assert e2 <= FP64_RTOL and einf <= FP64_RTOL, (name, e2, einf)
+
+
 def test_c2_rhs_fp32_against_oracle(gpu_lib, c2):
     import fvmgpu as F
 

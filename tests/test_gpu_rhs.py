@@ -214,8 +214,8 @@ def test_full_size_properties(gpu_lib):
 
 
 def test_rhs_pinned_host_buffers(gpu_lib):
-    """Page-locked host arrays take the zero-copy path (the permutation kernels read u and
-    write du over the host link); the result equals the pageable path bit for bit."""
+    """Page-locked host arrays take the one-launch path (host reads, product and host writes
+    overlapped); the result equals the pageable path bit for bit."""
     import torch
     import fvmgpu as F
 
@@ -229,4 +229,26 @@ def test_rhs_pinned_host_buffers(gpu_lib):
     u_pin.numpy()[:] = u
     for _ in range(2):
         F.fvm_eqs(du_pin.numpy(), u_pin.numpy(), prob, 0.0)
+        assert np.array_equal(du_pin.numpy(), ref)
+
+
+@pytest.mark.parametrize("make", [lambda: sine_diffusion(64), mixed_annulus, lambda: heat_convection(40)])
+def test_rhs_pinned_host_buffers_every_operator_form(gpu_lib, make):
+    """The one-launch host-array path on operators with Neumann constants (b), quadratic
+    diagonal terms (q), internal Dirichlet and Dudt rows: bit-identical to the pageable path,
+    and at t where time factors would enter b."""
+    import torch
+    import fvmgpu as F
+
+    spec = make()
+    prob = api_problem(spec)
+    n = spec.tri.num_points
+    rng = np.random.default_rng(9)
+    u_pin = torch.empty(n, dtype=torch.float64, pin_memory=True)
+    du_pin = torch.empty(n, dtype=torch.float64, pin_memory=True)
+    for _ in range(3):
+        u = np.asarray(spec.u0, dtype=np.float64) + rng.standard_normal(n)
+        ref = F.fvm_eqs(np.zeros(n), u, prob, 0.25)
+        u_pin.numpy()[:] = u
+        F.fvm_eqs(du_pin.numpy(), u_pin.numpy(), prob, 0.25)
         assert np.array_equal(du_pin.numpy(), ref)
