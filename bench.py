@@ -923,12 +923,83 @@ def run_adjoint(args, F, torch):
             "clocks": clocks}
 
 
+def _brusselator_system(F, n=100, tf=5.0):
+    """The Brusselator tutorial's system (unit square, fluxes -grad/4, sources Phi^2 Psi - 2 Phi
+    and -Phi^2 Psi + Phi, boundary values with exp(-t/2), exp(t/2) factors); its exact solution
+    is Phi = exp(-x - y - t/2), Psi = exp(x + y + t/2)."""
+    tri = F.triangulate_rectangle(0.0, 1.0, 0.0, 1.0, n, n, single_boundary=False)
+    mesh = F.FVMGeometry(tri)
+    phi_bc = (lambda x, y, t, u, p: -1 / 4 * np.exp(-x - t / 2), lambda x, y, t, u, p: 1 / 4 * np.exp(-1 - y - t / 2),
+              lambda x, y, t, u, p: np.exp(-1 - x - t / 2), lambda x, y, t, u, p: -1 / 4 * np.exp(-y - t / 2))
+    psi_bc = (lambda x, y, t, u, p: np.exp(x + t / 2), lambda x, y, t, u, p: -1 / 4 * np.exp(1 + y + t / 2),
+              lambda x, y, t, u, p: -1 / 4 * np.exp(1 + x + t / 2), lambda x, y, t, u, p: np.exp(y + t / 2))
+    P = tri.points
+    phi = F.FVMProblem(mesh, F.BoundaryConditions(mesh, phi_bc, (F.Neumann, F.Neumann, F.Dirichlet, F.Neumann)),
+                       flux_function=lambda x, y, t, a, b, g, p: (-a[0] / 4, -b[0] / 4),
+                       source_function=lambda x, y, t, u, p: u[0] ** 2 * u[1] - 2 * u[0],
+                       initial_condition=np.exp(-P[:, 0] - P[:, 1]), final_time=tf)
+    psi = F.FVMProblem(mesh, F.BoundaryConditions(mesh, psi_bc, (F.Dirichlet, F.Neumann, F.Neumann, F.Dirichlet)),
+                       flux_function=lambda x, y, t, a, b, g, p: (-a[1] / 4, -b[1] / 4),
+                       source_function=lambda x, y, t, u, p: -u[0] ** 2 * u[1] + u[0],
+                       initial_condition=np.exp(P[:, 0] + P[:, 1]), final_time=tf)
+    return tri, F.FVMSystem(phi, psi)
+
+
+def _steady_rows(F):
+    """SteadyFVMProblem: (1) the Laplace tutorial with an internal Dirichlet line (u = 0, 100y,
+    100, 100y on the unit square's sides, u = 0 on x = 1/2, y <= 2/5; a 201 x 201 lattice with a
+    column of points on the line), initial guess 100y, by NewtonRaphson and by DynamicSS;
+    (2) the Helmholtz tutorial at its size (div grad u + u = 0 on [-1, 1]^2, q.n = -1, 125 x 125),
+    NewtonRaphson from 0 and then DynamicSS from that solution, as the tutorial does."""
+    out = {}
+    tri = F.triangulate_rectangle(0.0, 1.0, 0.0, 1.0, 201, 201, single_boundary=False)
+    P = tri.points
+    on_line = (np.abs(P[:, 0] - 0.5) < 1e-12) & (P[:, 1] <= 0.4 + 1e-12)
+    mesh = F.FVMGeometry(tri)
+    BCs = F.BoundaryConditions(mesh, (lambda x, y, t, u, p: 0.0 * x, lambda x, y, t, u, p: 100 * y,
+                                      lambda x, y, t, u, p: 100.0 + 0.0 * x, lambda x, y, t, u, p: 100 * y),
+                               (F.Dirichlet,) * 4)
+    ICs = F.InternalConditions((lambda x, y, t, u, p: 0.0 * x,),
+                               dirichlet_nodes={int(i): 0 for i in np.nonzero(on_line)[0]})
+    u0 = np.where(on_line, 0.0, 100 * P[:, 1])
+    for name, alg in (("newton", F.NewtonRaphson()), ("dynamic_ss", F.DynamicSS(F.TRBDF2()))):
+        prob = F.FVMProblem(mesh, BCs, ICs, diffusion_function=lambda x, y, t, u, p: 1.0 + 0.0 * x,
+                            initial_condition=u0.copy(), final_time=np.inf)
+        t0 = time.perf_counter()
+        sol = F.solve(F.SteadyFVMProblem(prob), alg)
+        wall = time.perf_counter() - t0
+        out[f"laplace_internal_line_201x201_{name}"] = {
+            "points": tri.num_points, "wall_ms": 1e3 * wall, "device_ms": sol.stats["elapsed_ms"],
+            "iterations": sol.stats["iterations"], "krylov_iters": sol.stats["krylov_iters"],
+            "residual": sol.stats["residual"]}
+    tri = F.triangulate_rectangle(-1.0, 1.0, -1.0, 1.0, 125, 125, single_boundary=True)
+    mesh = F.FVMGeometry(tri)
+    prob = F.FVMProblem(mesh, F.BoundaryConditions(mesh, (lambda x, y, t, u, p: -1.0 + 0.0 * x,), (F.Neumann,)),
+                        diffusion_function=lambda x, y, t, u, p: 1.0 + 0.0 * x, source_function=lambda x, y, t, u, p: u,
+                        initial_condition=np.zeros(tri.num_points), final_time=np.inf)
+    steady = F.SteadyFVMProblem(prob)
+    t0 = time.perf_counter()
+    sol = F.solve(steady, F.NewtonRaphson())
+    wall_n = time.perf_counter() - t0
+    prob.initial_condition[:] = sol.u
+    t0 = time.perf_counter()
+    sol2 = F.solve(steady, F.DynamicSS(F.TRBDF2()))
+    wall_d = time.perf_counter() - t0
+    out["helmholtz_125x125"] = {"newton_wall_ms": 1e3 * wall_n, "newton_iterations": sol.stats["iterations"],
+                                "newton_krylov_iters": sol.stats["krylov_iters"], "newton_residual": sol.stats["residual"],
+                                "then_dynamic_ss_wall_ms": 1e3 * wall_d, "dynamic_ss_steps": sol2.stats["iterations"],
+                                "max_abs_change": float(np.max(np.abs(sol2.u - sol.u)))}
+    return out
+
+
 def run_implicit(F, c2_prob):
     """Implicit stepping (TR-BDF2 with the device JVP and matrix-free BiCGStab).  (1) The annulus
     tutorial (polar lattice stand-in, 2,304 vertices, time-dependent inner value, to t = 2,
     saveat 0.2) at the default tolerances: TR-BDF2 against Tsit5, which steps at its stability
     limit there.  (2) C2 (the 1M-vertex FVMProblem): 10 fixed TR-BDF2 steps of 1e-5, 100 times
-    the 1000-step Tsit5 row's dt."""
+    the 1000-step Tsit5 row's dt.  (3) The Brusselator tutorial's call, solve(system, TRBDF2(),
+    saveat = 1) on its 100 x 100 mesh to t = 5, against Tsit5 and the exact solution.  (4) The
+    steady-state tutorials' solves (SteadyFVMProblem with NewtonRaphson and DynamicSS)."""
     out = {}
     tri = F.triangulate_annulus(0.2, 1.0, 24, 96, nsegments=1)
     x, y = tri.points[:, 0], tri.points[:, 1]
@@ -960,7 +1031,33 @@ def run_implicit(F, c2_prob):
                                "newton_iters": sol.stats["newton_iters"], "krylov_iters": sol.stats["krylov_iters"],
                                "jvps": sol.stats["jvps"],
                                "krylov_iters_per_stage": sol.stats["krylov_iters"] / max(1, sol.stats["newton_iters"])}
+    try:
+        out["brusselator_tutorial_100x100"] = _brusselator_row(F)
+    except Exception as e:  # noqa: BLE001  (the rows above stand on their own)
+        out["brusselator_tutorial_100x100"] = {"error": repr(e)[:300]}
+    try:
+        out["steady_states"] = _steady_rows(F)
+    except Exception as e:  # noqa: BLE001
+        out["steady_states"] = {"error": repr(e)[:300]}
     return out
+
+
+def _brusselator_row(F):
+    tri, system = _brusselator_system(F)
+    P = tri.points
+    saveat = np.arange(0.0, 5.0 + 1e-12, 1.0)
+    row = {"points": tri.num_points, "unknowns": 2 * tri.num_points}
+    for name, alg in (("trbdf2", F.TRBDF2()), ("tsit5", F.Tsit5())):
+        t0 = time.perf_counter()
+        sol = F.solve(system, alg, saveat=saveat)
+        row[f"{name}_wall_ms"] = 1e3 * (time.perf_counter() - t0)
+        row[f"{name}_steps"] = sol.stats["naccept"]
+        if name == "trbdf2":
+            row["krylov_iters_per_newton"] = sol.stats["krylov_iters"] / max(1, sol.stats["newton_iters"])
+        ex = [np.stack([np.exp(-P[:, 0] - P[:, 1] - t / 2), np.exp(P[:, 0] + P[:, 1] + t / 2)]) for t in saveat]
+        row[f"{name}_max_rel_err_vs_exact"] = float(max(np.max(np.abs(u[c] - e[c])) / np.max(e[c])
+                                                        for u, e in zip(sol.u, ex) for c in range(2)))
+    return row
 
 
 def adjoint_dfma(npts, nnz, B, N, K):
