@@ -529,8 +529,11 @@ def run_c1(F, torch, reps=5):
     """C1, the README problem (triangulate_rectangle(0, 2, 0, 2, 50, 50, single_boundary=true),
     zero Dirichlet, D = 1/9, u0 = 50 where y <= 1): adaptive Tsit5 to t = 0.5 as the reference's
     documentation times it - the DiffusionEquation template with saveat = 0.05 (published
-    5.736 ms, hardware unstated) - and the FVMProblem with saveat = 0.001 (test/README.jl).
-    Wall time of the whole `solve` call, best of `reps` after one warm-up."""
+    5.736 ms, hardware unstated) - and the FVMProblem with saveat = 0.001 (test/README.jl); the
+    FVMProblem with TRBDF2 and saveat 0.05 (published 49.237 ms); the docs' 100 x 100 Poisson
+    problem as a SteadyFVMProblem with DynamicSS(TRBDF2) (published 189.406 ms) and as the
+    PoissonsEquation template (published 15.442 ms).  Wall time of the whole `solve` call, best
+    of `reps` after one warm-up."""
     from fvmgpu.meshes import triangulate_rectangle
 
     tri = triangulate_rectangle(0.0, 2.0, 0.0, 2.0, 50, 50, single_boundary=True)
@@ -554,6 +557,51 @@ def run_c1(F, torch, reps=5):
         out[name] = {"wall_ms": 1e3 * best, "device_ms": stats["elapsed_ms"], "steps": stats["naccept"],
                      "rejected": stats["nreject"], "saves": len(sol.u), "driver": stats["driver"]}
     out["template_saveat_0.05"]["published_reference_ms"] = 5.736
+    # the same FVMProblem with TRBDF2 (published 49.237 ms with KLU factorisations)
+    F.solve(prob, F.TRBDF2(), saveat=0.05)
+    best, stats = float("inf"), None
+    for _ in range(reps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sol = F.solve(prob, F.TRBDF2(), saveat=0.05)
+        best = min(best, time.perf_counter() - t0)
+        stats = sol.stats
+    out["fvmproblem_trbdf2_saveat_0.05"] = {"wall_ms": 1e3 * best, "device_ms": stats["elapsed_ms"],
+                                            "steps": stats["naccept"], "rejected": stats["nreject"],
+                                            "published_reference_ms": 49.237}
+    # docs/src/literate_wyos/poissons_equation.jl: the 100 x 100 Poisson problem as a
+    # SteadyFVMProblem solved by DynamicSS(TRBDF2) (published 189.406 ms) and as the template
+    # (published 15.442 ms with KLU); both against the exact solution at the docs' rtol 1e-4
+    tri = triangulate_rectangle(0.0, 1.0, 0.0, 1.0, 100, 100, single_boundary=True)
+    mesh = F.FVMGeometry(tri)
+    BCs = F.BoundaryConditions(mesh, zero_bc, F.Dirichlet)
+    P = tri.points
+    exact = np.sin(np.pi * P[:, 0]) * np.sin(np.pi * P[:, 1]) / (2 * np.pi ** 2)
+    rel = lambda u: float(np.linalg.norm(u - exact) / np.linalg.norm(exact))  # noqa: E731
+    sprob = F.FVMProblem(mesh, BCs, diffusion_function=lambda x, y, t, u, p: 1.0 + 0.0 * x,
+                         source_function=lambda x, y, t, u, p: np.sin(np.pi * x) * np.sin(np.pi * y),
+                         initial_condition=np.zeros(tri.num_points), final_time=np.inf)
+    steady = F.SteadyFVMProblem(sprob)
+    F.solve(steady, F.DynamicSS(F.TRBDF2()))
+    best, sol = float("inf"), None
+    for _ in range(reps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sol = F.solve(steady, F.DynamicSS(F.TRBDF2()))
+        best = min(best, time.perf_counter() - t0)
+    out["poisson_100x100_steady_dynamic_ss"] = {"wall_ms": 1e3 * best, "device_ms": sol.stats["elapsed_ms"],
+                                                "steps": sol.stats["iterations"], "rel_err_vs_exact": rel(sol.u),
+                                                "published_reference_ms": 189.406}
+    pois = F.PoissonsEquation(mesh, BCs, source_function=lambda x, y, p: -np.sin(np.pi * x) * np.sin(np.pi * y))
+    F.solve(pois)
+    best, sol = float("inf"), None
+    for _ in range(reps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sol = F.solve(pois)
+        best = min(best, time.perf_counter() - t0)
+    out["poisson_100x100_template"] = {"wall_ms": 1e3 * best, "iterations": sol.stats["iterations"],
+                                       "rel_err_vs_exact": rel(sol.u), "published_reference_ms": 15.442}
     return out
 
 
