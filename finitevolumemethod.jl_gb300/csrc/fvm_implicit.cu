@@ -21,6 +21,7 @@
 // are the cubic Hermite interpolant of (u_n, f_n), (u_{n+1}, f_{n+1}).  The Dirichlet update
 // runs after every accepted step, as with Tsit5.
 #include "fvm_internal.h"
+#include "fvm_tma.cuh"
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -264,6 +265,275 @@ __global__ void kd_rho_kernel(KDev* kd, const double* part) {
         kd->status = 2;
 }
 
+// ---------------------------------------------------------------------------------------
+// The whole BiCGStab solve in one cooperative launch, for an operator J = A (+ diag(2 q u))
+// held as a sliced-ELL matrix (the linear problems and the time-dependent templates).  At
+// small and medium sizes an iteration of the launch-per-step solver is a dozen launches of a
+// few microseconds each; here it is three grid barriers.  CTA c owns the contiguous slices
+// [S c / G, S (c+1) / G) for every vector operation and product, one warp per slice.  Each
+// iteration has three phases, each ending in a grid barrier:
+//   A  p = r + beta (p' - omega v') (ping-pong: p', v' are the previous iteration's, read by
+//      the neighbours' gathers, which form p on the fly), v = W (p / dw), partial <rhat, v>
+//   B  s = r - alpha v, t = W (s / dw) (the gathers form s on the fly), partials <t,s>, <t,t>
+//   C  x += alpha p/dw + omega s/dw, r = s - omega t, partials <rhat,r>, <r,r>
+// Every CTA sums the G partials in the same fixed tree, so every CTA holds the same scalars and
+// takes the same branch (converged, breakdown, iteration limit).  Values another CTA wrote in
+// this launch are read through L2 (ld.global.cg).  The grid barrier is a counter and a
+// generation word; its wait is bounded, and a barrier that runs out sets the error word and
+// ends the solve with a breakdown status.
+// ---------------------------------------------------------------------------------------
+constexpr int kCoopThreads = 256;
+constexpr int kCoopMaxCtas = 256;             // one partial per thread of the final sum
+constexpr unsigned kDevErrGridBarrier = 8u;   // a grid barrier of the cooperative solve ran out
+
+struct CoopResult {
+    int32_t status, it;  // 1 converged, 2 breakdown or iteration limit
+};
+
+struct CoopKrylov {
+    const int64_t* slice_ptr;
+    const int32_t* width;
+    const int32_t* col;
+    const double* val;   // A
+    const double* q;     // J = A + diag(2 q u), or null
+    const double* u;     // J's point (for q)
+    const double* mask;  // W = diag(mask) - c J, or null for I - c J
+    double c;
+    const double* dw;    // diag(W), the Jacobi preconditioner
+    const double* b;
+    double* x;
+    double *r, *rhat, *p0, *p1, *v0, *v1, *s, *t;
+    double* part;        // [2][kCoopMaxCtas]
+    unsigned *bar_count, *bar_gen, *err;
+    CoopResult* res;
+    int64_t n, nslices;
+    double tol2;
+    int maxit;
+    unsigned long long wait_ns;
+};
+
+__device__ __forceinline__ unsigned coop_ld_acquire(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void coop_st_release(unsigned* p, unsigned v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// all CTAs of the (co-resident) grid; false when the wait ran out
+__device__ bool coop_grid_barrier(const CoopKrylov& k, int* s_ok) {
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        const unsigned g = coop_ld_acquire(k.bar_gen);
+        if (atomicAdd(k.bar_count, 1u) + 1u == gridDim.x) {
+            atomicExch(k.bar_count, 0u);
+            __threadfence();
+            coop_st_release(k.bar_gen, g + 1u);
+        } else {
+            const unsigned long long t0 = global_ns();
+            while (coop_ld_acquire(k.bar_gen) == g) {
+                __nanosleep(32);
+                if (global_ns() - t0 > k.wait_ns) {
+                    atomicOr(k.err, kDevErrGridBarrier);
+                    ok = 0;
+                    break;
+                }
+            }
+        }
+        __threadfence();
+        *s_ok = ok;
+    }
+    __syncthreads();
+    return *s_ok != 0;
+}
+
+// the CTA's partial sums of a0 (and a1) into part[0][cta] (part[1][cta]), fixed order
+__device__ void coop_block_partials(double a0, double a1, const CoopKrylov& k, double (*red)[kCoopThreads / 32]) {
+    for (int o = 16; o > 0; o >>= 1) {
+        a0 += __shfl_down_sync(0xffffffffu, a0, o);
+        a1 += __shfl_down_sync(0xffffffffu, a1, o);
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) {
+        red[0][warp] = a0;
+        red[1][warp] = a1;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s0 = 0.0, s1 = 0.0;
+        for (int w = 0; w < kCoopThreads / 32; ++w) {
+            s0 += red[0][w];
+            s1 += red[1][w];
+        }
+        k.part[blockIdx.x] = s0;
+        k.part[kCoopMaxCtas + blockIdx.x] = s1;
+    }
+}
+
+// the two sums over the grid's partials, by the same fixed tree in every CTA (after a barrier)
+__device__ void coop_grid_sums(const CoopKrylov& k, double (*fin)[kCoopThreads], double& s0, double& s1) {
+    const int t = threadIdx.x;
+    fin[0][t] = t < (int)gridDim.x ? __ldcg(&k.part[t]) : 0.0;
+    fin[1][t] = t < (int)gridDim.x ? __ldcg(&k.part[kCoopMaxCtas + t]) : 0.0;
+    __syncthreads();
+    for (int w = kCoopThreads / 2; w > 0; w >>= 1) {
+        if (t < w) {
+            fin[0][t] += fin[0][t + w];
+            fin[1][t] += fin[1][t + w];
+        }
+        __syncthreads();
+    }
+    s0 = fin[0][0];
+    s1 = fin[1][0];
+    __syncthreads();  // fin is reused by the next sum
+}
+
+// the product W y at row i for y formed on the fly by ycol(col): y_i / dw_i times the mask (or 1)
+// minus c (A y + 2 q u y)_i
+template <class Y>
+__device__ __forceinline__ double coop_w_row(const CoopKrylov& k, int64_t s, int lane, int64_t i, double yi,
+                                             Y ycol) {
+    const int64_t base = __ldg(&k.slice_ptr[s]) + lane;
+    const int w = __ldg(&k.width[s]);
+    double acc = 0.0;
+#pragma unroll 4
+    for (int j = 0; j < w; ++j) {
+        const int64_t slot = base + (int64_t)j * 32;
+        const int32_t c = __ldg(&k.col[slot]);
+        acc += __ldg(&k.val[slot]) * (ycol(c) / __ldg(&k.dw[c]));
+    }
+    const double yh = yi / __ldg(&k.dw[i]);
+    if (k.q) acc += 2.0 * __ldg(&k.q[i]) * __ldg(&k.u[i]) * yh;
+    const double m = k.mask ? __ldg(&k.mask[i]) : 1.0;
+    return m * yh - k.c * acc;
+}
+
+__global__ void __launch_bounds__(kCoopThreads) coop_bicgstab_kernel(const CoopKrylov k) {
+    __shared__ double red[2][kCoopThreads / 32];
+    __shared__ double fin[2][kCoopThreads];
+    __shared__ int s_ok;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t s0 = k.nslices * blockIdx.x / gridDim.x, s1 = k.nslices * (blockIdx.x + 1) / gridDim.x;
+    constexpr int kWarps = kCoopThreads / 32;
+    // r = rhat = b, x = 0
+    double a0 = 0.0, a1 = 0.0;
+    for (int64_t s = s0 + warp; s < s1; s += kWarps) {
+        const int64_t i = s * 32 + lane;
+        if (i >= k.n) continue;
+        const double bi = __ldg(&k.b[i]);
+        k.r[i] = bi;
+        k.rhat[i] = bi;
+        k.x[i] = 0.0;
+        a0 += bi * bi;
+    }
+    coop_block_partials(a0, a0, k, red);
+    bool ok = coop_grid_barrier(k, &s_ok);
+    double rho, bb;
+    coop_grid_sums(k, fin, rho, bb);
+    double rho_prev = 1.0, alpha = 1.0, omega = 1.0;
+    int status = (ok && bb > 0.0) ? 0 : (ok ? 1 : 2);
+    int it = 0;
+    const double* po = k.p0;
+    const double* vo = k.v0;
+    double* pn = k.p1;
+    double* vn = k.v1;
+    while (status == 0) {
+        if (it >= k.maxit) {
+            status = 2;
+            break;
+        }
+        const double beta = it == 0 ? 0.0 : (rho / rho_prev) * (alpha / omega);
+        const bool first = it == 0;
+        // A: p = r + beta (p' - omega v'), v = W (p / dw)
+        const double* r = k.r;
+        auto pcol = [&](int32_t c) {
+            const double rc = __ldcg(&r[c]);
+            return first ? rc : rc + beta * (__ldcg(&po[c]) - omega * __ldcg(&vo[c]));
+        };
+        a0 = 0.0;
+        for (int64_t s = s0 + warp; s < s1; s += kWarps) {
+            const int64_t i = s * 32 + lane;
+            if (i >= k.n) continue;
+            const double pi = pcol((int32_t)i);
+            const double vi = coop_w_row(k, s, lane, i, pi, pcol);
+            pn[i] = pi;
+            vn[i] = vi;
+            a0 += __ldcg(&k.rhat[i]) * vi;
+        }
+        coop_block_partials(a0, 0.0, k, red);
+        ok = coop_grid_barrier(k, &s_ok);
+        double rv, unused;
+        coop_grid_sums(k, fin, rv, unused);
+        if (!ok || !(rv != 0.0) || !isfinite(rv)) {
+            status = 2;
+            break;
+        }
+        alpha = rho / rv;
+        // B: s = r - alpha v, t = W (s / dw)
+        auto scol = [&](int32_t c) { return __ldcg(&r[c]) - alpha * __ldcg(&vn[c]); };
+        a0 = a1 = 0.0;
+        for (int64_t s = s0 + warp; s < s1; s += kWarps) {
+            const int64_t i = s * 32 + lane;
+            if (i >= k.n) continue;
+            const double si = scol((int32_t)i);
+            const double ti = coop_w_row(k, s, lane, i, si, scol);
+            k.s[i] = si;
+            k.t[i] = ti;
+            a0 += ti * si;
+            a1 += ti * ti;
+        }
+        coop_block_partials(a0, a1, k, red);
+        ok = coop_grid_barrier(k, &s_ok);
+        double ts, tt;
+        coop_grid_sums(k, fin, ts, tt);
+        if (!ok) {
+            status = 2;
+            break;
+        }
+        omega = tt > 0.0 ? ts / tt : 0.0;
+        // C: x += alpha p/dw + omega s/dw, r = s - omega t
+        a0 = a1 = 0.0;
+        for (int64_t s = s0 + warp; s < s1; s += kWarps) {
+            const int64_t i = s * 32 + lane;
+            if (i >= k.n) continue;
+            const double dwi = __ldg(&k.dw[i]);
+            const double si = __ldcg(&k.s[i]);
+            k.x[i] = __ldcg(&k.x[i]) + alpha * (__ldcg(&pn[i]) / dwi) + omega * (si / dwi);
+            const double ri = si - omega * __ldcg(&k.t[i]);
+            k.r[i] = ri;
+            a0 += __ldcg(&k.rhat[i]) * ri;
+            a1 += ri * ri;
+        }
+        coop_block_partials(a0, a1, k, red);
+        ok = coop_grid_barrier(k, &s_ok);
+        double rho_new, rr;
+        coop_grid_sums(k, fin, rho_new, rr);
+        ++it;
+        rho_prev = rho;
+        rho = rho_new;
+        if (!ok || !isfinite(rr))
+            status = 2;
+        else if (rr <= k.tol2 * bb)
+            status = 1;
+        else if (!(omega != 0.0) || !(rho != 0.0))
+            status = 2;
+        // the next iteration reads this one's p and v
+        const double* tp = po;
+        po = pn;
+        pn = const_cast<double*>(tp);
+        const double* tv = vo;
+        vo = vn;
+        vn = const_cast<double*>(tv);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        k.res->status = status;
+        k.res->it = it;
+    }
+}
+
 // Hermite interpolation of a saved value inside a step
 __global__ void hermite_kernel(double* out, const double* u0, const double* f0, const double* u1, const double* f1,
                                double h, double th, int64_t n) {
@@ -394,6 +664,48 @@ struct Trbdf2 {
                               &r, &rhat, &pv, &ph, &v, &sv, &sh, &t, &x};
         for (int k = 0; k < nv; ++k) *slots[k] = q + (int64_t)k * n;
         kdev.alloc(sizeof(KDev));
+        if (R->op_pat && R->op_val && n > 0 && n <= kCoopMaxRows) {
+            int per_sm = 0, sms = 0, dev = 0;
+            FVM_CUDA(cudaGetDevice(&dev));
+            FVM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+            FVM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, coop_bicgstab_kernel, kCoopThreads, 0));
+            // about one slice per warp, within what can be co-resident
+            const int64_t want = (R->op_pat->nslices + kCoopThreads / 32 - 1) / (kCoopThreads / 32);
+            coop_grid = (int)std::min<int64_t>({want, (int64_t)per_sm * sms, (int64_t)kCoopMaxCtas});
+            if (coop_grid >= 1) {
+                coop_buf.alloc(sizeof(double) * 2 * kCoopMaxCtas + 64);
+                use_coop = true;
+            }
+        }
+    }
+    // the cooperative solve (one launch per Krylov solve) for small operators: measured faster up
+    // to 15,625 unknowns (2-2.3x per TR-BDF2 solve), slower at 40,401 (its barriers and chained
+    // gathers then cost more than the launches they save)
+    static constexpr int64_t kCoopMaxRows = 1 << 15;
+    bool use_coop = false;
+    int coop_grid = 0;
+    DBuf coop_buf;  // partials [2][kCoopMaxCtas], then the result and the barrier words
+    bool solve_coop(const double* b, double* xo, double rtol, int maxit) {
+        double* part = coop_buf.as<double>();
+        CoopResult* res = reinterpret_cast<CoopResult*>(part + 2 * kCoopMaxCtas);
+        unsigned* bar = reinterpret_cast<unsigned*>(res + 1);
+        FVM_CUDA(cudaMemsetAsync(res, 0, sizeof(CoopResult) + 2 * sizeof(unsigned), s));
+        const SellPattern& pat = *R->op_pat;
+        CoopKrylov k{pat.d_slice_ptr.as<int64_t>(), pat.d_width.as<int32_t>(), pat.d_col.as<int32_t>(), R->op_val,
+                     R->op_q, wu, wmask, wd, dw, b, xo, r, rhat, pv, ph, v, sh, sv, t, part, bar, bar + 1,
+                     device_error_word(), res, n, pat.nslices, rtol * rtol, maxit, kWaitLimitNs};
+        void* args[] = {&k};
+        FVM_CUDA(cudaLaunchCooperativeKernel((const void*)coop_bicgstab_kernel, dim3((unsigned)coop_grid),
+                                             dim3(kCoopThreads), args, 0, s));
+        CoopResult h{};
+        FVM_CUDA(cudaMemcpyAsync(&h, res, sizeof h, cudaMemcpyDeviceToHost, s));
+        FVM_CUDA(cudaStreamSynchronize(s));
+        if (unsigned e = take_device_error())
+            fail(FVM_ERR_CUDA, "the cooperative Krylov solve timed out in a bounded wait (device error bits " +
+                                   std::to_string(e) + ")");
+        krylov += h.it;
+        jvps += 2 * (int64_t)h.it;
+        return h.status == 1;
     }
     void rhs(const double* y, double* out, double tt) {
         R->f(y, out, tt, s);
@@ -422,6 +734,7 @@ struct Trbdf2 {
     // The iterations run without host round trips; the host reads the scalars every kCheck.
     static constexpr int kCheck = 8;
     bool solve(const double* b, double* xo, double rtol, int maxit) {
+        if (use_coop) return solve_coop(b, xo, rtol, maxit);
         FVM_CUDA(cudaMemsetAsync(xo, 0, sizeof(double) * n, s));
         FVM_CUDA(cudaMemcpyAsync(r, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
         FVM_CUDA(cudaMemcpyAsync(rhat, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
@@ -902,6 +1215,11 @@ int fvm_trbdf2_solve(fvm_problem* p, const double* u0, const fvm_ode_options* o,
         R.callback_varies = p->tdir_varies;
         R.affine = p->linear && !p->has_q && p->precision != FVM_FP32;
         fvm_mesh* m = p->mesh;
+        if (p->linear && p->precision == FVM_FP64) {  // J v = A v + 2 q u v, the assembled operator
+            R.op_pat = &m->pat;
+            R.op_val = p->d_val64.as<double>();
+            R.op_q = p->has_q ? p->d_q.as<double>() : nullptr;
+        }
         return trbdf2_run(R, m->d_perm.as<int32_t>(), m->d_iperm.as<int32_t>(), m->np, u0, o, out, st, ist, stream);
     });
 }
@@ -929,6 +1247,8 @@ int fvm_template_trbdf2_solve(fvm_template* T, const double* u0, const fvm_ode_o
                 T->d_val64.as<double>(), nullptr, m->np, d);
         };
         R.affine = true;
+        R.op_pat = &m->pat;
+        R.op_val = T->d_val64.as<double>();
         return trbdf2_run(R, m->d_perm.as<int32_t>(), m->d_iperm.as<int32_t>(), m->np, u0, o, out, st, ist, stream);
     });
 }
@@ -956,6 +1276,11 @@ int fvm_steady_solve(fvm_problem* p, const double* u0, const fvm_steady_options*
         R.callback_varies = p->tdir_varies;
         R.affine = p->linear && !p->has_q && p->precision != FVM_FP32;
         R.fixed = d_fixed.as<double>();
+        if (p->linear && p->precision == FVM_FP64) {
+            R.op_pat = &m->pat;
+            R.op_val = p->d_val64.as<double>();
+            R.op_q = p->has_q ? p->d_q.as<double>() : nullptr;
+        }
         steady_run(R, m->d_perm.as<int32_t>(), m->d_iperm.as<int32_t>(), m->np, u0, o, out, st, stream);
         return FVM_OK;
     });

@@ -489,6 +489,11 @@ struct ImplicitRhs {
     bool callback_varies = false;
     bool affine = false;
     const double* fixed = nullptr;  // steady Newton: 1 on the rows the problem fixes, else 0 (internal)
+    // when J v is exactly A v (+ 2 q u v) for a sliced-ELL A on op_pat: the Krylov solves may run
+    // as one cooperative launch (fvm_implicit.cu) instead of a launch per vector operation
+    const SellPattern* op_pat = nullptr;
+    const double* op_val = nullptr;
+    const double* op_q = nullptr;
 };
 // DynamicSS's stopping test on a TR-BDF2 run: after each accepted step, max|f(u)| <= abstol or
 // <= reltol max|f(u) + u| ends the run with u as its one output
