@@ -4,7 +4,10 @@
  * Every entry point returns an int status (FVM_OK = 0) and never aborts the
  * process; fvm_last_error() gives the message of the last failure on the
  * calling thread.  Handles are opaque and owned by the library; free them with
- * the matching *_destroy.  Input host arrays are copied at creation.  All
+ * the matching *_destroy.  A mesh and every handle built on it (its problems,
+ * templates, systems, batches) are used by one host thread at a time: they share
+ * per-mesh work state that is built and reused on demand.  Input host arrays are
+ * copied at creation.  All
  * vertex, triangle and edge indices are 0-based and in the caller's
  * ("reference") numbering; internally the library renumbers vertices along a
  * Hilbert curve and maps back at the boundary.
