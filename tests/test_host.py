@@ -281,3 +281,29 @@ def test_classification_checks_every_point():
                                            time=True)
     assert deg == 0 and tau[0] == 1.0 and abs(tau[2] + 1.0) < 1e-12
     assert abs(B[5] - 1.0) < 1e-12 and np.all(B[np.arange(n) != 5] == 0)
+
+
+def test_time_factor_fit_with_an_infinite_final_time():
+    """A steady problem's final time is Inf: the time-factor fit then samples t0 + [0, 1] and
+    still recovers a factor, or finds none for values that do not depend on t."""
+    x = np.linspace(0.0, 1.0, 7)
+    fit = forms.fit_time_factor(lambda t: 2.0 + x * np.exp(-0.5 * t), 0.0, np.inf, "test")
+    assert fit is not None
+    A, tau, B = fit
+    for t in (0.0, 0.3, 4.0):
+        assert np.allclose(A + tau(t) * B, 2.0 + x * np.exp(-0.5 * t), rtol=1e-12, atol=1e-12)
+    assert forms.fit_time_factor(lambda t: 1.0 + x, 0.0, np.inf, "test") is None
+
+
+def test_steady_types_without_a_device():
+    """SteadyFVMProblem wraps problems and systems only; the steady methods' defaults are
+    SteadyStateDiffEq's DynamicSS (abstol 1e-8, reltol 1e-6, tspan Inf) and a tight Newton."""
+    import fvmgpu as F
+
+    with pytest.raises(TypeError):
+        F.SteadyFVMProblem(object())
+    d = F.DynamicSS(F.TRBDF2())
+    assert (d.abstol, d.reltol, d.tspan) == (1e-8, 1e-6, float("inf"))
+    assert isinstance(d.alg, F.TRBDF2)
+    n = F.NewtonRaphson()
+    assert (n.abstol, n.reltol, n.max_iters) == (1e-10, 1e-10, 50)
