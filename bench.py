@@ -289,6 +289,37 @@ def cpu_baseline(tri, max_seconds=10.0, max_evals=200, nthreads=0):
             "ms_per_eval": 1e3 * dt / k}
 
 
+def _saveat_list(t0, tf, step):
+    """t0, t0 + step, ..., tf (the saves of `saveat = step`)."""
+    n = int(np.floor((tf - t0) / step + 1e-9))
+    ts = [t0 + step * k for k in range(n + 1)]
+    if ts[-1] < tf - 1e-12 * max(1.0, abs(tf)):
+        ts.append(tf)
+    return ts
+
+
+def cpu_trbdf2_baseline(tri, u0, D, tf, saveat):
+    """CPU baseline of an FVMProblem's TRBDF2 solve (zero Dirichlet, diffusivity D(x, y)): the
+    oracle's TR-BDF2 (the same step control as the device) with exact sparse LU solves of
+    W = I - d h J (scipy's SuperLU, the role KLU plays in the reference's tutorials) and the
+    oracle's fvm_eqs!, one host thread.  The Jacobian is formed once by coloured differences
+    (the problem is affine), inside the timed region."""
+    import fvm_oracle as O
+
+    conds = O.Conditions(tri, [lambda x, y, t, u: 0.0 * x] * tri.num_ghost_vertices,
+                         ["Dirichlet"] * tri.num_ghost_vertices)
+    prob = O.Problem(tri, conds, D=lambda x, y, t, u: D(x, y) + 0.0 * x, u0=u0, t0=0.0, tf=tf)
+    f = lambda u, t: O.fvm_eqs(prob, u, t)  # noqa: E731
+    cb = lambda u, t: O.update_dirichlet_nodes(prob, u, t)  # noqa: E731
+    ent, n = O.jacobian_sparsity(tri)
+    t0 = time.perf_counter()
+    J = O.colored_jacobian(f, u0, 0.0, ent, n, affine=True)
+    sol, st = O.trbdf2_solve(f, lambda u, t: J, u0, 0.0, tf, saveat, callback=cb, affine=True)
+    wall = time.perf_counter() - t0
+    return {"wall_ms": 1e3 * wall, "steps": st["naccept"], "rejected": st["nreject"], "kind": "port", "cores": 1,
+            "sample": "the whole solve: oracle TR-BDF2 with SuperLU factorisations, numpy fvm_eqs!"}
+
+
 def bench_config(tri, ws=1):
     """The `config` object both arms print (identical keys and values)."""
     return {"workload": WORKLOAD, "nv": tri.num_points, "nt": tri.num_triangles, "nbe": tri.num_boundary_edges,
@@ -504,7 +535,7 @@ def run_selected(args, F, torch, tri, mesh, prob, flush, u_int, peak):
             res[prec] = {k: r[k] for k in ("us", "gbs", "frac", "alg_bytes", "launches")}
         return res
 
-    rows = {"c1_readme": lambda: run_c1(F, torch), "rhs_fp32": rhs_fp32, "rhs_fp64_conservative": rhs_fp64_conservative,
+    rows = {"c1_readme": lambda: run_c1(F, torch, cpu=not args.no_cpu_baseline), "rhs_fp32": rhs_fp32, "rhs_fp64_conservative": rhs_fp64_conservative,
             "rhs_triangle_fp64": rhs_triangle_fp64, "tsit5_1000_steps": tsit5_1000_steps,
             "template_spmv": template_spmv, "batched_c4": lambda: run_batched(args, F, torch, flush, peak),
             "multimesh_c4": lambda: run_multimesh(args, F, torch), "adjoint_c5": lambda: run_adjoint(args, F, torch),
@@ -525,7 +556,7 @@ def run_selected(args, F, torch, tri, mesh, prob, flush, u_int, peak):
             emit_row(name, out)
 
 
-def run_c1(F, torch, reps=5):
+def run_c1(F, torch, reps=5, cpu=True):
     """C1, the README problem (triangulate_rectangle(0, 2, 0, 2, 50, 50, single_boundary=true),
     zero Dirichlet, D = 1/9, u0 = 50 where y <= 1): adaptive Tsit5 to t = 0.5 as the reference's
     documentation times it - the DiffusionEquation template with saveat = 0.05 (published
@@ -569,6 +600,12 @@ def run_c1(F, torch, reps=5):
     out["fvmproblem_trbdf2_saveat_0.05"] = {"wall_ms": 1e3 * best, "device_ms": stats["elapsed_ms"],
                                             "steps": stats["naccept"], "rejected": stats["nreject"],
                                             "published_reference_ms": 49.237}
+    if cpu:
+        try:
+            out["fvmproblem_trbdf2_saveat_0.05"]["cpu_baseline"] = cpu_trbdf2_baseline(
+                tri, u0, lambda x, y: 1 / 9 + 0.0 * x, 0.5, _saveat_list(0.0, 0.5, 0.05))
+        except Exception as e:  # noqa: BLE001
+            out["fvmproblem_trbdf2_saveat_0.05"]["cpu_baseline"] = {"error": repr(e)[:200]}
     # docs/src/literate_wyos/poissons_equation.jl: the 100 x 100 Poisson problem as a
     # SteadyFVMProblem solved by DynamicSS(TRBDF2) (published 189.406 ms) and as the template
     # (published 15.442 ms with KLU); both against the exact solution at the docs' rtol 1e-4
