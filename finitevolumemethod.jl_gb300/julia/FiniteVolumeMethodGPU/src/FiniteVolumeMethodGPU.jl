@@ -18,11 +18,14 @@ or the steady Krylov solve), batched instances (`GPUBatch`), the discrete adjoin
 templates (`GPUAdjoint`, with a `ChainRulesCore.rrule` for `adjoint_solve`) and device point
 location / interpolation (`locate`, `interpolate`).  With OrdinaryDiffEqTsit5 loaded, the package
 extension adds `CommonSolve.solve(prob, Tsit5(); saveat, ...)` methods for `FVMProblem`,
-`FVMSystem`, `DiffusionEquation` and `LinearReactionDiffusionEquation`, so scripts written for
-the reference run unchanged, and `CommonSolve.solve(tmpl, GPUKrylov())` for the steady templates.
+`FVMSystem`, `DiffusionEquation` and `LinearReactionDiffusionEquation`, and
+`CommonSolve.solve(prob, TRBDF2(...))` for all but the templates' steady kinds, so scripts written
+for the reference run unchanged; `CommonSolve.solve(tmpl, GPUKrylov())` solves the steady
+templates and `CommonSolve.solve(SteadyFVMProblem(prob), GPUSteady(...))` a steady problem.
 
-This layer has not been executed: Julia is not installed on the machines this build was
-developed and measured on.
+This layer has not been executed: Julia was not available where the library was developed and
+measured.  A CPU test checks every ccall's argument types and every struct's layout against the
+C header.
 """
 module FiniteVolumeMethodGPU
 
