@@ -19,7 +19,7 @@ templates (`GPUAdjoint`, with a `ChainRulesCore.rrule` for `adjoint_solve`) and 
 location / interpolation (`locate`, `interpolate`).  With OrdinaryDiffEqTsit5 loaded, the package
 extension adds `CommonSolve.solve(prob, Tsit5(); saveat, ...)` methods for `FVMProblem`,
 `FVMSystem`, `DiffusionEquation` and `LinearReactionDiffusionEquation`, and
-`CommonSolve.solve(prob, TRBDF2(...))` for all but the templates' steady kinds, so scripts written
+`CommonSolve.solve(prob, TRBDF2(...))` for the same four types, so scripts written
 for the reference run unchanged; `CommonSolve.solve(tmpl, GPUKrylov())` solves the steady
 templates and `CommonSolve.solve(SteadyFVMProblem(prob), GPUSteady(...))` a steady problem.
 
