@@ -298,26 +298,30 @@ def _saveat_list(t0, tf, step):
     return ts
 
 
-def cpu_trbdf2_baseline(tri, u0, D, tf, saveat):
-    """CPU baseline of an FVMProblem's TRBDF2 solve (zero Dirichlet, diffusivity D(x, y)): the
+def cpu_trbdf2_baseline(tri, u0, dconst, tf, saveat):
+    """CPU baseline of an FVMProblem's TRBDF2 solve (zero Dirichlet, constant diffusivity): the
     oracle's TR-BDF2 (the same step control as the device) with exact sparse LU solves of
-    W = I - d h J (scipy's SuperLU, the role KLU plays in the reference's tutorials) and the
-    oracle's fvm_eqs!, one host thread.  The Jacobian is formed once by coloured differences
-    (the problem is affine), inside the timed region."""
+    W = I - d h J (scipy's SuperLU, the role KLU plays in the reference's tutorials) and the C
+    restatement of fvm_eqs!, one host thread.  The Jacobian is formed once by coloured
+    differences (the problem is affine), inside the timed region."""
+    import build_oracle as B
     import fvm_oracle as O
 
     conds = O.Conditions(tri, [lambda x, y, t, u: 0.0 * x] * tri.num_ghost_vertices,
                          ["Dirichlet"] * tri.num_ghost_vertices)
-    prob = O.Problem(tri, conds, D=lambda x, y, t, u: D(x, y) + 0.0 * x, u0=u0, t0=0.0, tf=tf)
-    f = lambda u, t: O.fvm_eqs(prob, u, t)  # noqa: E731
+    prob = O.Problem(tri, conds, D=lambda x, y, t, u: dconst + 0.0 * x, u0=u0, t0=0.0, tf=tf)
+    cp = B.CProblem(prob.geo, tri, prob.code, B.D_CONST, (dconst,), prob.bnd_tri)
+    f = lambda u, t: cp.rhs_serial(np.ascontiguousarray(u), t)  # noqa: E731
     cb = lambda u, t: O.update_dirichlet_nodes(prob, u, t)  # noqa: E731
     ent, n = O.jacobian_sparsity(tri)
-    t0 = time.perf_counter()
-    J = O.colored_jacobian(f, u0, 0.0, ent, n, affine=True)
-    sol, st = O.trbdf2_solve(f, lambda u, t: J, u0, 0.0, tf, saveat, callback=cb, affine=True)
-    wall = time.perf_counter() - t0
+    wall = float("inf")
+    for _ in range(2):  # best of two: the first also loads the C library
+        t0 = time.perf_counter()
+        J = O.colored_jacobian(f, u0, 0.0, ent, n, affine=True)
+        sol, st = O.trbdf2_solve(f, lambda u, t: J, u0, 0.0, tf, saveat, callback=cb, affine=True)
+        wall = min(wall, time.perf_counter() - t0)
     return {"wall_ms": 1e3 * wall, "steps": st["naccept"], "rejected": st["nreject"], "kind": "port", "cores": 1,
-            "sample": "the whole solve: oracle TR-BDF2 with SuperLU factorisations, numpy fvm_eqs!"}
+            "sample": "the whole solve, best of two: oracle TR-BDF2 with SuperLU factorisations, C fvm_eqs!"}
 
 
 def bench_config(tri, ws=1):
@@ -603,7 +607,7 @@ def run_c1(F, torch, reps=5, cpu=True):
     if cpu:
         try:
             out["fvmproblem_trbdf2_saveat_0.05"]["cpu_baseline"] = cpu_trbdf2_baseline(
-                tri, u0, lambda x, y: 1 / 9 + 0.0 * x, 0.5, _saveat_list(0.0, 0.5, 0.05))
+                tri, u0, 1 / 9, 0.5, _saveat_list(0.0, 0.5, 0.05))
         except Exception as e:  # noqa: BLE001
             out["fvmproblem_trbdf2_saveat_0.05"]["cpu_baseline"] = {"error": repr(e)[:200]}
     # docs/src/literate_wyos/poissons_equation.jl: the 100 x 100 Poisson problem as a
