@@ -534,3 +534,26 @@ def test_oracle_steady_newton_mean_exit_time_disk():
     A, b = O.template_mean_exit_time(tri, conds, lambda x, y: 1.0 + 0.0 * x)
     T = O.steady_solve(A, b)
     assert np.max(np.abs(u - T)) <= 1e-9 * np.max(np.abs(T))
+
+
+def test_oracle_steady_newton_nonlinear_converges_to_the_kirchhoff_solution():
+    """div((1 + u^2) grad u) = 0 on the unit square with u + u^3/3 = x + y on the boundary: the
+    Kirchhoff transform w = u + u^3/3 is harmonic, so the exact steady state solves
+    u + u^3/3 = x + y.  The oracle's Newton steady solve (per-triangle nonlinear fluxes, a
+    coloured finite-difference Jacobian at every iteration) converges to it at second order."""
+
+    def exact(x, y):
+        w = x + y  # the real root of u^3/3 + u - w = 0 (Cardano)
+        s = np.sqrt(9 * w * w / 4 + 1)
+        return np.cbrt(1.5 * w + s) + np.cbrt(1.5 * w - s)
+
+    errs = []
+    for n in (9, 17, 33):
+        tri = triangulate_rectangle(0.0, 1.0, 0.0, 1.0, n, n, single_boundary=True)
+        _, f, jac, cb, fixed = _steady_oracle_problem(tri, [lambda x, y, t, u: exact(x, y)], ["Dirichlet"],
+                                                      D=lambda x, y, t, u: 1.0 + u * u)
+        u, it, res = O.steady_newton(f, jac, np.zeros(tri.num_points), 0.0, fixed, callback=cb)
+        assert 2 <= it <= 12 and res <= 1e-8
+        errs.append(np.max(np.abs(u - exact(tri.points[:, 0], tri.points[:, 1]))))
+    r1, r2 = errs[0] / errs[1], errs[1] / errs[2]
+    assert 3.0 < r1 < 5.0 and 3.0 < r2 < 5.0, (errs, r1, r2)
