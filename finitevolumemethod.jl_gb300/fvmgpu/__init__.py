@@ -8,6 +8,7 @@ from .meshes import (Triangulation, triangulate_rectangle, triangulate_annulus, 
 from .api import (ConditionType, Neumann, Dudt, Dirichlet, Constrained, ParametrisedFunction, BoundaryConditions,
                   InternalConditions, Conditions, TriangleProperties, FVMGeometry, FVMProblem, fvm_eqs,
                   update_dirichlet_nodes, DiffusionEquation, LinearReactionDiffusionEquation, PoissonsEquation,
+                  LaplacesEquation,
                   MeanExitTimeProblem, Tsit5, TRBDF2, KrylovSolver, SteadyFVMProblem, DynamicSS, NewtonRaphson,
                   SteadyStateSolution, ODESolution, LinearSolution, solve, BatchedProblem,
                   AdjointProblem, solve_rrule, FVMSystem, InvalidFluxError,
@@ -25,5 +26,5 @@ __all__ = [
     "disjoint_union", "AdjointProblem", "solve_rrule", "FVMSystem", "InvalidFluxError", "jacobian_sparsity", "compute_flux", "pl_interpolate", "interpolate",
     "two_point_interpolant", "construct_flux_function", "FVMError",
     "UnsupportedFormError", "NotConvergedError", "build", "lib_path", "TRBDF2", "jvp", "jacobian_diagonal",
-    "SteadyFVMProblem", "DynamicSS", "NewtonRaphson", "SteadyStateSolution",
+    "SteadyFVMProblem", "DynamicSS", "NewtonRaphson", "SteadyStateSolution", "LaplacesEquation",
 ]

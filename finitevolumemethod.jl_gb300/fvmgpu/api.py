@@ -1422,6 +1422,16 @@ class PoissonsEquation(_Template):
         self._create(mesh, BCs, ICs, diffusion_function, diffusion_parameters, source_function, source_parameters)
 
 
+class LaplacesEquation(PoissonsEquation):
+    """LaplacesEquation (laplaces_equation.jl:48-94): div(D grad u) = 0, assembled as the Poisson
+    template's A with b holding only the boundary terms (the Poisson template with f = 0)."""
+
+    def __init__(self, mesh, BCs, ICs=None, *, diffusion_function=lambda x, y, p: 1.0 + 0.0 * x,
+                 diffusion_parameters=None, **kwargs):
+        super().__init__(mesh, BCs, ICs, diffusion_function=diffusion_function,
+                         diffusion_parameters=diffusion_parameters, source_function=lambda x, y, p: 0.0 * x)
+
+
 class MeanExitTimeProblem(_Template):
     """MeanExitTimeProblem (mean_exit_time.jl:43-94): div(D grad T) = -1."""
 

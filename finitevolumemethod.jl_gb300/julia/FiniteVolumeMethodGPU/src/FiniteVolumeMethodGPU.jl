@@ -630,6 +630,7 @@ end
 template_kind(::FVM.DiffusionEquation) = FVM_TEMPLATE_DIFFUSION
 template_kind(::FVM.LinearReactionDiffusionEquation) = FVM_TEMPLATE_LINEAR_REACTION_DIFFUSION
 template_kind(::FVM.PoissonsEquation) = FVM_TEMPLATE_POISSON
+template_kind(::FVM.LaplacesEquation) = FVM_TEMPLATE_POISSON  # the Poisson template with f = 0
 template_kind(::FVM.MeanExitTimeProblem) = FVM_TEMPLATE_MEAN_EXIT_TIME
 
 """
@@ -674,7 +675,8 @@ function GPUTemplate(tmpl::FVM.AbstractFVMTemplate)
     src = zeros(0)
     sdeg = Int32(0)
     if kind == FVM_TEMPLATE_POISSON || kind == FVM_TEMPLATE_LINEAR_REACTION_DIFFUSION
-        S, Sp = tmpl.source_function, tmpl.source_parameters
+        S, Sp = tmpl isa FVM.LaplacesEquation ? ((x, y, p) -> 0.0, nothing) :
+                (tmpl.source_function, tmpl.source_parameters)
         sv = Float64[S(DT.getxy(DT.get_point(tri, i))..., Sp) for i in 1:np]
         if kind == FVM_TEMPLATE_LINEAR_REACTION_DIFFUSION  # the reaction coefficient: source c1 u
             src = vec(permutedims(hcat(zeros(np), sv)))
@@ -855,7 +857,8 @@ The steady template solved on the device in place of `solve(tmpl, KLUFactorizati
 (src/specific_problems/abstract_templates.jl:58-60): a named tuple with `u` (the solution) and
 `stats`.
 """
-function CommonSolve.solve(tmpl::Union{FVM.PoissonsEquation, FVM.MeanExitTimeProblem}, alg::GPUKrylov; kwargs...)
+function CommonSolve.solve(tmpl::Union{FVM.PoissonsEquation, FVM.LaplacesEquation, FVM.MeanExitTimeProblem},
+                           alg::GPUKrylov; kwargs...)
     x, st = steady_solve(gpu_object(tmpl), alg)
     return (u = x, stats = st)
 end

@@ -77,6 +77,22 @@ def test_poisson_exact_solution_gpu(gpu_lib):
         assert np.linalg.norm(sol.u - exact) <= 1e-4 * np.linalg.norm(exact)
 
 
+def test_laplace_template_is_poisson_without_a_source(gpu_lib):
+    """LaplacesEquation (laplaces_equation.jl:48-94) assembles as the Poisson template with f = 0:
+    its solution equals PoissonsEquation's with a zero source bit for bit, and with the boundary
+    values 0, 100y, 100, 100y it is u = 100y, which the scheme reproduces."""
+    import fvmgpu as F
+
+    tri = triangulate_rectangle(0.0, 1.0, 0.0, 1.0, 40, 40, single_boundary=False)
+    fns = [lambda x, y, t, u, p: 0.0 * x, lambda x, y, t, u, p: 100 * y, lambda x, y, t, u, p: 100.0 + 0.0 * x,
+           lambda x, y, t, u, p: 100 * y]
+    mesh, BCs = _mesh_bcs(F, tri, fns, ["Dirichlet"] * 4)
+    lap = F.solve(F.LaplacesEquation(mesh, BCs))
+    pois = F.solve(F.PoissonsEquation(mesh, BCs, source_function=lambda x, y, p: 0.0 * x))
+    assert np.array_equal(lap.u, pois.u)
+    assert np.max(np.abs(lap.u - 100 * tri.points[:, 1])) <= 1e-6 * 100
+
+
 @pytest.mark.parametrize("precond", ["jacobi", "chebyshev"])
 @pytest.mark.parametrize("mode", ["fp64", "mixed"])
 @pytest.mark.parametrize("jump", [False, True])
