@@ -557,3 +557,27 @@ def test_oracle_steady_newton_nonlinear_converges_to_the_kirchhoff_solution():
         errs.append(np.max(np.abs(u - exact(tri.points[:, 0], tri.points[:, 1]))))
     r1, r2 = errs[0] / errs[1], errs[1] / errs[2]
     assert 3.0 < r1 < 5.0 and 3.0 < r2 < 5.0, (errs, r1, r2)
+
+
+def test_oracle_system_steady_newton_reproduces_a_linear_solution():
+    """Two components with constant cross-diffusion, q_u = -(grad u + grad v / 2) and
+    q_v = -(grad u / 4 + grad v), sources v - (x - y) and u^2 - (x + y)^2, and Dirichlet values
+    u = x + y, v = x - y: the steady state is u = x + y, v = x - y (linear, so every flux is exact,
+    and both sources vanish there).  The oracle's system Newton steady solve from zero recovers
+    it to rounding."""
+    tri = triangulate_rectangle(0.0, 1.0, 0.0, 1.0, 15, 15, single_boundary=True)
+    conds = [O.Conditions(tri, [lambda x, y, t, u: x + y], ["Dirichlet"]),
+             O.Conditions(tri, [lambda x, y, t, u: x - y], ["Dirichlet"])]
+    fluxes = [lambda x, y, t, a, b, g: (-(a[0] + a[1] / 2), -(b[0] + b[1] / 2)),
+              lambda x, y, t, a, b, g: (-(a[0] / 4 + a[1]), -(b[0] / 4 + b[1]))]
+    sources = [lambda x, y, t, u: u[1] - (x - y), lambda x, y, t, u: u[0] * u[0] - (x + y) ** 2]
+    N, n = 2, tri.num_points
+    sys_ = O.System(tri, conds, fluxes, sources, u0=np.zeros((N, n)), t0=0.0, tf=np.inf)
+    f = lambda x, t: O.system_fvm_eqs(sys_, x.reshape(-1, N).T, t).T.ravel()  # noqa: E731
+    ent, nn = O.jacobian_sparsity(tri, N)
+    jac = lambda x, t: O.colored_jacobian(f, x, t, ent, nn)  # noqa: E731
+    cb = lambda x, t: O.system_update_dirichlet_nodes(sys_, x.reshape(-1, N).T, t).T.ravel()  # noqa: E731
+    u, it, res = O.steady_newton(f, jac, np.zeros(N * n), 0.0, O.fixed_rows(tri, conds), callback=cb)
+    P = tri.points
+    want = np.stack([P[:, 0] + P[:, 1], P[:, 0] - P[:, 1]], axis=1).ravel()
+    assert np.max(np.abs(u - want)) <= 1e-9 and it >= 2
